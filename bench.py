@@ -1,0 +1,380 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 solve path on the 3D Q2 convection-diffusion workload.
+
+Workload (default): unit cube, 32^3 hexahedra, Q2 (274,625 DOFs), eps = 1e-2,
+b = (1, 0.5, 0.25), u = 0 on the boundary, f from u = sin(pi x) sin(pi y) sin(pi z),
+Gauss 3x3x3 quadrature, FGMRES(30) preconditioned by a multigrid V(2,2) cycle with
+damped Jacobi (0.8) over 4 levels and a direct coarse solve, stopped at a 1e-8
+relative FP64 residual. Inputs are synthetic (generated mesh, manufactured data).
+
+One step = one solve request: assembly of all four levels on the device plus the
+FGMRES solve. `value` is the mixed-precision form (FP32 multigrid inside FP64
+FGMRES) in solves/s with the mesh resident in HBM; `e2e` is the same request
+through pm_problem_run_host with the mesh geometry copied in from pinned host
+memory and the solution copied back every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 (launched by torchrun): independent replicas, one per GPU, no collective
+on the data path; rank 0 prints max-over-ranks timing.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "solves/sec, DOFs/s at 1e-8 FP64 residual (mixed vs FP64); SpMV GB/s; p99"
+
+WORKLOADS = {
+    "cd3d_q2_32": dict(geometry=1, root_n=1, n_refine=5, n_levels=4, elem=2, eps=1e-2,
+                       b=(1.0, 0.5, 0.25), quad=3, restart=30, reduction=1e-8,
+                       desc="3D Q2 convection-diffusion, 32^3 hexahedra (274,625 DOFs), "
+                            "FGMRES(30) + MG V(2,2) Jacobi(0.8), 4 levels, to 1e-8"),
+    "cd2d_q1_128": dict(geometry=0, root_n=1, n_refine=7, n_levels=4, elem=1, eps=0.1,
+                        b=(1.0, 0.0, 0.0), quad=3, restart=20, reduction=1e-10,
+                        desc="2D Q1 convection-diffusion, 128^2 quadrilaterals (16,641 DOFs), "
+                             "FGMRES(20) + MG V(2,2) Jacobi(0.8), 4 levels, to 1e-10"),
+}
+
+
+def solver_db(w, precision):
+    import mymoonmd_gb300 as m
+    db = m.ParameterDatabase.solve_path_database()
+    db["solver_type"] = "iterative"
+    db["iterative_solver_type"] = "fgmres"
+    db["preconditioner"] = "multigrid"
+    db["residual_tolerance"] = 0.0
+    db["residual_reduction"] = w["reduction"]
+    db["max_n_iterations"] = 500
+    db["gmres_restart"] = w["restart"]
+    db["multigrid_n_levels"] = w["n_levels"]
+    db["multigrid_smoother"] = "jacobi"
+    db["multigrid_smoother_coarse"] = "direct_solve"
+    db["jacobi_damp"] = 0.8
+    db["multigrid_n_pre_smooth"] = 2
+    db["multigrid_n_post_smooth"] = 2
+    db["gpu_precision"] = precision
+    return db
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region"""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args, w, rank, world, local, pg):
+    import numpy as np
+    import mymoonmd_gb300 as m
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+
+    ctx = m.Context(local)
+    disc = m.Discretization(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"], m.KIND_CD, w["elem"])
+    cf = m.cd_coeffs(w["eps"], w["b"], 0.0, True)
+    fin = disc.level_info(w["n_levels"] - 1)
+    n_dofs, nnz = fin["n_dofs"], fin["nnz"]
+
+    results = {}
+    for precision in ("fp64", "mixed"):
+        prob = m.ConvectionDiffusion(ctx, disc, cf, solver_db(w, precision), quad_points=w["quad"])
+        for _ in range(args.warmup):
+            prob.assemble()
+            prob.solve()
+        its = []
+        step_ms = []
+        barrier(pg)
+        ctx.synchronize()
+        sampler = ClockSampler(local) if precision == "mixed" else None
+        if sampler:
+            sampler.start()
+        if precision == "mixed":
+            ctx.probe(nnz)
+        launches0 = ctx.kernel_launches()
+        t0 = time.perf_counter()
+        ctx.time_begin()
+        for _ in range(args.steps):
+            ctx_t = time.perf_counter()
+            prob.assemble()
+            prob.solve()
+            step_ms.append((time.perf_counter() - ctx_t) * 1e3)
+            its.append(prob.last_info()[0])
+        dev_ms = ctx.time_end()
+        wall = time.perf_counter() - t0
+        launches = ctx.kernel_launches() - launches0
+        clocks = sampler.stop() if sampler else None
+        probe = ctx.probe_result() if precision == "mixed" else None
+        ctx.probe(0)
+        barrier(pg)
+        ms = max_over_ranks(pg, dev_ms)
+        results[precision] = dict(ms=ms, wall=wall, its=its, step_ms=step_ms, launches=launches,
+                                  clocks=clocks, probe=probe, info=prob.last_info())
+        if precision == "mixed":
+            keep_prob = prob
+        else:
+            prob.close()
+
+    # end-to-end through the public API: geometry in from pinned host memory,
+    # solution back to pinned host memory, every step
+    prob = keep_prob
+    verts = [disc.cell_vertices(l) for l in range(w["n_levels"])]
+    pinned = []
+    for v in verts:
+        pa = m.PinnedArray(ctx, v.size)
+        pa.array[:] = v.ravel()
+        pinned.append(pa)
+    sol = m.PinnedArray(ctx, n_dofs)
+    h2d = sum(v.nbytes for v in verts) + 64
+    d2h = n_dofs * 8
+    for _ in range(max(1, args.warmup)):
+        prob.run_host(cf, [p.array for p in pinned], sol.array)
+    barrier(pg)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    ctx.time_begin()
+    for _ in range(args.steps):
+        prob.run_host(cf, [p.array for p in pinned], sol.array)
+    e2e_ms = max_over_ranks(pg, ctx.time_end())
+    del t0
+
+    # stand-alone SpMV bandwidth of the finest FP64 and FP32 matrices
+    A = prob.matrix(-1)
+    x = m.DeviceVector(ctx, n_dofs)
+    y = m.DeviceVector(ctx, n_dofs)
+    x32 = m.DeviceVector(ctx, n_dofs, np.float32)
+    y32 = m.DeviceVector(ctx, n_dofs, np.float32)
+    A.bench_apply(x, y, 5)
+    ms64, b64 = A.bench_apply(x, y, 50)
+    A.bench_apply(x32, y32, 5, fp32=True)
+    ms32, b32 = A.bench_apply(x32, y32, 50, fp32=True)
+
+    if rank != 0:
+        return None
+    mixed, fp64 = results["mixed"], results["fp64"]
+    K = args.steps
+    solves_s = world * K / (mixed["ms"] / 1e3)
+    fp64_solves_s = world * K / (fp64["ms"] / 1e3)
+    n_probe, probe_ms, probe_bytes = mixed["probe"]
+    achieved = (probe_bytes / n_probe) / (probe_ms / n_probe / 1e3) / 1e9 if n_probe else None
+    lat = sorted(mixed["step_ms"])
+    line = {
+        "metric": METRIC,
+        "value": round(solves_s, 3),
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": round(mixed["ms"] / K, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 multigrid inside f64 FGMRES (outer residuals f64)",
+        "data": "synthetic: generated unit-cube mesh and manufactured-solution coefficients",
+        "config": {"workload": w["desc"], "dofs": n_dofs, "nnz_finest": nnz,
+                   "parallelism": f"replicas x{world} (no collective)",
+                   "l2": "inputs larger than L2: finest FP64 matrix "
+                         f"{(nnz * 12 + n_dofs * 4) / 1e6:.0f} MB > 126 MB L2",
+                   "step": "assembly of all levels + FGMRES/MG solve to 1e-8 relative FP64 residual"},
+        "dofs_per_s": round(solves_s * n_dofs, 1),
+        "fgmres_iterations": mixed["its"][-1],
+        "final_relative_residual": mixed["info"][1] / mixed["info"][2],
+        "fp64": {"value": round(fp64_solves_s, 3), "unit": "solves/s", "ms_per_step": round(fp64["ms"] / K, 3),
+                 "fgmres_iterations": fp64["its"][-1], "dofs_per_s": round(fp64_solves_s * n_dofs, 1)},
+        "mixed_over_fp64": round(solves_s / fp64_solves_s, 3),
+        "latency_ms": {"p50": round(lat[len(lat) // 2], 3),
+                       "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3)},
+        "spmv": {"fp64_gbs": round(b64 / (ms64 / 1e3) / 1e9, 1), "fp32_gbs": round(b32 / (ms32 / 1e3) / 1e9, 1),
+                 "fp64_frac": round(b64 / (ms64 / 1e3) / 1e9 / hbm_peak, 3),
+                 "fp32_frac": round(b32 / (ms32 / 1e3) / 1e9 / hbm_peak, 3)},
+        "e2e": {"value": round(world * K / (e2e_ms / 1e3), 3), "unit": "solves/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": mixed["launches"],
+        "roofline": {"bound": "hbm", "kernel": "csr_kernel (finest-level SpMV, Jacobi sweeps, defects)",
+                     "achieved": round(achieved, 1) if achieved else None, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 3) if achieved else None,
+                     "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                     "launches_probed": n_probe},
+        "clocks": mixed["clocks"],
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w)
+    return line
+
+
+def _oracle_solve(wname):
+    """one oracle (CPU) request: assembly of all levels + FGMRES/MG solve"""
+    from oracle import cd as ocd
+    w = WORKLOADS[wname]
+    o = ocd.OracleCD(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"], w["elem"], w["eps"], w["b"],
+                     0.0, w["quad"])
+    t0 = time.perf_counter()
+    o.assemble()
+    o.build_mg(2, 2, 0.8, 1.0, "V")
+    sol, it, res, hist, st = o.solve("fgmres", 0.0, w["reduction"], 500, 0, w["restart"])
+    dt = time.perf_counter() - t0
+    return dt, it, st
+
+
+def cpu_baseline(w):
+    wname = [k for k, v in WORKLOADS.items() if v is w][0]
+    dt, it, st = _oracle_solve(wname)
+    return {"value": round(1.0 / dt, 5), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"one full request (assembly of all levels + FGMRES/MG solve, {it} iterations) "
+                      f"of the same workload by the C restatement in oracle/, single thread, {dt:.1f} s"}
+
+
+def run_reference(args, w, rank, world):
+    """the reference path's CPU implementation (the oracle port: the reference does not
+    build here) on all host cores: one independent request per core per step"""
+    import multiprocessing as mp
+    wname = [k for k, v in WORKLOADS.items() if v is w][0]
+    cores = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 2))
+    warm = min(args.warmup, 1)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(warm):
+            pool.map(_oracle_solve, [wname] * cores)
+        t0 = time.perf_counter()
+        its = []
+        for _ in range(steps):
+            its += [r[1] for r in pool.map(_oracle_solve, [wname] * cores)]
+        dt = time.perf_counter() - t0
+    value = steps * cores / dt
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "solves/s", "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": round(dt / steps * 1e3, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: generated unit-cube mesh and manufactured-solution coefficients",
+        "config": {"workload": w["desc"], "parallelism": f"{cores} independent CPU requests per step"},
+        "cpu_baseline": {"value": round(value, 5), "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{steps} step(s) (of {args.steps} requested) of {cores} concurrent full "
+                                   f"requests (assembly + FGMRES/MG, {its[-1] if its else 0} iterations), "
+                                   "one per host core, C restatement in oracle/ (the reference needs "
+                                   "CMake-generated headers, LAPACK and UMFPACK and is not built)"},
+        "e2e": {"value": round(value, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="cd3d_q2_32")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    rank, world, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args, w, rank, world)), flush=True)
+        return 0
+    if args.warmup < 3:
+        args.warmup = 3
+    line = run_ours(args, w, rank, world, local, pg)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,236 @@
+/*
+ * pmgpu.h - C ABI of the GB300-native finite element solve path.
+ *
+ * The library replaces, for one GPU, the element assembly, CSR SpMV, geometric
+ * multigrid and Krylov kernels behind ParMooN's (nahmedwias/MyMooNMD) solver
+ * interface. Every entry point names the reference interface it stands in for.
+ *
+ * Conventions
+ *   - All functions return a status (PM_OK == 0). The message of the last
+ *     failure of a context is returned by pm_last_error(). They never throw.
+ *     The reference reports the same failures by ErrThrow -> std::runtime_error
+ *     (include/General/MooNMD_Io.h:210).
+ *   - Host arrays are copied in; the caller keeps ownership. Pointers named
+ *     *_dev are device pointers (allocated with pm_dev_alloc or any CUDA
+ *     allocation on the context's device). Device buffers of handles belong to
+ *     the library and are freed by the matching *_destroy call.
+ *   - One context owns one CUDA stream. Calls on one context must be serialised
+ *     by the caller; different contexts may be used from different threads.
+ *   - Vectors are contiguous FP64 arrays laid out like BlockVector
+ *     (include/Matrix/BlockVector.h:43): blocks one after another, the
+ *     non-active (Dirichlet) DOFs at the tail of each block.
+ */
+#ifndef PMGPU_H
+#define PMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define PM_OK 0
+#define PM_E_INVALID 1     /* bad argument (ErrThrow on wrong sizes/keys)          */
+#define PM_E_OOM 2         /* device allocation failed / admission refused         */
+#define PM_E_DIVERGED 3    /* IterativeMethod::converged divergence branch         */
+#define PM_E_BREAKDOWN 4   /* FGMRES unhappy breakdown, BiCGStab omega == 0, zero pivot */
+#define PM_E_MAXIT 5       /* reserved: iteration cap (reported through info, not as failure) */
+#define PM_E_CUDA 6        /* CUDA runtime error                                   */
+#define PM_E_TIMEOUT 7     /* a bounded device wait gave up                        */
+#define PM_E_UNSUPPORTED 8 /* configuration outside what this library implements   */
+
+typedef struct pm_ctx pm_ctx;
+typedef struct pm_matrix pm_matrix;
+typedef struct pm_solver pm_solver;
+typedef struct pm_disc pm_disc;
+typedef struct pm_problem pm_problem;
+typedef struct pm_server pm_server;
+
+/* ------------------------------------------------------------ context ---- */
+int pm_ctx_create(int device, pm_ctx** out);
+void pm_ctx_destroy(pm_ctx* ctx);
+const char* pm_last_error(const pm_ctx* ctx);
+int pm_ctx_synchronize(pm_ctx* ctx);
+/* number of kernels this context launched since creation */
+int pm_ctx_kernel_launches(const pm_ctx* ctx, uint64_t* out);
+/* CUDA events on the context's stream, for timing (ms between two records) */
+int pm_ctx_time_begin(pm_ctx* ctx);
+int pm_ctx_time_end(pm_ctx* ctx, float* ms);
+int pm_version(void);
+/* Launch probe (no reference counterpart; measurement only): while enabled
+ * (nnz != 0), every SpMV-family launch (apply, defect, Jacobi sweep, transfer)
+ * on a matrix with exactly `nnz` nonzeros is bracketed by CUDA events on the
+ * context's stream. pm_ctx_probe_result returns the number of probed launches,
+ * their summed device time and their summed algorithmic bytes. */
+int pm_ctx_probe(pm_ctx* ctx, int64_t nnz);
+int pm_ctx_probe_result(pm_ctx* ctx, int* launches, double* total_ms, double* total_bytes);
+
+int pm_dev_alloc(pm_ctx* ctx, size_t bytes, void** out_dev);
+int pm_dev_free(pm_ctx* ctx, void* dev);
+int pm_memcpy_h2d(pm_ctx* ctx, void* dst_dev, const void* src_host, size_t bytes);
+int pm_memcpy_d2h(pm_ctx* ctx, void* dst_host, const void* src_dev, size_t bytes);
+int pm_memset_dev(pm_ctx* ctx, void* dst_dev, int value, size_t bytes);
+/* page-locked host memory for the host<->device copies of requests */
+int pm_host_alloc(pm_ctx* ctx, size_t bytes, void** out_host);
+int pm_host_free(pm_ctx* ctx, void* host);
+
+/* ------------------------------------------------------------ matrices --- */
+/* TMatrix / FEMatrix (include/Matrix/Matrix.h:47, include/Matrix/FEMatrix.h:27):
+ * CSR with ascending column indices per row (TStructure ColOrder = 1). Rows
+ * [n_active, n_rows) are non-active; FE matrices store a unit diagonal there
+ * (src/AssembleRoutines/Assemble3D.C:396-404). vals may be NULL (zeros). */
+int pm_matrix_create_csr(pm_ctx* ctx, int n_rows, int n_cols, int n_active,
+                         const int* row_ptr, const int* cols, const double* vals,
+                         pm_matrix** out);
+void pm_matrix_destroy(pm_matrix* A);
+/* BlockFEMatrix block layout of a combined square matrix
+ * (src/Matrix/BlockFEMatrix.C:1168 get_combined_submatrix): n_blocks <= 4
+ * blocks of the given lengths, the first actives[b] rows of block b active. */
+int pm_matrix_set_blocks(pm_matrix* A, int n_blocks, const int* lengths, const int* actives);
+int pm_matrix_info(const pm_matrix* A, int* n_rows, int* n_cols, int* n_active, int64_t* nnz);
+int pm_matrix_set_values(pm_matrix* A, const double* vals_host);
+int pm_matrix_get_values(const pm_matrix* A, double* vals_host);
+int pm_matrix_get_structure(const pm_matrix* A, int* row_ptr_host, int* cols_host);
+/* BlockFEMatrix::apply_scaled_add (src/Matrix/BlockFEMatrix.C:863):
+ * y += a*A*x on active rows, y += a*x on non-active rows. */
+int pm_matrix_apply_scaled_add(pm_matrix* A, const double* x_dev, double* y_dev, double a);
+/* BlockFEMatrix::apply (src/Matrix/BlockFEMatrix.C:855): y = A*x */
+int pm_matrix_apply(pm_matrix* A, const double* x_dev, double* y_dev);
+/* TMatrix::get_diagonal (src/Matrix/Matrix.C:298) */
+int pm_matrix_get_diagonal(pm_matrix* A, double* diag_dev);
+/* FP32 copy of the values for the mixed-precision preconditioner, and its SpMV
+ * y = A32*x (FP32 values, vectors and accumulation). */
+int pm_matrix_make_fp32(pm_matrix* A);
+int pm_matrix_apply_f32(pm_matrix* A, const float* x_dev, float* y_dev);
+/* Timed SpMV loop: `reps` applications y = A x on the context's stream, timed
+ * with CUDA events; returns ms per application and the algorithmic bytes. */
+int pm_matrix_bench_apply(pm_matrix* A, int fp32, const void* x_dev, void* y_dev, int reps,
+                          float* ms_per_apply, double* bytes_per_apply);
+
+/* ------------------------------------------------------------- BLAS-1 ---- */
+/* Ddot / Dnorm / Daxpy / Dscal (src/FE/Blas1.C:14-115) on device vectors;
+ * reductions use a fixed tree and are deterministic. */
+int pm_dot(pm_ctx* ctx, int n, const double* x_dev, const double* y_dev, double* out);
+int pm_norm(pm_ctx* ctx, int n, const double* x_dev, double* out);
+int pm_axpy(pm_ctx* ctx, int n, double a, const double* x_dev, double* y_dev);
+int pm_scal(pm_ctx* ctx, int n, double a, double* x_dev);
+
+/* --------------------------------------------------------------- solver --- */
+/* Solver<BlockFEMatrix, BlockVector> (include/Solver/Solver.h:31-127), driven
+ * by ParameterDatabase keys given as text, one "key: value" per line, with the
+ * reference's names and meaning (src/Solver/Solver.C:21-115,
+ * src/Multigrid/Multigrid.C:422-514), e.g.
+ *   solver_type: iterative       iterative_solver_type: fgmres
+ *   preconditioner: multigrid    residual_reduction: 1e-8
+ * New key: gpu_precision {fp64, mixed} (mixed = FP32 multigrid inside FP64
+ * FGMRES). Unknown keys are ignored like ParameterDatabase::merge(.., false). */
+int pm_solver_create(pm_ctx* ctx, const char* params, pm_solver** out);
+void pm_solver_destroy(pm_solver* s);
+/* Solver::update_matrix (src/Solver/Solver.C:261). With preconditioner
+ * multigrid the finest level is `A`; coarser levels come from
+ * pm_solver_set_multigrid_level (Multigrid::initialize, coarsest -> finest). */
+int pm_solver_update_matrix(pm_solver* s, pm_matrix* A);
+/* Multigrid level `level` (0 = coarsest) with its matrix and the prolongation
+ * from this level to the next finer one (fine rows x this level's columns,
+ * empty rows for non-active fine DOFs) - the operator GridTransfer::Prolongate
+ * applies (src/Multigrid/GridTransfer.C:665); restriction uses its transpose
+ * (GridTransfer::DefectRestriction, :943). The finest level passes P = NULL. */
+int pm_solver_set_multigrid_level(pm_solver* s, int level, int n_levels, pm_matrix* A,
+                                  int p_rows, int p_cols, const int* p_row_ptr,
+                                  const int* p_cols_idx, const double* p_vals);
+/* Solver::solve (src/Solver/Solver.C:415,493) on device vectors. */
+int pm_solver_solve(pm_solver* s, const double* rhs_dev, double* sol_dev);
+/* Same on host vectors (host->device copy in, device->host copy out). */
+int pm_solver_solve_host(pm_solver* s, const double* rhs_host, double* sol_host, int n);
+/* LoopInfo of the last solve: iterations and final residual. */
+int pm_solver_last_info(const pm_solver* s, int* iterations, double* residual,
+                        double* initial_residual);
+/* Residual history of the last solve (up to cap entries), returns count. */
+int pm_solver_residual_history(const pm_solver* s, double* out, int cap, int* count);
+/* Iteration_multigrid::apply (src/Solver/Iteration_multigrid.C:22): one
+ * multigrid cycle with rhs z, result r. */
+int pm_solver_apply_preconditioner(pm_solver* s, const double* z_dev, double* r_dev);
+
+/* ------------------------------------------------ discretisation set-up --- */
+/* Mesh hierarchy + FE spaces + CSR structures + transfer operators, restating
+ * TDomain refinement (src/Geometry/Domain.C:1045), TFESpace3D::ConstructSpace
+ * (src/FE/FESpace3D.C:506) and TStructure (src/Matrix/Structure.C:829).
+ * geometry: 0 unit square (quadrilaterals), 1 unit cube (hexahedra),
+ *           2 unit cube (tetrahedra, 6 per cube as Default_UnitCube_Tetra)
+ * root_n: root cells per side (1 = the reference's default meshes)
+ * n_refine: regular refinements; the finest n_levels levels are kept for MG.
+ * kind: 0 convection-diffusion (elem 1 = Q1, 2 = Q2 on quads/hexes),
+ *       1 Stokes P2/P1 Taylor-Hood on tetrahedra (elem ignored). */
+int pm_disc_create(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
+                   pm_disc** out);
+void pm_disc_destroy(pm_disc* d);
+/* per level (0 = coarsest kept level): cells, local DOFs per cell, DOFs,
+ * active DOFs and nnz of the level matrix (space 0 = velocity/scalar,
+ * space 1 = pressure for Stokes) */
+int pm_disc_level_info(const pm_disc* d, int level, int space, int* n_cells, int* nloc,
+                       int* n_dofs, int* n_active, int64_t* nnz);
+/* GlobalNumbers of the level (n_cells * nloc, BeginIndex[c] = c*nloc) */
+int pm_disc_dofmap(const pm_disc* d, int level, int space, int* out);
+/* cell vertex coordinates (n_cells * vertices * dim) */
+int pm_disc_cell_vertices(const pm_disc* d, int level, double* out);
+/* CSR pattern of the level system matrix (combined blocks for Stokes) */
+int pm_disc_structure(const pm_disc* d, int level, int* row_ptr, int* cols);
+/* prolongation from `level` to `level+1` (rows of level+1) */
+int pm_disc_prolongation_info(const pm_disc* d, int level, int* rows, int* cols, int64_t* nnz);
+int pm_disc_prolongation(const pm_disc* d, int level, int* row_ptr, int* cols, double* vals);
+
+/* ------------------------------------------------------------ assembly --- */
+/* Coefficients of the convection-diffusion problem
+ *   -eps Laplace(u) + b.grad(u) + c u = f, u = 0 on the boundary,
+ * with f from the manufactured solution u = prod_d sin(pi x_d)
+ * (manufactured = 1) or f = f_const (manufactured = 0). */
+typedef struct pm_cd_coeffs {
+  double eps;
+  double b[3];
+  double c;
+  int manufactured;
+  double f_const;
+} pm_cd_coeffs;
+
+/* Assemble2D / Assemble3D with LocalAssembling (ConvDiff Galerkin,
+ * src/AssembleRoutines/Assemble3D.C:37, LocalAssembling.C:669,
+ * ConvDiff.C:1794-1856) of one level on the device: element matrices over the
+ * quadrature points, gathered into the CSR in cell order; Dirichlet rows get a
+ * unit diagonal and zero right-hand side. quad_points: points per direction of
+ * the tensor Gauss rule (2..4); 0 picks the reference's default. */
+int pm_assemble_cd(pm_ctx* ctx, const pm_disc* d, int level, const pm_cd_coeffs* coeffs,
+                   int quad_points, pm_matrix* A, double* rhs_dev);
+
+/* ----------------------------------------------------- problem (system) --- */
+/* ConvectionDiffusion<d> / NavierStokes<3> (Stokes) system on the device: the
+ * level hierarchy of `disc`, assembled matrices, right-hand side and the solver
+ * built from `params`. */
+int pm_problem_create_cd(pm_ctx* ctx, const pm_disc* d, const pm_cd_coeffs* coeffs,
+                         int quad_points, const char* params, pm_problem** out);
+void pm_problem_destroy(pm_problem* p);
+/* ConvectionDiffusion::assemble (src/System/ConvectionDiffusion.C:174) */
+int pm_problem_assemble(pm_problem* p);
+/* ConvectionDiffusion::solve (src/System/ConvectionDiffusion.C:191) */
+int pm_problem_solve(pm_problem* p);
+int pm_problem_size(const pm_problem* p, int* n_dofs, int* n_active);
+int pm_problem_get_solution(const pm_problem* p, double* sol_host);
+int pm_problem_get_rhs(const pm_problem* p, double* rhs_host);
+int pm_problem_matrix(pm_problem* p, int level, pm_matrix** out);
+int pm_problem_solver(pm_problem* p, pm_solver** out);
+int pm_problem_solution_dev(pm_problem* p, double** sol_dev, double** rhs_dev);
+/* One request end to end from host memory: new coefficients, the cell vertex
+ * coordinates of every kept level (level_verts[l], NULL = keep the current
+ * geometry) copied to the device, assembly of all levels, solve, and the
+ * finest-level solution copied back into sol_host. */
+int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* coeffs, const double* const* level_verts,
+                        double* sol_host);
+/* Solver statistics of the problem's last solve. */
+int pm_problem_last_info(const pm_problem* p, int* iterations, double* residual,
+                         double* initial_residual);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMGPU_H */

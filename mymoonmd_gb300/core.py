@@ -1,0 +1,494 @@
+"""Python mirror of the reference's matrix / vector / solver classes over the C ABI.
+
+Context       - one GPU, one CUDA stream (pm_ctx)
+DeviceVector  - FP64 (or FP32) array on the device; BlockVector storage
+FEMatrix      - TMatrix/FEMatrix/BlockFEMatrix in CSR on the device (pm_matrix)
+Solver        - Solver<BlockFEMatrix, BlockVector> driven by a ParameterDatabase
+Discretization, ConvectionDiffusion - the set-up and system classes of the
+convection-diffusion solve path (ConvectionDiffusion<d>, src/System/ConvectionDiffusion.C)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from ._lib import CdCoeffs, PmError, check, lib
+from .parameter_database import ParameterDatabase
+
+GEO_SQUARE_QUAD = 0
+GEO_CUBE_HEXA = 1
+GEO_CUBE_TETRA = 2
+KIND_CD = 0
+KIND_STOKES = 1
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib.pm_ctx_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            lib.pm_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self) -> None:
+        check(lib.pm_ctx_synchronize(self.handle), self.handle)
+
+    def kernel_launches(self) -> int:
+        v = C.c_uint64()
+        check(lib.pm_ctx_kernel_launches(self.handle, C.byref(v)))
+        return int(v.value)
+
+    def time_begin(self) -> None:
+        check(lib.pm_ctx_time_begin(self.handle), self.handle)
+
+    def time_end(self) -> float:
+        ms = C.c_float()
+        check(lib.pm_ctx_time_end(self.handle, C.byref(ms)), self.handle)
+        return float(ms.value)
+
+    def probe(self, nnz: int) -> None:
+        """bracket SpMV-family launches on matrices with `nnz` nonzeros by events (0 = off)"""
+        check(lib.pm_ctx_probe(self.handle, int(nnz)), self.handle)
+
+    def probe_result(self) -> tuple[int, float, float]:
+        n, ms, b = C.c_int(), C.c_double(), C.c_double()
+        check(lib.pm_ctx_probe_result(self.handle, C.byref(n), C.byref(ms), C.byref(b)), self.handle)
+        return n.value, ms.value, b.value
+
+
+class PinnedArray:
+    """page-locked host array (cudaMallocHost through the library)"""
+
+    def __init__(self, ctx: Context, n: int, dtype=np.float64):
+        self.ctx = ctx
+        dt = np.dtype(dtype)
+        p = C.c_void_p()
+        check(lib.pm_host_alloc(ctx.handle, max(1, n * dt.itemsize), C.byref(p)), ctx.handle)
+        self.ptr = p
+        buf = (C.c_byte * max(1, n * dt.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dt, count=n)
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            lib.pm_host_free(self.ctx.handle, self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            if self.ptr and self.ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+class DeviceVector:
+    """Device array (FP64 by default) owned by Python."""
+
+    def __init__(self, ctx: Context, n: int, dtype=np.float64):
+        self.ctx = ctx
+        self.n = int(n)
+        self.dtype = np.dtype(dtype)
+        p = C.c_void_p()
+        check(lib.pm_dev_alloc(ctx.handle, max(1, self.n * self.dtype.itemsize), C.byref(p)), ctx.handle)
+        self.ptr = p
+        self.zero()
+
+    @classmethod
+    def from_numpy(cls, ctx: Context, a: np.ndarray) -> "DeviceVector":
+        a = np.ascontiguousarray(a)
+        v = cls(ctx, a.size, a.dtype)
+        v.upload(a)
+        return v
+
+    def upload(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        if a.size != self.n:
+            raise ValueError("length mismatch")
+        check(lib.pm_memcpy_h2d(self.ctx.handle, self.ptr, _ptr(a), a.nbytes), self.ctx.handle)
+
+    def numpy(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=self.dtype)
+        check(lib.pm_memcpy_d2h(self.ctx.handle, _ptr(out), self.ptr, out.nbytes), self.ctx.handle)
+        return out
+
+    def zero(self) -> None:
+        check(lib.pm_memset_dev(self.ctx.handle, self.ptr, 0, max(1, self.n * self.dtype.itemsize)),
+              self.ctx.handle)
+
+    def norm(self) -> float:
+        out = C.c_double()
+        check(lib.pm_norm(self.ctx.handle, self.n, self.ptr, C.byref(out)), self.ctx.handle)
+        return out.value
+
+    def dot(self, other: "DeviceVector") -> float:
+        out = C.c_double()
+        check(lib.pm_dot(self.ctx.handle, self.n, self.ptr, other.ptr, C.byref(out)), self.ctx.handle)
+        return out.value
+
+    def add_scaled(self, x: "DeviceVector", a: float) -> None:
+        check(lib.pm_axpy(self.ctx.handle, self.n, a, x.ptr, self.ptr), self.ctx.handle)
+
+    def scale(self, a: float) -> None:
+        check(lib.pm_scal(self.ctx.handle, self.n, a, self.ptr), self.ctx.handle)
+
+    def free(self) -> None:
+        if self.ptr:
+            lib.pm_dev_free(self.ctx.handle, self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            if self.ptr and self.ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+class FEMatrix:
+    """CSR matrix with an active bound on the device (TMatrix/FEMatrix/BlockFEMatrix)."""
+
+    def __init__(self, ctx: Context, handle, owned: bool = True):
+        self.ctx = ctx
+        self.handle = handle
+        self.owned = owned
+
+    @classmethod
+    def from_csr(cls, ctx: Context, row_ptr, cols, vals=None, n_active: Optional[int] = None,
+                 n_cols: Optional[int] = None) -> "FEMatrix":
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+        ci = np.ascontiguousarray(cols, dtype=np.int32)
+        n = rp.size - 1
+        nc = n if n_cols is None else int(n_cols)
+        na = n if n_active is None else int(n_active)
+        vv = None if vals is None else np.ascontiguousarray(vals, dtype=np.float64)
+        h = C.c_void_p()
+        check(lib.pm_matrix_create_csr(ctx.handle, n, nc, na, _ptr(rp), _ptr(ci),
+                                       _ptr(vv) if vv is not None else None, C.byref(h)), ctx.handle)
+        return cls(ctx, h)
+
+    def set_blocks(self, lengths, actives) -> None:
+        ln = np.ascontiguousarray(lengths, dtype=np.int32)
+        ac = np.ascontiguousarray(actives, dtype=np.int32)
+        check(lib.pm_matrix_set_blocks(self.handle, ln.size, _ptr(ln), _ptr(ac)), self.ctx.handle)
+
+    def info(self) -> tuple[int, int, int, int]:
+        r, c, a = C.c_int(), C.c_int(), C.c_int()
+        z = C.c_int64()
+        check(lib.pm_matrix_info(self.handle, C.byref(r), C.byref(c), C.byref(a), C.byref(z)))
+        return r.value, c.value, a.value, int(z.value)
+
+    @property
+    def n_rows(self) -> int:
+        return self.info()[0]
+
+    @property
+    def nnz(self) -> int:
+        return self.info()[3]
+
+    def values(self) -> np.ndarray:
+        out = np.empty(self.nnz, dtype=np.float64)
+        check(lib.pm_matrix_get_values(self.handle, _ptr(out)), self.ctx.handle)
+        return out
+
+    def set_values(self, vals) -> None:
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        check(lib.pm_matrix_set_values(self.handle, _ptr(v)), self.ctx.handle)
+
+    def structure(self) -> tuple[np.ndarray, np.ndarray]:
+        n, _, _, nnz = self.info()
+        rp = np.empty(n + 1, dtype=np.int32)
+        ci = np.empty(nnz, dtype=np.int32)
+        check(lib.pm_matrix_get_structure(self.handle, _ptr(rp), _ptr(ci)), self.ctx.handle)
+        return rp, ci
+
+    def apply_scaled_add(self, x: DeviceVector, y: DeviceVector, a: float = 1.0) -> None:
+        check(lib.pm_matrix_apply_scaled_add(self.handle, x.ptr, y.ptr, a), self.ctx.handle)
+
+    def apply(self, x: DeviceVector, y: DeviceVector) -> None:
+        check(lib.pm_matrix_apply(self.handle, x.ptr, y.ptr), self.ctx.handle)
+
+    def get_diagonal(self) -> np.ndarray:
+        n = self.n_rows
+        d = DeviceVector(self.ctx, n)
+        check(lib.pm_matrix_get_diagonal(self.handle, d.ptr), self.ctx.handle)
+        return d.numpy()
+
+    def make_fp32(self) -> None:
+        check(lib.pm_matrix_make_fp32(self.handle), self.ctx.handle)
+
+    def apply_f32(self, x: DeviceVector, y: DeviceVector) -> None:
+        check(lib.pm_matrix_apply_f32(self.handle, x.ptr, y.ptr), self.ctx.handle)
+
+    def bench_apply(self, x: DeviceVector, y: DeviceVector, reps: int, fp32: bool = False):
+        ms = C.c_float()
+        b = C.c_double()
+        check(lib.pm_matrix_bench_apply(self.handle, int(fp32), x.ptr, y.ptr, reps, C.byref(ms),
+                                        C.byref(b)), self.ctx.handle)
+        return float(ms.value), float(b.value)
+
+    def close(self) -> None:
+        if self.owned and self.handle:
+            lib.pm_matrix_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _db_text(db) -> str:
+    if db is None:
+        return ""
+    if isinstance(db, ParameterDatabase):
+        return db.to_text()
+    if isinstance(db, dict):
+        return "".join(f"{k}: {v}\n" for k, v in db.items())
+    return str(db)
+
+
+class Solver:
+    """Solver<BlockFEMatrix, BlockVector> (include/Solver/Solver.h:31-127)."""
+
+    def __init__(self, ctx: Context, db, handle=None, owned: bool = True):
+        self.ctx = ctx
+        if handle is None:
+            h = C.c_void_p()
+            check(lib.pm_solver_create(ctx.handle, _db_text(db).encode(), C.byref(h)), ctx.handle)
+            handle = h
+        self.handle = handle
+        self.owned = owned
+        self._keep = []
+
+    @staticmethod
+    def default_solver_database() -> ParameterDatabase:
+        return ParameterDatabase.default_solver_database()
+
+    def set_multigrid_level(self, level: int, n_levels: int, A: FEMatrix, P=None) -> None:
+        """Multigrid::initialize: level 0 = coarsest; P = (row_ptr, cols, vals, n_rows)
+        prolongation from this level to the next finer one."""
+        if P is None:
+            check(lib.pm_solver_set_multigrid_level(self.handle, level, n_levels, A.handle, 0, 0,
+                                                    None, None, None), self.ctx.handle)
+        else:
+            rp, ci, v = (np.ascontiguousarray(P[0], dtype=np.int32), np.ascontiguousarray(P[1], dtype=np.int32),
+                         np.ascontiguousarray(P[2], dtype=np.float64))
+            check(lib.pm_solver_set_multigrid_level(self.handle, level, n_levels, A.handle, rp.size - 1,
+                                                    A.n_rows, _ptr(rp), _ptr(ci), _ptr(v)), self.ctx.handle)
+        self._keep.append(A)
+
+    def update_matrix(self, A: FEMatrix) -> None:
+        check(lib.pm_solver_update_matrix(self.handle, A.handle), self.ctx.handle)
+        self._keep.append(A)
+
+    def solve(self, rhs, sol) -> None:
+        """solve(rhs, sol): device vectors, or numpy arrays (solution written back)."""
+        if isinstance(rhs, DeviceVector):
+            check(lib.pm_solver_solve(self.handle, rhs.ptr, sol.ptr), self.ctx.handle)
+        else:
+            r = np.ascontiguousarray(rhs, dtype=np.float64)
+            if not (isinstance(sol, np.ndarray) and sol.dtype == np.float64 and sol.flags.c_contiguous):
+                raise TypeError("host solution must be a contiguous float64 numpy array")
+            check(lib.pm_solver_solve_host(self.handle, _ptr(r), _ptr(sol), r.size), self.ctx.handle)
+
+    def apply_preconditioner(self, z: DeviceVector, r: DeviceVector) -> None:
+        check(lib.pm_solver_apply_preconditioner(self.handle, z.ptr, r.ptr), self.ctx.handle)
+
+    def last_info(self) -> tuple[int, float, float]:
+        it, res, init = C.c_int(), C.c_double(), C.c_double()
+        check(lib.pm_solver_last_info(self.handle, C.byref(it), C.byref(res), C.byref(init)))
+        return it.value, res.value, init.value
+
+    def residual_history(self) -> np.ndarray:
+        cnt = C.c_int()
+        buf = np.empty(100000, dtype=np.float64)
+        check(lib.pm_solver_residual_history(self.handle, _ptr(buf), buf.size, C.byref(cnt)))
+        return buf[: min(cnt.value, buf.size)].copy()
+
+    def close(self) -> None:
+        if self.owned and self.handle:
+            lib.pm_solver_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Discretization:
+    """Mesh hierarchy + FE spaces + structures + transfer (host set-up)."""
+
+    def __init__(self, geometry: int, root_n: int, n_refine: int, n_levels: int, kind: int = KIND_CD,
+                 elem: int = 1):
+        h = C.c_void_p()
+        check(lib.pm_disc_create(geometry, root_n, n_refine, n_levels, kind, elem, C.byref(h)))
+        self.handle = h
+        self.geometry, self.root_n, self.n_refine, self.n_levels = geometry, root_n, n_refine, n_levels
+        self.kind, self.elem = kind, elem
+        self.dim = 2 if geometry == GEO_SQUARE_QUAD else 3
+
+    def level_info(self, level: int, space: int = 0) -> dict:
+        nc, nl, nd, na = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        nz = C.c_int64()
+        check(lib.pm_disc_level_info(self.handle, level, space, C.byref(nc), C.byref(nl), C.byref(nd),
+                                     C.byref(na), C.byref(nz)))
+        return dict(n_cells=nc.value, nloc=nl.value, n_dofs=nd.value, n_active=na.value, nnz=int(nz.value))
+
+    def dofmap(self, level: int, space: int = 0) -> np.ndarray:
+        i = self.level_info(level, space)
+        out = np.empty(i["n_cells"] * i["nloc"], dtype=np.int32)
+        check(lib.pm_disc_dofmap(self.handle, level, space, _ptr(out)))
+        return out.reshape(i["n_cells"], i["nloc"])
+
+    def cell_vertices(self, level: int) -> np.ndarray:
+        i = self.level_info(level)
+        nv = 4 if self.geometry in (GEO_SQUARE_QUAD, GEO_CUBE_TETRA) else 8
+        out = np.empty(i["n_cells"] * nv * self.dim, dtype=np.float64)
+        check(lib.pm_disc_cell_vertices(self.handle, level, _ptr(out)))
+        return out.reshape(i["n_cells"], nv, self.dim)
+
+    def structure(self, level: int) -> tuple[np.ndarray, np.ndarray]:
+        i = self.level_info(level)
+        n = i["n_dofs"] if self.kind == KIND_CD else None
+        rp = np.empty((n if n is not None else 0) + 1, dtype=np.int32)
+        ci = np.empty(i["nnz"], dtype=np.int32)
+        check(lib.pm_disc_structure(self.handle, level, _ptr(rp), _ptr(ci)))
+        return rp, ci
+
+    def prolongation(self, level: int) -> tuple[np.ndarray, np.ndarray, np.ndarray, int, int]:
+        r, c = C.c_int(), C.c_int()
+        z = C.c_int64()
+        check(lib.pm_disc_prolongation_info(self.handle, level, C.byref(r), C.byref(c), C.byref(z)))
+        rp = np.empty(r.value + 1, dtype=np.int32)
+        ci = np.empty(int(z.value), dtype=np.int32)
+        v = np.empty(int(z.value), dtype=np.float64)
+        check(lib.pm_disc_prolongation(self.handle, level, _ptr(rp), _ptr(ci), _ptr(v)))
+        return rp, ci, v, r.value, c.value
+
+    def close(self) -> None:
+        if self.handle:
+            lib.pm_disc_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cd_coeffs(eps: float, b=(0.0, 0.0, 0.0), c: float = 0.0, manufactured: bool = True,
+              f_const: float = 0.0) -> CdCoeffs:
+    cf = CdCoeffs()
+    cf.eps = eps
+    bb = list(b) + [0.0] * (3 - len(b))
+    for i in range(3):
+        cf.b[i] = bb[i]
+    cf.c = c
+    cf.manufactured = 1 if manufactured else 0
+    cf.f_const = f_const
+    return cf
+
+
+def assemble_cd(ctx: Context, disc: Discretization, level: int, coeffs: CdCoeffs, quad_points: int,
+                A: FEMatrix, rhs: DeviceVector) -> None:
+    """Assemble2D/Assemble3D with the ConvDiff Galerkin local form, on the device."""
+    check(lib.pm_assemble_cd(ctx.handle, disc.handle, level, C.byref(coeffs), quad_points, A.handle,
+                             rhs.ptr), ctx.handle)
+
+
+class ConvectionDiffusion:
+    """ConvectionDiffusion<d> on one GPU: assemble() and solve() as in
+    src/System/ConvectionDiffusion.C:174-209."""
+
+    def __init__(self, ctx: Context, disc: Discretization, coeffs: CdCoeffs, db, quad_points: int = 0):
+        self.ctx = ctx
+        self.disc = disc
+        self.coeffs = coeffs
+        h = C.c_void_p()
+        check(lib.pm_problem_create_cd(ctx.handle, disc.handle, C.byref(coeffs), quad_points,
+                                       _db_text(db).encode(), C.byref(h)), ctx.handle)
+        self.handle = h
+
+    def assemble(self) -> None:
+        check(lib.pm_problem_assemble(self.handle), self.ctx.handle)
+
+    def solve(self) -> None:
+        check(lib.pm_problem_solve(self.handle), self.ctx.handle)
+
+    def size(self) -> tuple[int, int]:
+        n, na = C.c_int(), C.c_int()
+        check(lib.pm_problem_size(self.handle, C.byref(n), C.byref(na)))
+        return n.value, na.value
+
+    def solution(self) -> np.ndarray:
+        out = np.empty(self.size()[0], dtype=np.float64)
+        check(lib.pm_problem_get_solution(self.handle, _ptr(out)), self.ctx.handle)
+        return out
+
+    def rhs(self) -> np.ndarray:
+        out = np.empty(self.size()[0], dtype=np.float64)
+        check(lib.pm_problem_get_rhs(self.handle, _ptr(out)), self.ctx.handle)
+        return out
+
+    def matrix(self, level: int = -1) -> FEMatrix:
+        if level < 0:
+            level = self.disc.n_levels + level
+        h = C.c_void_p()
+        check(lib.pm_problem_matrix(self.handle, level, C.byref(h)))
+        return FEMatrix(self.ctx, h, owned=False)
+
+    def solver(self) -> Solver:
+        h = C.c_void_p()
+        check(lib.pm_problem_solver(self.handle, C.byref(h)))
+        return Solver(self.ctx, None, handle=h, owned=False)
+
+    def last_info(self) -> tuple[int, float, float]:
+        it, res, init = C.c_int(), C.c_double(), C.c_double()
+        check(lib.pm_problem_last_info(self.handle, C.byref(it), C.byref(res), C.byref(init)))
+        return it.value, res.value, init.value
+
+    def run_host(self, coeffs: Optional[CdCoeffs], level_verts, sol_out: np.ndarray) -> None:
+        """one request end to end from host memory (pm_problem_run_host)"""
+        arr = None
+        if level_verts is not None:
+            arr = (C.c_void_p * len(level_verts))(*[C.c_void_p(v.ctypes.data) if v is not None else None
+                                                    for v in level_verts])
+        check(lib.pm_problem_run_host(self.handle, C.byref(coeffs) if coeffs is not None else None,
+                                      arr, _ptr(sol_out)), self.ctx.handle)
+
+    def close(self) -> None:
+        if self.handle:
+            lib.pm_problem_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+__all__ = ["Context", "DeviceVector", "FEMatrix", "Solver", "Discretization", "ConvectionDiffusion",
+           "ParameterDatabase", "PmError", "cd_coeffs", "assemble_cd", "GEO_SQUARE_QUAD", "GEO_CUBE_HEXA",
+           "GEO_CUBE_TETRA", "KIND_CD", "KIND_STOKES"]

@@ -1,0 +1,340 @@
+// Element assembly of convection-diffusion systems on the device.
+//
+// Restates the ParMooN element loop for the Galerkin convection-diffusion form:
+//   Assemble3D (src/AssembleRoutines/Assemble3D.C:228-470) / Assemble2D
+//   (src/AssembleRoutines/Assemble2D.C:6940-7889), LocalAssembling::GetLocalForms
+//   (src/AssembleRoutines/LocalAssembling.C:669-765) and
+//   BilinearAssembleGalerkin<2,3> (src/AssembleRoutines/ConvDiff.C:1794-1856):
+//     K_ij += Mult_q [eps grad phi_i . grad phi_j + (b . grad phi_j) phi_i + c phi_j phi_i]
+//     F_i  += Mult_q phi_i f,      Mult_q = w_q |det J|
+// on affine quadrilaterals/hexahedra (QuadAffin / HexaAffin reference maps,
+// src/FE/QuadAffin.C:614, src/FE/HexaAffin.C:858) with tensor Gauss rules
+// (src/QuadFormulas/QuadFormulaHexa.C:41-120, QuadFormulaQuad.C:43).
+//
+// Stage 1 computes every element matrix into a scratch array, one group of
+// threads per cell. Stage 2 gathers them into the CSR values: every entry sums
+// its contributions in cell order - the order in which the reference's scatter
+// adds them - so the result is deterministic and does not depend on atomics.
+#include <cmath>
+#include <vector>
+
+#include "pm_assemble.h"
+
+namespace pm {
+
+// 1D Gauss rules in the reference's point order
+static void gauss1d(int n, std::vector<double>& x, std::vector<double>& w) {
+  if (n == 2) {
+    x = {-0.5773502691896257645091489, 0.5773502691896257645091489};
+    w = {1.0, 1.0};
+  } else if (n == 3) {
+    x = {-0.7745966692414833770358530, 0.0, 0.7745966692414833770358530};
+    w = {0.5555555555555555555555558, 0.8888888888888888888888888, 0.5555555555555555555555558};
+  } else if (n == 4) {
+    x = {0.33998104358485626480266576, 0.86113631159405257522394649,
+         -0.86113631159405257522394649, -0.33998104358485626480266576};
+    w = {0.652145154862546142626936051, 0.347854845137453857373063949,
+         0.347854845137453857373063949, 0.652145154862546142626936051};
+  } else {
+    throw Error(PM_E_UNSUPPORTED, "tensor Gauss rules with 2, 3 or 4 points per direction");
+  }
+}
+
+static void lag1d(int k, double x, double* l, double* dl) {
+  if (k == 1) {
+    l[0] = 0.5 * (1.0 - x);
+    l[1] = 0.5 * (1.0 + x);
+    dl[0] = -0.5;
+    dl[1] = 0.5;
+  } else {
+    l[0] = 0.5 * x * (x - 1.0);
+    l[1] = 1.0 - x * x;
+    l[2] = 0.5 * x * (x + 1.0);
+    dl[0] = x - 0.5;
+    dl[1] = -2.0 * x;
+    dl[2] = x + 0.5;
+  }
+}
+
+void build_qk_tables(int dim, int k, int qn, RefTables& t) {
+  std::vector<double> x1, w1;
+  gauss1d(qn, x1, w1);
+  const int nb1 = k + 1;
+  t.dim = dim;
+  t.nb = dim == 2 ? nb1 * nb1 : nb1 * nb1 * nb1;
+  t.nq = dim == 2 ? qn * qn : qn * qn * qn;
+  t.w.assign(t.nq, 0.0);
+  t.xi.assign(size_t(t.nq) * 3, 0.0);
+  t.phi.assign(size_t(t.nq) * t.nb, 0.0);
+  t.dphi.assign(size_t(3) * t.nq * t.nb, 0.0);
+  int q = 0;
+  for (int i = 0; i < (dim == 3 ? qn : 1); ++i)
+    for (int j = 0; j < qn; ++j)
+      for (int kk = 0; kk < qn; ++kk, ++q) {
+        const double xs = x1[kk], ys = x1[j], zs = dim == 3 ? x1[i] : 0.0;
+        t.xi[q * 3 + 0] = xs;
+        t.xi[q * 3 + 1] = ys;
+        t.xi[q * 3 + 2] = zs;
+        t.w[q] = dim == 3 ? w1[i] * w1[j] * w1[kk] : w1[j] * w1[kk];
+        double lx[3], ly[3], lz[3] = {1, 1, 1}, dx[3], dy[3], dz[3] = {0, 0, 0};
+        lag1d(k, xs, lx, dx);
+        lag1d(k, ys, ly, dy);
+        if (dim == 3) lag1d(k, zs, lz, dz);
+        int m = 0;
+        for (int c = 0; c < (dim == 3 ? nb1 : 1); ++c)
+          for (int b = 0; b < nb1; ++b)
+            for (int a = 0; a < nb1; ++a, ++m) {
+              const double zc = dim == 3 ? lz[c] : 1.0;
+              t.phi[size_t(q) * t.nb + m] = lx[a] * ly[b] * zc;
+              t.dphi[(size_t(0) * t.nq + q) * t.nb + m] = dx[a] * ly[b] * zc;
+              t.dphi[(size_t(1) * t.nq + q) * t.nb + m] = lx[a] * dy[b] * zc;
+              if (dim == 3) t.dphi[(size_t(2) * t.nq + q) * t.nb + m] = lx[a] * ly[b] * dz[c];
+            }
+      }
+}
+
+// -------------------------------------------------------------- kernels ----
+struct CdCoef {
+  double eps, b0, b1, b2, c, fconst;
+  int manufactured;
+};
+
+// affine map of cell `cell`: origin and Jacobian columns (QuadAffin/HexaAffin)
+template <int DIM>
+__device__ __forceinline__ void affine_map(const double* __restrict__ v, double* x0, double J[3][3]) {
+  if (DIM == 2) {
+    // vertices 0,1,3: xc0 = (x1+x3)/2, xc1 = (x1-x0)/2, xc2 = (x3-x0)/2
+    for (int d = 0; d < 2; ++d) {
+      x0[d] = (v[2 + d] + v[6 + d]) * 0.5;
+      J[d][0] = (v[2 + d] - v[d]) * 0.5;
+      J[d][1] = (v[6 + d] - v[d]) * 0.5;
+    }
+  } else {
+    for (int d = 0; d < 3; ++d) {
+      x0[d] = (v[3 + d] + v[9 + d] + v[12 + d] - v[d]) * 0.5;
+      J[d][0] = (v[3 + d] - v[d]) * 0.5;
+      J[d][1] = (v[9 + d] - v[d]) * 0.5;
+      J[d][2] = (v[12 + d] - v[d]) * 0.5;
+    }
+  }
+}
+
+__device__ __forceinline__ double rhs_value(const CdCoef& k, int dim, const double* x) {
+  if (!k.manufactured) return k.fconst;
+  const double p = 3.14159265358979323846;
+  // exact solution u = prod sin(pi x_d): values, gradient, Laplacian
+  double s[3], co[3];
+  for (int d = 0; d < dim; ++d) {
+    s[d] = sin(p * x[d]);
+    co[d] = cos(p * x[d]);
+  }
+  double u, ux, uy, uz = 0.0, lap;
+  if (dim == 2) {
+    u = s[0] * s[1];
+    ux = p * co[0] * s[1];
+    uy = p * s[0] * co[1];
+    lap = -2 * p * p * s[0] * s[1];
+  } else {
+    u = s[0] * s[1] * s[2];
+    ux = p * co[0] * s[1] * s[2];
+    uy = p * s[0] * co[1] * s[2];
+    uz = p * s[0] * s[1] * co[2];
+    lap = -3 * p * p * s[0] * s[1] * s[2];
+  }
+  double f = -k.eps * lap;
+  f += k.b0 * ux + k.b1 * uy + (dim == 3 ? k.b2 * uz : 0.0);
+  f += k.c * u;
+  return f;
+}
+
+// One group of TPC threads per cell, CPB cells per block. Shared memory per
+// cell: A[q][i][4] = Mult_q (eps dphi_i, phi_i), B[q][j][4] = (dphi_j, b.dphi_j + c phi_j);
+// K_ij = sum_q sum_d A[q][i][d] B[q][j][d].
+template <int DIM, int NB, int NQ, int CPB>
+__global__ void __launch_bounds__(256) k_elem_cd(int n_cells, const double* __restrict__ verts,
+                                                 const double* __restrict__ ref, CdCoef co,
+                                                 double* __restrict__ K, double* __restrict__ F) {
+  extern __shared__ double smem[];
+  constexpr int NV = DIM == 2 ? 4 : 8;
+  constexpr int TPC = 256 / CPB;
+  const int slot = threadIdx.x / TPC;
+  const int t = threadIdx.x % TPC;
+  const int cell = blockIdx.x * CPB + slot;
+  double* A = smem + size_t(slot) * (2 * NQ * NB * 4 + NQ);
+  double* B = A + NQ * NB * 4;
+  double* fq = B + NQ * NB * 4;  // Mult_q * f(x_q)
+  const double* phi = ref;
+  const double* dphi = ref + NQ * NB;
+  const double* w = ref + 4 * NQ * NB;
+  const double* xi = w + NQ;
+  const bool valid = cell < n_cells;
+  double x0[3] = {0, 0, 0}, J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  if (valid) affine_map<DIM>(verts + (size_t)cell * NV * DIM, x0, J);
+  // inverse transpose and |det J|
+  double G[3][3], det;
+  if (DIM == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const double r = 1.0 / det;
+    // grad phi = J^{-T} grad_ref phi
+    G[0][0] = J[1][1] * r;  G[0][1] = -J[1][0] * r;
+    G[1][0] = -J[0][1] * r; G[1][1] = J[0][0] * r;
+  } else {
+    det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+          J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+          J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    const double r = 1.0 / det;
+    // (J^{-1})^T = cofactor(J) / det
+    G[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * r;
+    G[0][1] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) * r;
+    G[0][2] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * r;
+    G[1][0] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * r;
+    G[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+    G[1][2] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * r;
+    G[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+    G[2][1] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) * r;
+    G[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+  }
+  const double adet = fabs(det);
+  // stage A: per (q, i) physical derivatives
+  for (int e = t; e < NQ * NB; e += TPC) {
+    const int q = e / NB, i = e % NB;
+    double g[3] = {0, 0, 0};
+    double dr[3];
+    for (int a = 0; a < DIM; ++a) dr[a] = dphi[(a * NQ + q) * NB + i];
+    for (int d = 0; d < DIM; ++d) {
+      double s = 0.0;
+      for (int a = 0; a < DIM; ++a) s += G[d][a] * dr[a];
+      g[d] = s;
+    }
+    const double ph = phi[q * NB + i];
+    const double mult = w[q] * adet;
+    double* Ai = A + (q * NB + i) * 4;
+    double* Bi = B + (q * NB + i) * 4;
+    Ai[0] = mult * co.eps * g[0];
+    Ai[1] = mult * co.eps * g[1];
+    Ai[2] = DIM == 3 ? mult * co.eps * g[2] : 0.0;
+    Ai[3] = mult * ph;
+    Bi[0] = g[0];
+    Bi[1] = g[1];
+    Bi[2] = DIM == 3 ? g[2] : 0.0;
+    Bi[3] = co.b0 * g[0] + co.b1 * g[1] + (DIM == 3 ? co.b2 * g[2] : 0.0) + co.c * ph;
+  }
+  for (int q = t; q < NQ; q += TPC) {
+    double x[3];
+    for (int d = 0; d < DIM; ++d) {
+      double s = x0[d];
+      for (int a = 0; a < DIM; ++a) s += J[d][a] * xi[q * 3 + a];
+      x[d] = s;
+    }
+    fq[q] = w[q] * adet * rhs_value(co, DIM, x);
+  }
+  __syncthreads();
+  if (!valid) return;
+  double* Kc = K + (size_t)cell * NB * NB;
+  for (int p = t; p < NB * NB; p += TPC) {
+    const int i = p / NB, j = p % NB;
+    double s = 0.0;
+#pragma unroll 3
+    for (int q = 0; q < NQ; ++q) {
+      const double* Ai = A + (q * NB + i) * 4;
+      const double* Bj = B + (q * NB + j) * 4;
+      s += Ai[0] * Bj[0] + Ai[1] * Bj[1] + Ai[2] * Bj[2] + Ai[3] * Bj[3];
+    }
+    Kc[p] = s;
+  }
+  for (int i = t; i < NB; i += TPC) {
+    double s = 0.0;
+    for (int q = 0; q < NQ; ++q) s += fq[q] * phi[q * NB + i];
+    F[(size_t)cell * NB + i] = s;
+  }
+}
+
+// stage 2: CSR values from the element matrices, in cell order
+__global__ void k_gather(int nnz, const int* __restrict__ ptr, const int* __restrict__ idx,
+                         const double* __restrict__ K, double* __restrict__ vals) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int t = ptr[e]; t < ptr[e + 1]; ++t) s += K[idx[t]];
+    vals[e] = s;
+  }
+}
+
+__global__ void k_set_unit(int n, const int* __restrict__ pos, double* __restrict__ vals) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) vals[pos[i]] = 1.0;
+}
+
+template <int DIM, int NB, int NQ, int CPB>
+static void launch_elem(pm_ctx* c, int n_cells, const double* verts, const double* ref,
+                        const CdCoef& co, double* K, double* F) {
+  const size_t sm = size_t(CPB) * (2 * NQ * NB * 4 + NQ) * sizeof(double);
+  auto kern = k_elem_cd<DIM, NB, NQ, CPB>;
+  if (sm > 48 * 1024) PM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+  const int grid = (n_cells + CPB - 1) / CPB;
+  kern<<<grid, 256, sm, c->stream>>>(n_cells, verts, ref, co, K, F);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+void DevAssemblyLevel::upload(pm_ctx* c, const DiscLevel& L, int dim, int nvc) {
+  n_cells = L.n_cells;
+  nloc = L.space.nloc;
+  n_dofs = L.sys.n_rows;
+  verts.upload(L.verts, c->stream);
+  gat_ptr.upload(L.gat_ptr, c->stream);
+  gat_idx.upload(L.gat_idx, c->stream);
+  rgat_ptr.upload(L.rgat_ptr, c->stream);
+  rgat_idx.upload(L.rgat_idx, c->stream);
+  diag_pos.upload(L.diag_pos, c->stream);
+  (void)dim;
+  (void)nvc;
+}
+
+void DevAssemblyLevel::scratch_sizes(size_t& k_elems, size_t& f_elems) const {
+  k_elems = size_t(n_cells) * nloc * nloc;
+  f_elems = size_t(n_cells) * nloc;
+}
+
+void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, int qn,
+                       const pm_cd_coeffs& cf, const DevRefTables& rt, DevCsr& A, double* rhs,
+                       double* K, double* F) {
+  CdCoef co{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured};
+  const int k = elem;
+  if (dim == 2 && k == 1 && qn == 3) launch_elem<2, 4, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 2 && k == 1 && qn == 2) launch_elem<2, 4, 4, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 2 && k == 2 && qn == 3) launch_elem<2, 9, 9, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 2 && k == 2 && qn == 4) launch_elem<2, 9, 16, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 1 && qn == 2) launch_elem<3, 8, 8, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 1 && qn == 3) launch_elem<3, 8, 27, 2>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 2 && qn == 3) launch_elem<3, 27, 27, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 2 && qn == 4) launch_elem<3, 27, 64, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else throw Error(PM_E_UNSUPPORTED, "element / quadrature combination not compiled");
+  const int nnz = int(A.nnz);
+  k_gather<<<std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16)), 256, 0, c->stream>>>(
+      nnz, L.gat_ptr.p, L.gat_idx.p, K, A.vals.p);
+  PM_CHECK_LAUNCH();
+  const int nd = int(L.diag_pos.n);
+  if (nd) {
+    k_set_unit<<<(nd + 255) / 256, 256, 0, c->stream>>>(nd, L.diag_pos.p, A.vals.p);
+    PM_CHECK_LAUNCH();
+  }
+  const int n = L.n_dofs;
+  k_gather<<<std::max(1, std::min((n + 255) / 256, c->num_sms * 16)), 256, 0, c->stream>>>(
+      n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += nd ? 3 : 2;
+}
+
+void DevRefTables::upload(pm_ctx* c, const RefTables& t) {
+  // layout: phi[nq][nb], dphi[3][nq][nb], w[nq], xi[nq][3]
+  std::vector<double> h;
+  h.insert(h.end(), t.phi.begin(), t.phi.end());
+  h.insert(h.end(), t.dphi.begin(), t.dphi.end());
+  h.insert(h.end(), t.w.begin(), t.w.end());
+  h.insert(h.end(), t.xi.begin(), t.xi.end());
+  data.upload(h, c->stream);
+  nb = t.nb;
+  nq = t.nq;
+}
+
+}  // namespace pm

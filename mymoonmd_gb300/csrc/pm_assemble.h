@@ -1,0 +1,38 @@
+// Device assembly of convection-diffusion levels (see pm_assemble.cu).
+#pragma once
+#include <vector>
+
+#include "pm_disc.h"
+#include "pm_linalg.cuh"
+
+namespace pm {
+
+// reference-element tables of a Qk element on a tensor Gauss rule
+struct RefTables {
+  int dim = 0, nb = 0, nq = 0;
+  std::vector<double> w, xi, phi, dphi;
+};
+void build_qk_tables(int dim, int k, int qn, RefTables& t);
+
+struct DevRefTables {
+  int nb = 0, nq = 0;
+  DBuf<double> data;
+  void upload(pm_ctx* c, const RefTables& t);
+};
+
+// device copy of one level's assembly inputs
+struct DevAssemblyLevel {
+  int n_cells = 0, nloc = 0, n_dofs = 0;
+  DBuf<double> verts;
+  DBuf<int> gat_ptr, gat_idx, rgat_ptr, rgat_idx, diag_pos;
+  void upload(pm_ctx* c, const DiscLevel& L, int dim, int nvc);
+  void scratch_sizes(size_t& k_elems, size_t& f_elems) const;
+};
+
+// assemble matrix values and right-hand side of one level; K and F are scratch
+// arrays of n_cells*nloc*nloc and n_cells*nloc doubles
+void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, int qn,
+                       const pm_cd_coeffs& cf, const DevRefTables& rt, DevCsr& A, double* rhs,
+                       double* K, double* F);
+
+}  // namespace pm

@@ -1,0 +1,106 @@
+// Core device plumbing of the GB300 solve path: context (one CUDA stream per
+// context), error state, device buffers and the kernel entry points shared by
+// the matrix, multigrid and Krylov layers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pmgpu.h"
+
+namespace pm {
+
+// Error raised inside the library; the C ABI turns it into a status code.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define PM_CUDA(call)                                                          \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      throw ::pm::Error(PM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define PM_CHECK_LAUNCH() PM_CUDA(cudaGetLastError())
+
+// device buffer owned by the library
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t count) { alloc(count); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count) {
+      cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+      if (e != cudaSuccess) {
+        p = nullptr;
+        cudaGetLastError();
+        throw Error(PM_E_OOM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed");
+      }
+    }
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    if (count != n) alloc(count);
+    if (count) PM_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void upload(const std::vector<T>& v, cudaStream_t s) { upload(v.data(), v.size(), s); }
+  void download(T* h, cudaStream_t s) const {
+    if (n) PM_CUDA(cudaMemcpyAsync(h, p, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+}  // namespace pm
+
+// The context behind the opaque pm_ctx handle.
+struct pm_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  std::string last_error;
+  int verbosity = 1;
+  // pinned host scratch for small device->host reads (residuals, flags)
+  double* host_scalars = nullptr;
+  pm::DBuf<double> dev_scalars;  // device-side scalars (dot results, Givens state)
+  pm::DBuf<double> partials;     // per-block partial sums of reductions
+  int n_partials = 0;
+  uint64_t kernel_launches = 0;  // kernels this library launched on the stream
+  // launch probe: CUDA events around every SpMV-family launch on matrices
+  // with probe_nnz nonzeros (0 = off); resolved by pm_ctx_probe_result
+  int64_t probe_nnz = 0;
+  std::vector<cudaEvent_t> probe_events;  // start/end pairs
+  std::vector<double> probe_bytes;        // algorithmic bytes of each probed launch
+  std::vector<cudaEvent_t> probe_pool;
+};
+
+namespace pm {
+// the number of thread blocks used by every deterministic reduction
+constexpr int kRedBlocks = 304;  // 2 per SM on GB300
+constexpr int kRedThreads = 256;
+
+void ctx_init(pm_ctx* c, int device);
+void ctx_destroy(pm_ctx* c);
+}  // namespace pm

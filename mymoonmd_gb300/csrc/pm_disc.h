@@ -1,0 +1,52 @@
+// Discretisation hierarchy (host): the levels a multigrid solve uses, each with
+// its FE space(s), system CSR pattern, gather plans for the device assembly and
+// the prolongation to the next finer level.
+#pragma once
+#include <memory>
+#include <vector>
+
+#include "pm_setup.h"
+
+namespace pm {
+
+enum ProblemKind { KIND_CD = 0, KIND_STOKES = 1 };
+
+struct DiscLevel {
+  int level_in_hierarchy = 0;
+  int n_cells = 0;
+  pmsetup::Space space;     // CD scalar space / Stokes velocity component space
+  pmsetup::Space pspace;    // Stokes pressure space (unused for CD)
+  pmsetup::Csr sys;         // system pattern (combined blocks for Stokes)
+  std::vector<double> verts;  // cell vertex coordinates
+  // assembly gather plan: for each CSR entry of an active row, the positions
+  // (cell * nloc * nloc + m * nloc + k) of the element-matrix entries that add
+  // to it, in cell order (the order Assemble3D.C:346-370 adds them)
+  std::vector<int> gat_ptr, gat_idx;
+  // right-hand side gather plan: for each active DOF, positions cell*nloc + m
+  std::vector<int> rgat_ptr, rgat_idx;
+  // Dirichlet rows: CSR position of the diagonal entry
+  std::vector<int> diag_pos;
+  // prolongation to the next finer level (rows of the finer level)
+  pmsetup::Csr P;
+  // Stokes block layout of the combined vector [u1 | u2 | u3 | p]
+  int n_blocks = 1;
+  int block_len[4] = {0, 0, 0, 0};
+  int block_active[4] = {0, 0, 0, 0};
+};
+
+struct Disc {
+  int kind = KIND_CD;
+  int geometry = 0, root_n = 1, n_refine = 0, n_levels = 1, elem = 1;
+  pmsetup::Hierarchy h;
+  std::vector<DiscLevel> levels;  // 0 = coarsest kept level
+  int dim() const { return h.dim; }
+  int nvc() const { return h.nvc; }
+};
+
+std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem);
+
+}  // namespace pm
+
+struct pm_disc {
+  std::unique_ptr<pm::Disc> d;
+};

@@ -1,0 +1,554 @@
+// Device linear algebra: CSR SpMV launchers, deterministic BLAS-1 reductions and
+// the dense coarse-grid inverse.
+#include <algorithm>
+#include <cmath>
+
+#include "pm_linalg.cuh"
+
+namespace pm {
+
+// ---------------------------------------------------------------- context ---
+void ctx_init(pm_ctx* c, int device) {
+  c->device = device;
+  PM_CUDA(cudaSetDevice(device));
+  PM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  PM_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+  PM_CUDA(cudaMallocHost(&c->host_scalars, 64 * sizeof(double)));
+  c->dev_scalars.alloc(256);
+  c->partials.alloc(4 * kRedBlocks);
+  c->n_partials = kRedBlocks;
+}
+
+void ctx_destroy(pm_ctx* c) {
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->dev_scalars.release();
+  c->partials.release();
+  if (c->host_scalars) cudaFreeHost(c->host_scalars);
+  c->host_scalars = nullptr;
+  if (c->stream) cudaStreamDestroy(c->stream);
+  c->stream = nullptr;
+}
+
+static inline int nblocks(long long n, int t) { return int((n + t - 1) / t); }
+
+// -------------------------------------------------------------------- CSR ---
+int choose_lanes(double avg) {
+  if (avg <= 6.0) return 4;
+  if (avg <= 12.0) return 8;
+  if (avg <= 28.0) return 16;
+  return 32;
+}
+
+void DevCsr::upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int* ci,
+                    const double* v) {
+  n_rows = nr;
+  n_cols = nc;
+  n_active = na;
+  nnz = rp[nr];
+  row_ptr.upload(rp, size_t(nr) + 1, c->stream);
+  cols.upload(ci, size_t(nnz), c->stream);
+  if (v) vals.upload(v, size_t(nnz), c->stream);
+  else {
+    vals.alloc(size_t(nnz));
+    if (nnz) PM_CUDA(cudaMemsetAsync(vals.p, 0, vals.bytes(), c->stream));
+  }
+  lanes = choose_lanes(nr ? double(nnz) / nr : 1.0);
+  set_single_block();
+}
+
+void DevCsr::set_single_block() {
+  mask = BlockMask{};
+  mask.nb = 1;
+  mask.start[0] = 0;
+  mask.active_end[0] = n_active;
+  mask.end[0] = n_rows;
+}
+
+void DevCsr::set_blocks(int nb, const int* lengths, const int* actives) {
+  if (nb < 1 || nb > 4) throw Error(PM_E_INVALID, "block vectors hold 1..4 blocks");
+  mask = BlockMask{};
+  mask.nb = nb;
+  int off = 0;
+  for (int b = 0; b < nb; ++b) {
+    mask.start[b] = off;
+    mask.active_end[b] = off + actives[b];
+    off += lengths[b];
+    mask.end[b] = off;
+  }
+  if (off != n_rows) throw Error(PM_E_INVALID, "block lengths do not add up to the matrix rows");
+  n_active = 0;
+  for (int b = 0; b < nb; ++b) n_active += actives[b];
+}
+
+__global__ void k_d2f(long long n, const double* __restrict__ x, float* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = float(x[i]);
+}
+__global__ void k_f2d(long long n, const float* __restrict__ x, double* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = double(x[i]);
+}
+
+static int grid_for(pm_ctx* c, long long n) {
+  long long b = (n + 255) / 256;
+  long long cap = (long long)c->num_sms * 8;
+  return int(std::max<long long>(1, std::min(b, cap)));
+}
+
+void DevCsr::make_fp32(pm_ctx* c) {
+  vals32.alloc(size_t(nnz));
+  if (nnz) {
+    k_d2f<<<grid_for(c, nnz), 256, 0, c->stream>>>(nnz, vals.p, vals32.p);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
+  if (diag.p) {
+    diag32.alloc(size_t(n_rows));
+    k_d2f<<<grid_for(c, n_rows), 256, 0, c->stream>>>(n_rows, diag.p, diag32.p);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
+}
+
+// diagonal entries (Iteration_jacobi: extract_diagonal_entries); a missing
+// diagonal entry is recorded as 0 and reported by the caller
+__global__ void k_diag(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                       const double* __restrict__ v, double* __restrict__ d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double r = 0.0;
+  for (int k = rp[i]; k < rp[i + 1]; ++k)
+    if (ci[k] == i) { r = v[k]; break; }
+  d[i] = r;
+}
+
+void DevCsr::make_diag(pm_ctx* c) {
+  diag.alloc(size_t(n_rows));
+  if (n_rows) {
+    k_diag<<<nblocks(n_rows, 256), 256, 0, c->stream>>>(n_rows, row_ptr.p, cols.p, vals.p, diag.p);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
+  if (vals32.p) {
+    diag32.alloc(size_t(n_rows));
+    if (n_rows) {
+      k_d2f<<<grid_for(c, n_rows), 256, 0, c->stream>>>(n_rows, diag.p, diag32.p);
+      PM_CHECK_LAUNCH();
+      c->kernel_launches++;
+    }
+  }
+}
+
+size_t DevCsr::spmv_bytes(int eb, bool read_y) const {
+  // values + column indices + row pointers + x gathered once + y written (+read)
+  return size_t(nnz) * (eb + 4) + size_t(n_rows + 1) * 4 + size_t(n_cols) * eb +
+         size_t(n_rows) * eb * (read_y ? 2 : 1);
+}
+
+template <class TV, class TX, class TA, int EPI>
+static void launch_epi(pm_ctx* c, int G, int n, const int* rp, const int* ci, const TV* v,
+                       const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
+  if (n <= 0) return;
+  const int threads = 256;
+  const int grid = nblocks((long long)n * G, threads);
+  switch (G) {
+    case 4: csr_kernel<TV, TX, TA, 4, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 8: csr_kernel<TV, TX, TA, 8, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 16: csr_kernel<TV, TX, TA, 16, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    default: csr_kernel<TV, TX, TA, 32, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+  }
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+static cudaEvent_t probe_event(pm_ctx* c) {
+  if (!c->probe_pool.empty()) {
+    cudaEvent_t e = c->probe_pool.back();
+    c->probe_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  PM_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+// algorithmic bytes of one SpMV-family launch: values, column indices, row
+// pointers, the gathered vector once, and the per-row vectors the epilogue
+// reads and writes
+static double epi_bytes(const DevCsr& A, int epi, int eb, int n) {
+  double rows_vec = 1.0;  // y written
+  if (epi == EPI_AXPY || epi == EPI_PROLONG) rows_vec += 1.0;  // y read
+  if (epi == EPI_DEFECT) rows_vec += 1.0;                      // b read
+  if (epi == EPI_JACOBI) rows_vec += 2.0;                      // b and diag read
+  return double(A.nnz) * (eb + 4) + double(n + 1) * 4 + double(A.n_cols) * eb + double(n) * eb * rows_vec;
+}
+
+template <class TV, class TX, class TA>
+static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* diag, int epi,
+                         const TX* x, TX* y, const TX* b, TA alpha, int n) {
+  const int G = A.lanes;
+  const int* rp = A.row_ptr.p;
+  const int* ci = A.cols.p;
+  const bool probe = c->probe_nnz != 0 && A.nnz == c->probe_nnz;
+  if (probe) {
+    cudaEvent_t e0 = probe_event(c);
+    PM_CUDA(cudaEventRecord(e0, c->stream));
+    c->probe_events.push_back(e0);
+    c->probe_bytes.push_back(epi_bytes(A, epi, int(sizeof(TV)), n));
+  }
+  switch (epi) {
+    case EPI_AXPY: launch_epi<TV, TX, TA, EPI_AXPY>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_SET: launch_epi<TV, TX, TA, EPI_SET>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_DEFECT: launch_epi<TV, TX, TA, EPI_DEFECT>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_JACOBI: launch_epi<TV, TX, TA, EPI_JACOBI>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_RESTRICT: launch_epi<TV, TX, TA, EPI_RESTRICT>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_PROLONG: launch_epi<TV, TX, TA, EPI_PROLONG>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
+  }
+  if (probe) {
+    cudaEvent_t e1 = probe_event(c);
+    PM_CUDA(cudaEventRecord(e1, c->stream));
+    c->probe_events.push_back(e1);
+  }
+}
+
+void probe_reset(pm_ctx* c, int64_t nnz) {
+  for (auto e : c->probe_events) c->probe_pool.push_back(e);
+  c->probe_events.clear();
+  c->probe_bytes.clear();
+  c->probe_nnz = nnz;
+}
+
+void probe_result(pm_ctx* c, int* count, double* total_ms, double* total_bytes) {
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  const int pairs = int(c->probe_events.size() / 2);
+  double ms = 0.0, bytes = 0.0;
+  for (int i = 0; i < pairs; ++i) {
+    float t = 0.0f;
+    PM_CUDA(cudaEventElapsedTime(&t, c->probe_events[2 * i], c->probe_events[2 * i + 1]));
+    ms += t;
+    bytes += c->probe_bytes[i];
+  }
+  *count = pairs;
+  *total_ms = ms;
+  *total_bytes = bytes;
+}
+
+void csr_apply(pm_ctx* c, const DevCsr& A, int epi, const double* x, double* y, const double* b,
+               double alpha, int n_rows_override) {
+  if (epi == EPI_JACOBI && !A.diag.p) throw Error(PM_E_INVALID, "Jacobi sweep without diagonal");
+  csr_dispatch<double, double, double>(c, A, A.vals.p, A.diag.p, epi, x, y, b, alpha,
+                                       n_rows_override >= 0 ? n_rows_override : A.n_rows);
+}
+
+void csr_apply32(pm_ctx* c, const DevCsr& A, int epi, const float* x, float* y, const float* b,
+                 float alpha, int n_rows_override) {
+  if (!A.vals32.p && A.nnz) throw Error(PM_E_INVALID, "matrix has no FP32 copy");
+  if (epi == EPI_JACOBI && !A.diag32.p) throw Error(PM_E_INVALID, "Jacobi sweep without FP32 diagonal");
+  csr_dispatch<float, float, float>(c, A, A.vals32.p, A.diag32.p, epi, x, y, b, alpha,
+                                    n_rows_override >= 0 ? n_rows_override : A.n_rows);
+}
+
+// ------------------------------------------------------------------ BLAS-1 ---
+// block-level sum with a fixed tree (deterministic)
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  const int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (t < s) sh[t] += sh[t + s];
+    __syncthreads();
+  }
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_dot_partials(int n, const T* __restrict__ x,
+                                                      const T* __restrict__ y,
+                                                      double* __restrict__ part) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    s += double(x[i]) * double(y[i]);
+  double r = block_sum(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+__global__ void k_finish_sum(const double* __restrict__ part, int np, double* out, int take_sqrt) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  double r = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = take_sqrt ? sqrt(r) : r;
+}
+
+void dot_partials(pm_ctx* c, int n, const double* x, const double* y, double* partials) {
+  k_dot_partials<double><<<kRedBlocks, kRedThreads, 0, c->stream>>>(n, x, y, partials);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+void finish_sum(pm_ctx* c, const double* partials, double* out, bool take_sqrt) {
+  k_finish_sum<<<1, 256, 0, c->stream>>>(partials, kRedBlocks, out, take_sqrt ? 1 : 0);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+double dot_host(pm_ctx* c, int n, const double* x, const double* y) {
+  dot_partials(c, n, x, y, c->partials.p);
+  finish_sum(c, c->partials.p, c->dev_scalars.p, false);
+  PM_CUDA(cudaMemcpyAsync(c->host_scalars, c->dev_scalars.p, sizeof(double),
+                          cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  return c->host_scalars[0];
+}
+
+template <class T>
+__global__ void k_copy(long long n, const T* __restrict__ x, T* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = x[i];
+}
+__global__ void k_set(long long n, double* __restrict__ y, double v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = v;
+}
+__global__ void k_scale(long long n, double* __restrict__ y, double a) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] *= a;
+}
+__global__ void k_axpy(long long n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+__global__ void k_axpby(long long n, double a, const double* __restrict__ x, double b,
+                        double* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+__global__ void k_div(long long n, const double* __restrict__ d, double* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] /= d[i];
+}
+template <class T>
+__global__ void k_init_sol(int n, BlockMask m, const T* __restrict__ rhs, T* __restrict__ sol) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    sol[i] = row_is_active(m, i) ? T(0) : rhs[i];
+}
+
+#define PM_LAUNCH1D(kern, n, ...)                                                     \
+  do {                                                                                \
+    if ((n) > 0) {                                                                    \
+      kern<<<grid_for(c, (n)), 256, 0, c->stream>>>(__VA_ARGS__);                     \
+      PM_CHECK_LAUNCH();                                                              \
+      c->kernel_launches++;                                                           \
+    }                                                                                 \
+  } while (0)
+
+void vcopy(pm_ctx* c, int n, const double* x, double* y) { PM_LAUNCH1D(k_copy<double>, n, n, x, y); }
+void vcopy32(pm_ctx* c, int n, const float* x, float* y) { PM_LAUNCH1D(k_copy<float>, n, n, x, y); }
+void vset(pm_ctx* c, int n, double* y, double v) { PM_LAUNCH1D(k_set, n, n, y, v); }
+void vscale(pm_ctx* c, int n, double* y, double a) { PM_LAUNCH1D(k_scale, n, n, y, a); }
+void vaxpy(pm_ctx* c, int n, double a, const double* x, double* y) { PM_LAUNCH1D(k_axpy, n, n, a, x, y); }
+void vaxpby(pm_ctx* c, int n, double a, const double* x, double b, double* y) {
+  PM_LAUNCH1D(k_axpby, n, n, a, x, b, y);
+}
+void vdiv(pm_ctx* c, int n, const double* d, double* y) { PM_LAUNCH1D(k_div, n, n, d, y); }
+void vcvt_d2f(pm_ctx* c, int n, const double* x, float* y) { PM_LAUNCH1D(k_d2f, n, n, x, y); }
+void vcvt_f2d(pm_ctx* c, int n, const float* x, double* y) { PM_LAUNCH1D(k_f2d, n, n, x, y); }
+void init_solution(pm_ctx* c, int n, const BlockMask& m, const double* rhs, double* sol) {
+  PM_LAUNCH1D(k_init_sol<double>, n, n, m, rhs, sol);
+}
+void init_solution32(pm_ctx* c, int n, const BlockMask& m, const float* rhs, float* sol) {
+  PM_LAUNCH1D(k_init_sol<float>, n, n, m, rhs, sol);
+}
+
+// ------------------------------------------------------- dense inverse ------
+__global__ void k_dense_fill(int na, const int* __restrict__ act, const int* __restrict__ pos,
+                             const int* __restrict__ rp, const int* __restrict__ ci,
+                             const double* __restrict__ v, double* __restrict__ M) {
+  int ia = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ia >= na) return;
+  const int i = act[ia];
+  double* row = M + (size_t)ia * na;
+  for (int j = 0; j < na; ++j) row[j] = 0.0;
+  for (int k = rp[i]; k < rp[i + 1]; ++k) {
+    const int jp = pos[ci[k]];
+    if (jp >= 0) row[jp] = v[k];
+  }
+}
+
+// pivot search, row swap and pivot-row scaling of Gauss-Jordan step k
+__global__ void __launch_bounds__(256) k_gj_pivot(int na, int k, double* __restrict__ M,
+                                                  int* __restrict__ perm, double* __restrict__ colk,
+                                                  int* __restrict__ flag) {
+  __shared__ double sv[256];
+  __shared__ int si[256];
+  const int t = threadIdx.x;
+  double best = -1.0;
+  int bi = na;
+  for (int i = k + t; i < na; i += blockDim.x) {
+    const double a = fabs(M[(size_t)i * na + k]);
+    if (a > best) { best = a; bi = i; }
+  }
+  sv[t] = best;
+  si[t] = bi;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (t < s) {
+      if (sv[t + s] > sv[t] || (sv[t + s] == sv[t] && si[t + s] < si[t])) {
+        sv[t] = sv[t + s];
+        si[t] = si[t + s];
+      }
+    }
+    __syncthreads();
+  }
+  const int p = si[0];
+  const bool singular = !(sv[0] > 0.0);
+  if (t == 0) {
+    perm[k] = singular ? k : p;
+    if (singular) *flag = 1;
+  }
+  if (!singular && p != k)
+    for (int j = t; j < na; j += blockDim.x) {
+      double a = M[(size_t)k * na + j];
+      M[(size_t)k * na + j] = M[(size_t)p * na + j];
+      M[(size_t)p * na + j] = a;
+    }
+  __syncthreads();
+  const double piv = singular ? 1.0 : M[(size_t)k * na + k];
+  for (int i = t; i < na; i += blockDim.x) {
+    colk[i] = (i == k) ? 0.0 : M[(size_t)i * na + k];
+  }
+  __syncthreads();
+  for (int i = t; i < na; i += blockDim.x)
+    if (i != k) M[(size_t)i * na + k] = 0.0;
+  __syncthreads();
+  if (t == 0) M[(size_t)k * na + k] = 1.0;
+  __syncthreads();
+  for (int j = t; j < na; j += blockDim.x) M[(size_t)k * na + j] /= piv;
+}
+
+__global__ void k_gj_update(int na, int k, double* __restrict__ M, const double* __restrict__ colk) {
+  const long long total = (long long)na * na;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = int(e / na), j = int(e % na);
+    if (i == k) continue;
+    const double f = colk[i];
+    if (f != 0.0) M[e] -= f * M[(size_t)k * na + j];
+  }
+}
+
+__global__ void k_gj_unswap(int na, double* __restrict__ M, const int* __restrict__ perm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= na) return;
+  double* row = M + (size_t)i * na;
+  for (int k = na - 1; k >= 0; --k) {
+    const int p = perm[k];
+    if (p != k) {
+      double a = row[k];
+      row[k] = row[p];
+      row[p] = a;
+    }
+  }
+}
+
+void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
+  n = A.n_rows;
+  std::vector<int> h_act, h_pos(n, -1);
+  for (int i = 0; i < n; ++i) {
+    bool active = false;
+    for (int b = 0; b < A.mask.nb; ++b)
+      if (i >= A.mask.start[b] && i < A.mask.end[b]) active = i < A.mask.active_end[b];
+    if (active) {
+      h_pos[i] = int(h_act.size());
+      h_act.push_back(i);
+    }
+  }
+  na = int(h_act.size());
+  if (na > 20000) throw Error(PM_E_UNSUPPORTED, "coarse direct solve limited to 20000 active rows");
+  act.upload(h_act, c->stream);
+  pos.upload(h_pos, c->stream);
+  inv.alloc(size_t(na) * na);
+  tmp.alloc(std::max(na, 1));
+  perm.alloc(std::max(na, 1));
+  flag.alloc(1);
+  PM_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c->stream));
+  if (na == 0) return;
+  k_dense_fill<<<nblocks(na, 128), 128, 0, c->stream>>>(na, act.p, pos.p, A.row_ptr.p, A.cols.p,
+                                                        A.vals.p, inv.p);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+  const int ugrid = std::max(1, std::min(nblocks((long long)na * na, 256), c->num_sms * 8));
+  for (int k = 0; k < na; ++k) {
+    k_gj_pivot<<<1, 256, 0, c->stream>>>(na, k, inv.p, perm.p, tmp.p, flag.p);
+    k_gj_update<<<ugrid, 256, 0, c->stream>>>(na, k, inv.p, tmp.p);
+    c->kernel_launches += 2;
+  }
+  PM_CHECK_LAUNCH();
+  k_gj_unswap<<<nblocks(na, 128), 128, 0, c->stream>>>(na, inv.p, perm.p);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+  int h_flag = 0;
+  PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  if (h_flag) throw Error(PM_E_BREAKDOWN, "coarse matrix is singular (zero pivot)");
+}
+
+// tmp_a = b_a - sum over non-active columns of A_{a,j} b_j
+__global__ void k_coarse_rhs(int na, const int* __restrict__ act, const int* __restrict__ pos,
+                             const int* __restrict__ rp, const int* __restrict__ ci,
+                             const double* __restrict__ v, const double* __restrict__ b,
+                             double* __restrict__ tmp) {
+  int ia = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ia >= na) return;
+  const int i = act[ia];
+  double r = b[i];
+  for (int k = rp[i]; k < rp[i + 1]; ++k)
+    if (pos[ci[k]] < 0) r -= v[k] * b[ci[k]];
+  tmp[ia] = r;
+}
+
+// x_a = inv * tmp (one warp per row), x_n = b_n
+__global__ void k_coarse_gemv(int n, int na, const int* __restrict__ act, const int* __restrict__ pos,
+                              const double* __restrict__ inv, const double* __restrict__ tmp,
+                              const double* __restrict__ b, double* __restrict__ x) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp < na) {
+    const double* row = inv + (size_t)warp * na;
+    double s = 0.0;
+    for (int j = lane; j < na; j += 32) s += row[j] * tmp[j];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) x[act[warp]] = s;
+  } else {
+    // remaining threads copy the non-active entries
+    const int t = (warp - na) * 32 + lane;
+    if (t < n && pos[t] < 0) x[t] = b[t];
+  }
+}
+
+void DenseInverse::solve(pm_ctx* c, const DevCsr& A, const double* b, double* x) {
+  if (na > 0) {
+    k_coarse_rhs<<<nblocks(na, 128), 128, 0, c->stream>>>(na, act.p, pos.p, A.row_ptr.p, A.cols.p,
+                                                          A.vals.p, b, tmp.p);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
+  const long long threads = (long long)(na + (n + 31) / 32) * 32;
+  k_coarse_gemv<<<nblocks(threads, 256), 256, 0, c->stream>>>(n, na, act.p, pos.p, inv.p, tmp.p, b, x);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+}  // namespace pm

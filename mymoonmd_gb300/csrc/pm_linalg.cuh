@@ -1,0 +1,75 @@
+// Internal device linear algebra: CSR matrices, deterministic BLAS-1, dense
+// coarse-grid inverse. Shared by the multigrid, Krylov, assembly and serving
+// layers; the C ABI in pm_capi.cpp wraps these.
+#pragma once
+#include "pm_core.h"
+#include "pm_spmv.cuh"
+
+namespace pm {
+
+// device CSR with optional FP32 copy of the values
+struct DevCsr {
+  int n_rows = 0, n_cols = 0, n_active = 0;
+  int64_t nnz = 0;
+  int lanes = 8;  // lanes per row in the SpMV kernels
+  BlockMask mask{};
+  DBuf<int> row_ptr, cols;
+  DBuf<double> vals;
+  DBuf<float> vals32;
+  DBuf<double> diag;
+  DBuf<float> diag32;
+
+  void upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int* ci, const double* v);
+  void set_single_block();
+  void set_blocks(int nb, const int* lengths, const int* actives);
+  void make_fp32(pm_ctx* c);
+  void make_diag(pm_ctx* c);  // FP64 diagonal (and FP32 copy if vals32 exists)
+  size_t spmv_bytes(int elem_bytes, bool read_y) const;
+};
+
+int choose_lanes(double avg_nnz_per_row);
+
+// y := epilogue(A x); see pm_spmv.cuh for the epilogue meanings
+void csr_apply(pm_ctx* c, const DevCsr& A, int epi, const double* x, double* y, const double* b,
+               double alpha, int n_rows_override = -1);
+void csr_apply32(pm_ctx* c, const DevCsr& A, int epi, const float* x, float* y, const float* b,
+                 float alpha, int n_rows_override = -1);
+
+// launch probe of SpMV-family kernels on matrices with `nnz` nonzeros
+void probe_reset(pm_ctx* c, int64_t nnz);
+void probe_result(pm_ctx* c, int* count, double* total_ms, double* total_bytes);
+
+// BLAS-1 (deterministic fixed-tree reductions)
+void dot_partials(pm_ctx* c, int n, const double* x, const double* y, double* partials);
+double dot_host(pm_ctx* c, int n, const double* x, const double* y);  // synchronising
+void finish_sum(pm_ctx* c, const double* partials, double* out, bool take_sqrt);
+void vcopy(pm_ctx* c, int n, const double* x, double* y);
+void vset(pm_ctx* c, int n, double* y, double v);
+void vscale(pm_ctx* c, int n, double* y, double a);
+void vaxpy(pm_ctx* c, int n, double a, const double* x, double* y);  // y += a x
+void vaxpby(pm_ctx* c, int n, double a, const double* x, double b, double* y);  // y = a x + b y
+void vcvt_d2f(pm_ctx* c, int n, const double* x, float* y);
+void vcvt_f2d(pm_ctx* c, int n, const float* x, double* y);
+void vcopy32(pm_ctx* c, int n, const float* x, float* y);
+// sol := 0 on active rows, rhs on non-active rows (Multigrid::cycle start)
+void init_solution(pm_ctx* c, int n, const BlockMask& m, const double* rhs, double* sol);
+void init_solution32(pm_ctx* c, int n, const BlockMask& m, const float* rhs, float* sol);
+void vdiv(pm_ctx* c, int n, const double* d, double* y);  // y /= d
+
+// dense inverse of the active block of a small CSR matrix (Gauss-Jordan with
+// partial pivoting on the device); used by the coarse-grid direct solve
+struct DenseInverse {
+  int n = 0;         // rows of the full matrix
+  int na = 0;        // active rows (the inverted block)
+  DBuf<double> inv;  // na x na row-major
+  DBuf<int> act;     // active row indices (na)
+  DBuf<int> pos;     // row -> position among the active rows, -1 if non-active
+  DBuf<double> tmp;  // na
+  DBuf<int> perm;    // pivot rows (na)
+  DBuf<int> flag;    // singular pivot flag
+  void build(pm_ctx* c, const DevCsr& A);
+  // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active)
+  void solve(pm_ctx* c, const DevCsr& A, const double* b, double* x);
+};
+
+}  // namespace pm

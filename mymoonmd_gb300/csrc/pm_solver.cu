@@ -1,0 +1,664 @@
+// Multigrid cycle and Krylov methods on the device.
+//
+// The control flow restates src/Multigrid/Multigrid.C:157-420 (cycle,
+// cycle_step, restriction, damped prolongation), src/Solver/Iteration_gmres.C
+// :376-532 (flexible GMRES with modified Gram-Schmidt and Givens rotations),
+// Iteration_cg.C:22-79, Iteration_bicgstab.C:28-206, Iteration_jacobi.C:31-105
+// and the stopping test of include/Solver/IterativeMethod.h:81-140. All vector
+// work stays on the device; FGMRES keeps H, the Givens state and the scalars
+// of Gram-Schmidt on the device and reads back one residual per iteration for
+// the host-side stopping test.
+#include <algorithm>
+#include <cmath>
+#include <sstream>
+
+#include "pm_solver.h"
+
+namespace pm {
+
+// ---------------------------------------------------------------- params ---
+static std::string trim(const std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r\"'");
+  size_t b = s.find_last_not_of(" \t\r\"'");
+  return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+Params Params::parse(const char* text) {
+  Params p;
+  if (!text) return p;
+  std::istringstream in(text);
+  std::string line;
+  while (std::getline(in, line)) {
+    size_t hash = line.find('#');
+    if (hash != std::string::npos) line = line.substr(0, hash);
+    size_t sep = line.find(':');
+    if (sep == std::string::npos) sep = line.find('=');
+    if (sep == std::string::npos) continue;
+    std::string k = trim(line.substr(0, sep)), v = trim(line.substr(sep + 1));
+    if (!k.empty()) p.kv[k] = v;
+  }
+  return p;
+}
+
+std::string Params::str(const std::string& k, const std::string& def) const {
+  auto it = kv.find(k);
+  return it == kv.end() ? def : it->second;
+}
+double Params::num(const std::string& k, double def) const {
+  auto it = kv.find(k);
+  if (it == kv.end()) return def;
+  char* end = nullptr;
+  double v = strtod(it->second.c_str(), &end);
+  if (end == it->second.c_str()) throw Error(PM_E_INVALID, "parameter " + k + " is not a number");
+  return v;
+}
+long Params::integer(const std::string& k, long def) const {
+  return long(num(k, double(def)));
+}
+
+// ------------------------------------------------------- cycle control -----
+static void fill_recursively(std::vector<int>& out, std::vector<int>& rec, int level, int n_levels,
+                             bool fcycle) {
+  if (level == 0) {
+    out.push_back(DIR_UP);
+    return;
+  }
+  for (int j = 0; j < rec[level]; ++j) {
+    out.push_back(DIR_DOWN);
+    fill_recursively(out, rec, level - 1, n_levels, fcycle);
+  }
+  if (fcycle) rec[level] = 1;
+  out.push_back(level == n_levels - 1 ? DIR_END : DIR_UP);
+}
+
+std::vector<int> cycle_control(const std::string& type, int n_levels) {
+  std::vector<int> rec(n_levels, type == "V" ? 1 : 2);
+  rec[n_levels - 1] = 1;
+  std::vector<int> out{DIR_DUMMY};
+  fill_recursively(out, rec, n_levels - 1, n_levels, type == "F");
+  return out;
+}
+
+// ------------------------------------------------------------ multigrid ----
+static int smoother_code(const std::string& s) {
+  if (s == "jacobi") return SM_JACOBI;
+  if (s == "direct_solve") return SM_DIRECT;
+  if (s == "cell_vanka") return SM_CELL_VANKA;
+  if (s == "cell_vanka_jacobi") return SM_CELL_VANKA_JACOBI;
+  throw Error(PM_E_UNSUPPORTED, "multigrid smoother '" + s + "' is not implemented on the GPU");
+}
+
+void Multigrid::configure(const Params& p) {
+  n_pre = int(p.integer("multigrid_n_pre_smooth", 1));
+  n_post = int(p.integer("multigrid_n_post_smooth", 1));
+  jacobi_damp = p.num("jacobi_damp", 1.0);
+  correction_damp = p.num("multigrid_correction_damp_factor", 1.0);
+  coarse_residual = p.num("multigrid_coarse_residual", 0.1);
+  coarse_max_it = int(p.integer("multigrid_coarse_max_n_iterations", 10));
+  cycle_type = p.str("multigrid_cycle_type", "V");
+  if (cycle_type != "V" && cycle_type != "W" && cycle_type != "F") cycle_type = "V";
+  smoother = smoother_code(p.str("multigrid_smoother", "jacobi"));
+  smoother_coarse = smoother_code(p.str("multigrid_smoother_coarse", "direct_solve"));
+  std::string type = p.str("multigrid_type", "standard");
+  if (type != "standard") throw Error(PM_E_UNSUPPORTED, "only standard multigrid is implemented");
+  mixed = p.str("gpu_precision", "fp64") == "mixed";
+}
+
+void Multigrid::update(pm_ctx* c) {
+  const int L = int(levels.size());
+  if (L < 2) throw Error(PM_E_INVALID, "for multigrid you need at least two multigrid levels");
+  for (int l = 0; l < L; ++l)
+    if (!levels[l].A) throw Error(PM_E_INVALID, "multigrid level " + std::to_string(l) + " has no matrix");
+  control = cycle_control(cycle_type, L);
+  for (int l = 0; l < L; ++l) {
+    MGLevel& lv = levels[l];
+    DevCsr& A = lv.A->csr;
+    lv.smoother = (l == 0) ? smoother_coarse : smoother;
+    if (lv.smoother == SM_CELL_VANKA || lv.smoother == SM_CELL_VANKA_JACOBI)
+      throw Error(PM_E_UNSUPPORTED, "Vanka smoothers need the Stokes problem set-up");
+    if (lv.smoother == SM_JACOBI) A.make_diag(c);
+    const int n = A.n_rows;
+    if (l < L - 1) {
+      if (!lv.P.row_ptr.p) throw Error(PM_E_INVALID, "missing prolongation of level " + std::to_string(l));
+      lv.P.mask = levels[l + 1].A->csr.mask;
+      lv.R.mask = A.mask;
+    }
+    if (mixed) {
+      if (!A.vals32.p) A.make_fp32(c);
+      else if (lv.smoother == SM_JACOBI && !A.diag32.p) A.make_fp32(c);
+      if (l < L - 1) {
+        lv.P.make_fp32(c);
+        lv.R.make_fp32(c);
+      }
+      lv.rhs32.alloc(n);
+      lv.sol32.alloc(n);
+      lv.alt32.alloc(n);
+      lv.defect32.alloc(n);
+    }
+    // FP64 buffers (the finest level uses the caller's vectors in FP64 mode
+    // but keeps its own for the Jacobi ping-pong)
+    lv.rhs.alloc(n);
+    lv.sol.alloc(n);
+    lv.alt.alloc(n);
+    lv.defect.alloc(n);
+    if (lv.smoother == SM_DIRECT) {
+      lv.coarse.build(c, A);
+      if (mixed) {
+        lv.coarse_rhs64.alloc(n);
+        lv.coarse_sol64.alloc(n);
+      }
+    }
+  }
+  ready = true;
+}
+
+void Multigrid::smooth(pm_ctx* c, int l) {
+  MGLevel& lv = levels[l];
+  const DevCsr& A = lv.A->csr;
+  if (lv.smoother == SM_JACOBI) {
+    if (mixed) {
+      csr_apply32(c, A, EPI_JACOBI, lv.cur32, lv.oth32, lv.rhs32.p, float(jacobi_damp));
+      std::swap(lv.cur32, lv.oth32);
+    } else {
+      csr_apply(c, A, EPI_JACOBI, lv.cur, lv.oth, lv.rhs.p, jacobi_damp);
+      std::swap(lv.cur, lv.oth);
+    }
+  } else if (lv.smoother == SM_DIRECT) {
+    coarse_solve(c);
+  }
+}
+
+void Multigrid::coarse_solve(pm_ctx* c) {
+  MGLevel& lv = levels[0];
+  const DevCsr& A = lv.A->csr;
+  if (mixed) {
+    vcvt_f2d(c, A.n_rows, lv.rhs32.p, lv.coarse_rhs64.p);
+    lv.coarse.solve(c, A, lv.coarse_rhs64.p, lv.coarse_sol64.p);
+    vcvt_d2f(c, A.n_rows, lv.coarse_sol64.p, lv.cur32);
+  } else {
+    lv.coarse.solve(c, A, lv.rhs.p, lv.cur);
+  }
+}
+
+void Multigrid::defect(pm_ctx* c, int l) {
+  MGLevel& lv = levels[l];
+  if (mixed) csr_apply32(c, lv.A->csr, EPI_DEFECT, lv.cur32, lv.defect32.p, lv.rhs32.p, 1.0f);
+  else csr_apply(c, lv.A->csr, EPI_DEFECT, lv.cur, lv.defect.p, lv.rhs.p, 1.0);
+}
+
+void Multigrid::restrict_to(pm_ctx* c, int l) {
+  MGLevel& fine = levels[l];
+  MGLevel& crs = levels[l - 1];
+  // DefectRestriction followed by ResetNonActive of the coarse rhs
+  if (mixed) csr_apply32(c, crs.R, EPI_RESTRICT, fine.defect32.p, crs.rhs32.p, nullptr, 1.0f);
+  else csr_apply(c, crs.R, EPI_RESTRICT, fine.defect.p, crs.rhs.p, nullptr, 1.0);
+}
+
+void Multigrid::prolongate_from(pm_ctx* c, int l) {
+  MGLevel& crs = levels[l];
+  MGLevel& fine = levels[l + 1];
+  if (mixed)
+    csr_apply32(c, crs.P, EPI_PROLONG, crs.cur32, fine.cur32, nullptr, float(correction_damp));
+  else
+    csr_apply(c, crs.P, EPI_PROLONG, crs.cur, fine.cur, nullptr, correction_damp);
+}
+
+void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol) {
+  if (!ready) throw Error(PM_E_INVALID, "multigrid used before update()");
+  const int L = int(levels.size());
+  const int finest = L - 1;
+  MGLevel& top = levels[finest];
+  const int nf = top.A->csr.n_rows;
+  for (auto& lv : levels) {
+    lv.cur = lv.sol.p;
+    lv.oth = lv.alt.p;
+    lv.cur32 = lv.sol32.p;
+    lv.oth32 = lv.alt32.p;
+  }
+  // set_finest_rhs / set_finest_sol; cycle(): solution := 0, copy_nonactive(rhs)
+  if (mixed) {
+    vcvt_d2f(c, nf, rhs, top.rhs32.p);
+    init_solution32(c, nf, top.A->csr.mask, top.rhs32.p, top.cur32);
+  } else {
+    vcopy(c, nf, rhs, top.rhs.p);
+    init_solution(c, nf, top.A->csr.mask, top.rhs.p, top.cur);
+  }
+  const int n_steps = int(control.size()) - 1;
+  int level = finest;
+  for (int step = 1; step <= n_steps && level >= 0; ++step) {
+    if (level == 0) {
+      // coarsest level: with the direct solver one application solves exactly;
+      // the defects the reference computes around it only feed its loop test
+      if (levels[0].smoother == SM_DIRECT) {
+        coarse_solve(c);
+      } else {
+        for (int i = 0; i < coarse_max_it; ++i) smooth(c, 0);
+      }
+      prolongate_from(c, 0);
+      level = 1;
+      continue;
+    }
+    const bool from_below = control[step - 1] == DIR_UP;
+    const bool up = control[step] == DIR_UP;
+    const bool down = control[step] == DIR_DOWN;
+    if (from_below)
+      for (int i = 0; i < n_post; ++i) smooth(c, level);
+    if (down) {
+      for (int i = 0; i < n_pre; ++i) smooth(c, level);
+      defect(c, level);
+      MGLevel& crs = levels[level - 1];
+      const int nc = crs.A->csr.n_rows;
+      if (mixed) PM_CUDA(cudaMemsetAsync(crs.cur32, 0, sizeof(float) * nc, c->stream));
+      else PM_CUDA(cudaMemsetAsync(crs.cur, 0, sizeof(double) * nc, c->stream));
+      restrict_to(c, level);
+      level -= 1;
+    } else if (up) {
+      prolongate_from(c, level);
+      level += 1;
+    } else {
+      level = -1;
+    }
+  }
+  if (mixed) vcvt_f2d(c, nf, top.cur32, sol);
+  else vcopy(c, nf, top.cur, sol);
+}
+
+static int grid_blocks_for(int n) { return std::max(1, std::min((n + 255) / 256, 1216)); }
+
+// ------------------------------------------------------ FGMRES kernels -----
+// every block sums the partials of the previous reduction in the same order
+__device__ __forceinline__ double sum_partials(const double* __restrict__ part, double* sh) {
+  const int t = threadIdx.x;
+  double s = 0.0;
+  for (int i = t; i < kRedBlocks; i += blockDim.x) s += part[i];
+  sh[t] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (t < k) sh[t] += sh[t + k];
+    __syncthreads();
+  }
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ void block_partial(double v, double* sh, double* out) {
+  const int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (t < k) sh[t] += sh[t + k];
+    __syncthreads();
+  }
+  if (t == 0) out[blockIdx.x] = sh[0];
+}
+
+// H(k,i) = <r, v_k>; r -= H(k,i) v_k; partial sums of <r, next>
+__global__ void __launch_bounds__(256) k_fg_mgs(int n, int ldh, int k, int i, double* __restrict__ r,
+                                                const double* __restrict__ vk,
+                                                const double* __restrict__ next,
+                                                const double* __restrict__ part_in,
+                                                double* __restrict__ part_out, double* __restrict__ H) {
+  __shared__ double sh[256];
+  const double h = sum_partials(part_in, sh);
+  if (blockIdx.x == 0 && threadIdx.x == 0) H[k + (size_t)ldh * i] = h;
+  double acc = 0.0;
+  const double mh = -h;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const double ri = r[idx] + mh * vk[idx];
+    r[idx] = ri;
+    const double nx = (next == r) ? ri : next[idx];
+    acc += ri * nx;
+  }
+  block_partial(acc, sh, part_out);
+}
+
+// H(i+1,i) = |r|; v_{i+1} = r * (1/H(i+1,i))
+__global__ void __launch_bounds__(256) k_fg_normalize(int n, int ldh, int i, const double* __restrict__ r,
+                                                      double* __restrict__ v,
+                                                      const double* __restrict__ part_in,
+                                                      double* __restrict__ H, int* __restrict__ flag) {
+  __shared__ double sh[256];
+  const double hn = sqrt(sum_partials(part_in, sh));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    H[(i + 1) + (size_t)ldh * i] = hn;
+    if (hn == 0.0) flag[0] = 1;
+  }
+  const double sc = hn != 0.0 ? 1.0 / hn : 0.0;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x)
+    v[idx] = r[idx] * sc;
+}
+
+// beta = |r|; v_0 = r * (1/beta); s = (beta, 0, ...)
+__global__ void __launch_bounds__(256) k_fg_start(int n, int m, const double* __restrict__ r,
+                                                  double* __restrict__ v0,
+                                                  const double* __restrict__ part_in,
+                                                  double* __restrict__ s, double* __restrict__ beta_out) {
+  __shared__ double sh[256];
+  const double beta = sqrt(sum_partials(part_in, sh));
+  if (blockIdx.x == 0) {
+    for (int k = threadIdx.x; k <= m; k += blockDim.x) s[k] = (k == 0) ? beta : 0.0;
+    if (threadIdx.x == 0) *beta_out = beta;
+  }
+  const double sc = 1.0 / beta;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x)
+    v0[idx] = r[idx] * sc;
+}
+
+__device__ void gen_rot(double dx, double dy, double& cs, double& sn) {
+  // GeneratePlaneRotation (src/Solver/Iteration_gmres.C:123)
+  if (dy == 0.0) {
+    cs = 1.0;
+    sn = 0.0;
+  } else if (fabs(dy) > fabs(dx)) {
+    double t = dx / dy;
+    sn = 1.0 / sqrt(1.0 + t * t);
+    cs = t * sn;
+  } else {
+    double t = dy / dx;
+    cs = 1.0 / sqrt(1.0 + t * t);
+    sn = t * cs;
+  }
+}
+__device__ void app_rot(double& dx, double& dy, double cs, double sn) {
+  // ApplyPlaneRotation (src/Solver/Iteration_gmres.C:144)
+  double t = cs * dx + sn * dy;
+  dy = -sn * dx + cs * dy;
+  dx = t;
+}
+
+__global__ void k_fg_givens(int ldh, int i, double* __restrict__ H, double* __restrict__ cs,
+                            double* __restrict__ sn, double* __restrict__ s, double* __restrict__ resid) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double* col = H + (size_t)ldh * i;
+  for (int k = 0; k < i; ++k) app_rot(col[k], col[k + 1], cs[k], sn[k]);
+  gen_rot(col[i], col[i + 1], cs[i], sn[i]);
+  app_rot(col[i], col[i + 1], cs[i], sn[i]);
+  app_rot(s[i], s[i + 1], cs[i], sn[i]);
+  *resid = fabs(s[i + 1]);
+}
+
+// Update (src/Solver/Iteration_gmres.C:152): back-solve H y = s
+__global__ void k_fg_backsolve(int ldh, int k, const double* __restrict__ H,
+                               const double* __restrict__ s, double* __restrict__ y) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int i = 0; i <= k; ++i) y[i] = s[i];
+  for (int i = k; i >= 0; --i) {
+    y[i] /= H[i + (size_t)ldh * i];
+    for (int j = i - 1; j >= 0; --j) y[j] -= H[j + (size_t)ldh * i] * y[i];
+  }
+}
+
+// x += sum_j y_j z_j  (accumulated in j order, then added)
+__global__ void __launch_bounds__(256) k_fg_combine(int n, int k, const double* __restrict__ Z, size_t ldz,
+                                                    const double* __restrict__ y, double* __restrict__ x) {
+  __shared__ double ys[64];
+  for (int j = threadIdx.x; j <= k; j += blockDim.x) ys[j] = y[j];
+  __syncthreads();
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j <= k; ++j) acc += ys[j] * Z[(size_t)j * ldz + idx];
+    x[idx] += acc;
+  }
+}
+
+}  // namespace pm
+
+using namespace pm;
+
+// ------------------------------------------------------------- solver ------
+void pm_solver::ensure_work(size_t n_vectors, int n) {
+  const size_t need = n_vectors * size_t(n);
+  if (work.n < need) work.alloc(need);
+  work_n = size_t(n);
+}
+
+bool pm_solver::converged(double r, unsigned it) {
+  if (it == 0) {
+    init_res = r;
+    prev_res = r;
+    history.clear();
+  }
+  history.push_back(r);
+  const bool small = r < tol;
+  const bool red = r < reduction * init_res;
+  const bool enough = it > (unsigned long)min_it || min_it == 0;
+  const bool stag = r > stagnation * prev_res;
+  const bool div = r > divergence * init_res;
+  bool conv = (small || red || stag || div) && enough;
+  if (it == (unsigned long)max_it) conv = true;
+  prev_res = r;
+  last_it = int(it);
+  last_res = r;
+  if (div)
+    throw Error(PM_E_DIVERGED, "Execution of the code stopped because of solver divergence.");
+  if (!std::isfinite(r)) throw Error(PM_E_DIVERGED, "residual is not finite");
+  return conv;
+}
+
+void pm_solver::precondition(const double* z, double* r) {
+  const int n = A->csr.n_rows;
+  if (use_mg) {
+    mg.apply(ctx, z, r);
+  } else if (prec == "jacobi") {
+    // Iteration_jacobi::apply: r = z / diag
+    vcopy(ctx, n, z, r);
+    vdiv(ctx, n, A->csr.diag.p, r);
+  } else {
+    vcopy(ctx, n, z, r);
+  }
+}
+
+void pm_solver::fgmres(const double* rhs, double* sol) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  const int m = int(restart);
+  if (m > 60) throw Error(PM_E_UNSUPPORTED, "gmres_restart above 60");
+  const int ldh = m + 1;
+  ensure_work(size_t(2 * m + 2), n);
+  double* r = work.p;
+  double* V = work.p + work_n;                     // m+1 vectors
+  double* Z = work.p + work_n * size_t(m + 2);     // m vectors
+  const size_t ld = work_n;
+  gm.alloc(size_t(ldh) * m + 4 * size_t(m + 1) + 8);
+  double* H = gm.p;
+  double* s = H + size_t(ldh) * m;
+  double* cs = s + (m + 1);
+  double* sn = cs + (m + 1);
+  double* y = sn + (m + 1);
+  double* dres = y + (m + 1);
+  flags.alloc(1);
+  PM_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), c->stream));
+  PM_CUDA(cudaMemsetAsync(H, 0, sizeof(double) * size_t(ldh) * m, c->stream));
+  double* partA = c->partials.p;
+  double* partB = c->partials.p + kRedBlocks;
+
+  csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);  // r = rhs - A sol
+  dot_partials(c, n, r, r, partA);
+  finish_sum(c, partA, dres, true);
+  PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  double resid = c->host_scalars[0];
+  if (converged(resid, 0)) return;
+
+  const int grid = kRedBlocks;
+  unsigned j = 1;
+  while (j <= (unsigned long)max_it) {
+    // v_0 = r / beta, s = (beta, 0, ...)   (partA holds <r,r>)
+    k_fg_start<<<grid, 256, 0, c->stream>>>(n, m, r, V, partA, s, dres + 1);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+    int i = 0;
+    bool done = false;
+    for (; i < m && j <= (unsigned long)max_it; ++i, ++j) {
+      double* vi = V + ld * i;
+      double* zi = Z + ld * i;
+      precondition(vi, zi);
+      csr_apply(c, M, EPI_SET, zi, r, nullptr, 1.0);  // r = A z_i
+      dot_partials(c, n, r, V, partA);                   // <r, v_0>
+      double* pin = partA;
+      double* pout = partB;
+      for (int k = 0; k <= i; ++k) {
+        const double* next = (k < i) ? V + ld * (k + 1) : r;
+        k_fg_mgs<<<grid, 256, 0, c->stream>>>(n, ldh, k, i, r, V + ld * k, next, pin, pout, H);
+        PM_CHECK_LAUNCH();
+        c->kernel_launches++;
+        std::swap(pin, pout);
+      }
+      k_fg_normalize<<<grid, 256, 0, c->stream>>>(n, ldh, i, r, V + ld * (i + 1), pin, H, flags.p);
+      PM_CHECK_LAUNCH();
+      k_fg_givens<<<1, 32, 0, c->stream>>>(ldh, i, H, cs, sn, s, dres);
+      PM_CHECK_LAUNCH();
+      c->kernel_launches += 2;
+      PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      PM_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(c->host_scalars + 1), flags.p, sizeof(int),
+                              cudaMemcpyDeviceToHost, c->stream));
+      PM_CUDA(cudaStreamSynchronize(c->stream));
+      resid = c->host_scalars[0];
+      if (*reinterpret_cast<int*>(c->host_scalars + 1))
+        throw Error(PM_E_BREAKDOWN, "Unhappy breakdown in flexible gmres Iteration " + std::to_string(j));
+      if (converged(resid, j)) {
+        k_fg_backsolve<<<1, 32, 0, c->stream>>>(ldh, i, H, s, y);
+        k_fg_combine<<<grid_blocks_for(n), 256, 0, c->stream>>>(n, i, Z, ld, y, sol);
+        PM_CHECK_LAUNCH();
+        c->kernel_launches += 2;
+        done = true;
+        break;
+      }
+    }
+    if (done) return;
+    k_fg_backsolve<<<1, 32, 0, c->stream>>>(ldh, m - 1, H, s, y);
+    k_fg_combine<<<grid_blocks_for(n), 256, 0, c->stream>>>(n, m - 1, Z, ld, y, sol);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches += 2;
+    csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+    dot_partials(c, n, r, r, partA);
+    if (converged(resid, j)) return;
+  }
+}
+
+
+// Iteration_cg::iterate (src/Solver/Iteration_cg.C:22-79)
+void pm_solver::cg(const double* rhs, double* sol) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  ensure_work(4, n);
+  double *r = work.p, *z = r + work_n, *p = z + work_n, *q = p + work_n;
+  csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+  double normb = std::sqrt(dot_host(c, n, rhs, rhs));
+  if (normb == 0.0) normb = 1.0;
+  double resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+  if (converged(resid, 0)) return;
+  double rho_1 = 0.0;
+  for (unsigned i = 1; i <= (unsigned long)max_it; ++i) {
+    precondition(r, z);
+    const double rho = dot_host(c, n, r, z);
+    if (i == 1) vcopy(c, n, z, p);
+    else vaxpby(c, n, 1.0, z, rho / rho_1, p);  // p = beta p + z
+    csr_apply(c, M, EPI_SET, p, q, nullptr, 1.0);
+    const double alpha = rho / dot_host(c, n, p, q);
+    vaxpy(c, n, alpha, p, sol);
+    vaxpy(c, n, -alpha, q, r);
+    resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+    if (converged(resid, i)) return;
+    rho_1 = rho;
+  }
+}
+
+// Iteration_bicgstab::iterate (src/Solver/Iteration_bicgstab.C:28-206)
+void pm_solver::bicgstab(const double* rhs, double* sol) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  ensure_work(8, n);
+  double *r = work.p, *rt = r + work_n, *p = rt + work_n, *ph = p + work_n, *s = ph + work_n,
+         *sh = s + work_n, *t = sh + work_n, *v = t + work_n;
+  double rho_2 = 1.0, alpha = 1.0, omega = 1.0;
+  csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+  vcopy(c, n, r, rt);
+  double normb = std::sqrt(dot_host(c, n, rhs, rhs));
+  if (normb == 0.0) normb = 1.0;
+  double resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+  if (converged(resid, 0)) return;
+  for (unsigned i = 1; i <= (unsigned long)max_it; ++i) {
+    const double rho_1 = dot_host(c, n, rt, r);
+    if (rho_1 == 0.0) {
+      last_it = int(i);
+      last_res = std::sqrt(dot_host(c, n, r, r)) / normb;
+      return;
+    }
+    if (i == 1) vcopy(c, n, r, p);
+    else {
+      const double beta = (rho_1 / rho_2) * (alpha / omega);
+      vaxpy(c, n, -omega, v, p);
+      vaxpby(c, n, 1.0, r, beta, p);  // p = beta p + r
+    }
+    precondition(p, ph);
+    csr_apply(c, M, EPI_SET, ph, v, nullptr, 1.0);
+    alpha = rho_1 / dot_host(c, n, rt, v);
+    vcopy(c, n, r, s);
+    vaxpy(c, n, -alpha, v, s);
+    resid = std::sqrt(dot_host(c, n, s, s)) / normb;
+    if (converged(resid, i)) {
+      vaxpy(c, n, alpha, ph, sol);
+      return;
+    }
+    precondition(s, sh);
+    csr_apply(c, M, EPI_SET, sh, t, nullptr, 1.0);
+    omega = dot_host(c, n, t, s) / dot_host(c, n, t, t);
+    vaxpy(c, n, alpha, ph, sol);
+    vaxpy(c, n, omega, sh, sol);
+    vcopy(c, n, s, r);
+    vaxpy(c, n, -omega, t, r);
+    rho_2 = rho_1;
+    resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+    if (converged(resid, i)) return;
+    if (omega == 0.0)
+      throw Error(PM_E_BREAKDOWN, "unhappy breakdown in Bi-CGStab. iteration " + std::to_string(i));
+  }
+}
+
+// Iteration_jacobi::iterate (src/Solver/Iteration_jacobi.C:31-90)
+void pm_solver::jacobi_iter(const double* rhs, double* sol) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  if (!M.diag.p) A->csr.make_diag(c);
+  ensure_work(2, n);
+  double *r = work.p, *xn = r + work_n;
+  csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+  double normb = std::sqrt(dot_host(c, n, rhs, rhs));
+  if (normb == 0.0) normb = 1.0;
+  double resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+  if (converged(resid, 0)) return;
+  for (unsigned i = 1; i <= (unsigned long)max_it; ++i) {
+    // x_new = x + w D^{-1}(b - A x); the fused sweep computes the defect itself
+    csr_apply(c, M, EPI_JACOBI, sol, xn, rhs, damping);
+    vcopy(c, n, xn, sol);
+    csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+    resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+    if (converged(resid, i)) return;
+  }
+}
+
+void pm_solver::solve(const double* rhs, double* sol) {
+  if (!A) throw Error(PM_E_INVALID, "Solver::solve called before update_matrix");
+  history.clear();
+  if (solver_type == "direct") {
+    if (!direct_ready) {
+      direct.build(ctx, A->csr);
+      direct_ready = true;
+    }
+    direct.solve(ctx, A->csr, rhs, sol);
+    last_it = 1;
+    last_res = 0.0;
+    return;
+  }
+  if (method == "fgmres" || method == "right_gmres") fgmres(rhs, sol);
+  else if (method == "cg") cg(rhs, sol);
+  else if (method == "bi_cgstab") bicgstab(rhs, sol);
+  else if (method == "jacobi") jacobi_iter(rhs, sol);
+  else throw Error(PM_E_UNSUPPORTED, "iterative_solver_type '" + method + "' is not implemented on the GPU");
+}

@@ -1,0 +1,107 @@
+// Multigrid (V/W/F cycles, damped-Jacobi / direct coarse) and Krylov solvers
+// (FGMRES, CG, BiCGStab, Jacobi iteration) on device vectors, driven by
+// ParameterDatabase keys.
+#pragma once
+#include <map>
+#include <string>
+#include <vector>
+
+#include "pm_linalg.cuh"
+
+struct pm_matrix {
+  pm_ctx* ctx = nullptr;
+  pm::DevCsr csr;
+  bool owned_by_problem = false;
+};
+
+namespace pm {
+
+// "key: value" parameter text (ParameterDatabase::read semantics for the keys
+// this library consumes, src/General/ParameterDatabase.C:1078)
+struct Params {
+  std::map<std::string, std::string> kv;
+  static Params parse(const char* text);
+  bool has(const std::string& k) const { return kv.count(k) != 0; }
+  std::string str(const std::string& k, const std::string& def) const;
+  double num(const std::string& k, double def) const;
+  long integer(const std::string& k, long def) const;
+};
+
+enum Smoother { SM_JACOBI = 0, SM_DIRECT = 1, SM_CELL_VANKA = 2, SM_CELL_VANKA_JACOBI = 3, SM_NONE = 4 };
+enum Dir { DIR_DUMMY = 0, DIR_DOWN = 1, DIR_UP = 2, DIR_END = 3 };
+
+struct MGLevel {
+  pm_matrix* A = nullptr;  // level matrix (not owned)
+  DevCsr P;                // prolongation to the next finer level (fine rows)
+  DevCsr R;                // restriction from the next finer level (this level's rows)
+  DBuf<double> rhs, sol, alt, defect;
+  DBuf<float> rhs32, sol32, alt32, defect32;
+  double* cur = nullptr;   // current iterate (sol or alt)
+  double* oth = nullptr;
+  float* cur32 = nullptr;
+  float* oth32 = nullptr;
+  int smoother = SM_JACOBI;
+  DenseInverse coarse;
+  DBuf<double> coarse_rhs64, coarse_sol64;
+};
+
+// CycleControl (src/Multigrid/CycleControl.C:17-110)
+std::vector<int> cycle_control(const std::string& type, int n_levels);
+
+struct Multigrid {
+  std::vector<MGLevel> levels;  // 0 = coarsest
+  std::vector<int> control;
+  int n_pre = 1, n_post = 1;
+  double jacobi_damp = 1.0, correction_damp = 1.0, coarse_residual = 0.1;
+  int coarse_max_it = 10;
+  int smoother = SM_JACOBI, smoother_coarse = SM_DIRECT;
+  std::string cycle_type = "V";
+  bool mixed = false;
+  bool ready = false;
+
+  void configure(const Params& p);
+  void update(pm_ctx* c);                                  // Multigrid::update
+  void apply(pm_ctx* c, const double* rhs, double* sol);  // Iteration_multigrid::apply
+  // pieces of one cycle (Multigrid::cycle_step)
+  void smooth(pm_ctx* c, int l);
+  void defect(pm_ctx* c, int l);
+  void restrict_to(pm_ctx* c, int l);  // from l to l-1
+  void prolongate_from(pm_ctx* c, int l);  // from l to l+1
+  void coarse_solve(pm_ctx* c);
+};
+
+}  // namespace pm
+
+struct pm_solver {
+  pm_ctx* ctx = nullptr;
+  pm::Params params;
+  std::string solver_type = "iterative";
+  std::string method = "fgmres";
+  std::string prec = "no_preconditioner";
+  double tol = 1e-8, reduction = 0.0, divergence = 1e10, stagnation = 1e10, damping = 1.0;
+  long max_it = 100, min_it = 0, restart = 20;
+  bool mixed = false;
+  pm_matrix* A = nullptr;
+  pm::Multigrid mg;
+  bool use_mg = false;
+  pm::DenseInverse direct;
+  bool direct_ready = false;
+  // Krylov work space
+  pm::DBuf<double> work;  // vectors
+  size_t work_n = 0;
+  pm::DBuf<double> gm;    // FGMRES H, s, cs, sn, y
+  pm::DBuf<int> flags;
+  // loop information of the last solve
+  int last_it = 0;
+  double last_res = 0.0, init_res = 0.0, prev_res = 0.0;
+  std::vector<double> history;
+  // host scalars
+  void ensure_work(size_t n_vectors, int n);
+  bool converged(double r, unsigned it);
+  void solve(const double* rhs, double* sol);
+  void precondition(const double* z, double* r);
+  void fgmres(const double* rhs, double* sol);
+  void cg(const double* rhs, double* sol);
+  void bicgstab(const double* rhs, double* sol);
+  void jacobi_iter(const double* rhs, double* sol);
+};

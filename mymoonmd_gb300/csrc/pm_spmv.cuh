@@ -1,0 +1,89 @@
+// CSR sparse matrix-vector kernels with fused epilogues.
+//
+// One group of G lanes (G = 4..32, a power of two) walks one CSR row: each lane
+// streams every G-th entry (values and column indices with evict-first loads so
+// that the gathered vector x stays resident in L2), the group reduces with
+// shuffles, and the group's first lane applies the epilogue. The epilogues give
+// the operations the reference builds from TMatrix::multiply
+// (src/Matrix/Matrix.C:430-451) and BlockFEMatrix::apply_scaled_add
+// (src/Matrix/BlockFEMatrix.C:863-925):
+//   AXPY    y_i += a * (A x)_i                      apply_scaled_add
+//   SET     y_i  = (A x)_i                          apply
+//   DEFECT  y_i  = b_i - (A x)_i                    MultigridLevel::calculate_defect
+//   JACOBI  y_i  = x_i + w * ((b_i - (A x)_i)/d_i)  JacobiSmoother::smooth
+//   RESTRICT y_i = active(i) ? (A x)_i : 0           DefectRestriction + ResetNonActive
+//   PROLONG y_i += active(i) ? w * (A x)_i : 0       update_solution_in_finer_grid
+// Non-active (Dirichlet) rows of FE matrices hold a single unit diagonal, so the
+// uniform row sum reproduces BlockVector::addScaledNonActive exactly.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace pm {
+
+enum Epi { EPI_AXPY = 0, EPI_SET = 1, EPI_DEFECT = 2, EPI_JACOBI = 3, EPI_RESTRICT = 4, EPI_PROLONG = 5 };
+
+// Up to four contiguous blocks [start, end) of a block vector; rows in
+// [active_end, end) of each block are non-active.
+struct BlockMask {
+  int nb;
+  int start[4];
+  int active_end[4];
+  int end[4];
+};
+
+__device__ __forceinline__ bool row_is_active(const BlockMask& m, int i) {
+#pragma unroll
+  for (int b = 0; b < 4; ++b)
+    if (b < m.nb && i >= m.start[b] && i < m.end[b]) return i < m.active_end[b];
+  return false;
+}
+
+template <class T>
+__device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
+
+template <class TV, class TX, class TA, int G, int EPI>
+__global__ void __launch_bounds__(256)
+csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+           const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
+           const TX* __restrict__ b, const TX* __restrict__ diag, const TX* __restrict__ xold,
+           TA alpha, BlockMask mask) {
+  const int lane = threadIdx.x & (G - 1);
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const bool valid = row < n_rows;  // whole groups share a row: no early exit before the shuffles
+  const int beg = valid ? __ldg(row_ptr + row) : 0;
+  const int end = valid ? __ldg(row_ptr + row + 1) : 0;
+  TA s0 = TA(0), s1 = TA(0);
+  int k = beg + lane;
+  // two independent accumulators for memory-level parallelism
+  for (; k + G < end; k += 2 * G) {
+    const TV v0 = ld_stream(vals + k);
+    const int c0 = ld_stream(cols + k);
+    const TV v1 = ld_stream(vals + k + G);
+    const int c1 = ld_stream(cols + k + G);
+    s0 += TA(v0) * TA(__ldg(x + c0));
+    s1 += TA(v1) * TA(__ldg(x + c1));
+  }
+  if (k < end) s0 += TA(ld_stream(vals + k)) * TA(__ldg(x + ld_stream(cols + k)));
+  TA s = s0 + s1;
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, G);
+  if (!valid) return;
+  if (lane != 0) return;
+  if constexpr (EPI == EPI_AXPY) {
+    y[row] = TX(TA(y[row]) + alpha * s);
+  } else if constexpr (EPI == EPI_SET) {
+    y[row] = TX(s);
+  } else if constexpr (EPI == EPI_DEFECT) {
+    y[row] = TX(TA(b[row]) - s);
+  } else if constexpr (EPI == EPI_JACOBI) {
+    const TA d = (TA(b[row]) - s) / TA(diag[row]);
+    y[row] = TX(TA(xold[row]) + alpha * d);
+  } else if constexpr (EPI == EPI_RESTRICT) {
+    y[row] = row_is_active(mask, row) ? TX(s) : TX(0);
+  } else if constexpr (EPI == EPI_PROLONG) {
+    if (row_is_active(mask, row)) y[row] = TX(TA(y[row]) + alpha * s);
+  }
+}
+
+}  // namespace pm

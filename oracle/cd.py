@@ -1,0 +1,190 @@
+"""Oracle drivers (test infrastructure only): convection-diffusion assembly,
+multigrid and Krylov solves of the C restatement in oracle.c, on the set-up of
+refsetup.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import build as _build
+from . import refsetup
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        vp, i32, f64 = C.c_void_p, C.c_int, C.c_double
+        L.orc_apply_scaled_add.argtypes = [i32, vp, vp, vp, vp, vp, vp, f64]
+        L.orc_multiply.argtypes = [i32, vp, vp, vp, vp, vp, f64]
+        L.orc_dot.argtypes = [i32, vp, vp]
+        L.orc_dot.restype = f64
+        L.orc_assemble_cd.argtypes = [i32, i32, i32, i32, vp, i32, vp, i32, i32, vp, vp, f64, vp, f64, i32,
+                                      f64, vp, vp]
+        L.orc_mg_create.argtypes = [i32, i32, i32, f64, f64, i32, i32, i32, f64]
+        L.orc_mg_create.restype = vp
+        L.orc_mg_set_level.argtypes = [vp, i32, i32, vp, vp, vp, vp]
+        L.orc_mg_set_transfer.argtypes = [vp, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32]
+        L.orc_mg_destroy.argtypes = [vp]
+        L.orc_mg_apply.argtypes = [vp, vp, vp]
+        L.orc_krylov_solve.argtypes = [i32, i32, vp, vp, vp, vp, vp, f64, f64, i32, i32, i32, vp, vp,
+                                       C.POINTER(i32), C.POINTER(f64), vp, i32, C.POINTER(i32)]
+        L.orc_prolongate_flat.argtypes = [i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]
+        L.orc_restrict_flat.argtypes = [i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]
+        L.orc_lu_factor.argtypes = [i32, vp, vp]
+        L.orc_lu_solve.argtypes = [i32, vp, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+def apply_scaled_add(rp, ci, v, active, x, y, a):
+    """BlockFEMatrix::apply_scaled_add on the CPU; returns the new y"""
+    y = np.array(y, dtype=np.float64, copy=True)
+    act = np.ascontiguousarray(active, dtype=np.uint8)
+    rp = np.ascontiguousarray(rp, dtype=np.int32)
+    ci = np.ascontiguousarray(ci, dtype=np.int32)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    lib().orc_apply_scaled_add(rp.size - 1, _p(act), _p(rp), _p(ci), _p(v), _p(x), _p(y), a)
+    return y
+
+
+def transfer(dim: int, k: int, coarse_level, fine_level, vec: np.ndarray, prolongate: bool) -> np.ndarray:
+    """GridTransfer::Prolongate (prolongate=True, vec on the coarse level) or
+    DefectRestriction (vec on the fine level) on the CPU"""
+    fd = np.ascontiguousarray(fine_level.dofmap, dtype=np.int32)
+    cd = np.ascontiguousarray(coarse_level.dofmap, dtype=np.int32)
+    fv = np.ascontiguousarray(fine_level.verts, dtype=np.float64)
+    cv = np.ascontiguousarray(coarse_level.verts, dtype=np.float64)
+    par = np.ascontiguousarray(fine_level.parent, dtype=np.int32)
+    vec = np.ascontiguousarray(vec, dtype=np.float64)
+    args = (dim, k, fine_level.n_cells, fine_level.nloc, _p(fd), _p(cd), _p(par), _p(fv), _p(cv),
+            fine_level.n_dofs, coarse_level.n_dofs)
+    if prolongate:
+        out = np.zeros(fine_level.n_dofs)
+        lib().orc_prolongate_flat(*args, _p(vec), _p(out))
+    else:
+        out = np.zeros(coarse_level.n_dofs)
+        lib().orc_restrict_flat(*args, _p(out), _p(vec))
+    return out
+
+
+class OracleCD:
+    """ConvectionDiffusion<d> restated on the CPU over a multigrid hierarchy."""
+
+    def __init__(self, geometry: int, root_n: int, n_refine: int, n_levels: int, elem: int,
+                 eps: float, b=(0.0, 0.0, 0.0), c: float = 0.0, quad_points: int = 3,
+                 manufactured: bool = True, f_const: float = 0.0):
+        self.geometry = geometry
+        self.dim = 2 if geometry == refsetup.GEO_SQUARE_QUAD else 3
+        self.elem = elem
+        self.levels = refsetup.cd_levels(geometry, root_n, n_refine, n_levels, elem)
+        self.eps, self.c = eps, c
+        self.b = np.array(list(b) + [0.0] * (3 - len(b)), dtype=np.float64)
+        self.qn = quad_points
+        self.manufactured, self.f_const = manufactured, f_const
+        self.vals = []
+        self.rhs = []
+        self._mg = None
+        self._keep = []
+
+    @property
+    def finest(self):
+        return self.levels[-1]
+
+    def assemble(self) -> None:
+        L = lib()
+        self.vals, self.rhs = [], []
+        for lv in self.levels:
+            vals = np.zeros(lv.cols.size, dtype=np.float64)
+            rhs = np.zeros(lv.n_dofs, dtype=np.float64)
+            verts = np.ascontiguousarray(lv.verts, dtype=np.float64)
+            dm = np.ascontiguousarray(lv.dofmap, dtype=np.int32)
+            rc = L.orc_assemble_cd(self.dim, self.elem, self.qn, lv.n_cells, _p(verts), lv.nloc, _p(dm),
+                                   lv.n_dofs, lv.n_active, _p(lv.row_ptr), _p(lv.cols), self.eps, _p(self.b),
+                                   self.c, int(self.manufactured), self.f_const, _p(vals), _p(rhs))
+            if rc != 0:
+                raise RuntimeError(f"oracle assembly failed ({rc})")
+            self.vals.append(vals)
+            self.rhs.append(rhs)
+
+    def active(self, l: int = -1) -> np.ndarray:
+        lv = self.levels[l]
+        a = np.zeros(lv.n_dofs, dtype=np.uint8)
+        a[: lv.n_active] = 1
+        return a
+
+    def build_mg(self, n_pre=2, n_post=2, jacobi_damp=0.8, correction_damp=1.0, cycle="V",
+                 coarse_direct=True, coarse_max_it=10, coarse_residual=0.1, n_mg_levels=None):
+        L = lib()
+        if self._mg:
+            L.orc_mg_destroy(self._mg)
+        nl = len(self.levels) if n_mg_levels is None else n_mg_levels
+        off = len(self.levels) - nl
+        mg = L.orc_mg_create(nl, n_pre, n_post, jacobi_damp, correction_damp, {"V": 0, "W": 1, "F": 2}[cycle],
+                             int(coarse_direct), coarse_max_it, coarse_residual)
+        keep = []
+        for l in range(nl):
+            lv = self.levels[off + l]
+            act = self.active(off + l)
+            keep.append(act)
+            rc = L.orc_mg_set_level(mg, l, lv.n_dofs, _p(act), _p(lv.row_ptr), _p(lv.cols), _p(self.vals[off + l]))
+            if rc != 0:
+                raise RuntimeError("oracle coarse factorisation failed")
+        for l in range(nl - 1):
+            cl, fl = self.levels[off + l], self.levels[off + l + 1]
+            fd = np.ascontiguousarray(fl.dofmap, dtype=np.int32)
+            cd = np.ascontiguousarray(cl.dofmap, dtype=np.int32)
+            fv = np.ascontiguousarray(fl.verts, dtype=np.float64)
+            cv = np.ascontiguousarray(cl.verts, dtype=np.float64)
+            par = np.ascontiguousarray(fl.parent, dtype=np.int32)
+            keep += [fd, cd, fv, cv, par]
+            L.orc_mg_set_transfer(mg, l, self.dim, self.elem, fl.n_cells, fl.nloc, _p(fd), _p(cd), _p(par),
+                                  _p(fv), _p(cv), fl.n_dofs, cl.n_dofs)
+        self._mg = mg
+        self._keep = keep
+        return mg
+
+    def mg_apply(self, z: np.ndarray) -> np.ndarray:
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        r = np.zeros_like(z)
+        lib().orc_mg_apply(self._mg, _p(z), _p(r))
+        return r
+
+    def solve(self, method: str = "fgmres", tol: float = 0.0, reduction: float = 1e-8, max_it: int = 100,
+              min_it: int = 0, restart: int = 20, use_mg: bool = True, sol0=None):
+        """returns (solution, iterations, residual, history, status)"""
+        lv = self.finest
+        act = self.active()
+        rhs = self.rhs[-1]
+        sol = np.zeros(lv.n_dofs) if sol0 is None else np.array(sol0, dtype=np.float64)
+        # copy_nonactive(rhs -> solution)
+        sol[lv.n_active:] = rhs[lv.n_active:]
+        it, res, nh = C.c_int(), C.c_double(), C.c_int()
+        hist = np.zeros(100000)
+        st = lib().orc_krylov_solve({"fgmres": 0, "cg": 1, "bi_cgstab": 2}[method], lv.n_dofs, _p(act),
+                                    _p(lv.row_ptr), _p(lv.cols), _p(self.vals[-1]),
+                                    self._mg if use_mg else None, tol, reduction, max_it, min_it, restart,
+                                    _p(rhs), _p(sol), C.byref(it), C.byref(res), _p(hist), hist.size,
+                                    C.byref(nh))
+        return sol, it.value, res.value, hist[: nh.value].copy(), st
+
+    def close(self):
+        if self._mg:
+            lib().orc_mg_destroy(self._mg)
+            self._mg = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,254 @@
+"""GPU parity of the solve path against the CPU oracle (all through the C ABI).
+
+Tolerances (FP64 unless stated):
+  SpMV                 1e-13 relative to sum_j |a_ij x_j|   (summation order differs)
+  assembled entries    1e-13 relative to max |entry|
+  multigrid cycle      1e-11 relative (max norm)
+  final solutions      1e-10 relative, Krylov iteration counts within one
+  mixed precision      FP64 residual reduction 1e-8 reached; error against the
+                       FP64 oracle solution stated in the assertion (<= 1e-7)
+"""
+import numpy as np
+import pytest
+
+import mymoonmd_gb300 as m
+from oracle import cd as ocd
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def mg_db(n_levels, restart=20, reduction=1e-10, precision="fp64", smoother_damp=0.8, pre=2, post=2,
+          cycle="V"):
+    db = m.ParameterDatabase.solve_path_database()
+    db["solver_type"] = "iterative"
+    db["iterative_solver_type"] = "fgmres"
+    db["preconditioner"] = "multigrid"
+    db["residual_tolerance"] = 0.0
+    db["residual_reduction"] = reduction
+    db["max_n_iterations"] = 200
+    db["gmres_restart"] = restart
+    db["multigrid_n_levels"] = n_levels
+    db["multigrid_smoother"] = "jacobi"
+    db["multigrid_smoother_coarse"] = "direct_solve"
+    db["jacobi_damp"] = smoother_damp
+    db["multigrid_n_pre_smooth"] = pre
+    db["multigrid_n_post_smooth"] = post
+    db["multigrid_cycle_type"] = cycle
+    db["gpu_precision"] = precision
+    return db
+
+
+CASES = {
+    # name: geometry, root_n, n_refine, n_levels, elem, eps, b, quad
+    "q1_2d": (m.GEO_SQUARE_QUAD, 1, 5, 3, 1, 0.1, (1.0, 0.0, 0.0), 3),
+    "q2_2d": (m.GEO_SQUARE_QUAD, 1, 4, 3, 2, 0.05, (0.6, 0.8, 0.0), 3),
+    "q1_3d": (m.GEO_CUBE_HEXA, 1, 3, 3, 1, 0.1, (1.0, 0.5, 0.25), 3),
+    "q2_3d": (m.GEO_CUBE_HEXA, 1, 3, 3, 2, 1e-2, (1.0, 0.5, 0.25), 3),
+    "q2_3d_root3": (m.GEO_CUBE_HEXA, 3, 1, 2, 2, 0.1, (1.0, 0.5, 0.25), 3),
+}
+
+
+def make_pair(ctx, case, db):
+    geo, root, nref, nlev, elem, eps, b, qn = CASES[case]
+    disc = m.Discretization(geo, root, nref, nlev, m.KIND_CD, elem)
+    cf = m.cd_coeffs(eps, b, 0.0, True)
+    prob = m.ConvectionDiffusion(ctx, disc, cf, db, quad_points=qn)
+    prob.assemble()
+    ora = ocd.OracleCD(geo, root, nref, nlev, elem, eps, b, 0.0, qn)
+    ora.assemble()
+    return disc, prob, ora
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_assembly_matches_oracle(ctx, case):
+    disc, prob, ora = make_pair(ctx, case, mg_db(CASES[case][3]))
+    for l in range(disc.n_levels):
+        vals = prob.matrix(l).values()
+        assert rel(vals, ora.vals[l]) <= 1e-13, (case, l)
+    assert rel(prob.rhs(), ora.rhs[-1]) <= 1e-13
+
+
+def test_spmv_known_answer(ctx):
+    """test/matrix_test.c++:143-147 through the GPU: y = -0.5*CB*x"""
+    B = np.zeros((3, 4))
+    B[0, 0], B[0, 3], B[1, 2], B[2, 1], B[2, 3] = 4, 1, 5, 6, 1
+    C = np.zeros((4, 3))
+    C[0, 0], C[0, 2], C[1, 0], C[1, 1], C[2, 1], C[2, 2], C[3, 0], C[3, 2] = 7, 8, 9, 10, 11, 12, 13, 14
+    CB = C @ B
+    rp = [0]
+    ci, v = [], []
+    for row in CB:
+        for j, a in enumerate(row):
+            if a != 0:
+                ci.append(j)
+                v.append(a)
+        rp.append(len(ci))
+    A = m.FEMatrix.from_csr(ctx, rp, ci, v)
+    x = m.DeviceVector.from_numpy(ctx, np.array([1.0, -2.5, 11.34, -0.004]))
+    y = m.DeviceVector(ctx, 4)
+    A.apply_scaled_add(x, y, -0.5)
+    assert np.allclose(y.numpy(), [46.03, -301.482, -221.826, 79.054], rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("case", ["q1_2d", "q2_3d"])
+def test_spmv_apply_scaled_add_matches_oracle(ctx, case):
+    disc, prob, ora = make_pair(ctx, case, mg_db(CASES[case][3]))
+    lv = ora.finest
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(lv.n_dofs)
+    y0 = rng.standard_normal(lv.n_dofs)
+    A = prob.matrix(-1)
+    xd, yd = m.DeviceVector.from_numpy(ctx, x), m.DeviceVector.from_numpy(ctx, y0)
+    A.apply_scaled_add(xd, yd, -0.7)
+    ref = ocd.apply_scaled_add(lv.row_ptr, lv.cols, ora.vals[-1], ora.active(), x, y0, -0.7)
+    scale = ocd.apply_scaled_add(lv.row_ptr, lv.cols, np.abs(ora.vals[-1]), ora.active(), np.abs(x),
+                                 np.abs(y0), 0.7)
+    assert np.all(np.abs(yd.numpy() - ref) <= 1e-13 * scale)
+
+
+def test_spmv_fp32_matches_fp64_within_fp32_rounding(ctx):
+    disc, prob, ora = make_pair(ctx, "q2_3d", mg_db(3))
+    A = prob.matrix(-1)
+    A.make_fp32()
+    lv = ora.finest
+    x = np.random.default_rng(4).standard_normal(lv.n_dofs)
+    y = m.DeviceVector(ctx, lv.n_dofs, np.float32)
+    A.apply_f32(m.DeviceVector.from_numpy(ctx, x.astype(np.float32)), y)
+    ref = ocd.apply_scaled_add(lv.row_ptr, lv.cols, ora.vals[-1], ora.active(), x, np.zeros(lv.n_dofs), 1.0)
+    scale = ocd.apply_scaled_add(lv.row_ptr, lv.cols, np.abs(ora.vals[-1]), ora.active(), np.abs(x),
+                                 np.zeros(lv.n_dofs), 1.0)
+    assert np.all(np.abs(y.numpy() - ref) <= 2e-6 * scale + 1e-30)
+
+
+@pytest.mark.parametrize("case", ["q1_2d", "q2_3d", "q2_3d_root3"])
+def test_multigrid_cycle_matches_oracle(ctx, case):
+    nl = CASES[case][3]
+    disc, prob, ora = make_pair(ctx, case, mg_db(nl))
+    prob.solve()  # builds the hierarchy (update_matrix)
+    ora.build_mg(2, 2, 0.8, 1.0, "V")
+    rng = np.random.default_rng(5)
+    z = rng.standard_normal(ora.finest.n_dofs)
+    zd = m.DeviceVector.from_numpy(ctx, z)
+    rd = m.DeviceVector(ctx, z.size)
+    prob.solver().apply_preconditioner(zd, rd)
+    assert rel(rd.numpy(), ora.mg_apply(z)) <= 1e-11
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_fgmres_multigrid_solution_matches_oracle(ctx, case):
+    nl = CASES[case][3]
+    disc, prob, ora = make_pair(ctx, case, mg_db(nl))
+    prob.solve()
+    it, res, init = prob.last_info()
+    ora.build_mg(2, 2, 0.8, 1.0, "V")
+    sol, oit, ores, hist, st = ora.solve("fgmres", 0.0, 1e-10, 200, 0, 20)
+    assert st == 0
+    assert abs(it - oit) <= 1, (it, oit)
+    assert rel(prob.solution(), sol) <= 1e-10
+    assert res < 1e-10 * init
+
+
+def test_w_cycle_and_restart_match_oracle(ctx):
+    db = mg_db(3, restart=3, cycle="W")
+    disc, prob, ora = make_pair(ctx, "q1_2d", db)
+    prob.solve()
+    it, res, init = prob.last_info()
+    ora.build_mg(2, 2, 0.8, 1.0, "W")
+    sol, oit, ores, hist, st = ora.solve("fgmres", 0.0, 1e-10, 200, 0, 3)
+    assert abs(it - oit) <= 1
+    assert rel(prob.solution(), sol) <= 1e-10
+
+
+def test_mixed_precision_reaches_fp64_target(ctx):
+    db = mg_db(3, restart=30, reduction=1e-8, precision="mixed")
+    disc, prob, ora = make_pair(ctx, "q2_3d", db)
+    prob.solve()
+    x = prob.solution()
+    lv = ora.finest
+    b = ora.rhs[-1]
+    x0 = np.zeros_like(b)
+    x0[lv.n_active:] = b[lv.n_active:]
+    r0 = ocd.apply_scaled_add(lv.row_ptr, lv.cols, ora.vals[-1], ora.active(), x0, b, -1.0)
+    r = ocd.apply_scaled_add(lv.row_ptr, lv.cols, ora.vals[-1], ora.active(), x, b, -1.0)
+    assert np.linalg.norm(r) <= 1.05e-8 * np.linalg.norm(r0)
+    ora.build_mg(2, 2, 0.8, 1.0, "V")
+    sol, *_ = ora.solve("fgmres", 0.0, 1e-8, 200, 0, 30)
+    err = rel(x, sol)
+    assert err <= 1e-7, f"mixed vs FP64 oracle relative error {err:.3e}"
+
+
+@pytest.mark.parametrize("method", ["fgmres", "cg", "bi_cgstab"])
+def test_krylov_on_reference_test_system(ctx, method):
+    """the 7x7 block system of test/iterative_solver_test.c++ solved on the GPU"""
+    A = np.diag([5.5, 7.53, 10.0, 15.0])
+    B = np.zeros((3, 4))
+    B[0, 0], B[0, 3], B[1, 2], B[2, 1], B[2, 3] = 4, 1, 5, 6, 1
+    D = np.array([[50, 0, 0], [0, 19, 0.1], [0, 0.1, 85.6]])
+    M = np.block([[A, B.T], [B, D]])
+    rp, ci, v = [0], [], []
+    for row in M:
+        for j, a in enumerate(row):
+            if a != 0:
+                ci.append(j)
+                v.append(a)
+        rp.append(len(ci))
+    mat = m.FEMatrix.from_csr(ctx, rp, ci, v)
+    exact = np.arange(7.0)
+    rhs = M @ exact
+    db = m.ParameterDatabase.solve_path_database()
+    db["solver_type"] = "iterative"
+    db["iterative_solver_type"] = method
+    db["residual_tolerance"] = 1e-11
+    db["max_n_iterations"] = 1000
+    db["preconditioner"] = "jacobi"
+    s = m.Solver(ctx, db)
+    s.update_matrix(mat)
+    sol = np.zeros(7)
+    s.solve(rhs, sol)
+    assert np.linalg.norm(sol - exact) <= 100 * 1e-11
+
+
+def test_solves_are_deterministic(ctx):
+    db = mg_db(3, restart=30, reduction=1e-8)
+    disc, prob, ora = make_pair(ctx, "q2_3d", db)
+    prob.solve()
+    a = prob.solution()
+    prob.assemble()
+    prob.run_host(None, None, np.empty_like(a))
+    b = prob.solution()
+    assert np.array_equal(a, b)
+
+
+def test_direct_solver(ctx):
+    disc, prob, ora = make_pair(ctx, "q1_2d", mg_db(3))
+    lv = ora.finest
+    A = m.FEMatrix.from_csr(ctx, lv.row_ptr, lv.cols, ora.vals[-1], n_active=lv.n_active)
+    db = m.ParameterDatabase.solve_path_database()
+    s = m.Solver(ctx, db)
+    s.update_matrix(A)
+    b = ora.rhs[-1]
+    x = np.zeros_like(b)
+    s.solve(b, x)
+    r = ocd.apply_scaled_add(lv.row_ptr, lv.cols, ora.vals[-1], ora.active(), x, b, -1.0)
+    assert np.linalg.norm(r) <= 1e-12 * np.linalg.norm(b)
+
+
+def test_config_2d_q1_128_full_size_against_oracle(ctx):
+    """2D Q1 128^2, FGMRES(20) + V(2,2) Jacobi(0.8), 4 levels, to 1e-10"""
+    disc = m.Discretization(m.GEO_SQUARE_QUAD, 1, 7, 4, m.KIND_CD, 1)
+    cf = m.cd_coeffs(0.1, (1.0, 0.0), 0.0, True)
+    prob = m.ConvectionDiffusion(ctx, disc, cf, mg_db(4, restart=20, reduction=1e-10), quad_points=3)
+    prob.assemble()
+    prob.solve()
+    it, res, init = prob.last_info()
+    ora = ocd.OracleCD(0, 1, 7, 4, 1, 0.1, (1.0, 0.0), 0.0, 3)
+    ora.assemble()
+    ora.build_mg(2, 2, 0.8, 1.0, "V")
+    sol, oit, ores, hist, st = ora.solve("fgmres", 0.0, 1e-10, 200, 0, 20)
+    assert abs(it - oit) <= 1
+    assert rel(prob.solution(), sol) <= 1e-10
+    assert rel(prob.matrix(-1).values(), ora.vals[-1]) <= 1e-13
