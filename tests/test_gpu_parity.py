@@ -47,7 +47,7 @@ CASES = {
     "q1_2d": (m.GEO_SQUARE_QUAD, 1, 5, 3, 1, 0.1, (1.0, 0.0, 0.0), 3),
     "q2_2d": (m.GEO_SQUARE_QUAD, 1, 4, 3, 2, 0.05, (0.6, 0.8, 0.0), 3),
     "q1_3d": (m.GEO_CUBE_HEXA, 1, 3, 3, 1, 0.1, (1.0, 0.5, 0.25), 3),
-    "q2_3d": (m.GEO_CUBE_HEXA, 1, 3, 3, 2, 1e-2, (1.0, 0.5, 0.25), 3),
+    "q2_3d": (m.GEO_CUBE_HEXA, 1, 3, 3, 2, 0.1, (1.0, 0.5, 0.25), 3),
     "q2_3d_root3": (m.GEO_CUBE_HEXA, 3, 1, 2, 2, 0.1, (1.0, 0.5, 0.25), 3),
 }
 
