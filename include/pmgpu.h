@@ -104,6 +104,10 @@ int pm_matrix_get_diagonal(pm_matrix* A, double* diag_dev);
  * y = A32*x (FP32 values, vectors and accumulation). */
 int pm_matrix_make_fp32(pm_matrix* A);
 int pm_matrix_apply_f32(pm_matrix* A, const float* x_dev, float* y_dev);
+/* Launch shape of the CSR kernels of this matrix (no reference counterpart;
+ * tuning only): lanes per row (4, 8, 16, 32) and entries per lane per chunk
+ * (2, 4, 8). 0 keeps the current value. */
+int pm_matrix_set_kernel(pm_matrix* A, int lanes, int unroll);
 /* Timed SpMV loop: `reps` applications y = A x on the context's stream, timed
  * with CUDA events; returns ms per application and the algorithmic bytes. */
 int pm_matrix_bench_apply(pm_matrix* A, int fp32, const void* x_dev, void* y_dev, int reps,
@@ -212,8 +216,12 @@ int pm_problem_create_cd(pm_ctx* ctx, const pm_disc* d, const pm_cd_coeffs* coef
 void pm_problem_destroy(pm_problem* p);
 /* ConvectionDiffusion::assemble (src/System/ConvectionDiffusion.C:174) */
 int pm_problem_assemble(pm_problem* p);
-/* ConvectionDiffusion::solve (src/System/ConvectionDiffusion.C:191) */
+/* ConvectionDiffusion::solve (src/System/ConvectionDiffusion.C:191). Like the
+ * reference, the solve starts from the current solution vector. */
 int pm_problem_solve(pm_problem* p);
+/* Zero initial guess for the next request (the state after construction,
+ * ConvectionDiffusion.C:73). */
+int pm_problem_reset_solution(pm_problem* p);
 int pm_problem_size(const pm_problem* p, int* n_dofs, int* n_active);
 int pm_problem_get_solution(const pm_problem* p, double* sol_host);
 int pm_problem_get_rhs(const pm_problem* p, double* rhs_host);

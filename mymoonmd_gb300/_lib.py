@@ -85,6 +85,7 @@ _SIGS = {
     "pm_matrix_get_diagonal": (i32, [vp, vp]),
     "pm_matrix_make_fp32": (i32, [vp]),
     "pm_matrix_apply_f32": (i32, [vp, vp, vp]),
+    "pm_matrix_set_kernel": (i32, [vp, i32, i32]),
     "pm_matrix_bench_apply": (i32, [vp, i32, vp, vp, i32, C.POINTER(C.c_float), pf64]),
     "pm_dot": (i32, [vp, i32, vp, vp, pf64]),
     "pm_norm": (i32, [vp, i32, vp, pf64]),
@@ -112,6 +113,7 @@ _SIGS = {
     "pm_problem_destroy": (None, [vp]),
     "pm_problem_assemble": (i32, [vp]),
     "pm_problem_solve": (i32, [vp]),
+    "pm_problem_reset_solution": (i32, [vp]),
     "pm_problem_size": (i32, [vp, pi32, pi32]),
     "pm_problem_get_solution": (i32, [vp, vp]),
     "pm_problem_get_rhs": (i32, [vp, vp]),

@@ -236,6 +236,9 @@ class FEMatrix:
     def apply_f32(self, x: DeviceVector, y: DeviceVector) -> None:
         check(lib.pm_matrix_apply_f32(self.handle, x.ptr, y.ptr), self.ctx.handle)
 
+    def set_kernel(self, lanes: int = 0, unroll: int = 0) -> None:
+        check(lib.pm_matrix_set_kernel(self.handle, lanes, unroll), self.ctx.handle)
+
     def bench_apply(self, x: DeviceVector, y: DeviceVector, reps: int, fp32: bool = False):
         ms = C.c_float()
         b = C.c_double()
@@ -435,6 +438,9 @@ class ConvectionDiffusion:
 
     def solve(self) -> None:
         check(lib.pm_problem_solve(self.handle), self.ctx.handle)
+
+    def reset_solution(self) -> None:
+        check(lib.pm_problem_reset_solution(self.handle), self.ctx.handle)
 
     def size(self) -> tuple[int, int]:
         n, na = C.c_int(), C.c_int()

@@ -299,6 +299,17 @@ int pm_matrix_apply_f32(pm_matrix* A, const float* x, float* y) {
   PM_CATCH(A->ctx)
 }
 
+int pm_matrix_set_kernel(pm_matrix* A, int lanes, int unroll) {
+  if (!A) return PM_E_INVALID;
+  if (lanes && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+    return fail(A->ctx, PM_E_INVALID, "lanes per row must be 4, 8, 16 or 32");
+  if (unroll && unroll != 2 && unroll != 4 && unroll != 8)
+    return fail(A->ctx, PM_E_INVALID, "entries per lane must be 2, 4 or 8");
+  if (lanes) A->csr.lanes = lanes;
+  if (unroll) A->csr.unroll = unroll;
+  return PM_OK;
+}
+
 int pm_matrix_bench_apply(pm_matrix* A, int fp32, const void* x, void* y, int reps, float* ms,
                           double* bytes) {
   if (!A || !x || !y || reps < 1) return PM_E_INVALID;
@@ -726,6 +737,14 @@ int pm_problem_solve(pm_problem* p) {
   }
   p->solver->solve(p->rhs.p, p->sol.p);
   PM_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  return PM_OK;
+  PM_CATCH(p->ctx)
+}
+
+int pm_problem_reset_solution(pm_problem* p) {
+  if (!p) return PM_E_INVALID;
+  PM_TRY
+  PM_CUDA(cudaMemsetAsync(p->sol.p, 0, p->sol.bytes(), p->ctx->stream));
   return PM_OK;
   PM_CATCH(p->ctx)
 }

@@ -147,17 +147,26 @@ size_t DevCsr::spmv_bytes(int eb, bool read_y) const {
          size_t(n_rows) * eb * (read_y ? 2 : 1);
 }
 
+template <class TV, class TX, class TA, int G, int EPI>
+static void launch_gu(pm_ctx* c, int U, int grid, int n, const int* rp, const int* ci, const TV* v,
+                      const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
+  switch (U) {
+    case 2: csr_kernel<TV, TX, TA, G, 2, EPI><<<grid, 256, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 4: csr_kernel<TV, TX, TA, G, 4, EPI><<<grid, 256, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    default: csr_kernel<TV, TX, TA, G, 8, EPI><<<grid, 256, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+  }
+}
+
 template <class TV, class TX, class TA, int EPI>
-static void launch_epi(pm_ctx* c, int G, int n, const int* rp, const int* ci, const TV* v,
+static void launch_epi(pm_ctx* c, int G, int U, int n, const int* rp, const int* ci, const TV* v,
                        const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
   if (n <= 0) return;
-  const int threads = 256;
-  const int grid = nblocks((long long)n * G, threads);
+  const int grid = nblocks((long long)n * G, 256);
   switch (G) {
-    case 4: csr_kernel<TV, TX, TA, 4, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    case 8: csr_kernel<TV, TX, TA, 8, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    case 16: csr_kernel<TV, TX, TA, 16, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    default: csr_kernel<TV, TX, TA, 32, EPI><<<grid, threads, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 4: launch_gu<TV, TX, TA, 4, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
+    case 8: launch_gu<TV, TX, TA, 8, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
+    case 16: launch_gu<TV, TX, TA, 16, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
+    default: launch_gu<TV, TX, TA, 32, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
   }
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
@@ -189,6 +198,7 @@ template <class TV, class TX, class TA>
 static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* diag, int epi,
                          const TX* x, TX* y, const TX* b, TA alpha, int n) {
   const int G = A.lanes;
+  const int U = A.unroll;
   const int* rp = A.row_ptr.p;
   const int* ci = A.cols.p;
   const bool probe = c->probe_nnz != 0 && A.nnz == c->probe_nnz;
@@ -199,12 +209,12 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
     c->probe_bytes.push_back(epi_bytes(A, epi, int(sizeof(TV)), n));
   }
   switch (epi) {
-    case EPI_AXPY: launch_epi<TV, TX, TA, EPI_AXPY>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_SET: launch_epi<TV, TX, TA, EPI_SET>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_DEFECT: launch_epi<TV, TX, TA, EPI_DEFECT>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_JACOBI: launch_epi<TV, TX, TA, EPI_JACOBI>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_RESTRICT: launch_epi<TV, TX, TA, EPI_RESTRICT>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_PROLONG: launch_epi<TV, TX, TA, EPI_PROLONG>(c, G, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_AXPY: launch_epi<TV, TX, TA, EPI_AXPY>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_SET: launch_epi<TV, TX, TA, EPI_SET>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_DEFECT: launch_epi<TV, TX, TA, EPI_DEFECT>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_JACOBI: launch_epi<TV, TX, TA, EPI_JACOBI>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_RESTRICT: launch_epi<TV, TX, TA, EPI_RESTRICT>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_PROLONG: launch_epi<TV, TX, TA, EPI_PROLONG>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
     default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
   }
   if (probe) {

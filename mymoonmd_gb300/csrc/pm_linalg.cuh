@@ -11,7 +11,8 @@ namespace pm {
 struct DevCsr {
   int n_rows = 0, n_cols = 0, n_active = 0;
   int64_t nnz = 0;
-  int lanes = 8;  // lanes per row in the SpMV kernels
+  int lanes = 8;   // lanes per row in the SpMV kernels
+  int unroll = 4;  // entries per lane per chunk
   BlockMask mask{};
   DBuf<int> row_ptr, cols;
   DBuf<double> vals;

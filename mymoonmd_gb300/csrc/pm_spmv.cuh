@@ -42,7 +42,10 @@ __device__ __forceinline__ bool row_is_active(const BlockMask& m, int i) {
 template <class T>
 __device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
 
-template <class TV, class TX, class TA, int G, int EPI>
+// G lanes per row, U entries per lane per chunk: a lane first issues its U
+// value and U column loads, then its U gathers of x, then the U products, so
+// that every lane keeps U independent DRAM requests in flight.
+template <class TV, class TX, class TA, int G, int U, int EPI>
 __global__ void __launch_bounds__(256)
 csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ cols,
            const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
@@ -53,19 +56,27 @@ csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ 
   const bool valid = row < n_rows;  // whole groups share a row: no early exit before the shuffles
   const int beg = valid ? __ldg(row_ptr + row) : 0;
   const int end = valid ? __ldg(row_ptr + row + 1) : 0;
-  TA s0 = TA(0), s1 = TA(0);
-  int k = beg + lane;
-  // two independent accumulators for memory-level parallelism
-  for (; k + G < end; k += 2 * G) {
-    const TV v0 = ld_stream(vals + k);
-    const int c0 = ld_stream(cols + k);
-    const TV v1 = ld_stream(vals + k + G);
-    const int c1 = ld_stream(cols + k + G);
-    s0 += TA(v0) * TA(__ldg(x + c0));
-    s1 += TA(v1) * TA(__ldg(x + c1));
+  TA s = TA(0);
+  for (int base = beg; base < end; base += G * U) {
+    TV v[U];
+    int c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = base + u * G + lane;
+      if (k < end) {
+        v[u] = ld_stream(vals + k);
+        c[u] = ld_stream(cols + k);
+      } else {
+        v[u] = TV(0);
+        c[u] = 0;  // x[0] exists whenever the row has entries
+      }
+    }
+    TX xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) s += TA(v[u]) * TA(xv[u]);
   }
-  if (k < end) s0 += TA(ld_stream(vals + k)) * TA(__ldg(x + ld_stream(cols + k)));
-  TA s = s0 + s1;
 #pragma unroll
   for (int off = G / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, G);
   if (!valid) return;
