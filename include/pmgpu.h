@@ -106,7 +106,8 @@ int pm_matrix_make_fp32(pm_matrix* A);
 int pm_matrix_apply_f32(pm_matrix* A, const float* x_dev, float* y_dev);
 /* Launch shape of the CSR kernels of this matrix (no reference counterpart;
  * tuning only): lanes per row (4, 8, 16, 32) and entries per lane per chunk
- * (2, 4, 8). 0 keeps the current value. */
+ * (2, 4, 8) of the per-row-group kernel; (0, 0) selects the default row-block
+ * streaming kernel. */
 int pm_matrix_set_kernel(pm_matrix* A, int lanes, int unroll);
 /* Timed SpMV loop: `reps` applications y = A x on the context's stream, timed
  * with CUDA events; returns ms per application and the algorithmic bytes. */

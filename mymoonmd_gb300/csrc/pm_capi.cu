@@ -307,6 +307,9 @@ int pm_matrix_set_kernel(pm_matrix* A, int lanes, int unroll) {
     return fail(A->ctx, PM_E_INVALID, "entries per lane must be 2, 4 or 8");
   if (lanes) A->csr.lanes = lanes;
   if (unroll) A->csr.unroll = unroll;
+  // an explicit group shape selects the per-row-group kernel; (0, 0) goes back
+  // to the row-block streaming kernel
+  A->csr.stream = (lanes == 0 && unroll == 0);
   return PM_OK;
 }
 

@@ -53,7 +53,28 @@ void DevCsr::upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int*
     if (nnz) PM_CUDA(cudaMemsetAsync(vals.p, 0, vals.bytes(), c->stream));
   }
   lanes = choose_lanes(nr ? double(nnz) / nr : 1.0);
+  unroll = 8;
+  std::vector<int> rb = build_row_blocks(nr, rp, kStreamNnz, 1024);
+  n_rblocks = rb.empty() ? 0 : int(rb.size()) - 1;
+  if (n_rblocks) rblock.upload(rb, c->stream);
+  else rblock.release();
   set_single_block();
+}
+
+std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int max_rows) {
+  std::vector<int> rb;
+  if (n_rows <= 0) return rb;
+  rb.push_back(0);
+  int r0 = 0;
+  for (int i = 0; i < n_rows; ++i) {
+    if (rp[i + 1] - rp[i] > max_nnz) return std::vector<int>();
+    if (rp[i + 1] - rp[r0] > max_nnz || i - r0 >= max_rows) {
+      rb.push_back(i);
+      r0 = i;
+    }
+  }
+  rb.push_back(n_rows);
+  return rb;
 }
 
 void DevCsr::set_single_block() {
@@ -159,8 +180,16 @@ static void launch_gu(pm_ctx* c, int U, int grid, int n, const int* rp, const in
 
 template <class TV, class TX, class TA, int EPI>
 static void launch_epi(pm_ctx* c, int G, int U, int n, const int* rp, const int* ci, const TV* v,
-                       const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
+                       const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m,
+                       const int* rblock = nullptr, int n_rblocks = 0) {
   if (n <= 0) return;
+  if (rblock && n_rblocks > 0) {
+    csr_stream_kernel<TV, TX, TA, kStreamNnz, EPI><<<n_rblocks, 256, 0, c->stream>>>(
+        rblock, rp, ci, v, x, y, b, d, alpha, m);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+    return;
+  }
   const int grid = nblocks((long long)n * G, 256);
   switch (G) {
     case 4: launch_gu<TV, TX, TA, 4, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
@@ -199,6 +228,9 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
                          const TX* x, TX* y, const TX* b, TA alpha, int n) {
   const int G = A.lanes;
   const int U = A.unroll;
+  const bool use_stream = A.stream && A.n_rblocks > 0 && n == A.n_rows;
+  const int* rb = use_stream ? A.rblock.p : nullptr;
+  const int nrb = use_stream ? A.n_rblocks : 0;
   const int* rp = A.row_ptr.p;
   const int* ci = A.cols.p;
   const bool probe = c->probe_nnz != 0 && A.nnz == c->probe_nnz;
@@ -209,12 +241,12 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
     c->probe_bytes.push_back(epi_bytes(A, epi, int(sizeof(TV)), n));
   }
   switch (epi) {
-    case EPI_AXPY: launch_epi<TV, TX, TA, EPI_AXPY>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_SET: launch_epi<TV, TX, TA, EPI_SET>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_DEFECT: launch_epi<TV, TX, TA, EPI_DEFECT>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_JACOBI: launch_epi<TV, TX, TA, EPI_JACOBI>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_RESTRICT: launch_epi<TV, TX, TA, EPI_RESTRICT>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
-    case EPI_PROLONG: launch_epi<TV, TX, TA, EPI_PROLONG>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask); break;
+    case EPI_AXPY: launch_epi<TV, TX, TA, EPI_AXPY>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask, rb, nrb); break;
+    case EPI_SET: launch_epi<TV, TX, TA, EPI_SET>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask, rb, nrb); break;
+    case EPI_DEFECT: launch_epi<TV, TX, TA, EPI_DEFECT>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask, rb, nrb); break;
+    case EPI_JACOBI: launch_epi<TV, TX, TA, EPI_JACOBI>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask, rb, nrb); break;
+    case EPI_RESTRICT: launch_epi<TV, TX, TA, EPI_RESTRICT>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask, rb, nrb); break;
+    case EPI_PROLONG: launch_epi<TV, TX, TA, EPI_PROLONG>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask, rb, nrb); break;
     default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
   }
   if (probe) {

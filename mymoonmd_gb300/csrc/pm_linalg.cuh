@@ -13,6 +13,11 @@ struct DevCsr {
   int64_t nnz = 0;
   int lanes = 8;   // lanes per row in the SpMV kernels
   int unroll = 4;  // entries per lane per chunk
+  // row blocks of the streaming kernel (consecutive rows with at most
+  // kStreamNnz entries); empty when a row is longer than that
+  DBuf<int> rblock;
+  int n_rblocks = 0;
+  bool stream = true;  // use the streaming kernel when row blocks exist
   BlockMask mask{};
   DBuf<int> row_ptr, cols;
   DBuf<double> vals;
@@ -29,6 +34,9 @@ struct DevCsr {
 };
 
 int choose_lanes(double avg_nnz_per_row);
+constexpr int kStreamNnz = 2048;  // entries per row block of the streaming kernel
+// greedy row blocks over a host row-pointer array; empty if a row is too long
+std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int max_rows);
 
 // y := epilogue(A x); see pm_spmv.cuh for the epilogue meanings
 void csr_apply(pm_ctx* c, const DevCsr& A, int epi, const double* x, double* y, const double* b,

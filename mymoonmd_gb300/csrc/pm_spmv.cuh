@@ -97,4 +97,68 @@ csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ 
   }
 }
 
+// Row-block streaming variant. Block b owns the consecutive rows
+// [rblock[b], rblock[b+1]) whose entries, at most NNZB, form one contiguous
+// slice of the CSR arrays. Phase 1: the block streams that slice with
+// warp-contiguous loads (every thread keeps NNZB/256 independent loads in
+// flight), gathers x and stages the products in shared memory. Phase 2: one
+// warp per row sums the row's products (lane-strided partial sums, then a
+// shuffle tree - a fixed order, so results are deterministic) and applies the
+// epilogue.
+template <class TV, class TX, class TA, int NNZB, int EPI>
+__global__ void __launch_bounds__(256)
+csr_stream_kernel(const int* __restrict__ rblock, const int* __restrict__ row_ptr,
+                  const int* __restrict__ cols, const TV* __restrict__ vals, const TX* __restrict__ x,
+                  TX* __restrict__ y, const TX* __restrict__ b, const TX* __restrict__ diag,
+                  TA alpha, BlockMask mask) {
+  constexpr int PER = NNZB / 256;
+  __shared__ TA prod[NNZB];
+  const int r0 = __ldg(rblock + blockIdx.x), r1 = __ldg(rblock + blockIdx.x + 1);
+  const int s = __ldg(row_ptr + r0), e = __ldg(row_ptr + r1);
+  const int t = threadIdx.x;
+  TV v[PER];
+  int c[PER];
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int k = s + u * 256 + t;
+    if (k < e) {
+      v[u] = ld_stream(vals + k);
+      c[u] = ld_stream(cols + k);
+    } else {
+      v[u] = TV(0);
+      c[u] = -1;
+    }
+  }
+  TX xv[PER];
+#pragma unroll
+  for (int u = 0; u < PER; ++u) xv[u] = c[u] >= 0 ? __ldg(x + c[u]) : TX(0);
+#pragma unroll
+  for (int u = 0; u < PER; ++u) prod[u * 256 + t] = TA(v[u]) * TA(xv[u]);
+  __syncthreads();
+  const int warp = t >> 5, lane = t & 31;
+  for (int row = r0 + warp; row < r1; row += 8) {
+    const int a = __ldg(row_ptr + row) - s, z = __ldg(row_ptr + row + 1) - s;
+    TA sum = TA(0);
+    for (int k = a + lane; k < z; k += 32) sum += prod[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+    if (lane == 0) {
+      if constexpr (EPI == EPI_AXPY) {
+        y[row] = TX(TA(y[row]) + alpha * sum);
+      } else if constexpr (EPI == EPI_SET) {
+        y[row] = TX(sum);
+      } else if constexpr (EPI == EPI_DEFECT) {
+        y[row] = TX(TA(b[row]) - sum);
+      } else if constexpr (EPI == EPI_JACOBI) {
+        const TA d = (TA(b[row]) - sum) / TA(diag[row]);
+        y[row] = TX(TA(x[row]) + alpha * d);
+      } else if constexpr (EPI == EPI_RESTRICT) {
+        y[row] = row_is_active(mask, row) ? TX(sum) : TX(0);
+      } else if constexpr (EPI == EPI_PROLONG) {
+        if (row_is_active(mask, row)) y[row] = TX(TA(y[row]) + alpha * sum);
+      }
+    }
+  }
+}
+
 }  // namespace pm
