@@ -101,10 +101,11 @@ csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ 
 // [rblock[b], rblock[b+1]) whose entries, at most NNZB, form one contiguous
 // slice of the CSR arrays. Phase 1: the block streams that slice with
 // warp-contiguous loads (every thread keeps NNZB/256 independent loads in
-// flight), gathers x and stages the products in shared memory. Phase 2: one
-// warp per row sums the row's products (lane-strided partial sums, then a
-// shuffle tree - a fixed order, so results are deterministic) and applies the
-// epilogue.
+// flight), gathers x and stages (value, x) pairs in shared memory. Phase 2:
+// four lanes per row accumulate the row's pairs with one fused multiply-add
+// per entry and combine with two shuffle steps (a fixed order, so results are
+// deterministic), then apply the epilogue. One FMA per entry matters on GB300,
+// whose FP64 pipe is narrow enough for extra FP64 adds to become the limit.
 template <class TV, class TX, class TA, int NNZB, int EPI>
 __global__ void __launch_bounds__(256)
 csr_stream_kernel(const int* __restrict__ rblock, const int* __restrict__ row_ptr,
@@ -112,7 +113,8 @@ csr_stream_kernel(const int* __restrict__ rblock, const int* __restrict__ row_pt
                   TX* __restrict__ y, const TX* __restrict__ b, const TX* __restrict__ diag,
                   TA alpha, BlockMask mask) {
   constexpr int PER = NNZB / 256;
-  __shared__ TA prod[NNZB];
+  __shared__ TV sv[NNZB];
+  __shared__ TX sx[NNZB];
   const int r0 = __ldg(rblock + blockIdx.x), r1 = __ldg(rblock + blockIdx.x + 1);
   const int s = __ldg(row_ptr + r0), e = __ldg(row_ptr + r1);
   const int t = threadIdx.x;
@@ -133,16 +135,23 @@ csr_stream_kernel(const int* __restrict__ rblock, const int* __restrict__ row_pt
 #pragma unroll
   for (int u = 0; u < PER; ++u) xv[u] = c[u] >= 0 ? __ldg(x + c[u]) : TX(0);
 #pragma unroll
-  for (int u = 0; u < PER; ++u) prod[u * 256 + t] = TA(v[u]) * TA(xv[u]);
+  for (int u = 0; u < PER; ++u) {
+    sv[u * 256 + t] = v[u];
+    sx[u * 256 + t] = xv[u];
+  }
   __syncthreads();
-  const int warp = t >> 5, lane = t & 31;
-  for (int row = r0 + warp; row < r1; row += 8) {
-    const int a = __ldg(row_ptr + row) - s, z = __ldg(row_ptr + row + 1) - s;
+  const int slot = t >> 2, lane = t & 3;
+  // every thread runs the same number of row rounds so the shuffles see full warps
+  for (int base = r0; base < r1; base += 64) {
+    const int row = base + slot;
+    const bool has_row = row < r1;
+    const int a = has_row ? __ldg(row_ptr + row) - s : 0;
+    const int z = has_row ? __ldg(row_ptr + row + 1) - s : 0;
     TA sum = TA(0);
-    for (int k = a + lane; k < z; k += 32) sum += prod[k];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
-    if (lane == 0) {
+    for (int k = a + lane; k < z; k += 4) sum = fma(TA(sv[k]), TA(sx[k]), sum);
+    sum += __shfl_down_sync(0xffffffffu, sum, 2, 4);
+    sum += __shfl_down_sync(0xffffffffu, sum, 1, 4);
+    if (has_row && lane == 0) {
       if constexpr (EPI == EPI_AXPY) {
         y[row] = TX(TA(y[row]) + alpha * sum);
       } else if constexpr (EPI == EPI_SET) {
