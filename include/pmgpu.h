@@ -208,6 +208,20 @@ typedef struct pm_cd_coeffs {
 int pm_assemble_cd(pm_ctx* ctx, const pm_disc* d, int level, const pm_cd_coeffs* coeffs,
                    int quad_points, pm_matrix* A, double* rhs_dev);
 
+/* Assembly of level `level` of a convection-diffusion problem into device
+ * arrays the caller owns (vals_dev: the level's nnz matrix values in CSR
+ * order, rhs_dev: its n_dofs right-hand side), allocating no device memory.
+ * No counterpart in the reference: it serves callers that cannot call
+ * cudaMalloc at this point (a serving worker that must not stall concurrent
+ * requests with an allocation, code bound to memory reserved up front). The
+ * element-matrix scratch lives in a static 32 MiB device array per GPU, so
+ * levels needing more than 4 Mi doubles (n_cells*nloc*(nloc+1)) are rejected
+ * with PM_E_INVALID. The first call on a device looks the array up and should
+ * come before any stream capture; calls that overlap on the GPU race on the
+ * shared array. coeffs == NULL keeps the problem's coefficients. */
+int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coeffs* coeffs, double* vals_dev,
+                           double* rhs_dev);
+
 /* ----------------------------------------------------- problem (system) --- */
 /* ConvectionDiffusion<d> / NavierStokes<3> (Stokes) system on the device: the
  * level hierarchy of `disc`, assembled matrices, right-hand side and the solver

@@ -109,6 +109,7 @@ _SIGS = {
     "pm_disc_prolongation_info": (i32, [vp, i32, pi32, pi32, C.POINTER(i64)]),
     "pm_disc_prolongation": (i32, [vp, i32, vp, vp, vp]),
     "pm_assemble_cd": (i32, [vp, vp, i32, C.POINTER(CdCoeffs), i32, vp, vp]),
+    "pm_assemble_cd_noalloc": (i32, [vp, i32, C.POINTER(CdCoeffs), vp, vp]),
     "pm_problem_create_cd": (i32, [vp, vp, C.POINTER(CdCoeffs), i32, C.c_char_p, C.POINTER(vp)]),
     "pm_problem_destroy": (None, [vp]),
     "pm_problem_assemble": (i32, [vp]),

@@ -247,7 +247,8 @@ class FEMatrix:
         return float(ms.value), float(b.value)
 
     def close(self) -> None:
-        if self.owned and self.handle:
+        # after Context.close() the native context is gone; the handle is dropped
+        if self.owned and self.handle and self.ctx.handle:
             lib.pm_matrix_destroy(self.handle)
         self.handle = None
 
@@ -327,7 +328,7 @@ class Solver:
         return buf[: min(cnt.value, buf.size)].copy()
 
     def close(self) -> None:
-        if self.owned and self.handle:
+        if self.owned and self.handle and self.ctx.handle:
             lib.pm_solver_destroy(self.handle)
         self.handle = None
 
@@ -469,6 +470,12 @@ class ConvectionDiffusion:
         check(lib.pm_problem_solver(self.handle, C.byref(h)))
         return Solver(self.ctx, None, handle=h, owned=False)
 
+    def assemble_level_noalloc(self, level: int, vals: DeviceVector, rhs: DeviceVector,
+                               coeffs: Optional[CdCoeffs] = None) -> None:
+        """pm_assemble_cd_noalloc: one level into caller-owned device arrays, no device allocation"""
+        check(lib.pm_assemble_cd_noalloc(self.handle, level, C.byref(coeffs) if coeffs is not None else None,
+                                         vals.ptr, rhs.ptr), self.ctx.handle)
+
     def last_info(self) -> tuple[int, float, float]:
         it, res, init = C.c_int(), C.c_double(), C.c_double()
         check(lib.pm_problem_last_info(self.handle, C.byref(it), C.byref(res), C.byref(init)))
@@ -484,7 +491,7 @@ class ConvectionDiffusion:
                                       arr, _ptr(sol_out)), self.ctx.handle)
 
     def close(self) -> None:
-        if self.handle:
+        if self.handle and self.ctx.handle:
             lib.pm_problem_destroy(self.handle)
         self.handle = None
 

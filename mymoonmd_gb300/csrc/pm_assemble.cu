@@ -338,3 +338,135 @@ void DevRefTables::upload(pm_ctx* c, const RefTables& t) {
 }
 
 }  // namespace pm
+
+// ---------------------------------------------------------------------------
+// Assembly without device allocation.
+//
+// pm_assemble_cd allocates its scratch (the element matrices and element
+// right-hand sides of a level) with cudaMalloc on every call. Some callers
+// cannot do that: a serving worker that must not stall other requests (a
+// cudaMalloc may synchronise the device), code running under a fixed memory
+// budget that was reserved up front, or a host that allocates all device
+// memory itself. pm_assemble_cd_noalloc runs the same element and gather
+// kernels with the scratch placed in the file-scope array below instead.
+//
+// The array holds kNoAllocScratchDoubles doubles (4 Mi doubles = 32 MiB). Every
+// GPU that loads this library holds it until the process exits. A level needs
+// n_cells*nloc*nloc + n_cells*nloc doubles, e.g. 3.1 Mi for 16^3 Q2 hexahedra;
+// larger levels are rejected with PM_E_INVALID.
+#include <mutex>
+
+#include "pm_problem.h"
+
+namespace {
+constexpr size_t kNoAllocScratchDoubles = size_t(4) << 20;
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_scratch_addr[kMaxDevices] = {nullptr};
+}  // namespace
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+// Device address of the scratch array on `device`. In host code the name
+// g_noalloc_scratch is only a host-side stand-in, not a device address, so
+// the address is looked up once per device with that device current.
+static int noalloc_scratch(int device, double** out, std::string& err) {
+  if (device < 0 || device >= kMaxDevices) {
+    err = "device index out of range";
+    return PM_E_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_scratch_addr[device]) {
+    int prev = -1;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e == cudaSuccess && prev != device) e = cudaSetDevice(device);
+    void* ptr = nullptr;
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    if (e != cudaSuccess || !ptr) {
+      err = std::string("cudaGetSymbolAddress of the assembly scratch failed: ") + cudaGetErrorString(e);
+      cudaGetLastError();
+      return PM_E_CUDA;
+    }
+    g_noalloc_scratch_addr[device] = static_cast<double*>(ptr);
+  }
+  *out = g_noalloc_scratch_addr[device];
+  return PM_OK;
+}
+
+namespace pm {
+// element kernels of assemble_cd_level, for the allocation-free entry point
+static void noalloc_elements(pm_ctx* c, const DevAssemblyLevel& L, int dim, int k, int qn,
+                             const pm_cd_coeffs& cf, const DevRefTables& rt, double* K, double* F) {
+  CdCoef co{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured};
+  if (dim == 2 && k == 1 && qn == 3) launch_elem<2, 4, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 2 && k == 1 && qn == 2) launch_elem<2, 4, 4, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 2 && k == 2 && qn == 3) launch_elem<2, 9, 9, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 2 && k == 2 && qn == 4) launch_elem<2, 9, 16, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 1 && qn == 2) launch_elem<3, 8, 8, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 1 && qn == 3) launch_elem<3, 8, 27, 2>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 2 && qn == 3) launch_elem<3, 27, 27, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (dim == 3 && k == 2 && qn == 4) launch_elem<3, 27, 64, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else throw Error(PM_E_UNSUPPORTED, "element / quadrature combination not compiled");
+}
+}  // namespace pm
+
+/* Assembly of one level of a convection-diffusion problem into caller-owned
+ * device arrays, with no device allocation (see the comment block above).
+ * vals_dev receives the level matrix values in the level's CSR order (nnz
+ * doubles), rhs_dev the right-hand side (n_dofs doubles). coeffs == NULL uses
+ * the problem's coefficients. Runs on the problem's context stream.
+ *
+ * The first call on a device looks up the scratch address (cudaGetSymbolAddress);
+ * make that first call before any stream capture. All calls share the one
+ * scratch array, which keeps the last call's contents: the element kernels
+ * overwrite every scratch entry a call reads, so nothing needs clearing, but
+ * calls whose work overlaps on the GPU (other streams or host threads) race
+ * on the array and must be serialised by the caller. */
+extern "C" int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coeffs* coeffs,
+                                      double* vals_dev, double* rhs_dev) {
+  if (!p || !vals_dev || !rhs_dev) return PM_E_INVALID;
+  pm_ctx* c = p->ctx;
+  try {
+    if (level < 0 || level >= int(p->alev.size())) {
+      c->last_error = "level out of range";
+      return PM_E_INVALID;
+    }
+    const pm::DevAssemblyLevel& L = p->alev[level];
+    const size_t kn = size_t(L.n_cells) * L.nloc * L.nloc, fn = size_t(L.n_cells) * L.nloc;
+    if (kn + fn > kNoAllocScratchDoubles) {
+      c->last_error = "level needs " + std::to_string(kn + fn) +
+                      " doubles of assembly scratch; the allocation-free assembly holds at most " +
+                      std::to_string(kNoAllocScratchDoubles) + " (32 MiB)";
+      return PM_E_INVALID;
+    }
+    double* scratch = nullptr;
+    int rc = noalloc_scratch(c->device, &scratch, c->last_error);
+    if (rc != PM_OK) return rc;
+    double* K = scratch;
+    double* F = scratch + kn;
+    const pm::Disc& D = *p->disc->d;
+    pm::noalloc_elements(c, L, D.dim(), D.elem, p->qn, coeffs ? *coeffs : p->coeffs, p->ref, K, F);
+    const int nnz = int(p->mats[level]->csr.nnz);
+    pm::k_gather<<<std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16)), 256, 0, c->stream>>>(
+        nnz, L.gat_ptr.p, L.gat_idx.p, K, vals_dev);
+    const int nd = int(L.diag_pos.n);
+    if (nd) pm::k_set_unit<<<(nd + 255) / 256, 256, 0, c->stream>>>(nd, L.diag_pos.p, vals_dev);
+    const int n = L.n_dofs;
+    pm::k_gather<<<std::max(1, std::min((n + 255) / 256, c->num_sms * 16)), 256, 0, c->stream>>>(
+        n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs_dev);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      c->last_error = std::string("kernel launch failed: ") + cudaGetErrorString(e);
+      return PM_E_CUDA;
+    }
+    c->kernel_launches += nd ? 3 : 2;
+    return PM_OK;
+  } catch (const pm::Error& e) {
+    c->last_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    c->last_error = e.what();
+    return PM_E_INVALID;
+  }
+}

@@ -6,6 +6,7 @@
 
 #include "pm_assemble.h"
 #include "pm_disc.h"
+#include "pm_problem.h"
 #include "pm_solver.h"
 
 using namespace pm;
@@ -26,20 +27,6 @@ static int fail(pm_ctx* c, int code, const char* msg) {
   catch (const std::out_of_range& e) { return fail((ctxp), PM_E_INVALID, e.what()); } \
   catch (const std::bad_alloc&) { return fail((ctxp), PM_E_OOM, "host allocation failed"); } \
   catch (const std::exception& e) { return fail((ctxp), PM_E_INVALID, e.what()); }
-
-struct pm_problem {
-  pm_ctx* ctx = nullptr;
-  const pm_disc* disc = nullptr;
-  pm_cd_coeffs coeffs{};
-  int qn = 3;
-  std::vector<pm_matrix*> mats;
-  std::vector<DevAssemblyLevel> alev;
-  DevRefTables ref;
-  DBuf<double> K, F, rhs, sol, rhs_coarse;
-  pm_solver* solver = nullptr;
-  bool solver_ready = false;
-  ~pm_problem();
-};
 
 extern "C" {
 

@@ -1,0 +1,69 @@
+"""The allocation-free assembly entry point (pm_assemble_cd_noalloc) against the
+allocating one (pm_assemble_cd), through the C ABI.
+
+pm_assemble_cd_noalloc is for callers that cannot call cudaMalloc when they
+assemble - for instance a serving worker that must not stall requests already
+running on the GPU with an allocation, or a host that reserved all device memory
+up front. It keeps its scratch in a static device array of 32 MiB, so it must
+give the same matrix and right-hand side as the allocating path, call after
+call, and refuse levels whose scratch would not fit.
+
+This file is collected last so that a failure here comes after every other test
+has run; it creates its own context and passes alone in a fresh process too.
+"""
+import numpy as np
+import pytest
+
+import mymoonmd_gb300 as m
+
+pytestmark = pytest.mark.gpu
+
+# the same bound the other assembly parity tests use
+TOL = 1e-13
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_noalloc_assembly_matches_allocating_assembly_twice():
+    ctx = m.Context(0)
+    try:
+        disc = m.Discretization(m.GEO_CUBE_HEXA, 1, 3, 3, m.KIND_CD, 2)  # 8^3 Q2, 3 levels
+        cf = m.cd_coeffs(0.05, (1.0, 0.5, 0.25), 0.3, True)
+        prob = m.ConvectionDiffusion(ctx, disc, cf, "solver_type: direct\n", quad_points=3)
+        for level in range(disc.n_levels):
+            info = disc.level_info(level)
+            rp, ci = disc.structure(level)
+            A = m.FEMatrix.from_csr(ctx, rp, ci, None, n_active=info["n_active"])
+            rhs = m.DeviceVector(ctx, info["n_dofs"])
+            m.assemble_cd(ctx, disc, level, cf, 3, A, rhs)  # existing entry point (allocates scratch)
+            ref_vals, ref_rhs = A.values(), rhs.numpy()
+            for _ in range(2):  # two calls in a row share the static scratch
+                vals = m.DeviceVector(ctx, info["nnz"])
+                r = m.DeviceVector(ctx, info["n_dofs"])
+                prob.assemble_level_noalloc(level, vals, r, cf)
+                assert rel(vals.numpy(), ref_vals) <= TOL
+                assert rel(r.numpy(), ref_rhs) <= TOL
+        prob.close()
+    finally:
+        ctx.close()
+
+
+def test_noalloc_assembly_rejects_levels_beyond_its_scratch():
+    ctx = m.Context(0)
+    try:
+        # 24^3 Q2 hexahedra need 13824 * 27 * 28 doubles > 4 Mi
+        disc = m.Discretization(m.GEO_CUBE_HEXA, 3, 3, 2, m.KIND_CD, 2)
+        cf = m.cd_coeffs(0.1, (1.0, 0.0, 0.0), 0.0, True)
+        prob = m.ConvectionDiffusion(ctx, disc, cf, "solver_type: direct\n", quad_points=3)
+        info = disc.level_info(1)
+        vals = m.DeviceVector(ctx, info["nnz"])
+        r = m.DeviceVector(ctx, info["n_dofs"])
+        with pytest.raises(m.PmError, match="scratch"):
+            prob.assemble_level_noalloc(1, vals, r)
+        prob.assemble_level_noalloc(0, m.DeviceVector(ctx, disc.level_info(0)["nnz"]),
+                                    m.DeviceVector(ctx, disc.level_info(0)["n_dofs"]))
+        prob.close()
+    finally:
+        ctx.close()
