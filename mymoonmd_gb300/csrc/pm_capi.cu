@@ -380,6 +380,7 @@ int pm_solver_create(pm_ctx* c, const char* params, pm_solver** out) {
     s->restart = p.integer("gmres_restart", 20);
     s->damping = p.num("damping_factor", 1.0);
     s->mixed = p.str("gpu_precision", "fp64") == "mixed";
+    s->use_graphs = p.integer("gpu_cuda_graphs", 1) != 0;
     if (s->prec != "no_preconditioner" && s->prec != "jacobi" && s->prec != "multigrid")
       throw Error(PM_E_UNSUPPORTED, "preconditioner '" + s->prec + "' is not implemented on the GPU");
     s->use_mg = s->solver_type == "iterative" && s->prec == "multigrid";
@@ -431,6 +432,7 @@ int pm_solver_set_multigrid_level(pm_solver* s, int level, int n_levels, pm_matr
     throw Error(PM_E_INVALID, "multigrid_n_levels does not match the number of levels given");
   if (level < 0 || level >= n_levels) throw Error(PM_E_INVALID, "multigrid level out of range");
   MGLevel& lv = s->mg.levels[level];
+  s->drop_graphs();
   lv.A = A;
   if (level < n_levels - 1) {
     if (!p_rp || !p_ci || !p_v) throw Error(PM_E_INVALID, "coarse levels need a prolongation");

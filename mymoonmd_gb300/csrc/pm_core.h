@@ -57,6 +57,10 @@ struct DBuf {
     }
     n = count;
   }
+  // keep the allocation (and its address) when the size already matches
+  void ensure(size_t count) {
+    if (count != n || (count && !p)) alloc(count);
+  }
   void release() {
     if (p) cudaFree(p);
     p = nullptr;

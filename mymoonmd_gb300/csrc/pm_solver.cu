@@ -130,22 +130,22 @@ void Multigrid::update(pm_ctx* c) {
         lv.P.make_fp32(c);
         lv.R.make_fp32(c);
       }
-      lv.rhs32.alloc(n);
-      lv.sol32.alloc(n);
-      lv.alt32.alloc(n);
-      lv.defect32.alloc(n);
+      lv.rhs32.ensure(n);
+      lv.sol32.ensure(n);
+      lv.alt32.ensure(n);
+      lv.defect32.ensure(n);
     }
-    // FP64 buffers (the finest level uses the caller's vectors in FP64 mode
-    // but keeps its own for the Jacobi ping-pong)
-    lv.rhs.alloc(n);
-    lv.sol.alloc(n);
-    lv.alt.alloc(n);
-    lv.defect.alloc(n);
+    // FP64 buffers (kept at the same addresses across updates, so captured
+    // graphs stay valid)
+    lv.rhs.ensure(n);
+    lv.sol.ensure(n);
+    lv.alt.ensure(n);
+    lv.defect.ensure(n);
     if (lv.smoother == SM_DIRECT) {
       lv.coarse.build(c, A);
       if (mixed) {
-        lv.coarse_rhs64.alloc(n);
-        lv.coarse_sol64.alloc(n);
+        lv.coarse_rhs64.ensure(n);
+        lv.coarse_sol64.ensure(n);
       }
     }
   }
@@ -409,8 +409,49 @@ using namespace pm;
 // ------------------------------------------------------------- solver ------
 void pm_solver::ensure_work(size_t n_vectors, int n) {
   const size_t need = n_vectors * size_t(n);
-  if (work.n < need) work.alloc(need);
+  if (work.n < need || work_n != size_t(n)) {
+    drop_graphs();
+    if (work.n < need) work.alloc(need);
+  }
   work_n = size_t(n);
+}
+
+void pm_solver::drop_graphs() {
+  for (auto& g : arnoldi_graphs)
+    if (g) cudaGraphExecDestroy(g);
+  arnoldi_graphs.clear();
+  arnoldi_launches.clear();
+}
+
+pm_solver::~pm_solver() { drop_graphs(); }
+
+// hash of every device address a captured Arnoldi step reads or writes
+size_t pm_solver::layout_signature() const {
+  size_t h = 1469598103934665603ull;
+  auto mix = [&h](const void* p) {
+    h ^= reinterpret_cast<size_t>(p);
+    h *= 1099511628211ull;
+  };
+  mix(A);
+  if (A) {
+    mix(A->csr.vals.p); mix(A->csr.row_ptr.p); mix(A->csr.cols.p); mix(A->csr.rblock.p); mix(A->csr.diag.p);
+  }
+  for (const auto& lv : mg.levels) {
+    mix(lv.A);
+    if (lv.A) {
+      mix(lv.A->csr.vals.p); mix(lv.A->csr.vals32.p); mix(lv.A->csr.diag.p); mix(lv.A->csr.diag32.p);
+      mix(lv.A->csr.row_ptr.p); mix(lv.A->csr.cols.p); mix(lv.A->csr.rblock.p);
+    }
+    mix(lv.P.vals.p); mix(lv.P.vals32.p); mix(lv.R.vals.p); mix(lv.R.vals32.p);
+    mix(lv.rhs.p); mix(lv.sol.p); mix(lv.alt.p); mix(lv.defect.p);
+    mix(lv.rhs32.p); mix(lv.sol32.p); mix(lv.alt32.p); mix(lv.defect32.p);
+    mix(lv.coarse.inv.p); mix(lv.coarse.act.p); mix(lv.coarse.pos.p); mix(lv.coarse.tmp.p);
+    mix(lv.coarse_rhs64.p); mix(lv.coarse_sol64.p);
+  }
+  mix(work.p); mix(gm.p); mix(flags.p);
+  mix(ctx->partials.p); mix(ctx->host_scalars);
+  h ^= size_t(restart) * 31 + size_t(work_n);
+  return h;
 }
 
 bool pm_solver::converged(double r, unsigned it) {
@@ -461,16 +502,30 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   double* V = work.p + work_n;                     // m+1 vectors
   double* Z = work.p + work_n * size_t(m + 2);     // m vectors
   const size_t ld = work_n;
-  gm.alloc(size_t(ldh) * m + 4 * size_t(m + 1) + 8);
+  const size_t gm_need = size_t(ldh) * m + 4 * size_t(m + 1) + 8;
+  if (gm.n != gm_need) {
+    drop_graphs();
+    gm.alloc(gm_need);
+  }
   double* H = gm.p;
   double* s = H + size_t(ldh) * m;
   double* cs = s + (m + 1);
   double* sn = cs + (m + 1);
   double* y = sn + (m + 1);
   double* dres = y + (m + 1);
-  flags.alloc(1);
+  if (!flags.p) {
+    drop_graphs();
+    flags.alloc(1);
+  }
   PM_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), c->stream));
   PM_CUDA(cudaMemsetAsync(H, 0, sizeof(double) * size_t(ldh) * m, c->stream));
+  {
+    const size_t sig = layout_signature();
+    if (sig != graphs_signature) {
+      drop_graphs();
+      graphs_signature = sig;
+    }
+  }
   double* partA = c->partials.p;
   double* partB = c->partials.p + kRedBlocks;
 
@@ -492,28 +547,65 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
     int i = 0;
     bool done = false;
     for (; i < m && j <= (unsigned long)max_it; ++i, ++j) {
-      double* vi = V + ld * i;
-      double* zi = Z + ld * i;
-      precondition(vi, zi);
-      csr_apply(c, M, EPI_SET, zi, r, nullptr, 1.0);  // r = A z_i
-      dot_partials(c, n, r, V, partA);                   // <r, v_0>
-      double* pin = partA;
-      double* pout = partB;
-      for (int k = 0; k <= i; ++k) {
-        const double* next = (k < i) ? V + ld * (k + 1) : r;
-        k_fg_mgs<<<grid, 256, 0, c->stream>>>(n, ldh, k, i, r, V + ld * k, next, pin, pout, H);
+      // one Arnoldi step: z_i = M^-1 v_i, r = A z_i, modified Gram-Schmidt,
+      // H(i+1,i), v_{i+1}, Givens rotation, residual copied to the host
+      auto arnoldi_step = [&]() {
+        double* vi = V + ld * i;
+        double* zi = Z + ld * i;
+        precondition(vi, zi);
+        csr_apply(c, M, EPI_SET, zi, r, nullptr, 1.0);  // r = A z_i
+        dot_partials(c, n, r, V, partA);                   // <r, v_0>
+        double* pin = partA;
+        double* pout = partB;
+        for (int k = 0; k <= i; ++k) {
+          const double* next = (k < i) ? V + ld * (k + 1) : r;
+          k_fg_mgs<<<grid, 256, 0, c->stream>>>(n, ldh, k, i, r, V + ld * k, next, pin, pout, H);
+          PM_CHECK_LAUNCH();
+          c->kernel_launches++;
+          std::swap(pin, pout);
+        }
+        k_fg_normalize<<<grid, 256, 0, c->stream>>>(n, ldh, i, r, V + ld * (i + 1), pin, H, flags.p);
         PM_CHECK_LAUNCH();
-        c->kernel_launches++;
-        std::swap(pin, pout);
+        k_fg_givens<<<1, 32, 0, c->stream>>>(ldh, i, H, cs, sn, s, dres);
+        PM_CHECK_LAUNCH();
+        c->kernel_launches += 2;
+        PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        PM_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(c->host_scalars + 1), flags.p, sizeof(int),
+                                cudaMemcpyDeviceToHost, c->stream));
+      };
+      // the probe brackets launches with events one by one: no graphs then
+      const bool graphs = use_graphs && c->probe_nnz == 0;
+      if (graphs) {
+        if (arnoldi_graphs.size() != size_t(m)) {
+          drop_graphs();
+          arnoldi_graphs.assign(m, nullptr);
+          arnoldi_launches.assign(m, 0);
+        }
+        if (!arnoldi_graphs[i]) {
+          const uint64_t before = c->kernel_launches;
+          cudaGraph_t g = nullptr;
+          PM_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+          try {
+            arnoldi_step();
+          } catch (...) {
+            cudaStreamEndCapture(c->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+          }
+          PM_CUDA(cudaStreamEndCapture(c->stream, &g));
+          cudaGraphExec_t ex = nullptr;
+          cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+          cudaGraphDestroy(g);
+          PM_CUDA(e);
+          arnoldi_graphs[i] = ex;
+          arnoldi_launches[i] = c->kernel_launches - before;
+          c->kernel_launches = before;
+        }
+        PM_CUDA(cudaGraphLaunch(arnoldi_graphs[i], c->stream));
+        c->kernel_launches += arnoldi_launches[i];
+      } else {
+        arnoldi_step();
       }
-      k_fg_normalize<<<grid, 256, 0, c->stream>>>(n, ldh, i, r, V + ld * (i + 1), pin, H, flags.p);
-      PM_CHECK_LAUNCH();
-      k_fg_givens<<<1, 32, 0, c->stream>>>(ldh, i, H, cs, sn, s, dres);
-      PM_CHECK_LAUNCH();
-      c->kernel_launches += 2;
-      PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-      PM_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(c->host_scalars + 1), flags.p, sizeof(int),
-                              cudaMemcpyDeviceToHost, c->stream));
       PM_CUDA(cudaStreamSynchronize(c->stream));
       resid = c->host_scalars[0];
       if (*reinterpret_cast<int*>(c->host_scalars + 1))

@@ -91,6 +91,16 @@ struct pm_solver {
   size_t work_n = 0;
   pm::DBuf<double> gm;    // FGMRES H, s, cs, sn, y
   pm::DBuf<int> flags;
+  // one captured CUDA graph per Arnoldi index i (preconditioner, SpMV,
+  // Gram-Schmidt, Givens rotation, residual read-back); rebuilt whenever the
+  // buffers they reference are reallocated
+  std::vector<cudaGraphExec_t> arnoldi_graphs;
+  std::vector<uint64_t> arnoldi_launches;  // kernels inside each graph
+  bool use_graphs = true;
+  size_t graphs_signature = 0;  // addresses the captured graphs were built with
+  size_t layout_signature() const;
+  void drop_graphs();
+  ~pm_solver();
   // loop information of the last solve
   int last_it = 0;
   double last_res = 0.0, init_res = 0.0, prev_res = 0.0;

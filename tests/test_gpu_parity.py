@@ -94,14 +94,18 @@ def test_spmv_known_answer(ctx):
     assert np.allclose(y.numpy(), [46.03, -301.482, -221.826, 79.054], rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("shape", [None, (0, 0), (8, 2), (32, 4)])
 @pytest.mark.parametrize("case", ["q1_2d", "q2_3d"])
-def test_spmv_apply_scaled_add_matches_oracle(ctx, case):
+def test_spmv_apply_scaled_add_matches_oracle(ctx, case, shape):
+    """default launch shape, the row-block streaming kernel (0, 0) and other group shapes"""
     disc, prob, ora = make_pair(ctx, case, mg_db(CASES[case][3]))
     lv = ora.finest
     rng = np.random.default_rng(3)
     x = rng.standard_normal(lv.n_dofs)
     y0 = rng.standard_normal(lv.n_dofs)
     A = prob.matrix(-1)
+    if shape is not None:
+        A.set_kernel(*shape)
     xd, yd = m.DeviceVector.from_numpy(ctx, x), m.DeviceVector.from_numpy(ctx, y0)
     A.apply_scaled_add(xd, yd, -0.7)
     ref = ocd.apply_scaled_add(lv.row_ptr, lv.cols, ora.vals[-1], ora.active(), x, y0, -0.7)
