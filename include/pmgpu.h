@@ -59,6 +59,11 @@ int pm_ctx_kernel_launches(const pm_ctx* ctx, uint64_t* out);
 int pm_ctx_time_begin(pm_ctx* ctx);
 int pm_ctx_time_end(pm_ctx* ctx, float* ms);
 int pm_version(void);
+/* Context options (no reference counterpart):
+ *   "assembly_quadrature_loop" 0|1 - element matrices by the per-quadrature-
+ *   point loop of LocalAssembling instead of the reference-tensor contraction
+ *   (same quadrature, different summation order). */
+int pm_ctx_set_option(pm_ctx* ctx, const char* key, int value);
 /* Launch probe (no reference counterpart; measurement only): while enabled
  * (nnz != 0), every SpMV-family launch (apply, defect, Jacobi sweep, transfer)
  * on a matrix with exactly `nnz` nonzeros is bracketed by CUDA events on the

@@ -63,6 +63,7 @@ _SIGS = {
     "pm_ctx_destroy": (None, [vp]),
     "pm_last_error": (C.c_char_p, [vp]),
     "pm_ctx_synchronize": (i32, [vp]),
+    "pm_ctx_set_option": (i32, [vp, C.c_char_p, i32]),
     "pm_ctx_kernel_launches": (i32, [vp, C.POINTER(C.c_uint64)]),
     "pm_ctx_time_begin": (i32, [vp]),
     "pm_ctx_time_end": (i32, [vp, C.POINTER(C.c_float)]),

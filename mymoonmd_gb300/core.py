@@ -49,6 +49,9 @@ class Context:
     def synchronize(self) -> None:
         check(lib.pm_ctx_synchronize(self.handle), self.handle)
 
+    def set_option(self, key: str, value: int) -> None:
+        check(lib.pm_ctx_set_option(self.handle, key.encode(), int(value)), self.handle)
+
     def kernel_launches(self) -> int:
         v = C.c_uint64()
         check(lib.pm_ctx_kernel_launches(self.handle, C.byref(v)))

@@ -147,6 +147,31 @@ __device__ __forceinline__ double rhs_value(const CdCoef& k, int dim, const doub
   return f;
 }
 
+// the same right-hand side with sin(pi x) and cos(pi x) from one sincospi call
+__device__ __forceinline__ double rhs_value_pi(const CdCoef& k, int dim, const double* x) {
+  if (!k.manufactured) return k.fconst;
+  const double p = 3.14159265358979323846;
+  double s[3], co[3];
+  for (int d = 0; d < dim; ++d) sincospi(x[d], &s[d], &co[d]);
+  double u, ux, uy, uz = 0.0, lap;
+  if (dim == 2) {
+    u = s[0] * s[1];
+    ux = p * co[0] * s[1];
+    uy = p * s[0] * co[1];
+    lap = -2 * p * p * s[0] * s[1];
+  } else {
+    u = s[0] * s[1] * s[2];
+    ux = p * co[0] * s[1] * s[2];
+    uy = p * s[0] * co[1] * s[2];
+    uz = p * s[0] * s[1] * co[2];
+    lap = -3 * p * p * s[0] * s[1] * s[2];
+  }
+  double f = -k.eps * lap;
+  f += k.b0 * ux + k.b1 * uy + (dim == 3 ? k.b2 * uz : 0.0);
+  f += k.c * u;
+  return f;
+}
+
 // One group of TPC threads per cell, CPB cells per block. Shared memory per
 // cell: A[q][i][4] = Mult_q (eps dphi_i, phi_i), B[q][j][4] = (dphi_j, b.dphi_j + c phi_j);
 // K_ij = sum_q sum_d A[q][i][d] B[q][j][d].
@@ -249,6 +274,147 @@ __global__ void __launch_bounds__(256) k_elem_cd(int n_cells, const double* __re
   }
 }
 
+// Reference-tensor element kernel. On an affine cell with cell-constant eps,
+// b, c the quadrature sum of BilinearAssembleGalerkin factors into
+//   K_e = |det J| ( sum_{a<=b} A_ab S_ab + sum_a beta_a C_a + c M ),
+//   A_ab = eps sum_d G_da G_db,  beta_a = sum_d b_d G_da,  G = J^{-T},
+// with the reference tensors S, C, M (sums over the same quadrature points,
+// computed once per element type). This is the same quadrature applied in a
+// different summation order: NT FMAs per entry instead of 4 per quadrature
+// point. The right-hand side keeps the per-point loop (f varies in the cell).
+template <int DIM, int NB, int NQ, int CHUNK>
+__global__ void __launch_bounds__(256) k_elem_cd_tensor(int n_cells, const double* __restrict__ verts,
+                                                        const double* __restrict__ ref,
+                                                        const double* __restrict__ T, CdCoef co,
+                                                        double* __restrict__ K, double* __restrict__ F) {
+  constexpr int NV = DIM == 2 ? 4 : 8;
+  constexpr int NT = DIM * (DIM + 1) / 2 + DIM + 1;
+  __shared__ double coef[CHUNK][NT];
+  __shared__ double fq[CHUNK][NQ];
+  __shared__ double geo[CHUNK][13];  // x0, J (row-major), |det J|
+  const double* phi = ref;
+  const double* w = ref + 4 * NQ * NB;
+  const double* xi = w + NQ;
+  const int c0 = blockIdx.x * CHUNK;
+  const int nc = min(CHUNK, n_cells - c0);
+  const int t = threadIdx.x;
+  double x0[3] = {0, 0, 0}, J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  // per-cell coefficients (one thread per cell)
+  if (t < nc) {
+    affine_map<DIM>(verts + (size_t)(c0 + t) * NV * DIM, x0, J);
+    double G[3][3] = {{0}}, det;
+    if (DIM == 2) {
+      det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      const double r = 1.0 / det;
+      G[0][0] = J[1][1] * r;  G[0][1] = -J[1][0] * r;
+      G[1][0] = -J[0][1] * r; G[1][1] = J[0][0] * r;
+    } else {
+      det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+            J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+            J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      const double r = 1.0 / det;
+      G[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * r;
+      G[0][1] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) * r;
+      G[0][2] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * r;
+      G[1][0] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * r;
+      G[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+      G[1][2] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * r;
+      G[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+      G[2][1] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) * r;
+      G[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    }
+    const double adet = fabs(det);
+    const double bv[3] = {co.b0, co.b1, co.b2};
+    int k = 0;
+    for (int a = 0; a < DIM; ++a)
+      for (int b = a; b < DIM; ++b) {
+        double s = 0.0;
+        for (int d = 0; d < DIM; ++d) s += G[d][a] * G[d][b];
+        coef[t][k++] = adet * co.eps * s;
+      }
+    for (int a = 0; a < DIM; ++a) {
+      double s = 0.0;
+      for (int d = 0; d < DIM; ++d) s += bv[d] * G[d][a];
+      coef[t][k++] = adet * s;
+    }
+    coef[t][k] = adet * co.c;
+    for (int d = 0; d < 3; ++d) {
+      geo[t][d] = x0[d];
+      for (int a = 0; a < 3; ++a) geo[t][3 + d * 3 + a] = J[d][a];
+    }
+    geo[t][12] = adet;
+  }
+  __syncthreads();
+  // quadrature weights times |det J| times f at the mapped points, one
+  // (cell, point) pair per thread
+  for (int e = t; e < nc * NQ; e += blockDim.x) {
+    const int cl = e / NQ, q = e % NQ;
+    double x[3];
+    for (int d = 0; d < DIM; ++d) {
+      double s = geo[cl][d];
+      for (int a = 0; a < DIM; ++a) s += geo[cl][3 + d * 3 + a] * xi[q * 3 + a];
+      x[d] = s;
+    }
+    fq[cl][q] = w[q] * geo[cl][12] * rhs_value_pi(co, DIM, x);
+  }
+  __syncthreads();
+  for (int e = t; e < nc * NB * NB; e += blockDim.x) {
+    const int cl = e / (NB * NB), p = e % (NB * NB);
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) s = fma(coef[cl][k], __ldg(T + k * NB * NB + p), s);
+    K[(size_t)(c0 + cl) * NB * NB + p] = s;
+  }
+  for (int e = t; e < nc * NB; e += blockDim.x) {
+    const int cl = e / NB, i = e % NB;
+    double s = 0.0;
+    for (int q = 0; q < NQ; ++q) s += fq[cl][q] * phi[q * NB + i];
+    F[(size_t)(c0 + cl) * NB + i] = s;
+  }
+}
+
+void build_ref_tensors(const RefTables& t, std::vector<double>& out) {
+  const int D = t.dim, nb = t.nb, nq = t.nq;
+  const int nt = n_ref_tensors(D);
+  out.assign(size_t(nt) * nb * nb, 0.0);
+  auto dphi = [&](int a, int q, int i) { return t.dphi[(size_t(a) * nq + q) * nb + i]; };
+  int k = 0;
+  for (int a = 0; a < D; ++a)
+    for (int b = a; b < D; ++b, ++k)
+      for (int i = 0; i < nb; ++i)
+        for (int j = 0; j < nb; ++j) {
+          double s = 0.0;
+          for (int q = 0; q < nq; ++q) {
+            s += t.w[q] * dphi(a, q, i) * dphi(b, q, j);
+            if (a != b) s += t.w[q] * dphi(b, q, i) * dphi(a, q, j);
+          }
+          out[(size_t(k) * nb + i) * nb + j] = s;
+        }
+  for (int a = 0; a < D; ++a, ++k)
+    for (int i = 0; i < nb; ++i)
+      for (int j = 0; j < nb; ++j) {
+        double s = 0.0;
+        for (int q = 0; q < nq; ++q) s += t.w[q] * t.phi[size_t(q) * nb + i] * dphi(a, q, j);
+        out[(size_t(k) * nb + i) * nb + j] = s;
+      }
+  for (int i = 0; i < nb; ++i)
+    for (int j = 0; j < nb; ++j) {
+      double s = 0.0;
+      for (int q = 0; q < nq; ++q) s += t.w[q] * t.phi[size_t(q) * nb + i] * t.phi[size_t(q) * nb + j];
+      out[(size_t(k) * nb + i) * nb + j] = s;
+    }
+}
+
+template <int DIM, int NB, int NQ>
+static void launch_elem_tensor(pm_ctx* c, int n_cells, const double* verts, const double* ref,
+                               const double* T, const CdCoef& co, double* K, double* F) {
+  constexpr int CHUNK = 64;
+  const int grid = (n_cells + CHUNK - 1) / CHUNK;
+  k_elem_cd_tensor<DIM, NB, NQ, CHUNK><<<grid, 256, 0, c->stream>>>(n_cells, verts, ref, T, co, K, F);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
 // stage 2: CSR values from the element matrices, in cell order
 __global__ void k_gather(int nnz, const int* __restrict__ ptr, const int* __restrict__ idx,
                          const double* __restrict__ K, double* __restrict__ vals) {
@@ -300,7 +466,18 @@ void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, 
                        double* K, double* F) {
   CdCoef co{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured};
   const int k = elem;
-  if (dim == 2 && k == 1 && qn == 3) launch_elem<2, 4, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  const double* T = rt.tensors.p;
+  if (!c->assembly_quadrature_loop && T) {
+    if (dim == 2 && k == 1 && qn == 3) launch_elem_tensor<2, 4, 9>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (dim == 2 && k == 1 && qn == 2) launch_elem_tensor<2, 4, 4>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (dim == 2 && k == 2 && qn == 3) launch_elem_tensor<2, 9, 9>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (dim == 2 && k == 2 && qn == 4) launch_elem_tensor<2, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (dim == 3 && k == 1 && qn == 2) launch_elem_tensor<3, 8, 8>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (dim == 3 && k == 1 && qn == 3) launch_elem_tensor<3, 8, 27>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (dim == 3 && k == 2 && qn == 3) launch_elem_tensor<3, 27, 27>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (dim == 3 && k == 2 && qn == 4) launch_elem_tensor<3, 27, 64>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else throw Error(PM_E_UNSUPPORTED, "element / quadrature combination not compiled");
+  } else if (dim == 2 && k == 1 && qn == 3) launch_elem<2, 4, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 2 && k == 1 && qn == 2) launch_elem<2, 4, 4, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 2 && k == 2 && qn == 3) launch_elem<2, 9, 9, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 2 && k == 2 && qn == 4) launch_elem<2, 9, 16, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
@@ -335,6 +512,10 @@ void DevRefTables::upload(pm_ctx* c, const RefTables& t) {
   data.upload(h, c->stream);
   nb = t.nb;
   nq = t.nq;
+  std::vector<double> tens;
+  build_ref_tensors(t, tens);
+  tensors.upload(tens, c->stream);
+  nt = n_ref_tensors(t.dim);
 }
 
 }  // namespace pm

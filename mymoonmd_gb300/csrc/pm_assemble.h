@@ -15,10 +15,17 @@ struct RefTables {
 void build_qk_tables(int dim, int k, int qn, RefTables& t);
 
 struct DevRefTables {
-  int nb = 0, nq = 0;
+  int nb = 0, nq = 0, nt = 0;
   DBuf<double> data;
+  // reference tensors of the bilinear form (sum over the quadrature points
+  // of the reference element): stiffness S_ab (a<=b, S_ab+S_ba for a<b),
+  // convection C_a[i][j] = sum_q w phi_i d_a phi_j, mass M; nt x nb x nb
+  DBuf<double> tensors;
   void upload(pm_ctx* c, const RefTables& t);
 };
+// number of reference tensors: dim*(dim+1)/2 + dim + 1
+inline int n_ref_tensors(int dim) { return dim * (dim + 1) / 2 + dim + 1; }
+void build_ref_tensors(const RefTables& t, std::vector<double>& out);
 
 // device copy of one level's assembly inputs
 struct DevAssemblyLevel {

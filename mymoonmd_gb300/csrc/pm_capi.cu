@@ -65,6 +65,15 @@ int pm_ctx_synchronize(pm_ctx* c) {
   PM_CATCH(c)
 }
 
+int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
+  if (!c || !key) return PM_E_INVALID;
+  if (std::string(key) == "assembly_quadrature_loop") {
+    c->assembly_quadrature_loop = value != 0;
+    return PM_OK;
+  }
+  return fail(c, PM_E_INVALID, (std::string("unknown context option ") + key).c_str());
+}
+
 int pm_ctx_kernel_launches(const pm_ctx* c, uint64_t* out) {
   if (!c || !out) return PM_E_INVALID;
   *out = c->kernel_launches;

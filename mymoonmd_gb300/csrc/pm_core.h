@@ -92,6 +92,9 @@ struct pm_ctx {
   pm::DBuf<double> partials;     // per-block partial sums of reductions
   int n_partials = 0;
   uint64_t kernel_launches = 0;  // kernels this library launched on the stream
+  // element matrices by the per-quadrature-point loop instead of the
+  // reference-tensor contraction (option "assembly_quadrature_loop")
+  int assembly_quadrature_loop = 0;
   // launch probe: CUDA events around every SpMV-family launch on matrices
   // with probe_nnz nonzeros (0 = off); resolved by pm_ctx_probe_result
   int64_t probe_nnz = 0;

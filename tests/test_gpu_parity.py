@@ -63,13 +63,19 @@ def make_pair(ctx, case, db):
     return disc, prob, ora
 
 
+@pytest.mark.parametrize("qloop", [0, 1])
 @pytest.mark.parametrize("case", list(CASES))
-def test_assembly_matches_oracle(ctx, case):
-    disc, prob, ora = make_pair(ctx, case, mg_db(CASES[case][3]))
-    for l in range(disc.n_levels):
-        vals = prob.matrix(l).values()
-        assert rel(vals, ora.vals[l]) <= 1e-13, (case, l)
-    assert rel(prob.rhs(), ora.rhs[-1]) <= 1e-13
+def test_assembly_matches_oracle(ctx, case, qloop):
+    """reference-tensor contraction (default) and per-quadrature-point loop"""
+    ctx.set_option("assembly_quadrature_loop", qloop)
+    try:
+        disc, prob, ora = make_pair(ctx, case, mg_db(CASES[case][3]))
+        for l in range(disc.n_levels):
+            vals = prob.matrix(l).values()
+            assert rel(vals, ora.vals[l]) <= 1e-13, (case, l)
+        assert rel(prob.rhs(), ora.rhs[-1]) <= 1e-13
+    finally:
+        ctx.set_option("assembly_quadrature_loop", 0)
 
 
 def test_spmv_known_answer(ctx):
