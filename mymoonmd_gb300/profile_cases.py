@@ -1,0 +1,82 @@
+"""Small, fixed workloads for kernel profiling (ncu) of the solve path.
+
+    python -m mymoonmd_gb300.profile_cases request [--precision mixed|fp64]
+        one warm-up request, then one request (assembly + solve) of the 3D Q2
+        32^3 convection-diffusion workload (274,625 DOFs, 4 levels)
+    python -m mymoonmd_gb300.profile_cases spmv
+        the finest 32^3 Q2 matrix: two FP64 and two FP32 SpMV launches
+    python -m mymoonmd_gb300.profile_cases assembly
+        one assembly of the four 32^3 Q2 levels
+
+Each case prints what it ran; device memory stays below 2 GB.
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+
+from . import core as m
+from .parameter_database import ParameterDatabase
+
+
+def _db(precision: str) -> ParameterDatabase:
+    db = ParameterDatabase.solve_path_database()
+    db["solver_type"] = "iterative"
+    db["iterative_solver_type"] = "fgmres"
+    db["preconditioner"] = "multigrid"
+    db["residual_tolerance"] = 0.0
+    db["residual_reduction"] = 1e-8
+    db["max_n_iterations"] = 500
+    db["gmres_restart"] = 30
+    db["multigrid_n_levels"] = 4
+    db["multigrid_smoother"] = "jacobi"
+    db["multigrid_smoother_coarse"] = "direct_solve"
+    db["jacobi_damp"] = 0.8
+    db["multigrid_n_pre_smooth"] = 2
+    db["multigrid_n_post_smooth"] = 2
+    db["gpu_precision"] = precision
+    return db
+
+
+def problem(ctx, precision="mixed", n_levels=4):
+    disc = m.Discretization(m.GEO_CUBE_HEXA, 1, 5, n_levels, m.KIND_CD, 2)
+    cf = m.cd_coeffs(1e-2, (1.0, 0.5, 0.25), 0.0, True)
+    return disc, m.ConvectionDiffusion(ctx, disc, cf, _db(precision), quad_points=3)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["request", "spmv", "assembly"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    args = ap.parse_args()
+    ctx = m.Context(0)
+    disc, prob = problem(ctx, args.precision)
+    if args.case == "request":
+        for _ in range(2):
+            prob.reset_solution()
+            prob.assemble()
+            prob.solve()
+        print("request", args.precision, "iterations", prob.last_info()[0])
+    elif args.case == "assembly":
+        prob.assemble()
+        ctx.synchronize()
+        print("assembly of 4 levels")
+    else:
+        prob.assemble()
+        A = prob.matrix(-1)
+        A.make_fp32()
+        n = A.n_rows
+        x = m.DeviceVector.from_numpy(ctx, np.random.default_rng(0).standard_normal(n))
+        y = m.DeviceVector(ctx, n)
+        x32 = m.DeviceVector.from_numpy(ctx, np.random.default_rng(0).standard_normal(n).astype(np.float32))
+        y32 = m.DeviceVector(ctx, n, np.float32)
+        ms, b = A.bench_apply(x, y, 2)
+        ms32, b32 = A.bench_apply(x32, y32, 2, fp32=True)
+        print(f"spmv fp64 {b / ms / 1e6:.0f} GB/s, fp32 {b32 / ms32 / 1e6:.0f} GB/s (2 launches each)")
+    prob.close()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
