@@ -569,13 +569,15 @@ __global__ void k_coarse_rhs(int na, const int* __restrict__ act, const int* __r
 // x_a = inv * tmp (one warp per row), x_n = b_n
 __global__ void k_coarse_gemv(int n, int na, const int* __restrict__ act, const int* __restrict__ pos,
                               const double* __restrict__ inv, const double* __restrict__ tmp,
-                              const double* __restrict__ b, double* __restrict__ x) {
+                              const double* __restrict__ b, double* __restrict__ x,
+                              const int* __restrict__ gather) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp < na) {
     const double* row = inv + (size_t)warp * na;
     double s = 0.0;
-    for (int j = lane; j < na; j += 32) s += row[j] * tmp[j];
+    // gather != null: the right-hand side's non-actives are zero, read b directly
+    for (int j = lane; j < na; j += 32) s += row[j] * (gather ? b[gather[j]] : tmp[j]);
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if (lane == 0) x[act[warp]] = s;
   } else {
@@ -585,15 +587,16 @@ __global__ void k_coarse_gemv(int n, int na, const int* __restrict__ act, const 
   }
 }
 
-void DenseInverse::solve(pm_ctx* c, const DevCsr& A, const double* b, double* x) {
-  if (na > 0) {
+void DenseInverse::solve(pm_ctx* c, const DevCsr& A, const double* b, double* x, bool rhs_nonactive_zero) {
+  if (na > 0 && !rhs_nonactive_zero) {
     k_coarse_rhs<<<nblocks(na, 128), 128, 0, c->stream>>>(na, act.p, pos.p, A.row_ptr.p, A.cols.p,
                                                           A.vals.p, b, tmp.p);
     PM_CHECK_LAUNCH();
     c->kernel_launches++;
   }
   const long long threads = (long long)(na + (n + 31) / 32) * 32;
-  k_coarse_gemv<<<nblocks(threads, 256), 256, 0, c->stream>>>(n, na, act.p, pos.p, inv.p, tmp.p, b, x);
+  k_coarse_gemv<<<nblocks(threads, 256), 256, 0, c->stream>>>(n, na, act.p, pos.p, inv.p, tmp.p, b, x,
+                                                              rhs_nonactive_zero ? act.p : nullptr);
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
 }

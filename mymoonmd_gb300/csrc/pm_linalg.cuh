@@ -77,8 +77,10 @@ struct DenseInverse {
   DBuf<int> perm;    // pivot rows (na)
   DBuf<int> flag;    // singular pivot flag
   void build(pm_ctx* c, const DevCsr& A);
-  // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active)
-  void solve(pm_ctx* c, const DevCsr& A, const double* b, double* x);
+  // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active);
+  // rhs_nonactive_zero skips the b_n correction (the multigrid coarse rhs has
+  // its non-actives reset to zero)
+  void solve(pm_ctx* c, const DevCsr& A, const double* b, double* x, bool rhs_nonactive_zero = false);
 };
 
 }  // namespace pm

@@ -172,11 +172,13 @@ void Multigrid::coarse_solve(pm_ctx* c) {
   MGLevel& lv = levels[0];
   const DevCsr& A = lv.A->csr;
   if (mixed) {
+    // the coarse rhs comes from the restriction with its non-actives reset
     vcvt_f2d(c, A.n_rows, lv.rhs32.p, lv.coarse_rhs64.p);
-    lv.coarse.solve(c, A, lv.coarse_rhs64.p, lv.coarse_sol64.p);
+    lv.coarse.solve(c, A, lv.coarse_rhs64.p, lv.coarse_sol64.p, true);
     vcvt_d2f(c, A.n_rows, lv.coarse_sol64.p, lv.cur32);
   } else {
-    lv.coarse.solve(c, A, lv.rhs.p, lv.cur);
+    // the coarse rhs comes from the restriction with its non-actives reset
+    lv.coarse.solve(c, A, lv.rhs.p, lv.cur, true);
   }
 }
 
@@ -345,6 +347,59 @@ __global__ void __launch_bounds__(256) k_fg_start(int n, int m, const double* __
     v0[idx] = r[idx] * sc;
 }
 
+// Classical Gram-Schmidt with one re-orthogonalisation (CGS2), the batched
+// alternative to the modified Gram-Schmidt loop: the i+1 projections of one
+// pass are computed in one sweep over the vectors and subtracted in another.
+// Partial sums: part[k * kRedBlocks + block], CH accumulators per sweep.
+template <int CH>
+__global__ void __launch_bounds__(256) k_multidot(int n, int nk, const double* __restrict__ r,
+                                                  const double* __restrict__ V, size_t ld,
+                                                  double* __restrict__ part) {
+  __shared__ double sh[256];
+  for (int k0 = 0; k0 < nk; k0 += CH) {
+    double acc[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) acc[u] = 0.0;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+      const double ri = r[idx];
+#pragma unroll
+      for (int u = 0; u < CH; ++u)
+        if (k0 + u < nk) acc[u] += ri * V[(size_t)(k0 + u) * ld + idx];
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u)
+      if (k0 + u < nk) block_partial(acc[u], sh, part + (size_t)(k0 + u) * kRedBlocks);
+  }
+}
+
+// h[k] = sum of the partials of projection k (one block per k); with hsum,
+// also H(k, col) = hsum[k] + h[k]
+__global__ void __launch_bounds__(256) k_reduce_proj(const double* __restrict__ part, double* __restrict__ h,
+                                                     const double* __restrict__ hsum, double* __restrict__ H,
+                                                     int ldh, int col) {
+  __shared__ double sh[256];
+  const int k = blockIdx.x;
+  const double s = sum_partials(part + (size_t)k * kRedBlocks, sh);
+  if (threadIdx.x == 0) {
+    h[k] = s;
+    if (hsum) H[k + (size_t)ldh * col] = hsum[k] + s;
+  }
+}
+
+// r -= sum_k h[k] V_k, subtracted in k order
+__global__ void __launch_bounds__(256) k_cgs_update(int n, int nk, double* __restrict__ r,
+                                                    const double* __restrict__ V, size_t ld,
+                                                    const double* __restrict__ h) {
+  __shared__ double hs[64];
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) hs[k] = h[k];
+  __syncthreads();
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    double ri = r[idx];
+    for (int k = 0; k < nk; ++k) ri -= hs[k] * V[(size_t)k * ld + idx];
+    r[idx] = ri;
+  }
+}
+
 __device__ void gen_rot(double dx, double dy, double& cs, double& sn) {
   // GeneratePlaneRotation (src/Solver/Iteration_gmres.C:123)
   if (dy == 0.0) {
@@ -502,7 +557,7 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   double* V = work.p + work_n;                     // m+1 vectors
   double* Z = work.p + work_n * size_t(m + 2);     // m vectors
   const size_t ld = work_n;
-  const size_t gm_need = size_t(ldh) * m + 4 * size_t(m + 1) + 8;
+  const size_t gm_need = size_t(ldh) * m + 4 * size_t(m + 1) + 8 + 64 * size_t(kRedBlocks) + 128;
   if (gm.n != gm_need) {
     drop_graphs();
     gm.alloc(gm_need);
@@ -513,6 +568,9 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   double* sn = cs + (m + 1);
   double* y = sn + (m + 1);
   double* dres = y + (m + 1);
+  double* cgs_part = dres + 8;                 // 64 x kRedBlocks partial sums
+  double* h1 = cgs_part + 64 * size_t(kRedBlocks);
+  double* h2 = h1 + 64;
   if (!flags.p) {
     drop_graphs();
     flags.alloc(1);
@@ -538,6 +596,7 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   if (converged(resid, 0)) return;
 
   const int grid = kRedBlocks;
+  const bool cgs2 = gram_schmidt == "cgs2";
   unsigned j = 1;
   while (j <= (unsigned long)max_it) {
     // v_0 = r / beta, s = (beta, 0, ...)   (partA holds <r,r>)
@@ -554,15 +613,31 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
         double* zi = Z + ld * i;
         precondition(vi, zi);
         csr_apply(c, M, EPI_SET, zi, r, nullptr, 1.0);  // r = A z_i
-        dot_partials(c, n, r, V, partA);                   // <r, v_0>
         double* pin = partA;
-        double* pout = partB;
-        for (int k = 0; k <= i; ++k) {
-          const double* next = (k < i) ? V + ld * (k + 1) : r;
-          k_fg_mgs<<<grid, 256, 0, c->stream>>>(n, ldh, k, i, r, V + ld * k, next, pin, pout, H);
+        if (cgs2) {
+          // two passes of classical Gram-Schmidt; H(:,i) = h1 + h2
+          const int nk = i + 1;
+          const int ub = grid_blocks_for(n);
+          k_multidot<8><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
+          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i);
+          k_cgs_update<<<ub, 256, 0, c->stream>>>(n, nk, r, V, ld, h1);
+          k_multidot<8><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
+          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h2, h1, H, ldh, i);
+          k_cgs_update<<<ub, 256, 0, c->stream>>>(n, nk, r, V, ld, h2);
           PM_CHECK_LAUNCH();
-          c->kernel_launches++;
-          std::swap(pin, pout);
+          c->kernel_launches += 6;
+          dot_partials(c, n, r, r, partA);
+        } else {
+          // modified Gram-Schmidt in the reference's order (Iteration_gmres.C:452-461)
+          dot_partials(c, n, r, V, partA);                   // <r, v_0>
+          double* pout = partB;
+          for (int k = 0; k <= i; ++k) {
+            const double* next = (k < i) ? V + ld * (k + 1) : r;
+            k_fg_mgs<<<grid, 256, 0, c->stream>>>(n, ldh, k, i, r, V + ld * k, next, pin, pout, H);
+            PM_CHECK_LAUNCH();
+            c->kernel_launches++;
+            std::swap(pin, pout);
+          }
         }
         k_fg_normalize<<<grid, 256, 0, c->stream>>>(n, ldh, i, r, V + ld * (i + 1), pin, H, flags.p);
         PM_CHECK_LAUNCH();

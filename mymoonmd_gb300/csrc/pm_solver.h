@@ -81,6 +81,9 @@ struct pm_solver {
   double tol = 1e-8, reduction = 0.0, divergence = 1e10, stagnation = 1e10, damping = 1.0;
   long max_it = 100, min_it = 0, restart = 20;
   bool mixed = false;
+  // Arnoldi orthogonalisation: "mgs" (the reference's modified Gram-Schmidt)
+  // or "cgs2" (classical Gram-Schmidt, two passes, batched; FP64 as well)
+  std::string gram_schmidt = "mgs";
   pm_matrix* A = nullptr;
   pm::Multigrid mg;
   bool use_mg = false;

@@ -162,6 +162,20 @@ def test_fgmres_multigrid_solution_matches_oracle(ctx, case):
     assert res < 1e-10 * init
 
 
+def test_cgs2_orthogonalisation_matches_mgs_oracle(ctx):
+    """FP64 FGMRES with batched classical Gram-Schmidt (two passes) against the
+    oracle's modified Gram-Schmidt: same solution within 1e-10, iterations within one"""
+    db = mg_db(3)
+    db.add("gpu_gram_schmidt", "cgs2")
+    disc, prob, ora = make_pair(ctx, "q2_3d", db)
+    prob.solve()
+    it, res, init = prob.last_info()
+    ora.build_mg(2, 2, 0.8, 1.0, "V")
+    sol, oit, ores, hist, st = ora.solve("fgmres", 0.0, 1e-10, 200, 0, 20)
+    assert abs(it - oit) <= 1, (it, oit)
+    assert rel(prob.solution(), sol) <= 1e-10
+
+
 def test_w_cycle_and_restart_match_oracle(ctx):
     db = mg_db(3, restart=3, cycle="W")
     disc, prob, ora = make_pair(ctx, "q1_2d", db)
