@@ -297,12 +297,12 @@ int pm_matrix_apply_f32(pm_matrix* A, const float* x, float* y) {
 
 int pm_matrix_set_kernel(pm_matrix* A, int lanes, int unroll) {
   if (!A) return PM_E_INVALID;
-  if (lanes && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
-    return fail(A->ctx, PM_E_INVALID, "lanes per row must be 4, 8, 16 or 32");
-  if (unroll && unroll != 2 && unroll != 4 && unroll != 8)
-    return fail(A->ctx, PM_E_INVALID, "entries per lane must be 2, 4 or 8");
-  if (lanes) A->csr.lanes = lanes;
-  if (unroll) A->csr.unroll = unroll;
+  if (lanes && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+    return fail(A->ctx, PM_E_INVALID, "lanes per row must be 1, 2, 4, 8, 16 or 32");
+  if (unroll && unroll != 2 && unroll != 4 && unroll != 8 && unroll != 16)
+    return fail(A->ctx, PM_E_INVALID, "entries per lane must be 2, 4, 8 or 16");
+  if (lanes) A->csr.lanes = A->csr.lanes32 = lanes;
+  if (unroll) A->csr.unroll = A->csr.unroll32 = unroll;
   // an explicit group shape selects the per-row-group kernel; (0, 0) goes back
   // to the row-block streaming kernel
   A->csr.stream = (lanes == 0 && unroll == 0);

@@ -11,8 +11,10 @@ namespace pm {
 struct DevCsr {
   int n_rows = 0, n_cols = 0, n_active = 0;
   int64_t nnz = 0;
-  int lanes = 8;   // lanes per row in the SpMV kernels
-  int unroll = 4;  // entries per lane per chunk
+  int lanes = 8;   // lanes per row in the SpMV kernels (FP64 values)
+  int unroll = 4;  // entries per lane per chunk (FP64 values)
+  int lanes32 = 8;   // the same for the FP32 copy of the values
+  int unroll32 = 16;
   // row blocks of the streaming kernel (consecutive rows with at most
   // kStreamNnz entries); empty when a row is longer than that
   DBuf<int> rblock;
