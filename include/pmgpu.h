@@ -234,6 +234,15 @@ int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coeffs* coeffs,
 int pm_problem_create_cd(pm_ctx* ctx, const pm_disc* d, const pm_cd_coeffs* coeffs,
                          int quad_points, const char* params, pm_problem** out);
 void pm_problem_destroy(pm_problem* p);
+/* NavierStokes<3> with FLOW_PROBLEM_TYPE Stokes (src/System/NavierStokes.C:407,
+ * 878) on a Stokes discretisation (P2/P1 on tetrahedra): -nu Lap u + grad p =
+ * f, div u = 0, no-slip walls, f from the manufactured velocity
+ * u = curl(psi (1,1,1)), psi = (sin pi x sin pi y sin pi z)^2, and pressure
+ * p = x + y + z - 3/2. Vector layout [u1 | u2 | u3 | p]. The multigrid levels
+ * get the projected combined matrices and cell-Vanka data
+ * (multigrid_smoother cell_vanka | cell_vanka_jacobi, VankaSmoother.C). */
+int pm_problem_create_stokes(pm_ctx* ctx, const pm_disc* d, double nu, const char* params,
+                             pm_problem** out);
 /* ConvectionDiffusion::assemble (src/System/ConvectionDiffusion.C:174) */
 int pm_problem_assemble(pm_problem* p);
 /* ConvectionDiffusion::solve (src/System/ConvectionDiffusion.C:191). Like the

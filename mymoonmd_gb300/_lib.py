@@ -113,6 +113,7 @@ _SIGS = {
     "pm_assemble_cd_noalloc": (i32, [vp, i32, C.POINTER(CdCoeffs), vp, vp]),
     "pm_problem_create_cd": (i32, [vp, vp, C.POINTER(CdCoeffs), i32, C.c_char_p, C.POINTER(vp)]),
     "pm_problem_destroy": (None, [vp]),
+    "pm_problem_create_stokes": (i32, [vp, vp, f64, C.c_char_p, C.POINTER(vp)]),
     "pm_problem_assemble": (i32, [vp]),
     "pm_problem_solve": (i32, [vp]),
     "pm_problem_reset_solution": (i32, [vp]),

@@ -505,6 +505,27 @@ class ConvectionDiffusion:
             pass
 
 
-__all__ = ["Context", "DeviceVector", "FEMatrix", "Solver", "Discretization", "ConvectionDiffusion",
+class StokesProblem(ConvectionDiffusion):
+    """NavierStokes<3> for the Stokes problem (P2/P1 on tetrahedra) on one GPU:
+    assemble() and solve() as NavierStokes::assemble_linear_terms / solve
+    (src/System/NavierStokes.C:407, 878). Vector layout [u1 | u2 | u3 | p]."""
+
+    def __init__(self, ctx: Context, disc: Discretization, nu: float, db):
+        self.ctx = ctx
+        self.disc = disc
+        self.nu = nu
+        h = C.c_void_p()
+        check(lib.pm_problem_create_stokes(ctx.handle, disc.handle, nu, _db_text(db).encode(), C.byref(h)),
+              ctx.handle)
+        self.handle = h
+
+    def blocks(self) -> tuple[int, int, int]:
+        """(velocity DOFs per component, active velocity DOFs, pressure DOFs)"""
+        lv = self.disc.n_levels - 1
+        v, p = self.disc.level_info(lv, 0), self.disc.level_info(lv, 1)
+        return v["n_dofs"], v["n_active"], p["n_dofs"]
+
+
+__all__ = ["Context", "StokesProblem", "DeviceVector", "FEMatrix", "Solver", "Discretization", "ConvectionDiffusion",
            "ParameterDatabase", "PmError", "cd_coeffs", "assemble_cd", "GEO_SQUARE_QUAD", "GEO_CUBE_HEXA",
            "GEO_CUBE_TETRA", "KIND_CD", "KIND_STOKES"]

@@ -708,12 +708,95 @@ int pm_problem_create_cd(pm_ctx* c, const pm_disc* d, const pm_cd_coeffs* cf, in
 
 void pm_problem_destroy(pm_problem* p) { delete p; }
 
+int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char* params, pm_problem** out) {
+  if (!c || !d || !out) return fail(c, PM_E_INVALID, "null argument");
+  PM_TRY
+  if (d->d->kind != KIND_STOKES) throw Error(PM_E_INVALID, "the discretisation is not a Stokes set-up");
+  auto* p = new pm_problem();
+  try {
+    p->ctx = c;
+    p->disc = d;
+    p->kind = KIND_STOKES;
+    p->nu = nu;
+    const Disc& D = *d->d;
+    const int nl = int(D.levels.size());
+    p->stab.upload(c);
+    size_t kmax = 0, fmax = 0;
+    p->slev.resize(nl);
+    for (int l = 0; l < nl; ++l) {
+      const DiscLevel& L = D.levels[l];
+      pm_matrix* A = new pm_matrix();
+      A->ctx = c;
+      A->owned_by_problem = true;
+      p->mats.push_back(A);
+      A->csr.upload(c, L.sys.n_rows, L.sys.n_cols, L.sys.n_active, L.sys.row_ptr.data(), L.sys.cols.data(),
+                    nullptr);
+      A->csr.set_blocks(L.n_blocks, L.block_len, L.block_active);
+      p->slev[l].upload(c, L);
+      auto pr = std::make_unique<ProjectedMatrix>();
+      pr->build(c, L.sys, L.pressure_row0, A->csr.mask);
+      p->proj.push_back(std::move(pr));
+      auto vk = std::make_unique<DevVanka>();
+      vk->setup(c, L);
+      p->vanka.push_back(std::move(vk));
+      kmax = std::max(kmax, size_t(L.n_cells) * L.elem_stride);
+      fmax = std::max(fmax, size_t(L.n_cells) * L.rhs_stride);
+    }
+    p->K.alloc(kmax);
+    p->F.alloc(fmax);
+    const int n = D.levels.back().sys.n_rows;
+    p->rhs.alloc(n);
+    p->sol.alloc(n);
+    p->rhs_coarse.alloc(n);
+    PM_CUDA(cudaMemsetAsync(p->sol.p, 0, sizeof(double) * n, c->stream));
+    std::string text = params ? params : "";
+    Params prm = Params::parse(text.c_str());
+    if (prm.str("preconditioner", "") == "multigrid" && !prm.has("multigrid_n_levels"))
+      text += "\nmultigrid_n_levels: " + std::to_string(nl) + "\n";
+    int rc = pm_solver_create(c, text.c_str(), &p->solver);
+    if (rc != PM_OK) throw Error(rc, c->last_error);
+    if (p->solver->use_mg) {
+      const int ml = int(p->solver->mg.levels.size());
+      if (ml > nl) throw Error(PM_E_INVALID, "more multigrid levels requested than the discretisation keeps");
+      for (int l = 0; l < ml; ++l) {
+        const int dl = nl - ml + l;
+        const DiscLevel& L = D.levels[dl];
+        if (l < ml - 1)
+          rc = pm_solver_set_multigrid_level(p->solver, l, ml, p->mats[dl], L.P.n_rows, L.P.n_cols,
+                                             L.P.row_ptr.data(), L.P.cols.data(), L.P.vals.data());
+        else
+          rc = pm_solver_set_multigrid_level(p->solver, l, ml, p->mats[dl], 0, 0, nullptr, nullptr, nullptr);
+        if (rc != PM_OK) throw Error(rc, c->last_error);
+        p->solver->mg.levels[l].proj = p->proj[dl].get();
+        p->solver->mg.levels[l].vanka = p->vanka[dl].get();
+      }
+    }
+  } catch (...) {
+    delete p;
+    throw;
+  }
+  *out = p;
+  return PM_OK;
+  PM_CATCH(c)
+}
+
 int pm_problem_assemble(pm_problem* p) {
   if (!p) return PM_E_INVALID;
   PM_TRY
   pm_ctx* c = p->ctx;
   const Disc& D = *p->disc->d;
   const int nl = int(D.levels.size());
+  if (p->kind == KIND_STOKES) {
+    // NavierStokes<3>::assemble_linear_terms for the Stokes problem
+    for (int l = 0; l < nl; ++l) {
+      double* r = (l == nl - 1) ? p->rhs.p : p->rhs_coarse.p;
+      assemble_stokes_level(c, p->slev[l], p->stab, p->nu, p->mats[l]->csr, r, p->K.p, p->F.p);
+    }
+    const DevCsr& top = p->mats.back()->csr;
+    copy_nonactive(c, top.n_rows, top.mask, p->rhs.p, p->sol.p);
+    p->solver_ready = false;
+    return PM_OK;
+  }
   for (int l = 0; l < nl; ++l) {
     double* r = (l == nl - 1) ? p->rhs.p : p->rhs_coarse.p;
     assemble_cd_level(c, p->alev[l], D.dim(), D.elem, p->qn, p->coeffs, p->ref, p->mats[l]->csr, r,
@@ -804,10 +887,11 @@ int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* cf, const double* con
   pm_ctx* c = p->ctx;
   if (cf) p->coeffs = *cf;
   if (level_verts)
-    for (size_t l = 0; l < p->alev.size(); ++l)
+    for (size_t l = 0; l < p->mats.size(); ++l) {
+      DBuf<double>& verts = p->kind == KIND_STOKES ? p->slev[l].verts : p->alev[l].verts;
       if (level_verts[l])
-        PM_CUDA(cudaMemcpyAsync(p->alev[l].verts.p, level_verts[l], p->alev[l].verts.bytes(),
-                                cudaMemcpyHostToDevice, c->stream));
+        PM_CUDA(cudaMemcpyAsync(verts.p, level_verts[l], verts.bytes(), cudaMemcpyHostToDevice, c->stream));
+    }
   // a new request starts from the zero initial guess
   PM_CUDA(cudaMemsetAsync(p->sol.p, 0, p->sol.bytes(), c->stream));
   int rc = pm_problem_assemble(p);

@@ -60,6 +60,187 @@ static void build_gather(DiscLevel& L, int nloc, const std::vector<int>& gdof,
     if (!row_active[i]) L.diag_pos.push_back(find(i, i));
 }
 
+// --------------------------------------------------------------- Stokes ----
+// Combined local DOF m of a P2/P1 cell: 0..29 velocity (component m/10, local
+// m%10), 30..33 pressure. Block (bm, bk) is non-zero for the diagonal A
+// blocks, B^T (velocity rows, pressure columns) and B (pressure rows, velocity
+// columns) - the NSTYPE 4 Stokes blocks with the Laplace form
+// (src/Matrix/BlockFEMatrix.C:616-664, NSE_local_assembling_routines.C:82-225).
+static inline int stokes_block(int m) { return m < 30 ? m / 10 : 3; }
+static inline bool stokes_nonzero(int m, int k) {
+  const int bm = stokes_block(m), bk = stokes_block(k);
+  if (bm < 3 && bk < 3) return bm == bk;
+  return !(bm == 3 && bk == 3);
+}
+// element storage of a cell: A (10x10) then B_0, B_1, B_2 (4x10 each)
+static inline int stokes_pos(int c, int m, int k) {
+  const int bm = stokes_block(m), bk = stokes_block(k);
+  const size_t base = size_t(c) * 220;
+  if (bm < 3 && bk < 3) return bm == bk ? int(base + (m % 10) * 10 + (k % 10)) : -1;
+  if (bm < 3) return int(base + 100 + bm * 40 + (k - 30) * 10 + (m % 10));  // B^T = B transposed
+  if (bk < 3) return int(base + 100 + bk * 40 + (m - 30) * 10 + (k % 10));
+  return -1;
+}
+
+static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L) {
+  L.space = build_space(h, lvl, EL_P2, BND_DIRICHLET);
+  L.pspace = build_space(h, lvl, EL_P1, BND_NEUMANN);
+  const int nu = L.space.n_dofs, np = L.pspace.n_dofs, nau = L.space.n_active;
+  const int N = 3 * nu + np, nc = L.n_cells;
+  L.cdof.resize(size_t(nc) * 34);
+  for (int c = 0; c < nc; ++c)
+    for (int m = 0; m < 34; ++m)
+      L.cdof[size_t(c) * 34 + m] = m < 30 ? (m / 10) * nu + L.space.dofmap[size_t(c) * 10 + m % 10]
+                                          : 3 * nu + L.pspace.dofmap[size_t(c) * 4 + (m - 30)];
+  std::vector<char> act(N, 1);
+  for (int b = 0; b < 3; ++b)
+    for (int i = nau; i < nu; ++i) act[size_t(b) * nu + i] = 0;
+  // incidence: combined DOF -> (cell, local index), cells in order
+  std::vector<int> iptr(N + 1, 0), inc;
+  for (size_t t = 0; t < L.cdof.size(); ++t) iptr[L.cdof[t] + 1]++;
+  for (int i = 0; i < N; ++i) iptr[i + 1] += iptr[i];
+  inc.resize(iptr[N]);
+  {
+    std::vector<int> fill(iptr.begin(), iptr.end() - 1);
+    for (size_t t = 0; t < L.cdof.size(); ++t) inc[fill[L.cdof[t]]++] = int(t);
+  }
+  // combined pattern
+  Csr& A = L.sys;
+  A = Csr();
+  A.n_rows = A.n_cols = N;
+  A.n_active = 3 * nau + np;
+  A.row_ptr.assign(N + 1, 0);
+  std::vector<int> marker(N, -1), row;
+  for (int i = 0; i < N; ++i) {
+    row.clear();
+    if (act[i]) {
+      for (int e = iptr[i]; e < iptr[i + 1]; ++e) {
+        const int c = inc[e] / 34, m = inc[e] % 34;
+        for (int k = 0; k < 34; ++k) {
+          if (!stokes_nonzero(m, k)) continue;
+          const int j = L.cdof[size_t(c) * 34 + k];
+          if (marker[j] != i) {
+            marker[j] = i;
+            row.push_back(j);
+          }
+        }
+      }
+      std::sort(row.begin(), row.end());
+    } else {
+      row.push_back(i);
+    }
+    A.cols.insert(A.cols.end(), row.begin(), row.end());
+    A.row_ptr[i + 1] = int(A.cols.size());
+  }
+  A.vals.assign(A.cols.size(), 0.0);
+  // gather plans into the compact element storage
+  const int nnz = A.row_ptr[N];
+  auto find = [&](int r, int col) {
+    const int* b = A.cols.data() + A.row_ptr[r];
+    const int* e = A.cols.data() + A.row_ptr[r + 1];
+    const int* it = std::lower_bound(b, e, col);
+    if (it == e || *it != col) throw std::logic_error("Stokes element entry outside the pattern");
+    return int(it - A.cols.data());
+  };
+  std::vector<int> cnt(size_t(nnz) + 1, 0);
+  std::vector<std::pair<int, int>> contrib;  // (entry, element storage position), cell order
+  contrib.reserve(size_t(nc) * 34 * 14);
+  for (int c = 0; c < nc; ++c)
+    for (int m = 0; m < 34; ++m) {
+      const int r = L.cdof[size_t(c) * 34 + m];
+      if (!act[r]) continue;
+      for (int k = 0; k < 34; ++k) {
+        const int p = stokes_pos(c, m, k);
+        if (p < 0) continue;
+        const int e = find(r, L.cdof[size_t(c) * 34 + k]);
+        contrib.push_back({e, p});
+        cnt[e + 1]++;
+      }
+    }
+  for (int e = 0; e < nnz; ++e) cnt[e + 1] += cnt[e];
+  L.gat_ptr = cnt;
+  L.gat_idx.assign(cnt[nnz], 0);
+  {
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (auto& pr : contrib) L.gat_idx[fill[pr.first]++] = pr.second;
+  }
+  L.rgat_ptr.assign(N + 1, 0);
+  for (size_t t = 0; t < L.cdof.size(); ++t)
+    if (act[L.cdof[t]]) L.rgat_ptr[L.cdof[t] + 1]++;
+  for (int i = 0; i < N; ++i) L.rgat_ptr[i + 1] += L.rgat_ptr[i];
+  L.rgat_idx.assign(L.rgat_ptr[N], 0);
+  {
+    std::vector<int> fill(L.rgat_ptr.begin(), L.rgat_ptr.end() - 1);
+    for (size_t t = 0; t < L.cdof.size(); ++t)
+      if (act[L.cdof[t]]) L.rgat_idx[fill[L.cdof[t]]++] = int(t);  // rhs storage: cell*34 + m
+  }
+  L.diag_pos.clear();
+  for (int i = 0; i < N; ++i)
+    if (!act[i]) L.diag_pos.push_back(find(i, i));
+  L.elem_stride = 220;
+  L.rhs_stride = 34;
+  L.n_blocks = 4;
+  for (int b = 0; b < 3; ++b) {
+    L.block_len[b] = nu;
+    L.block_active[b] = nau;
+  }
+  L.block_len[3] = np;
+  L.block_active[3] = np;
+  L.pressure_row0 = 3 * nu;
+  // Vanka patches (sorted combined DOFs of each cell) and a greedy colouring
+  L.patch_dofs = L.cdof;
+  for (int c = 0; c < nc; ++c) std::sort(L.patch_dofs.begin() + size_t(c) * 34, L.patch_dofs.begin() + size_t(c + 1) * 34);
+  std::vector<int> color(nc, -1), seen;
+  int n_colors = 0;
+  for (int c = 0; c < nc; ++c) {
+    seen.assign(n_colors + 1, 0);
+    for (int m = 0; m < 34; ++m) {
+      const int d = L.cdof[size_t(c) * 34 + m];
+      for (int e = iptr[d]; e < iptr[d + 1]; ++e) {
+        const int oc = inc[e] / 34;
+        if (oc < c && color[oc] >= 0) seen[color[oc]] = 1;
+      }
+    }
+    int col = 0;
+    while (col < n_colors && seen[col]) ++col;
+    color[c] = col;
+    if (col == n_colors) ++n_colors;
+  }
+  L.color_ptr.assign(n_colors + 1, 0);
+  for (int c = 0; c < nc; ++c) L.color_ptr[color[c] + 1]++;
+  for (int k = 0; k < n_colors; ++k) L.color_ptr[k + 1] += L.color_ptr[k];
+  L.color_cells.assign(nc, 0);
+  {
+    std::vector<int> fill(L.color_ptr.begin(), L.color_ptr.end() - 1);
+    for (int c = 0; c < nc; ++c) L.color_cells[fill[color[c]]++] = c;
+  }
+}
+
+// block-diagonal prolongation of the combined vector between two Stokes levels
+static void build_stokes_transfer(const Hierarchy& h, DiscLevel& Lc, const DiscLevel& Lf) {
+  Csr Pu, Ru, Pp, Rp;
+  build_transfer(h, Lf.level_in_hierarchy, Lc.space, Lf.space, Pu, Ru);
+  build_transfer(h, Lf.level_in_hierarchy, Lc.pspace, Lf.pspace, Pp, Rp);
+  const int nuf = Lf.space.n_dofs, npf = Lf.pspace.n_dofs, nuc = Lc.space.n_dofs, npc = Lc.pspace.n_dofs;
+  Csr& P = Lc.P;
+  P = Csr();
+  P.n_rows = 3 * nuf + npf;
+  P.n_cols = 3 * nuc + npc;
+  P.n_active = 3 * Lf.space.n_active + npf;
+  P.row_ptr.assign(P.n_rows + 1, 0);
+  for (int b = 0; b < 4; ++b) {
+    const Csr& S = b < 3 ? Pu : Pp;
+    const int roff = b < 3 ? b * nuf : 3 * nuf, coff = b < 3 ? b * nuc : 3 * nuc;
+    for (int i = 0; i < S.n_rows; ++i) {
+      for (int k = S.row_ptr[i]; k < S.row_ptr[i + 1]; ++k) {
+        P.cols.push_back(coff + S.cols[k]);
+        P.vals.push_back(S.vals[k]);
+      }
+      P.row_ptr[roff + i + 1] = int(P.cols.size());
+    }
+  }
+}
+
 std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem) {
   if (n_levels < 1 || n_levels > n_refine + 1)
     throw std::invalid_argument("multigrid levels must be between 1 and refinements + 1");
@@ -74,7 +255,20 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
     if (geometry == GEO_CUBE_TETRA) throw std::invalid_argument("convection-diffusion uses quadrilaterals or hexahedra");
     if (elem != EL_Q1 && elem != EL_Q2) throw std::invalid_argument("convection-diffusion elements are Q1 or Q2");
   } else {
-    throw std::invalid_argument("Stokes set-up is not available in this build");
+    if (geometry != GEO_CUBE_TETRA) throw std::invalid_argument("Stokes P2/P1 uses the tetrahedral unit cube");
+    D->elem = EL_P2;
+    D->h = build_hierarchy(geometry, root_n, n_refine);
+    const int first = n_refine + 1 - n_levels;
+    D->levels.resize(n_levels);
+    for (int l = 0; l < n_levels; ++l) {
+      DiscLevel& L = D->levels[l];
+      L.level_in_hierarchy = first + l;
+      L.n_cells = D->h.levels[first + l].n_cells;
+      L.verts = cell_vertices(D->h, first + l);
+      build_stokes_level(D->h, first + l, L);
+    }
+    for (int l = 0; l + 1 < n_levels; ++l) build_stokes_transfer(D->h, D->levels[l], D->levels[l + 1]);
+    return D;
   }
   D->h = build_hierarchy(geometry, root_n, n_refine);
   const int first = n_refine + 1 - n_levels;

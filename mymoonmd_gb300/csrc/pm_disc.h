@@ -32,6 +32,18 @@ struct DiscLevel {
   int n_blocks = 1;
   int block_len[4] = {0, 0, 0, 0};
   int block_active[4] = {0, 0, 0, 0};
+  // Stokes: combined local DOFs per cell (3 x 10 velocity + 4 pressure,
+  // global combined indices) and the element storage per cell (10x10 A block
+  // + 3 x 4x10 B blocks)
+  std::vector<int> cdof;  // n_cells * 34
+  int elem_stride = 0;    // doubles of element-matrix storage per cell
+  int rhs_stride = 0;     // doubles of element right-hand side per cell
+  // Vanka: per cell, its 34 combined DOFs sorted ascending (DofPatch order),
+  // and a colouring of the cells such that cells of one colour share no DOF
+  std::vector<int> patch_dofs;  // n_cells * 34
+  std::vector<int> color_ptr, color_cells;
+  // position of the first pressure row's diagonal in `sys` (pressure projection)
+  int pressure_row0 = -1;
 };
 
 struct Disc {

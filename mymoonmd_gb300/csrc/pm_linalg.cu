@@ -420,6 +420,14 @@ void vaxpby(pm_ctx* c, int n, double a, const double* x, double b, double* y) {
 void vdiv(pm_ctx* c, int n, const double* d, double* y) { PM_LAUNCH1D(k_div, n, n, d, y); }
 void vcvt_d2f(pm_ctx* c, int n, const double* x, float* y) { PM_LAUNCH1D(k_d2f, n, n, x, y); }
 void vcvt_f2d(pm_ctx* c, int n, const float* x, double* y) { PM_LAUNCH1D(k_f2d, n, n, x, y); }
+__global__ void k_copy_nonactive(int n, BlockMask m, const double* __restrict__ src, double* __restrict__ dst) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (!row_is_active(m, i)) dst[i] = src[i];
+}
+void copy_nonactive(pm_ctx* c, int n, const BlockMask& m, const double* src, double* dst) {
+  PM_LAUNCH1D(k_copy_nonactive, n, n, m, src, dst);
+}
+
 void init_solution(pm_ctx* c, int n, const BlockMask& m, const double* rhs, double* sol) {
   PM_LAUNCH1D(k_init_sol<double>, n, n, m, rhs, sol);
 }

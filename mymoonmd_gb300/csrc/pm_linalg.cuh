@@ -66,6 +66,8 @@ void vcopy32(pm_ctx* c, int n, const float* x, float* y);
 void init_solution(pm_ctx* c, int n, const BlockMask& m, const double* rhs, double* sol);
 void init_solution32(pm_ctx* c, int n, const BlockMask& m, const float* rhs, float* sol);
 void vdiv(pm_ctx* c, int n, const double* d, double* y);  // y /= d
+// BlockVector::copy_nonactive: dst := src on the non-active rows
+void copy_nonactive(pm_ctx* c, int n, const BlockMask& m, const double* src, double* dst);
 
 // dense inverse of the active block of a small CSR matrix (Gauss-Jordan with
 // partial pivoting on the device); used by the coarse-grid direct solve

@@ -1,16 +1,24 @@
 // The device-resident convection-diffusion system behind the pm_problem handle:
 // level matrices, assembly inputs, right-hand side, solution and solver.
 #pragma once
+#include <memory>
 #include <vector>
 
 #include "pm_assemble.h"
 #include "pm_solver.h"
+#include "pm_stokes.h"
 
 struct pm_problem {
   pm_ctx* ctx = nullptr;
   const pm_disc* disc = nullptr;
+  int kind = 0;  // 0 convection-diffusion, 1 Stokes
   pm_cd_coeffs coeffs{};
+  double nu = 1.0;  // Stokes viscosity
   int qn = 3;
+  std::vector<pm::DevStokesLevel> slev;
+  pm::DevStokesTables stab;
+  std::vector<std::unique_ptr<pm::ProjectedMatrix>> proj;
+  std::vector<std::unique_ptr<pm::DevVanka>> vanka;
   std::vector<pm_matrix*> mats;
   std::vector<pm::DevAssemblyLevel> alev;
   pm::DevRefTables ref;

@@ -92,6 +92,7 @@ void Multigrid::configure(const Params& p) {
   n_pre = int(p.integer("multigrid_n_pre_smooth", 1));
   n_post = int(p.integer("multigrid_n_post_smooth", 1));
   jacobi_damp = p.num("jacobi_damp", 1.0);
+  vanka_damp = p.num("multigrid_vanka_damp_factor", 1.0);
   correction_damp = p.num("multigrid_correction_damp_factor", 1.0);
   coarse_residual = p.num("multigrid_coarse_residual", 0.1);
   coarse_max_it = int(p.integer("multigrid_coarse_max_n_iterations", 10));
@@ -114,8 +115,12 @@ void Multigrid::update(pm_ctx* c) {
     MGLevel& lv = levels[l];
     DevCsr& A = lv.A->csr;
     lv.smoother = (l == 0) ? smoother_coarse : smoother;
-    if (lv.smoother == SM_CELL_VANKA || lv.smoother == SM_CELL_VANKA_JACOBI)
+    const bool vanka = lv.smoother == SM_CELL_VANKA || lv.smoother == SM_CELL_VANKA_JACOBI;
+    if (vanka && (!lv.vanka || !lv.proj))
       throw Error(PM_E_UNSUPPORTED, "Vanka smoothers need the Stokes problem set-up");
+    // get_combined_matrix of this level (values copied from the system matrix)
+    if (lv.proj) lv.proj->refresh(c, A, mixed);
+    if (vanka) lv.vanka->factor(c, lv.proj->csr, mixed);
     if (lv.smoother == SM_JACOBI) A.make_diag(c);
     const int n = A.n_rows;
     if (l < L - 1) {
@@ -142,7 +147,8 @@ void Multigrid::update(pm_ctx* c) {
     lv.alt.ensure(n);
     lv.defect.ensure(n);
     if (lv.smoother == SM_DIRECT) {
-      lv.coarse.build(c, A);
+      // DirectSolver factorises get_combined_matrix (with the pressure projection)
+      lv.coarse.build(c, lv.proj ? lv.proj->csr : A);
       if (mixed) {
         lv.coarse_rhs64.ensure(n);
         lv.coarse_sol64.ensure(n);
@@ -165,6 +171,13 @@ void Multigrid::smooth(pm_ctx* c, int l) {
     }
   } else if (lv.smoother == SM_DIRECT) {
     coarse_solve(c);
+  } else if (lv.smoother == SM_CELL_VANKA_JACOBI) {
+    // additive cell Vanka, in place; the level's defect buffer holds the residual
+    if (mixed) lv.vanka->sweep_jacobi32(c, lv.proj->csr, lv.rhs32.p, lv.cur32, lv.defect32.p, float(vanka_damp));
+    else lv.vanka->sweep_jacobi(c, lv.proj->csr, lv.rhs.p, lv.cur, lv.defect.p, vanka_damp);
+  } else if (lv.smoother == SM_CELL_VANKA) {
+    if (mixed) lv.vanka->sweep_colored32(c, lv.proj->csr, lv.rhs32.p, lv.cur32, float(vanka_damp));
+    else lv.vanka->sweep_colored(c, lv.proj->csr, lv.rhs.p, lv.cur, vanka_damp);
   }
 }
 

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "pm_linalg.cuh"
+#include "pm_stokes.h"
 
 struct pm_matrix {
   pm_ctx* ctx = nullptr;
@@ -43,6 +44,10 @@ struct MGLevel {
   int smoother = SM_JACOBI;
   DenseInverse coarse;
   DBuf<double> coarse_rhs64, coarse_sol64;
+  // saddle point levels: the projected combined matrix (Vanka, direct solve)
+  // and the cell Vanka data; owned by the problem
+  ProjectedMatrix* proj = nullptr;
+  DevVanka* vanka = nullptr;
 };
 
 // CycleControl (src/Multigrid/CycleControl.C:17-110)
@@ -52,7 +57,7 @@ struct Multigrid {
   std::vector<MGLevel> levels;  // 0 = coarsest
   std::vector<int> control;
   int n_pre = 1, n_post = 1;
-  double jacobi_damp = 1.0, correction_damp = 1.0, coarse_residual = 0.1;
+  double jacobi_damp = 1.0, correction_damp = 1.0, coarse_residual = 0.1, vanka_damp = 1.0;
   int coarse_max_it = 10;
   int smoother = SM_JACOBI, smoother_coarse = SM_DIRECT;
   std::string cycle_type = "V";

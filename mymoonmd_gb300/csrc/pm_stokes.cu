@@ -1,0 +1,540 @@
+// Stokes P2/P1 (Taylor-Hood) on tetrahedra: element assembly, projected
+// combined matrix and cell Vanka.
+//
+// Assembly restates NSLaplaceGradGrad, NSDivergenceBlocks and NSGradientBlocks
+// (src/AssembleRoutinesSaddle/NSE_local_assembling_routines.C:82-225) for the
+// Stokes Galerkin form with the Laplace operator on affine tetrahedra
+// (src/FE/TetraAffin.C:886) and the P4Tetra rule (P4Exact,
+// src/QuadFormulas/QuadFormulaTetra.C:73): per cell
+//   A_ij   =  nu sum_q w |det J| grad phi_i . grad phi_j   (same in A11,A22,A33)
+//   B_k,ij = -sum_q w |det J| psi_i d_k phi_j,   B^T_k = B_k transposed
+// computed as contractions of reference tensors over the same quadrature.
+// The projected matrix is get_combined_submatrix with the pressure projection
+// (src/Matrix/BlockFEMatrix.C:1168-1345). Cell Vanka restates
+// VankaSmoother::smooth (src/Multigrid/VankaSmoother.C:110-292).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "pm_stokes.h"
+
+namespace pm {
+
+// ------------------------------------------------------------- tables ------
+static const double kP4w[11] = {-.0131555555555555555555555555556, .00762222222222222222222222222222,
+                                .00762222222222222222222222222222, .00762222222222222222222222222222,
+                                .00762222222222222222222222222222, .0248888888888888888888888888889,
+                                .0248888888888888888888888888889, .0248888888888888888888888888889,
+                                .0248888888888888888888888888889, .0248888888888888888888888888889,
+                                .0248888888888888888888888888889};
+static const double kP4x[11] = {.25, .0714285714285714285714285714286, .785714285714285714285714285714,
+                                .0714285714285714285714285714286, .0714285714285714285714285714286,
+                                .399403576166799204996102147462, .399403576166799204996102147462,
+                                .100596423833200795003897852538, .100596423833200795003897852538,
+                                .100596423833200795003897852538, .399403576166799204996102147462};
+static const double kP4y[11] = {.25, .0714285714285714285714285714286, .0714285714285714285714285714286,
+                                .785714285714285714285714285714, .0714285714285714285714285714286,
+                                .399403576166799204996102147462, .100596423833200795003897852538,
+                                .399403576166799204996102147462, .100596423833200795003897852538,
+                                .399403576166799204996102147462, .100596423833200795003897852538};
+static const double kP4z[11] = {.25, .0714285714285714285714285714286, .0714285714285714285714285714286,
+                                .0714285714285714285714285714286, .785714285714285714285714285714,
+                                .100596423833200795003897852538, .399403576166799204996102147462,
+                                .399403576166799204996102147462, .399403576166799204996102147462,
+                                .100596423833200795003897852538, .100596423833200795003897852538};
+
+// C_T_P2_3D values and derivatives (include/FE3D/BF_C_T_P2_3D.h)
+static void p2_eval(double x, double y, double z, double* v, double* dx, double* dy, double* dz) {
+  v[0] = 1 - 3 * x - 3 * y - 3 * z + 2 * x * x + 4 * x * y + 4 * x * z + 2 * y * y + 4 * y * z + 2 * z * z;
+  v[1] = 4 * x - 4 * x * x - 4 * x * y - 4 * x * z;
+  v[2] = -x + 2 * x * x;
+  v[3] = 4 * y - 4 * x * y - 4 * y * y - 4 * y * z;
+  v[4] = 4 * x * y;
+  v[5] = -y + 2 * y * y;
+  v[6] = 4 * z - 4 * x * z - 4 * y * z - 4 * z * z;
+  v[7] = 4 * x * z;
+  v[8] = 4 * y * z;
+  v[9] = -z + 2 * z * z;
+  const double g0 = -3 + 4 * x + 4 * y + 4 * z;
+  const double dxs[10] = {g0, 4 - 8 * x - 4 * y - 4 * z, -1 + 4 * x, -4 * y, 4 * y, 0, -4 * z, 4 * z, 0, 0};
+  const double dys[10] = {g0, -4 * x, 0, 4 - 4 * x - 8 * y - 4 * z, 4 * x, -1 + 4 * y, -4 * z, 0, 4 * z, 0};
+  const double dzs[10] = {g0, -4 * x, 0, -4 * y, 0, 0, 4 - 4 * x - 4 * y - 8 * z, 4 * x, 4 * y, -1 + 4 * z};
+  for (int i = 0; i < 10; ++i) {
+    dx[i] = dxs[i];
+    dy[i] = dys[i];
+    dz[i] = dzs[i];
+  }
+}
+
+// layout: S[6][100] | D[3][40] | phi2[11][10] | w[11] | xi[11][3]
+static constexpr int kOffS = 0, kOffD = 600, kOffPhi = 720, kOffW = 830, kOffXi = 841, kTabSize = 874;
+
+void DevStokesTables::upload(pm_ctx* c) {
+  std::vector<double> t(kTabSize, 0.0);
+  double phi[11][10], d[3][11][10], psi[11][4];
+  for (int q = 0; q < 11; ++q) {
+    p2_eval(kP4x[q], kP4y[q], kP4z[q], phi[q], d[0][q], d[1][q], d[2][q]);
+    psi[q][0] = 1 - kP4x[q] - kP4y[q] - kP4z[q];
+    psi[q][1] = kP4x[q];
+    psi[q][2] = kP4y[q];
+    psi[q][3] = kP4z[q];
+  }
+  int k = 0;
+  for (int a = 0; a < 3; ++a)
+    for (int b = a; b < 3; ++b, ++k)
+      for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 10; ++j) {
+          double s = 0.0;
+          for (int q = 0; q < 11; ++q) {
+            s += kP4w[q] * d[a][q][i] * d[b][q][j];
+            if (a != b) s += kP4w[q] * d[b][q][i] * d[a][q][j];
+          }
+          t[kOffS + k * 100 + i * 10 + j] = s;
+        }
+  for (int a = 0; a < 3; ++a)
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 10; ++j) {
+        double s = 0.0;
+        for (int q = 0; q < 11; ++q) s += kP4w[q] * psi[q][i] * d[a][q][j];
+        t[kOffD + a * 40 + i * 10 + j] = s;
+      }
+  for (int q = 0; q < 11; ++q) {
+    for (int i = 0; i < 10; ++i) t[kOffPhi + q * 10 + i] = phi[q][i];
+    t[kOffW + q] = kP4w[q];
+    t[kOffXi + q * 3 + 0] = kP4x[q];
+    t[kOffXi + q * 3 + 1] = kP4y[q];
+    t[kOffXi + q * 3 + 2] = kP4z[q];
+  }
+  data.upload(t, c->stream);
+}
+
+void DevStokesLevel::upload(pm_ctx* c, const DiscLevel& L) {
+  n_cells = L.n_cells;
+  n = L.sys.n_rows;
+  verts.upload(L.verts, c->stream);
+  gat_ptr.upload(L.gat_ptr, c->stream);
+  gat_idx.upload(L.gat_idx, c->stream);
+  rgat_ptr.upload(L.rgat_ptr, c->stream);
+  rgat_idx.upload(L.rgat_idx, c->stream);
+  diag_pos.upload(L.diag_pos, c->stream);
+}
+
+// right-hand side f = -nu Lap u + grad p of the manufactured Stokes solution
+__device__ void stokes_f(double nu, const double* x, double* f) {
+  const double p = 3.14159265358979323846;
+  double S[3], S1[3], S2[3], S3[3];
+  for (int d = 0; d < 3; ++d) {
+    double s, c;
+    sincospi(x[d], &s, &c);
+    double s2, c2;
+    sincospi(2.0 * x[d], &s2, &c2);
+    S[d] = s * s;                    // sin^2(pi t)
+    S1[d] = p * s2;                  // d/dt
+    S2[d] = 2 * p * p * c2;          // d2/dt2
+    S3[d] = -4 * p * p * p * s2;     // d3/dt3
+  }
+  // derivatives of Lap psi, psi = S(x) S(y) S(z)
+  const double lx = S3[0] * S[1] * S[2] + S1[0] * S2[1] * S[2] + S1[0] * S[1] * S2[2];
+  const double ly = S2[0] * S1[1] * S[2] + S[0] * S3[1] * S[2] + S[0] * S1[1] * S2[2];
+  const double lz = S2[0] * S[1] * S1[2] + S[0] * S2[1] * S1[2] + S[0] * S[1] * S3[2];
+  // Lap u = curl(Lap psi (1,1,1)); grad p = (1,1,1)
+  f[0] = -nu * (ly - lz) + 1.0;
+  f[1] = -nu * (lz - lx) + 1.0;
+  f[2] = -nu * (lx - ly) + 1.0;
+}
+
+template <int CHUNK>
+__global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* __restrict__ verts,
+                                                     const double* __restrict__ tab, double nu,
+                                                     double* __restrict__ K, double* __restrict__ F) {
+  __shared__ double cS[CHUNK][6];
+  __shared__ double cB[CHUNK][9];
+  __shared__ double geo[CHUNK][13];
+  __shared__ double fq[CHUNK][11][3];
+  const int c0 = blockIdx.x * CHUNK;
+  const int nc = min(CHUNK, n_cells - c0);
+  const int t = threadIdx.x;
+  if (t < nc) {
+    const double* v = verts + (size_t)(c0 + t) * 12;
+    double J[3][3];
+    for (int d = 0; d < 3; ++d) {
+      J[d][0] = v[3 + d] - v[d];
+      J[d][1] = v[6 + d] - v[d];
+      J[d][2] = v[9 + d] - v[d];
+    }
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    const double r = 1.0 / det;
+    double G[3][3];
+    G[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * r;
+    G[0][1] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) * r;
+    G[0][2] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * r;
+    G[1][0] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * r;
+    G[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+    G[1][2] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * r;
+    G[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+    G[2][1] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) * r;
+    G[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    const double adet = fabs(det);
+    int k = 0;
+    for (int a = 0; a < 3; ++a)
+      for (int b = a; b < 3; ++b) {
+        double s = 0.0;
+        for (int d = 0; d < 3; ++d) s += G[d][a] * G[d][b];
+        cS[t][k++] = nu * adet * s;
+      }
+    for (int kk = 0; kk < 3; ++kk)
+      for (int a = 0; a < 3; ++a) cB[t][kk * 3 + a] = -adet * G[kk][a];
+    for (int d = 0; d < 3; ++d) {
+      geo[t][d] = v[d];
+      for (int a = 0; a < 3; ++a) geo[t][3 + d * 3 + a] = J[d][a];
+    }
+    geo[t][12] = adet;
+  }
+  __syncthreads();
+  for (int e = t; e < nc * 11; e += blockDim.x) {
+    const int cl = e / 11, q = e % 11;
+    double x[3];
+    for (int d = 0; d < 3; ++d) {
+      double s = geo[cl][d];
+      for (int a = 0; a < 3; ++a) s += geo[cl][3 + d * 3 + a] * tab[kOffXi + q * 3 + a];
+      x[d] = s;
+    }
+    double f[3];
+    stokes_f(nu, x, f);
+    const double m = tab[kOffW + q] * geo[cl][12];
+    for (int d = 0; d < 3; ++d) fq[cl][q][d] = m * f[d];
+  }
+  __syncthreads();
+  for (int e = t; e < nc * 220; e += blockDim.x) {
+    const int cl = e / 220, p = e % 220;
+    double s = 0.0;
+    if (p < 100) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s = fma(cS[cl][k], __ldg(tab + kOffS + k * 100 + p), s);
+    } else {
+      const int kk = (p - 100) / 40, ij = (p - 100) % 40;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) s = fma(cB[cl][kk * 3 + a], __ldg(tab + kOffD + a * 40 + ij), s);
+    }
+    K[(size_t)(c0 + cl) * 220 + p] = s;
+  }
+  for (int e = t; e < nc * 34; e += blockDim.x) {
+    const int cl = e / 34, m = e % 34;
+    double s = 0.0;
+    if (m < 30) {
+      const int comp = m / 10, i = m % 10;
+      for (int q = 0; q < 11; ++q) s += fq[cl][q][comp] * tab[kOffPhi + q * 10 + i];
+    }
+    F[(size_t)(c0 + cl) * 34 + m] = s;
+  }
+}
+
+__global__ void k_gather_stokes(int nnz, const int* __restrict__ ptr, const int* __restrict__ idx,
+                                const double* __restrict__ K, double* __restrict__ vals) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int t = ptr[e]; t < ptr[e + 1]; ++t) s += K[idx[t]];
+    vals[e] = s;
+  }
+}
+
+__global__ void k_unit_diag(int n, const int* __restrict__ pos, double* __restrict__ vals) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) vals[pos[i]] = 1.0;
+}
+
+void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu,
+                           DevCsr& A, double* rhs, double* K, double* F) {
+  constexpr int CHUNK = 32;
+  k_elem_stokes<CHUNK><<<(L.n_cells + CHUNK - 1) / CHUNK, 256, 0, c->stream>>>(L.n_cells, L.verts.p, t.data.p,
+                                                                              nu, K, F);
+  PM_CHECK_LAUNCH();
+  const int nnz = int(A.nnz);
+  const int g = std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16));
+  k_gather_stokes<<<g, 256, 0, c->stream>>>(nnz, L.gat_ptr.p, L.gat_idx.p, K, A.vals.p);
+  PM_CHECK_LAUNCH();
+  const int nd = int(L.diag_pos.n);
+  if (nd) {
+    k_unit_diag<<<(nd + 255) / 256, 256, 0, c->stream>>>(nd, L.diag_pos.p, A.vals.p);
+    PM_CHECK_LAUNCH();
+  }
+  const int gr = std::max(1, std::min((L.n + 255) / 256, c->num_sms * 16));
+  k_gather_stokes<<<gr, 256, 0, c->stream>>>(L.n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += nd ? 4 : 3;
+}
+
+// --------------------------------------------------- projected matrix ------
+void ProjectedMatrix::build(pm_ctx* c, const pmsetup::Csr& sys, int p0, const BlockMask& mask) {
+  std::vector<int> rp(sys.n_rows + 1, 0), ci, sr;
+  for (int i = 0; i < sys.n_rows; ++i) {
+    if (i == p0) {
+      ci.push_back(p0);
+      sr.push_back(-1);
+    } else {
+      for (int k = sys.row_ptr[i]; k < sys.row_ptr[i + 1]; ++k) {
+        ci.push_back(sys.cols[k]);
+        sr.push_back(k);
+      }
+    }
+    rp[i + 1] = int(ci.size());
+  }
+  csr.upload(c, sys.n_rows, sys.n_cols, sys.n_active, rp.data(), ci.data(), nullptr);
+  csr.mask = mask;
+  src.upload(sr, c->stream);
+}
+
+__global__ void k_project_vals(int nnz, const int* __restrict__ src, const double* __restrict__ v,
+                               double* __restrict__ out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += gridDim.x * blockDim.x) {
+    const int s = src[e];
+    out[e] = s >= 0 ? v[s] : 1.0;
+  }
+}
+
+void ProjectedMatrix::refresh(pm_ctx* c, const DevCsr& sys, bool fp32) {
+  const int nnz = int(csr.nnz);
+  k_project_vals<<<std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16)), 256, 0, c->stream>>>(
+      nnz, src.p, sys.vals.p, csr.vals.p);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+  if (fp32) csr.make_fp32(c);
+}
+
+// ------------------------------------------------------------- Vanka -------
+void DevVanka::setup(pm_ctx* c, const DiscLevel& L) {
+  n_cells = L.n_cells;
+  n = L.sys.n_rows;
+  patch.upload(L.patch_dofs, c->stream);
+  std::vector<int> ip(n + 1, 0), ix, cnt(n, 0);
+  for (int d : L.patch_dofs) ip[d + 1]++;
+  for (int i = 0; i < n; ++i) {
+    cnt[i] = ip[i + 1];
+    ip[i + 1] += ip[i];
+  }
+  ix.resize(ip[n]);
+  std::vector<int> fill(ip.begin(), ip.end() - 1);
+  for (size_t t = 0; t < L.patch_dofs.size(); ++t) ix[fill[L.patch_dofs[t]]++] = int(t);
+  inc_ptr.upload(ip, c->stream);
+  inc_idx.upload(ix, c->stream);
+  count.upload(cnt, c->stream);
+  color_ptr = L.color_ptr;
+  color_cells.upload(L.color_cells, c->stream);
+  sol.ensure(size_t(n_cells) * 34);
+  flag.ensure(1);
+}
+
+// local matrix of one cell from the projected CSR, inverted by Gauss-Jordan
+// with partial pivoting in shared memory; stored column-major
+template <class T>
+__global__ void __launch_bounds__(128) k_vanka_factor(int n_cells, const int* __restrict__ patch,
+                                                      const int* __restrict__ rp, const int* __restrict__ ci,
+                                                      const T* __restrict__ v, T* __restrict__ inv,
+                                                      int* __restrict__ flag) {
+  __shared__ T M[34][35];
+  __shared__ T Inv[34][35];
+  __shared__ int dof[34];
+  __shared__ int piv_row;
+  __shared__ T colk[34];
+  const int cell = blockIdx.x;
+  const int t = threadIdx.x;
+  if (cell >= n_cells) return;
+  if (t < 34) dof[t] = patch[(size_t)cell * 34 + t];
+  for (int e = t; e < 34 * 35; e += blockDim.x) {
+    (&M[0][0])[e] = T(0);
+    (&Inv[0][0])[e] = T(0);
+  }
+  __syncthreads();
+  if (t < 34) {
+    Inv[t][t] = T(1);
+    // entries of global row dof[t] whose column is in the patch
+    const int r = dof[t];
+    for (int k = rp[r]; k < rp[r + 1]; ++k) {
+      const T a = v[k];
+      if (a == T(0)) continue;
+      const int col = ci[k];
+      int lo = 0, hi = 33;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (dof[mid] < col) lo = mid + 1;
+        else hi = mid;
+      }
+      if (dof[lo] == col) M[t][lo] = a;
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < 34; ++k) {
+    if (t == 0) {
+      int p = k;
+      T best = fabs(M[k][k]);
+      for (int i = k + 1; i < 34; ++i)
+        if (fabs(M[i][k]) > best) {
+          best = fabs(M[i][k]);
+          p = i;
+        }
+      piv_row = p;
+      if (!(best > T(0))) atomicExch(flag, 1);
+    }
+    __syncthreads();
+    const int p = piv_row;
+    if (p != k)
+      for (int j = t; j < 34; j += blockDim.x) {
+        T a = M[k][j];
+        M[k][j] = M[p][j];
+        M[p][j] = a;
+        T b = Inv[k][j];
+        Inv[k][j] = Inv[p][j];
+        Inv[p][j] = b;
+      }
+    __syncthreads();
+    const T pivv = M[k][k] != T(0) ? M[k][k] : T(1);
+    if (t < 34) colk[t] = M[t][k];
+    __syncthreads();
+    for (int j = t; j < 34; j += blockDim.x) {
+      M[k][j] /= pivv;
+      Inv[k][j] /= pivv;
+    }
+    __syncthreads();
+    for (int e = t; e < 34 * 34; e += blockDim.x) {
+      const int i = e / 34, j = e % 34;
+      if (i == k) continue;
+      const T f = colk[i];
+      M[i][j] -= f * M[k][j];
+      Inv[i][j] -= f * Inv[k][j];
+    }
+    __syncthreads();
+  }
+  T* out = inv + (size_t)cell * 34 * 34;
+  for (int e = t; e < 34 * 34; e += blockDim.x) {
+    const int j = e / 34, i = e % 34;  // column-major: out[j*34 + i] = Inv[i][j]
+    out[e] = Inv[i][j];
+  }
+}
+
+void DevVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
+  PM_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c->stream));
+  if (fp32) {
+    inv32.ensure(size_t(n_cells) * 34 * 34);
+    sol32.ensure(size_t(n_cells) * 34);
+    k_vanka_factor<float><<<n_cells, 128, 0, c->stream>>>(n_cells, patch.p, V.row_ptr.p, V.cols.p,
+                                                          V.vals32.p, inv32.p, flag.p);
+  } else {
+    inv.ensure(size_t(n_cells) * 34 * 34);
+    k_vanka_factor<double><<<n_cells, 128, 0, c->stream>>>(n_cells, patch.p, V.row_ptr.p, V.cols.p,
+                                                           V.vals.p, inv.p, flag.p);
+  }
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+  int h = 0;
+  PM_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  if (h) throw Error(PM_E_BREAKDOWN, "singular local Vanka system");
+}
+
+// one warp per cell: s = damp * inv * r[patch]; written per cell (Jacobi) or
+// added into x (colour-ordered sweep, after all local right-hand sides of
+// the colour are computed)
+template <class T>
+__global__ void __launch_bounds__(256) k_vanka_local(int n_cells, const int* __restrict__ cells,
+                                                     const int* __restrict__ patch, const T* __restrict__ inv,
+                                                     const T* __restrict__ r, const T* __restrict__ rloc,
+                                                     T* __restrict__ out, T* __restrict__ x, T damp) {
+  __shared__ T rl[8][34];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int idx = blockIdx.x * 8 + w;
+  const bool valid = idx < n_cells;
+  const int cell = valid ? (cells ? cells[idx] : idx) : 0;
+  if (valid) {
+    for (int j = lane; j < 34; j += 32)
+      rl[w][j] = rloc ? rloc[(size_t)cell * 34 + j] : r[patch[(size_t)cell * 34 + j]];
+  }
+  __syncwarp();
+  if (!valid) return;
+  const T* I = inv + (size_t)cell * 1156;
+  for (int i = lane; i < 34; i += 32) {
+    T s = T(0);
+    for (int j = 0; j < 34; ++j) s += I[j * 34 + i] * rl[w][j];
+    if (x) x[patch[(size_t)cell * 34 + i]] += damp * s;
+    else out[(size_t)cell * 34 + i] = damp * s;
+  }
+}
+
+// x[d] += (sum over the patches containing d, in cell order) / count[d]
+template <class T>
+__global__ void k_vanka_average(int n, const int* __restrict__ ip, const int* __restrict__ ix,
+                                const int* __restrict__ cnt, const T* __restrict__ sol, T* __restrict__ x) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
+    if (cnt[d] == 0) continue;
+    T s = T(0);
+    for (int t = ip[d]; t < ip[d + 1]; ++t) s += sol[ix[t]];
+    x[d] += s / T(cnt[d]);
+  }
+}
+
+// local right-hand sides b - V x of the cells of one colour (one warp per cell)
+template <class T>
+__global__ void __launch_bounds__(256) k_vanka_rhs(int n_cells, const int* __restrict__ cells,
+                                                   const int* __restrict__ patch, const int* __restrict__ rp,
+                                                   const int* __restrict__ ci, const T* __restrict__ v,
+                                                   const T* __restrict__ b, const T* __restrict__ x,
+                                                   T* __restrict__ rloc) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= n_cells) return;
+  const int cell = cells[w];
+  for (int i = lane; i < 34; i += 32) {
+    const int r = patch[(size_t)cell * 34 + i];
+    T s = b[r];
+    for (int k = rp[r]; k < rp[r + 1]; ++k) s -= v[k] * x[ci[k]];
+    rloc[(size_t)cell * 34 + i] = s;
+  }
+}
+
+template <class T>
+static void jacobi_sweep(pm_ctx* c, DevVanka& vk, const DevCsr& V, const T* vals, const T* inv, T* sol,
+                         const T* b, T* x, T* r, T damp) {
+  // residual with the projected matrix (residual_glo in the reference)
+  if constexpr (sizeof(T) == 8) csr_apply(c, V, EPI_DEFECT, x, r, b, 1.0);
+  else csr_apply32(c, V, EPI_DEFECT, x, r, b, 1.0f);
+  (void)vals;
+  k_vanka_local<T><<<(vk.n_cells + 7) / 8, 256, 0, c->stream>>>(vk.n_cells, nullptr, vk.patch.p, inv, r,
+                                                                nullptr, sol, nullptr, damp);
+  const int g = std::max(1, std::min((vk.n + 255) / 256, c->num_sms * 16));
+  k_vanka_average<T><<<g, 256, 0, c->stream>>>(vk.n, vk.inc_ptr.p, vk.inc_idx.p, vk.count.p, sol, x);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 2;
+}
+
+void DevVanka::sweep_jacobi(pm_ctx* c, const DevCsr& V, const double* b, double* x, double* r, double damp) {
+  jacobi_sweep<double>(c, *this, V, V.vals.p, inv.p, sol.p, b, x, r, damp);
+}
+void DevVanka::sweep_jacobi32(pm_ctx* c, const DevCsr& V, const float* b, float* x, float* r, float damp) {
+  jacobi_sweep<float>(c, *this, V, V.vals32.p, inv32.p, sol32.p, b, x, r, damp);
+}
+
+template <class T>
+static void colored_sweep(pm_ctx* c, DevVanka& vk, const DevCsr& V, const T* vals, const T* inv, T* rloc,
+                          const T* b, T* x, T damp) {
+  const int ncol = int(vk.color_ptr.size()) - 1;
+  for (int k = 0; k < ncol; ++k) {
+    const int beg = vk.color_ptr[k], cnt = vk.color_ptr[k + 1] - beg;
+    if (!cnt) continue;
+    const int* cells = vk.color_cells.p + beg;
+    k_vanka_rhs<T><<<(cnt * 32 + 255) / 256, 256, 0, c->stream>>>(cnt, cells, vk.patch.p, V.row_ptr.p, V.cols.p,
+                                                                   vals, b, x, rloc);
+    k_vanka_local<T><<<(cnt + 7) / 8, 256, 0, c->stream>>>(cnt, cells, vk.patch.p, inv, nullptr, rloc, nullptr,
+                                                           x, damp);
+    c->kernel_launches += 2;
+  }
+  PM_CHECK_LAUNCH();
+}
+
+void DevVanka::sweep_colored(pm_ctx* c, const DevCsr& V, const double* b, double* x, double damp) {
+  colored_sweep<double>(c, *this, V, V.vals.p, inv.p, sol.p, b, x, damp);
+}
+void DevVanka::sweep_colored32(pm_ctx* c, const DevCsr& V, const float* b, float* x, float damp) {
+  colored_sweep<float>(c, *this, V, V.vals32.p, inv32.p, sol32.p, b, x, damp);
+}
+
+}  // namespace pm

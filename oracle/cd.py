@@ -30,6 +30,8 @@ def lib() -> C.CDLL:
         L.orc_mg_create.restype = vp
         L.orc_mg_set_level.argtypes = [vp, i32, i32, vp, vp, vp, vp]
         L.orc_mg_set_transfer.argtypes = [vp, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32]
+        L.orc_mg_finalize.argtypes = [vp]
+        L.orc_mg_finalize.restype = i32
         L.orc_mg_destroy.argtypes = [vp]
         L.orc_mg_apply.argtypes = [vp, vp, vp]
         L.orc_krylov_solve.argtypes = [i32, i32, vp, vp, vp, vp, vp, f64, f64, i32, i32, i32, vp, vp,
@@ -150,6 +152,8 @@ class OracleCD:
             keep += [fd, cd, fv, cv, par]
             L.orc_mg_set_transfer(mg, l, self.dim, self.elem, fl.n_cells, fl.nloc, _p(fd), _p(cd), _p(par),
                                   _p(fv), _p(cv), fl.n_dofs, cl.n_dofs)
+        if L.orc_mg_finalize(mg) != 0:
+            raise RuntimeError("oracle coarse factorisation failed")
         self._mg = mg
         self._keep = keep
         return mg

@@ -289,7 +289,7 @@ int orc_assemble_cd(int dim, int k, int qn, int n_cells, const double* verts, in
  * values are averaged over the cells sharing them. Restriction divides the
  * fine defect by that multiplicity and applies QQ^T. */
 typedef struct {
-  int dim, k;
+  int dim, k;  /* k: Qk degree; for tetrahedra k = 11 (P1) or 12 (P2) */
   int n_fine_cells, nloc;
   const int* fine_dofmap;
   const int* coarse_dofmap;
@@ -298,6 +298,58 @@ typedef struct {
   const double* coarse_verts;
   int n_fine, n_coarse;
 } orc_transfer;
+
+/* P1 / P2 on the reference tetrahedron (include/FE3D/BF_C_T_P1_3D.h,
+ * BF_C_T_P2_3D.h): values at (x, y, z) in local DOF order */
+static void tet_eval(int elem, double x, double y, double z, double* v) {
+  if (elem == 11) {
+    v[0] = 1 - x - y - z; v[1] = x; v[2] = y; v[3] = z;
+    return;
+  }
+  v[0] = 1 - 3 * x - 3 * y - 3 * z + 2 * x * x + 4 * x * y + 4 * x * z + 2 * y * y + 4 * y * z + 2 * z * z;
+  v[1] = 4 * x - 4 * x * x - 4 * x * y - 4 * x * z;
+  v[2] = -x + 2 * x * x;
+  v[3] = 4 * y - 4 * x * y - 4 * y * y - 4 * y * z;
+  v[4] = 4 * x * y;
+  v[5] = -y + 2 * y * y;
+  v[6] = 4 * z - 4 * x * z - 4 * y * z - 4 * z * z;
+  v[7] = 4 * x * z;
+  v[8] = 4 * y * z;
+  v[9] = -z + 2 * z * z;
+}
+
+/* nodes of a tetrahedral cell in local DOF order: P1 vertices; P2 v0, m01,
+ * v1, m02, m12, v2, m03, m13, m23, v3 */
+static void tet_nodes(int elem, const double* v, double X[][3]) {
+  static const int pr[10][2] = {{0, 0}, {0, 1}, {1, 1}, {0, 2}, {1, 2}, {2, 2}, {0, 3}, {1, 3}, {2, 3}, {3, 3}};
+  if (elem == 11) {
+    for (int m = 0; m < 4; ++m)
+      for (int d = 0; d < 3; ++d) X[m][d] = v[m * 3 + d];
+    return;
+  }
+  for (int m = 0; m < 10; ++m)
+    for (int d = 0; d < 3; ++d) X[m][d] = 0.5 * (v[pr[m][0] * 3 + d] + v[pr[m][1] * 3 + d]);
+}
+
+/* barycentric-type reference coordinates of x in the tetrahedron v */
+static void tet_ref(const double* v, const double* x, double* xi) {
+  double A[3][3], r[3];
+  for (int d = 0; d < 3; ++d) {
+    A[d][0] = v[3 + d] - v[d];
+    A[d][1] = v[6 + d] - v[d];
+    A[d][2] = v[9 + d] - v[d];
+    r[d] = x[d] - v[d];
+  }
+  double det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+               A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+  for (int kk = 0; kk < 3; ++kk) {
+    double B[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) B[i][j] = (j == kk) ? r[i] : A[i][j];
+    xi[kk] = (B[0][0] * (B[1][1] * B[2][2] - B[1][2] * B[2][1]) - B[0][1] * (B[1][0] * B[2][2] - B[1][2] * B[2][0]) +
+              B[0][2] * (B[1][0] * B[2][1] - B[1][1] * B[2][0])) / det;
+  }
+}
 
 static void ref_coords(int dim, const double* v, const double* x, double* xi) {
   /* solve x = v0 + A t, A = [v1-v0, v3-v0(, v4-v0)], xi = 2t - 1 */
@@ -332,6 +384,19 @@ static void ref_coords(int dim, const double* v, const double* x, double* xi) {
 
 /* QQ[j][kk] of fine cell `cell`: coarse basis kk at fine node j */
 static void local_qq(const orc_transfer* t, int cell, double QQ[MAXNB][MAXNB]) {
+  if (t->k >= 11) {
+    /* tetrahedra: fine nodes in the parent's reference coordinates */
+    const double* fv = t->fine_verts + (size_t)cell * 12;
+    const double* cv = t->coarse_verts + (size_t)t->parent[cell] * 12;
+    double X[10][3];
+    tet_nodes(t->k, fv, X);
+    for (int m = 0; m < t->nloc; ++m) {
+      double xi[3];
+      tet_ref(cv, X[m], xi);
+      tet_eval(t->k, xi[0], xi[1], xi[2], QQ[m]);
+    }
+    return;
+  }
   const int nv = t->dim == 2 ? 4 : 8;
   const double* fv = t->fine_verts + (size_t)cell * nv * t->dim;
   const double* cv = t->coarse_verts + (size_t)t->parent[cell] * nv * t->dim;
@@ -451,15 +516,28 @@ typedef struct {
   double *rhs, *sol, *defect, *diag;
   double* lu;
   int* piv;
-  orc_transfer up; /* transfer to the next finer level */
+  /* transfer to the next finer level, one per block of the block vector */
+  orc_transfer up[4];
+  int n_up, foff[4], coff[4];
+  /* saddle point levels: projected combined matrix and cell-Vanka patches */
+  const int *vrp, *vci;
+  const double* vv;
+  const int* patch;
+  int n_patches;
+  const int *color_ptr, *color_cells;
+  int n_colors;
+  const int* n_freeze;
 } orc_level;
+
+enum { SM_JAC = 0, SM_DIR = 1, SM_VANKA = 2, SM_VANKA_JAC = 3, SM_VANKA_COLOR = 4 };
 
 typedef struct {
   int n_levels;
   orc_level* lv;
   int n_pre, n_post, coarse_max_it, cycle; /* cycle: 0 V, 1 W, 2 F */
-  double jacobi_damp, correction_damp, coarse_residual;
+  double jacobi_damp, correction_damp, coarse_residual, vanka_damp;
   int coarse_direct;
+  int smoother, smoother_coarse;
   int* control;
   int n_control;
 } orc_mg;
@@ -489,6 +567,9 @@ orc_mg* orc_mg_create(int n_levels, int n_pre, int n_post, double jacobi_damp, d
   m->coarse_direct = coarse_direct;
   m->coarse_max_it = coarse_max_it;
   m->coarse_residual = coarse_residual;
+  m->smoother = SM_JAC;
+  m->smoother_coarse = coarse_direct ? SM_DIR : SM_JAC;
+  m->vanka_damp = 1.0;
   int* rec = (int*)malloc(sizeof(int) * (size_t)n_levels);
   for (int i = 0; i < n_levels; ++i) rec[i] = cycle == 0 ? 1 : 2;
   rec[n_levels - 1] = 1;
@@ -518,27 +599,71 @@ int orc_mg_set_level(orc_mg* m, int l, int n, const unsigned char* active, const
   for (int i = 0; i < n; ++i)
     for (int k = rp[i]; k < rp[i + 1]; ++k)
       if (ci[k] == i) L->diag[i] = v[k];
-  if (l == 0 && m->coarse_direct) {
-    /* DirectSolver on get_combined_matrix: unit rows for non-actives */
-    L->lu = (double*)calloc((size_t)n * n, sizeof(double));
-    L->piv = (int*)malloc(sizeof(int) * (size_t)n);
-    for (int i = 0; i < n; ++i) {
-      if (!active[i]) { L->lu[(size_t)i * n + i] = 1.0; continue; }
-      for (int k = rp[i]; k < rp[i + 1]; ++k) L->lu[(size_t)i * n + ci[k]] = v[k];
-    }
-    if (orc_lu_factor(n, L->lu, L->piv)) return -1;
-  }
   return 0;
+}
+
+/* smoothers: 0 Jacobi, 1 direct, 2 cell Vanka (cell order), 3 cell Vanka
+ * Jacobi, 4 cell Vanka in colour order */
+void orc_mg_set_smoothers(orc_mg* m, int fine, int coarse, double vanka_damp) {
+  m->smoother = fine;
+  m->smoother_coarse = coarse;
+  m->coarse_direct = coarse == SM_DIR;
+  m->vanka_damp = vanka_damp;
+}
+
+/* saddle point level: projected combined matrix (get_combined_matrix) and the
+ * cell patches (sorted combined DOFs, 34 per cell) with their colouring */
+void orc_mg_set_vanka(orc_mg* m, int l, const int* vrp, const int* vci, const double* vv, const int* patch,
+                      int n_patches, const int* color_ptr, const int* color_cells, int n_colors,
+                      const int* n_freeze) {
+  orc_level* L = &m->lv[l];
+  L->vrp = vrp; L->vci = vci; L->vv = vv;
+  L->patch = patch; L->n_patches = n_patches;
+  L->color_ptr = color_ptr; L->color_cells = color_cells; L->n_colors = n_colors;
+  L->n_freeze = n_freeze;
+}
+
+/* DirectSolver on get_combined_matrix of the coarsest level: the projected
+ * matrix when given, else the system with unit rows for non-actives */
+int orc_mg_finalize(orc_mg* m) {
+  orc_level* L = &m->lv[0];
+  if (!m->coarse_direct) return 0;
+  const int n = L->n;
+  free(L->lu);
+  free(L->piv);
+  L->lu = (double*)calloc((size_t)n * n, sizeof(double));
+  L->piv = (int*)malloc(sizeof(int) * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    if (L->vrp) {
+      for (int k = L->vrp[i]; k < L->vrp[i + 1]; ++k) L->lu[(size_t)i * n + L->vci[k]] = L->vv[k];
+    } else {
+      if (!L->active[i]) { L->lu[(size_t)i * n + i] = 1.0; continue; }
+      for (int k = L->rp[i]; k < L->rp[i + 1]; ++k) L->lu[(size_t)i * n + L->ci[k]] = L->v[k];
+    }
+  }
+  return orc_lu_factor(n, L->lu, L->piv) ? -1 : 0;
+}
+
+void orc_mg_set_transfer_block(orc_mg* m, int l, int block, int fine_off, int coarse_off, int dim, int k,
+                               int n_fine_cells, int nloc, const int* fine_dofmap, const int* coarse_dofmap,
+                               const int* parent, const double* fine_verts, const double* coarse_verts,
+                               int n_fine, int n_coarse) {
+  orc_level* L = &m->lv[l];
+  orc_transfer* t = &L->up[block];
+  t->dim = dim; t->k = k; t->n_fine_cells = n_fine_cells; t->nloc = nloc;
+  t->fine_dofmap = fine_dofmap; t->coarse_dofmap = coarse_dofmap; t->parent = parent;
+  t->fine_verts = fine_verts; t->coarse_verts = coarse_verts;
+  t->n_fine = n_fine; t->n_coarse = n_coarse;
+  L->foff[block] = fine_off;
+  L->coff[block] = coarse_off;
+  if (block + 1 > L->n_up) L->n_up = block + 1;
 }
 
 void orc_mg_set_transfer(orc_mg* m, int l, int dim, int k, int n_fine_cells, int nloc, const int* fine_dofmap,
                          const int* coarse_dofmap, const int* parent, const double* fine_verts,
                          const double* coarse_verts, int n_fine, int n_coarse) {
-  orc_transfer* t = &m->lv[l].up;
-  t->dim = dim; t->k = k; t->n_fine_cells = n_fine_cells; t->nloc = nloc;
-  t->fine_dofmap = fine_dofmap; t->coarse_dofmap = coarse_dofmap; t->parent = parent;
-  t->fine_verts = fine_verts; t->coarse_verts = coarse_verts;
-  t->n_fine = n_fine; t->n_coarse = n_coarse;
+  orc_mg_set_transfer_block(m, l, 0, 0, 0, dim, k, n_fine_cells, nloc, fine_dofmap, coarse_dofmap, parent,
+                            fine_verts, coarse_verts, n_fine, n_coarse);
 }
 
 void orc_mg_destroy(orc_mg* m) {
@@ -558,11 +683,22 @@ static double calc_defect(orc_level* L) {
   return sqrt(orc_dot(L->n, L->defect, L->defect));
 }
 
+void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int* rp, const int* ci,
+                     const double* v, const double* b, double* x, double damp, const int* color_ptr,
+                     const int* color_cells, int n_colors, const int* n_freeze);
+
 static void smooth(orc_mg* m, int l) {
   orc_level* L = &m->lv[l];
-  if (l == 0 && m->coarse_direct) {
+  const int code = l == 0 ? m->smoother_coarse : m->smoother;
+  if (code == SM_DIR) {
     memcpy(L->sol, L->rhs, sizeof(double) * (size_t)L->n);
     orc_lu_solve(L->n, L->lu, L->piv, L->sol);
+    return;
+  }
+  if (code == SM_VANKA || code == SM_VANKA_JAC || code == SM_VANKA_COLOR) {
+    orc_vanka_sweep(code == SM_VANKA ? 0 : code == SM_VANKA_JAC ? 1 : 2, L->n_patches, L->patch, L->n, L->vrp,
+                    L->vci, L->vv, L->rhs, L->sol, m->vanka_damp, L->color_ptr, L->color_cells, L->n_colors,
+                    L->n_freeze);
     return;
   }
   /* JacobiSmoother::smooth */
@@ -578,7 +714,8 @@ static void prolong_add(orc_mg* m, int l) {
   orc_level* C = &m->lv[l];
   orc_level* F = &m->lv[l + 1];
   double* tmp = (double*)malloc(sizeof(double) * (size_t)F->n);
-  orc_prolongate(&C->up, C->sol, tmp);
+  for (int b = 0; b < C->n_up; ++b)
+    orc_prolongate(&C->up[b], C->sol + C->coff[b], tmp + C->foff[b]);
   /* damped addition on the actives (Multigrid.C:357-418) */
   for (int j = 0; j < F->n; ++j)
     if (F->active[j]) F->sol[j] += m->correction_damp * tmp[j];
@@ -606,7 +743,8 @@ static int cycle_step(orc_mg* m, int step, int level) {
     calc_defect(&m->lv[level]);
     orc_level* C = &m->lv[level - 1];
     memset(C->sol, 0, sizeof(double) * (size_t)C->n);
-    orc_restrict(&C->up, C->rhs, m->lv[level].defect);
+    for (int b = 0; b < C->n_up; ++b)
+      orc_restrict(&C->up[b], C->rhs + C->coff[b], m->lv[level].defect + C->foff[b]);
     for (int j = 0; j < C->n; ++j)
       if (!C->active[j]) C->rhs[j] = 0.0; /* ResetNonActive */
     return level - 1;
@@ -880,4 +1018,257 @@ void orc_restrict_flat(int dim, int k, int n_fine_cells, int nloc, const int* fi
   orc_transfer t = {dim, k, n_fine_cells, nloc, fine_dofmap, coarse_dofmap, parent,
                     fine_verts, coarse_verts, n_fine, n_coarse};
   orc_restrict(&t, coarse, fine);
+}
+
+/* ------------------------------------------------------ cell Vanka ---------
+ * VankaSmoother::smooth (src/Multigrid/VankaSmoother.C:110-292) on the
+ * projected combined matrix. type 0: CELL (multiplicative, cells in order),
+ * type 1: CELL_JACOBI (global residual once, corrections averaged over the
+ * patches sharing a DOF), type 2: CELL in colour order (all local right-hand
+ * sides of a colour from the same iterate, then the colour's updates).
+ *
+ * Frozen pressure DOFs: a cell with a single active velocity node (3 active
+ * velocity rows against 4 pressure columns) has an exactly singular local
+ * matrix, on which the reference's LAPACK LU throws or returns a blown-up
+ * correction. n_freeze[cell] (4 - 3 x active velocity nodes, clamped to
+ * 0..4) trailing pressure entries of the sorted patch are decoupled (unit
+ * row and column) and receive no update. n_freeze == NULL keeps every
+ * local matrix as the reference builds it. */
+#define VP 34
+static void vanka_local_matrix(const int* dof, const int* rp, const int* ci, const double* v, int nf,
+                               double* M) {
+  for (int e = 0; e < VP * VP; ++e) M[e] = 0.0;
+  for (int r = 0; r < VP; ++r) {
+    const int rg = dof[r];
+    int c = 0;
+    for (int j = rp[rg]; j < rp[rg + 1]; ++j) {
+      const double entry = v[j];
+      if (entry == 0) continue; /* don't copy zeroes */
+      const int cg = ci[j];
+      while (dof[c] < cg) {
+        ++c;
+        if (c == VP) break;
+      }
+      if (c == VP) break;
+      if (dof[c] == cg) M[r * VP + c] = entry;
+    }
+  }
+  for (int f = VP - nf; f < VP; ++f) {
+    for (int k = 0; k < VP; ++k) M[f * VP + k] = M[k * VP + f] = 0.0;
+    M[f * VP + f] = 1.0;
+  }
+}
+
+static void vanka_local_solve(const int* dof, const int* rp, const int* ci, const double* v, int nf,
+                              double* loc) {
+  double M[VP * VP];
+  int piv[VP];
+  vanka_local_matrix(dof, rp, ci, v, nf, M);
+  orc_lu_factor(VP, M, piv);
+  orc_lu_solve(VP, M, piv, loc);
+  for (int f = VP - nf; f < VP; ++f) loc[f] = 0.0;
+}
+
+static void vanka_local_rhs(const int* dof, const int* rp, const int* ci, const double* v, const double* b,
+                            const double* x, double* loc) {
+  for (int r = 0; r < VP; ++r) {
+    const int rg = dof[r];
+    double t = b[rg];
+    for (int j = rp[rg]; j < rp[rg + 1]; ++j) t -= v[j] * x[ci[j]];
+    loc[r] = t;
+  }
+}
+
+void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int* rp, const int* ci,
+                     const double* v, const double* b, double* x, double damp, const int* color_ptr,
+                     const int* color_cells, int n_colors, const int* n_freeze) {
+  double loc[VP];
+  if (type == 1) {
+    double* res = (double*)malloc(sizeof(double) * (size_t)n);
+    double* upd = (double*)calloc((size_t)n, sizeof(double));
+    double* cnt = (double*)calloc((size_t)n, sizeof(double));
+    memcpy(res, b, sizeof(double) * (size_t)n);
+    orc_multiply(n, rp, ci, v, x, res, -1.0);
+    for (int p = 0; p < n_patches; ++p) {
+      const int* dof = patch + (size_t)p * VP;
+      for (int r = 0; r < VP; ++r) loc[r] = res[dof[r]];
+      vanka_local_solve(dof, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
+      for (int r = 0; r < VP; ++r) {
+        upd[dof[r]] += damp * loc[r];
+        cnt[dof[r]] += 1;
+      }
+    }
+    for (int i = 0; i < n; ++i)
+      if (cnt[i] != 0) x[i] += upd[i] / cnt[i];
+    free(res); free(upd); free(cnt);
+    return;
+  }
+  if (type == 0) {
+    for (int p = 0; p < n_patches; ++p) {
+      const int* dof = patch + (size_t)p * VP;
+      vanka_local_rhs(dof, rp, ci, v, b, x, loc);
+      vanka_local_solve(dof, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
+      for (int r = 0; r < VP; ++r) x[dof[r]] += damp * loc[r];
+    }
+    return;
+  }
+  /* colour order */
+  for (int k = 0; k < n_colors; ++k) {
+    const int beg = color_ptr[k], end = color_ptr[k + 1];
+    double* rl = (double*)malloc(sizeof(double) * (size_t)(end - beg) * VP);
+    for (int q = beg; q < end; ++q)
+      vanka_local_rhs(patch + (size_t)color_cells[q] * VP, rp, ci, v, b, x, rl + (size_t)(q - beg) * VP);
+    for (int q = beg; q < end; ++q) {
+      const int cell = color_cells[q];
+      const int* dof = patch + (size_t)cell * VP;
+      double* l = rl + (size_t)(q - beg) * VP;
+      vanka_local_solve(dof, rp, ci, v, n_freeze ? n_freeze[cell] : 0, l);
+      for (int r = 0; r < VP; ++r) x[dof[r]] += damp * l[r];
+    }
+    free(rl);
+  }
+}
+
+/* ---------------------------------------------------- Stokes assembly ------
+ * Assemble3D with the NSE Galerkin local forms for Stokes, Laplace form
+ * (NSLaplaceGradGrad, NSDivergenceBlocks with sign 1, NSGradientBlocks,
+ * NSRightHandSide: src/AssembleRoutinesSaddle/NSE_local_assembling_routines.C
+ * :82-254), P2/P1 on affine tetrahedra with the P4Tetra rule
+ * (src/QuadFormulas/QuadFormulaTetra.C:73). cdof: 34 combined DOFs per cell
+ * ([u1 | u2 | u3 | p] numbering). Right-hand side of the manufactured
+ * solution u = curl(psi (1,1,1)), psi = (sin pi x sin pi y sin pi z)^2,
+ * p = x + y + z - 3/2. */
+static void stokes_f(double nu, const double* x, double* f) {
+  const double p = 3.14159265358979323846;
+  double S[3], S1[3], S2[3], S3[3];
+  for (int d = 0; d < 3; ++d) {
+    const double s = sin(p * x[d]);
+    S[d] = s * s;
+    S1[d] = p * sin(2 * p * x[d]);
+    S2[d] = 2 * p * p * cos(2 * p * x[d]);
+    S3[d] = -4 * p * p * p * sin(2 * p * x[d]);
+  }
+  const double lx = S3[0] * S[1] * S[2] + S1[0] * S2[1] * S[2] + S1[0] * S[1] * S2[2];
+  const double ly = S2[0] * S1[1] * S[2] + S[0] * S3[1] * S[2] + S[0] * S1[1] * S2[2];
+  const double lz = S2[0] * S[1] * S1[2] + S[0] * S2[1] * S1[2] + S[0] * S[1] * S3[2];
+  f[0] = -nu * (ly - lz) + 1.0;
+  f[1] = -nu * (lz - lx) + 1.0;
+  f[2] = -nu * (lx - ly) + 1.0;
+}
+
+static const double P4W[11] = {-.0131555555555555555555555555556, .00762222222222222222222222222222,
+  .00762222222222222222222222222222, .00762222222222222222222222222222, .00762222222222222222222222222222,
+  .0248888888888888888888888888889, .0248888888888888888888888888889, .0248888888888888888888888888889,
+  .0248888888888888888888888888889, .0248888888888888888888888888889, .0248888888888888888888888888889};
+static const double P4X[11] = {.25, .0714285714285714285714285714286, .785714285714285714285714285714,
+  .0714285714285714285714285714286, .0714285714285714285714285714286, .399403576166799204996102147462,
+  .399403576166799204996102147462, .100596423833200795003897852538, .100596423833200795003897852538,
+  .100596423833200795003897852538, .399403576166799204996102147462};
+static const double P4Y[11] = {.25, .0714285714285714285714285714286, .0714285714285714285714285714286,
+  .785714285714285714285714285714, .0714285714285714285714285714286, .399403576166799204996102147462,
+  .100596423833200795003897852538, .399403576166799204996102147462, .100596423833200795003897852538,
+  .399403576166799204996102147462, .100596423833200795003897852538};
+static const double P4Z[11] = {.25, .0714285714285714285714285714286, .0714285714285714285714285714286,
+  .0714285714285714285714285714286, .785714285714285714285714285714, .100596423833200795003897852538,
+  .399403576166799204996102147462, .399403576166799204996102147462, .399403576166799204996102147462,
+  .100596423833200795003897852538, .100596423833200795003897852538};
+
+static void p2_grad(double x, double y, double z, double* dx, double* dy, double* dz) {
+  const double g0 = -3 + 4 * x + 4 * y + 4 * z;
+  const double a[10] = {g0, 4 - 8 * x - 4 * y - 4 * z, -1 + 4 * x, -4 * y, 4 * y, 0, -4 * z, 4 * z, 0, 0};
+  const double b[10] = {g0, -4 * x, 0, 4 - 4 * x - 8 * y - 4 * z, 4 * x, -1 + 4 * y, -4 * z, 0, 4 * z, 0};
+  const double c[10] = {g0, -4 * x, 0, -4 * y, 0, 0, 4 - 4 * x - 4 * y - 8 * z, 4 * x, 4 * y, -1 + 4 * z};
+  for (int i = 0; i < 10; ++i) { dx[i] = a[i]; dy[i] = b[i]; dz[i] = c[i]; }
+}
+
+static int add_entry(const int* rp, const int* ci, double* vals, int row, int col, double val) {
+  for (int n = rp[row]; n < rp[row + 1]; ++n)
+    if (ci[n] == col) { vals[n] += val; return 0; }
+  return -1;
+}
+
+int orc_assemble_stokes(int n_cells, const double* verts, double nu, const int* cdof, int n_rows,
+                        const unsigned char* active, const int* rp, const int* ci, double* vals, double* rhs) {
+  memset(vals, 0, sizeof(double) * (size_t)rp[n_rows]);
+  memset(rhs, 0, sizeof(double) * (size_t)n_rows);
+  for (int cell = 0; cell < n_cells; ++cell) {
+    const double* v = verts + (size_t)cell * 12;
+    double J[3][3];
+    for (int d = 0; d < 3; ++d) {
+      J[d][0] = v[3 + d] - v[d]; J[d][1] = v[6 + d] - v[d]; J[d][2] = v[9 + d] - v[d];
+    }
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    double G[3][3];
+    G[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+    G[0][1] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) / det;
+    G[0][2] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+    G[1][0] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) / det;
+    G[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+    G[1][2] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) / det;
+    G[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+    G[2][1] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) / det;
+    G[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    const double adet = fabs(det);
+    double A[10][10] = {{0}}, B[3][4][10] = {{{0}}}, BT[3][10][4] = {{{0}}}, F[3][10] = {{0}};
+    for (int q = 0; q < 11; ++q) {
+      const double xi = P4X[q], et = P4Y[q], ze = P4Z[q];
+      double rx[10], ry[10], rz[10], ux[10], uy[10], uz[10], u[10], ps[4];
+      tet_eval(12, xi, et, ze, u);
+      tet_eval(11, xi, et, ze, ps);
+      p2_grad(xi, et, ze, rx, ry, rz);
+      for (int i = 0; i < 10; ++i) {
+        ux[i] = G[0][0] * rx[i] + G[0][1] * ry[i] + G[0][2] * rz[i];
+        uy[i] = G[1][0] * rx[i] + G[1][1] * ry[i] + G[1][2] * rz[i];
+        uz[i] = G[2][0] * rx[i] + G[2][1] * ry[i] + G[2][2] * rz[i];
+      }
+      double X[3];
+      for (int d = 0; d < 3; ++d) X[d] = v[d] + J[d][0] * xi + J[d][1] * et + J[d][2] * ze;
+      double f[3];
+      stokes_f(nu, X, f);
+      const double Mult = P4W[q] * adet;
+      for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 10; ++j) A[i][j] += Mult * nu * (ux[i] * ux[j] + uy[i] * uy[j] + uz[i] * uz[j]);
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 10; ++j) {
+          B[0][i][j] -= 1 * Mult * ps[i] * ux[j];
+          B[1][i][j] -= 1 * Mult * ps[i] * uy[j];
+          B[2][i][j] -= Mult * 1 * ps[i] * uz[j];
+        }
+      for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 4; ++j) {
+          BT[0][i][j] -= Mult * ps[j] * ux[i];
+          BT[1][i][j] -= Mult * ps[j] * uy[i];
+          BT[2][i][j] -= Mult * ps[j] * uz[i];
+        }
+      for (int i = 0; i < 10; ++i)
+        for (int d = 0; d < 3; ++d) F[d][i] += Mult * u[i] * f[d];
+    }
+    const int* D = cdof + (size_t)cell * 34;
+    for (int m = 0; m < 34; ++m) {
+      const int r = D[m];
+      if (!active[r]) {
+        for (int n = rp[r]; n < rp[r + 1]; ++n)
+          if (ci[n] == r) vals[n] = 1.0;
+        continue;
+      }
+      for (int k = 0; k < 34; ++k) {
+        const int bm = m < 30 ? m / 10 : 3, bk = k < 30 ? k / 10 : 3;
+        double val;
+        if (bm < 3 && bk < 3) {
+          if (bm != bk) continue;
+          val = A[m % 10][k % 10];
+        } else if (bm < 3) {
+          val = BT[bm][m % 10][k - 30];
+        } else if (bk < 3) {
+          val = B[bk][m - 30][k % 10];
+        } else {
+          continue;
+        }
+        if (add_entry(rp, ci, vals, r, D[k], val)) return -3;
+      }
+      if (m < 30) rhs[r] += F[m / 10][m % 10];
+    }
+  }
+  return 0;
 }

@@ -1,0 +1,296 @@
+"""Oracle Stokes P2/P1 driver (test infrastructure only).
+
+Restates the NSE3D Stokes set-up of the solve path with numpy and drives the C
+restatement in oracle.c:
+
+  spaces      : velocity C_T_P2_3D with Dirichlet boundary, pressure C_T_P1_3D
+                with Neumann boundary (all pressure DOFs active), numbered as
+                TFESpace3D::ConstructSpace (src/FE/FESpace3D.C:506-2092)
+  combined    : BlockFEMatrix::NSE3D_Type4 Stokes blocks (A11 = A22 = A33,
+                B^T, B; src/Matrix/BlockFEMatrix.C:616-664) flattened as
+                get_combined_matrix ([u1 | u2 | u3 | p] ordering,
+                BlockFEMatrix.C:1168-1345); non-active rows hold a unit
+                diagonal
+  projection  : first pressure row replaced by a unit row
+                (get_combined_submatrix with pressure projection)
+  Vanka       : patches = sorted combined DOFs of a cell
+                (VankaSmoother::set_up_cell_patches, src/Multigrid/VankaSmoother.C:305)
+                plus a greedy cell colouring for the colour-ordered sweep
+  multigrid   : block-diagonal transfer, P2 for the velocity components and
+                P1 for the pressure (GridTransfer on each space)
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import refsetup
+from .cd import _p, lib as _cd_lib
+
+SM_JAC, SM_DIR, SM_VANKA, SM_VANKA_JAC, SM_VANKA_COLOR = 0, 1, 2, 3, 4
+VANKA_TYPES = {"cell": SM_VANKA, "cell_jacobi": SM_VANKA_JAC, "cell_color": SM_VANKA_COLOR,
+               "direct_solve": SM_DIR, "jacobi": SM_JAC}
+
+
+def lib() -> C.CDLL:
+    L = _cd_lib()
+    if not getattr(L, "_stokes_sigs", False):
+        vp, i32, f64 = C.c_void_p, C.c_int, C.c_double
+        L.orc_assemble_stokes.argtypes = [i32, vp, f64, vp, i32, vp, vp, vp, vp, vp]
+        L.orc_assemble_stokes.restype = i32
+        L.orc_vanka_sweep.argtypes = [i32, i32, vp, i32, vp, vp, vp, vp, vp, f64, vp, vp, i32, vp]
+        L.orc_mg_set_smoothers.argtypes = [vp, i32, i32, f64]
+        L.orc_mg_set_vanka.argtypes = [vp, i32, vp, vp, vp, vp, i32, vp, vp, i32, vp]
+        L.orc_mg_finalize.argtypes = [vp]
+        L.orc_mg_finalize.restype = i32
+        L.orc_mg_set_transfer_block.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp,
+                                                i32, i32]
+        L._stokes_sigs = True
+    return L
+
+
+_P4_W = np.array([-.0131555555555555555555555555556] + [.00762222222222222222222222222222] * 4
+                 + [.0248888888888888888888888888889] * 6)
+_A, _B, _C, _D = (.0714285714285714285714285714286, .785714285714285714285714285714,
+                  .399403576166799204996102147462, .100596423833200795003897852538)
+_P4_X = np.array([[.25, .25, .25], [_A, _A, _A], [_B, _A, _A], [_A, _B, _A], [_A, _A, _B], [_C, _C, _D],
+                  [_C, _D, _C], [_D, _C, _C], [_D, _D, _C], [_D, _C, _D], [_C, _D, _D]])
+_RANKS = None
+
+
+def coupling_rank_table() -> np.ndarray:
+    """rank of the coupling int psi_j grad phi_n (P1 pressures j, P2 velocity
+    nodes n of the reference tetrahedron) restricted to the nodes of each of the
+    1024 active-node masks; an affine map keeps the rank"""
+    global _RANKS
+    if _RANKS is None:
+        G = np.zeros((10, 3, 4))
+        for q in range(11):
+            x, y, z = _P4_X[q]
+            g0 = -3 + 4 * x + 4 * y + 4 * z
+            d = np.array([[g0, 4 - 8 * x - 4 * y - 4 * z, -1 + 4 * x, -4 * y, 4 * y, 0, -4 * z, 4 * z, 0, 0],
+                          [g0, -4 * x, 0, 4 - 4 * x - 8 * y - 4 * z, 4 * x, -1 + 4 * y, -4 * z, 0, 4 * z, 0],
+                          [g0, -4 * x, 0, -4 * y, 0, 0, 4 - 4 * x - 4 * y - 8 * z, 4 * x, 4 * y, -1 + 4 * z]])
+            psi = np.array([1 - x - y - z, x, y, z])
+            G += _P4_W[q] * np.einsum("dn,j->ndj", d, psi)
+        r = np.zeros(1024, dtype=np.int64)
+        for m in range(1, 1024):
+            rows = G[[n for n in range(10) if m >> n & 1]].reshape(-1, 4)
+            r[m] = np.linalg.matrix_rank(rows, tol=1e-10)
+        _RANKS = r
+    return _RANKS
+
+
+def _nonzero_pattern() -> np.ndarray:
+    """34x34 local coupling pattern of the Stokes blocks"""
+    blk = np.array([m // 10 if m < 30 else 3 for m in range(34)])
+    bm, bk = blk[:, None], blk[None, :]
+    return np.where((bm < 3) & (bk < 3), bm == bk, ~((bm == 3) & (bk == 3)))
+
+
+class StokesLevel:
+    def __init__(self, verts_lattice, parent, scale):
+        geo = refsetup.GEO_CUBE_TETRA
+        self.verts_lattice = verts_lattice
+        self.parent = None if parent is None else parent.astype(np.int32)
+        self.n_cells = verts_lattice.shape[0]
+        self.verts = (verts_lattice * (1.0 / scale)).astype(np.float64)
+        self.udofmap, self.nu, self.nu_active, self.ucoords = refsetup.number_dofs(
+            refsetup.local_nodes(geo, 12, verts_lattice), scale, dirichlet=True)
+        self.pdofmap, self.np_, _, self.pcoords = refsetup.number_dofs(
+            refsetup.local_nodes(geo, 11, verts_lattice), scale, dirichlet=False)
+        nu, np_ = self.nu, self.np_
+        self.n = 3 * nu + np_
+        self.cdof = np.concatenate([self.udofmap + b * nu for b in range(3)] + [self.pdofmap + 3 * nu],
+                                   axis=1).astype(np.int32)
+        act = np.ones(self.n, dtype=np.uint8)
+        for b in range(3):
+            act[b * nu + self.nu_active: (b + 1) * nu] = 0
+        self.active = act
+        self.p0 = 3 * nu
+        self._structure()
+        self._projected()
+        self.patch = np.ascontiguousarray(np.sort(self.cdof, axis=1), dtype=np.int32)
+        # cells whose active velocity rows couple to the four pressures with
+        # rank < 4 have a singular local matrix: their pressures are frozen
+        masks = (self.active[self.udofmap].astype(np.int64) << np.arange(10)).sum(axis=1)
+        self.n_freeze = np.ascontiguousarray(np.where(coupling_rank_table()[masks] < 4, 4, 0), dtype=np.int32)
+        self._colouring()
+
+    def _structure(self):
+        pat = _nonzero_pattern()
+        mm, kk = np.nonzero(pat)
+        rows = self.cdof[:, mm].ravel().astype(np.int64)
+        cols = self.cdof[:, kk].ravel().astype(np.int64)
+        keep = self.active[rows] == 1
+        rows, cols = rows[keep], cols[keep]
+        d = np.nonzero(self.active == 0)[0].astype(np.int64)
+        rows = np.concatenate([rows, d])
+        cols = np.concatenate([cols, d])
+        key = np.unique(rows * self.n + cols)
+        r = key // self.n
+        self.cols = (key % self.n).astype(np.int32)
+        rp = np.zeros(self.n + 1, dtype=np.int64)
+        np.add.at(rp, r + 1, 1)
+        self.row_ptr = np.cumsum(rp).astype(np.int32)
+
+    def _projected(self):
+        rp, ci = self.row_ptr, self.cols
+        lens = np.diff(rp).astype(np.int64)
+        lens[self.p0] = 1
+        self.vrow_ptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+        src = np.concatenate([np.arange(rp[i], rp[i + 1]) if i != self.p0 else np.array([-1])
+                              for i in range(self.n)]).astype(np.int64)
+        self.vsrc = src
+        vc = np.where(src >= 0, ci[np.maximum(src, 0)], self.p0)
+        self.vcols = np.ascontiguousarray(vc, dtype=np.int32)
+
+    def project(self, vals: np.ndarray) -> np.ndarray:
+        return np.where(self.vsrc >= 0, vals[np.maximum(self.vsrc, 0)], 1.0)
+
+    def _colouring(self):
+        """greedy colouring in cell order: the smallest colour not used by an
+        earlier cell that shares a DOF"""
+        nc = self.n_cells
+        flat = self.cdof.ravel()
+        order = np.argsort(flat, kind="stable")
+        sorted_dofs = flat[order]
+        starts = np.searchsorted(sorted_dofs, np.arange(self.n))
+        ends = np.searchsorted(sorted_dofs, np.arange(self.n), side="right")
+        cells_of = [order[starts[d]:ends[d]] // 34 for d in range(self.n)]
+        color = np.full(nc, -1, dtype=np.int64)
+        n_colors = 0
+        for c in range(nc):
+            nb = np.unique(np.concatenate([cells_of[d] for d in self.cdof[c]]))
+            nb = nb[nb < c]
+            used = set(color[nb].tolist())
+            col = 0
+            while col in used:
+                col += 1
+            color[c] = col
+            n_colors = max(n_colors, col + 1)
+        self.color_ptr = np.zeros(n_colors + 1, dtype=np.int32)
+        np.add.at(self.color_ptr, color + 1, 1)
+        self.color_ptr = np.cumsum(self.color_ptr).astype(np.int32)
+        self.color_cells = np.argsort(color, kind="stable").astype(np.int32)
+        self.n_colors = n_colors
+
+
+def stokes_levels(root_n: int, n_refine: int, n_levels: int):
+    meshes, parents, scale = refsetup.hierarchy(refsetup.GEO_CUBE_TETRA, root_n, n_refine)
+    first = n_refine + 1 - n_levels
+    return [StokesLevel(meshes[l], parents[l], scale) for l in range(first, n_refine + 1)]
+
+
+def vanka_sweep(kind: str, lv: StokesLevel, pvals: np.ndarray, b: np.ndarray, x: np.ndarray,
+                damp: float = 1.0, freeze: bool = True) -> np.ndarray:
+    """one VankaSmoother::smooth sweep on the projected matrix; returns the new x
+    (freeze=False builds every local matrix as the reference does)"""
+    x = np.array(x, dtype=np.float64, copy=True)
+    pv = np.ascontiguousarray(pvals, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    t = {"cell": 0, "cell_jacobi": 1, "cell_color": 2}[kind]
+    lib().orc_vanka_sweep(t, lv.n_cells, _p(lv.patch), lv.n, _p(lv.vrow_ptr), _p(lv.vcols), _p(pv), _p(b),
+                          _p(x), damp, _p(lv.color_ptr), _p(lv.color_cells), lv.n_colors,
+                          _p(lv.n_freeze) if freeze else None)
+    return x
+
+
+class OracleStokes:
+    """NavierStokes<3> (Stokes, Laplace form) restated on the CPU."""
+
+    def __init__(self, root_n: int, n_refine: int, n_levels: int, nu: float = 1.0):
+        self.levels = stokes_levels(root_n, n_refine, n_levels)
+        self.nu = nu
+        self.vals, self.pvals, self.rhs = [], [], []
+        self._mg = None
+        self._keep = []
+
+    @property
+    def finest(self) -> StokesLevel:
+        return self.levels[-1]
+
+    def assemble(self) -> None:
+        L = lib()
+        self.vals, self.pvals, self.rhs = [], [], []
+        for lv in self.levels:
+            vals = np.zeros(lv.cols.size)
+            rhs = np.zeros(lv.n)
+            rc = L.orc_assemble_stokes(lv.n_cells, _p(lv.verts), self.nu, _p(lv.cdof), lv.n, _p(lv.active),
+                                       _p(lv.row_ptr), _p(lv.cols), _p(vals), _p(rhs))
+            if rc != 0:
+                raise RuntimeError(f"oracle Stokes assembly failed ({rc})")
+            self.vals.append(vals)
+            self.pvals.append(np.ascontiguousarray(lv.project(vals)))
+            self.rhs.append(rhs)
+
+    def build_mg(self, smoother="cell_jacobi", coarse_smoother="direct_solve", n_pre=2, n_post=2,
+                 vanka_damp=1.0, correction_damp=1.0, cycle="V", coarse_max_it=10, coarse_residual=0.1,
+                 n_mg_levels=None):
+        L = lib()
+        if self._mg:
+            L.orc_mg_destroy(self._mg)
+        nl = len(self.levels) if n_mg_levels is None else n_mg_levels
+        off = len(self.levels) - nl
+        coarse_direct = coarse_smoother == "direct_solve"
+        mg = L.orc_mg_create(nl, n_pre, n_post, 1.0, correction_damp, {"V": 0, "W": 1, "F": 2}[cycle],
+                             int(coarse_direct), coarse_max_it, coarse_residual)
+        L.orc_mg_set_smoothers(mg, VANKA_TYPES[smoother], VANKA_TYPES[coarse_smoother], vanka_damp)
+        keep = []
+        for l in range(nl):
+            lv = self.levels[off + l]
+            L.orc_mg_set_level(mg, l, lv.n, _p(lv.active), _p(lv.row_ptr), _p(lv.cols), _p(self.vals[off + l]))
+            L.orc_mg_set_vanka(mg, l, _p(lv.vrow_ptr), _p(lv.vcols), _p(self.pvals[off + l]), _p(lv.patch),
+                               lv.n_cells, _p(lv.color_ptr), _p(lv.color_cells), lv.n_colors, _p(lv.n_freeze))
+        for l in range(nl - 1):
+            cl, fl = self.levels[off + l], self.levels[off + l + 1]
+            cv = np.ascontiguousarray(cl.verts)
+            fv = np.ascontiguousarray(fl.verts)
+            par = np.ascontiguousarray(fl.parent)
+            fu = np.ascontiguousarray(fl.udofmap, dtype=np.int32)
+            cu = np.ascontiguousarray(cl.udofmap, dtype=np.int32)
+            fp = np.ascontiguousarray(fl.pdofmap, dtype=np.int32)
+            cp = np.ascontiguousarray(cl.pdofmap, dtype=np.int32)
+            keep += [cv, fv, par, fu, cu, fp, cp]
+            for b in range(3):
+                L.orc_mg_set_transfer_block(mg, l, b, b * fl.nu, b * cl.nu, 3, 12, fl.n_cells, 10, _p(fu), _p(cu),
+                                            _p(par), _p(fv), _p(cv), fl.nu, cl.nu)
+            L.orc_mg_set_transfer_block(mg, l, 3, 3 * fl.nu, 3 * cl.nu, 3, 11, fl.n_cells, 4, _p(fp), _p(cp),
+                                        _p(par), _p(fv), _p(cv), fl.np_, cl.np_)
+        if L.orc_mg_finalize(mg) != 0:
+            raise RuntimeError("oracle coarse factorisation failed")
+        self._mg = mg
+        self._keep = keep
+        return mg
+
+    def mg_apply(self, z: np.ndarray) -> np.ndarray:
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        r = np.zeros_like(z)
+        lib().orc_mg_apply(self._mg, _p(z), _p(r))
+        return r
+
+    def solve(self, tol: float = 0.0, reduction: float = 1e-8, max_it: int = 100, restart: int = 20):
+        """FGMRES with the multigrid preconditioner; returns
+        (solution, iterations, residual, history, status)"""
+        lv = self.finest
+        rhs = self.rhs[-1]
+        sol = np.zeros(lv.n)
+        sol[lv.active == 0] = rhs[lv.active == 0]
+        it, res, nh = C.c_int(), C.c_double(), C.c_int()
+        hist = np.zeros(100000)
+        st = lib().orc_krylov_solve(0, lv.n, _p(lv.active), _p(lv.row_ptr), _p(lv.cols), _p(self.vals[-1]),
+                                    self._mg, tol, reduction, max_it, 0, restart, _p(rhs), _p(sol),
+                                    C.byref(it), C.byref(res), _p(hist), hist.size, C.byref(nh))
+        return sol, it.value, res.value, hist[: nh.value].copy(), st
+
+    def close(self):
+        if self._mg:
+            lib().orc_mg_destroy(self._mg)
+            self._mg = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
