@@ -211,6 +211,9 @@ def run_ours(args, w, rank, world, local, pg):
             # per-launch device times of the finest-level SpMV family: events around
             # every launch, over requests run right after the timed ones (the
             # captured graphs are bypassed while the probe brackets launches)
+            # (the dominant kernel only: the FP32 damped Jacobi sweep)
+            ctx.set_option("probe_epilogue", PROBE_EPILOGUE)
+            ctx.set_option("probe_precision", 4)
             ctx.probe(nnz)
             for _ in range(min(args.steps, 3)):
                 prob.reset_solution()
@@ -218,6 +221,8 @@ def run_ours(args, w, rank, world, local, pg):
                 prob.solve()
             probe = ctx.probe_result()
             ctx.probe(0)
+            ctx.set_option("probe_epilogue", -1)
+            ctx.set_option("probe_precision", 0)
         barrier(pg)
         ms = max_over_ranks(pg, dev_ms)
         results[precision] = dict(ms=ms, wall=wall, its=its, step_ms=step_ms, launches=launches,
@@ -305,18 +310,39 @@ def run_ours(args, w, rank, world, local, pg):
         "e2e": {"value": round(world * K / (e2e_ms / 1e3), 3), "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": mixed["launches"],
-        "roofline": {"bound": "hbm", "kernel": "csr_kernel (finest-level SpMV, Jacobi sweeps, defects)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "csr_kernel<float,float,float,8,16,EPI_JACOBI>: finest-level damped Jacobi "
+                               "sweep in FP32 (the largest share of a mixed request's GPU time)",
                      "achieved": round(achieved, 1) if achieved else None, "peak": hbm_peak,
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 3) if achieved else None,
-                     "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": profiled_traffic(args.workload), "algorithmic_bytes_per_launch":
+                         round(probe_bytes / n_probe) if n_probe else None,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
                      "launches_probed": n_probe,
-                     "probe": f"CUDA events around each finest-level launch over {min(K, 3)} requests "
-                              "run right after the timed ones"},
+                     "probe": f"CUDA events around each finest-level FP32 Jacobi sweep over {min(K, 3)} "
+                              "requests run right after the timed ones"},
         "clocks": mixed["clocks"],
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w)
     return line
+
+
+PROBE_EPILOGUE = 3  # EPI_JACOBI (include/pmgpu.h, probe_epilogue)
+
+
+def profiled_traffic(wname):
+    """DRAM bytes (read + write) per launch of the probed kernel, from the ncu
+    summary committed for this workload, or None"""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                        f"csr_kernel_jacobi32_{wname}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
 
 
 def _oracle_solve(wname):

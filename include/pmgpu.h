@@ -62,7 +62,12 @@ int pm_version(void);
 /* Context options (no reference counterpart):
  *   "assembly_quadrature_loop" 0|1 - element matrices by the per-quadrature-
  *   point loop of LocalAssembling instead of the reference-tensor contraction
- *   (same quadrature, different summation order). */
+ *   (same quadrature, different summation order);
+ *   "probe_epilogue" -1..5 - the launch probe below brackets only launches of
+ *   this SpMV epilogue (0 y+=aAx, 1 y=Ax, 2 defect, 3 damped Jacobi sweep,
+ *   4 restriction, 5 prolongation add; -1 = all);
+ *   "probe_precision" 0|4|8 - only launches whose matrix values have this
+ *   size in bytes (0 = all). */
 int pm_ctx_set_option(pm_ctx* ctx, const char* key, int value);
 /* Launch probe (no reference counterpart; measurement only): while enabled
  * (nnz != 0), every SpMV-family launch (apply, defect, Jacobi sweep, transfer)

@@ -376,8 +376,10 @@ class Discretization:
 
     def structure(self, level: int) -> tuple[np.ndarray, np.ndarray]:
         i = self.level_info(level)
-        n = i["n_dofs"] if self.kind == KIND_CD else None
-        rp = np.empty((n if n is not None else 0) + 1, dtype=np.int32)
+        n = i["n_dofs"]
+        if self.kind == KIND_STOKES:  # combined [u1 | u2 | u3 | p] system
+            n = 3 * n + self.level_info(level, 1)["n_dofs"]
+        rp = np.empty(n + 1, dtype=np.int32)
         ci = np.empty(i["nnz"], dtype=np.int32)
         check(lib.pm_disc_structure(self.handle, level, _ptr(rp), _ptr(ci)))
         return rp, ci

@@ -98,6 +98,8 @@ struct pm_ctx {
   // launch probe: CUDA events around every SpMV-family launch on matrices
   // with probe_nnz nonzeros (0 = off); resolved by pm_ctx_probe_result
   int64_t probe_nnz = 0;
+  int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
+  int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)
   std::vector<cudaEvent_t> probe_events;  // start/end pairs
   std::vector<double> probe_bytes;        // algorithmic bytes of each probed launch
   std::vector<cudaEvent_t> probe_pool;

@@ -246,7 +246,9 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
   const int nrb = use_stream ? A.n_rblocks : 0;
   const int* rp = A.row_ptr.p;
   const int* ci = A.cols.p;
-  const bool probe = c->probe_nnz != 0 && A.nnz == c->probe_nnz;
+  const bool probe = c->probe_nnz != 0 && A.nnz == c->probe_nnz &&
+                     (c->probe_epilogue < 0 || c->probe_epilogue == epi) &&
+                     (c->probe_precision == 0 || c->probe_precision == int(sizeof(TV)));
   if (probe) {
     cudaEvent_t e0 = probe_event(c);
     PM_CUDA(cudaEventRecord(e0, c->stream));

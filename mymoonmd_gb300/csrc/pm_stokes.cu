@@ -14,6 +14,7 @@
 // VankaSmoother::smooth (src/Multigrid/VankaSmoother.C:110-292).
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "pm_stokes.h"
@@ -304,10 +305,65 @@ void ProjectedMatrix::refresh(pm_ctx* c, const DevCsr& sys, bool fp32) {
 }
 
 // ------------------------------------------------------------- Vanka -------
+int stokes_coupling_rank(unsigned mask) {
+  static int table[1024];
+  static bool ready = false;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ready) {
+    double G[10][3][4] = {};
+    for (int q = 0; q < 11; ++q) {
+      double v[10], d[3][10];
+      p2_eval(kP4x[q], kP4y[q], kP4z[q], v, d[0], d[1], d[2]);
+      const double psi[4] = {1 - kP4x[q] - kP4y[q] - kP4z[q], kP4x[q], kP4y[q], kP4z[q]};
+      for (int nn = 0; nn < 10; ++nn)
+        for (int a = 0; a < 3; ++a)
+          for (int j = 0; j < 4; ++j) G[nn][a][j] += kP4w[q] * d[a][nn] * psi[j];
+    }
+    for (unsigned m = 0; m < 1024; ++m) {
+      // rank of the stacked 3-row blocks of the nodes in m, by elimination
+      double R[30][4];
+      int rows = 0;
+      for (int nn = 0; nn < 10; ++nn)
+        if (m >> nn & 1u)
+          for (int a = 0; a < 3; ++a, ++rows)
+            for (int j = 0; j < 4; ++j) R[rows][j] = G[nn][a][j];
+      int rank = 0;
+      for (int col = 0; col < 4 && rank < rows; ++col) {
+        int best = rank;
+        for (int r = rank + 1; r < rows; ++r)
+          if (std::fabs(R[r][col]) > std::fabs(R[best][col])) best = r;
+        if (std::fabs(R[best][col]) < 1e-10) continue;
+        for (int j = 0; j < 4; ++j) std::swap(R[rank][j], R[best][j]);
+        for (int r = rank + 1; r < rows; ++r) {
+          const double f = R[r][col] / R[rank][col];
+          for (int j = 0; j < 4; ++j) R[r][j] -= f * R[rank][j];
+        }
+        ++rank;
+      }
+      table[m] = rank;
+    }
+    ready = true;
+  }
+  return table[mask & 1023u];
+}
+
 void DevVanka::setup(pm_ctx* c, const DiscLevel& L) {
   n_cells = L.n_cells;
   n = L.sys.n_rows;
   patch.upload(L.patch_dofs, c->stream);
+  std::vector<int> fz(n_cells, 0);
+  n_frozen = 0;
+  for (int cell = 0; cell < n_cells; ++cell) {
+    unsigned m = 0;
+    for (int k = 0; k < 10; ++k)
+      if (L.space.dofmap[size_t(cell) * 10 + k] < L.space.n_active) m |= 1u << k;
+    if (stokes_coupling_rank(m) < 4) {
+      fz[cell] = 4;
+      ++n_frozen;
+    }
+  }
+  freeze.upload(fz, c->stream);
   std::vector<int> ip(n + 1, 0), ix, cnt(n, 0);
   for (int d : L.patch_dofs) ip[d + 1]++;
   for (int i = 0; i < n; ++i) {
@@ -331,8 +387,8 @@ void DevVanka::setup(pm_ctx* c, const DiscLevel& L) {
 template <class T>
 __global__ void __launch_bounds__(128) k_vanka_factor(int n_cells, const int* __restrict__ patch,
                                                       const int* __restrict__ rp, const int* __restrict__ ci,
-                                                      const T* __restrict__ v, T* __restrict__ inv,
-                                                      int* __restrict__ flag) {
+                                                      const T* __restrict__ v, const int* __restrict__ freeze,
+                                                      T* __restrict__ inv, int* __restrict__ flag) {
   __shared__ T M[34][35];
   __shared__ T Inv[34][35];
   __shared__ int dof[34];
@@ -365,6 +421,18 @@ __global__ void __launch_bounds__(128) k_vanka_factor(int n_cells, const int* __
     }
   }
   __syncthreads();
+  const int nf = freeze[cell];
+  if (nf) {
+    // frozen trailing pressures: unit rows and columns
+    for (int e = t; e < 34 * nf; e += blockDim.x) {
+      const int f = 34 - nf + e / 34, k = e % 34;
+      M[f][k] = T(0);
+      M[k][f] = T(0);
+    }
+    __syncthreads();
+    if (t < nf) M[34 - nf + t][34 - nf + t] = T(1);
+    __syncthreads();
+  }
   for (int k = 0; k < 34; ++k) {
     if (t == 0) {
       int p = k;
@@ -409,7 +477,7 @@ __global__ void __launch_bounds__(128) k_vanka_factor(int n_cells, const int* __
   T* out = inv + (size_t)cell * 34 * 34;
   for (int e = t; e < 34 * 34; e += blockDim.x) {
     const int j = e / 34, i = e % 34;  // column-major: out[j*34 + i] = Inv[i][j]
-    out[e] = Inv[i][j];
+    out[e] = (i >= 34 - nf || j >= 34 - nf) ? T(0) : Inv[i][j];  // frozen: no update
   }
 }
 
@@ -419,11 +487,11 @@ void DevVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
     inv32.ensure(size_t(n_cells) * 34 * 34);
     sol32.ensure(size_t(n_cells) * 34);
     k_vanka_factor<float><<<n_cells, 128, 0, c->stream>>>(n_cells, patch.p, V.row_ptr.p, V.cols.p,
-                                                          V.vals32.p, inv32.p, flag.p);
+                                                          V.vals32.p, freeze.p, inv32.p, flag.p);
   } else {
     inv.ensure(size_t(n_cells) * 34 * 34);
     k_vanka_factor<double><<<n_cells, 128, 0, c->stream>>>(n_cells, patch.p, V.row_ptr.p, V.cols.p,
-                                                           V.vals.p, inv.p, flag.p);
+                                                           V.vals.p, freeze.p, inv.p, flag.p);
   }
   PM_CHECK_LAUNCH();
   c->kernel_launches++;

@@ -523,6 +523,7 @@ typedef struct {
   const int *vrp, *vci;
   const double* vv;
   const int* patch;
+  const int* patch_ptr; /* NULL: 34 DOFs per patch */
   int n_patches;
   const int *color_ptr, *color_cells;
   int n_colors;
@@ -612,13 +613,14 @@ void orc_mg_set_smoothers(orc_mg* m, int fine, int coarse, double vanka_damp) {
 }
 
 /* saddle point level: projected combined matrix (get_combined_matrix) and the
- * cell patches (sorted combined DOFs, 34 per cell) with their colouring */
+ * Vanka patches (sorted combined DOFs; patch_ptr NULL: 34 per cell) with their
+ * colouring */
 void orc_mg_set_vanka(orc_mg* m, int l, const int* vrp, const int* vci, const double* vv, const int* patch,
                       int n_patches, const int* color_ptr, const int* color_cells, int n_colors,
-                      const int* n_freeze) {
+                      const int* n_freeze, const int* patch_ptr) {
   orc_level* L = &m->lv[l];
   L->vrp = vrp; L->vci = vci; L->vv = vv;
-  L->patch = patch; L->n_patches = n_patches;
+  L->patch = patch; L->n_patches = n_patches; L->patch_ptr = patch_ptr;
   L->color_ptr = color_ptr; L->color_cells = color_cells; L->n_colors = n_colors;
   L->n_freeze = n_freeze;
 }
@@ -683,9 +685,9 @@ static double calc_defect(orc_level* L) {
   return sqrt(orc_dot(L->n, L->defect, L->defect));
 }
 
-void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int* rp, const int* ci,
-                     const double* v, const double* b, double* x, double damp, const int* color_ptr,
-                     const int* color_cells, int n_colors, const int* n_freeze);
+void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* patch, int n, const int* rp,
+                         const int* ci, const double* v, const double* b, double* x, double damp,
+                         const int* color_ptr, const int* color_cells, int n_colors, const int* n_freeze);
 
 static void smooth(orc_mg* m, int l) {
   orc_level* L = &m->lv[l];
@@ -696,7 +698,7 @@ static void smooth(orc_mg* m, int l) {
     return;
   }
   if (code == SM_VANKA || code == SM_VANKA_JAC || code == SM_VANKA_COLOR) {
-    orc_vanka_sweep(code == SM_VANKA ? 0 : code == SM_VANKA_JAC ? 1 : 2, L->n_patches, L->patch, L->n, L->vrp,
+    orc_vanka_sweep_var(code == SM_VANKA ? 0 : code == SM_VANKA_JAC ? 1 : 2, L->n_patches, L->patch_ptr, L->patch, L->n, L->vrp,
                     L->vci, L->vv, L->rhs, L->sol, m->vanka_damp, L->color_ptr, L->color_cells, L->n_colors,
                     L->n_freeze);
     return;
@@ -1034,11 +1036,11 @@ void orc_restrict_flat(int dim, int k, int n_fine_cells, int nloc, const int* fi
  * 0..4) trailing pressure entries of the sorted patch are decoupled (unit
  * row and column) and receive no update. n_freeze == NULL keeps every
  * local matrix as the reference builds it. */
-#define VP 34
-static void vanka_local_matrix(const int* dof, const int* rp, const int* ci, const double* v, int nf,
+/* patch p: dofs[ptr[p] .. ptr[p+1]), sorted combined DOFs */
+static void vanka_local_matrix(const int* dof, int sz, const int* rp, const int* ci, const double* v, int nf,
                                double* M) {
-  for (int e = 0; e < VP * VP; ++e) M[e] = 0.0;
-  for (int r = 0; r < VP; ++r) {
+  for (size_t e = 0; e < (size_t)sz * sz; ++e) M[e] = 0.0;
+  for (int r = 0; r < sz; ++r) {
     const int rg = dof[r];
     int c = 0;
     for (int j = rp[rg]; j < rp[rg + 1]; ++j) {
@@ -1047,31 +1049,33 @@ static void vanka_local_matrix(const int* dof, const int* rp, const int* ci, con
       const int cg = ci[j];
       while (dof[c] < cg) {
         ++c;
-        if (c == VP) break;
+        if (c == sz) break;
       }
-      if (c == VP) break;
-      if (dof[c] == cg) M[r * VP + c] = entry;
+      if (c == sz) break;
+      if (dof[c] == cg) M[(size_t)r * sz + c] = entry;
     }
   }
-  for (int f = VP - nf; f < VP; ++f) {
-    for (int k = 0; k < VP; ++k) M[f * VP + k] = M[k * VP + f] = 0.0;
-    M[f * VP + f] = 1.0;
+  for (int f = sz - nf; f < sz; ++f) {
+    for (int k = 0; k < sz; ++k) M[(size_t)f * sz + k] = M[(size_t)k * sz + f] = 0.0;
+    M[(size_t)f * sz + f] = 1.0;
   }
 }
 
-static void vanka_local_solve(const int* dof, const int* rp, const int* ci, const double* v, int nf,
+static void vanka_local_solve(const int* dof, int sz, const int* rp, const int* ci, const double* v, int nf,
                               double* loc) {
-  double M[VP * VP];
-  int piv[VP];
-  vanka_local_matrix(dof, rp, ci, v, nf, M);
-  orc_lu_factor(VP, M, piv);
-  orc_lu_solve(VP, M, piv, loc);
-  for (int f = VP - nf; f < VP; ++f) loc[f] = 0.0;
+  double* M = (double*)malloc(sizeof(double) * (size_t)sz * sz);
+  int* piv = (int*)malloc(sizeof(int) * (size_t)sz);
+  vanka_local_matrix(dof, sz, rp, ci, v, nf, M);
+  orc_lu_factor(sz, M, piv);
+  orc_lu_solve(sz, M, piv, loc);
+  for (int f = sz - nf; f < sz; ++f) loc[f] = 0.0;
+  free(M);
+  free(piv);
 }
 
-static void vanka_local_rhs(const int* dof, const int* rp, const int* ci, const double* v, const double* b,
+static void vanka_local_rhs(const int* dof, int sz, const int* rp, const int* ci, const double* v, const double* b,
                             const double* x, double* loc) {
-  for (int r = 0; r < VP; ++r) {
+  for (int r = 0; r < sz; ++r) {
     const int rg = dof[r];
     double t = b[rg];
     for (int j = rp[rg]; j < rp[rg + 1]; ++j) t -= v[j] * x[ci[j]];
@@ -1079,10 +1083,17 @@ static void vanka_local_rhs(const int* dof, const int* rp, const int* ci, const 
   }
 }
 
-void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int* rp, const int* ci,
-                     const double* v, const double* b, double* x, double damp, const int* color_ptr,
-                     const int* color_cells, int n_colors, const int* n_freeze) {
-  double loc[VP];
+/* patches of any size: ptr == NULL means 34 DOFs per patch (cell patches of
+ * P2/P1 tetrahedra) */
+void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* patch, int n, const int* rp,
+                         const int* ci, const double* v, const double* b, double* x, double damp,
+                         const int* color_ptr, const int* color_cells, int n_colors, const int* n_freeze) {
+#define PB(p) (ptr ? ptr[p] : 34 * (p))
+#define PS(p) (ptr ? ptr[(p) + 1] - ptr[p] : 34)
+  int maxsz = 0;
+  for (int p = 0; p < n_patches; ++p)
+    if (PS(p) > maxsz) maxsz = PS(p);
+  double* loc = (double*)malloc(sizeof(double) * (size_t)(maxsz > 0 ? maxsz : 1));
   if (type == 1) {
     double* res = (double*)malloc(sizeof(double) * (size_t)n);
     double* upd = (double*)calloc((size_t)n, sizeof(double));
@@ -1090,43 +1101,65 @@ void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int
     memcpy(res, b, sizeof(double) * (size_t)n);
     orc_multiply(n, rp, ci, v, x, res, -1.0);
     for (int p = 0; p < n_patches; ++p) {
-      const int* dof = patch + (size_t)p * VP;
-      for (int r = 0; r < VP; ++r) loc[r] = res[dof[r]];
-      vanka_local_solve(dof, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
-      for (int r = 0; r < VP; ++r) {
+      const int* dof = patch + PB(p);
+      const int sz = PS(p);
+      for (int r = 0; r < sz; ++r) loc[r] = res[dof[r]];
+      vanka_local_solve(dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
+      for (int r = 0; r < sz; ++r) {
         upd[dof[r]] += damp * loc[r];
         cnt[dof[r]] += 1;
       }
     }
     for (int i = 0; i < n; ++i)
       if (cnt[i] != 0) x[i] += upd[i] / cnt[i];
-    free(res); free(upd); free(cnt);
+    free(res); free(upd); free(cnt); free(loc);
     return;
   }
   if (type == 0) {
     for (int p = 0; p < n_patches; ++p) {
-      const int* dof = patch + (size_t)p * VP;
-      vanka_local_rhs(dof, rp, ci, v, b, x, loc);
-      vanka_local_solve(dof, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
-      for (int r = 0; r < VP; ++r) x[dof[r]] += damp * loc[r];
+      const int* dof = patch + PB(p);
+      const int sz = PS(p);
+      vanka_local_rhs(dof, sz, rp, ci, v, b, x, loc);
+      vanka_local_solve(dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
+      for (int r = 0; r < sz; ++r) x[dof[r]] += damp * loc[r];
     }
+    free(loc);
     return;
   }
   /* colour order */
   for (int k = 0; k < n_colors; ++k) {
     const int beg = color_ptr[k], end = color_ptr[k + 1];
-    double* rl = (double*)malloc(sizeof(double) * (size_t)(end - beg) * VP);
-    for (int q = beg; q < end; ++q)
-      vanka_local_rhs(patch + (size_t)color_cells[q] * VP, rp, ci, v, b, x, rl + (size_t)(q - beg) * VP);
+    size_t tot = 0;
+    for (int q = beg; q < end; ++q) tot += (size_t)PS(color_cells[q]);
+    double* rl = (double*)malloc(sizeof(double) * (tot > 0 ? tot : 1));
+    size_t off = 0;
     for (int q = beg; q < end; ++q) {
-      const int cell = color_cells[q];
-      const int* dof = patch + (size_t)cell * VP;
-      double* l = rl + (size_t)(q - beg) * VP;
-      vanka_local_solve(dof, rp, ci, v, n_freeze ? n_freeze[cell] : 0, l);
-      for (int r = 0; r < VP; ++r) x[dof[r]] += damp * l[r];
+      const int p = color_cells[q];
+      vanka_local_rhs(patch + PB(p), PS(p), rp, ci, v, b, x, rl + off);
+      off += (size_t)PS(p);
+    }
+    off = 0;
+    for (int q = beg; q < end; ++q) {
+      const int p = color_cells[q];
+      const int* dof = patch + PB(p);
+      const int sz = PS(p);
+      double* l = rl + off;
+      vanka_local_solve(dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, l);
+      for (int r = 0; r < sz; ++r) x[dof[r]] += damp * l[r];
+      off += (size_t)sz;
     }
     free(rl);
   }
+  free(loc);
+#undef PB
+#undef PS
+}
+
+void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int* rp, const int* ci,
+                     const double* v, const double* b, double* x, double damp, const int* color_ptr,
+                     const int* color_cells, int n_colors, const int* n_freeze) {
+  orc_vanka_sweep_var(type, n_patches, NULL, patch, n, rp, ci, v, b, x, damp, color_ptr, color_cells, n_colors,
+                      n_freeze);
 }
 
 /* ---------------------------------------------------- Stokes assembly ------

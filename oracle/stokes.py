@@ -29,8 +29,15 @@ from . import refsetup
 from .cd import _p, lib as _cd_lib
 
 SM_JAC, SM_DIR, SM_VANKA, SM_VANKA_JAC, SM_VANKA_COLOR = 0, 1, 2, 3, 4
-VANKA_TYPES = {"cell": SM_VANKA, "cell_jacobi": SM_VANKA_JAC, "cell_color": SM_VANKA_COLOR,
-               "direct_solve": SM_DIR, "jacobi": SM_JAC}
+# smoother name -> (code, patches): "cell" patches are the 34 combined DOFs of a
+# cell (VankaType::CELL / CELL_JACOBI), "nodal" patches one pressure DOF with
+# the velocity nodes it couples to through B (VankaType::NODAL). Sweeps: in
+# patch order (the reference), additive with averaged corrections (jacobi),
+# or by colour (the GPU's multiplicative order).
+VANKA_TYPES = {"cell": (SM_VANKA, "cell"), "cell_jacobi": (SM_VANKA_JAC, "cell"),
+               "cell_color": (SM_VANKA_COLOR, "cell"), "nodal": (SM_VANKA, "nodal"),
+               "nodal_jacobi": (SM_VANKA_JAC, "nodal"), "nodal_color": (SM_VANKA_COLOR, "nodal"),
+               "direct_solve": (SM_DIR, None), "jacobi": (SM_JAC, None)}
 
 
 def lib() -> C.CDLL:
@@ -41,7 +48,8 @@ def lib() -> C.CDLL:
         L.orc_assemble_stokes.restype = i32
         L.orc_vanka_sweep.argtypes = [i32, i32, vp, i32, vp, vp, vp, vp, vp, f64, vp, vp, i32, vp]
         L.orc_mg_set_smoothers.argtypes = [vp, i32, i32, f64]
-        L.orc_mg_set_vanka.argtypes = [vp, i32, vp, vp, vp, vp, i32, vp, vp, i32, vp]
+        L.orc_mg_set_vanka.argtypes = [vp, i32, vp, vp, vp, vp, i32, vp, vp, i32, vp, vp]
+        L.orc_vanka_sweep_var.argtypes = [i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, f64, vp, vp, i32, vp]
         L.orc_mg_finalize.argtypes = [vp]
         L.orc_mg_finalize.restype = i32
         L.orc_mg_set_transfer_block.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp,
@@ -177,6 +185,48 @@ class StokesLevel:
         self.n_colors = n_colors
 
 
+def _greedy_colours(members: list, n_shared: int):
+    """greedy colouring in patch order: the smallest colour not used by an
+    earlier patch sharing an entry of `members` (arrays of shared ids)"""
+    owners = [[] for _ in range(n_shared)]
+    for p, mem in enumerate(members):
+        for d in mem:
+            owners[d].append(p)
+    color = np.full(len(members), -1, dtype=np.int64)
+    n_colors = 0
+    for p, mem in enumerate(members):
+        used = {color[q] for d in mem for q in owners[d] if q < p}
+        col = 0
+        while col in used:
+            col += 1
+        color[p] = col
+        n_colors = max(n_colors, col + 1)
+    cp = np.zeros(n_colors + 1, dtype=np.int64)
+    np.add.at(cp, color + 1, 1)
+    return (np.cumsum(cp).astype(np.int32), np.argsort(color, kind="stable").astype(np.int32), n_colors)
+
+
+def nodal_patches(lv: "StokesLevel"):
+    """VankaType::NODAL patches (VankaSmoother::set_up_pressure_patches /
+    set_up_velocity_patches, src/Multigrid/VankaSmoother.C:302-420): pressure
+    DOF i with the velocity nodes in row i of the coupling block B1, all three
+    components; returns (ptr, dofs, colour_ptr, colour_patches, n_colours)"""
+    if getattr(lv, "_nodal", None) is None:
+        nu, rp, ci = lv.nu, lv.row_ptr, lv.cols
+        vel, dofs, ptr = [], [], [0]
+        for i in range(lv.np_):
+            r = 3 * nu + i
+            cols = ci[rp[r]:rp[r + 1]]
+            vn = cols[cols < nu]
+            vel.append(vn)
+            dofs.append(np.concatenate([vn + k * nu for k in range(3)] + [np.array([r])]))
+            ptr.append(ptr[-1] + dofs[-1].size)
+        cptr, cpat, nc = _greedy_colours(vel, nu)
+        lv._nodal = (np.array(ptr, dtype=np.int32), np.ascontiguousarray(np.concatenate(dofs), dtype=np.int32),
+                     cptr, cpat, nc)
+    return lv._nodal
+
+
 def stokes_levels(root_n: int, n_refine: int, n_levels: int):
     meshes, parents, scale = refsetup.hierarchy(refsetup.GEO_CUBE_TETRA, root_n, n_refine)
     first = n_refine + 1 - n_levels
@@ -190,10 +240,16 @@ def vanka_sweep(kind: str, lv: StokesLevel, pvals: np.ndarray, b: np.ndarray, x:
     x = np.array(x, dtype=np.float64, copy=True)
     pv = np.ascontiguousarray(pvals, dtype=np.float64)
     b = np.ascontiguousarray(b, dtype=np.float64)
-    t = {"cell": 0, "cell_jacobi": 1, "cell_color": 2}[kind]
-    lib().orc_vanka_sweep(t, lv.n_cells, _p(lv.patch), lv.n, _p(lv.vrow_ptr), _p(lv.vcols), _p(pv), _p(b),
-                          _p(x), damp, _p(lv.color_ptr), _p(lv.color_cells), lv.n_colors,
-                          _p(lv.n_freeze) if freeze else None)
+    code, patches = VANKA_TYPES[kind]
+    t = {SM_VANKA: 0, SM_VANKA_JAC: 1, SM_VANKA_COLOR: 2}[code]
+    if patches == "cell":
+        args = (lv.n_cells, None, _p(lv.patch), lv.n, _p(lv.vrow_ptr), _p(lv.vcols), _p(pv), _p(b), _p(x), damp,
+                _p(lv.color_ptr), _p(lv.color_cells), lv.n_colors, _p(lv.n_freeze) if freeze else None)
+    else:
+        ptr, dofs, cptr, cpat, nc = nodal_patches(lv)
+        args = (lv.np_, _p(ptr), _p(dofs), lv.n, _p(lv.vrow_ptr), _p(lv.vcols), _p(pv), _p(b), _p(x), damp,
+                _p(cptr), _p(cpat), nc, None)
+    lib().orc_vanka_sweep_var(t, *args)
     return x
 
 
@@ -236,13 +292,21 @@ class OracleStokes:
         coarse_direct = coarse_smoother == "direct_solve"
         mg = L.orc_mg_create(nl, n_pre, n_post, 1.0, correction_damp, {"V": 0, "W": 1, "F": 2}[cycle],
                              int(coarse_direct), coarse_max_it, coarse_residual)
-        L.orc_mg_set_smoothers(mg, VANKA_TYPES[smoother], VANKA_TYPES[coarse_smoother], vanka_damp)
+        (fine_code, fine_kind), (coarse_code, coarse_kind) = VANKA_TYPES[smoother], VANKA_TYPES[coarse_smoother]
+        L.orc_mg_set_smoothers(mg, fine_code, coarse_code, vanka_damp)
         keep = []
         for l in range(nl):
             lv = self.levels[off + l]
             L.orc_mg_set_level(mg, l, lv.n, _p(lv.active), _p(lv.row_ptr), _p(lv.cols), _p(self.vals[off + l]))
-            L.orc_mg_set_vanka(mg, l, _p(lv.vrow_ptr), _p(lv.vcols), _p(self.pvals[off + l]), _p(lv.patch),
-                               lv.n_cells, _p(lv.color_ptr), _p(lv.color_cells), lv.n_colors, _p(lv.n_freeze))
+            kind = coarse_kind if l == 0 else fine_kind
+            if kind == "nodal":
+                ptr, dofs, cptr, cpat, nc = nodal_patches(lv)
+                L.orc_mg_set_vanka(mg, l, _p(lv.vrow_ptr), _p(lv.vcols), _p(self.pvals[off + l]), _p(dofs), lv.np_,
+                                   _p(cptr), _p(cpat), nc, None, _p(ptr))
+            else:
+                L.orc_mg_set_vanka(mg, l, _p(lv.vrow_ptr), _p(lv.vcols), _p(self.pvals[off + l]), _p(lv.patch),
+                                   lv.n_cells, _p(lv.color_ptr), _p(lv.color_cells), lv.n_colors, _p(lv.n_freeze),
+                                   None)
         for l in range(nl - 1):
             cl, fl = self.levels[off + l], self.levels[off + l + 1]
             cv = np.ascontiguousarray(cl.verts)

@@ -1,0 +1,105 @@
+"""Stokes P2/P1 (Taylor-Hood on tetrahedra) through the GPU library against the
+oracle: the combined system from assembly, the multigrid preconditioner with
+Vanka smoothers, and FGMRES iterates.
+
+The pressure of the all-Dirichlet Stokes system is determined up to a
+constant; solutions are compared after removing the pressure mean."""
+import numpy as np
+import pytest
+
+import mymoonmd_gb300 as m
+from oracle import stokes as ost
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def stokes_db(n_levels, smoother, damp, coarse="direct_solve", pre=1, post=1, max_it=30, reduction=1e-10,
+              precision="fp64", restart=30):
+    db = m.ParameterDatabase.solve_path_database()
+    db["solver_type"] = "iterative"
+    db["iterative_solver_type"] = "fgmres"
+    db["preconditioner"] = "multigrid"
+    db["residual_tolerance"] = 0.0
+    db["residual_reduction"] = reduction
+    db["max_n_iterations"] = max_it
+    db["gmres_restart"] = restart
+    db["multigrid_n_levels"] = n_levels
+    db["multigrid_smoother"] = smoother
+    db["multigrid_smoother_coarse"] = coarse
+    db["multigrid_vanka_damp_factor"] = damp
+    db["multigrid_n_pre_smooth"] = pre
+    db["multigrid_n_post_smooth"] = post
+    db["gpu_precision"] = precision
+    return db
+
+
+def make_pair(ctx, root, nref, nlev, db, nu=1.0):
+    disc = m.Discretization(m.GEO_CUBE_TETRA, root, nref, nlev, m.KIND_STOKES, 12)
+    prob = m.StokesProblem(ctx, disc, nu, db)
+    prob.assemble()
+    ora = ost.OracleStokes(root, nref, nlev, nu)
+    ora.assemble()
+    return disc, prob, ora
+
+
+def split(x, lv):
+    """velocity and mean-free pressure of a combined vector"""
+    p = x[3 * lv.nu:]
+    return x[: 3 * lv.nu], p - p.mean()
+
+
+@pytest.mark.parametrize("nu", [1.0, 0.01])
+@pytest.mark.parametrize("root,nref", [(1, 2), (2, 1)])
+def test_stokes_assembly_matches_oracle(ctx, root, nref, nu):
+    nlev = nref + 1
+    disc, prob, ora = make_pair(ctx, root, nref, nlev, stokes_db(nlev, "cell_vanka_jacobi", 0.8), nu)
+    for l in range(nlev):
+        assert rel(prob.matrix(l).values(), ora.vals[l]) <= 1e-13, l
+    assert rel(prob.rhs(), ora.rhs[-1]) <= 1e-13
+
+
+VANKA = [
+    # library smoother, oracle sweep, damping
+    ("cell_vanka_jacobi", "cell_jacobi", 0.8),
+    ("cell_vanka", "cell_color", 1.0),
+]
+
+
+@pytest.mark.parametrize("smoother,okind,damp", VANKA)
+def test_stokes_multigrid_cycle_matches_oracle(ctx, smoother, okind, damp):
+    """one V(1,1) cycle on three levels (coarse direct solve on the projected
+    matrix); includes the cells whose pressures are frozen"""
+    db = stokes_db(3, smoother, damp)
+    disc, prob, ora = make_pair(ctx, 1, 3, 3, db)
+    prob.solve()  # builds the hierarchy
+    ora.build_mg(smoother=okind, vanka_damp=damp, n_pre=1, n_post=1)
+    assert ora.finest.n_freeze.max() == 4  # the singular cells are part of the case
+    z = np.random.default_rng(7).standard_normal(ora.finest.n)
+    zd = m.DeviceVector.from_numpy(ctx, z)
+    rd = m.DeviceVector(ctx, z.size)
+    prob.solver().apply_preconditioner(zd, rd)
+    ref = ora.mg_apply(z)
+    assert rel(rd.numpy(), ref) <= 1e-10
+
+
+@pytest.mark.parametrize("smoother,okind,damp", VANKA)
+def test_stokes_fgmres_iterates_match_oracle(ctx, smoother, okind, damp):
+    """eight FGMRES iterations: residual history and iterate (cell Vanka on a
+    continuous pressure converges slowly; the iterates are compared, not a
+    converged solution)"""
+    db = stokes_db(2, smoother, damp, max_it=8)
+    disc, prob, ora = make_pair(ctx, 1, 2, 2, db)
+    prob.solve()
+    hist = prob.solver().residual_history()
+    ora.build_mg(smoother=okind, vanka_damp=damp, n_pre=1, n_post=1)
+    sol, oit, ores, ohist, st = ora.solve(reduction=1e-10, max_it=8, restart=30)
+    assert prob.last_info()[0] == oit == 8
+    n = min(hist.size, ohist.size)
+    assert n >= 8 and rel(hist[:n], ohist[:n]) <= 1e-9
+    u, p = split(prob.solution(), ora.finest)
+    ou, op = split(sol, ora.finest)
+    assert rel(u, ou) <= 1e-9 and rel(p, op) <= 1e-9
