@@ -44,6 +44,15 @@ WORKLOADS = {
                         b=(1.0, 0.0, 0.0), quad=3, restart=20, reduction=1e-10,
                         desc="2D Q1 convection-diffusion, 128^2 quadrilaterals (16,641 DOFs), "
                              "FGMRES(20) + MG V(2,2) Jacobi(0.8), 4 levels, to 1e-10"),
+    # Stokes P2/P1 on 24^3 cubes x 6 tetrahedra; nodal Vanka (cell Vanka is
+    # singular on the cells along the cube edges and converges poorly with a
+    # continuous pressure)
+    "stokes3d_p2p1_24": dict(kind="stokes", geometry=2, root_n=3, n_refine=3, n_levels=3, elem=12, nu=1.0,
+                             restart=30, reduction=1e-8, smoother="nodal_vanka", damp=1.0, pre=1, post=1,
+                             sample=dict(root_n=3, n_refine=2, n_levels=3),
+                             desc="3D Stokes P2/P1, 24^3 cubes x 6 tetrahedra (352,947 velocity + 15,625 "
+                                  "pressure DOFs), FGMRES(30) + MG V(1,1) nodal Vanka (colour order), "
+                                  "3 levels, coarse direct, to 1e-8"),
 }
 
 
@@ -58,11 +67,12 @@ def solver_db(w, precision):
     db["max_n_iterations"] = 500
     db["gmres_restart"] = w["restart"]
     db["multigrid_n_levels"] = w["n_levels"]
-    db["multigrid_smoother"] = "jacobi"
+    db["multigrid_smoother"] = w.get("smoother", "jacobi")
     db["multigrid_smoother_coarse"] = "direct_solve"
     db["jacobi_damp"] = 0.8
-    db["multigrid_n_pre_smooth"] = 2
-    db["multigrid_n_post_smooth"] = 2
+    db["multigrid_vanka_damp_factor"] = w.get("damp", 1.0)
+    db["multigrid_n_pre_smooth"] = w.get("pre", 2)
+    db["multigrid_n_post_smooth"] = w.get("post", 2)
     db["gpu_precision"] = precision
     return db
 
@@ -165,14 +175,23 @@ def run_ours(args, w, rank, world, local, pg):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
 
     ctx = m.Context(local)
-    disc = m.Discretization(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"], m.KIND_CD, w["elem"])
-    cf = m.cd_coeffs(w["eps"], w["b"], 0.0, True)
+    stokes = w.get("kind") == "stokes"
+    disc = m.Discretization(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"],
+                            m.KIND_STOKES if stokes else m.KIND_CD, w["elem"])
+    cf = None if stokes else m.cd_coeffs(w["eps"], w["b"], 0.0, True)
     fin = disc.level_info(w["n_levels"] - 1)
     n_dofs, nnz = fin["n_dofs"], fin["nnz"]
+    if stokes:
+        n_dofs = 3 * n_dofs + disc.level_info(w["n_levels"] - 1, 1)["n_dofs"]
+
+    def make_problem(precision):
+        if stokes:
+            return m.StokesProblem(ctx, disc, w["nu"], solver_db(w, precision))
+        return m.ConvectionDiffusion(ctx, disc, cf, solver_db(w, precision), quad_points=w["quad"])
 
     results = {}
     for precision in ("fp64", "mixed"):
-        prob = m.ConvectionDiffusion(ctx, disc, cf, solver_db(w, precision), quad_points=w["quad"])
+        prob = make_problem(precision)
         for _ in range(args.warmup):
             prob.reset_solution()
             prob.assemble()
@@ -212,8 +231,8 @@ def run_ours(args, w, rank, world, local, pg):
             # every launch, over requests run right after the timed ones (the
             # captured graphs are bypassed while the probe brackets launches)
             # (the dominant kernel only: the FP32 damped Jacobi sweep)
-            ctx.set_option("probe_epilogue", PROBE_EPILOGUE)
-            ctx.set_option("probe_precision", 4)
+            ctx.set_option("probe_epilogue", -1 if stokes else PROBE_EPILOGUE)
+            ctx.set_option("probe_precision", 0 if stokes else 4)
             ctx.probe(nnz)
             for _ in range(min(args.steps, 3)):
                 prob.reset_solution()
@@ -293,6 +312,7 @@ def run_ours(args, w, rank, world, local, pg):
                    "parallelism": f"replicas x{world} (no collective)",
                    "l2": "inputs larger than L2: finest FP64 matrix "
                          f"{(nnz * 12 + n_dofs * 4) / 1e6:.0f} MB > 126 MB L2",
+                   "smoother": w.get("smoother", "jacobi"),
                    "step": "assembly of all levels + FGMRES/MG solve to 1e-8 relative FP64 residual"},
         "dofs_per_s": round(solves_s * n_dofs, 1),
         "fgmres_iterations": mixed["its"][-1],
@@ -311,20 +331,22 @@ def run_ours(args, w, rank, world, local, pg):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": mixed["launches"],
         "roofline": {"bound": "hbm",
-                     "kernel": "csr_kernel<float,float,float,8,16,EPI_JACOBI>: finest-level damped Jacobi "
-                               "sweep in FP32 (the largest share of a mixed request's GPU time)",
+                     "kernel": ("csr_kernel family on the finest combined Stokes matrix (FGMRES SpMV, defects)"
+                                if stokes else
+                                "csr_kernel<float,float,float,8,16,EPI_JACOBI>: finest-level damped Jacobi "
+                                "sweep in FP32 (the largest share of a mixed request's GPU time)"),
                      "achieved": round(achieved, 1) if achieved else None, "peak": hbm_peak,
                      "unit": "GB/s", "frac": round(achieved / hbm_peak, 3) if achieved else None,
                      "traffic": profiled_traffic(args.workload), "algorithmic_bytes_per_launch":
                          round(probe_bytes / n_probe) if n_probe else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
                      "launches_probed": n_probe,
-                     "probe": f"CUDA events around each finest-level FP32 Jacobi sweep over {min(K, 3)} "
+                     "probe": f"CUDA events around each probed finest-level launch over {min(K, 3)} "
                               "requests run right after the timed ones"},
         "clocks": mixed["clocks"],
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w)
+        line["cpu_baseline"] = cpu_baseline(w, n_dofs)
     return line
 
 
@@ -349,6 +371,17 @@ def _oracle_solve(wname):
     """one oracle (CPU) request: assembly of all levels + FGMRES/MG solve"""
     from oracle import cd as ocd
     w = WORKLOADS[wname]
+    if w.get("kind") == "stokes":
+        # the bounded sample: the same family on the 12^3 mesh (three levels)
+        from oracle import stokes as ost
+        smp = w["sample"]
+        o = ost.OracleStokes(smp["root_n"], smp["n_refine"], smp["n_levels"], w["nu"])
+        t0 = time.perf_counter()
+        o.assemble()
+        kind = {"nodal_vanka": "nodal", "nodal_vanka_jacobi": "nodal_jacobi"}[w["smoother"]]
+        o.build_mg(smoother=kind, vanka_damp=w["damp"], n_pre=w["pre"], n_post=w["post"])
+        sol, it, res, hist, st = o.solve(reduction=w["reduction"], max_it=500, restart=w["restart"])
+        return time.perf_counter() - t0, it, st, o.finest.n
     o = ocd.OracleCD(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"], w["elem"], w["eps"], w["b"],
                      0.0, w["quad"])
     t0 = time.perf_counter()
@@ -356,15 +389,22 @@ def _oracle_solve(wname):
     o.build_mg(2, 2, 0.8, 1.0, "V")
     sol, it, res, hist, st = o.solve("fgmres", 0.0, w["reduction"], 500, 0, w["restart"])
     dt = time.perf_counter() - t0
-    return dt, it, st
+    return dt, it, st, o.finest.n_dofs
 
 
-def cpu_baseline(w):
+def cpu_baseline(w, n_dofs):
     wname = [k for k, v in WORKLOADS.items() if v is w][0]
-    dt, it, st = _oracle_solve(wname)
-    return {"value": round(1.0 / dt, 5), "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": f"one full request (assembly of all levels + FGMRES/MG solve, {it} iterations) "
-                      f"of the same workload by the C restatement in oracle/, single thread, {dt:.1f} s"}
+    dt, it, st, n_sample = _oracle_solve(wname)
+    if n_sample == n_dofs:
+        return {"value": round(1.0 / dt, 5), "unit": "solves/s", "cores": 1, "kind": "port",
+                "sample": f"one full request (assembly of all levels + FGMRES/MG solve, {it} iterations) "
+                          f"of the same workload by the C restatement in oracle/, single thread, {dt:.1f} s"}
+    # a smaller mesh of the same family, scaled by the DOF ratio (work per
+    # request grows at least linearly with the DOFs, so this overstates the CPU)
+    return {"value": round(n_sample / n_dofs / dt, 6), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"one full request on the 12^3 mesh of the same family ({n_sample} DOFs, {it} "
+                      f"iterations, {dt:.1f} s single thread, C restatement in oracle/), scaled by "
+                      f"{n_sample}/{n_dofs} DOFs"}
 
 
 def run_reference(args, w, rank, world):
@@ -380,11 +420,21 @@ def run_reference(args, w, rank, world):
         for _ in range(warm):
             pool.map(_oracle_solve, [wname] * cores)
         t0 = time.perf_counter()
-        its = []
+        its, n_sample = [], 0
         for _ in range(steps):
-            its += [r[1] for r in pool.map(_oracle_solve, [wname] * cores)]
+            rs = pool.map(_oracle_solve, [wname] * cores)
+            its += [r[1] for r in rs]
+            n_sample = rs[0][3]
         dt = time.perf_counter() - t0
     value = steps * cores / dt
+    scale_note = ""
+    if w.get("kind") == "stokes":
+        # the CPU runs the 12^3 mesh of the family; scaled to the 24^3 workload by DOFs
+        import mymoonmd_gb300 as m
+        d = m.Discretization(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"], m.KIND_STOKES, w["elem"])
+        n_full = 3 * d.level_info(w["n_levels"] - 1)["n_dofs"] + d.level_info(w["n_levels"] - 1, 1)["n_dofs"]
+        value *= n_sample / n_full
+        scale_note = f"; requests on the 12^3 mesh ({n_sample} DOFs) scaled by {n_sample}/{n_full} DOFs"
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "solves/s", "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": round(dt / steps * 1e3, 1), "higher_is_better": True,
@@ -395,7 +445,7 @@ def run_reference(args, w, rank, world):
                          "sample": f"{steps} step(s) (of {args.steps} requested) of {cores} concurrent full "
                                    f"requests (assembly + FGMRES/MG, {its[-1] if its else 0} iterations), "
                                    "one per host core, C restatement in oracle/ (the reference needs "
-                                   "CMake-generated headers, LAPACK and UMFPACK and is not built)"},
+                                   "CMake-generated headers, LAPACK and UMFPACK and is not built)" + scale_note},
         "e2e": {"value": round(value, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -408,8 +458,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="cd3d_q2_32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--smoother", default=None, help="override the workload's multigrid smoother")
+    ap.add_argument("--damp", type=float, default=None, help="override the Vanka damping factor")
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.smoother:
+        w["smoother"] = args.smoother
+    if args.damp is not None:
+        w["damp"] = args.damp
+    WORKLOADS[args.workload] = w
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank == 0:

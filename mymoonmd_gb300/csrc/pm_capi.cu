@@ -732,6 +732,9 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
     p->stab.upload(c);
     size_t kmax = 0, fmax = 0;
     p->slev.resize(nl);
+    const Params pre = Params::parse(params ? params : "");
+    const bool want_nodal = pre.str("multigrid_smoother", "").rfind("nodal_vanka", 0) == 0 ||
+                            pre.str("multigrid_smoother_coarse", "").rfind("nodal_vanka", 0) == 0;
     for (int l = 0; l < nl; ++l) {
       const DiscLevel& L = D.levels[l];
       pm_matrix* A = new pm_matrix();
@@ -748,6 +751,11 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
       auto vk = std::make_unique<DevVanka>();
       vk->setup(c, L);
       p->vanka.push_back(std::move(vk));
+      if (want_nodal) {
+        auto nv = std::make_unique<DevNodalVanka>();
+        nv->setup(c, L);
+        p->nodal.push_back(std::move(nv));
+      }
       kmax = std::max(kmax, size_t(L.n_cells) * L.elem_stride);
       fmax = std::max(fmax, size_t(L.n_cells) * L.rhs_stride);
     }
@@ -778,6 +786,7 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
         if (rc != PM_OK) throw Error(rc, c->last_error);
         p->solver->mg.levels[l].proj = p->proj[dl].get();
         p->solver->mg.levels[l].vanka = p->vanka[dl].get();
+        if (want_nodal) p->solver->mg.levels[l].nodal = p->nodal[dl].get();
       }
     }
   } catch (...) {

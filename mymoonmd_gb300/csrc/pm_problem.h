@@ -19,6 +19,7 @@ struct pm_problem {
   pm::DevStokesTables stab;
   std::vector<std::unique_ptr<pm::ProjectedMatrix>> proj;
   std::vector<std::unique_ptr<pm::DevVanka>> vanka;
+  std::vector<std::unique_ptr<pm::DevNodalVanka>> nodal;  // built when a nodal smoother is chosen
   std::vector<pm_matrix*> mats;
   std::vector<pm::DevAssemblyLevel> alev;
   pm::DevRefTables ref;

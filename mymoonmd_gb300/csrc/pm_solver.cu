@@ -85,6 +85,13 @@ static int smoother_code(const std::string& s) {
   if (s == "direct_solve") return SM_DIRECT;
   if (s == "cell_vanka") return SM_CELL_VANKA;
   if (s == "cell_vanka_jacobi") return SM_CELL_VANKA_JACOBI;
+  // the reference's *_store variants keep the local factorisations; here they
+  // are always kept
+  if (s == "cell_vanka_store") return SM_CELL_VANKA;
+  if (s == "cell_vanka_jacobi_store") return SM_CELL_VANKA_JACOBI;
+  if (s == "nodal_vanka" || s == "nodal_vanka_store") return SM_NODAL_VANKA;
+  // additive nodal Vanka (the CELL_JACOBI treatment on nodal patches)
+  if (s == "nodal_vanka_jacobi") return SM_NODAL_VANKA_JACOBI;
   throw Error(PM_E_UNSUPPORTED, "multigrid smoother '" + s + "' is not implemented on the GPU");
 }
 
@@ -116,11 +123,13 @@ void Multigrid::update(pm_ctx* c) {
     DevCsr& A = lv.A->csr;
     lv.smoother = (l == 0) ? smoother_coarse : smoother;
     const bool vanka = lv.smoother == SM_CELL_VANKA || lv.smoother == SM_CELL_VANKA_JACOBI;
-    if (vanka && (!lv.vanka || !lv.proj))
+    const bool nodal = lv.smoother == SM_NODAL_VANKA || lv.smoother == SM_NODAL_VANKA_JACOBI;
+    if ((vanka && (!lv.vanka || !lv.proj)) || (nodal && (!lv.nodal || !lv.proj)))
       throw Error(PM_E_UNSUPPORTED, "Vanka smoothers need the Stokes problem set-up");
     // get_combined_matrix of this level (values copied from the system matrix)
     if (lv.proj) lv.proj->refresh(c, A, mixed);
     if (vanka) lv.vanka->factor(c, lv.proj->csr, mixed);
+    if (nodal) lv.nodal->factor(c, lv.proj->csr, mixed);
     if (lv.smoother == SM_JACOBI) A.make_diag(c);
     const int n = A.n_rows;
     if (l < L - 1) {
@@ -178,6 +187,12 @@ void Multigrid::smooth(pm_ctx* c, int l) {
   } else if (lv.smoother == SM_CELL_VANKA) {
     if (mixed) lv.vanka->sweep_colored32(c, lv.proj->csr, lv.rhs32.p, lv.cur32, float(vanka_damp));
     else lv.vanka->sweep_colored(c, lv.proj->csr, lv.rhs.p, lv.cur, vanka_damp);
+  } else if (lv.smoother == SM_NODAL_VANKA_JACOBI) {
+    if (mixed) lv.nodal->sweep_jacobi32(c, lv.proj->csr, lv.rhs32.p, lv.cur32, lv.defect32.p, float(vanka_damp));
+    else lv.nodal->sweep_jacobi(c, lv.proj->csr, lv.rhs.p, lv.cur, lv.defect.p, vanka_damp);
+  } else if (lv.smoother == SM_NODAL_VANKA) {
+    if (mixed) lv.nodal->sweep_colored32(c, lv.proj->csr, lv.rhs32.p, lv.cur32, float(vanka_damp));
+    else lv.nodal->sweep_colored(c, lv.proj->csr, lv.rhs.p, lv.cur, vanka_damp);
   }
 }
 

@@ -28,7 +28,10 @@ struct Params {
   long integer(const std::string& k, long def) const;
 };
 
-enum Smoother { SM_JACOBI = 0, SM_DIRECT = 1, SM_CELL_VANKA = 2, SM_CELL_VANKA_JACOBI = 3, SM_NONE = 4 };
+enum Smoother {
+  SM_JACOBI = 0, SM_DIRECT = 1, SM_CELL_VANKA = 2, SM_CELL_VANKA_JACOBI = 3, SM_NONE = 4,
+  SM_NODAL_VANKA = 5, SM_NODAL_VANKA_JACOBI = 6
+};
 enum Dir { DIR_DUMMY = 0, DIR_DOWN = 1, DIR_UP = 2, DIR_END = 3 };
 
 struct MGLevel {
@@ -48,6 +51,7 @@ struct MGLevel {
   // and the cell Vanka data; owned by the problem
   ProjectedMatrix* proj = nullptr;
   DevVanka* vanka = nullptr;
+  DevNodalVanka* nodal = nullptr;
 };
 
 // CycleControl (src/Multigrid/CycleControl.C:17-110)

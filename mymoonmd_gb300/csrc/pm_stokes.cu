@@ -606,3 +606,416 @@ void DevVanka::sweep_colored32(pm_ctx* c, const DevCsr& V, const float* b, float
 }
 
 }  // namespace pm
+
+// ------------------------------------------------------- nodal Vanka -------
+namespace pm {
+
+void DevNodalVanka::setup(pm_ctx* c, const DiscLevel& L) {
+  nu = L.space.n_dofs;
+  np = L.pspace.n_dofs;
+  n = L.sys.n_rows;
+  const pmsetup::Csr& S = L.sys;
+  std::vector<int> vp(np + 1, 0), vi;
+  for (int i = 0; i < np; ++i) {
+    const int r = 3 * nu + i;
+    for (int k = S.row_ptr[r]; k < S.row_ptr[r + 1]; ++k)
+      if (S.cols[k] < nu) vi.push_back(S.cols[k]);  // columns of B1 (sorted)
+    vp[i + 1] = int(vi.size());
+  }
+  max_nodes = 0;
+  std::vector<int64_t> ao(np + 1, 0);
+  for (int i = 0; i < np; ++i) {
+    const int m = vp[i + 1] - vp[i];
+    max_nodes = std::max(max_nodes, m);
+    ao[i + 1] = ao[i] + int64_t(m) * m;
+  }
+  if (max_nodes > kNodalMaxNodes)
+    throw Error(PM_E_UNSUPPORTED, "nodal Vanka patch with " + std::to_string(max_nodes) +
+                                      " velocity nodes exceeds the supported " + std::to_string(kNodalMaxNodes));
+  ainv_len = ao[np];
+  vptr.upload(vp, c->stream);
+  vidx.upload(vi, c->stream);
+  aoff.upload(ao, c->stream);
+  // incidence of the combined DOFs in the local storage
+  std::vector<int> cnt(n, 0);
+  for (int i = 0; i < np; ++i) {
+    for (int k = 0; k < 3; ++k)
+      for (int t = vp[i]; t < vp[i + 1]; ++t) cnt[k * nu + vi[t]]++;
+    cnt[3 * nu + i]++;
+  }
+  std::vector<int> ip(n + 1, 0);
+  for (int d = 0; d < n; ++d) ip[d + 1] = ip[d] + cnt[d];
+  std::vector<int> ix(ip[n]);
+  {
+    std::vector<int> fill(ip.begin(), ip.end() - 1);
+    for (int i = 0; i < np; ++i) {
+      const int m = vp[i + 1] - vp[i], off = 3 * vp[i] + i;
+      for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < m; ++a) ix[fill[k * nu + vi[vp[i] + a]]++] = off + k * m + a;
+      ix[fill[3 * nu + i]++] = off + 3 * m;
+    }
+  }
+  inc_ptr.upload(ip, c->stream);
+  inc_idx.upload(ix, c->stream);
+  count.upload(cnt, c->stream);
+  // greedy colouring in pressure-DOF order: patches of one colour share no
+  // velocity node (and so no DOF)
+  std::vector<int> np_ptr(nu + 1, 0), np_idx(vi.size());
+  for (int v : vi) np_ptr[v + 1]++;
+  for (int v = 0; v < nu; ++v) np_ptr[v + 1] += np_ptr[v];
+  {
+    std::vector<int> fill(np_ptr.begin(), np_ptr.end() - 1);
+    for (int i = 0; i < np; ++i)
+      for (int t = vp[i]; t < vp[i + 1]; ++t) np_idx[fill[vi[t]]++] = i;
+  }
+  std::vector<int> color(np, -1), seen;
+  int n_colors = 0;
+  for (int i = 0; i < np; ++i) {
+    seen.assign(n_colors + 1, 0);
+    for (int t = vp[i]; t < vp[i + 1]; ++t) {
+      const int v = vi[t];
+      for (int e = np_ptr[v]; e < np_ptr[v + 1]; ++e) {
+        const int j = np_idx[e];
+        if (j < i) seen[color[j]] = 1;
+      }
+    }
+    int col = 0;
+    while (col < n_colors && seen[col]) ++col;
+    color[i] = col;
+    if (col == n_colors) ++n_colors;
+  }
+  color_ptr.assign(n_colors + 1, 0);
+  for (int i = 0; i < np; ++i) color_ptr[color[i] + 1]++;
+  for (int k = 0; k < n_colors; ++k) color_ptr[k + 1] += color_ptr[k];
+  std::vector<int> cp(np);
+  {
+    std::vector<int> fill(color_ptr.begin(), color_ptr.end() - 1);
+    for (int i = 0; i < np; ++i) cp[fill[color[i]]++] = i;
+  }
+  color_patches.upload(cp, c->stream);
+  flag.ensure(1);
+}
+
+}  // namespace pm
+
+namespace pm {
+
+static __device__ __forceinline__ int find_sorted(const int* a, int n, int key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < n && a[lo] == key) ? lo : -1;
+}
+
+// one block per pressure DOF: the velocity block of the patch from the
+// projected matrix (non-zero entries only, as the reference copies them),
+// inverted by Gauss-Jordan with partial pivoting in shared memory; then
+// t_k = A^{-1} bt_k and the Schur complement S
+template <class T>
+__global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int* __restrict__ vptr,
+                                                      const int* __restrict__ vidx,
+                                                      const int64_t* __restrict__ aoff,
+                                                      const int* __restrict__ rp, const int* __restrict__ ci,
+                                                      const T* __restrict__ v, T* __restrict__ ainv,
+                                                      T* __restrict__ tb, T* __restrict__ sinv,
+                                                      int* __restrict__ flag) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int i = blockIdx.x;
+  if (i >= np) return;
+  const int m = vptr[i + 1] - vptr[i];
+  const int ld = m + 1;
+  T* M = reinterpret_cast<T*>(smem_raw);
+  T* Inv = M + m * ld;
+  T* bt = Inv + m * ld;  // 3 m
+  T* bv = bt + 3 * m;    // 3 m
+  T* colk = bv + 3 * m;  // m
+  T* tk = colk + m;      // 3 m: t_k = A^{-1} bt_k
+  T* red = tk + 3 * m;   // 32
+  int* nodes = reinterpret_cast<int*>(red + 32);
+  __shared__ int piv_row;
+  __shared__ T cdiag;
+  const int t = threadIdx.x;
+  for (int a = t; a < m; a += blockDim.x) nodes[a] = vidx[vptr[i] + a];
+  for (int e = t; e < m * ld; e += blockDim.x) {
+    M[e] = T(0);
+    Inv[e] = T(0);
+  }
+  for (int e = t; e < 6 * m; e += blockDim.x) bt[e] = T(0);
+  if (t == 0) cdiag = T(0);
+  __syncthreads();
+  const int prow = 3 * nu + i;
+  for (int a = t; a < m; a += blockDim.x) {
+    Inv[a * ld + a] = T(1);
+    const int r = nodes[a];
+    for (int k = rp[r]; k < rp[r + 1]; ++k) {
+      const T val = v[k];
+      if (val == T(0)) continue;
+      const int col = ci[k];
+      if (col < nu) {
+        const int b = find_sorted(nodes, m, col);
+        if (b >= 0) M[a * ld + b] = val;
+      } else if (col == prow) {
+        bt[a] = val;
+      }
+    }
+    for (int comp = 1; comp < 3; ++comp) {
+      const int rr = comp * nu + r;
+      const int k = find_sorted(ci + rp[rr], rp[rr + 1] - rp[rr], prow);
+      if (k >= 0) bt[comp * m + a] = v[rp[rr] + k];
+    }
+  }
+  for (int k = rp[prow] + t; k < rp[prow + 1]; k += blockDim.x) {
+    const T val = v[k];
+    if (val == T(0)) continue;
+    const int col = ci[k];
+    if (col == prow) {
+      cdiag = val;
+    } else if (col < 3 * nu) {
+      const int comp = col / nu, b = find_sorted(nodes, m, col - comp * nu);
+      if (b >= 0) bv[comp * m + b] = val;
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    if (t == 0) {
+      int p = k;
+      T best = fabs(M[k * ld + k]);
+      for (int r = k + 1; r < m; ++r)
+        if (fabs(M[r * ld + k]) > best) {
+          best = fabs(M[r * ld + k]);
+          p = r;
+        }
+      piv_row = p;
+      if (!(best > T(0))) atomicExch(flag, 1);
+    }
+    __syncthreads();
+    const int p = piv_row;
+    if (p != k)
+      for (int j = t; j < m; j += blockDim.x) {
+        T x0 = M[k * ld + j];
+        M[k * ld + j] = M[p * ld + j];
+        M[p * ld + j] = x0;
+        T x1 = Inv[k * ld + j];
+        Inv[k * ld + j] = Inv[p * ld + j];
+        Inv[p * ld + j] = x1;
+      }
+    __syncthreads();
+    const T pv = M[k * ld + k] != T(0) ? M[k * ld + k] : T(1);
+    for (int r = t; r < m; r += blockDim.x) colk[r] = M[r * ld + k];
+    __syncthreads();
+    for (int j = t; j < m; j += blockDim.x) {
+      M[k * ld + j] /= pv;
+      Inv[k * ld + j] /= pv;
+    }
+    __syncthreads();
+    for (int e = t; e < m * m; e += blockDim.x) {
+      const int r = e / m, j = e % m;
+      if (r == k) continue;
+      const T f = colk[r];
+      M[r * ld + j] -= f * M[k * ld + j];
+      Inv[r * ld + j] -= f * Inv[k * ld + j];
+    }
+    __syncthreads();
+  }
+  // t_k = Inv bt_k
+  for (int e = t; e < 3 * m; e += blockDim.x) {
+    const int comp = e / m, a = e % m;
+    T s = T(0);
+    for (int b = 0; b < m; ++b) s += Inv[a * ld + b] * bt[comp * m + b];
+    tk[e] = s;
+  }
+  __syncthreads();
+  // S = c - sum_k b_k . t_k, reduced in a fixed order
+  T part = T(0);
+  for (int e = t; e < 3 * m; e += blockDim.x) part += bv[e] * tk[e];
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((t & 31) == 0) red[t >> 5] = part;
+  __syncthreads();
+  if (t == 0) {
+    T s = T(0);
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) s += red[w];
+    const T S = cdiag - s;
+    if (!(S != T(0))) atomicExch(flag, 1);
+    sinv[i] = S != T(0) ? T(1) / S : T(0);
+  }
+  T* out = ainv + aoff[i];
+  for (int e = t; e < m * m; e += blockDim.x) {
+    const int b = e / m, a = e % m;  // column-major: out[b*m + a] = Inv[a][b]
+    out[e] = Inv[a * ld + b];
+  }
+  T* otb = tb + 6 * size_t(vptr[i]);
+  for (int e = t; e < 3 * m; e += blockDim.x) {
+    otb[e] = tk[e];
+    otb[3 * m + e] = bv[e];
+  }
+}
+
+template <class T>
+static size_t nodal_factor_smem(int m) {
+  return sizeof(T) * (size_t(2) * m * (m + 1) + 10 * size_t(m) + 32) + sizeof(int) * size_t(m);
+}
+
+void DevNodalVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
+  PM_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c->stream));
+  if (fp32) {
+    ainv32.ensure(size_t(ainv_len));
+    tb32.ensure(size_t(6) * vidx.n);
+    sinv32.ensure(np);
+    sol32.ensure(size_t(3) * vidx.n + np);
+    const size_t sm = nodal_factor_smem<float>(max_nodes);
+    PM_CUDA(cudaFuncSetAttribute(k_nodal_factor<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    k_nodal_factor<float><<<np, 256, sm, c->stream>>>(np, nu, vptr.p, vidx.p, aoff.p, V.row_ptr.p, V.cols.p,
+                                                     V.vals32.p, ainv32.p, tb32.p, sinv32.p, flag.p);
+  } else {
+    ainv.ensure(size_t(ainv_len));
+    tb.ensure(size_t(6) * vidx.n);
+    sinv.ensure(np);
+    sol.ensure(size_t(3) * vidx.n + np);
+    const size_t sm = nodal_factor_smem<double>(max_nodes);
+    PM_CUDA(cudaFuncSetAttribute(k_nodal_factor<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    k_nodal_factor<double><<<np, 256, sm, c->stream>>>(np, nu, vptr.p, vidx.p, aoff.p, V.row_ptr.p, V.cols.p,
+                                                      V.vals.p, ainv.p, tb.p, sinv.p, flag.p);
+  }
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+  int h = 0;
+  PM_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  if (h) throw Error(PM_E_BREAKDOWN, "singular local nodal Vanka system");
+}
+
+}  // namespace pm
+
+namespace pm {
+
+// one warp per patch: local residual (gathered from the global residual r or
+// read from rloc), w_k = A^{-1} r_k, p, u_k; the damped correction is written
+// to the local storage (additive sweep) or added into x (colour sweep)
+template <class T>
+__global__ void __launch_bounds__(128) k_nodal_local(int cnt, const int* __restrict__ patches, int nu,
+                                                     const int* __restrict__ vptr, const int* __restrict__ vidx,
+                                                     const int64_t* __restrict__ aoff, const T* __restrict__ ainv,
+                                                     const T* __restrict__ tb, const T* __restrict__ sinv,
+                                                     const T* __restrict__ r, const T* __restrict__ rloc,
+                                                     T* __restrict__ out, T* __restrict__ x, T damp) {
+  __shared__ T rl[4][3 * kNodalMaxNodes + 1];
+  __shared__ T w[4][3 * kNodalMaxNodes];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int idx = blockIdx.x * 4 + wi;
+  if (idx >= cnt) return;  // uniform per warp; no block-wide barrier below
+  const int i = patches ? patches[idx] : idx;
+  const int m = vptr[i + 1] - vptr[i];
+  const int* nodes = vidx + vptr[i];
+  const size_t off = 3 * size_t(vptr[i]) + i;
+  for (int e = lane; e < 3 * m + 1; e += 32) {
+    T val;
+    if (rloc) {
+      val = rloc[off + e];
+    } else {
+      const int g = e < 3 * m ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
+      val = r[g];
+    }
+    rl[wi][e] = val;
+  }
+  __syncwarp();
+  const T* A = ainv + aoff[i];
+  for (int a = lane; a < m; a += 32) {
+    T s0 = T(0), s1 = T(0), s2 = T(0);
+    for (int b = 0; b < m; ++b) {
+      const T q = A[size_t(b) * m + a];
+      s0 += q * rl[wi][b];
+      s1 += q * rl[wi][m + b];
+      s2 += q * rl[wi][2 * m + b];
+    }
+    w[wi][a] = s0;
+    w[wi][m + a] = s1;
+    w[wi][2 * m + a] = s2;
+  }
+  __syncwarp();
+  const T* t = tb + 6 * size_t(vptr[i]);
+  const T* bb = t + 3 * m;
+  T part = T(0);
+  for (int e = lane; e < 3 * m; e += 32) part += bb[e] * w[wi][e];
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  part = __shfl_sync(0xffffffffu, part, 0);  // one value for every lane
+  const T p = sinv[i] * (rl[wi][3 * m] - part);
+  for (int e = lane; e < 3 * m; e += 32) {
+    const T u = damp * (w[wi][e] - t[e] * p);
+    if (x) x[(e / m) * nu + nodes[e % m]] += u;
+    else out[off + e] = u;
+  }
+  if (lane == 0) {
+    if (x) x[3 * nu + i] += damp * p;
+    else out[off + 3 * m] = damp * p;
+  }
+}
+
+// local residuals b - V x of the patches of one colour (one warp per patch)
+template <class T>
+__global__ void __launch_bounds__(128) k_nodal_rhs(int cnt, const int* __restrict__ patches, int nu,
+                                                   const int* __restrict__ vptr, const int* __restrict__ vidx,
+                                                   const int* __restrict__ rp, const int* __restrict__ ci,
+                                                   const T* __restrict__ v, const T* __restrict__ b,
+                                                   const T* __restrict__ x, T* __restrict__ rloc) {
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int idx = blockIdx.x * 4 + wi;
+  if (idx >= cnt) return;
+  const int i = patches[idx];
+  const int m = vptr[i + 1] - vptr[i];
+  const int* nodes = vidx + vptr[i];
+  const size_t off = 3 * size_t(vptr[i]) + i;
+  for (int e = lane; e < 3 * m + 1; e += 32) {
+    const int g = e < 3 * m ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
+    T s = b[g];
+    for (int k = rp[g]; k < rp[g + 1]; ++k) s -= v[k] * x[ci[k]];
+    rloc[off + e] = s;
+  }
+}
+
+template <class T>
+static void nodal_jacobi(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T* ainv, const T* tb, const T* sinv,
+                         T* sol, const T* b, T* x, T* r, T damp) {
+  if constexpr (sizeof(T) == 8) csr_apply(c, V, EPI_DEFECT, x, r, b, 1.0);
+  else csr_apply32(c, V, EPI_DEFECT, x, r, b, 1.0f);
+  k_nodal_local<T><<<(nv.np + 3) / 4, 128, 0, c->stream>>>(nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
+                                                          ainv, tb, sinv, r, nullptr, sol, nullptr, damp);
+  const int g = std::max(1, std::min((nv.n + 255) / 256, c->num_sms * 16));
+  k_vanka_average<T><<<g, 256, 0, c->stream>>>(nv.n, nv.inc_ptr.p, nv.inc_idx.p, nv.count.p, sol, x);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 2;
+}
+
+template <class T>
+static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T* vals, const T* ainv, const T* tb,
+                          const T* sinv, T* rloc, const T* b, T* x, T damp) {
+  const int ncol = int(nv.color_ptr.size()) - 1;
+  for (int k = 0; k < ncol; ++k) {
+    const int beg = nv.color_ptr[k], cnt = nv.color_ptr[k + 1] - beg;
+    if (!cnt) continue;
+    const int* pts = nv.color_patches.p + beg;
+    k_nodal_rhs<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
+                                                        V.cols.p, vals, b, x, rloc);
+    k_nodal_local<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
+                                                          tb, sinv, nullptr, rloc, nullptr, x, damp);
+    c->kernel_launches += 2;
+  }
+  PM_CHECK_LAUNCH();
+}
+
+void DevNodalVanka::sweep_jacobi(pm_ctx* c, const DevCsr& V, const double* b, double* x, double* r, double damp) {
+  nodal_jacobi<double>(c, *this, V, ainv.p, tb.p, sinv.p, sol.p, b, x, r, damp);
+}
+void DevNodalVanka::sweep_jacobi32(pm_ctx* c, const DevCsr& V, const float* b, float* x, float* r, float damp) {
+  nodal_jacobi<float>(c, *this, V, ainv32.p, tb32.p, sinv32.p, sol32.p, b, x, r, damp);
+}
+void DevNodalVanka::sweep_colored(pm_ctx* c, const DevCsr& V, const double* b, double* x, double damp) {
+  nodal_colored<double>(c, *this, V, V.vals.p, ainv.p, tb.p, sinv.p, sol.p, b, x, damp);
+}
+void DevNodalVanka::sweep_colored32(pm_ctx* c, const DevCsr& V, const float* b, float* x, float damp) {
+  nodal_colored<float>(c, *this, V, V.vals32.p, ainv32.p, tb32.p, sinv32.p, sol32.p, b, x, damp);
+}
+
+}  // namespace pm

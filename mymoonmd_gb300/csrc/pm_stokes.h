@@ -71,4 +71,45 @@ struct DevVanka {
   void sweep_colored32(pm_ctx* c, const DevCsr& V, const float* b, float* x, float damp);
 };
 
+// nodal Vanka (VankaType::NODAL, src/Multigrid/VankaSmoother.C:302-420): one
+// patch per pressure DOF i, holding i and, in all three velocity components,
+// the velocity nodes of row i of the coupling block B1. The local system
+//   A u_k + bt_k p = r_k (k = 0, 1, 2),   sum_k b_k . u_k + c p = r_p
+// is solved through the Schur complement of its single pressure:
+//   w_k = A^{-1} r_k,  p = (r_p - sum_k b_k . w_k) / S,  u_k = w_k - t_k p,
+//   t_k = A^{-1} bt_k, S = c - sum_k b_k . t_k,
+// with one stored inverse A^{-1} of the velocity block (the three diagonal
+// blocks are the same matrix in the Laplace-form Stokes system; the
+// off-diagonal velocity blocks are zero). The reference factorises the whole
+// (3n+1) x (3n+1) local matrix with LAPACK; the solution is the same up to
+// rounding.
+constexpr int kNodalMaxNodes = 96;
+
+struct DevNodalVanka {
+  int np = 0, nu = 0, n = 0, max_nodes = 0;
+  int64_t ainv_len = 0;
+  DBuf<int> vptr, vidx;      // per pressure DOF: velocity nodes (sorted)
+  DBuf<int64_t> aoff;        // offsets of the n_i x n_i inverses
+  DBuf<double> ainv;         // column-major inverses of the velocity blocks
+  DBuf<float> ainv32;
+  DBuf<double> tb;           // per patch at 6 vptr[i]: t_0, t_1, t_2, b_0, b_1, b_2 (n_i each)
+  DBuf<float> tb32;
+  DBuf<double> sinv;         // 1 / S per patch
+  DBuf<float> sinv32;
+  DBuf<int> inc_ptr, inc_idx, count;  // per combined DOF: positions in the local storage
+  std::vector<int> color_ptr;          // host: colour ranges into color_patches
+  DBuf<int> color_patches;
+  DBuf<double> sol;  // local corrections / residuals: patch i at 3 vptr[i] + i, 3 n_i + 1 entries
+  DBuf<float> sol32;
+  DBuf<int> flag;
+  void setup(pm_ctx* c, const DiscLevel& L);
+  void factor(pm_ctx* c, const DevCsr& V, bool fp32);
+  // additive sweep: x += average of damp * local corrections from one residual
+  void sweep_jacobi(pm_ctx* c, const DevCsr& V, const double* b, double* x, double* r, double damp);
+  void sweep_jacobi32(pm_ctx* c, const DevCsr& V, const float* b, float* x, float* r, float damp);
+  // multiplicative sweep, patches grouped by colour
+  void sweep_colored(pm_ctx* c, const DevCsr& V, const double* b, double* x, double damp);
+  void sweep_colored32(pm_ctx* c, const DevCsr& V, const float* b, float* x, float damp);
+};
+
 }  // namespace pm

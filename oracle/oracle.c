@@ -528,9 +528,13 @@ typedef struct {
   const int *color_ptr, *color_cells;
   int n_colors;
   const int* n_freeze;
+  void* store; /* stored local factorisations */
 } orc_level;
 
 enum { SM_JAC = 0, SM_DIR = 1, SM_VANKA = 2, SM_VANKA_JAC = 3, SM_VANKA_COLOR = 4 };
+
+void* orc_vanka_store_create(int n_patches);
+void orc_vanka_store_destroy(void* st);
 
 typedef struct {
   int n_levels;
@@ -623,6 +627,8 @@ void orc_mg_set_vanka(orc_mg* m, int l, const int* vrp, const int* vci, const do
   L->patch = patch; L->n_patches = n_patches; L->patch_ptr = patch_ptr;
   L->color_ptr = color_ptr; L->color_cells = color_cells; L->n_colors = n_colors;
   L->n_freeze = n_freeze;
+  orc_vanka_store_destroy(L->store);
+  L->store = orc_vanka_store_create(n_patches);
 }
 
 /* DirectSolver on get_combined_matrix of the coarsest level: the projected
@@ -673,6 +679,7 @@ void orc_mg_destroy(orc_mg* m) {
     orc_level* L = &m->lv[l];
     free(L->active); free(L->rhs); free(L->sol); free(L->defect); free(L->diag);
     free(L->lu); free(L->piv);
+    orc_vanka_store_destroy(L->store);
   }
   free(m->lv);
   free(m->control);
@@ -687,7 +694,9 @@ static double calc_defect(orc_level* L) {
 
 void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* patch, int n, const int* rp,
                          const int* ci, const double* v, const double* b, double* x, double damp,
-                         const int* color_ptr, const int* color_cells, int n_colors, const int* n_freeze);
+                         const int* color_ptr, const int* color_cells, int n_colors, const int* n_freeze,
+                         void* store);
+
 
 static void smooth(orc_mg* m, int l) {
   orc_level* L = &m->lv[l];
@@ -700,7 +709,7 @@ static void smooth(orc_mg* m, int l) {
   if (code == SM_VANKA || code == SM_VANKA_JAC || code == SM_VANKA_COLOR) {
     orc_vanka_sweep_var(code == SM_VANKA ? 0 : code == SM_VANKA_JAC ? 1 : 2, L->n_patches, L->patch_ptr, L->patch, L->n, L->vrp,
                     L->vci, L->vv, L->rhs, L->sol, m->vanka_damp, L->color_ptr, L->color_cells, L->n_colors,
-                    L->n_freeze);
+                    L->n_freeze, L->store);
     return;
   }
   /* JacobiSmoother::smooth */
@@ -1061,16 +1070,56 @@ static void vanka_local_matrix(const int* dof, int sz, const int* rp, const int*
   }
 }
 
-static void vanka_local_solve(const int* dof, int sz, const int* rp, const int* ci, const double* v, int nf,
-                              double* loc) {
-  double* M = (double*)malloc(sizeof(double) * (size_t)sz * sz);
-  int* piv = (int*)malloc(sizeof(int) * (size_t)sz);
-  vanka_local_matrix(dof, sz, rp, ci, v, nf, M);
-  orc_lu_factor(sz, M, piv);
+/* stored local factorisations (the reference's *_store Vanka variants; the
+ * factors do not change while the matrix is the same, so results agree with
+ * refactorising every sweep) */
+typedef struct {
+  int n_patches;
+  double** lu;
+  int** piv;
+} orc_vanka_store;
+
+static orc_vanka_store* vanka_store_new(int n_patches) {
+  orc_vanka_store* st = (orc_vanka_store*)calloc(1, sizeof(orc_vanka_store));
+  st->n_patches = n_patches;
+  st->lu = (double**)calloc((size_t)n_patches, sizeof(double*));
+  st->piv = (int**)calloc((size_t)n_patches, sizeof(int*));
+  return st;
+}
+
+static void vanka_store_free(orc_vanka_store* st) {
+  if (!st) return;
+  for (int p = 0; p < st->n_patches; ++p) {
+    free(st->lu[p]);
+    free(st->piv[p]);
+  }
+  free(st->lu);
+  free(st->piv);
+  free(st);
+}
+
+static void vanka_local_solve(orc_vanka_store* st, int p, const int* dof, int sz, const int* rp, const int* ci,
+                              const double* v, int nf, double* loc) {
+  double* M;
+  int* piv;
+  if (st && st->lu[p]) {
+    M = st->lu[p];
+    piv = st->piv[p];
+  } else {
+    M = (double*)malloc(sizeof(double) * (size_t)sz * sz);
+    piv = (int*)malloc(sizeof(int) * (size_t)sz);
+    vanka_local_matrix(dof, sz, rp, ci, v, nf, M);
+    orc_lu_factor(sz, M, piv);
+  }
   orc_lu_solve(sz, M, piv, loc);
   for (int f = sz - nf; f < sz; ++f) loc[f] = 0.0;
-  free(M);
-  free(piv);
+  if (st) {
+    st->lu[p] = M;
+    st->piv[p] = piv;
+  } else {
+    free(M);
+    free(piv);
+  }
 }
 
 static void vanka_local_rhs(const int* dof, int sz, const int* rp, const int* ci, const double* v, const double* b,
@@ -1087,7 +1136,9 @@ static void vanka_local_rhs(const int* dof, int sz, const int* rp, const int* ci
  * P2/P1 tetrahedra) */
 void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* patch, int n, const int* rp,
                          const int* ci, const double* v, const double* b, double* x, double damp,
-                         const int* color_ptr, const int* color_cells, int n_colors, const int* n_freeze) {
+                         const int* color_ptr, const int* color_cells, int n_colors, const int* n_freeze,
+                         void* store) {
+  orc_vanka_store* st = (orc_vanka_store*)store;
 #define PB(p) (ptr ? ptr[p] : 34 * (p))
 #define PS(p) (ptr ? ptr[(p) + 1] - ptr[p] : 34)
   int maxsz = 0;
@@ -1104,7 +1155,7 @@ void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* pat
       const int* dof = patch + PB(p);
       const int sz = PS(p);
       for (int r = 0; r < sz; ++r) loc[r] = res[dof[r]];
-      vanka_local_solve(dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
+      vanka_local_solve(st, p, dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
       for (int r = 0; r < sz; ++r) {
         upd[dof[r]] += damp * loc[r];
         cnt[dof[r]] += 1;
@@ -1120,7 +1171,7 @@ void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* pat
       const int* dof = patch + PB(p);
       const int sz = PS(p);
       vanka_local_rhs(dof, sz, rp, ci, v, b, x, loc);
-      vanka_local_solve(dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
+      vanka_local_solve(st, p, dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, loc);
       for (int r = 0; r < sz; ++r) x[dof[r]] += damp * loc[r];
     }
     free(loc);
@@ -1144,7 +1195,7 @@ void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* pat
       const int* dof = patch + PB(p);
       const int sz = PS(p);
       double* l = rl + off;
-      vanka_local_solve(dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, l);
+      vanka_local_solve(st, p, dof, sz, rp, ci, v, n_freeze ? n_freeze[p] : 0, l);
       for (int r = 0; r < sz; ++r) x[dof[r]] += damp * l[r];
       off += (size_t)sz;
     }
@@ -1155,11 +1206,14 @@ void orc_vanka_sweep_var(int type, int n_patches, const int* ptr, const int* pat
 #undef PS
 }
 
+void* orc_vanka_store_create(int n_patches) { return vanka_store_new(n_patches); }
+void orc_vanka_store_destroy(void* st) { vanka_store_free((orc_vanka_store*)st); }
+
 void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int* rp, const int* ci,
                      const double* v, const double* b, double* x, double damp, const int* color_ptr,
                      const int* color_cells, int n_colors, const int* n_freeze) {
   orc_vanka_sweep_var(type, n_patches, NULL, patch, n, rp, ci, v, b, x, damp, color_ptr, color_cells, n_colors,
-                      n_freeze);
+                      n_freeze, NULL);
 }
 
 /* ---------------------------------------------------- Stokes assembly ------

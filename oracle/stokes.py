@@ -49,7 +49,7 @@ def lib() -> C.CDLL:
         L.orc_vanka_sweep.argtypes = [i32, i32, vp, i32, vp, vp, vp, vp, vp, f64, vp, vp, i32, vp]
         L.orc_mg_set_smoothers.argtypes = [vp, i32, i32, f64]
         L.orc_mg_set_vanka.argtypes = [vp, i32, vp, vp, vp, vp, i32, vp, vp, i32, vp, vp]
-        L.orc_vanka_sweep_var.argtypes = [i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, f64, vp, vp, i32, vp]
+        L.orc_vanka_sweep_var.argtypes = [i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, f64, vp, vp, i32, vp, vp]
         L.orc_mg_finalize.argtypes = [vp]
         L.orc_mg_finalize.restype = i32
         L.orc_mg_set_transfer_block.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp,
@@ -249,7 +249,7 @@ def vanka_sweep(kind: str, lv: StokesLevel, pvals: np.ndarray, b: np.ndarray, x:
         ptr, dofs, cptr, cpat, nc = nodal_patches(lv)
         args = (lv.np_, _p(ptr), _p(dofs), lv.n, _p(lv.vrow_ptr), _p(lv.vcols), _p(pv), _p(b), _p(x), damp,
                 _p(cptr), _p(cpat), nc, None)
-    lib().orc_vanka_sweep_var(t, *args)
+    lib().orc_vanka_sweep_var(t, *args, None)
     return x
 
 

@@ -67,9 +67,13 @@ VANKA = [
     ("cell_vanka_jacobi", "cell_jacobi", 0.8),
     ("cell_vanka", "cell_color", 1.0),
 ]
+NODAL = [
+    ("nodal_vanka_jacobi", "nodal_jacobi", 0.8),
+    ("nodal_vanka", "nodal_color", 1.0),
+]
 
 
-@pytest.mark.parametrize("smoother,okind,damp", VANKA)
+@pytest.mark.parametrize("smoother,okind,damp", VANKA + NODAL)
 def test_stokes_multigrid_cycle_matches_oracle(ctx, smoother, okind, damp):
     """one V(1,1) cycle on three levels (coarse direct solve on the projected
     matrix); includes the cells whose pressures are frozen"""
@@ -77,7 +81,8 @@ def test_stokes_multigrid_cycle_matches_oracle(ctx, smoother, okind, damp):
     disc, prob, ora = make_pair(ctx, 1, 3, 3, db)
     prob.solve()  # builds the hierarchy
     ora.build_mg(smoother=okind, vanka_damp=damp, n_pre=1, n_post=1)
-    assert ora.finest.n_freeze.max() == 4  # the singular cells are part of the case
+    if okind.startswith("cell"):
+        assert ora.finest.n_freeze.max() == 4  # the singular cells are part of the case
     z = np.random.default_rng(7).standard_normal(ora.finest.n)
     zd = m.DeviceVector.from_numpy(ctx, z)
     rd = m.DeviceVector(ctx, z.size)
@@ -103,3 +108,57 @@ def test_stokes_fgmres_iterates_match_oracle(ctx, smoother, okind, damp):
     u, p = split(prob.solution(), ora.finest)
     ou, op = split(sol, ora.finest)
     assert rel(u, ou) <= 1e-9 and rel(p, op) <= 1e-9
+
+
+@pytest.mark.parametrize("smoother,okind,damp", NODAL)
+def test_stokes_nodal_vanka_solution_matches_oracle(ctx, smoother, okind, damp):
+    """FGMRES(30) with nodal-Vanka V(1,1) multigrid on three levels to 1e-10:
+    iteration counts within one, solutions within 1e-10"""
+    db = stokes_db(3, smoother, damp, max_it=100, reduction=1e-10)
+    disc, prob, ora = make_pair(ctx, 1, 3, 3, db)
+    prob.solve()
+    it, res, init = prob.last_info()
+    ora.build_mg(smoother=okind, vanka_damp=damp, n_pre=1, n_post=1)
+    sol, oit, ores, ohist, st = ora.solve(reduction=1e-10, max_it=100, restart=30)
+    assert st == 0 and oit < 100
+    assert abs(it - oit) <= 1, (it, oit)
+    assert res <= 1e-10 * init
+    u, p = split(prob.solution(), ora.finest)
+    ou, op = split(sol, ora.finest)
+    assert rel(u, ou) <= 1e-10 and rel(p, op) <= 1e-9
+
+
+def test_stokes_mixed_precision_reaches_fp64_target(ctx):
+    """FP32 nodal-Vanka multigrid inside FP64 FGMRES: the FP64 residual reaches
+    1e-8 and the solution agrees with the FP64 oracle"""
+    db = stokes_db(3, "nodal_vanka_jacobi", 0.8, max_it=100, reduction=1e-8, precision="mixed")
+    disc, prob, ora = make_pair(ctx, 1, 3, 3, db)
+    prob.solve()
+    it, res, init = prob.last_info()
+    assert res <= 1e-8 * init and it < 100
+    ora.build_mg(smoother="nodal_jacobi", vanka_damp=0.8, n_pre=1, n_post=1)
+    sol, oit, ores, ohist, st = ora.solve(reduction=1e-10, max_it=100, restart=30)
+    u, p = split(prob.solution(), ora.finest)
+    ou, op = split(sol, ora.finest)
+    assert rel(u, ou) <= 1e-6 and rel(p, op) <= 1e-5
+
+
+def test_stokes_discrete_solution_converges_to_manufactured_solution(ctx):
+    """the discrete velocity approaches u = curl(psi (1,1,1)) under refinement
+    (nodal values; P2 gives at least second order on these meshes)"""
+    errs = []
+    for nref in (2, 3):
+        db = stokes_db(nref + 1, "nodal_vanka", 1.0, max_it=100, reduction=1e-10)
+        disc = m.Discretization(m.GEO_CUBE_TETRA, 1, nref, nref + 1, m.KIND_STOKES, 12)
+        prob = m.StokesProblem(ctx, disc, 1.0, db)
+        prob.assemble()
+        prob.solve()
+        lv = ost.stokes_levels(1, nref, 1)[0]
+        X = lv.ucoords / lv.ucoords.max()
+        x, y, z = X[:, 0], X[:, 1], X[:, 2]
+        S = lambda t: np.sin(np.pi * t) ** 2
+        D = lambda t: np.pi * np.sin(2 * np.pi * t)
+        px, py, pz = D(x) * S(y) * S(z), S(x) * D(y) * S(z), S(x) * S(y) * D(z)
+        exact = np.concatenate([py - pz, pz - px, px - py])
+        errs.append(np.abs(prob.solution()[: 3 * lv.nu] - exact).max())
+    assert errs[1] < errs[0] / 3.5, errs
