@@ -115,9 +115,9 @@ int pm_matrix_get_diagonal(pm_matrix* A, double* diag_dev);
 int pm_matrix_make_fp32(pm_matrix* A);
 int pm_matrix_apply_f32(pm_matrix* A, const float* x_dev, float* y_dev);
 /* Launch shape of the CSR kernels of this matrix (no reference counterpart;
- * tuning only): lanes per row (4, 8, 16, 32) and entries per lane per chunk
- * (2, 4, 8) of the per-row-group kernel; (0, 0) selects the default row-block
- * streaming kernel. */
+ * tuning only): lanes per row (1, 2, 4, 8, 16, 32) and entries per lane per chunk
+ * (2, 4, 8, 16) of the per-row-group kernel (the default); (0, 0) selects the
+ * row-block streaming kernel. */
 int pm_matrix_set_kernel(pm_matrix* A, int lanes, int unroll);
 /* Timed SpMV loop: `reps` applications y = A x on the context's stream, timed
  * with CUDA events; returns ms per application and the algorithmic bytes. */
@@ -271,6 +271,58 @@ int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* coeffs, const double*
 /* Solver statistics of the problem's last solve. */
 int pm_problem_last_info(const pm_problem* p, int* iterations, double* residual,
                          double* initial_residual);
+
+/* ---------------------------------------------------------------------------
+ * Request executor (no reference counterpart: the batched stream and the
+ * serving loop). Independent solves run on one GPU by n_workers host threads,
+ * each with its own context (CUDA stream). A worker keeps the device-resident
+ * problem of every set-up it has served (mesh, spaces, structures, level
+ * matrices, solver and its captured graphs) and reuses it for later requests
+ * with the same set-up; new coefficients are assembled on the device. Set-ups
+ * (host mesh hierarchies) are shared between the workers. The estimated device
+ * footprint of the cached problems is kept under hbm_cap_bytes by evicting the
+ * least recently used ones of the worker that needs room; a problem whose own
+ * footprint exceeds the cap is solved and then released instead of being kept
+ * (0 = no cap). A device allocation failure is reported as PM_E_OOM in the
+ * result. params_cd / params_stokes: the solver parameters of
+ * the two problem kinds (ParameterDatabase text, as pm_solver_create; the
+ * number of multigrid levels comes from the request). */
+typedef struct {
+  int kind;     /* 0 convection-diffusion, 1 Stokes */
+  int geometry; /* as pm_disc_create: 0 square, 1 cube (hexahedra), 2 cube (tetrahedra) */
+  int root_n, n_refine, n_levels, elem;
+  pm_cd_coeffs coeffs; /* convection-diffusion */
+  double nu;           /* Stokes viscosity */
+  double* solution_out; /* host buffer for the finest-level solution, or NULL */
+  uint64_t tag;         /* caller's identifier, returned in the result */
+} pm_request;
+
+typedef struct {
+  uint64_t tag;
+  int status;      /* PM_OK converged; PM_E_MAXIT stopped at the iteration cap; other codes on failure */
+  int iterations;
+  double residual, initial_residual;
+  int n_dofs;
+  int worker;
+  int cache_hit;   /* 1 if the worker's problem for this set-up was reused */
+  double queue_ms; /* submit -> start on a worker (host clock) */
+  double setup_ms; /* set-up and problem creation, 0 on a cache hit */
+  double run_ms;   /* assembly + solve + solution copy */
+  double latency_ms; /* submit -> completion */
+} pm_result;
+
+int pm_server_create(int device, int n_workers, const char* params_cd, const char* params_stokes,
+                     size_t hbm_cap_bytes, pm_server** out);
+void pm_server_destroy(pm_server* s);
+/* enqueue (non-blocking, first in first out) */
+int pm_server_submit(pm_server* s, const pm_request* req);
+/* completed results in completion order; blocks until at least min_results
+ * are available (0 = do not block) and returns at most max_results */
+int pm_server_poll(pm_server* s, pm_result* out, int max_results, int min_results, int* n_out);
+/* blocks until every submitted request has completed */
+int pm_server_drain(pm_server* s);
+/* bytes held by cached problems (estimate), requests served, evictions */
+int pm_server_stats(pm_server* s, size_t* cached_bytes, uint64_t* served, uint64_t* evictions);
 
 #ifdef __cplusplus
 }

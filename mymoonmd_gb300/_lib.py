@@ -40,6 +40,19 @@ class CdCoeffs(C.Structure):
                 ("manufactured", C.c_int), ("f_const", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("geometry", C.c_int), ("root_n", C.c_int), ("n_refine", C.c_int),
+                ("n_levels", C.c_int), ("elem", C.c_int), ("coeffs", CdCoeffs), ("nu", C.c_double),
+                ("solution_out", C.POINTER(C.c_double)), ("tag", C.c_uint64)]
+
+
+class Result(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("status", C.c_int), ("iterations", C.c_int), ("residual", C.c_double),
+                ("initial_residual", C.c_double), ("n_dofs", C.c_int), ("worker", C.c_int),
+                ("cache_hit", C.c_int), ("queue_ms", C.c_double), ("setup_ms", C.c_double),
+                ("run_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
 def _load() -> C.CDLL:
     if not _LIB_PATH.exists():
         raise ImportError(
@@ -125,6 +138,12 @@ _SIGS = {
     "pm_problem_solution_dev": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "pm_problem_run_host": (i32, [vp, C.POINTER(CdCoeffs), vp, vp]),
     "pm_problem_last_info": (i32, [vp, pi32, pf64, pf64]),
+    "pm_server_create": (i32, [i32, i32, C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
+    "pm_server_destroy": (None, [vp]),
+    "pm_server_submit": (i32, [vp, C.POINTER(Request)]),
+    "pm_server_poll": (i32, [vp, C.POINTER(Result), i32, i32, pi32]),
+    "pm_server_drain": (i32, [vp]),
+    "pm_server_stats": (i32, [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "pm_ctx_probe": (i32, [vp, i64]),
     "pm_ctx_probe_result": (i32, [vp, pi32, pf64, pf64]),
 }

@@ -528,6 +528,71 @@ class StokesProblem(ConvectionDiffusion):
         return v["n_dofs"], v["n_active"], p["n_dofs"]
 
 
-__all__ = ["Context", "StokesProblem", "DeviceVector", "FEMatrix", "Solver", "Discretization", "ConvectionDiffusion",
+class Server:
+    """Request executor (pm_server_*): independent convection-diffusion and
+    Stokes solves on one GPU by `n_workers` threads, each with its own stream
+    and a cache of device-resident problems per set-up; the cached footprint is
+    kept under `hbm_cap_bytes` by evicting least recently used problems."""
+
+    def __init__(self, device: int = 0, n_workers: int = 4, db_cd=None, db_stokes=None,
+                 hbm_cap_bytes: int = 150 * 10**9):
+        from ._lib import Request, Result
+        self._Request, self._Result = Request, Result
+        h = C.c_void_p()
+        check(lib.pm_server_create(device, n_workers, _db_text(db_cd).encode() if db_cd is not None else b"",
+                                   _db_text(db_stokes).encode() if db_stokes is not None else b"",
+                                   hbm_cap_bytes, C.byref(h)))
+        self.handle = h
+        self._outputs = {}
+
+    def submit(self, kind: int, geometry: int, root_n: int, n_refine: int, n_levels: int, elem: int,
+               coeffs: Optional[CdCoeffs] = None, nu: float = 1.0, solution_out: Optional[np.ndarray] = None,
+               tag: int = 0) -> None:
+        rq = self._Request()
+        rq.kind, rq.geometry, rq.root_n, rq.n_refine, rq.n_levels, rq.elem = (kind, geometry, root_n, n_refine,
+                                                                           n_levels, elem)
+        if coeffs is not None:
+            rq.coeffs = coeffs
+        rq.nu = nu
+        if solution_out is not None:
+            if solution_out.dtype != np.float64 or not solution_out.flags.c_contiguous:
+                raise TypeError("solution_out must be a contiguous float64 array")
+            rq.solution_out = solution_out.ctypes.data_as(C.POINTER(C.c_double))
+            self._outputs[tag] = solution_out  # kept alive until its result is polled
+        rq.tag = tag
+        check(lib.pm_server_submit(self.handle, C.byref(rq)))
+
+    def poll(self, max_results: int = 1024, min_results: int = 0) -> list:
+        buf = (self._Result * max_results)()
+        n = C.c_int()
+        check(lib.pm_server_poll(self.handle, buf, max_results, min_results, C.byref(n)))
+        out = []
+        for r in buf[: n.value]:
+            d = {f: getattr(r, f) for f, _ in self._Result._fields_}
+            self._outputs.pop(d["tag"], None)
+            out.append(d)
+        return out
+
+    def drain(self) -> None:
+        check(lib.pm_server_drain(self.handle))
+
+    def stats(self) -> dict:
+        b, s, e = C.c_size_t(), C.c_uint64(), C.c_uint64()
+        check(lib.pm_server_stats(self.handle, C.byref(b), C.byref(s), C.byref(e)))
+        return {"cached_bytes": b.value, "served": s.value, "evictions": e.value}
+
+    def close(self) -> None:
+        if self.handle:
+            lib.pm_server_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+__all__ = ["Context", "Server", "StokesProblem", "DeviceVector", "FEMatrix", "Solver", "Discretization", "ConvectionDiffusion",
            "ParameterDatabase", "PmError", "cd_coeffs", "assemble_cd", "GEO_SQUARE_QUAD", "GEO_CUBE_HEXA",
            "GEO_CUBE_TETRA", "KIND_CD", "KIND_STOKES"]

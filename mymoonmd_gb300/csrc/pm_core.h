@@ -31,6 +31,10 @@ struct Error : std::runtime_error {
 #define PM_CHECK_LAUNCH() PM_CUDA(cudaGetLastError())
 
 // device buffer owned by the library
+// device bytes held by DBufs allocated on this host thread (the request
+// executor's footprint estimate of its cached problems)
+inline thread_local int64_t g_thread_dev_bytes = 0;
+
 template <class T>
 struct DBuf {
   T* p = nullptr;
@@ -54,6 +58,7 @@ struct DBuf {
         cudaGetLastError();
         throw Error(PM_E_OOM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed");
       }
+      g_thread_dev_bytes += int64_t(count * sizeof(T));
     }
     n = count;
   }
@@ -62,7 +67,10 @@ struct DBuf {
     if (count != n || (count && !p)) alloc(count);
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_thread_dev_bytes -= int64_t(n * sizeof(T));
+    }
     p = nullptr;
     n = 0;
   }

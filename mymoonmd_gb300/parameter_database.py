@@ -31,12 +31,14 @@ _MG_DEFAULTS: dict[str, tuple[Any, tuple | None]] = {
     "multigrid_n_levels": (2, None),
     "multigrid_type": ("standard", ("standard", "mdml")),
     "multigrid_cycle_type": ("V", ("V", "W", "F")),
+    # the reference's choices, plus "nodal_vanka_jacobi" (additive nodal Vanka,
+    # the CELL_JACOBI treatment on nodal patches), which only this library has
     "multigrid_smoother": ("nodal_vanka", ("jacobi", "sor", "ssor", "nodal_vanka", "cell_vanka",
                                            "patch_vanka", "cell_vanka_jacobi", "nodal_vanka_store",
-                                           "cell_vanka_store", "patch_vanka_store")),
+                                           "cell_vanka_store", "patch_vanka_store", "nodal_vanka_jacobi")),
     "multigrid_smoother_coarse": ("direct_solve", ("direct_solve", "jacobi", "sor", "ssor",
                                                    "nodal_vanka", "cell_vanka", "patch_vanka",
-                                                   "cell_vanka_jacobi")),
+                                                   "cell_vanka_jacobi", "nodal_vanka_jacobi")),
     "multigrid_correction_damp_factor": (1.0, None),
     "multigrid_n_pre_smooth": (1, None),
     "multigrid_n_post_smooth": (1, None),

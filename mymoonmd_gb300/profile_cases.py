@@ -7,6 +7,9 @@
         the finest 32^3 Q2 matrix: two FP64 and two FP32 SpMV launches
     python -m mymoonmd_gb300.profile_cases assembly
         one assembly of the four 32^3 Q2 levels
+    python -m mymoonmd_gb300.profile_cases stokes [--precision ...] [--smoother ...] [--coarse ...]
+        one warm-up request, then one request of the 3D Stokes P2/P1 workload
+        (24^3 cubes x 6 tetrahedra, 368,572 DOFs, 3 levels, V(1,1) Vanka)
 
 Each case prints what it ran; device memory stays below 2 GB.
 """
@@ -47,10 +50,30 @@ def problem(ctx, precision="mixed", n_levels=4):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["request", "spmv", "assembly"])
+    ap.add_argument("case", choices=["request", "spmv", "assembly", "stokes"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--smoother", default="nodal_vanka")
+    ap.add_argument("--coarse", default="direct_solve")
     args = ap.parse_args()
     ctx = m.Context(0)
+    if args.case == "stokes":
+        db = _db(args.precision)
+        db["multigrid_n_levels"] = 3
+        db["multigrid_smoother"] = args.smoother
+        db["multigrid_smoother_coarse"] = args.coarse
+        db["multigrid_vanka_damp_factor"] = 0.8 if args.smoother.endswith("jacobi") else 1.0
+        db["multigrid_n_pre_smooth"] = 1
+        db["multigrid_n_post_smooth"] = 1
+        disc = m.Discretization(m.GEO_CUBE_TETRA, 3, 3, 3, m.KIND_STOKES, 12)
+        prob = m.StokesProblem(ctx, disc, 1.0, db)
+        for _ in range(2):
+            prob.reset_solution()
+            prob.assemble()
+            prob.solve()
+        print("stokes", args.precision, args.smoother, args.coarse, "iterations", prob.last_info()[0])
+        prob.close()
+        ctx.close()
+        return
     disc, prob = problem(ctx, args.precision)
     if args.case == "request":
         for _ in range(2):
