@@ -105,6 +105,9 @@ struct pm_ctx {
   int assembly_quadrature_loop = 0;
   // launch probe: CUDA events around every SpMV-family launch on matrices
   // with probe_nnz nonzeros (0 = off); resolved by pm_ctx_probe_result
+  // device flag passed to the SpMV-family and Vanka launches of this context
+  // while set (nullptr = none): a set flag turns those launches into no-ops
+  const int* guard = nullptr;
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

@@ -193,21 +193,23 @@ static void launch_epi(pm_ctx* c, int G, int U, int n, const int* rp, const int*
                        const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m,
                        const int* rblock = nullptr, int n_rblocks = 0) {
   if (n <= 0) return;
+  BlockMask mg = m;
+  mg.guard = c->guard;
   if (rblock && n_rblocks > 0) {
     csr_stream_kernel<TV, TX, TA, kStreamNnz, EPI><<<n_rblocks, 256, 0, c->stream>>>(
-        rblock, rp, ci, v, x, y, b, d, alpha, m);
+        rblock, rp, ci, v, x, y, b, d, alpha, mg);
     PM_CHECK_LAUNCH();
     c->kernel_launches++;
     return;
   }
   const int grid = nblocks((long long)n * G, 256);
   switch (G) {
-    case 1: launch_gu<TV, TX, TA, 1, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
-    case 2: launch_gu<TV, TX, TA, 2, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
-    case 4: launch_gu<TV, TX, TA, 4, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
-    case 8: launch_gu<TV, TX, TA, 8, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
-    case 16: launch_gu<TV, TX, TA, 16, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
-    default: launch_gu<TV, TX, TA, 32, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, m); break;
+    case 1: launch_gu<TV, TX, TA, 1, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
+    case 2: launch_gu<TV, TX, TA, 2, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
+    case 4: launch_gu<TV, TX, TA, 4, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
+    case 8: launch_gu<TV, TX, TA, 8, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
+    case 16: launch_gu<TV, TX, TA, 16, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
+    default: launch_gu<TV, TX, TA, 32, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
   }
   PM_CHECK_LAUNCH();
   c->kernel_launches++;

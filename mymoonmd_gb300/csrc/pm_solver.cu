@@ -210,6 +210,63 @@ void Multigrid::coarse_solve(pm_ctx* c) {
   }
 }
 
+// sum of squares of x in kRedBlocks partial sums (fixed order)
+template <class T>
+__global__ void __launch_bounds__(256) k_sumsq_partials(int n, const T* __restrict__ x,
+                                                        double* __restrict__ part) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = double(x[i]);
+    s += v * v;
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (int(threadIdx.x) < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// res = sqrt(sum of the partials); the loop goes on while res > tol
+__global__ void k_stop_if_small(const double* __restrict__ part, int n_part, double tol, int* __restrict__ flag) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n_part; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (int(threadIdx.x) < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && !(sqrt(sh[0]) > tol)) *flag = 1;
+}
+
+void Multigrid::coarse_iterate(pm_ctx* c) {
+  MGLevel& lv = levels[0];
+  const int n = lv.A->csr.n_rows;
+  coarse_flag.ensure(1);
+  coarse_part.ensure(kRedBlocks);
+  PM_CUDA(cudaMemsetAsync(coarse_flag.p, 0, sizeof(int), c->stream));
+  c->guard = coarse_flag.p;
+  try {
+    for (int i = 0; i < coarse_max_it; ++i) {
+      smooth(c, 0);
+      defect(c, 0);
+      if (mixed) k_sumsq_partials<float><<<kRedBlocks, 256, 0, c->stream>>>(n, lv.defect32.p, coarse_part.p);
+      else k_sumsq_partials<double><<<kRedBlocks, 256, 0, c->stream>>>(n, lv.defect.p, coarse_part.p);
+      k_stop_if_small<<<1, 256, 0, c->stream>>>(coarse_part.p, kRedBlocks, coarse_residual, coarse_flag.p);
+      PM_CHECK_LAUNCH();
+      c->kernel_launches += 2;
+    }
+  } catch (...) {
+    c->guard = nullptr;
+    throw;
+  }
+  c->guard = nullptr;
+}
+
 void Multigrid::defect(pm_ctx* c, int l) {
   MGLevel& lv = levels[l];
   if (mixed) csr_apply32(c, lv.A->csr, EPI_DEFECT, lv.cur32, lv.defect32.p, lv.rhs32.p, 1.0f);
@@ -259,11 +316,8 @@ void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol) {
     if (level == 0) {
       // coarsest level: with the direct solver one application solves exactly;
       // the defects the reference computes around it only feed its loop test
-      if (levels[0].smoother == SM_DIRECT) {
-        coarse_solve(c);
-      } else {
-        for (int i = 0; i < coarse_max_it; ++i) smooth(c, 0);
-      }
+      if (levels[0].smoother == SM_DIRECT) coarse_solve(c);
+      else coarse_iterate(c);
       prolongate_from(c, 0);
       level = 1;
       continue;

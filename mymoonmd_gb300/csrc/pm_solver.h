@@ -77,6 +77,13 @@ struct Multigrid {
   void restrict_to(pm_ctx* c, int l);  // from l to l-1
   void prolongate_from(pm_ctx* c, int l);  // from l to l+1
   void coarse_solve(pm_ctx* c);
+  // iterative coarsest level (Multigrid::cycle_step): at most coarse_max_it
+  // sweeps, each followed by the defect, stopping once its norm is at or below
+  // coarse_residual; the test runs on the device (a flag that turns the
+  // remaining sweeps into no-ops), so the cycle needs no host round trip
+  void coarse_iterate(pm_ctx* c);
+  DBuf<int> coarse_flag;
+  DBuf<double> coarse_part;
 };
 
 }  // namespace pm

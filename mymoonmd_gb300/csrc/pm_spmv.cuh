@@ -30,7 +30,12 @@ struct BlockMask {
   int start[4];
   int active_end[4];
   int end[4];
+  // device flag: when set, the launch does nothing (the coarse-level smoothing
+  // loop stops once its residual is small enough, without a host round trip)
+  const int* guard = nullptr;
 };
+
+__device__ __forceinline__ bool guarded(const int* g) { return g != nullptr && *(volatile const int*)g != 0; }
 
 __device__ __forceinline__ bool row_is_active(const BlockMask& m, int i) {
 #pragma unroll
@@ -51,6 +56,13 @@ csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ 
            const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
            const TX* __restrict__ b, const TX* __restrict__ diag, const TX* __restrict__ xold,
            TA alpha, BlockMask mask) {
+  if (guarded(mask.guard)) {  // uniform for the whole grid
+    // a skipped Jacobi sweep leaves the iterate as it is (the caller swaps
+    // the two iterate buffers after every sweep)
+    if (EPI == EPI_JACOBI)
+      for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_rows; i += gridDim.x * blockDim.x) y[i] = xold[i];
+    return;
+  }
   const int lane = threadIdx.x & (G - 1);
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) / G;
   const bool valid = row < n_rows;  // whole groups share a row: no early exit before the shuffles
@@ -115,6 +127,13 @@ csr_stream_kernel(const int* __restrict__ rblock, const int* __restrict__ row_pt
   constexpr int PER = NNZB / 256;
   __shared__ TV sv[NNZB];
   __shared__ TX sx[NNZB];
+  if (guarded(mask.guard)) {  // uniform for the whole grid
+    if (EPI == EPI_JACOBI) {
+      const int g0 = __ldg(rblock + blockIdx.x), g1 = __ldg(rblock + blockIdx.x + 1);
+      for (int i = g0 + int(threadIdx.x); i < g1; i += blockDim.x) y[i] = x[i];
+    }
+    return;
+  }
   const int r0 = __ldg(rblock + blockIdx.x), r1 = __ldg(rblock + blockIdx.x + 1);
   const int s = __ldg(row_ptr + r0), e = __ldg(row_ptr + r1);
   const int t = threadIdx.x;

@@ -14,7 +14,6 @@
 // VankaSmoother::smooth (src/Multigrid/VankaSmoother.C:110-292).
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 #include <vector>
 
 #include "pm_stokes.h"
@@ -305,49 +304,6 @@ void ProjectedMatrix::refresh(pm_ctx* c, const DevCsr& sys, bool fp32) {
 }
 
 // ------------------------------------------------------------- Vanka -------
-int stokes_coupling_rank(unsigned mask) {
-  static int table[1024];
-  static bool ready = false;
-  static std::mutex mu;
-  std::lock_guard<std::mutex> lock(mu);
-  if (!ready) {
-    double G[10][3][4] = {};
-    for (int q = 0; q < 11; ++q) {
-      double v[10], d[3][10];
-      p2_eval(kP4x[q], kP4y[q], kP4z[q], v, d[0], d[1], d[2]);
-      const double psi[4] = {1 - kP4x[q] - kP4y[q] - kP4z[q], kP4x[q], kP4y[q], kP4z[q]};
-      for (int nn = 0; nn < 10; ++nn)
-        for (int a = 0; a < 3; ++a)
-          for (int j = 0; j < 4; ++j) G[nn][a][j] += kP4w[q] * d[a][nn] * psi[j];
-    }
-    for (unsigned m = 0; m < 1024; ++m) {
-      // rank of the stacked 3-row blocks of the nodes in m, by elimination
-      double R[30][4];
-      int rows = 0;
-      for (int nn = 0; nn < 10; ++nn)
-        if (m >> nn & 1u)
-          for (int a = 0; a < 3; ++a, ++rows)
-            for (int j = 0; j < 4; ++j) R[rows][j] = G[nn][a][j];
-      int rank = 0;
-      for (int col = 0; col < 4 && rank < rows; ++col) {
-        int best = rank;
-        for (int r = rank + 1; r < rows; ++r)
-          if (std::fabs(R[r][col]) > std::fabs(R[best][col])) best = r;
-        if (std::fabs(R[best][col]) < 1e-10) continue;
-        for (int j = 0; j < 4; ++j) std::swap(R[rank][j], R[best][j]);
-        for (int r = rank + 1; r < rows; ++r) {
-          const double f = R[r][col] / R[rank][col];
-          for (int j = 0; j < 4; ++j) R[r][j] -= f * R[rank][j];
-        }
-        ++rank;
-      }
-      table[m] = rank;
-    }
-    ready = true;
-  }
-  return table[mask & 1023u];
-}
-
 void DevVanka::setup(pm_ctx* c, const DiscLevel& L) {
   n_cells = L.n_cells;
   n = L.sys.n_rows;
@@ -355,10 +311,16 @@ void DevVanka::setup(pm_ctx* c, const DiscLevel& L) {
   std::vector<int> fz(n_cells, 0);
   n_frozen = 0;
   for (int cell = 0; cell < n_cells; ++cell) {
-    unsigned m = 0;
+    // the 3 rows of each active velocity node must control the cell's
+    // pressures: 4, or 3 when the cell holds the first pressure DOF, whose row
+    // is a unit row of the projected matrix; otherwise the local matrix is
+    // singular
+    int n_act = 0, need = 4;
     for (int k = 0; k < 10; ++k)
-      if (L.space.dofmap[size_t(cell) * 10 + k] < L.space.n_active) m |= 1u << k;
-    if (stokes_coupling_rank(m) < 4) {
+      if (L.space.dofmap[size_t(cell) * 10 + k] < L.space.n_active) ++n_act;
+    for (int j = 0; j < 4; ++j)
+      if (L.pspace.dofmap[size_t(cell) * 4 + j] == 0) need = 3;
+    if (3 * n_act < need) {
       fz[cell] = 4;
       ++n_frozen;
     }
@@ -505,10 +467,11 @@ void DevVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
 // added into x (colour-ordered sweep, after all local right-hand sides of
 // the colour are computed)
 template <class T>
-__global__ void __launch_bounds__(256) k_vanka_local(int n_cells, const int* __restrict__ cells,
+__global__ void __launch_bounds__(256) k_vanka_local(const int* __restrict__ guard, int n_cells, const int* __restrict__ cells,
                                                      const int* __restrict__ patch, const T* __restrict__ inv,
                                                      const T* __restrict__ r, const T* __restrict__ rloc,
                                                      T* __restrict__ out, T* __restrict__ x, T damp) {
+  if (guarded(guard)) return;  // uniform for the whole grid
   __shared__ T rl[8][34];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int idx = blockIdx.x * 8 + w;
@@ -531,8 +494,9 @@ __global__ void __launch_bounds__(256) k_vanka_local(int n_cells, const int* __r
 
 // x[d] += (sum over the patches containing d, in cell order) / count[d]
 template <class T>
-__global__ void k_vanka_average(int n, const int* __restrict__ ip, const int* __restrict__ ix,
+__global__ void k_vanka_average(const int* __restrict__ guard, int n, const int* __restrict__ ip, const int* __restrict__ ix,
                                 const int* __restrict__ cnt, const T* __restrict__ sol, T* __restrict__ x) {
+  if (guarded(guard)) return;  // uniform for the whole grid
   for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
     if (cnt[d] == 0) continue;
     T s = T(0);
@@ -543,11 +507,12 @@ __global__ void k_vanka_average(int n, const int* __restrict__ ip, const int* __
 
 // local right-hand sides b - V x of the cells of one colour (one warp per cell)
 template <class T>
-__global__ void __launch_bounds__(256) k_vanka_rhs(int n_cells, const int* __restrict__ cells,
+__global__ void __launch_bounds__(256) k_vanka_rhs(const int* __restrict__ guard, int n_cells, const int* __restrict__ cells,
                                                    const int* __restrict__ patch, const int* __restrict__ rp,
                                                    const int* __restrict__ ci, const T* __restrict__ v,
                                                    const T* __restrict__ b, const T* __restrict__ x,
                                                    T* __restrict__ rloc) {
+  if (guarded(guard)) return;  // uniform for the whole grid
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= n_cells) return;
   const int cell = cells[w];
@@ -566,10 +531,10 @@ static void jacobi_sweep(pm_ctx* c, DevVanka& vk, const DevCsr& V, const T* vals
   if constexpr (sizeof(T) == 8) csr_apply(c, V, EPI_DEFECT, x, r, b, 1.0);
   else csr_apply32(c, V, EPI_DEFECT, x, r, b, 1.0f);
   (void)vals;
-  k_vanka_local<T><<<(vk.n_cells + 7) / 8, 256, 0, c->stream>>>(vk.n_cells, nullptr, vk.patch.p, inv, r,
+  k_vanka_local<T><<<(vk.n_cells + 7) / 8, 256, 0, c->stream>>>(c->guard, vk.n_cells, nullptr, vk.patch.p, inv, r,
                                                                 nullptr, sol, nullptr, damp);
   const int g = std::max(1, std::min((vk.n + 255) / 256, c->num_sms * 16));
-  k_vanka_average<T><<<g, 256, 0, c->stream>>>(vk.n, vk.inc_ptr.p, vk.inc_idx.p, vk.count.p, sol, x);
+  k_vanka_average<T><<<g, 256, 0, c->stream>>>(c->guard, vk.n, vk.inc_ptr.p, vk.inc_idx.p, vk.count.p, sol, x);
   PM_CHECK_LAUNCH();
   c->kernel_launches += 2;
 }
@@ -589,9 +554,9 @@ static void colored_sweep(pm_ctx* c, DevVanka& vk, const DevCsr& V, const T* val
     const int beg = vk.color_ptr[k], cnt = vk.color_ptr[k + 1] - beg;
     if (!cnt) continue;
     const int* cells = vk.color_cells.p + beg;
-    k_vanka_rhs<T><<<(cnt * 32 + 255) / 256, 256, 0, c->stream>>>(cnt, cells, vk.patch.p, V.row_ptr.p, V.cols.p,
+    k_vanka_rhs<T><<<(cnt * 32 + 255) / 256, 256, 0, c->stream>>>(c->guard, cnt, cells, vk.patch.p, V.row_ptr.p, V.cols.p,
                                                                    vals, b, x, rloc);
-    k_vanka_local<T><<<(cnt + 7) / 8, 256, 0, c->stream>>>(cnt, cells, vk.patch.p, inv, nullptr, rloc, nullptr,
+    k_vanka_local<T><<<(cnt + 7) / 8, 256, 0, c->stream>>>(c->guard, cnt, cells, vk.patch.p, inv, nullptr, rloc, nullptr,
                                                            x, damp);
     c->kernel_launches += 2;
   }
@@ -895,12 +860,13 @@ namespace pm {
 // read from rloc), w_k = A^{-1} r_k, p, u_k; the damped correction is written
 // to the local storage (additive sweep) or added into x (colour sweep)
 template <class T>
-__global__ void __launch_bounds__(128) k_nodal_local(int cnt, const int* __restrict__ patches, int nu,
+__global__ void __launch_bounds__(128) k_nodal_local(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                      const int* __restrict__ vptr, const int* __restrict__ vidx,
                                                      const int64_t* __restrict__ aoff, const T* __restrict__ ainv,
                                                      const T* __restrict__ tb, const T* __restrict__ sinv,
                                                      const T* __restrict__ r, const T* __restrict__ rloc,
                                                      T* __restrict__ out, T* __restrict__ x, T damp) {
+  if (guarded(guard)) return;  // uniform for the whole grid
   __shared__ T rl[4][3 * kNodalMaxNodes + 1];
   __shared__ T w[4][3 * kNodalMaxNodes];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -955,11 +921,12 @@ __global__ void __launch_bounds__(128) k_nodal_local(int cnt, const int* __restr
 
 // local residuals b - V x of the patches of one colour (one warp per patch)
 template <class T>
-__global__ void __launch_bounds__(128) k_nodal_rhs(int cnt, const int* __restrict__ patches, int nu,
+__global__ void __launch_bounds__(128) k_nodal_rhs(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                    const int* __restrict__ vptr, const int* __restrict__ vidx,
                                                    const int* __restrict__ rp, const int* __restrict__ ci,
                                                    const T* __restrict__ v, const T* __restrict__ b,
                                                    const T* __restrict__ x, T* __restrict__ rloc) {
+  if (guarded(guard)) return;  // uniform for the whole grid
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int idx = blockIdx.x * 4 + wi;
   if (idx >= cnt) return;
@@ -980,10 +947,10 @@ static void nodal_jacobi(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T*
                          T* sol, const T* b, T* x, T* r, T damp) {
   if constexpr (sizeof(T) == 8) csr_apply(c, V, EPI_DEFECT, x, r, b, 1.0);
   else csr_apply32(c, V, EPI_DEFECT, x, r, b, 1.0f);
-  k_nodal_local<T><<<(nv.np + 3) / 4, 128, 0, c->stream>>>(nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
+  k_nodal_local<T><<<(nv.np + 3) / 4, 128, 0, c->stream>>>(c->guard, nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
                                                           ainv, tb, sinv, r, nullptr, sol, nullptr, damp);
   const int g = std::max(1, std::min((nv.n + 255) / 256, c->num_sms * 16));
-  k_vanka_average<T><<<g, 256, 0, c->stream>>>(nv.n, nv.inc_ptr.p, nv.inc_idx.p, nv.count.p, sol, x);
+  k_vanka_average<T><<<g, 256, 0, c->stream>>>(c->guard, nv.n, nv.inc_ptr.p, nv.inc_idx.p, nv.count.p, sol, x);
   PM_CHECK_LAUNCH();
   c->kernel_launches += 2;
 }
@@ -996,9 +963,9 @@ static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T
     const int beg = nv.color_ptr[k], cnt = nv.color_ptr[k + 1] - beg;
     if (!cnt) continue;
     const int* pts = nv.color_patches.p + beg;
-    k_nodal_rhs<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
+    k_nodal_rhs<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
                                                         V.cols.p, vals, b, x, rloc);
-    k_nodal_local<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
+    k_nodal_local<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
                                                           tb, sinv, nullptr, rloc, nullptr, x, damp);
     c->kernel_launches += 2;
   }

@@ -36,16 +36,13 @@ struct ProjectedMatrix {
   void refresh(pm_ctx* c, const DevCsr& sys, bool fp32);  // copy values from the system
 };
 
-// rank of the coupling int psi_j grad phi_n between the P1 pressures j and
-// the P2 velocity nodes n set in `mask` (bit n = local node n) on the
-// reference tetrahedron; an affine map keeps the rank
-int stokes_coupling_rank(unsigned mask);
-
 // cell Vanka (src/Multigrid/VankaSmoother.C:110-292) with stored local inverses.
-// A cell whose active velocity rows couple to its four pressures with rank < 4
-// has a singular local matrix (the reference's LAPACK LU throws or returns a
-// blown-up correction there): its pressures are frozen - unit rows and
-// columns in the local matrix and no update.
+// A cell whose active velocity nodes are too few to control its pressures
+// (3 rows per node against 4 pressures, or 3 when the cell holds the first
+// pressure DOF, a unit row of the projected matrix) has a singular local
+// matrix; the reference's LAPACK LU throws or returns a blown-up correction
+// there. Such cells have their pressures frozen: unit rows and columns in the
+// local matrix and no update.
 struct DevVanka {
   int n_cells = 0, n = 0;
   DBuf<int> patch;        // n_cells x 34 sorted combined DOFs

@@ -58,38 +58,6 @@ def lib() -> C.CDLL:
     return L
 
 
-_P4_W = np.array([-.0131555555555555555555555555556] + [.00762222222222222222222222222222] * 4
-                 + [.0248888888888888888888888888889] * 6)
-_A, _B, _C, _D = (.0714285714285714285714285714286, .785714285714285714285714285714,
-                  .399403576166799204996102147462, .100596423833200795003897852538)
-_P4_X = np.array([[.25, .25, .25], [_A, _A, _A], [_B, _A, _A], [_A, _B, _A], [_A, _A, _B], [_C, _C, _D],
-                  [_C, _D, _C], [_D, _C, _C], [_D, _D, _C], [_D, _C, _D], [_C, _D, _D]])
-_RANKS = None
-
-
-def coupling_rank_table() -> np.ndarray:
-    """rank of the coupling int psi_j grad phi_n (P1 pressures j, P2 velocity
-    nodes n of the reference tetrahedron) restricted to the nodes of each of the
-    1024 active-node masks; an affine map keeps the rank"""
-    global _RANKS
-    if _RANKS is None:
-        G = np.zeros((10, 3, 4))
-        for q in range(11):
-            x, y, z = _P4_X[q]
-            g0 = -3 + 4 * x + 4 * y + 4 * z
-            d = np.array([[g0, 4 - 8 * x - 4 * y - 4 * z, -1 + 4 * x, -4 * y, 4 * y, 0, -4 * z, 4 * z, 0, 0],
-                          [g0, -4 * x, 0, 4 - 4 * x - 8 * y - 4 * z, 4 * x, -1 + 4 * y, -4 * z, 0, 4 * z, 0],
-                          [g0, -4 * x, 0, -4 * y, 0, 0, 4 - 4 * x - 4 * y - 8 * z, 4 * x, 4 * y, -1 + 4 * z]])
-            psi = np.array([1 - x - y - z, x, y, z])
-            G += _P4_W[q] * np.einsum("dn,j->ndj", d, psi)
-        r = np.zeros(1024, dtype=np.int64)
-        for m in range(1, 1024):
-            rows = G[[n for n in range(10) if m >> n & 1]].reshape(-1, 4)
-            r[m] = np.linalg.matrix_rank(rows, tol=1e-10)
-        _RANKS = r
-    return _RANKS
-
-
 def _nonzero_pattern() -> np.ndarray:
     """34x34 local coupling pattern of the Stokes blocks"""
     blk = np.array([m // 10 if m < 30 else 3 for m in range(34)])
@@ -120,10 +88,13 @@ class StokesLevel:
         self._structure()
         self._projected()
         self.patch = np.ascontiguousarray(np.sort(self.cdof, axis=1), dtype=np.int32)
-        # cells whose active velocity rows couple to the four pressures with
-        # rank < 4 have a singular local matrix: their pressures are frozen
-        masks = (self.active[self.udofmap].astype(np.int64) << np.arange(10)).sum(axis=1)
-        self.n_freeze = np.ascontiguousarray(np.where(coupling_rank_table()[masks] < 4, 4, 0), dtype=np.int32)
+        # a cell's local matrix is singular when the 3 rows of each active
+        # velocity node cannot control the pressures of the cell: 4 of them, or
+        # 3 when the cell holds p0, whose row is a unit row of the projected
+        # matrix. The pressures of such cells are frozen.
+        n_act = self.active[self.udofmap].sum(axis=1).astype(np.int64)
+        need = np.where((self.pdofmap == 0).any(axis=1), 3, 4)
+        self.n_freeze = np.ascontiguousarray(np.where(3 * n_act < need, 4, 0), dtype=np.int32)
         self._colouring()
 
     def _structure(self):

@@ -276,3 +276,22 @@ def test_config_2d_q1_128_full_size_against_oracle(ctx):
     assert abs(it - oit) <= 1
     assert rel(prob.solution(), sol) <= 1e-10
     assert rel(prob.matrix(-1).values(), ora.vals[-1]) <= 1e-13
+
+
+@pytest.mark.parametrize("coarse_residual", [0.0, 1.0])
+def test_multigrid_iterative_coarse_level_matches_oracle(ctx, coarse_residual):
+    """Jacobi on the coarsest level: at most 10 sweeps, stopping once the coarse
+    defect norm is <= multigrid_coarse_residual (Multigrid.C cycle_step); 1.0
+    stops the loop early on this case, 0.0 runs all 10 sweeps"""
+    db = mg_db(3)
+    db["multigrid_smoother_coarse"] = "jacobi"
+    db["multigrid_coarse_max_n_iterations"] = 10
+    db["multigrid_coarse_residual"] = coarse_residual
+    disc, prob, ora = make_pair(ctx, "q1_2d", db)
+    prob.solve()
+    ora.build_mg(2, 2, 0.8, 1.0, "V", coarse_direct=False, coarse_max_it=10, coarse_residual=coarse_residual)
+    z = np.random.default_rng(5).standard_normal(ora.finest.n_dofs)
+    zd = m.DeviceVector.from_numpy(ctx, z)
+    rd = m.DeviceVector(ctx, z.size)
+    prob.solver().apply_preconditioner(zd, rd)
+    assert rel(rd.numpy(), ora.mg_apply(z)) <= 1e-11
