@@ -67,7 +67,11 @@ int pm_version(void);
  *   this SpMV epilogue (0 y+=aAx, 1 y=Ax, 2 defect, 3 damped Jacobi sweep,
  *   4 restriction, 5 prolongation add; -1 = all);
  *   "probe_precision" 0|4|8 - only launches whose matrix values have this
- *   size in bytes (0 = all). */
+ *   size in bytes (0 = all);
+ *   "fp32_bulk_spmv" 0|1 - FP32 SpMV-family launches on full matrices by the
+ *   bulk-copy kernel (row chunks streamed into shared memory with
+ *   cp.async.bulk; default 1) or by the per-row-group kernel; both give the
+ *   same bits. */
 int pm_ctx_set_option(pm_ctx* ctx, const char* key, int value);
 /* Launch probe (no reference counterpart; measurement only): while enabled
  * (nnz != 0), every SpMV-family launch (apply, defect, Jacobi sweep, transfer)

@@ -71,6 +71,10 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->assembly_quadrature_loop = value != 0;
     return PM_OK;
   }
+  if (std::string(key) == "fp32_bulk_spmv") {
+    c->bulk_spmv = value != 0;
+    return PM_OK;
+  }
   if (std::string(key) == "probe_epilogue") {
     c->probe_epilogue = value;
     return PM_OK;
@@ -300,6 +304,7 @@ int pm_matrix_apply_f32(pm_matrix* A, const float* x, float* y) {
   if (!A || !x || !y) return PM_E_INVALID;
   PM_TRY
   csr_apply32(A->ctx, A->csr, EPI_SET, x, y, nullptr, 1.0f);
+  check_device_error(A->ctx);
   return PM_OK;
   PM_CATCH(A->ctx)
 }
@@ -492,7 +497,7 @@ int pm_solver_solve(pm_solver* s, const double* rhs, double* sol) {
   if (!s || !rhs || !sol) return fail(s ? s->ctx : nullptr, PM_E_INVALID, "null argument");
   PM_TRY
   s->solve(rhs, sol);
-  PM_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  check_device_error(s->ctx);
   return PM_OK;
   PM_CATCH(s->ctx)
 }
@@ -507,7 +512,7 @@ int pm_solver_solve_host(pm_solver* s, const double* rhs_h, double* sol_h, int n
   x.upload(sol_h, n, c->stream);
   s->solve(r.p, x.p);
   x.download(sol_h, c->stream);
-  PM_CUDA(cudaStreamSynchronize(c->stream));
+  check_device_error(c);
   return PM_OK;
   PM_CATCH(s->ctx)
 }
@@ -533,7 +538,7 @@ int pm_solver_apply_preconditioner(pm_solver* s, const double* z, double* r) {
   PM_TRY
   if (!s->A) throw Error(PM_E_INVALID, "preconditioner used before update_matrix");
   s->precondition(z, r);
-  PM_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  check_device_error(s->ctx);
   return PM_OK;
   PM_CATCH(s->ctx)
 }
@@ -841,7 +846,7 @@ int pm_problem_solve(pm_problem* p) {
     p->solver_ready = true;
   }
   p->solver->solve(p->rhs.p, p->sol.p);
-  PM_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  check_device_error(p->ctx);
   return PM_OK;
   PM_CATCH(p->ctx)
 }

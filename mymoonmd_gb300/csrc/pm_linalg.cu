@@ -3,6 +3,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "pm_linalg.cuh"
 
 namespace pm {
@@ -17,12 +19,25 @@ void ctx_init(pm_ctx* c, int device) {
   c->dev_scalars.alloc(256);
   c->partials.alloc(4 * kRedBlocks);
   c->n_partials = kRedBlocks;
+  c->dev_error.alloc(1);
+  PM_CUDA(cudaMemsetAsync(c->dev_error.p, 0, sizeof(int), c->stream));
+}
+
+void check_device_error(pm_ctx* c) {
+  int h = 0;
+  PM_CUDA(cudaMemcpyAsync(&h, c->dev_error.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  if (h) {
+    PM_CUDA(cudaMemsetAsync(c->dev_error.p, 0, sizeof(int), c->stream));
+    throw Error(PM_E_TIMEOUT, "a bounded wait of a bulk-copy SpMV kernel gave up");
+  }
 }
 
 void ctx_destroy(pm_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->dev_scalars.release();
   c->partials.release();
+  c->dev_error.release();
   if (c->host_scalars) cudaFreeHost(c->host_scalars);
   c->host_scalars = nullptr;
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -46,7 +61,12 @@ void DevCsr::upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int*
   n_active = na;
   nnz = rp[nr];
   row_ptr.upload(rp, size_t(nr) + 1, c->stream);
-  cols.upload(ci, size_t(nnz), c->stream);
+  // column indices readable up to nnz rounded up to 4 entries (bulk copies
+  // move 16-byte aligned spans); the tail holds zeros
+  cols.alloc(size_t(nnz4()));
+  if (nnz) PM_CUDA(cudaMemcpyAsync(cols.p, ci, size_t(nnz) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  if (nnz4() > nnz)
+    PM_CUDA(cudaMemsetAsync(cols.p + nnz, 0, size_t(nnz4() - nnz) * sizeof(int), c->stream));
   if (v) vals.upload(v, size_t(nnz), c->stream);
   else {
     vals.alloc(size_t(nnz));
@@ -67,7 +87,28 @@ void DevCsr::upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int*
   n_rblocks = rb.empty() ? 0 : int(rb.size()) - 1;
   if (n_rblocks) rblock.upload(rb, c->stream);
   else rblock.release();
+  std::vector<int> ch = build_bulk_chunks(nr, rp, kBulkEntries);
+  n_chunks = ch.empty() ? 0 : int(ch.size()) - 1;
+  if (n_chunks) chunk_rows.upload(ch, c->stream);
+  else chunk_rows.release();
   set_single_block();
+}
+
+std::vector<int> build_bulk_chunks(int n_rows, const int* rp, int max_entries) {
+  std::vector<int> ch;
+  if (n_rows <= 0) return ch;
+  ch.push_back(0);
+  int r0 = 0;
+  auto span = [&](int a, int b) { return ((rp[b] + 3) & ~3) - (rp[a] & ~3); };
+  for (int i = 0; i < n_rows; ++i) {
+    if (span(i, i + 1) > max_entries) return std::vector<int>();  // a row alone does not fit
+    if (span(r0, i + 1) > max_entries) {
+      ch.push_back(i);
+      r0 = i;
+    }
+  }
+  ch.push_back(n_rows);
+  return ch;
 }
 
 std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int max_rows) {
@@ -128,7 +169,9 @@ static int grid_for(pm_ctx* c, long long n) {
 }
 
 void DevCsr::make_fp32(pm_ctx* c) {
-  vals32.ensure(size_t(nnz));
+  vals32.ensure(size_t(nnz4()));
+  if (nnz4() > nnz)
+    PM_CUDA(cudaMemsetAsync(vals32.p + nnz, 0, size_t(nnz4() - nnz) * sizeof(float), c->stream));
   if (nnz) {
     k_d2f<<<grid_for(c, nnz), 256, 0, c->stream>>>(nnz, vals.p, vals32.p);
     PM_CHECK_LAUNCH();
@@ -237,6 +280,37 @@ static double epi_bytes(const DevCsr& A, int epi, int eb, int n) {
   return double(A.nnz) * (eb + 4) + double(n + 1) * 4 + double(A.n_cols) * eb + double(n) * eb * rows_vec;
 }
 
+// the bulk-copy FP32 kernel: persistent grid, two 32 KB buffers per block
+template <int G, int EPI>
+static void launch_bulk_g(pm_ctx* c, const DevCsr& A, const float* vals, const float* x, float* y, const float* b,
+                          const float* d, float alpha, const BlockMask& m) {
+  constexpr size_t smem = 4 * size_t(kBulkEntries) * 4 + 2 * sizeof(uint64_t);
+  static int per_sm = -1;  // per instantiation; the attribute and occupancy do not change
+  if (per_sm < 0) {
+    PM_CUDA(cudaFuncSetAttribute(csr_bulk_kernel<G, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    int bps = 0;
+    PM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, csr_bulk_kernel<G, EPI>, 256, smem));
+    per_sm = std::max(1, bps);
+  }
+  const int grid = std::max(1, std::min(A.n_chunks, c->num_sms * per_sm));
+  csr_bulk_kernel<G, EPI><<<grid, 256, smem, c->stream>>>(A.n_chunks, A.chunk_rows.p, A.row_ptr.p, A.cols.p, vals,
+                                                         x, y, b, d, alpha, m, c->dev_error.p);
+}
+
+template <int EPI>
+static void launch_bulk(pm_ctx* c, const DevCsr& A, const float* vals, const float* x, float* y, const float* b,
+                        const float* d, float alpha, const BlockMask& m) {
+  BlockMask mg = m;
+  mg.guard = c->guard;
+  switch (A.lanes32) {
+    case 4: launch_bulk_g<4, EPI>(c, A, vals, x, y, b, d, alpha, mg); break;
+    case 16: launch_bulk_g<16, EPI>(c, A, vals, x, y, b, d, alpha, mg); break;
+    default: launch_bulk_g<8, EPI>(c, A, vals, x, y, b, d, alpha, mg); break;
+  }
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
 template <class TV, class TX, class TA>
 static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* diag, int epi,
                          const TX* x, TX* y, const TX* b, TA alpha, int n) {
@@ -256,6 +330,33 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
     PM_CUDA(cudaEventRecord(e0, c->stream));
     c->probe_events.push_back(e0);
     c->probe_bytes.push_back(epi_bytes(A, epi, int(sizeof(TV)), n));
+  }
+  const bool bulk = sizeof(TV) == 4 && c->bulk_spmv && A.bulk32 && A.n_chunks > 0 && n == A.n_rows &&
+                    (G == 4 || G == 8 || G == 16);
+  if constexpr (sizeof(TV) == 4) {
+    if (bulk) {
+      const float* fv = reinterpret_cast<const float*>(vals);
+      const float* fx = reinterpret_cast<const float*>(x);
+      float* fy = reinterpret_cast<float*>(y);
+      const float* fb = reinterpret_cast<const float*>(b);
+      const float* fd = reinterpret_cast<const float*>(diag);
+      const float fa = float(alpha);
+      switch (epi) {
+        case EPI_AXPY: launch_bulk<EPI_AXPY>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
+        case EPI_SET: launch_bulk<EPI_SET>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
+        case EPI_DEFECT: launch_bulk<EPI_DEFECT>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
+        case EPI_JACOBI: launch_bulk<EPI_JACOBI>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
+        case EPI_RESTRICT: launch_bulk<EPI_RESTRICT>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
+        case EPI_PROLONG: launch_bulk<EPI_PROLONG>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
+        default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
+      }
+      if (probe) {
+        cudaEvent_t e1 = probe_event(c);
+        PM_CUDA(cudaEventRecord(e1, c->stream));
+        c->probe_events.push_back(e1);
+      }
+      return;
+    }
   }
   switch (epi) {
     case EPI_AXPY: launch_epi<TV, TX, TA, EPI_AXPY>(c, G, U, n, rp, ci, vals, x, y, b, diag, alpha, A.mask, rb, nrb); break;
@@ -530,6 +631,98 @@ __global__ void k_gj_unswap(int na, double* __restrict__ M, const int* __restric
   }
 }
 
+// The whole Gauss-Jordan elimination in one cooperative launch (all blocks
+// resident; cooperative_groups grid barriers, two per column). Every block owns
+// a contiguous range of rows. Step k: every block reduces the per-block
+// partial arg-max of column k in the same fixed order (largest magnitude, the
+// smallest row on ties: the pivot rule of k_gj_pivot), then writes its share of
+// the scaled pivot row, the old row k and the column multipliers; after the
+// barrier each block eliminates its own rows and records the partial arg-max
+// of column k+1. The values are those of k_gj_pivot + k_gj_update (same
+// operations per entry), without 2 launches per column.
+__global__ void __launch_bounds__(256) k_gj_coop(int na, double* __restrict__ M, int* __restrict__ perm,
+                                                 double* __restrict__ rowk, double* __restrict__ oldk,
+                                                 double* __restrict__ colk, double* __restrict__ part_v,
+                                                 int* __restrict__ part_i, int* __restrict__ flag) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ double sv[256];
+  __shared__ int si[256];
+  __shared__ int s_p;
+  __shared__ double s_pv;
+  const int t = threadIdx.x, nb = gridDim.x, b = blockIdx.x;
+  const int per = (na + nb - 1) / nb;
+  const int r0 = min(na, b * per), r1 = min(na, r0 + per);
+  auto block_argmax = [&](int col, int from) {
+    double best = -1.0;
+    int bi = na;
+    for (int i = max(r0, from) + t; i < r1; i += blockDim.x) {
+      const double a = fabs(M[(size_t)i * na + col]);
+      if (a > best) { best = a; bi = i; }
+    }
+    sv[t] = best;
+    si[t] = bi;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (t < s && (sv[t + s] > sv[t] || (sv[t + s] == sv[t] && si[t + s] < si[t]))) {
+        sv[t] = sv[t + s];
+        si[t] = si[t + s];
+      }
+      __syncthreads();
+    }
+    if (t == 0) {
+      part_v[b] = sv[0];
+      part_i[b] = si[0];
+    }
+  };
+  block_argmax(0, 0);
+  for (int k = 0; k < na; ++k) {
+    grid.sync();
+    // pivot of column k: the same reduction in every block
+    if (t == 0) {
+      double best = -1.0;
+      int bi = na;
+      for (int q = 0; q < nb; ++q)
+        if (part_v[q] > best || (part_v[q] == best && part_i[q] < bi)) {
+          best = part_v[q];
+          bi = part_i[q];
+        }
+      const bool singular = !(best > 0.0);
+      s_p = singular ? k : bi;
+      s_pv = singular ? 1.0 : M[(size_t)bi * na + k];
+      if (b == 0) {
+        perm[k] = s_p;
+        if (singular) *flag = 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    const double pv = s_pv;
+    // scaled pivot row, old row k and the multipliers (rows after the swap)
+    for (int e = b * blockDim.x + t; e < na; e += nb * blockDim.x) {
+      rowk[e] = (e == k ? 1.0 : M[(size_t)p * na + e]) / pv;
+      oldk[e] = M[(size_t)k * na + e];
+      colk[e] = (e == p && p != k) ? M[(size_t)k * na + k] : M[(size_t)e * na + k];
+    }
+    grid.sync();
+    // elimination of this block's rows
+    const long long cnt = (long long)(r1 - r0) * na;
+    for (long long e = t; e < cnt; e += blockDim.x) {
+      const int i = r0 + int(e / na), j = int(e % na);
+      double* Mi = M + (size_t)i * na;
+      if (i == k) {
+        Mi[j] = rowk[j];
+      } else {
+        const double base = (i == p && p != k) ? oldk[j] : Mi[j];
+        const double f = colk[i];
+        Mi[j] = (j == k ? 0.0 : base) - f * rowk[j];
+      }
+    }
+    __syncthreads();
+    if (k + 1 < na) block_argmax(k + 1, k + 1);
+  }
+}
+
 void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
   n = A.n_rows;
   std::vector<int> h_act, h_pos(n, -1);
@@ -556,11 +749,35 @@ void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
                                                         A.vals.p, inv.p);
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
-  const int ugrid = std::max(1, std::min(nblocks((long long)na * na, 256), c->num_sms * 8));
-  for (int k = 0; k < na; ++k) {
-    k_gj_pivot<<<1, 256, 0, c->stream>>>(na, k, inv.p, perm.p, tmp.p, flag.p);
-    k_gj_update<<<ugrid, 256, 0, c->stream>>>(na, k, inv.p, tmp.p);
-    c->kernel_launches += 2;
+  int coop = 0, per_sm = 0;
+  PM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
+  PM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
+  if (coop && per_sm > 0) {
+    // one cooperative launch; at most one block per SM and about 8 rows per block
+    int nb = std::min(c->num_sms, std::max(1, (na + 7) / 8));
+    rowk.ensure(na);
+    oldk.ensure(na);
+    part_v.ensure(nb);
+    part_i.ensure(nb);
+    double* M = inv.p;
+    int* pp = perm.p;
+    double* rk = rowk.p;
+    double* ok = oldk.p;
+    double* ck = tmp.p;
+    double* pv = part_v.p;
+    int* pi = part_i.p;
+    int* fl = flag.p;
+    int nan_ = na;
+    void* args[] = {&nan_, &M, &pp, &rk, &ok, &ck, &pv, &pi, &fl};
+    PM_CUDA(cudaLaunchCooperativeKernel((const void*)k_gj_coop, dim3(nb), dim3(256), args, 0, c->stream));
+    c->kernel_launches++;
+  } else {
+    const int ugrid = std::max(1, std::min(nblocks((long long)na * na, 256), c->num_sms * 8));
+    for (int k = 0; k < na; ++k) {
+      k_gj_pivot<<<1, 256, 0, c->stream>>>(na, k, inv.p, perm.p, tmp.p, flag.p);
+      k_gj_update<<<ugrid, 256, 0, c->stream>>>(na, k, inv.p, tmp.p);
+      c->kernel_launches += 2;
+    }
   }
   PM_CHECK_LAUNCH();
   k_gj_unswap<<<nblocks(na, 128), 128, 0, c->stream>>>(na, inv.p, perm.p);

@@ -20,6 +20,12 @@ struct DevCsr {
   DBuf<int> rblock;
   int n_rblocks = 0;
   bool stream = true;  // use the streaming kernel when row blocks exist
+  // chunks of consecutive rows for the bulk-copy FP32 kernel (empty when a
+  // row's aligned span exceeds a buffer); bulk32 selects that kernel
+  DBuf<int> chunk_rows;
+  int n_chunks = 0;
+  bool bulk32 = true;
+  int64_t nnz4() const { return (nnz + 3) & ~int64_t(3); }
   BlockMask mask{};
   DBuf<int> row_ptr, cols;
   DBuf<double> vals;
@@ -39,6 +45,11 @@ int choose_lanes(double avg_nnz_per_row);
 constexpr int kStreamNnz = 2048;  // entries per row block of the streaming kernel
 // greedy row blocks over a host row-pointer array; empty if a row is too long
 std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int max_rows);
+// chunks of consecutive rows whose 4-entry aligned span holds at most
+// max_entries entries; empty if one row alone does not fit
+std::vector<int> build_bulk_chunks(int n_rows, const int* rp, int max_entries);
+// reads and clears the context's device error flag; throws PM_E_TIMEOUT if set
+void check_device_error(pm_ctx* c);
 
 // y := epilogue(A x); see pm_spmv.cuh for the epilogue meanings
 void csr_apply(pm_ctx* c, const DevCsr& A, int epi, const double* x, double* y, const double* b,
@@ -80,6 +91,8 @@ struct DenseInverse {
   DBuf<double> tmp;  // na
   DBuf<int> perm;    // pivot rows (na)
   DBuf<int> flag;    // singular pivot flag
+  DBuf<double> rowk, oldk, part_v;  // cooperative elimination: pivot row, old row k, block arg-max
+  DBuf<int> part_i;
   void build(pm_ctx* c, const DevCsr& A);
   // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active);
   // rhs_nonactive_zero skips the b_n correction (the multigrid coarse rhs has

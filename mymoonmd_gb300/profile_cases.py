@@ -53,7 +53,7 @@ def main() -> None:
     ap.add_argument("case", choices=["request", "spmv", "assembly", "stokes"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
-    ap.add_argument("--coarse", default="direct_solve")
+    ap.add_argument("--coarse", default="nodal_vanka")
     args = ap.parse_args()
     ctx = m.Context(0)
     if args.case == "stokes":

@@ -162,3 +162,21 @@ def test_stokes_discrete_solution_converges_to_manufactured_solution(ctx):
         exact = np.concatenate([py - pz, pz - px, px - py])
         errs.append(np.abs(prob.solution()[: 3 * lv.nu] - exact).max())
     assert errs[1] < errs[0] / 3.5, errs
+
+
+@pytest.mark.parametrize("coarse_residual", [0.0, 0.1])
+def test_stokes_iterative_coarse_level_matches_oracle(ctx, coarse_residual):
+    """nodal Vanka also on the coarsest level: at most 10 colour-ordered sweeps,
+    stopping at multigrid_coarse_residual (checked on the device)"""
+    db = stokes_db(3, "nodal_vanka", 1.0, coarse="nodal_vanka")
+    db["multigrid_coarse_max_n_iterations"] = 10
+    db["multigrid_coarse_residual"] = coarse_residual
+    disc, prob, ora = make_pair(ctx, 1, 3, 3, db)
+    prob.solve()
+    ora.build_mg(smoother="nodal_color", coarse_smoother="nodal_color", vanka_damp=1.0, n_pre=1, n_post=1,
+                 coarse_max_it=10, coarse_residual=coarse_residual)
+    z = np.random.default_rng(11).standard_normal(ora.finest.n)
+    zd = m.DeviceVector.from_numpy(ctx, z)
+    rd = m.DeviceVector(ctx, z.size)
+    prob.solver().apply_preconditioner(zd, rd)
+    assert rel(rd.numpy(), ora.mg_apply(z)) <= 1e-10
