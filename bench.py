@@ -21,6 +21,7 @@ on the data path; rank 0 prints max-over-ranks timing.
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import statistics
@@ -497,7 +498,7 @@ def run_stream(args, rank, world, local, pg):
     import numpy as np
     import mymoonmd_gb300 as m
     from mymoonmd_gb300 import workloads as wl
-    reqs = wl.stream_requests(512, 0)
+    reqs = wl.stream_requests(args.requests, 0)
     outs = [np.empty(wl.dofs_of(r)) for r in reqs]
     total_dofs = sum(wl.dofs_of(r) for r in reqs)
     res = {}
@@ -622,6 +623,7 @@ def run_serve(args, rank, world, local, pg):
 
 
 def main():
+    faulthandler.enable()
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -629,6 +631,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS) + ["stream512", "serve"], default="cd3d_q2_32")
     ap.add_argument("--workers", type=int, default=4, help="executor worker streams (stream512, serve)")
+    ap.add_argument("--requests", type=int, default=512, help="stream512: requests per pass")
     ap.add_argument("--rates", default="50,100,200,400", help="serve: offered request rates per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--no-cpu-baseline", action="store_true")

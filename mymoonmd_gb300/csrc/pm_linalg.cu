@@ -2,6 +2,7 @@
 // the dense coarse-grid inverse.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include <cooperative_groups.h>
 
@@ -285,13 +286,18 @@ template <int G, int EPI>
 static void launch_bulk_g(pm_ctx* c, const DevCsr& A, const float* vals, const float* x, float* y, const float* b,
                           const float* d, float alpha, const BlockMask& m) {
   constexpr size_t smem = 4 * size_t(kBulkEntries) * 4 + 2 * sizeof(uint64_t);
-  static int per_sm = -1;  // per instantiation; the attribute and occupancy do not change
-  if (per_sm < 0) {
-    PM_CUDA(cudaFuncSetAttribute(csr_bulk_kernel<G, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  // per instantiation, once per process (several host threads may launch)
+  static std::once_flag once;
+  static int per_sm = 1;
+  static cudaError_t init_err = cudaSuccess;
+  std::call_once(once, [&] {
+    init_err = cudaFuncSetAttribute(csr_bulk_kernel<G, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     int bps = 0;
-    PM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, csr_bulk_kernel<G, EPI>, 256, smem));
+    if (init_err == cudaSuccess)
+      init_err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, csr_bulk_kernel<G, EPI>, 256, smem);
     per_sm = std::max(1, bps);
-  }
+  });
+  PM_CUDA(init_err);
   const int grid = std::max(1, std::min(A.n_chunks, c->num_sms * per_sm));
   csr_bulk_kernel<G, EPI><<<grid, 256, smem, c->stream>>>(A.n_chunks, A.chunk_rows.p, A.row_ptr.p, A.cols.p, vals,
                                                          x, y, b, d, alpha, m, c->dev_error.p);
