@@ -70,7 +70,7 @@ int pm_version(void);
  *   size in bytes (0 = all);
  *   "fp32_bulk_spmv" 0|1 - FP32 SpMV-family launches on full matrices by the
  *   bulk-copy kernel (row chunks streamed into shared memory with
- *   cp.async.bulk; default 1) or by the per-row-group kernel; both give the
+ *   cp.async.bulk) or by the per-row-group kernel (default 0); both give the
  *   same bits. */
 int pm_ctx_set_option(pm_ctx* ctx, const char* key, int value);
 /* Launch probe (no reference counterpart; measurement only): while enabled

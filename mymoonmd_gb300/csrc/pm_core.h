@@ -110,7 +110,7 @@ struct pm_ctx {
   const int* guard = nullptr;
   // set by kernels whose bounded waits gave up (checked after each solve)
   pm::DBuf<int> dev_error;
-  bool bulk_spmv = true;  // FP32 SpMV by the bulk-copy kernel where a matrix allows it
+  bool bulk_spmv = false;  // FP32 SpMV by the bulk-copy kernel where a matrix allows it
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

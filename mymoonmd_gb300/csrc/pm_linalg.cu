@@ -282,7 +282,7 @@ static double epi_bytes(const DevCsr& A, int epi, int eb, int n) {
 }
 
 // the bulk-copy FP32 kernel: persistent grid, two 32 KB buffers per block
-template <int G, int EPI>
+template <int G, int U, int EPI>
 static void launch_bulk_g(pm_ctx* c, const DevCsr& A, const float* vals, const float* x, float* y, const float* b,
                           const float* d, float alpha, const BlockMask& m) {
   constexpr size_t smem = 4 * size_t(kBulkEntries) * 4 + 2 * sizeof(uint64_t);
@@ -291,15 +291,15 @@ static void launch_bulk_g(pm_ctx* c, const DevCsr& A, const float* vals, const f
   static int per_sm = 1;
   static cudaError_t init_err = cudaSuccess;
   std::call_once(once, [&] {
-    init_err = cudaFuncSetAttribute(csr_bulk_kernel<G, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    init_err = cudaFuncSetAttribute(csr_bulk_kernel<G, U, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     int bps = 0;
     if (init_err == cudaSuccess)
-      init_err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, csr_bulk_kernel<G, EPI>, 256, smem);
+      init_err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, csr_bulk_kernel<G, U, EPI>, 256, smem);
     per_sm = std::max(1, bps);
   });
   PM_CUDA(init_err);
   const int grid = std::max(1, std::min(A.n_chunks, c->num_sms * per_sm));
-  csr_bulk_kernel<G, EPI><<<grid, 256, smem, c->stream>>>(A.n_chunks, A.chunk_rows.p, A.row_ptr.p, A.cols.p, vals,
+  csr_bulk_kernel<G, U, EPI><<<grid, 256, smem, c->stream>>>(A.n_chunks, A.chunk_rows.p, A.row_ptr.p, A.cols.p, vals,
                                                          x, y, b, d, alpha, m, c->dev_error.p);
 }
 
@@ -308,11 +308,8 @@ static void launch_bulk(pm_ctx* c, const DevCsr& A, const float* vals, const flo
                         const float* d, float alpha, const BlockMask& m) {
   BlockMask mg = m;
   mg.guard = c->guard;
-  switch (A.lanes32) {
-    case 4: launch_bulk_g<4, EPI>(c, A, vals, x, y, b, d, alpha, mg); break;
-    case 16: launch_bulk_g<16, EPI>(c, A, vals, x, y, b, d, alpha, mg); break;
-    default: launch_bulk_g<8, EPI>(c, A, vals, x, y, b, d, alpha, mg); break;
-  }
+  if (A.lanes32 == 4) launch_bulk_g<4, 4, EPI>(c, A, vals, x, y, b, d, alpha, mg);
+  else launch_bulk_g<8, 16, EPI>(c, A, vals, x, y, b, d, alpha, mg);
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
 }
@@ -337,8 +334,9 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
     c->probe_events.push_back(e0);
     c->probe_bytes.push_back(epi_bytes(A, epi, int(sizeof(TV)), n));
   }
+  // the bulk kernel exists for the two FP32 launch shapes the matrices choose
   const bool bulk = sizeof(TV) == 4 && c->bulk_spmv && A.bulk32 && A.n_chunks > 0 && n == A.n_rows &&
-                    (G == 4 || G == 8 || G == 16);
+                    ((G == 4 && U == 4) || (G == 8 && U == 16));
   if constexpr (sizeof(TV) == 4) {
     if (bulk) {
       const float* fv = reinterpret_cast<const float*>(vals);

@@ -25,6 +25,9 @@
 #include <tuple>
 #include <vector>
 
+#include <cstdio>
+#include <cstdlib>
+
 #include "pm_problem.h"
 #include "pmgpu.h"
 
@@ -85,6 +88,7 @@ struct pm_server {
   std::atomic<uint64_t> served{0}, evictions{0};
   std::string create_error;
   std::atomic<int> workers_ready{0}, workers_failed{0};
+  bool trace = std::getenv("PMGPU_SERVER_TRACE") != nullptr;  // request start/finish lines on stderr
 
   std::shared_ptr<SharedSetup> setup_for(const SetupKey& k) {
     std::shared_ptr<SharedSetup> s;
@@ -107,13 +111,15 @@ struct pm_server {
 
 void pm_server::worker(int index) {
   pm_ctx* ctx = nullptr;
-  if (pm_ctx_create(device, &ctx) != PM_OK) {
-    workers_failed++;
-    cv_done.notify_all();
-    return;
+  const int rc0 = pm_ctx_create(device, &ctx);
+  {
+    // under the mutex: the creator tests these counts and waits on cv_done
+    std::lock_guard<std::mutex> g(mu);
+    if (rc0 != PM_OK) workers_failed++;
+    else workers_ready++;
   }
-  workers_ready++;
   cv_done.notify_all();
+  if (rc0 != PM_OK) return;
   std::map<SetupKey, Cached> cache;
   uint64_t tick = 0;
   for (;;) {
@@ -126,6 +132,10 @@ void pm_server::worker(int index) {
       jobs.pop_front();
     }
     const pm_request& rq = job.req;
+    if (trace)
+      std::fprintf(stderr, "[pm_server] worker %d start tag %llu kind %d geo %d root %d refine %d levels %d elem %d\n",
+                   index, (unsigned long long)rq.tag, rq.kind, rq.geometry, rq.root_n, rq.n_refine, rq.n_levels,
+                   rq.elem);
     pm_result res{};
     res.tag = rq.tag;
     res.worker = index;
@@ -215,6 +225,10 @@ void pm_server::worker(int index) {
     }
     res.status = rc;
     const auto t_end = Clock::now();
+    if (trace)
+      std::fprintf(stderr, "[pm_server] worker %d done tag %llu status %d its %d setup %.1f ms run %.1f ms%s%s\n", index,
+                   (unsigned long long)rq.tag, rc, res.iterations, res.setup_ms, ms_since(t_setup, t_end),
+                   rc == PM_OK || rc == PM_E_MAXIT ? "" : " error: ", rc == PM_OK || rc == PM_E_MAXIT ? "" : pm_last_error(ctx));
     res.run_ms = ms_since(t_setup, t_end);
     res.latency_ms = ms_since(job.submitted, t_end);
     served++;

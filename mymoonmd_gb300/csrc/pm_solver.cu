@@ -118,6 +118,10 @@ void Multigrid::update(pm_ctx* c) {
   for (int l = 0; l < L; ++l)
     if (!levels[l].A) throw Error(PM_E_INVALID, "multigrid level " + std::to_string(l) + " has no matrix");
   control = cycle_control(cycle_type, L);
+  // the coarse loop's device flag and partial sums (allocated here: the cycle
+  // itself may run inside a graph capture, where allocation is not allowed)
+  coarse_flag.ensure(1);
+  coarse_part.ensure(kRedBlocks);
   for (int l = 0; l < L; ++l) {
     MGLevel& lv = levels[l];
     DevCsr& A = lv.A->csr;
@@ -246,8 +250,6 @@ __global__ void k_stop_if_small(const double* __restrict__ part, int n_part, dou
 void Multigrid::coarse_iterate(pm_ctx* c) {
   MGLevel& lv = levels[0];
   const int n = lv.A->csr.n_rows;
-  coarse_flag.ensure(1);
-  coarse_part.ensure(kRedBlocks);
   PM_CUDA(cudaMemsetAsync(coarse_flag.p, 0, sizeof(int), c->stream));
   c->guard = coarse_flag.p;
   try {

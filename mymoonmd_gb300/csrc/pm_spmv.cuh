@@ -207,8 +207,9 @@ csr_stream_kernel(const int* __restrict__ rblock, const int* __restrict__ row_pt
 // thread streams the next chunk's values and column indices into shared
 // memory with cp.async.bulk (completion counted on an mbarrier) while the
 // block computes the current chunk: G lanes per row, each lane summing the
-// entries beg+lane, beg+lane+G, ... in order, then the same shuffle tree as
-// csr_kernel<.., G, U, ..>, so the results are bit-identical to it. The
+// entries beg+lane, beg+lane+G, ... in rounds of U (gathers first), then the
+// same shuffle tree as csr_kernel<.., G, U, ..>, so the results are
+// bit-identical to it. The
 // arrays must be readable up to nnz rounded up to a multiple of 4 entries.
 namespace bulk {
 
@@ -253,7 +254,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 
 constexpr int kBulkEntries = 4096;  // entries per buffer: 16 KB values + 16 KB indices
 
-template <int G, int EPI>
+template <int G, int U, int EPI>
 __global__ void __launch_bounds__(256)
 csr_bulk_kernel(int n_chunks, const int* __restrict__ chunk_rows, const int* __restrict__ row_ptr,
                 const int* __restrict__ cols, const float* __restrict__ vals, const float* __restrict__ x,
@@ -330,8 +331,21 @@ csr_bulk_kernel(int n_chunks, const int* __restrict__ chunk_rows, const int* __r
           pre_x = __ldg(x + row);
         }
       }
+      // U entries per lane per round, all gathers issued before the products
+      // (the order and the zero padding of csr_kernel<.., G, U, ..>)
       float s = 0.f;
-      for (int k = beg + lane; k < end; k += G) s += V[k] * __ldg(x + Cc[k]);
+      for (int base = beg; base < end; base += G * U) {
+        float vv[U], xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int k = base + u * G + lane;
+          const bool in = k < end;
+          vv[u] = in ? V[k] : 0.f;
+          xv[u] = __ldg(x + (in ? Cc[k] : 0));
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) s += vv[u] * xv[u];
+      }
 #pragma unroll
       for (int off = G / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, G);
       if (valid && lane == 0) {

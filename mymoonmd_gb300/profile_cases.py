@@ -96,7 +96,11 @@ def main() -> None:
         y32 = m.DeviceVector(ctx, n, np.float32)
         ms, b = A.bench_apply(x, y, 2)
         ms32, b32 = A.bench_apply(x32, y32, 2, fp32=True)
-        print(f"spmv fp64 {b / ms / 1e6:.0f} GB/s, fp32 {b32 / ms32 / 1e6:.0f} GB/s (2 launches each)")
+        ctx.set_option("fp32_bulk_spmv", 1)
+        msb, bb = A.bench_apply(x32, y32, 2, fp32=True)
+        ctx.set_option("fp32_bulk_spmv", 0)
+        print(f"spmv fp64 {b / ms / 1e6:.0f} GB/s, fp32 {b32 / ms32 / 1e6:.0f} GB/s, "
+              f"fp32 bulk-copy kernel {bb / msb / 1e6:.0f} GB/s (2 launches each)")
     prob.close()
     ctx.close()
 

@@ -320,6 +320,6 @@ def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
             prob.solver().apply_preconditioner(z, r)
             out[flag] = (y.numpy(), r.numpy())
     finally:
-        ctx.set_option("fp32_bulk_spmv", 1)
+        ctx.set_option("fp32_bulk_spmv", 0)  # the library default
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
