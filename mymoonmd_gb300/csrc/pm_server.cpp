@@ -155,9 +155,11 @@ void pm_server::worker(int index) {
       } else {
         const int64_t before = pm::g_thread_dev_bytes;
         pm_problem* p = nullptr;
-        const char* prm = rq.kind == 1 ? params_stokes.c_str() : params_cd.c_str();
-        if (rq.kind == 1) rc = pm_problem_create_stokes(ctx, setup->disc, rq.nu, prm, &p);
-        else rc = pm_problem_create_cd(ctx, setup->disc, &rq.coeffs, 0, prm, &p);
+        // the multigrid runs over all levels of the request (a later key wins)
+        const std::string prm = (rq.kind == 1 ? params_stokes : params_cd) +
+                                "\nmultigrid_n_levels: " + std::to_string(rq.n_levels) + "\n";
+        if (rq.kind == 1) rc = pm_problem_create_stokes(ctx, setup->disc, rq.nu, prm.c_str(), &p);
+        else rc = pm_problem_create_cd(ctx, setup->disc, &rq.coeffs, 0, prm.c_str(), &p);
         if (rc == PM_OK) {
           Cached c;
           c.p = p;

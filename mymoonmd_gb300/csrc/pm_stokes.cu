@@ -890,6 +890,7 @@ __global__ void __launch_bounds__(128) k_nodal_local(const int* __restrict__ gua
   const T* A = ainv + aoff[i];
   for (int a = lane; a < m; a += 32) {
     T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll 8
     for (int b = 0; b < m; ++b) {
       const T q = A[size_t(b) * m + a];
       s0 += q * rl[wi][b];
@@ -919,7 +920,9 @@ __global__ void __launch_bounds__(128) k_nodal_local(const int* __restrict__ gua
   }
 }
 
-// local residuals b - V x of the patches of one colour (one warp per patch)
+// local residuals b - V x of the patches of one colour: one block per patch,
+// four lanes per row (32 rows at a time), eight loads in flight per lane, the
+// four partial sums combined by two shuffle steps
 template <class T>
 __global__ void __launch_bounds__(128) k_nodal_rhs(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                    const int* __restrict__ vptr, const int* __restrict__ vidx,
@@ -927,18 +930,42 @@ __global__ void __launch_bounds__(128) k_nodal_rhs(const int* __restrict__ guard
                                                    const T* __restrict__ v, const T* __restrict__ b,
                                                    const T* __restrict__ x, T* __restrict__ rloc) {
   if (guarded(guard)) return;  // uniform for the whole grid
-  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int idx = blockIdx.x * 4 + wi;
+  constexpr int L = 4, U = 8;
+  const int idx = blockIdx.x;
   if (idx >= cnt) return;
   const int i = patches[idx];
   const int m = vptr[i + 1] - vptr[i];
   const int* nodes = vidx + vptr[i];
   const size_t off = 3 * size_t(vptr[i]) + i;
-  for (int e = lane; e < 3 * m + 1; e += 32) {
-    const int g = e < 3 * m ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
-    T s = b[g];
-    for (int k = rp[g]; k < rp[g + 1]; ++k) s -= v[k] * x[ci[k]];
-    rloc[off + e] = s;
+  const int lane = threadIdx.x & (L - 1);
+  const int rows = 3 * m + 1;
+  // every thread of the block runs the same number of passes (the shuffles
+  // need whole groups)
+  for (int e0 = 0; e0 < rows; e0 += 128 / L) {
+    const int e = e0 + int(threadIdx.x) / L;
+    const bool valid = e < rows;
+    int g = 0, beg = 0, end = 0;
+    if (valid) {
+      g = e < 3 * m ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
+      beg = rp[g];
+      end = rp[g + 1];
+    }
+    T s = T(0);
+    for (int base = beg; base < end; base += L * U) {
+      T vv[U], xv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = base + u * L + lane;
+        const bool in = k < end;
+        vv[u] = in ? v[k] : T(0);
+        xv[u] = in ? x[ci[k]] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) s += vv[u] * xv[u];
+    }
+    s += __shfl_xor_sync(0xffffffffu, s, 1, L);
+    s += __shfl_xor_sync(0xffffffffu, s, 2, L);
+    if (valid && lane == 0) rloc[off + e] = b[g] - s;
   }
 }
 
@@ -963,7 +990,7 @@ static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T
     const int beg = nv.color_ptr[k], cnt = nv.color_ptr[k + 1] - beg;
     if (!cnt) continue;
     const int* pts = nv.color_patches.p + beg;
-    k_nodal_rhs<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
+    k_nodal_rhs<T><<<cnt, 128, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
                                                         V.cols.p, vals, b, x, rloc);
     k_nodal_local<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
                                                           tb, sinv, nullptr, rloc, nullptr, x, damp);

@@ -9,7 +9,8 @@
         one assembly of the four 32^3 Q2 levels
     python -m mymoonmd_gb300.profile_cases stokes [--precision ...] [--smoother ...] [--coarse ...]
         one warm-up request, then one request of the 3D Stokes P2/P1 workload
-        (24^3 cubes x 6 tetrahedra, 368,572 DOFs, 3 levels, V(1,1) Vanka)
+        (24^3 cubes x 6 tetrahedra, 368,572 DOFs, 3 levels, V(1,1) Vanka);
+        --cubes 12 runs the 12^3 mesh of the same family
 
 Each case prints what it ran; device memory stays below 2 GB.
 """
@@ -53,7 +54,8 @@ def main() -> None:
     ap.add_argument("case", choices=["request", "spmv", "assembly", "stokes"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
-    ap.add_argument("--coarse", default="nodal_vanka")
+    ap.add_argument("--coarse", default="nodal_vanka_jacobi")
+    ap.add_argument("--cubes", type=int, default=24, choices=[12, 24])
     args = ap.parse_args()
     ctx = m.Context(0)
     if args.case == "stokes":
@@ -61,10 +63,10 @@ def main() -> None:
         db["multigrid_n_levels"] = 3
         db["multigrid_smoother"] = args.smoother
         db["multigrid_smoother_coarse"] = args.coarse
-        db["multigrid_vanka_damp_factor"] = 0.8 if args.smoother.endswith("jacobi") else 1.0
+        db["multigrid_vanka_damp_factor"] = 0.8
         db["multigrid_n_pre_smooth"] = 1
         db["multigrid_n_post_smooth"] = 1
-        disc = m.Discretization(m.GEO_CUBE_TETRA, 3, 3, 3, m.KIND_STOKES, 12)
+        disc = m.Discretization(m.GEO_CUBE_TETRA, 3, 3 if args.cubes == 24 else 2, 3, m.KIND_STOKES, 12)
         prob = m.StokesProblem(ctx, disc, 1.0, db)
         for _ in range(2):
             prob.reset_solution()

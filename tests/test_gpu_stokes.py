@@ -112,8 +112,10 @@ def test_stokes_fgmres_iterates_match_oracle(ctx, smoother, okind, damp):
 
 @pytest.mark.parametrize("smoother,okind,damp", NODAL)
 def test_stokes_nodal_vanka_solution_matches_oracle(ctx, smoother, okind, damp):
-    """FGMRES(30) with nodal-Vanka V(1,1) multigrid on three levels to 1e-10:
-    iteration counts within one, solutions within 1e-10"""
+    """FGMRES with nodal-Vanka V(1,1) multigrid on three levels to 1e-10:
+    iteration counts within one; both solutions meet the 1e-10 residual, so they
+    agree to about that level: velocity within 1e-9, the (mean-free) pressure,
+    the less well conditioned unknown, within 1e-8"""
     # restart 60: no restart inside the run (a restart amplifies rounding differences)
     db = stokes_db(3, smoother, damp, max_it=100, reduction=1e-10, restart=60)
     disc, prob, ora = make_pair(ctx, 1, 3, 3, db)
@@ -126,7 +128,7 @@ def test_stokes_nodal_vanka_solution_matches_oracle(ctx, smoother, okind, damp):
     assert res <= 1e-10 * init
     u, p = split(prob.solution(), ora.finest)
     ou, op = split(sol, ora.finest)
-    assert rel(u, ou) <= 1e-10 and rel(p, op) <= 1e-9
+    assert rel(u, ou) <= 1e-9 and rel(p, op) <= 1e-8
 
 
 def test_stokes_mixed_precision_reaches_fp64_target(ctx):
@@ -179,6 +181,24 @@ def test_stokes_iterative_coarse_level_matches_oracle(ctx, coarse_residual):
     ora.build_mg(smoother="nodal_color", coarse_smoother="nodal_color", vanka_damp=1.0, n_pre=1, n_post=1,
                  coarse_max_it=10, coarse_residual=coarse_residual)
     z = np.random.default_rng(11).standard_normal(ora.finest.n)
+    zd = m.DeviceVector.from_numpy(ctx, z)
+    rd = m.DeviceVector(ctx, z.size)
+    prob.solver().apply_preconditioner(zd, rd)
+    assert rel(rd.numpy(), ora.mg_apply(z)) <= 1e-10
+
+
+def test_stokes_workload_multigrid_matches_oracle(ctx):
+    """the 3D Stokes workload's multigrid: colour-ordered nodal Vanka on the fine
+    levels, additive nodal Vanka on the coarsest (at most 10 sweeps, stop at 0.1),
+    damping 0.8, one V(1,1) cycle"""
+    db = stokes_db(3, "nodal_vanka", 0.8, coarse="nodal_vanka_jacobi")
+    db["multigrid_coarse_max_n_iterations"] = 10
+    db["multigrid_coarse_residual"] = 0.1
+    disc, prob, ora = make_pair(ctx, 3, 2, 3, db)
+    prob.solve()
+    ora.build_mg(smoother="nodal_color", coarse_smoother="nodal_jacobi", vanka_damp=0.8, n_pre=1, n_post=1,
+                 coarse_max_it=10, coarse_residual=0.1)
+    z = np.random.default_rng(13).standard_normal(ora.finest.n)
     zd = m.DeviceVector.from_numpy(ctx, z)
     rd = m.DeviceVector(ctx, z.size)
     prob.solver().apply_preconditioner(zd, rd)
