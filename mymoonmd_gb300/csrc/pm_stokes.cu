@@ -856,27 +856,33 @@ void DevNodalVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
 
 namespace pm {
 
-// one warp per patch: local residual (gathered from the global residual r or
-// read from rloc), w_k = A^{-1} r_k, p, u_k; the damped correction is written
-// to the local storage (additive sweep) or added into x (colour sweep)
+// one block of 256 threads per patch: local residual (gathered from the
+// global residual r or read from rloc), w_k = A^{-1} r_k for the three
+// components (four threads per row, each summing a quarter of the columns of
+// A^{-1}, combined in a fixed order), the pressure from the Schur complement,
+// u_k = w_k - t_k p; the damped correction is written to the local storage
+// (additive sweep) or added into x (colour sweep)
 template <class T>
-__global__ void __launch_bounds__(128) k_nodal_local(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
+__global__ void __launch_bounds__(256) k_nodal_local(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                      const int* __restrict__ vptr, const int* __restrict__ vidx,
                                                      const int64_t* __restrict__ aoff, const T* __restrict__ ainv,
                                                      const T* __restrict__ tb, const T* __restrict__ sinv,
                                                      const T* __restrict__ r, const T* __restrict__ rloc,
                                                      T* __restrict__ out, T* __restrict__ x, T damp) {
   if (guarded(guard)) return;  // uniform for the whole grid
-  __shared__ T rl[4][3 * kNodalMaxNodes + 1];
-  __shared__ T w[4][3 * kNodalMaxNodes];
-  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int idx = blockIdx.x * 4 + wi;
-  if (idx >= cnt) return;  // uniform per warp; no block-wide barrier below
+  constexpr int P = 4;  // threads per row
+  __shared__ T rl[3 * kNodalMaxNodes + 1];
+  __shared__ T w[3 * kNodalMaxNodes];
+  __shared__ T part[P][3][64];
+  __shared__ T red[8];
+  const int idx = blockIdx.x;
+  if (idx >= cnt) return;
+  const int t = threadIdx.x;
   const int i = patches ? patches[idx] : idx;
   const int m = vptr[i + 1] - vptr[i];
   const int* nodes = vidx + vptr[i];
   const size_t off = 3 * size_t(vptr[i]) + i;
-  for (int e = lane; e < 3 * m + 1; e += 32) {
+  for (int e = t; e < 3 * m + 1; e += blockDim.x) {
     T val;
     if (rloc) {
       val = rloc[off + e];
@@ -884,53 +890,71 @@ __global__ void __launch_bounds__(128) k_nodal_local(const int* __restrict__ gua
       const int g = e < 3 * m ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
       val = r[g];
     }
-    rl[wi][e] = val;
+    rl[e] = val;
   }
-  __syncwarp();
+  __syncthreads();
   const T* A = ainv + aoff[i];
-  for (int a = lane; a < m; a += 32) {
+  const int q = t >> 6;        // column quarter
+  const int lr = t & 63;       // row within the pass
+  const int qlen = (m + P - 1) / P;
+  const int b0 = q * qlen, b1 = min(m, b0 + qlen);
+  for (int a0 = 0; a0 < m; a0 += 64) {
+    const int a = a0 + lr;
     T s0 = T(0), s1 = T(0), s2 = T(0);
-#pragma unroll 8
-    for (int b = 0; b < m; ++b) {
-      const T q = A[size_t(b) * m + a];
-      s0 += q * rl[wi][b];
-      s1 += q * rl[wi][m + b];
-      s2 += q * rl[wi][2 * m + b];
+    if (a < m) {
+#pragma unroll 4
+      for (int bb = b0; bb < b1; ++bb) {
+        const T qv = A[size_t(bb) * m + a];
+        s0 += qv * rl[bb];
+        s1 += qv * rl[m + bb];
+        s2 += qv * rl[2 * m + bb];
+      }
     }
-    w[wi][a] = s0;
-    w[wi][m + a] = s1;
-    w[wi][2 * m + a] = s2;
+    part[q][0][lr] = s0;
+    part[q][1][lr] = s1;
+    part[q][2][lr] = s2;
+    __syncthreads();
+    if (t < 64 && a < m) {
+      for (int k = 0; k < 3; ++k) w[k * m + a] = ((part[0][k][t] + part[1][k][t]) + part[2][k][t]) + part[3][k][t];
+    }
+    __syncthreads();
   }
-  __syncwarp();
-  const T* t = tb + 6 * size_t(vptr[i]);
-  const T* bb = t + 3 * m;
-  T part = T(0);
-  for (int e = lane; e < 3 * m; e += 32) part += bb[e] * w[wi][e];
-  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-  part = __shfl_sync(0xffffffffu, part, 0);  // one value for every lane
-  const T p = sinv[i] * (rl[wi][3 * m] - part);
-  for (int e = lane; e < 3 * m; e += 32) {
-    const T u = damp * (w[wi][e] - t[e] * p);
+  const T* tt = tb + 6 * size_t(vptr[i]);
+  const T* bb = tt + 3 * m;
+  T d = T(0);
+  for (int e = t; e < 3 * m; e += blockDim.x) d += bb[e] * w[e];
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  if ((t & 31) == 0) red[t >> 5] = d;
+  __syncthreads();
+  if (t == 0) {
+    T sum = T(0);
+    for (int k = 0; k < 8; ++k) sum += red[k];
+    red[0] = sum;
+  }
+  __syncthreads();
+  const T p = sinv[i] * (rl[3 * m] - red[0]);
+  for (int e = t; e < 3 * m; e += blockDim.x) {
+    const T u = damp * (w[e] - tt[e] * p);
     if (x) x[(e / m) * nu + nodes[e % m]] += u;
     else out[off + e] = u;
   }
-  if (lane == 0) {
+  if (t == 0) {
     if (x) x[3 * nu + i] += damp * p;
     else out[off + 3 * m] = damp * p;
   }
 }
 
 // local residuals b - V x of the patches of one colour: one block per patch,
-// four lanes per row (32 rows at a time), eight loads in flight per lane, the
+// four lanes per row (64 rows at a time), eight loads in flight per lane, the
 // four partial sums combined by two shuffle steps
 template <class T>
-__global__ void __launch_bounds__(128) k_nodal_rhs(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
+__global__ void __launch_bounds__(256) k_nodal_rhs(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                    const int* __restrict__ vptr, const int* __restrict__ vidx,
                                                    const int* __restrict__ rp, const int* __restrict__ ci,
                                                    const T* __restrict__ v, const T* __restrict__ b,
                                                    const T* __restrict__ x, T* __restrict__ rloc) {
   if (guarded(guard)) return;  // uniform for the whole grid
-  constexpr int L = 4, U = 8;
+  constexpr int L = 4, U = 8;  // lanes per row, loads in flight per lane
   const int idx = blockIdx.x;
   if (idx >= cnt) return;
   const int i = patches[idx];
@@ -941,7 +965,7 @@ __global__ void __launch_bounds__(128) k_nodal_rhs(const int* __restrict__ guard
   const int rows = 3 * m + 1;
   // every thread of the block runs the same number of passes (the shuffles
   // need whole groups)
-  for (int e0 = 0; e0 < rows; e0 += 128 / L) {
+  for (int e0 = 0; e0 < rows; e0 += int(blockDim.x) / L) {
     const int e = e0 + int(threadIdx.x) / L;
     const bool valid = e < rows;
     int g = 0, beg = 0, end = 0;
@@ -974,7 +998,7 @@ static void nodal_jacobi(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T*
                          T* sol, const T* b, T* x, T* r, T damp) {
   if constexpr (sizeof(T) == 8) csr_apply(c, V, EPI_DEFECT, x, r, b, 1.0);
   else csr_apply32(c, V, EPI_DEFECT, x, r, b, 1.0f);
-  k_nodal_local<T><<<(nv.np + 3) / 4, 128, 0, c->stream>>>(c->guard, nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
+  k_nodal_local<T><<<nv.np, 256, 0, c->stream>>>(c->guard, nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
                                                           ainv, tb, sinv, r, nullptr, sol, nullptr, damp);
   const int g = std::max(1, std::min((nv.n + 255) / 256, c->num_sms * 16));
   k_vanka_average<T><<<g, 256, 0, c->stream>>>(c->guard, nv.n, nv.inc_ptr.p, nv.inc_idx.p, nv.count.p, sol, x);
@@ -990,9 +1014,9 @@ static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T
     const int beg = nv.color_ptr[k], cnt = nv.color_ptr[k + 1] - beg;
     if (!cnt) continue;
     const int* pts = nv.color_patches.p + beg;
-    k_nodal_rhs<T><<<cnt, 128, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
+    k_nodal_rhs<T><<<cnt, 256, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
                                                         V.cols.p, vals, b, x, rloc);
-    k_nodal_local<T><<<(cnt + 3) / 4, 128, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
+    k_nodal_local<T><<<cnt, 256, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
                                                           tb, sinv, nullptr, rloc, nullptr, x, damp);
     c->kernel_launches += 2;
   }
