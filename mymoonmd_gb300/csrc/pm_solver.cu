@@ -110,9 +110,27 @@ void Multigrid::configure(const Params& p) {
   std::string type = p.str("multigrid_type", "standard");
   if (type != "standard") throw Error(PM_E_UNSUPPORTED, "only standard multigrid is implemented");
   mixed = p.str("gpu_precision", "fp64") == "mixed";
+  mixed_cfg = mixed;
+}
+
+void Multigrid::set_mixed(pm_ctx* c, bool on) {
+  if (on == mixed) return;
+  if (on && !mixed_cfg) throw Error(PM_E_INVALID, "the multigrid was not set up for the mixed form");
+  if (!on && !fp64_smoothers) {
+    for (auto& lv : levels) {
+      const bool vanka = lv.smoother == SM_CELL_VANKA || lv.smoother == SM_CELL_VANKA_JACOBI;
+      const bool nodal = lv.smoother == SM_NODAL_VANKA || lv.smoother == SM_NODAL_VANKA_JACOBI;
+      if (vanka) lv.vanka->factor(c, lv.proj->csr, false);
+      if (nodal) lv.nodal->factor(c, lv.proj->csr, false);
+    }
+    fp64_smoothers = true;
+  }
+  mixed = on;
 }
 
 void Multigrid::update(pm_ctx* c) {
+  mixed = mixed_cfg;
+  fp64_smoothers = !mixed;
   const int L = int(levels.size());
   if (L < 2) throw Error(PM_E_INVALID, "for multigrid you need at least two multigrid levels");
   for (int l = 0; l < L; ++l)
@@ -670,6 +688,8 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   }
   double* partA = c->partials.p;
   double* partB = c->partials.p + kRedBlocks;
+  if (use_mg && mg.mixed_cfg) mg.set_mixed(c, true);  // every solve starts in the mixed form
+  std::vector<double> res_hist;  // residual after each iteration (for the fallback test)
 
   csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);  // r = rhs - A sol
   dot_partials(c, n, r, r, partA);
@@ -734,13 +754,15 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
       };
       // the probe brackets launches with events one by one: no graphs then
       const bool graphs = use_graphs && c->probe_nnz == 0;
+      // one graph per Arnoldi index and multigrid precision
+      const int gi = i + ((use_mg && !mg.mixed && mg.mixed_cfg) ? m : 0);
       if (graphs) {
-        if (arnoldi_graphs.size() != size_t(m)) {
+        if (arnoldi_graphs.size() != size_t(2 * m)) {
           drop_graphs();
-          arnoldi_graphs.assign(m, nullptr);
-          arnoldi_launches.assign(m, 0);
+          arnoldi_graphs.assign(2 * m, nullptr);
+          arnoldi_launches.assign(2 * m, 0);
         }
-        if (!arnoldi_graphs[i]) {
+        if (!arnoldi_graphs[gi]) {
           const uint64_t before = c->kernel_launches;
           cudaGraph_t g = nullptr;
           PM_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -756,12 +778,12 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
           cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
           cudaGraphDestroy(g);
           PM_CUDA(e);
-          arnoldi_graphs[i] = ex;
-          arnoldi_launches[i] = c->kernel_launches - before;
+          arnoldi_graphs[gi] = ex;
+          arnoldi_launches[gi] = c->kernel_launches - before;
           c->kernel_launches = before;
         }
-        PM_CUDA(cudaGraphLaunch(arnoldi_graphs[i], c->stream));
-        c->kernel_launches += arnoldi_launches[i];
+        PM_CUDA(cudaGraphLaunch(arnoldi_graphs[gi], c->stream));
+        c->kernel_launches += arnoldi_launches[gi];
       } else {
         arnoldi_step();
       }
@@ -769,6 +791,10 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
       resid = c->host_scalars[0];
       if (*reinterpret_cast<int*>(c->host_scalars + 1))
         throw Error(PM_E_BREAKDOWN, "Unhappy breakdown in flexible gmres Iteration " + std::to_string(j));
+      res_hist.push_back(resid);
+      if (use_mg && mg.mixed && mixed_fallback && res_hist.size() > 10 &&
+          !(resid <= 0.5 * res_hist[res_hist.size() - 11]))
+        mg.set_mixed(c, false);  // the FP32 cycle stalled: FP64 from the next iteration on
       if (converged(resid, j)) {
         k_fg_backsolve<<<1, 32, 0, c->stream>>>(ldh, i, H, s, y);
         k_fg_combine<<<grid_blocks_for(n), 256, 0, c->stream>>>(n, i, Z, ld, y, sol);

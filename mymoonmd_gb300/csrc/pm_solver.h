@@ -65,7 +65,9 @@ struct Multigrid {
   int coarse_max_it = 10;
   int smoother = SM_JACOBI, smoother_coarse = SM_DIRECT;
   std::string cycle_type = "V";
-  bool mixed = false;
+  bool mixed = false;       // the precision the cycle runs in now
+  bool mixed_cfg = false;   // the precision the database asked for
+  bool fp64_smoothers = false;  // FP64 Vanka factors exist for the current matrices
   bool ready = false;
 
   void configure(const Params& p);
@@ -77,6 +79,10 @@ struct Multigrid {
   void restrict_to(pm_ctx* c, int l);  // from l to l-1
   void prolongate_from(pm_ctx* c, int l);  // from l to l+1
   void coarse_solve(pm_ctx* c);
+  // switch the cycle between FP32 and FP64 (FGMRES is flexible, so the
+  // preconditioner may change between iterations); FP64 Vanka factors are
+  // computed on the first switch after an update
+  void set_mixed(pm_ctx* c, bool on);
   // iterative coarsest level (Multigrid::cycle_step): at most coarse_max_it
   // sweeps, each followed by the defect, stopping once its norm is at or below
   // coarse_residual; the test runs on the device (a flag that turns the
@@ -100,6 +106,9 @@ struct pm_solver {
   // Arnoldi orthogonalisation: "mgs" (the reference's modified Gram-Schmidt)
   // or "cgs2" (classical Gram-Schmidt, two passes, batched; FP64 as well)
   std::string gram_schmidt = "mgs";
+  // mixed form: switch the multigrid to FP64 for the rest of a solve when
+  // the FP64 residual has fallen by less than half over 10 iterations
+  bool mixed_fallback = true;
   pm_matrix* A = nullptr;
   pm::Multigrid mg;
   bool use_mg = false;

@@ -3,7 +3,8 @@ allowed values for the solve path.
 
 Defaults follow Solver<>::default_solver_database (src/Solver/Solver.C:21-115)
 and Multigrid::default_multigrid_database (src/Multigrid/Multigrid.C:422-514).
-`gpu_precision` is the one new key (fp64 | mixed).
+New keys with defaults here: `gpu_precision` (fp64 | mixed) and `gpu_mixed_fallback`
+(0 | 1); `gpu_gram_schmidt` and `gpu_cuda_graphs` can be added with `add`.
 """
 from __future__ import annotations
 
@@ -50,6 +51,9 @@ _MG_DEFAULTS: dict[str, tuple[Any, tuple | None]] = {
 
 _GPU_DEFAULTS: dict[str, tuple[Any, tuple | None]] = {
     "gpu_precision": ("fp64", ("fp64", "mixed")),
+    # mixed form: the multigrid switches to FP64 for the rest of a solve when
+    # the FP64 residual falls by less than half over 10 FGMRES iterations
+    "gpu_mixed_fallback": (1, (0, 1)),
 }
 
 

@@ -323,3 +323,33 @@ def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
         ctx.set_option("fp32_bulk_spmv", 0)  # the library default
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+FALLBACK_CASES = [(3, 16, 2, 1e-3, (0.8, 0.6, 0.0)), (2, 64, 1, 2e-3, (1.0, 0.0)), (3, 8, 2, 5e-3, (0.0, 0.6, 0.8)),
+                  (2, 128, 2, 1.5e-3, (0.6, -0.8))]
+
+
+@pytest.mark.parametrize("dim,cells,elem,eps,b", FALLBACK_CASES)
+def test_mixed_form_with_fallback_converges_where_fp64_does(ctx, dim, cells, elem, eps, b):
+    """convection-dominated requests of the batched stream's kind: the FP32
+    multigrid may stall; the mixed form then switches the multigrid to FP64
+    (gpu_mixed_fallback, on by default) and must still reach the 1e-8 FP64
+    residual wherever the FP64 form does, with the same solution"""
+    from mymoonmd_gb300 import workloads as wl
+    rq = wl.cd_request(dim, cells, elem, eps, b)
+    disc = m.Discretization(rq["geometry"], rq["root_n"], rq["n_refine"], rq["n_levels"], m.KIND_CD, elem)
+    cf = m.cd_coeffs(eps, rq["b"], 0.0, True)
+    out = {}
+    for precision in ("fp64", "mixed"):
+        db = mg_db(rq["n_levels"], restart=30, reduction=1e-8, precision=precision)
+        db["max_n_iterations"] = 200
+        prob = m.ConvectionDiffusion(ctx, disc, cf, db)
+        prob.assemble()
+        prob.solve()
+        out[precision] = (prob.solution(), *prob.last_info())
+    sol64, it64, res64, init64 = out["fp64"]
+    if not res64 <= 1e-8 * init64:
+        pytest.skip("the FP64 form does not converge on this case either")
+    solm, itm, resm, initm = out["mixed"]
+    assert resm <= 1e-8 * initm, (itm, it64)
+    assert rel(solm, sol64) <= 1e-6
