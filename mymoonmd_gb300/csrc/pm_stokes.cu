@@ -856,25 +856,25 @@ void DevNodalVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
 
 namespace pm {
 
-// one block of 256 threads per patch: local residual (gathered from the
+// one block of 512 threads per patch: local residual (gathered from the
 // global residual r or read from rloc), w_k = A^{-1} r_k for the three
 // components (four threads per row, each summing a quarter of the columns of
 // A^{-1}, combined in a fixed order), the pressure from the Schur complement,
 // u_k = w_k - t_k p; the damped correction is written to the local storage
 // (additive sweep) or added into x (colour sweep)
 template <class T>
-__global__ void __launch_bounds__(256) k_nodal_local(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
+__global__ void __launch_bounds__(512) k_nodal_local(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                      const int* __restrict__ vptr, const int* __restrict__ vidx,
                                                      const int64_t* __restrict__ aoff, const T* __restrict__ ainv,
                                                      const T* __restrict__ tb, const T* __restrict__ sinv,
                                                      const T* __restrict__ r, const T* __restrict__ rloc,
                                                      T* __restrict__ out, T* __restrict__ x, T damp) {
   if (guarded(guard)) return;  // uniform for the whole grid
-  constexpr int P = 4;  // threads per row
+  constexpr int P = 4, R = 128;  // threads per row, rows per pass
   __shared__ T rl[3 * kNodalMaxNodes + 1];
   __shared__ T w[3 * kNodalMaxNodes];
-  __shared__ T part[P][3][64];
-  __shared__ T red[8];
+  __shared__ T part[P][3][R];
+  __shared__ T red[16];
   const int idx = blockIdx.x;
   if (idx >= cnt) return;
   const int t = threadIdx.x;
@@ -894,11 +894,11 @@ __global__ void __launch_bounds__(256) k_nodal_local(const int* __restrict__ gua
   }
   __syncthreads();
   const T* A = ainv + aoff[i];
-  const int q = t >> 6;        // column quarter
-  const int lr = t & 63;       // row within the pass
+  const int q = t / R;        // column quarter
+  const int lr = t % R;       // row within the pass
   const int qlen = (m + P - 1) / P;
   const int b0 = q * qlen, b1 = min(m, b0 + qlen);
-  for (int a0 = 0; a0 < m; a0 += 64) {
+  for (int a0 = 0; a0 < m; a0 += R) {
     const int a = a0 + lr;
     T s0 = T(0), s1 = T(0), s2 = T(0);
     if (a < m) {
@@ -914,7 +914,7 @@ __global__ void __launch_bounds__(256) k_nodal_local(const int* __restrict__ gua
     part[q][1][lr] = s1;
     part[q][2][lr] = s2;
     __syncthreads();
-    if (t < 64 && a < m) {
+    if (t < R && a < m) {
       for (int k = 0; k < 3; ++k) w[k * m + a] = ((part[0][k][t] + part[1][k][t]) + part[2][k][t]) + part[3][k][t];
     }
     __syncthreads();
@@ -928,7 +928,7 @@ __global__ void __launch_bounds__(256) k_nodal_local(const int* __restrict__ gua
   __syncthreads();
   if (t == 0) {
     T sum = T(0);
-    for (int k = 0; k < 8; ++k) sum += red[k];
+    for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
     red[0] = sum;
   }
   __syncthreads();
@@ -945,10 +945,10 @@ __global__ void __launch_bounds__(256) k_nodal_local(const int* __restrict__ gua
 }
 
 // local residuals b - V x of the patches of one colour: one block per patch,
-// four lanes per row (64 rows at a time), eight loads in flight per lane, the
+// four lanes per row (128 rows at a time), eight loads in flight per lane, the
 // four partial sums combined by two shuffle steps
 template <class T>
-__global__ void __launch_bounds__(256) k_nodal_rhs(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
+__global__ void __launch_bounds__(512) k_nodal_rhs(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                    const int* __restrict__ vptr, const int* __restrict__ vidx,
                                                    const int* __restrict__ rp, const int* __restrict__ ci,
                                                    const T* __restrict__ v, const T* __restrict__ b,
@@ -998,7 +998,7 @@ static void nodal_jacobi(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T*
                          T* sol, const T* b, T* x, T* r, T damp) {
   if constexpr (sizeof(T) == 8) csr_apply(c, V, EPI_DEFECT, x, r, b, 1.0);
   else csr_apply32(c, V, EPI_DEFECT, x, r, b, 1.0f);
-  k_nodal_local<T><<<nv.np, 256, 0, c->stream>>>(c->guard, nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
+  k_nodal_local<T><<<nv.np, 512, 0, c->stream>>>(c->guard, nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
                                                           ainv, tb, sinv, r, nullptr, sol, nullptr, damp);
   const int g = std::max(1, std::min((nv.n + 255) / 256, c->num_sms * 16));
   k_vanka_average<T><<<g, 256, 0, c->stream>>>(c->guard, nv.n, nv.inc_ptr.p, nv.inc_idx.p, nv.count.p, sol, x);
@@ -1014,9 +1014,9 @@ static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T
     const int beg = nv.color_ptr[k], cnt = nv.color_ptr[k + 1] - beg;
     if (!cnt) continue;
     const int* pts = nv.color_patches.p + beg;
-    k_nodal_rhs<T><<<cnt, 256, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
+    k_nodal_rhs<T><<<cnt, 512, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
                                                         V.cols.p, vals, b, x, rloc);
-    k_nodal_local<T><<<cnt, 256, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
+    k_nodal_local<T><<<cnt, 512, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
                                                           tb, sinv, nullptr, rloc, nullptr, x, damp);
     c->kernel_launches += 2;
   }
