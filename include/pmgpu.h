@@ -143,8 +143,17 @@ int pm_scal(pm_ctx* ctx, int n, double a, double* x_dev);
  * src/Multigrid/Multigrid.C:422-514), e.g.
  *   solver_type: iterative       iterative_solver_type: fgmres
  *   preconditioner: multigrid    residual_reduction: 1e-8
- * New key: gpu_precision {fp64, mixed} (mixed = FP32 multigrid inside FP64
- * FGMRES). Unknown keys are ignored like ParameterDatabase::merge(.., false). */
+ * New keys (no reference counterpart):
+ *   gpu_precision {fp64, mixed}: mixed = FP32 multigrid inside FP64 FGMRES;
+ *   gpu_mixed_fallback {1, 0}: in the mixed form, the multigrid switches to
+ *     FP64 for the rest of a solve once the FP64 residual has fallen by less
+ *     than half over 10 iterations (FGMRES is flexible);
+ *   gpu_gram_schmidt {mgs, cgs2, cgs2_cond}: Arnoldi orthogonalisation; mgs is
+ *     the reference's (default for fp64), cgs2 two batched classical passes,
+ *     cgs2_cond the second pass only when the first lost more than a factor
+ *     1/sqrt(2) of the norm (default for mixed);
+ *   gpu_cuda_graphs {1, 0}: Arnoldi steps captured as CUDA graphs.
+ * Unknown keys are ignored like ParameterDatabase::merge(.., false). */
 int pm_solver_create(pm_ctx* ctx, const char* params, pm_solver** out);
 void pm_solver_destroy(pm_solver* s);
 /* Solver::update_matrix (src/Solver/Solver.C:261). With preconditioner

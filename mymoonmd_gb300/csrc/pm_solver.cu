@@ -453,11 +453,23 @@ __global__ void __launch_bounds__(256) k_fg_start(int n, int m, const double* __
 // alternative to the modified Gram-Schmidt loop: the i+1 projections of one
 // pass are computed in one sweep over the vectors and subtracted in another.
 // Partial sums: part[k * kRedBlocks + block], CH accumulators per sweep.
+// with_rr: also <r, r> into slot nk (the norm before the pass, for the
+// conditional second pass); guard: a set flag skips the launch
 template <int CH>
 __global__ void __launch_bounds__(256) k_multidot(int n, int nk, const double* __restrict__ r,
                                                   const double* __restrict__ V, size_t ld,
-                                                  double* __restrict__ part) {
+                                                  double* __restrict__ part, int with_rr,
+                                                  const int* __restrict__ guard) {
   __shared__ double sh[256];
+  if (guarded(guard)) return;  // uniform for the whole grid
+  if (with_rr) {
+    double acc = 0.0;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+      const double ri = r[idx];
+      acc += ri * ri;
+    }
+    block_partial(acc, sh, part + (size_t)nk * kRedBlocks);
+  }
   for (int k0 = 0; k0 < nk; k0 += CH) {
     double acc[CH];
 #pragma unroll
@@ -476,11 +488,19 @@ __global__ void __launch_bounds__(256) k_multidot(int n, int nk, const double* _
 
 // h[k] = sum of the partials of projection k (one block per k); with hsum,
 // also H(k, col) = hsum[k] + h[k]
+// guard set (second pass skipped): h[k] = 0 and H(k, col) = hsum[k]
 __global__ void __launch_bounds__(256) k_reduce_proj(const double* __restrict__ part, double* __restrict__ h,
                                                      const double* __restrict__ hsum, double* __restrict__ H,
-                                                     int ldh, int col) {
+                                                     int ldh, int col, const int* __restrict__ guard) {
   __shared__ double sh[256];
   const int k = blockIdx.x;
+  if (guarded(guard)) {  // uniform for the whole grid
+    if (threadIdx.x == 0) {
+      h[k] = 0.0;
+      if (hsum) H[k + (size_t)ldh * col] = hsum[k];
+    }
+    return;
+  }
   const double s = sum_partials(part + (size_t)k * kRedBlocks, sh);
   if (threadIdx.x == 0) {
     h[k] = s;
@@ -491,8 +511,9 @@ __global__ void __launch_bounds__(256) k_reduce_proj(const double* __restrict__ 
 // r -= sum_k h[k] V_k, subtracted in k order
 __global__ void __launch_bounds__(256) k_cgs_update(int n, int nk, double* __restrict__ r,
                                                     const double* __restrict__ V, size_t ld,
-                                                    const double* __restrict__ h) {
+                                                    const double* __restrict__ h, const int* __restrict__ guard) {
   __shared__ double hs[64];
+  if (guarded(guard)) return;  // uniform for the whole grid
   for (int k = threadIdx.x; k < nk; k += blockDim.x) hs[k] = h[k];
   __syncthreads();
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
@@ -500,6 +521,15 @@ __global__ void __launch_bounds__(256) k_cgs_update(int n, int nk, double* __res
     for (int k = 0; k < nk; ++k) ri -= hs[k] * V[(size_t)k * ld + idx];
     r[idx] = ri;
   }
+}
+
+// DGKS test after the first classical Gram-Schmidt pass: the second pass is
+// needed only if |r after| < |r before| / sqrt(2); flag = 1 skips it
+__global__ void k_cgs_decide(const double* __restrict__ part_after, const double* __restrict__ rr_before,
+                             int* __restrict__ flag) {
+  __shared__ double sh[256];
+  const double after = sum_partials(part_after, sh);
+  if (threadIdx.x == 0) *flag = (after >= 0.5 * rr_before[0]) ? 1 : 0;
 }
 
 __device__ void gen_rot(double dx, double dy, double& cs, double& sn) {
@@ -673,9 +703,9 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   double* cgs_part = dres + 8;                 // 64 x kRedBlocks partial sums
   double* h1 = cgs_part + 64 * size_t(kRedBlocks);
   double* h2 = h1 + 64;
-  if (!flags.p) {
+  if (flags.n < 2) {  // [0] breakdown, [1] skip of the second Gram-Schmidt pass
     drop_graphs();
-    flags.alloc(1);
+    flags.alloc(2);
   }
   PM_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), c->stream));
   PM_CUDA(cudaMemsetAsync(H, 0, sizeof(double) * size_t(ldh) * m, c->stream));
@@ -700,7 +730,8 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   if (converged(resid, 0)) return;
 
   const int grid = kRedBlocks;
-  const bool cgs2 = gram_schmidt == "cgs2";
+  const bool cgs_cond = gram_schmidt == "cgs2_cond";
+  const bool cgs2 = gram_schmidt == "cgs2" || cgs_cond;
   unsigned j = 1;
   while (j <= (unsigned long)max_it) {
     // v_0 = r / beta, s = (beta, 0, ...)   (partA holds <r,r>)
@@ -719,15 +750,24 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
         csr_apply(c, M, EPI_SET, zi, r, nullptr, 1.0);  // r = A z_i
         double* pin = partA;
         if (cgs2) {
-          // two passes of classical Gram-Schmidt; H(:,i) = h1 + h2
+          // two passes of classical Gram-Schmidt; H(:,i) = h1 + h2. With the
+          // conditional variant the second pass runs only when the first lost
+          // more than a factor 1/sqrt(2) of the norm (decided on the device)
           const int nk = i + 1;
           const int ub = grid_blocks_for(n);
-          k_multidot<8><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
-          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i);
-          k_cgs_update<<<ub, 256, 0, c->stream>>>(n, nk, r, V, ld, h1);
-          k_multidot<8><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
-          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h2, h1, H, ldh, i);
-          k_cgs_update<<<ub, 256, 0, c->stream>>>(n, nk, r, V, ld, h2);
+          k_multidot<8><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part, cgs_cond ? 1 : 0, nullptr);
+          k_reduce_proj<<<nk + (cgs_cond ? 1 : 0), 256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i, nullptr);
+          k_cgs_update<<<ub, 256, 0, c->stream>>>(n, nk, r, V, ld, h1, nullptr);
+          const int* skip = nullptr;
+          if (cgs_cond) {
+            dot_partials(c, n, r, r, partB);
+            k_cgs_decide<<<1, 256, 0, c->stream>>>(partB, h1 + nk, flags.p + 1);
+            c->kernel_launches++;
+            skip = flags.p + 1;
+          }
+          k_multidot<8><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part, 0, skip);
+          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h2, h1, H, ldh, i, skip);
+          k_cgs_update<<<ub, 256, 0, c->stream>>>(n, nk, r, V, ld, h2, skip);
           PM_CHECK_LAUNCH();
           c->kernel_launches += 6;
           dot_partials(c, n, r, r, partA);

@@ -103,8 +103,10 @@ struct pm_solver {
   double tol = 1e-8, reduction = 0.0, divergence = 1e10, stagnation = 1e10, damping = 1.0;
   long max_it = 100, min_it = 0, restart = 20;
   bool mixed = false;
-  // Arnoldi orthogonalisation: "mgs" (the reference's modified Gram-Schmidt)
-  // or "cgs2" (classical Gram-Schmidt, two passes, batched; FP64 as well)
+  // Arnoldi orthogonalisation: "mgs" (the reference's modified Gram-Schmidt),
+  // "cgs2" (classical Gram-Schmidt, two passes, batched; FP64 as well) or
+  // "cgs2_cond" (the second pass only when the first lost more than a factor
+  // 1/sqrt(2) of the norm, the DGKS criterion, decided on the device)
   std::string gram_schmidt = "mgs";
   // mixed form: switch the multigrid to FP64 for the rest of a solve when
   // the FP64 residual has fallen by less than half over 10 iterations

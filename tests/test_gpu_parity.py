@@ -162,11 +162,13 @@ def test_fgmres_multigrid_solution_matches_oracle(ctx, case):
     assert res < 1e-10 * init
 
 
-def test_cgs2_orthogonalisation_matches_mgs_oracle(ctx):
-    """FP64 FGMRES with batched classical Gram-Schmidt (two passes) against the
-    oracle's modified Gram-Schmidt: same solution within 1e-10, iterations within one"""
+@pytest.mark.parametrize("gs", ["cgs2", "cgs2_cond"])
+def test_cgs2_orthogonalisation_matches_mgs_oracle(ctx, gs):
+    """FP64 FGMRES with batched classical Gram-Schmidt (two passes, or the
+    second pass only when the DGKS test asks for it) against the oracle's
+    modified Gram-Schmidt: same solution within 1e-10, iterations within one"""
     db = mg_db(3)
-    db.add("gpu_gram_schmidt", "cgs2")
+    db.add("gpu_gram_schmidt", gs)
     disc, prob, ora = make_pair(ctx, "q2_3d", db)
     prob.solve()
     it, res, init = prob.last_info()
