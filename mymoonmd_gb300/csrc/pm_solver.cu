@@ -740,6 +740,7 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
     c->kernel_launches++;
     int i = 0;
     bool done = false;
+    bool restart_fp64 = false;
     for (; i < m && j <= (unsigned long)max_it; ++i, ++j) {
       // one Arnoldi step: z_i = M^-1 v_i, r = A z_i, modified Gram-Schmidt,
       // H(i+1,i), v_{i+1}, Givens rotation, residual copied to the host
@@ -831,6 +832,13 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
       resid = c->host_scalars[0];
       if (*reinterpret_cast<int*>(c->host_scalars + 1))
         throw Error(PM_E_BREAKDOWN, "Unhappy breakdown in flexible gmres Iteration " + std::to_string(j));
+      if (!std::isfinite(resid) && use_mg && mg.mixed && mixed_fallback) {
+        // the FP32 cycle overflowed: the cycle's Krylov basis is lost; restart
+        // from the current solution with the FP64 multigrid
+        mg.set_mixed(c, false);
+        restart_fp64 = true;
+        break;
+      }
       res_hist.push_back(resid);
       if (use_mg && mg.mixed && mixed_fallback && res_hist.size() > 10 &&
           !(resid <= 0.5 * res_hist[res_hist.size() - 11]))
@@ -845,6 +853,18 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
       }
     }
     if (done) return;
+    if (restart_fp64) {
+      // the solution is unchanged since the start of this cycle
+      csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+      dot_partials(c, n, r, r, partA);
+      finish_sum(c, partA, dres, true);
+      PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      PM_CUDA(cudaStreamSynchronize(c->stream));
+      resid = c->host_scalars[0];
+      if (converged(resid, j)) return;
+      ++j;  // the lost iteration counts
+      continue;
+    }
     k_fg_backsolve<<<1, 32, 0, c->stream>>>(ldh, m - 1, H, s, y);
     k_fg_combine<<<grid_blocks_for(n), 256, 0, c->stream>>>(n, m - 1, Z, ld, y, sol);
     PM_CHECK_LAUNCH();

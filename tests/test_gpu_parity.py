@@ -327,8 +327,8 @@ def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
     assert np.array_equal(out[0][1], out[1][1])
 
 
-FALLBACK_CASES = [(3, 16, 2, 1e-3, (0.8, 0.6, 0.0)), (2, 64, 1, 2e-3, (1.0, 0.0)), (3, 8, 2, 5e-3, (0.0, 0.6, 0.8)),
-                  (2, 128, 2, 1.5e-3, (0.6, -0.8))]
+FALLBACK_CASES = [(3, 16, 2, 1e-2, (0.8, 0.6, 0.0)), (2, 64, 2, 5e-3, (0.8, 0.0)), (3, 24, 1, 3e-3, (0.0, 0.6, 0.8)),
+                  (2, 128, 1, 4e-3, (0.48, -0.64)), (3, 16, 2, 2e-3, (0.5, 0.5, 0.5))]
 
 
 @pytest.mark.parametrize("dim,cells,elem,eps,b", FALLBACK_CASES)
@@ -344,7 +344,7 @@ def test_mixed_form_with_fallback_converges_where_fp64_does(ctx, dim, cells, ele
     out = {}
     for precision in ("fp64", "mixed"):
         db = mg_db(rq["n_levels"], restart=30, reduction=1e-8, precision=precision)
-        db["max_n_iterations"] = 200
+        db["max_n_iterations"] = 300
         prob = m.ConvectionDiffusion(ctx, disc, cf, db)
         prob.assemble()
         prob.solve()
