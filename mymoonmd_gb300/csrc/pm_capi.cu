@@ -408,8 +408,6 @@ int pm_solver_create(pm_ctx* c, const char* params, pm_solver** out) {
     s->gram_schmidt = p.str("gpu_gram_schmidt", s->mixed ? "cgs2_cond" : "mgs");
     if (s->gram_schmidt != "mgs" && s->gram_schmidt != "cgs2" && s->gram_schmidt != "cgs2_cond")
       throw Error(PM_E_INVALID, "gpu_gram_schmidt is mgs, cgs2 or cgs2_cond");
-    if (s->gram_schmidt != "mgs" && s->gram_schmidt != "cgs2")
-      throw Error(PM_E_INVALID, "gpu_gram_schmidt must be mgs or cgs2");
     if (s->prec != "no_preconditioner" && s->prec != "jacobi" && s->prec != "multigrid")
       throw Error(PM_E_UNSUPPORTED, "preconditioner '" + s->prec + "' is not implemented on the GPU");
     s->use_mg = s->solver_type == "iterative" && s->prec == "multigrid";
