@@ -149,9 +149,9 @@ int pm_scal(pm_ctx* ctx, int n, double a, double* x_dev);
  *     FP64 for the rest of a solve once the FP64 residual has fallen by less
  *     than half over 10 iterations (FGMRES is flexible);
  *   gpu_gram_schmidt {mgs, cgs2, cgs2_cond}: Arnoldi orthogonalisation; mgs is
- *     the reference's (default for fp64), cgs2 two batched classical passes,
- *     cgs2_cond the second pass only when the first lost more than a factor
- *     1/sqrt(2) of the norm (default for mixed);
+ *     the reference's (default for fp64), cgs2 two batched classical passes
+ *     (default for mixed), cgs2_cond the second pass only when the first lost
+ *     more than a factor 1/sqrt(2) of the norm;
  *   gpu_cuda_graphs {1, 0}: Arnoldi steps captured as CUDA graphs.
  * Unknown keys are ignored like ParameterDatabase::merge(.., false). */
 int pm_solver_create(pm_ctx* ctx, const char* params, pm_solver** out);

@@ -405,7 +405,7 @@ int pm_solver_create(pm_ctx* c, const char* params, pm_solver** out) {
     s->mixed = p.str("gpu_precision", "fp64") == "mixed";
     s->use_graphs = p.integer("gpu_cuda_graphs", 1) != 0;
     s->mixed_fallback = p.integer("gpu_mixed_fallback", 1) != 0;
-    s->gram_schmidt = p.str("gpu_gram_schmidt", s->mixed ? "cgs2_cond" : "mgs");
+    s->gram_schmidt = p.str("gpu_gram_schmidt", s->mixed ? "cgs2" : "mgs");
     if (s->gram_schmidt != "mgs" && s->gram_schmidt != "cgs2" && s->gram_schmidt != "cgs2_cond")
       throw Error(PM_E_INVALID, "gpu_gram_schmidt is mgs, cgs2 or cgs2_cond");
     if (s->prec != "no_preconditioner" && s->prec != "jacobi" && s->prec != "multigrid")
