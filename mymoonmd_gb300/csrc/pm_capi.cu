@@ -1,6 +1,8 @@
 // extern "C" entry points (include/pmgpu.h). Every call catches the library's
 // exceptions and turns them into status codes plus a per-context message.
+#include <algorithm>
 #include <cstring>
+#include <iterator>
 #include <new>
 #include <string>
 
@@ -73,6 +75,14 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
   }
   if (std::string(key) == "fp32_bulk_spmv") {
     c->bulk_spmv = value != 0;
+    return PM_OK;
+  }
+  if (std::string(key) == "fp32_sliced_spmv") {
+    static const int shapes[] = {0, 140, 141, 180, 240, 241, 280, 440, 441, 480, 481, 840, 841, 881};
+    if (std::find(std::begin(shapes), std::end(shapes), value) == std::end(shapes))
+      return fail(c, PM_E_INVALID,
+                  "fp32_sliced_spmv is 0 or one of 140 141 180 240 241 280 440 441 480 481 840 841 881");
+    c->sell_shape = value;
     return PM_OK;
   }
   if (std::string(key) == "probe_epilogue") {

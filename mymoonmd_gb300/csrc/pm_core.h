@@ -111,6 +111,10 @@ struct pm_ctx {
   // set by kernels whose bounded waits gave up (checked after each solve)
   pm::DBuf<int> dev_error;
   bool bulk_spmv = false;  // FP32 SpMV by the bulk-copy kernel where a matrix allows it
+  // FP32 SpMV by the sliced-ELL kernel: 0 = off, else 100 L + 10 U + P (L lanes
+  // per row, U steps in flight, P = 1: next steps' loads issued before the
+  // current gathers); the matrix copies are laid out for L in make_fp32
+  int sell_shape = 441;
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

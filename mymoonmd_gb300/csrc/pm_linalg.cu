@@ -128,6 +128,87 @@ std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int ma
   return rb;
 }
 
+bool build_sell_layout(int n_rows, const int* rp, const int* ci, int L, int window, std::vector<int>& perm,
+                       std::vector<int>& off, std::vector<int>& cols, std::vector<int>& src) {
+  const int C = 32 / L;
+  if (L < 1 || 32 % L != 0 || window % C != 0) throw Error(PM_E_INVALID, "sliced layout: bad lanes or window");
+  const int n_sl = (n_rows + C - 1) / C;
+  perm.assign(size_t(n_sl) * C, -1);
+  // rows sorted by length, longest first, ties in row order, per window
+  std::vector<int> idx;
+  for (int w0 = 0; w0 < n_rows; w0 += window) {
+    const int w1 = std::min(n_rows, w0 + window);
+    idx.resize(size_t(w1 - w0));
+    for (int i = w0; i < w1; ++i) idx[size_t(i - w0)] = i;
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int a, int b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
+    std::copy(idx.begin(), idx.end(), perm.begin() + w0);
+  }
+  off.assign(size_t(n_sl) + 1, 0);
+  int64_t total = 0;
+  for (int sl = 0; sl < n_sl; ++sl) {
+    int width = 0;
+    for (int q = 0; q < C; ++q) {
+      const int r = perm[size_t(sl) * C + q];
+      if (r >= 0) width = std::max(width, rp[r + 1] - rp[r]);
+    }
+    total += int64_t(32) * ((width + L - 1) / L);
+    if (total > int64_t(0x7fffffff)) return false;
+    off[size_t(sl) + 1] = int(total);
+  }
+  cols.assign(size_t(total), 0);
+  src.assign(size_t(total), -1);
+  for (int sl = 0; sl < n_sl; ++sl) {
+    const int T = (off[size_t(sl) + 1] - off[size_t(sl)]) / 32;
+    for (int q = 0; q < C; ++q) {
+      const int r = perm[size_t(sl) * C + q];
+      const int len = r >= 0 ? rp[r + 1] - rp[r] : 0;
+      // padding repeats the row's last column (its x is already cached)
+      const int pad_col = len > 0 ? ci[rp[r] + len - 1] : 0;
+      for (int t = 0; t < T; ++t)
+        for (int sub = 0; sub < L; ++sub) {
+          const int j = t * L + sub;
+          const size_t slot = size_t(off[size_t(sl)]) + size_t(t) * 32 + size_t(sub) * C + q;
+          if (j < len) {
+            cols[slot] = ci[rp[r] + j];
+            src[slot] = rp[r] + j;
+          } else {
+            cols[slot] = pad_col;
+          }
+        }
+    }
+  }
+  return true;
+}
+
+void DevCsr::build_sell(pm_ctx* c, int L) {
+  sell_lanes = 0;
+  n_slices = 0;
+  sell_entries = 0;
+  std::vector<int> rp(static_cast<size_t>(n_rows) + 1), ci(static_cast<size_t>(nnz));
+  PM_CUDA(cudaMemcpyAsync(rp.data(), row_ptr.p, rp.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (nnz) PM_CUDA(cudaMemcpyAsync(ci.data(), cols.p, ci.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<int> perm, off, sc, src;
+  if (!build_sell_layout(n_rows, rp.data(), ci.data(), L, kSellWindow, perm, off, sc, src)) {
+    sell_perm.release();
+    sell_off.release();
+    sell_cols.release();
+    sell_src.release();
+    sell_vals.release();
+    return;
+  }
+  sell_perm.upload(perm, c->stream);
+  sell_off.upload(off, c->stream);
+  sell_cols.upload(sc, c->stream);
+  sell_src.upload(src, c->stream);
+  sell_vals.ensure(sc.size());
+  PM_CUDA(cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
+  sell_lanes = L;
+  n_slices = int(off.size()) - 1;
+  sell_entries = int64_t(sc.size());
+}
+
 void DevCsr::set_single_block() {
   mask = BlockMask{};
   mask.nb = 1;
@@ -169,7 +250,25 @@ static int grid_for(pm_ctx* c, long long n) {
   return int(std::max<long long>(1, std::min(b, cap)));
 }
 
+__global__ void k_sell_fill(long long n, const int* __restrict__ src, const double* __restrict__ v,
+                            float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = src[i];
+    out[i] = k >= 0 ? float(v[k]) : 0.0f;
+  }
+}
+
 void DevCsr::make_fp32(pm_ctx* c) {
+  // the sliced copy: rows of more than 16 entries on average (the operators
+  // whose FP32 SpMV streams many bytes per row); laid out once per lane count
+  const int want = c->sell_shape / 100;
+  if (want > 0 && want != sell_lanes && nnz > 16 * int64_t(n_rows)) build_sell(c, want);
+  if (sell_lanes && sell_entries) {
+    k_sell_fill<<<grid_for(c, sell_entries), 256, 0, c->stream>>>(sell_entries, sell_src.p, vals.p, sell_vals.p);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
   vals32.ensure(size_t(nnz4()));
   if (nnz4() > nnz)
     PM_CUDA(cudaMemsetAsync(vals32.p + nnz, 0, size_t(nnz4() - nnz) * sizeof(float), c->stream));
@@ -314,6 +413,50 @@ static void launch_bulk(pm_ctx* c, const DevCsr& A, const float* vals, const flo
   c->kernel_launches++;
 }
 
+template <int L, int U, bool P>
+static void launch_sell_shape(pm_ctx* c, const DevCsr& A, int epi, const float* x, float* y, const float* b,
+                              const float* d, float alpha, const BlockMask& m) {
+  const int grid = nblocks(A.n_slices, 4);  // four warps (slices) per block
+  const int* pe = A.sell_perm.p;
+  const int* so = A.sell_off.p;
+  const int* sc = A.sell_cols.p;
+  const float* sv = A.sell_vals.p;
+  const int ns = A.n_slices;
+  switch (epi) {
+    case EPI_AXPY: sell_kernel<L, U, P, EPI_AXPY><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
+    case EPI_SET: sell_kernel<L, U, P, EPI_SET><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
+    case EPI_DEFECT: sell_kernel<L, U, P, EPI_DEFECT><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
+    case EPI_JACOBI: sell_kernel<L, U, P, EPI_JACOBI><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
+    case EPI_RESTRICT: sell_kernel<L, U, P, EPI_RESTRICT><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
+    case EPI_PROLONG: sell_kernel<L, U, P, EPI_PROLONG><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
+    default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
+  }
+}
+
+static void launch_sell(pm_ctx* c, const DevCsr& A, int epi, const float* x, float* y, const float* b,
+                        const float* d, float alpha) {
+  BlockMask mg = A.mask;
+  mg.guard = c->guard;
+  switch (c->sell_shape) {
+    case 140: launch_sell_shape<1, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 141: launch_sell_shape<1, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 180: launch_sell_shape<1, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 240: launch_sell_shape<2, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 241: launch_sell_shape<2, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 280: launch_sell_shape<2, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 440: launch_sell_shape<4, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 441: launch_sell_shape<4, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 480: launch_sell_shape<4, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 481: launch_sell_shape<4, 8, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 840: launch_sell_shape<8, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 841: launch_sell_shape<8, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 881: launch_sell_shape<8, 8, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    default: throw Error(PM_E_INVALID, "unknown sliced SpMV shape " + std::to_string(c->sell_shape));
+  }
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
 template <class TV, class TX, class TA>
 static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* diag, int epi,
                          const TX* x, TX* y, const TX* b, TA alpha, int n) {
@@ -333,6 +476,19 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
     PM_CUDA(cudaEventRecord(e0, c->stream));
     c->probe_events.push_back(e0);
     c->probe_bytes.push_back(epi_bytes(A, epi, int(sizeof(TV)), n));
+  }
+  if constexpr (sizeof(TV) == 4) {
+    if (!(c->bulk_spmv && A.bulk32 && A.n_chunks > 0) && c->sell_shape > 0 && A.sell_lanes == c->sell_shape / 100 &&
+        A.n_slices > 0 && n == A.n_rows) {
+      launch_sell(c, A, epi, reinterpret_cast<const float*>(x), reinterpret_cast<float*>(y),
+                  reinterpret_cast<const float*>(b), reinterpret_cast<const float*>(diag), float(alpha));
+      if (probe) {
+        cudaEvent_t e1 = probe_event(c);
+        PM_CUDA(cudaEventRecord(e1, c->stream));
+        c->probe_events.push_back(e1);
+      }
+      return;
+    }
   }
   // the bulk kernel exists for the two FP32 launch shapes the matrices choose
   const bool bulk = sizeof(TV) == 4 && c->bulk_spmv && A.bulk32 && A.n_chunks > 0 && n == A.n_rows &&
@@ -727,6 +883,141 @@ __global__ void __launch_bounds__(256) k_gj_coop(int na, double* __restrict__ M,
   }
 }
 
+// (value, position) arg-max with the pivot rule of k_gj_pivot: the largest
+// |a|, the smallest position on ties; NaN never wins
+__device__ __forceinline__ void gj_merge(double& v, int& i, double v2, int i2) {
+  if (v2 > v || (v2 == v && i2 < i)) {
+    v = v2;
+    i = i2;
+  }
+}
+
+__device__ __forceinline__ void gj_warp_argmax(double& v, int& i) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+    gj_merge(v, i, v2, i2);
+  }
+}
+
+// Gauss-Jordan inverse with the rows resident in shared memory: block b owns
+// positions [b R, b R + R). One grid barrier per column: after step k every
+// block publishes its best pivot candidate for column k+1 (the arg-max value,
+// the position and the whole row) and the owner of position k+1 publishes that
+// row; at step k+1 every block picks the same pivot from the published
+// candidates, reads the pivot row and the old row k+1 from the published
+// copies and eliminates its own rows in shared memory. The operations per
+// entry are those of k_gj_pivot + k_gj_update, so the inverse is identical.
+__global__ void __launch_bounds__(256) k_gj_rows(int na, int R, double* __restrict__ M, int* __restrict__ perm,
+                                                 double* __restrict__ pub_rows, double* __restrict__ pub_v,
+                                                 int* __restrict__ pub_i, int* __restrict__ flag) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ double gj_smem[];
+  __shared__ double s_f[32];  // multipliers of the own rows (R <= 32)
+  __shared__ double wv[8];
+  __shared__ int wi[8];
+  __shared__ int s_p, s_src, s_cand;
+  __shared__ double s_pv;
+  const int t = threadIdx.x, nb = gridDim.x, b = blockIdx.x;
+  const int lane = t & 31, warp = t >> 5;
+  const int r0 = min(na, b * R), r1 = min(na, r0 + R), nr = r1 - r0;
+  double* own = gj_smem;                 // [R][na]
+  double* prow = own + (size_t)R * na;   // scaled pivot row of the step
+  double* orow = prow + na;              // row k before the step
+  const size_t slot = (size_t)(nb + 1) * na;
+  for (int e = t; e < nr * na; e += blockDim.x) own[e] = M[(size_t)r0 * na + e];
+  __syncthreads();
+  // candidates of column col (positions >= col) into buffer buf
+  auto publish = [&](int col, int buf) {
+    if (warp == 0) {
+      double v = -1.0;
+      int i = na;
+      if (lane < nr && r0 + lane >= col) {
+        const double a = fabs(own[(size_t)lane * na + col]);
+        if (a > v) {
+          v = a;
+          i = r0 + lane;
+        }
+      }
+      gj_warp_argmax(v, i);
+      if (lane == 0) {
+        pub_v[buf * nb + b] = v;
+        pub_i[buf * nb + b] = i;
+        s_cand = i < na ? i - r0 : -1;
+      }
+    }
+    __syncthreads();
+    double* out = pub_rows + buf * slot;
+    if (s_cand >= 0)
+      for (int j = t; j < na; j += blockDim.x) out[(size_t)b * na + j] = own[(size_t)s_cand * na + j];
+    if (col >= r0 && col < r1)
+      for (int j = t; j < na; j += blockDim.x) out[(size_t)nb * na + j] = own[(size_t)(col - r0) * na + j];
+  };
+  publish(0, 0);
+  grid.sync();
+  for (int k = 0; k < na; ++k) {
+    const int buf = k & 1;
+    const double* pub = pub_rows + buf * slot;
+    {  // the pivot: the same reduction in every block
+      double v = -1.0;
+      int i = na;
+      for (int q = t; q < nb; q += blockDim.x) gj_merge(v, i, pub_v[buf * nb + q], pub_i[buf * nb + q]);
+      gj_warp_argmax(v, i);
+      if (lane == 0) {
+        wv[warp] = v;
+        wi[warp] = i;
+      }
+      __syncthreads();
+      if (t == 0) {
+        double best = wv[0];
+        int bi = wi[0];
+        for (int w = 1; w < int(blockDim.x >> 5); ++w) gj_merge(best, bi, wv[w], wi[w]);
+        const bool singular = !(best > 0.0);
+        s_p = singular ? k : bi;
+        s_src = singular ? nb : bi / R;
+        s_pv = singular ? 1.0 : pub[(size_t)(bi / R) * na + k];
+        if (b == 0) {
+          perm[k] = s_p;
+          if (singular) *flag = 1;
+        }
+      }
+      __syncthreads();
+    }
+    const int p = s_p;
+    const double pv = s_pv;
+    const double* src = pub + (size_t)s_src * na;
+    const double* old = pub + (size_t)nb * na;
+    for (int j = t; j < na; j += blockDim.x) {
+      prow[j] = (j == k ? 1.0 : src[j]) / pv;
+      orow[j] = old[j];
+    }
+    if (t < nr) {
+      const int i = r0 + t;
+      s_f[t] = (i == p && p != k) ? old[k] : own[(size_t)t * na + k];
+    }
+    __syncthreads();
+    for (int e = t; e < nr * na; e += blockDim.x) {
+      const int ii = e / na, j = e - ii * na;
+      const int i = r0 + ii;
+      double* Mi = own + (size_t)ii * na;
+      if (i == k) {
+        Mi[j] = prow[j];
+      } else {
+        const double base = (i == p && p != k) ? orow[j] : Mi[j];
+        Mi[j] = (j == k ? 0.0 : base) - s_f[ii] * prow[j];
+      }
+    }
+    __syncthreads();
+    if (k + 1 < na) publish(k + 1, buf ^ 1);
+    grid.sync();
+  }
+  for (int e = t; e < nr * na; e += blockDim.x) M[(size_t)r0 * na + e] = own[e];
+}
+
+constexpr size_t kGjRowsSmem = 160 * 1024;  // dynamic shared memory cap of k_gj_rows
+
 void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
   n = A.n_rows;
   std::vector<int> h_act, h_pos(n, -1);
@@ -756,7 +1047,36 @@ void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
   int coop = 0, per_sm = 0;
   PM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
   PM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
-  if (coop && per_sm > 0) {
+  // row-resident variant: R rows per block (at most 32), rows and two row
+  // buffers in shared memory
+  const int R = std::max(2, (na + c->num_sms - 1) / c->num_sms);
+  const size_t rsmem = size_t(R + 2) * na * sizeof(double);
+  const int rblocks = (na + R - 1) / R;
+  int rows_per_sm = 0;
+  if (coop && R <= 32 && rsmem <= kGjRowsSmem) {
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+      attr_err = cudaFuncSetAttribute(k_gj_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGjRowsSmem));
+    });
+    PM_CUDA(attr_err);
+    PM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rows_per_sm, k_gj_rows, 256, rsmem));
+  }
+  if (rows_per_sm > 0 && rows_per_sm * c->num_sms >= rblocks) {
+    pub_rows.ensure(2 * size_t(rblocks + 1) * na);
+    pub_v.ensure(2 * size_t(rblocks));
+    pub_i.ensure(2 * size_t(rblocks));
+    double* M = inv.p;
+    int* pp = perm.p;
+    double* pr = pub_rows.p;
+    double* pv = pub_v.p;
+    int* pi = pub_i.p;
+    int* fl = flag.p;
+    int nan_ = na, R_ = R;
+    void* args[] = {&nan_, &R_, &M, &pp, &pr, &pv, &pi, &fl};
+    PM_CUDA(cudaLaunchCooperativeKernel((const void*)k_gj_rows, dim3(rblocks), dim3(256), args, rsmem, c->stream));
+    c->kernel_launches++;
+  } else if (coop && per_sm > 0) {
     // one cooperative launch; at most one block per SM and about 8 rows per block
     int nb = std::min(c->num_sms, std::max(1, (na + 7) / 8));
     rowk.ensure(na);

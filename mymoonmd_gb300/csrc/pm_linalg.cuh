@@ -26,6 +26,14 @@ struct DevCsr {
   int n_chunks = 0;
   bool bulk32 = true;
   int64_t nnz4() const { return (nnz + 3) & ~int64_t(3); }
+  // sliced-ELL copy of the FP32 values (sell_kernel): built by make_fp32 for
+  // matrices with more than 16 entries per row when the context asks for it;
+  // sell_lanes = lanes per row of the layout (0: none)
+  int sell_lanes = 0;
+  int n_slices = 0;
+  int64_t sell_entries = 0;
+  DBuf<int> sell_perm, sell_off, sell_cols, sell_src;  // sell_src: CSR entry of each slot, -1 = padding
+  DBuf<float> sell_vals;
   BlockMask mask{};
   DBuf<int> row_ptr, cols;
   DBuf<double> vals;
@@ -36,7 +44,8 @@ struct DevCsr {
   void upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int* ci, const double* v);
   void set_single_block();
   void set_blocks(int nb, const int* lengths, const int* actives);
-  void make_fp32(pm_ctx* c);
+  void make_fp32(pm_ctx* c);  // FP32 values (and the sliced copy, see sell_lanes)
+  void build_sell(pm_ctx* c, int lanes);
   void make_diag(pm_ctx* c);  // FP64 diagonal (and FP32 copy if vals32 exists)
   size_t spmv_bytes(int elem_bytes, bool read_y) const;
 };
@@ -48,6 +57,11 @@ std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int ma
 // chunks of consecutive rows whose 4-entry aligned span holds at most
 // max_entries entries; empty if one row alone does not fit
 std::vector<int> build_bulk_chunks(int n_rows, const int* rp, int max_entries);
+// sliced-ELL layout (see sell_kernel) of a host CSR structure with `lanes`
+// lanes per row and sorting windows of `window` rows; false if the padded
+// layout would exceed 2^31 - 1 entries
+bool build_sell_layout(int n_rows, const int* rp, const int* ci, int lanes, int window, std::vector<int>& perm,
+                       std::vector<int>& off, std::vector<int>& cols, std::vector<int>& src);
 // reads and clears the context's device error flag; throws PM_E_TIMEOUT if set
 void check_device_error(pm_ctx* c);
 
@@ -93,6 +107,11 @@ struct DenseInverse {
   DBuf<int> flag;    // singular pivot flag
   DBuf<double> rowk, oldk, part_v;  // cooperative elimination: pivot row, old row k, block arg-max
   DBuf<int> part_i;
+  // row-resident elimination: per step, every block's candidate pivot row and
+  // the old row k, double-buffered ([2][blocks + 1][na]), and the candidates'
+  // arg-max values and positions ([2][blocks])
+  DBuf<double> pub_rows, pub_v;
+  DBuf<int> pub_i;
   void build(pm_ctx* c, const DevCsr& A);
   // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active);
   // rhs_nonactive_zero skips the b_n correction (the multigrid coarse rhs has

@@ -160,8 +160,9 @@ void Multigrid::update(pm_ctx* c) {
       lv.R.mask = A.mask;
     }
     if (mixed) {
-      if (!A.vals32.p) A.make_fp32(c);
-      else if (lv.smoother == SM_JACOBI && !A.diag32.p) A.make_fp32(c);
+      // the FP32 copy of this update's values: the matrix may have been
+      // re-assembled (new coefficients or geometry) since the last update
+      A.make_fp32(c);
       if (l < L - 1) {
         lv.P.make_fp32(c);
         lv.R.make_fp32(c);
@@ -619,17 +620,20 @@ size_t pm_solver::layout_signature() const {
     h ^= reinterpret_cast<size_t>(p);
     h *= 1099511628211ull;
   };
+  // the sliced copies are chosen per launch by the context's kernel options
+  auto mix_csr = [&mix](const DevCsr& M) {
+    mix(M.vals.p); mix(M.vals32.p); mix(M.diag.p); mix(M.diag32.p);
+    mix(M.row_ptr.p); mix(M.cols.p); mix(M.rblock.p); mix(M.chunk_rows.p);
+    mix(M.sell_perm.p); mix(M.sell_off.p); mix(M.sell_cols.p); mix(M.sell_vals.p);
+  };
   mix(A);
-  if (A) {
-    mix(A->csr.vals.p); mix(A->csr.row_ptr.p); mix(A->csr.cols.p); mix(A->csr.rblock.p); mix(A->csr.diag.p);
-  }
+  if (A) mix_csr(A->csr);
   for (const auto& lv : mg.levels) {
     mix(lv.A);
-    if (lv.A) {
-      mix(lv.A->csr.vals.p); mix(lv.A->csr.vals32.p); mix(lv.A->csr.diag.p); mix(lv.A->csr.diag32.p);
-      mix(lv.A->csr.row_ptr.p); mix(lv.A->csr.cols.p); mix(lv.A->csr.rblock.p);
-    }
-    mix(lv.P.vals.p); mix(lv.P.vals32.p); mix(lv.R.vals.p); mix(lv.R.vals32.p);
+    if (lv.A) mix_csr(lv.A->csr);
+    if (lv.proj) mix_csr(lv.proj->csr);
+    mix_csr(lv.P);
+    mix_csr(lv.R);
     mix(lv.rhs.p); mix(lv.sol.p); mix(lv.alt.p); mix(lv.defect.p);
     mix(lv.rhs32.p); mix(lv.sol32.p); mix(lv.alt32.p); mix(lv.defect32.p);
     mix(lv.coarse.inv.p); mix(lv.coarse.act.p); mix(lv.coarse.pos.p); mix(lv.coarse.tmp.p);
@@ -638,6 +642,7 @@ size_t pm_solver::layout_signature() const {
   mix(work.p); mix(gm.p); mix(flags.p);
   mix(ctx->partials.p); mix(ctx->host_scalars);
   h ^= size_t(restart) * 31 + size_t(work_n);
+  h = h * 1099511628211ull ^ (size_t(ctx->sell_shape) * 2 + size_t(ctx->bulk_spmv));
   return h;
 }
 

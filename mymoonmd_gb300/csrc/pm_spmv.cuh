@@ -373,4 +373,111 @@ csr_bulk_kernel(int n_chunks, const int* __restrict__ chunk_rows, const int* __r
       if (((issued >> q) & 1u) && !bulk::mbar_wait(&bar[q], (phase >> q) & 1u)) atomicExch(err, 1);
 }
 
+// Sliced-ELL copy of an FP32 matrix (SELL-C-sigma, C = 32/L rows per slice).
+// Rows are sorted by length, longest first (ties in row order), inside windows
+// of kSellWindow consecutive rows; slice s holds C consecutive sorted rows,
+// padded to the slice's longest row and stored step-major: step t of the
+// slice is 32 consecutive entries at soff[s] + 32 t, lane sub*C + p holding
+// entry t*L + sub of the slice's p-th row. One warp walks one slice, so every
+// value and index load of a warp is one aligned 128-byte line, and with L = 1
+// a thread owns a whole row (no shuffles). Padding entries hold value 0 and a
+// column index of their own row. Each lane sums its entries in row order; the
+// L partial sums of a row combine in a fixed order, so results are
+// deterministic (but rounded differently from csr_kernel's row groups).
+// PIPE issues the value and index loads of the next U steps before the
+// gathers of the current ones.
+constexpr int kSellWindow = 1024;
+
+template <int L, int U, bool PIPE, int EPI>
+__global__ void __launch_bounds__(128)
+sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ soff,
+            const int* __restrict__ scols, const float* __restrict__ svals, const float* __restrict__ x,
+            float* __restrict__ y, const float* __restrict__ b, const float* __restrict__ diag, float alpha,
+            BlockMask mask) {
+  constexpr int C = 32 / L;
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= n_slices) return;  // whole warps leave: the shuffles below stay full-warp
+  const int lane = threadIdx.x & 31;
+  const int p = lane % C, sub = lane / C;
+  const int row = __ldg(perm + s * C + p);  // -1: padding row of the last window
+  if (guarded(mask.guard)) {  // uniform for the whole grid
+    if (EPI == EPI_JACOBI && row >= 0 && sub == 0) y[row] = x[row];
+    return;
+  }
+  const int beg = __ldg(soff + s);
+  const int T = (__ldg(soff + s + 1) - beg) >> 5;
+  float pre_b = 0.f, pre_d = 1.f, pre_x = 0.f, pre_y = 0.f;
+  if (row >= 0 && sub == 0) {
+    if constexpr (EPI == EPI_AXPY || EPI == EPI_PROLONG) pre_y = y[row];
+    if constexpr (EPI == EPI_DEFECT || EPI == EPI_JACOBI) pre_b = __ldg(b + row);
+    if constexpr (EPI == EPI_JACOBI) {
+      pre_d = __ldg(diag + row);
+      pre_x = __ldg(x + row);
+    }
+  }
+  const float* vp = svals + beg + lane;
+  const int* cp = scols + beg + lane;
+  float acc = 0.f;
+  if constexpr (!PIPE) {
+    for (int t0 = 0; t0 < T; t0 += U) {
+      float v[U], xv[U];
+      int c[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const bool in = t0 + u < T;
+        v[u] = in ? ld_stream(vp + (t0 + u) * 32) : 0.f;
+        c[u] = in ? ld_stream(cp + (t0 + u) * 32) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc = fmaf(v[u], xv[u], acc);
+    }
+  } else {
+    float v[U];
+    int c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool in = u < T;
+      v[u] = in ? ld_stream(vp + u * 32) : 0.f;
+      c[u] = in ? ld_stream(cp + u * 32) : 0;
+    }
+    for (int t0 = 0; t0 < T; t0 += U) {
+      float vn[U], xv[U];
+      int cn[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const bool in = t0 + U + u < T;
+        vn[u] = in ? ld_stream(vp + (t0 + U + u) * 32) : 0.f;
+        cn[u] = in ? ld_stream(cp + (t0 + U + u) * 32) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        acc = fmaf(v[u], xv[u], acc);
+        v[u] = vn[u];
+        c[u] = cn[u];
+      }
+    }
+  }
+#pragma unroll
+  for (int off = 16; off >= C; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if (row < 0 || sub != 0) return;
+  if constexpr (EPI == EPI_AXPY) {
+    y[row] = pre_y + alpha * acc;
+  } else if constexpr (EPI == EPI_SET) {
+    y[row] = acc;
+  } else if constexpr (EPI == EPI_DEFECT) {
+    y[row] = pre_b - acc;
+  } else if constexpr (EPI == EPI_JACOBI) {
+    const float d = (pre_b - acc) / pre_d;
+    y[row] = pre_x + alpha * d;
+  } else if constexpr (EPI == EPI_RESTRICT) {
+    y[row] = row_is_active(mask, row) ? acc : 0.f;
+  } else if constexpr (EPI == EPI_PROLONG) {
+    if (row_is_active(mask, row)) y[row] = pre_y + alpha * acc;
+  }
+}
+
 }  // namespace pm

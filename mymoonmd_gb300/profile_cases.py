@@ -5,6 +5,11 @@
         32^3 convection-diffusion workload (274,625 DOFs, 4 levels)
     python -m mymoonmd_gb300.profile_cases spmv
         the finest 32^3 Q2 matrix: two FP64 and two FP32 SpMV launches
+    python -m mymoonmd_gb300.profile_cases sliced
+        the request above once per FP32 SpMV kernel shape (option
+        fp32_sliced_spmv: 0 = row groups, else sliced-ELL shapes): request time,
+        iterations, and the finest-level Jacobi sweep and defect bandwidths
+        from the launch probe
     python -m mymoonmd_gb300.profile_cases assembly
         one assembly of the four 32^3 Q2 levels
     python -m mymoonmd_gb300.profile_cases stokes [--precision ...] [--smoother ...] [--coarse ...]
@@ -51,7 +56,8 @@ def problem(ctx, precision="mixed", n_levels=4):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["request", "spmv", "assembly", "stokes"])
+    ap.add_argument("case", choices=["request", "spmv", "assembly", "stokes", "sliced"])
+    ap.add_argument("--shapes", default="0,140,141,180,240,241,280,440,441,480,481,840,841,881")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
     ap.add_argument("--coarse", default="nodal_vanka_jacobi")
@@ -77,7 +83,42 @@ def main() -> None:
         ctx.close()
         return
     disc, prob = problem(ctx, args.precision)
-    if args.case == "request":
+    if args.case == "sliced":
+        import time
+        nnz = prob.matrix(-1).nnz
+        for shape in [int(v) for v in args.shapes.split(",")]:
+            ctx.set_option("fp32_sliced_spmv", shape)
+            for _ in range(2):  # lays out the sliced copies, captures the graphs
+                prob.reset_solution()
+                prob.assemble()
+                prob.solve()
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                prob.reset_solution()
+                prob.assemble()
+                prob.solve()
+            ctx.synchronize()
+            ms = (time.perf_counter() - t0) / 3 * 1e3
+            its = prob.last_info()[0]
+            bw = {}
+            for epi in (3, 2):  # Jacobi sweep, defect
+                ctx.set_option("probe_epilogue", epi)
+                ctx.set_option("probe_precision", 4)
+                ctx.probe(nnz)
+                prob.reset_solution()
+                prob.assemble()
+                prob.solve()
+                n, pms, pb = ctx.probe_result()
+                ctx.probe(0)
+                bw[epi] = (pb / pms / 1e6 if pms > 0 else 0.0, n)
+            ctx.set_option("probe_epilogue", -1)
+            ctx.set_option("probe_precision", 0)
+            print(f"shape {shape:3d}: request {ms:7.2f} ms, {its} iterations, finest Jacobi "
+                  f"{bw[3][0]:6.0f} GB/s ({bw[3][1]} launches), defect {bw[2][0]:6.0f} GB/s ({bw[2][1]})",
+                  flush=True)
+        ctx.set_option("fp32_sliced_spmv", 441)
+    elif args.case == "request":
         for _ in range(2):
             prob.reset_solution()
             prob.assemble()
@@ -98,6 +139,13 @@ def main() -> None:
         y32 = m.DeviceVector(ctx, n, np.float32)
         ms, b = A.bench_apply(x, y, 2)
         ms32, b32 = A.bench_apply(x32, y32, 2, fp32=True)
+        for shape in [int(v) for v in args.shapes.split(",")]:
+            ctx.set_option("fp32_sliced_spmv", shape)
+            A.make_fp32()  # lays out the sliced copy for the shape's lanes per row
+            A.bench_apply(x32, y32, 1, fp32=True)
+            mss, bs = A.bench_apply(x32, y32, 2, fp32=True)
+            print(f"fp32 sliced shape {shape}: {bs / mss / 1e6:.0f} GB/s")
+        ctx.set_option("fp32_sliced_spmv", 0)
         ctx.set_option("fp32_bulk_spmv", 1)
         msb, bb = A.bench_apply(x32, y32, 2, fp32=True)
         ctx.set_option("fp32_bulk_spmv", 0)

@@ -207,6 +207,32 @@ def test_mixed_precision_reaches_fp64_target(ctx):
     assert err <= 1e-7, f"mixed vs FP64 oracle relative error {err:.3e}"
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_reassembled_problem_solves_like_a_fresh_one(ctx, precision):
+    """a cached problem re-assembled with new coefficients (the request
+    executor's reuse) gives the bits of a problem created with them: every
+    matrix copy the multigrid reads (FP64, FP32, sliced) follows the new values"""
+    geo, root, nref, nlev, elem, eps, b, qn = CASES["q2_3d"]
+    disc = m.Discretization(geo, root, nref, nlev, m.KIND_CD, elem)
+    first = m.cd_coeffs(eps, b, 0.0, True)
+    second = m.cd_coeffs(2e-3, (0.2, -0.9, 0.4), 0.0, True)
+    db = mg_db(nlev, restart=30, reduction=1e-8, precision=precision)
+    n = disc.level_info(nlev - 1)["n_dofs"]
+    reused = m.ConvectionDiffusion(ctx, disc, first, db, quad_points=qn)
+    x1 = np.empty(n)
+    reused.run_host(first, None, x1)
+    x2 = np.empty(n)
+    reused.run_host(second, None, x2)
+    info_reused = reused.last_info()
+    fresh = m.ConvectionDiffusion(ctx, disc, second, db, quad_points=qn)
+    x3 = np.empty(n)
+    fresh.run_host(second, None, x3)
+    assert info_reused == fresh.last_info()
+    assert np.array_equal(x2, x3)
+    reused.close()
+    fresh.close()
+
+
 @pytest.mark.parametrize("method", ["fgmres", "cg", "bi_cgstab"])
 def test_krylov_on_reference_test_system(ctx, method):
     """the 7x7 block system of test/iterative_solver_test.c++ solved on the GPU"""
@@ -314,6 +340,7 @@ def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
     z = m.DeviceVector.from_numpy(ctx, rng.standard_normal(n))
     out = {}
     try:
+        ctx.set_option("fp32_sliced_spmv", 0)  # the row-group kernel is the comparison
         for flag in (1, 0):
             ctx.set_option("fp32_bulk_spmv", flag)
             y = m.DeviceVector(ctx, n, np.float32)
@@ -322,7 +349,8 @@ def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
             prob.solver().apply_preconditioner(z, r)
             out[flag] = (y.numpy(), r.numpy())
     finally:
-        ctx.set_option("fp32_bulk_spmv", 0)  # the library default
+        ctx.set_option("fp32_bulk_spmv", 0)  # the library defaults
+        ctx.set_option("fp32_sliced_spmv", 441)
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
 
