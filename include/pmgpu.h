@@ -71,7 +71,16 @@ int pm_version(void);
  *   "fp32_bulk_spmv" 0|1 - FP32 SpMV-family launches on full matrices by the
  *   bulk-copy kernel (row chunks streamed into shared memory with
  *   cp.async.bulk) or by the per-row-group kernel (default 0); both give the
- *   same bits. */
+ *   same bits;
+ *   "fp32_sliced_spmv" 0|100 L + 10 U + P - FP32 SpMV-family launches on
+ *   matrices with more than 16 entries per row by the sliced-ELL kernel: L
+ *   lanes per row (1, 2, 4, 8), U steps in flight (4, 8), P = 1 issues the next
+ *   steps' loads before the current gathers; accepted: 140 141 180 240 241 280
+ *   440 441 480 481 840 841 881; 0 = the row-group kernel on the CSR arrays.
+ *   Default 481. The sliced copy (rows sorted by length in windows of 1024,
+ *   slices of 32/L rows, padded to the slice's longest row) is laid out when
+ *   the FP32 values are made (pm_matrix_make_fp32, the multigrid update) for
+ *   the shape's L. Shapes with the same L give the same bits. */
 int pm_ctx_set_option(pm_ctx* ctx, const char* key, int value);
 /* Launch probe (no reference counterpart; measurement only): while enabled
  * (nnz != 0), every SpMV-family launch (apply, defect, Jacobi sweep, transfer)

@@ -114,7 +114,7 @@ struct pm_ctx {
   // FP32 SpMV by the sliced-ELL kernel: 0 = off, else 100 L + 10 U + P (L lanes
   // per row, U steps in flight, P = 1: next steps' loads issued before the
   // current gathers); the matrix copies are laid out for L in make_fp32
-  int sell_shape = 441;
+  int sell_shape = 481;
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

@@ -524,6 +524,129 @@ __global__ void __launch_bounds__(256) k_cgs_update(int n, int nk, double* __res
   }
 }
 
+// CGS2 for up to kCgsFused basis vectors in three sweeps over V: projections
+// of pass 1 (k_mdot), the pass-1 update fused with the projections of pass 2
+// (k_cgs_update_mdot: the updated r_idx meets the V values still in registers),
+// the pass-2 update fused with the partial sums of |r|^2 (k_cgs_update_norm).
+// 128 threads per block, grid kRedBlocks; partial sums per block in a fixed
+// order: each thread in index order, warps by xor shuffles, warps in order.
+constexpr int kCgsFused = 32;
+
+template <int CH>
+__device__ __forceinline__ void block_partials_multi(double (&acc)[CH], double* red, double* __restrict__ part,
+                                                     int k0, int nk) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int u = 0; u < CH; ++u) {
+    double v = acc[u];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp * CH + u] = v;
+  }
+  __syncthreads();
+  const int k = threadIdx.x;
+  if (k < CH && k0 + k < nk) {
+    double sum = 0.0;
+    for (int w = 0; w < nw; ++w) sum += red[w * CH + k];
+    part[(size_t)(k0 + k) * kRedBlocks + blockIdx.x] = sum;
+  }
+  __syncthreads();
+}
+
+// partials of <r, V_k>, k < nk, CH projections per sweep, two indices per
+// thread in flight
+template <int CH>
+__global__ void __launch_bounds__(128) k_mdot(int n, int nk, const double* __restrict__ r,
+                                              const double* __restrict__ V, size_t ld, double* __restrict__ part) {
+  __shared__ double red[4 * CH];
+  const int stride = gridDim.x * blockDim.x;
+  for (int k0 = 0; k0 < nk; k0 += CH) {
+    double acc[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) acc[u] = 0.0;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += 2 * stride) {
+      const int idx2 = idx + stride;
+      const bool two = idx2 < n;
+      const double ra = r[idx];
+      const double rb = two ? r[idx2] : 0.0;
+      double va[CH], vb[CH];
+#pragma unroll
+      for (int u = 0; u < CH; ++u) {
+        const bool in = k0 + u < nk;
+        const double* Vk = V + (size_t)(k0 + u) * ld;
+        va[u] = in ? Vk[idx] : 0.0;
+        vb[u] = (in && two) ? Vk[idx2] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < CH; ++u) {
+        acc[u] += ra * va[u];
+        acc[u] += rb * vb[u];
+      }
+    }
+    block_partials_multi<CH>(acc, red, part, k0, nk);
+  }
+}
+
+// r -= sum_k h[k] V_k (k order, the operations of k_cgs_update), then the
+// partials of <r_new, V_k>
+__global__ void __launch_bounds__(128) k_cgs_update_mdot(int n, int nk, double* __restrict__ r,
+                                                         const double* __restrict__ V, size_t ld,
+                                                         const double* __restrict__ h, double* __restrict__ part) {
+  constexpr int NK = kCgsFused;
+  __shared__ double hs[NK];
+  __shared__ double red[4 * NK];
+  if (threadIdx.x < NK) hs[threadIdx.x] = int(threadIdx.x) < nk ? h[threadIdx.x] : 0.0;
+  __syncthreads();
+  double acc[NK];
+#pragma unroll
+  for (int u = 0; u < NK; ++u) acc[u] = 0.0;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    double v[NK];
+#pragma unroll
+    for (int u = 0; u < NK; ++u) v[u] = u < nk ? V[(size_t)u * ld + idx] : 0.0;
+    double ri = r[idx];
+#pragma unroll
+    for (int u = 0; u < NK; ++u)
+      if (u < nk) ri -= hs[u] * v[u];
+    r[idx] = ri;
+#pragma unroll
+    for (int u = 0; u < NK; ++u) acc[u] += ri * v[u];
+  }
+  block_partials_multi<NK>(acc, red, part, 0, nk);
+}
+
+// r -= sum_k h[k] V_k (k order), then the block's partial sum of |r_new|^2
+__global__ void __launch_bounds__(128) k_cgs_update_norm(int n, int nk, double* __restrict__ r,
+                                                         const double* __restrict__ V, size_t ld,
+                                                         const double* __restrict__ h, double* __restrict__ part) {
+  constexpr int NK = kCgsFused;
+  __shared__ double hs[NK];
+  __shared__ double red[4];
+  if (threadIdx.x < NK) hs[threadIdx.x] = int(threadIdx.x) < nk ? h[threadIdx.x] : 0.0;
+  __syncthreads();
+  double acc = 0.0;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    double v[NK];
+#pragma unroll
+    for (int u = 0; u < NK; ++u) v[u] = u < nk ? V[(size_t)u * ld + idx] : 0.0;
+    double ri = r[idx];
+#pragma unroll
+    for (int u = 0; u < NK; ++u)
+      if (u < nk) ri -= hs[u] * v[u];
+    r[idx] = ri;
+    acc += ri * ri;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) sum += red[w];
+    part[blockIdx.x] = sum;
+  }
+}
+
 // DGKS test after the first classical Gram-Schmidt pass: the second pass is
 // needed only if |r after| < |r before| / sqrt(2); flag = 1 skips it
 __global__ void k_cgs_decide(const double* __restrict__ part_after, const double* __restrict__ rr_before,
@@ -755,7 +878,18 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
         precondition(vi, zi);
         csr_apply(c, M, EPI_SET, zi, r, nullptr, 1.0);  // r = A z_i
         double* pin = partA;
-        if (cgs2) {
+        if (cgs2 && !cgs_cond && i + 1 <= kCgsFused) {
+          // two classical Gram-Schmidt passes in three sweeps over the basis;
+          // H(:,i) = h1 + h2, |r|^2 partials into partA
+          const int nk = i + 1;
+          k_mdot<16><<<kRedBlocks, 128, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
+          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i, nullptr);
+          k_cgs_update_mdot<<<kRedBlocks, 128, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
+          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h2, h1, H, ldh, i, nullptr);
+          k_cgs_update_norm<<<kRedBlocks, 128, 0, c->stream>>>(n, nk, r, V, ld, h2, partA);
+          PM_CHECK_LAUNCH();
+          c->kernel_launches += 5;
+        } else if (cgs2) {
           // two passes of classical Gram-Schmidt; H(:,i) = h1 + h2. With the
           // conditional variant the second pass runs only when the first lost
           // more than a factor 1/sqrt(2) of the norm (decided on the device)

@@ -117,7 +117,7 @@ def main() -> None:
             print(f"shape {shape:3d}: request {ms:7.2f} ms, {its} iterations, finest Jacobi "
                   f"{bw[3][0]:6.0f} GB/s ({bw[3][1]} launches), defect {bw[2][0]:6.0f} GB/s ({bw[2][1]})",
                   flush=True)
-        ctx.set_option("fp32_sliced_spmv", 441)
+        ctx.set_option("fp32_sliced_spmv", 481)
     elif args.case == "request":
         for _ in range(2):
             prob.reset_solution()

@@ -350,7 +350,7 @@ def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
             out[flag] = (y.numpy(), r.numpy())
     finally:
         ctx.set_option("fp32_bulk_spmv", 0)  # the library defaults
-        ctx.set_option("fp32_sliced_spmv", 441)
+        ctx.set_option("fp32_sliced_spmv", 481)
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
 

@@ -16,7 +16,7 @@ from test_gpu_parity import CASES, make_pair, mg_db, rel
 pytestmark = pytest.mark.gpu
 
 SHAPES = [140, 141, 180, 240, 241, 280, 440, 441, 480, 481, 840, 841, 881]
-DEFAULT = 441
+DEFAULT = 481
 
 
 @pytest.fixture
@@ -80,7 +80,7 @@ def test_sliced_shapes_with_equal_lanes_give_equal_bits(ctx, sliced):
     assert not np.array_equal(out[140][1], out[440][1])
 
 
-@pytest.mark.parametrize("shape", [0, 180, 241, 441, 841])
+@pytest.mark.parametrize("shape", [0, 180, 241, 481, 841])
 def test_mixed_precision_with_each_fp32_kernel_reaches_fp64_target(ctx, sliced, shape):
     """the mixed form on the row-group kernel (0) and on sliced shapes: the
     1e-8 FP64 residual reduction and the FP64 oracle solution within 1e-7"""
