@@ -80,7 +80,10 @@ int pm_version(void);
  *   Default 481. The sliced copy (rows sorted by length in windows of 1024,
  *   slices of 32/L rows, padded to the slice's longest row) is laid out when
  *   the FP32 values are made (pm_matrix_make_fp32, the multigrid update) for
- *   the shape's L. Shapes with the same L give the same bits. */
+ *   the shape's L. Shapes with the same L give the same bits;
+ *   "pdl" 0|1 - sliced-ELL launches with programmatic stream serialization:
+ *   a sweep loads its slice layout and first values while the previous
+ *   kernel finishes, and waits for it before reading vectors (default 1). */
 int pm_ctx_set_option(pm_ctx* ctx, const char* key, int value);
 /* Launch probe (no reference counterpart; measurement only): while enabled
  * (nnz != 0), every SpMV-family launch (apply, defect, Jacobi sweep, transfer)

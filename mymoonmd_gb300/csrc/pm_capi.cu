@@ -85,6 +85,10 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->sell_shape = value;
     return PM_OK;
   }
+  if (std::string(key) == "pdl") {
+    c->pdl = value != 0;
+    return PM_OK;
+  }
   if (std::string(key) == "probe_epilogue") {
     c->probe_epilogue = value;
     return PM_OK;

@@ -115,6 +115,8 @@ struct pm_ctx {
   // per row, U steps in flight, P = 1: next steps' loads issued before the
   // current gathers); the matrix copies are laid out for L in make_fp32
   int sell_shape = 481;
+  // sliced-ELL launches with programmatic stream serialization (option "pdl")
+  bool pdl = true;
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

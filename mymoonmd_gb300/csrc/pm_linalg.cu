@@ -413,22 +413,34 @@ static void launch_bulk(pm_ctx* c, const DevCsr& A, const float* vals, const flo
   c->kernel_launches++;
 }
 
+template <int L, int U, bool P, int EPI>
+static void launch_sell_epi(pm_ctx* c, const DevCsr& A, const float* x, float* y, const float* b, const float* d,
+                            float alpha, const BlockMask& m) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(nblocks(A.n_slices, 4)));  // four warps (slices) per block
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = c->pdl ? 1 : 0;
+  PM_CUDA(cudaLaunchKernelEx(&cfg, sell_kernel<L, U, P, EPI>, A.n_slices, (const int*)A.sell_perm.p,
+                             (const int*)A.sell_off.p, (const int*)A.sell_cols.p, (const float*)A.sell_vals.p, x, y,
+                             b, d, alpha, m));
+}
+
 template <int L, int U, bool P>
 static void launch_sell_shape(pm_ctx* c, const DevCsr& A, int epi, const float* x, float* y, const float* b,
                               const float* d, float alpha, const BlockMask& m) {
-  const int grid = nblocks(A.n_slices, 4);  // four warps (slices) per block
-  const int* pe = A.sell_perm.p;
-  const int* so = A.sell_off.p;
-  const int* sc = A.sell_cols.p;
-  const float* sv = A.sell_vals.p;
-  const int ns = A.n_slices;
   switch (epi) {
-    case EPI_AXPY: sell_kernel<L, U, P, EPI_AXPY><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
-    case EPI_SET: sell_kernel<L, U, P, EPI_SET><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
-    case EPI_DEFECT: sell_kernel<L, U, P, EPI_DEFECT><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
-    case EPI_JACOBI: sell_kernel<L, U, P, EPI_JACOBI><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
-    case EPI_RESTRICT: sell_kernel<L, U, P, EPI_RESTRICT><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
-    case EPI_PROLONG: sell_kernel<L, U, P, EPI_PROLONG><<<grid, 128, 0, c->stream>>>(ns, pe, so, sc, sv, x, y, b, d, alpha, m); break;
+    case EPI_AXPY: launch_sell_epi<L, U, P, EPI_AXPY>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_SET: launch_sell_epi<L, U, P, EPI_SET>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_DEFECT: launch_sell_epi<L, U, P, EPI_DEFECT>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_JACOBI: launch_sell_epi<L, U, P, EPI_JACOBI>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_RESTRICT: launch_sell_epi<L, U, P, EPI_RESTRICT>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_PROLONG: launch_sell_epi<L, U, P, EPI_PROLONG>(c, A, x, y, b, d, alpha, m); break;
     default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
   }
 }

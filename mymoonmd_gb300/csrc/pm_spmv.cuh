@@ -47,6 +47,13 @@ __device__ __forceinline__ bool row_is_active(const BlockMask& m, int i) {
 template <class T>
 __device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
 
+// Programmatic dependent launch: pdl_trigger lets the next kernel on the
+// stream (if launched with programmatic stream serialization) start once all
+// blocks of this one have started; pdl_wait blocks until the previous kernel
+// has completed and its writes are visible (a no-op without the attribute).
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // G lanes per row, U entries per lane per chunk: a lane first issues its U
 // value and U column loads, then its U gathers of x, then the U products, so
 // that every lane keeps U independent DRAM requests in flight.
@@ -56,6 +63,7 @@ csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ 
            const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
            const TX* __restrict__ b, const TX* __restrict__ diag, const TX* __restrict__ xold,
            TA alpha, BlockMask mask) {
+  pdl_trigger();
   if (guarded(mask.guard)) {  // uniform for the whole grid
     // a skipped Jacobi sweep leaves the iterate as it is (the caller swaps
     // the two iterate buffers after every sweep)
@@ -385,7 +393,9 @@ csr_bulk_kernel(int n_chunks, const int* __restrict__ chunk_rows, const int* __r
 // L partial sums of a row combine in a fixed order, so results are
 // deterministic (but rounded differently from csr_kernel's row groups).
 // PIPE issues the value and index loads of the next U steps before the
-// gathers of the current ones.
+// gathers of the current ones. Launched with programmatic stream
+// serialization, a sweep loads its permutation, slice offsets and (PIPE) first
+// U steps while the previous kernel finishes.
 constexpr int kSellWindow = 1024;
 
 template <int L, int U, bool PIPE, int EPI>
@@ -395,17 +405,33 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
             float* __restrict__ y, const float* __restrict__ b, const float* __restrict__ diag, float alpha,
             BlockMask mask) {
   constexpr int C = 32 / L;
+  pdl_trigger();
   const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (s >= n_slices) return;  // whole warps leave: the shuffles below stay full-warp
   const int lane = threadIdx.x & 31;
   const int p = lane % C, sub = lane / C;
+  // the matrix arrays are not written by the kernels that precede a sweep:
+  // their loads start before the wait for the previous kernel
   const int row = __ldg(perm + s * C + p);  // -1: padding row of the last window
+  const int beg = __ldg(soff + s);
+  const int T = (__ldg(soff + s + 1) - beg) >> 5;
+  const float* vp = svals + beg + lane;
+  const int* cp = scols + beg + lane;
+  float v[U];
+  int c[U];
+  if constexpr (PIPE) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool in = u < T;
+      v[u] = in ? ld_stream(vp + u * 32) : 0.f;
+      c[u] = in ? ld_stream(cp + u * 32) : 0;
+    }
+  }
+  pdl_wait();  // x, b, y and the guard flag come from earlier kernels
   if (guarded(mask.guard)) {  // uniform for the whole grid
     if (EPI == EPI_JACOBI && row >= 0 && sub == 0) y[row] = x[row];
     return;
   }
-  const int beg = __ldg(soff + s);
-  const int T = (__ldg(soff + s + 1) - beg) >> 5;
   float pre_b = 0.f, pre_d = 1.f, pre_x = 0.f, pre_y = 0.f;
   if (row >= 0 && sub == 0) {
     if constexpr (EPI == EPI_AXPY || EPI == EPI_PROLONG) pre_y = y[row];
@@ -415,13 +441,10 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
       pre_x = __ldg(x + row);
     }
   }
-  const float* vp = svals + beg + lane;
-  const int* cp = scols + beg + lane;
   float acc = 0.f;
   if constexpr (!PIPE) {
     for (int t0 = 0; t0 < T; t0 += U) {
-      float v[U], xv[U];
-      int c[U];
+      float xv[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const bool in = t0 + u < T;
@@ -434,14 +457,6 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
       for (int u = 0; u < U; ++u) acc = fmaf(v[u], xv[u], acc);
     }
   } else {
-    float v[U];
-    int c[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const bool in = u < T;
-      v[u] = in ? ld_stream(vp + u * 32) : 0.f;
-      c[u] = in ? ld_stream(cp + u * 32) : 0;
-    }
     for (int t0 = 0; t0 < T; t0 += U) {
       float vn[U], xv[U];
       int cn[U];

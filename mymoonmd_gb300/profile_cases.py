@@ -58,12 +58,14 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["request", "spmv", "assembly", "stokes", "sliced"])
     ap.add_argument("--shapes", default="0,140,141,180,240,241,280,440,441,480,481,840,841,881")
+    ap.add_argument("--pdl", type=int, default=1, choices=[0, 1])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
     ap.add_argument("--coarse", default="nodal_vanka_jacobi")
     ap.add_argument("--cubes", type=int, default=24, choices=[12, 24])
     args = ap.parse_args()
     ctx = m.Context(0)
+    ctx.set_option("pdl", args.pdl)
     if args.case == "stokes":
         db = _db(args.precision)
         db["multigrid_n_levels"] = 3
