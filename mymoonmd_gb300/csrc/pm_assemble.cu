@@ -500,6 +500,7 @@ void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, 
       n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
   PM_CHECK_LAUNCH();
   c->kernel_launches += nd ? 3 : 2;
+  A.values_changed(c);
 }
 
 void DevRefTables::upload(pm_ctx* c, const RefTables& t) {

@@ -85,6 +85,12 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->sell_shape = value;
     return PM_OK;
   }
+  if (std::string(key) == "fp64_sliced_spmv") {
+    if (value != 0 && value != 441 && value != 481 && value != 841)
+      return fail(c, PM_E_INVALID, "fp64_sliced_spmv is 0, 441, 481 or 841");
+    c->sell_shape64 = value;
+    return PM_OK;
+  }
   if (std::string(key) == "pdl") {
     c->pdl = value != 0;
     return PM_OK;
@@ -254,6 +260,7 @@ int pm_matrix_set_values(pm_matrix* A, const double* vals) {
   if (!A || !vals) return PM_E_INVALID;
   PM_TRY
   A->csr.vals.upload(vals, size_t(A->csr.nnz), A->ctx->stream);
+  A->csr.values_changed(A->ctx);
   if (A->csr.vals32.p) A->csr.make_fp32(A->ctx);
   if (A->csr.diag.p) A->csr.make_diag(A->ctx);
   PM_CUDA(cudaStreamSynchronize(A->ctx->stream));
@@ -500,7 +507,10 @@ int pm_solver_update_matrix(pm_solver* s, pm_matrix* A) {
     if (top.A && top.A != A) throw Error(PM_E_INVALID, "finest multigrid level must be the solver's matrix");
     top.A = A;
     s->mg.update(s->ctx);
-  } else if (s->prec == "jacobi" || s->method == "jacobi") {
+  } else {
+    A->csr.make_sliced64(s->ctx);
+  }
+  if (!s->use_mg && (s->prec == "jacobi" || s->method == "jacobi")) {
     A->csr.make_diag(s->ctx);
   }
   PM_CUDA(cudaStreamSynchronize(s->ctx->stream));

@@ -115,6 +115,9 @@ struct pm_ctx {
   // per row, U steps in flight, P = 1: next steps' loads issued before the
   // current gathers); the matrix copies are laid out for L in make_fp32
   int sell_shape = 481;
+  // FP64 SpMV-family launches by the sliced-ELL kernel (same encoding; the
+  // layout's lanes must equal those of the FP32 shape when both are used)
+  int sell_shape64 = 441;
   // sliced-ELL launches with programmatic stream serialization (option "pdl")
   bool pdl = true;
   int64_t probe_nnz = 0;

@@ -73,6 +73,7 @@ void DevCsr::upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int*
     vals.alloc(size_t(nnz));
     if (nnz) PM_CUDA(cudaMemsetAsync(vals.p, 0, vals.bytes(), c->stream));
   }
+  drop_sell();  // a new structure: no sliced layout yet
   // measured on GB300 (3D Q2, 15.8 M and 54.5 M nonzeros): four lanes per row
   // with eight loads in flight per lane is the fastest launch shape for both
   // FP64 and FP32 values; short rows take four loads per lane
@@ -181,21 +182,32 @@ bool build_sell_layout(int n_rows, const int* rp, const int* ci, int L, int wind
   return true;
 }
 
-void DevCsr::build_sell(pm_ctx* c, int L) {
+void DevCsr::drop_sell() {
   sell_lanes = 0;
   n_slices = 0;
   sell_entries = 0;
+  sell64_ok = false;
+  sell_perm.release();
+  sell_off.release();
+  sell_cols.release();
+  sell_src.release();
+  sell_vals.release();
+  sell_vals64.release();
+}
+
+void DevCsr::build_sell(pm_ctx* c, int L) {
+  const bool had64 = sell_vals64.p != nullptr;
+  sell_lanes = 0;
+  n_slices = 0;
+  sell_entries = 0;
+  sell64_ok = false;
   std::vector<int> rp(static_cast<size_t>(n_rows) + 1), ci(static_cast<size_t>(nnz));
   PM_CUDA(cudaMemcpyAsync(rp.data(), row_ptr.p, rp.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   if (nnz) PM_CUDA(cudaMemcpyAsync(ci.data(), cols.p, ci.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   PM_CUDA(cudaStreamSynchronize(c->stream));
   std::vector<int> perm, off, sc, src;
   if (!build_sell_layout(n_rows, rp.data(), ci.data(), L, kSellWindow, perm, off, sc, src)) {
-    sell_perm.release();
-    sell_off.release();
-    sell_cols.release();
-    sell_src.release();
-    sell_vals.release();
+    drop_sell();
     return;
   }
   sell_perm.upload(perm, c->stream);
@@ -207,6 +219,10 @@ void DevCsr::build_sell(pm_ctx* c, int L) {
   sell_lanes = L;
   n_slices = int(off.size()) - 1;
   sell_entries = int64_t(sc.size());
+  if (had64) {  // the FP64 copy follows the new layout
+    sell_vals64.ensure(sc.size());
+    values_changed(c);
+  }
 }
 
 void DevCsr::set_single_block() {
@@ -250,13 +266,34 @@ static int grid_for(pm_ctx* c, long long n) {
   return int(std::max<long long>(1, std::min(b, cap)));
 }
 
+template <class TO>
 __global__ void k_sell_fill(long long n, const int* __restrict__ src, const double* __restrict__ v,
-                            float* __restrict__ out) {
+                            TO* __restrict__ out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const int k = src[i];
-    out[i] = k >= 0 ? float(v[k]) : 0.0f;
+    out[i] = k >= 0 ? TO(v[k]) : TO(0);
   }
+}
+
+void DevCsr::values_changed(pm_ctx* c) {
+  sell64_ok = false;
+  if (sell_lanes && sell_entries && sell_vals64.p) {
+    k_sell_fill<double><<<grid_for(c, sell_entries), 256, 0, c->stream>>>(sell_entries, sell_src.p, vals.p,
+                                                                         sell_vals64.p);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+    sell64_ok = true;
+  }
+}
+
+void DevCsr::make_sliced64(pm_ctx* c) {
+  const int want = c->sell_shape64 / 100;
+  if (want <= 0 || nnz <= 16 * int64_t(n_rows)) return;
+  if (sell_lanes == 0) build_sell(c, want);
+  if (sell_lanes != want || !sell_entries) return;
+  if (!sell_vals64.p) sell_vals64.ensure(size_t(sell_entries));
+  if (!sell64_ok) values_changed(c);
 }
 
 void DevCsr::make_fp32(pm_ctx* c) {
@@ -265,7 +302,8 @@ void DevCsr::make_fp32(pm_ctx* c) {
   const int want = c->sell_shape / 100;
   if (want > 0 && want != sell_lanes && nnz > 16 * int64_t(n_rows)) build_sell(c, want);
   if (sell_lanes && sell_entries) {
-    k_sell_fill<<<grid_for(c, sell_entries), 256, 0, c->stream>>>(sell_entries, sell_src.p, vals.p, sell_vals.p);
+    k_sell_fill<float><<<grid_for(c, sell_entries), 256, 0, c->stream>>>(sell_entries, sell_src.p, vals.p,
+                                                                       sell_vals.p);
     PM_CHECK_LAUNCH();
     c->kernel_launches++;
   }
@@ -413,9 +451,16 @@ static void launch_bulk(pm_ctx* c, const DevCsr& A, const float* vals, const flo
   c->kernel_launches++;
 }
 
-template <int L, int U, bool P, int EPI>
-static void launch_sell_epi(pm_ctx* c, const DevCsr& A, const float* x, float* y, const float* b, const float* d,
-                            float alpha, const BlockMask& m) {
+template <class T>
+static const T* sell_values(const DevCsr& A);
+template <>
+const float* sell_values<float>(const DevCsr& A) { return A.sell_vals.p; }
+template <>
+const double* sell_values<double>(const DevCsr& A) { return A.sell_vals64.p; }
+
+template <class T, int L, int U, bool P, int EPI>
+static void launch_sell_epi(pm_ctx* c, const DevCsr& A, const T* x, T* y, const T* b, const T* d, T alpha,
+                            const BlockMask& m) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(unsigned(nblocks(A.n_slices, 4)));  // four warps (slices) per block
   cfg.blockDim = dim3(128);
@@ -426,21 +471,21 @@ static void launch_sell_epi(pm_ctx* c, const DevCsr& A, const float* x, float* y
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = c->pdl ? 1 : 0;
-  PM_CUDA(cudaLaunchKernelEx(&cfg, sell_kernel<L, U, P, EPI>, A.n_slices, (const int*)A.sell_perm.p,
-                             (const int*)A.sell_off.p, (const int*)A.sell_cols.p, (const float*)A.sell_vals.p, x, y,
-                             b, d, alpha, m));
+  PM_CUDA(cudaLaunchKernelEx(&cfg, sell_kernel<T, L, U, P, EPI>, A.n_slices, (const int*)A.sell_perm.p,
+                             (const int*)A.sell_off.p, (const int*)A.sell_cols.p, sell_values<T>(A), x, y, b, d,
+                             alpha, m));
 }
 
-template <int L, int U, bool P>
-static void launch_sell_shape(pm_ctx* c, const DevCsr& A, int epi, const float* x, float* y, const float* b,
-                              const float* d, float alpha, const BlockMask& m) {
+template <class T, int L, int U, bool P>
+static void launch_sell_shape(pm_ctx* c, const DevCsr& A, int epi, const T* x, T* y, const T* b, const T* d,
+                              T alpha, const BlockMask& m) {
   switch (epi) {
-    case EPI_AXPY: launch_sell_epi<L, U, P, EPI_AXPY>(c, A, x, y, b, d, alpha, m); break;
-    case EPI_SET: launch_sell_epi<L, U, P, EPI_SET>(c, A, x, y, b, d, alpha, m); break;
-    case EPI_DEFECT: launch_sell_epi<L, U, P, EPI_DEFECT>(c, A, x, y, b, d, alpha, m); break;
-    case EPI_JACOBI: launch_sell_epi<L, U, P, EPI_JACOBI>(c, A, x, y, b, d, alpha, m); break;
-    case EPI_RESTRICT: launch_sell_epi<L, U, P, EPI_RESTRICT>(c, A, x, y, b, d, alpha, m); break;
-    case EPI_PROLONG: launch_sell_epi<L, U, P, EPI_PROLONG>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_AXPY: launch_sell_epi<T, L, U, P, EPI_AXPY>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_SET: launch_sell_epi<T, L, U, P, EPI_SET>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_DEFECT: launch_sell_epi<T, L, U, P, EPI_DEFECT>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_JACOBI: launch_sell_epi<T, L, U, P, EPI_JACOBI>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_RESTRICT: launch_sell_epi<T, L, U, P, EPI_RESTRICT>(c, A, x, y, b, d, alpha, m); break;
+    case EPI_PROLONG: launch_sell_epi<T, L, U, P, EPI_PROLONG>(c, A, x, y, b, d, alpha, m); break;
     default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
   }
 }
@@ -450,20 +495,34 @@ static void launch_sell(pm_ctx* c, const DevCsr& A, int epi, const float* x, flo
   BlockMask mg = A.mask;
   mg.guard = c->guard;
   switch (c->sell_shape) {
-    case 140: launch_sell_shape<1, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 141: launch_sell_shape<1, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 180: launch_sell_shape<1, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 240: launch_sell_shape<2, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 241: launch_sell_shape<2, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 280: launch_sell_shape<2, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 440: launch_sell_shape<4, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 441: launch_sell_shape<4, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 480: launch_sell_shape<4, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 481: launch_sell_shape<4, 8, true>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 840: launch_sell_shape<8, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 841: launch_sell_shape<8, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
-    case 881: launch_sell_shape<8, 8, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 140: launch_sell_shape<float, 1, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 141: launch_sell_shape<float, 1, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 180: launch_sell_shape<float, 1, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 240: launch_sell_shape<float, 2, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 241: launch_sell_shape<float, 2, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 280: launch_sell_shape<float, 2, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 440: launch_sell_shape<float, 4, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 441: launch_sell_shape<float, 4, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 480: launch_sell_shape<float, 4, 8, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 481: launch_sell_shape<float, 4, 8, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 840: launch_sell_shape<float, 8, 4, false>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 841: launch_sell_shape<float, 8, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 881: launch_sell_shape<float, 8, 8, true>(c, A, epi, x, y, b, d, alpha, mg); break;
     default: throw Error(PM_E_INVALID, "unknown sliced SpMV shape " + std::to_string(c->sell_shape));
+  }
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+static void launch_sell64(pm_ctx* c, const DevCsr& A, int epi, const double* x, double* y, const double* b,
+                          const double* d, double alpha) {
+  BlockMask mg = A.mask;
+  mg.guard = c->guard;
+  switch (c->sell_shape64) {
+    case 441: launch_sell_shape<double, 4, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 481: launch_sell_shape<double, 4, 8, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    case 841: launch_sell_shape<double, 8, 4, true>(c, A, epi, x, y, b, d, alpha, mg); break;
+    default: throw Error(PM_E_INVALID, "unknown FP64 sliced SpMV shape " + std::to_string(c->sell_shape64));
   }
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
@@ -488,6 +547,19 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
     PM_CUDA(cudaEventRecord(e0, c->stream));
     c->probe_events.push_back(e0);
     c->probe_bytes.push_back(epi_bytes(A, epi, int(sizeof(TV)), n));
+  }
+  if constexpr (sizeof(TV) == 8) {
+    if (c->sell_shape64 > 0 && A.sell64_ok && A.sell_lanes == c->sell_shape64 / 100 && A.n_slices > 0 &&
+        n == A.n_rows) {
+      launch_sell64(c, A, epi, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y),
+                    reinterpret_cast<const double*>(b), reinterpret_cast<const double*>(diag), double(alpha));
+      if (probe) {
+        cudaEvent_t e1 = probe_event(c);
+        PM_CUDA(cudaEventRecord(e1, c->stream));
+        c->probe_events.push_back(e1);
+      }
+      return;
+    }
   }
   if constexpr (sizeof(TV) == 4) {
     if (!(c->bulk_spmv && A.bulk32 && A.n_chunks > 0) && c->sell_shape > 0 && A.sell_lanes == c->sell_shape / 100 &&

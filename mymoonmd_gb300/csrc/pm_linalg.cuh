@@ -34,6 +34,10 @@ struct DevCsr {
   int64_t sell_entries = 0;
   DBuf<int> sell_perm, sell_off, sell_cols, sell_src;  // sell_src: CSR entry of each slot, -1 = padding
   DBuf<float> sell_vals;
+  // FP64 values in the sliced layout (make_sliced64); sell64_ok: they are the
+  // current values (every writer of vals calls values_changed)
+  DBuf<double> sell_vals64;
+  bool sell64_ok = false;
   BlockMask mask{};
   DBuf<int> row_ptr, cols;
   DBuf<double> vals;
@@ -46,6 +50,12 @@ struct DevCsr {
   void set_blocks(int nb, const int* lengths, const int* actives);
   void make_fp32(pm_ctx* c);  // FP32 values (and the sliced copy, see sell_lanes)
   void build_sell(pm_ctx* c, int lanes);
+  void drop_sell();
+  // FP64 sliced copy for the context's fp64 shape (lays out the slices if the
+  // matrix has none yet)
+  void make_sliced64(pm_ctx* c);
+  // to be called after every write of vals: refreshes the FP64 sliced copy
+  void values_changed(pm_ctx* c);
   void make_diag(pm_ctx* c);  // FP64 diagonal (and FP32 copy if vals32 exists)
   size_t spmv_bytes(int elem_bytes, bool read_y) const;
 };

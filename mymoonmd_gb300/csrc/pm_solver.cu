@@ -153,11 +153,13 @@ void Multigrid::update(pm_ctx* c) {
     if (vanka) lv.vanka->factor(c, lv.proj->csr, mixed);
     if (nodal) lv.nodal->factor(c, lv.proj->csr, mixed);
     if (lv.smoother == SM_JACOBI) A.make_diag(c);
+    A.make_sliced64(c);  // FP64 sweeps, defects and the Krylov SpMV on the sliced copy
     const int n = A.n_rows;
     if (l < L - 1) {
       if (!lv.P.row_ptr.p) throw Error(PM_E_INVALID, "missing prolongation of level " + std::to_string(l));
       lv.P.mask = levels[l + 1].A->csr.mask;
       lv.R.mask = A.mask;
+      lv.R.make_sliced64(c);
     }
     if (mixed) {
       // the FP32 copy of this update's values: the matrix may have been
@@ -526,11 +528,15 @@ __global__ void __launch_bounds__(256) k_cgs_update(int n, int nk, double* __res
 
 // CGS2 for up to kCgsFused basis vectors in three sweeps over V: projections
 // of pass 1 (k_mdot), the pass-1 update fused with the projections of pass 2
-// (k_cgs_update_mdot: the updated r_idx meets the V values still in registers),
-// the pass-2 update fused with the partial sums of |r|^2 (k_cgs_update_norm).
-// 128 threads per block, grid kRedBlocks; partial sums per block in a fixed
-// order: each thread in index order, warps by xor shuffles, warps in order.
+// (k_cgs_update_mdot), the pass-2 update fused with the partial sums of |r|^2
+// (k_cgs_update_norm). The FP64 pipe bounds these sweeps on GB300 (about one
+// FP64 FMA per clock per SM), so they run 16 warps per SM and keep the update
+// chains short: V is read in chunks of 8 vectors, the pass-2 projections read
+// the chunk again (from L1/L2) after the update. 256 threads per block, grid
+// kRedBlocks; partial sums per block in a fixed order: each thread in index
+// order, warps by xor shuffles, warps in order.
 constexpr int kCgsFused = 32;
+constexpr int kCgsChunk = 8;
 
 template <int CH>
 __device__ __forceinline__ void block_partials_multi(double (&acc)[CH], double* red, double* __restrict__ part,
@@ -553,86 +559,92 @@ __device__ __forceinline__ void block_partials_multi(double (&acc)[CH], double* 
   __syncthreads();
 }
 
-// partials of <r, V_k>, k < nk, CH projections per sweep, two indices per
-// thread in flight
+// partials of <r, V_k>, k < nk, CH projections per sweep
 template <int CH>
-__global__ void __launch_bounds__(128) k_mdot(int n, int nk, const double* __restrict__ r,
+__global__ void __launch_bounds__(256, 2) k_mdot(int n, int nk, const double* __restrict__ r,
                                               const double* __restrict__ V, size_t ld, double* __restrict__ part) {
-  __shared__ double red[4 * CH];
-  const int stride = gridDim.x * blockDim.x;
+  __shared__ double red[8 * CH];
   for (int k0 = 0; k0 < nk; k0 += CH) {
     double acc[CH];
 #pragma unroll
     for (int u = 0; u < CH; ++u) acc[u] = 0.0;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += 2 * stride) {
-      const int idx2 = idx + stride;
-      const bool two = idx2 < n;
-      const double ra = r[idx];
-      const double rb = two ? r[idx2] : 0.0;
-      double va[CH], vb[CH];
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+      const double ri = r[idx];
+      double v[CH];
 #pragma unroll
-      for (int u = 0; u < CH; ++u) {
-        const bool in = k0 + u < nk;
-        const double* Vk = V + (size_t)(k0 + u) * ld;
-        va[u] = in ? Vk[idx] : 0.0;
-        vb[u] = (in && two) ? Vk[idx2] : 0.0;
-      }
+      for (int u = 0; u < CH; ++u) v[u] = k0 + u < nk ? V[(size_t)(k0 + u) * ld + idx] : 0.0;
 #pragma unroll
-      for (int u = 0; u < CH; ++u) {
-        acc[u] += ra * va[u];
-        acc[u] += rb * vb[u];
-      }
+      for (int u = 0; u < CH; ++u) acc[u] += ri * v[u];
     }
     block_partials_multi<CH>(acc, red, part, k0, nk);
   }
 }
 
-// r -= sum_k h[k] V_k (k order, the operations of k_cgs_update), then the
-// partials of <r_new, V_k>
-__global__ void __launch_bounds__(128) k_cgs_update_mdot(int n, int nk, double* __restrict__ r,
-                                                         const double* __restrict__ V, size_t ld,
-                                                         const double* __restrict__ h, double* __restrict__ part) {
-  constexpr int NK = kCgsFused;
+// ri -= sum_k h[k] V_k(idx) in k order (the operations of k_cgs_update)
+template <int NK>
+__device__ __forceinline__ double cgs_update_entry(double ri, int idx, int nk, const double* __restrict__ V,
+                                                   size_t ld, const double* hs) {
+#pragma unroll
+  for (int c = 0; c < NK / kCgsChunk; ++c) {
+    if (c * kCgsChunk < nk) {
+      double v[kCgsChunk];
+#pragma unroll
+      for (int u = 0; u < kCgsChunk; ++u) {
+        const int k = c * kCgsChunk + u;
+        v[u] = k < nk ? V[(size_t)k * ld + idx] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kCgsChunk; ++u)
+        if (c * kCgsChunk + u < nk) ri -= hs[c * kCgsChunk + u] * v[u];
+    }
+  }
+  return ri;
+}
+
+// r -= sum_k h[k] V_k, then the partials of <r_new, V_k> (nk <= NK)
+template <int NK>
+__global__ void __launch_bounds__(256, 2) k_cgs_update_mdot(int n, int nk, double* __restrict__ r,
+                                                            const double* __restrict__ V, size_t ld,
+                                                            const double* __restrict__ h, double* __restrict__ part) {
   __shared__ double hs[NK];
-  __shared__ double red[4 * NK];
+  __shared__ double red[8 * NK];
   if (threadIdx.x < NK) hs[threadIdx.x] = int(threadIdx.x) < nk ? h[threadIdx.x] : 0.0;
   __syncthreads();
   double acc[NK];
 #pragma unroll
   for (int u = 0; u < NK; ++u) acc[u] = 0.0;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
-    double v[NK];
-#pragma unroll
-    for (int u = 0; u < NK; ++u) v[u] = u < nk ? V[(size_t)u * ld + idx] : 0.0;
-    double ri = r[idx];
-#pragma unroll
-    for (int u = 0; u < NK; ++u)
-      if (u < nk) ri -= hs[u] * v[u];
+    const double ri = cgs_update_entry<NK>(r[idx], idx, nk, V, ld, hs);
     r[idx] = ri;
 #pragma unroll
-    for (int u = 0; u < NK; ++u) acc[u] += ri * v[u];
+    for (int c = 0; c < NK / kCgsChunk; ++c) {
+      if (c * kCgsChunk < nk) {
+        double v[kCgsChunk];
+#pragma unroll
+        for (int u = 0; u < kCgsChunk; ++u) {
+          const int k = c * kCgsChunk + u;
+          v[u] = k < nk ? V[(size_t)k * ld + idx] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kCgsChunk; ++u) acc[c * kCgsChunk + u] += ri * v[u];
+      }
+    }
   }
   block_partials_multi<NK>(acc, red, part, 0, nk);
 }
 
-// r -= sum_k h[k] V_k (k order), then the block's partial sum of |r_new|^2
-__global__ void __launch_bounds__(128) k_cgs_update_norm(int n, int nk, double* __restrict__ r,
+// r -= sum_k h[k] V_k, then the block's partial sum of |r_new|^2
+__global__ void __launch_bounds__(256, 2) k_cgs_update_norm(int n, int nk, double* __restrict__ r,
                                                          const double* __restrict__ V, size_t ld,
                                                          const double* __restrict__ h, double* __restrict__ part) {
   constexpr int NK = kCgsFused;
   __shared__ double hs[NK];
-  __shared__ double red[4];
+  __shared__ double red[8];
   if (threadIdx.x < NK) hs[threadIdx.x] = int(threadIdx.x) < nk ? h[threadIdx.x] : 0.0;
   __syncthreads();
   double acc = 0.0;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
-    double v[NK];
-#pragma unroll
-    for (int u = 0; u < NK; ++u) v[u] = u < nk ? V[(size_t)u * ld + idx] : 0.0;
-    double ri = r[idx];
-#pragma unroll
-    for (int u = 0; u < NK; ++u)
-      if (u < nk) ri -= hs[u] * v[u];
+    const double ri = cgs_update_entry<NK>(r[idx], idx, nk, V, ld, hs);
     r[idx] = ri;
     acc += ri * ri;
   }
@@ -747,7 +759,7 @@ size_t pm_solver::layout_signature() const {
   auto mix_csr = [&mix](const DevCsr& M) {
     mix(M.vals.p); mix(M.vals32.p); mix(M.diag.p); mix(M.diag32.p);
     mix(M.row_ptr.p); mix(M.cols.p); mix(M.rblock.p); mix(M.chunk_rows.p);
-    mix(M.sell_perm.p); mix(M.sell_off.p); mix(M.sell_cols.p); mix(M.sell_vals.p);
+    mix(M.sell_perm.p); mix(M.sell_off.p); mix(M.sell_cols.p); mix(M.sell_vals.p); mix(M.sell_vals64.p);
   };
   mix(A);
   if (A) mix_csr(A->csr);
@@ -766,6 +778,7 @@ size_t pm_solver::layout_signature() const {
   mix(ctx->partials.p); mix(ctx->host_scalars);
   h ^= size_t(restart) * 31 + size_t(work_n);
   h = h * 1099511628211ull ^ (size_t(ctx->sell_shape) * 2 + size_t(ctx->bulk_spmv));
+  h = h * 1099511628211ull ^ (size_t(ctx->sell_shape64) * 2 + size_t(ctx->pdl));
   return h;
 }
 
@@ -882,11 +895,12 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
           // two classical Gram-Schmidt passes in three sweeps over the basis;
           // H(:,i) = h1 + h2, |r|^2 partials into partA
           const int nk = i + 1;
-          k_mdot<16><<<kRedBlocks, 128, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
+          k_mdot<16><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
           k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i, nullptr);
-          k_cgs_update_mdot<<<kRedBlocks, 128, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
+          if (nk <= 16) k_cgs_update_mdot<16><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
+          else k_cgs_update_mdot<kCgsFused><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
           k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h2, h1, H, ldh, i, nullptr);
-          k_cgs_update_norm<<<kRedBlocks, 128, 0, c->stream>>>(n, nk, r, V, ld, h2, partA);
+          k_cgs_update_norm<<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h2, partA);
           PM_CHECK_LAUNCH();
           c->kernel_launches += 5;
         } else if (cgs2) {

@@ -398,11 +398,18 @@ csr_bulk_kernel(int n_chunks, const int* __restrict__ chunk_rows, const int* __r
 // U steps while the previous kernel finishes.
 constexpr int kSellWindow = 1024;
 
-template <int L, int U, bool PIPE, int EPI>
+template <class T>
+__device__ __forceinline__ T fmadd(T a, T b, T c);
+template <>
+__device__ __forceinline__ float fmadd<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <>
+__device__ __forceinline__ double fmadd<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <class T, int L, int U, bool PIPE, int EPI>
 __global__ void __launch_bounds__(128)
 sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ soff,
-            const int* __restrict__ scols, const float* __restrict__ svals, const float* __restrict__ x,
-            float* __restrict__ y, const float* __restrict__ b, const float* __restrict__ diag, float alpha,
+            const int* __restrict__ scols, const T* __restrict__ svals, const T* __restrict__ x,
+            T* __restrict__ y, const T* __restrict__ b, const T* __restrict__ diag, T alpha,
             BlockMask mask) {
   constexpr int C = 32 / L;
   pdl_trigger();
@@ -414,16 +421,16 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
   // their loads start before the wait for the previous kernel
   const int row = __ldg(perm + s * C + p);  // -1: padding row of the last window
   const int beg = __ldg(soff + s);
-  const int T = (__ldg(soff + s + 1) - beg) >> 5;
-  const float* vp = svals + beg + lane;
+  const int NT = (__ldg(soff + s + 1) - beg) >> 5;
+  const T* vp = svals + beg + lane;
   const int* cp = scols + beg + lane;
-  float v[U];
+  T v[U];
   int c[U];
   if constexpr (PIPE) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const bool in = u < T;
-      v[u] = in ? ld_stream(vp + u * 32) : 0.f;
+      const bool in = u < NT;
+      v[u] = in ? ld_stream(vp + u * 32) : T(0);
       c[u] = in ? ld_stream(cp + u * 32) : 0;
     }
   }
@@ -432,7 +439,7 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
     if (EPI == EPI_JACOBI && row >= 0 && sub == 0) y[row] = x[row];
     return;
   }
-  float pre_b = 0.f, pre_d = 1.f, pre_x = 0.f, pre_y = 0.f;
+  T pre_b = T(0), pre_d = T(1), pre_x = T(0), pre_y = T(0);
   if (row >= 0 && sub == 0) {
     if constexpr (EPI == EPI_AXPY || EPI == EPI_PROLONG) pre_y = y[row];
     if constexpr (EPI == EPI_DEFECT || EPI == EPI_JACOBI) pre_b = __ldg(b + row);
@@ -441,36 +448,36 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
       pre_x = __ldg(x + row);
     }
   }
-  float acc = 0.f;
+  T acc = T(0);
   if constexpr (!PIPE) {
-    for (int t0 = 0; t0 < T; t0 += U) {
-      float xv[U];
+    for (int t0 = 0; t0 < NT; t0 += U) {
+      T xv[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const bool in = t0 + u < T;
-        v[u] = in ? ld_stream(vp + (t0 + u) * 32) : 0.f;
+        const bool in = t0 + u < NT;
+        v[u] = in ? ld_stream(vp + (t0 + u) * 32) : T(0);
         c[u] = in ? ld_stream(cp + (t0 + u) * 32) : 0;
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) xv[u] = __ldg(x + c[u]);
 #pragma unroll
-      for (int u = 0; u < U; ++u) acc = fmaf(v[u], xv[u], acc);
+      for (int u = 0; u < U; ++u) acc = fmadd(v[u], xv[u], acc);
     }
   } else {
-    for (int t0 = 0; t0 < T; t0 += U) {
-      float vn[U], xv[U];
+    for (int t0 = 0; t0 < NT; t0 += U) {
+      T vn[U], xv[U];
       int cn[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const bool in = t0 + U + u < T;
-        vn[u] = in ? ld_stream(vp + (t0 + U + u) * 32) : 0.f;
+        const bool in = t0 + U + u < NT;
+        vn[u] = in ? ld_stream(vp + (t0 + U + u) * 32) : T(0);
         cn[u] = in ? ld_stream(cp + (t0 + U + u) * 32) : 0;
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) xv[u] = __ldg(x + c[u]);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        acc = fmaf(v[u], xv[u], acc);
+        acc = fmadd(v[u], xv[u], acc);
         v[u] = vn[u];
         c[u] = cn[u];
       }
@@ -486,10 +493,10 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
   } else if constexpr (EPI == EPI_DEFECT) {
     y[row] = pre_b - acc;
   } else if constexpr (EPI == EPI_JACOBI) {
-    const float d = (pre_b - acc) / pre_d;
+    const T d = (pre_b - acc) / pre_d;
     y[row] = pre_x + alpha * d;
   } else if constexpr (EPI == EPI_RESTRICT) {
-    y[row] = row_is_active(mask, row) ? acc : 0.f;
+    y[row] = row_is_active(mask, row) ? acc : T(0);
   } else if constexpr (EPI == EPI_PROLONG) {
     if (row_is_active(mask, row)) y[row] = pre_y + alpha * acc;
   }

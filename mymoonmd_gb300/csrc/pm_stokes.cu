@@ -264,6 +264,7 @@ void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTa
   k_gather_stokes<<<gr, 256, 0, c->stream>>>(L.n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
   PM_CHECK_LAUNCH();
   c->kernel_launches += nd ? 4 : 3;
+  A.values_changed(c);
 }
 
 // --------------------------------------------------- projected matrix ------
@@ -300,6 +301,8 @@ void ProjectedMatrix::refresh(pm_ctx* c, const DevCsr& sys, bool fp32) {
       nnz, src.p, sys.vals.p, csr.vals.p);
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
+  csr.values_changed(c);
+  csr.make_sliced64(c);
   if (fp32) csr.make_fp32(c);
 }
 

@@ -6,10 +6,10 @@
     python -m mymoonmd_gb300.profile_cases spmv
         the finest 32^3 Q2 matrix: two FP64 and two FP32 SpMV launches
     python -m mymoonmd_gb300.profile_cases sliced
-        the request above once per FP32 SpMV kernel shape (option
-        fp32_sliced_spmv: 0 = row groups, else sliced-ELL shapes): request time,
-        iterations, and the finest-level Jacobi sweep and defect bandwidths
-        from the launch probe
+        the request above once per SpMV kernel shape (option fp32_sliced_spmv,
+        or fp64_sliced_spmv with --precision fp64: 0 = row groups, else
+        sliced-ELL shapes): request time, iterations, and the finest-level
+        Jacobi sweep and defect bandwidths from the launch probe
     python -m mymoonmd_gb300.profile_cases assembly
         one assembly of the four 32^3 Q2 levels
     python -m mymoonmd_gb300.profile_cases stokes [--precision ...] [--smoother ...] [--coarse ...]
@@ -88,8 +88,10 @@ def main() -> None:
     if args.case == "sliced":
         import time
         nnz = prob.matrix(-1).nnz
+        fp64 = args.precision == "fp64"
+        opt = "fp64_sliced_spmv" if fp64 else "fp32_sliced_spmv"
         for shape in [int(v) for v in args.shapes.split(",")]:
-            ctx.set_option("fp32_sliced_spmv", shape)
+            ctx.set_option(opt, shape)
             for _ in range(2):  # lays out the sliced copies, captures the graphs
                 prob.reset_solution()
                 prob.assemble()
@@ -106,7 +108,7 @@ def main() -> None:
             bw = {}
             for epi in (3, 2):  # Jacobi sweep, defect
                 ctx.set_option("probe_epilogue", epi)
-                ctx.set_option("probe_precision", 4)
+                ctx.set_option("probe_precision", 8 if fp64 else 4)
                 ctx.probe(nnz)
                 prob.reset_solution()
                 prob.assemble()
@@ -119,7 +121,7 @@ def main() -> None:
             print(f"shape {shape:3d}: request {ms:7.2f} ms, {its} iterations, finest Jacobi "
                   f"{bw[3][0]:6.0f} GB/s ({bw[3][1]} launches), defect {bw[2][0]:6.0f} GB/s ({bw[2][1]})",
                   flush=True)
-        ctx.set_option("fp32_sliced_spmv", 481)
+        ctx.set_option(opt, 441 if fp64 else 481)
     elif args.case == "request":
         for _ in range(2):
             prob.reset_solution()

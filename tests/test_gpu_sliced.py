@@ -1,6 +1,8 @@
-"""The sliced-ELL FP32 SpMV kernel (context option fp32_sliced_spmv) against
-the FP64 oracle, against the row-group FP32 kernel, and inside the mixed
-multigrid (Jacobi sweeps, defects and restriction run on the sliced copies).
+"""The sliced-ELL SpMV kernel (context options fp32_sliced_spmv and
+fp64_sliced_spmv) against the FP64 oracle, against the row-group kernels, and
+inside the multigrid (Jacobi sweeps, defects and restriction run on the sliced
+copies). The cases have more than 16 entries per row on their finest level,
+the matrices that get a sliced copy.
 
 Tolerances: FP32 SpMV within 2e-6 of sum_j |a_ij x_j| (FP32 rounding of about
 60 products per row); shapes with the same lanes per row sum in the same order
@@ -35,7 +37,7 @@ def fp32_spmv(ctx, A, x):
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-@pytest.mark.parametrize("case", ["q1_3d", "q2_3d"])
+@pytest.mark.parametrize("case", ["q2_3d", "q2_3d_root3"])
 def test_sliced_spmv_matches_fp64_within_fp32_rounding(ctx, sliced, case, shape):
     disc, prob, ora = make_pair(ctx, case, mg_db(CASES[case][3]))
     A = prob.matrix(-1)
@@ -115,3 +117,64 @@ def test_sliced_kernel_in_iterative_coarse_loop(ctx, sliced, coarse_residual):
         out[shape] = r.numpy()
         prob.close()
     assert rel(out[DEFAULT], out[0]) <= 1e-4
+
+
+SHAPES64 = [441, 481, 841]
+DEFAULT64 = 441
+
+
+@pytest.fixture
+def sliced64(ctx):
+    """sets the FP64 shape for one test and puts the library default back"""
+    def set_shape(shape):
+        ctx.set_option("fp64_sliced_spmv", shape)
+    yield set_shape
+    ctx.set_option("fp64_sliced_spmv", DEFAULT64)
+
+
+@pytest.mark.parametrize("shape", SHAPES64)
+@pytest.mark.parametrize("case", ["q2_3d", "q2_3d_root3"])
+def test_fp64_sliced_spmv_matches_oracle(ctx, sliced64, case, shape):
+    """the FP64 sliced copy (laid out by the solver's update) gives
+    apply_scaled_add within 1e-13 of sum_j |a_ij x_j| of the oracle. With 4
+    lanes per row it sums each row in the order of the FP64 row-group kernel
+    (4 lanes, entries j = lane mod 4, pairs combined (0+2)+(1+3)): the same
+    bits; with 8 lanes the order differs (the sliced kernel is in use)"""
+    sliced64(shape)
+    disc, prob, ora = make_pair(ctx, case, mg_db(CASES[case][3]))
+    prob.solve()  # update: the FP64 sliced copies of every level
+    A = prob.matrix(-1)
+    lv = ora.finest
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(lv.n_dofs)
+    y0 = rng.standard_normal(lv.n_dofs)
+    out = {}
+    for s in (shape, 0):
+        sliced64(s)
+        xd, yd = m.DeviceVector.from_numpy(ctx, x), m.DeviceVector.from_numpy(ctx, y0)
+        A.apply_scaled_add(xd, yd, -0.7)
+        out[s] = yd.numpy()
+    ref = ocd.apply_scaled_add(lv.row_ptr, lv.cols, ora.vals[-1], ora.active(), x, y0, -0.7)
+    scale = ocd.apply_scaled_add(lv.row_ptr, lv.cols, np.abs(ora.vals[-1]), ora.active(), np.abs(x),
+                                 np.abs(y0), 0.7)
+    assert np.all(np.abs(out[shape] - ref) <= 1e-13 * scale)
+    if shape // 100 == 4:
+        assert np.array_equal(out[shape], out[0])
+    else:
+        assert not np.array_equal(out[shape], out[0])
+
+
+@pytest.mark.parametrize("shape", [0, 441, 841])
+def test_fp64_form_with_each_kernel_matches_oracle(ctx, sliced64, shape):
+    """the FP64 form (Krylov SpMV, Jacobi sweeps, defects, restriction on the
+    FP64 sliced copies): final solution within 1e-10 of the oracle's, FGMRES
+    iteration counts within one"""
+    sliced64(shape)
+    db = mg_db(3, restart=20, reduction=1e-10)
+    disc, prob, ora = make_pair(ctx, "q2_3d", db)
+    prob.solve()
+    it, res, init = prob.last_info()
+    ora.build_mg(2, 2, 0.8, 1.0, "V")
+    sol, oit, ores, ohist, st = ora.solve("fgmres", 0.0, 1e-10, 200, 0, 20)
+    assert abs(it - oit) <= 1
+    assert rel(prob.solution(), sol) <= 1e-10
