@@ -83,7 +83,13 @@ int pm_version(void);
  *   the shape's L. Shapes with the same L give the same bits;
  *   "pdl" 0|1 - sliced-ELL launches with programmatic stream serialization:
  *   a sweep loads its slice layout and first values while the previous
- *   kernel finishes, and waits for it before reading vectors (default 1). */
+ *   kernel finishes, and waits for it before reading vectors (default 1);
+ *   "fp64_sliced_spmv" 0|441|481|841 - the same for FP64 values (the Krylov
+ *   SpMV, the FP64 multigrid); used when its L equals the layout's (default 441);
+ *   "jacobi_zero_start" 0|1 - the first damped Jacobi sweep of a multigrid level
+ *   whose iterate is exactly zero (coarse levels after their reset; the finest
+ *   level inside FGMRES when the initial residual has zero non-actives) as the
+ *   diagonal scaling x = w b / d, which gives the sweep's bits (default 1). */
 int pm_ctx_set_option(pm_ctx* ctx, const char* key, int value);
 /* Launch probe (no reference counterpart; measurement only): while enabled
  * (nnz != 0), every SpMV-family launch (apply, defect, Jacobi sweep, transfer)

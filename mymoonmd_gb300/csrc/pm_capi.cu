@@ -91,6 +91,10 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->sell_shape64 = value;
     return PM_OK;
   }
+  if (std::string(key) == "jacobi_zero_start") {
+    c->jacobi_zero_start = value != 0;
+    return PM_OK;
+  }
   if (std::string(key) == "pdl") {
     c->pdl = value != 0;
     return PM_OK;

@@ -120,6 +120,9 @@ struct pm_ctx {
   int sell_shape64 = 441;
   // sliced-ELL launches with programmatic stream serialization (option "pdl")
   bool pdl = true;
+  // first Jacobi sweep from an exactly zero iterate as a diagonal scaling
+  // (option "jacobi_zero_start"; same bits as the full sweep)
+  bool jacobi_zero_start = true;
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

@@ -777,11 +777,39 @@ void copy_nonactive(pm_ctx* c, int n, const BlockMask& m, const double* src, dou
   PM_LAUNCH1D(k_copy_nonactive, n, n, m, src, dst);
 }
 
+// flag := 1 if a non-active entry of x is not zero
+__global__ void k_nonactive_nonzero(BlockMask m, const double* __restrict__ x, int* __restrict__ flag) {
+  for (int b = 0; b < m.nb; ++b)
+    for (int i = m.active_end[b] + blockIdx.x * blockDim.x + threadIdx.x; i < m.end[b];
+         i += gridDim.x * blockDim.x)
+      if (x[i] != 0.0) *flag = 1;
+}
+void nonactive_nonzero(pm_ctx* c, const BlockMask& m, const double* x, int* flag) {
+  k_nonactive_nonzero<<<kRedBlocks, 256, 0, c->stream>>>(m, x, flag);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
 void init_solution(pm_ctx* c, int n, const BlockMask& m, const double* rhs, double* sol) {
   PM_LAUNCH1D(k_init_sol<double>, n, n, m, rhs, sol);
 }
 void init_solution32(pm_ctx* c, int n, const BlockMask& m, const float* rhs, float* sol) {
   PM_LAUNCH1D(k_init_sol<float>, n, n, m, rhs, sol);
+}
+
+// x = 0 + w ((b - 0) / d): the damped Jacobi sweep of an exactly zero iterate
+// (the sweep's row sums of a_ij * 0 are +0; fma(w, q, +0) rounds like its
+// x + w q with x = +0)
+template <class T>
+__global__ void k_jacobi_zero(int n, const T* __restrict__ b, const T* __restrict__ d, T w, T* __restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = fmadd(w, (b[i] - T(0)) / d[i], T(0));
+}
+void jacobi_from_zero(pm_ctx* c, int n, const double* b, const double* d, double w, double* x) {
+  PM_LAUNCH1D(k_jacobi_zero<double>, n, n, b, d, w, x);
+}
+void jacobi_from_zero32(pm_ctx* c, int n, const float* b, const float* d, float w, float* x) {
+  PM_LAUNCH1D(k_jacobi_zero<float>, n, n, b, d, w, x);
 }
 
 // ------------------------------------------------------- dense inverse ------

@@ -100,9 +100,14 @@ void vcopy32(pm_ctx* c, int n, const float* x, float* y);
 // sol := 0 on active rows, rhs on non-active rows (Multigrid::cycle start)
 void init_solution(pm_ctx* c, int n, const BlockMask& m, const double* rhs, double* sol);
 void init_solution32(pm_ctx* c, int n, const BlockMask& m, const float* rhs, float* sol);
+// x := w (b / d), the damped Jacobi sweep from x = 0
+void jacobi_from_zero(pm_ctx* c, int n, const double* b, const double* d, double w, double* x);
+void jacobi_from_zero32(pm_ctx* c, int n, const float* b, const float* d, float w, float* x);
 void vdiv(pm_ctx* c, int n, const double* d, double* y);  // y /= d
 // BlockVector::copy_nonactive: dst := src on the non-active rows
 void copy_nonactive(pm_ctx* c, int n, const BlockMask& m, const double* src, double* dst);
+// *flag := 1 if some non-active entry of x is not zero (the caller clears it)
+void nonactive_nonzero(pm_ctx* c, const BlockMask& m, const double* x, int* flag);
 
 // dense inverse of the active block of a small CSR matrix (Gauss-Jordan with
 // partial pivoting on the device); used by the coarse-grid direct solve

@@ -221,6 +221,19 @@ void Multigrid::smooth(pm_ctx* c, int l) {
   }
 }
 
+void Multigrid::smooth_from_zero(pm_ctx* c, int l) {
+  MGLevel& lv = levels[l];
+  const DevCsr& A = lv.A->csr;
+  if (lv.smoother != SM_JACOBI || !c->jacobi_zero_start) {
+    smooth(c, l);
+    return;
+  }
+  // the iterate stays in its buffer (the sweep's swap of the two buffers is
+  // not needed: x0 is not read)
+  if (mixed) jacobi_from_zero32(c, A.n_rows, lv.rhs32.p, A.diag32.p, float(jacobi_damp), lv.cur32);
+  else jacobi_from_zero(c, A.n_rows, lv.rhs.p, A.diag.p, jacobi_damp, lv.cur);
+}
+
 void Multigrid::coarse_solve(pm_ctx* c) {
   MGLevel& lv = levels[0];
   const DevCsr& A = lv.A->csr;
@@ -313,7 +326,7 @@ void Multigrid::prolongate_from(pm_ctx* c, int l) {
     csr_apply(c, crs.P, EPI_PROLONG, crs.cur, fine.cur, nullptr, correction_damp);
 }
 
-void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol) {
+void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol, bool rhs_nonactive_zero) {
   if (!ready) throw Error(PM_E_INVALID, "multigrid used before update()");
   const int L = int(levels.size());
   const int finest = L - 1;
@@ -333,6 +346,11 @@ void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol) {
     vcopy(c, nf, rhs, top.rhs.p);
     init_solution(c, nf, top.A->csr.mask, top.rhs.p, top.cur);
   }
+  // levels whose iterate is exactly zero now: the finest one when its rhs has
+  // zero non-actives (init_solution copies them), the coarser ones after their
+  // reset below (their rhs has its non-actives reset by the restriction)
+  std::vector<char> zero(L, 0);
+  zero[finest] = rhs_nonactive_zero ? 1 : 0;
   const int n_steps = int(control.size()) - 1;
   int level = finest;
   for (int step = 1; step <= n_steps && level >= 0; ++step) {
@@ -341,7 +359,9 @@ void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol) {
       // the defects the reference computes around it only feed its loop test
       if (levels[0].smoother == SM_DIRECT) coarse_solve(c);
       else coarse_iterate(c);
+      zero[0] = 0;
       prolongate_from(c, 0);
+      zero[1] = 0;
       level = 1;
       continue;
     }
@@ -351,16 +371,22 @@ void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol) {
     if (from_below)
       for (int i = 0; i < n_post; ++i) smooth(c, level);
     if (down) {
-      for (int i = 0; i < n_pre; ++i) smooth(c, level);
+      for (int i = 0; i < n_pre; ++i) {
+        if (i == 0 && zero[level]) smooth_from_zero(c, level);
+        else smooth(c, level);
+        zero[level] = 0;
+      }
       defect(c, level);
       MGLevel& crs = levels[level - 1];
       const int nc = crs.A->csr.n_rows;
       if (mixed) PM_CUDA(cudaMemsetAsync(crs.cur32, 0, sizeof(float) * nc, c->stream));
       else PM_CUDA(cudaMemsetAsync(crs.cur, 0, sizeof(double) * nc, c->stream));
+      zero[level - 1] = 1;
       restrict_to(c, level);
       level -= 1;
     } else if (up) {
       prolongate_from(c, level);
+      zero[level + 1] = 0;
       level += 1;
     } else {
       level = -1;
@@ -778,7 +804,7 @@ size_t pm_solver::layout_signature() const {
   mix(ctx->partials.p); mix(ctx->host_scalars);
   h ^= size_t(restart) * 31 + size_t(work_n);
   h = h * 1099511628211ull ^ (size_t(ctx->sell_shape) * 2 + size_t(ctx->bulk_spmv));
-  h = h * 1099511628211ull ^ (size_t(ctx->sell_shape64) * 2 + size_t(ctx->pdl));
+  h = h * 1099511628211ull ^ (size_t(ctx->sell_shape64) * 4 + size_t(ctx->pdl) * 2 + size_t(ctx->jacobi_zero_start));
   return h;
 }
 
@@ -805,10 +831,10 @@ bool pm_solver::converged(double r, unsigned it) {
   return conv;
 }
 
-void pm_solver::precondition(const double* z, double* r) {
+void pm_solver::precondition(const double* z, double* r, bool z_nonactive_zero) {
   const int n = A->csr.n_rows;
   if (use_mg) {
-    mg.apply(ctx, z, r);
+    mg.apply(ctx, z, r, z_nonactive_zero);
   } else if (prec == "jacobi") {
     // Iteration_jacobi::apply: r = z / diag
     vcopy(ctx, n, z, r);
@@ -844,30 +870,40 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
   double* cgs_part = dres + 8;                 // 64 x kRedBlocks partial sums
   double* h1 = cgs_part + 64 * size_t(kRedBlocks);
   double* h2 = h1 + 64;
-  if (flags.n < 2) {  // [0] breakdown, [1] skip of the second Gram-Schmidt pass
+  if (flags.n < 3) {  // [0] breakdown, [1] skip of the second Gram-Schmidt pass, [2] non-zero non-actives
     drop_graphs();
-    flags.alloc(2);
+    flags.alloc(3);
   }
   PM_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), c->stream));
   PM_CUDA(cudaMemsetAsync(H, 0, sizeof(double) * size_t(ldh) * m, c->stream));
-  {
-    const size_t sig = layout_signature();
-    if (sig != graphs_signature) {
-      drop_graphs();
-      graphs_signature = sig;
-    }
-  }
   double* partA = c->partials.p;
   double* partB = c->partials.p + kRedBlocks;
   if (use_mg && mg.mixed_cfg) mg.set_mixed(c, true);  // every solve starts in the mixed form
   std::vector<double> res_hist;  // residual after each iteration (for the fallback test)
 
   csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);  // r = rhs - A sol
+  // exact zeros in the non-active entries of the initial residual carry over
+  // to every basis vector (A's non-active rows are unit rows and the
+  // multigrid copies non-actives through): the cycles may then start the
+  // finest level from an exactly zero iterate
+  PM_CUDA(cudaMemsetAsync(flags.p + 2, 0, sizeof(int), c->stream));
+  nonactive_nonzero(c, M.mask, r, flags.p + 2);
   dot_partials(c, n, r, r, partA);
   finish_sum(c, partA, dres, true);
   PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(c->host_scalars + 2), flags.p + 2, sizeof(int),
+                          cudaMemcpyDeviceToHost, c->stream));
   PM_CUDA(cudaStreamSynchronize(c->stream));
   double resid = c->host_scalars[0];
+  const bool na_zero = *reinterpret_cast<int*>(c->host_scalars + 2) == 0;
+  {
+    // the captured Arnoldi steps depend on the buffers and on na_zero
+    const size_t sig = layout_signature() * 1099511628211ull ^ (na_zero ? 0x9e3779b9ull : 0ull);
+    if (sig != graphs_signature) {
+      drop_graphs();
+      graphs_signature = sig;
+    }
+  }
   if (converged(resid, 0)) return;
 
   const int grid = kRedBlocks;
@@ -888,7 +924,7 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
       auto arnoldi_step = [&]() {
         double* vi = V + ld * i;
         double* zi = Z + ld * i;
-        precondition(vi, zi);
+        precondition(vi, zi, na_zero);
         csr_apply(c, M, EPI_SET, zi, r, nullptr, 1.0);  // r = A z_i
         double* pin = partA;
         if (cgs2 && !cgs_cond && i + 1 <= kCgsFused) {

@@ -72,9 +72,16 @@ struct Multigrid {
 
   void configure(const Params& p);
   void update(pm_ctx* c);                                  // Multigrid::update
-  void apply(pm_ctx* c, const double* rhs, double* sol);  // Iteration_multigrid::apply
+  // Iteration_multigrid::apply; rhs_nonactive_zero: the caller guarantees
+  // exact zeros in the non-active entries of rhs (FGMRES basis vectors whose
+  // initial residual had them), so the finest iterate starts at exact zero
+  void apply(pm_ctx* c, const double* rhs, double* sol, bool rhs_nonactive_zero = false);
   // pieces of one cycle (Multigrid::cycle_step)
   void smooth(pm_ctx* c, int l);
+  // the first smoothing step from an iterate that is exactly zero: a damped
+  // Jacobi sweep reduces to x = w (b / d) with the sweep's bits (A*0 sums to
+  // +0); other smoothers sweep as usual
+  void smooth_from_zero(pm_ctx* c, int l);
   void defect(pm_ctx* c, int l);
   void restrict_to(pm_ctx* c, int l);  // from l to l-1
   void prolongate_from(pm_ctx* c, int l);  // from l to l+1
@@ -139,7 +146,7 @@ struct pm_solver {
   void ensure_work(size_t n_vectors, int n);
   bool converged(double r, unsigned it);
   void solve(const double* rhs, double* sol);
-  void precondition(const double* z, double* r);
+  void precondition(const double* z, double* r, bool z_nonactive_zero = false);
   void fgmres(const double* rhs, double* sol);
   void cg(const double* rhs, double* sol);
   void bicgstab(const double* rhs, double* sol);

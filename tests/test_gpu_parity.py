@@ -233,6 +233,28 @@ def test_reassembled_problem_solves_like_a_fresh_one(ctx, precision):
     fresh.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("cycle", ["V", "W"])
+def test_jacobi_zero_start_gives_the_full_sweeps_bits(ctx, precision, cycle):
+    """the first Jacobi sweep from an exactly zero iterate, done as a diagonal
+    scaling, leaves every FGMRES iterate and the solution bit for bit unchanged
+    (W cycles revisit levels whose iterate is no longer zero)"""
+    out = {}
+    try:
+        for flag in (1, 0):
+            ctx.set_option("jacobi_zero_start", flag)
+            db = mg_db(3, restart=20, reduction=1e-10, precision=precision, cycle=cycle)
+            disc, prob, ora = make_pair(ctx, "q2_3d", db)
+            prob.solve()
+            out[flag] = (prob.solution(), prob.last_info(), prob.solver().residual_history())
+            prob.close()
+    finally:
+        ctx.set_option("jacobi_zero_start", 1)
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])
+    assert np.array_equal(out[0][0], out[1][0])
+
+
 @pytest.mark.parametrize("method", ["fgmres", "cg", "bi_cgstab"])
 def test_krylov_on_reference_test_system(ctx, method):
     """the 7x7 block system of test/iterative_solver_test.c++ solved on the GPU"""
