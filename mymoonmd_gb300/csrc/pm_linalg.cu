@@ -1130,7 +1130,211 @@ __global__ void __launch_bounds__(256) k_gj_rows(int na, int R, double* __restri
 
 constexpr size_t kGjRowsSmem = 160 * 1024;  // dynamic shared memory cap of k_gj_rows
 
-void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
+// Gauss-Jordan inverse in FP32 on one cluster of kGjCluster thread blocks:
+// block r keeps positions [r R, r R + R) in its shared memory, and the blocks
+// read each other's published rows through distributed shared memory. Per
+// column one cluster barrier: after step k every block publishes its pivot
+// candidate for column k+1 (arg-max value, position and the row, double
+// buffered) and the owner of position k+1 publishes that row; at step k+1
+// every block picks the pivot from the candidates (the rule of k_gj_pivot:
+// largest |a|, smallest position on ties), copies the pivot row and the old
+// row k+1 and eliminates its own rows. The column swaps are undone on the
+// rows in shared memory before they are written out.
+constexpr int kGjCluster = 8;
+constexpr int kGjClusterThreads = 512;
+constexpr size_t kGjClusterSmem = 220 * 1024;
+
+__device__ __forceinline__ void gj_merge32(float& v, int& i, float v2, int i2) {
+  if (v2 > v || (v2 == v && i2 < i)) {
+    v = v2;
+    i = i2;
+  }
+}
+
+__global__ void __cluster_dims__(kGjCluster, 1, 1) __launch_bounds__(kGjClusterThreads)
+k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ out, int* __restrict__ flag) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) float gjc_smem[];
+  __shared__ float cand_v[2];
+  __shared__ int cand_i[2];
+  __shared__ float s_f[128];  // multipliers of the own rows (R <= 128)
+  __shared__ int s_p, s_src, s_cand, s_sing;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int rank = int(cluster.block_rank());
+  const int r0 = min(na, rank * R), r1 = min(na, r0 + R), nr = r1 - r0;
+  float* own = gjc_smem;                    // [R][na]
+  float* pubrow = own + (size_t)R * na;     // [2][na] pivot candidate for the next column
+  float* pubold = pubrow + 2 * (size_t)na;  // [2][na] the row at the next position (its owner)
+  float* prow = pubold + 2 * (size_t)na;    // scaled pivot row of the step
+  float* orow = prow + na;                  // row k before the step
+  int* perm_s = reinterpret_cast<int*>(orow + na);  // pivot positions
+  for (int e = t; e < nr * na; e += blockDim.x) own[e] = float(M[(size_t)r0 * na + e]);
+  if (t == 0) s_sing = 0;
+  __syncthreads();
+  auto publish = [&](int col, int buf) {
+    if (warp == 0) {
+      float v = -1.0f;
+      int i = na;
+      for (int q = lane; q < nr; q += 32)
+        if (r0 + q >= col) gj_merge32(v, i, fabsf(own[(size_t)q * na + col]), r0 + q);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        gj_merge32(v, i, v2, i2);
+      }
+      if (lane == 0) {
+        cand_v[buf] = v;
+        cand_i[buf] = i;
+        s_cand = i < na ? i - r0 : -1;
+      }
+    }
+    __syncthreads();
+    if (s_cand >= 0)
+      for (int j = t; j < na; j += blockDim.x) pubrow[(size_t)buf * na + j] = own[(size_t)s_cand * na + j];
+    if (col >= r0 && col < r1)
+      for (int j = t; j < na; j += blockDim.x) pubold[(size_t)buf * na + j] = own[(size_t)(col - r0) * na + j];
+  };
+  publish(0, 0);
+  cluster.sync();
+  for (int k = 0; k < na; ++k) {
+    const int buf = k & 1;
+    if (warp == 0) {  // the pivot: the same reduction in every block
+      float v = -1.0f;
+      int i = na;
+      if (lane < kGjCluster) {
+        const float* rv = cluster.map_shared_rank(cand_v, lane);
+        const int* ri = cluster.map_shared_rank(cand_i, lane);
+        v = rv[buf];
+        i = ri[buf];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        gj_merge32(v, i, v2, i2);
+      }
+      if (lane == 0) {
+        const bool singular = !(v > 0.0f);
+        s_p = singular ? k : i;
+        s_src = singular ? -1 : i / R;  // -1: the pivot row is the old row k
+        perm_s[k] = s_p;
+        if (singular) s_sing = 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    const int owner_k = k / R;
+    const float* old = cluster.map_shared_rank(pubold, owner_k) + (size_t)buf * na;
+    const float* src = s_src < 0 ? old : cluster.map_shared_rank(pubrow, s_src) + (size_t)buf * na;
+    const float pv = s_src < 0 ? 1.0f : src[k];
+    for (int j = t; j < na; j += blockDim.x) {
+      prow[j] = (j == k ? 1.0f : src[j]) / pv;
+      orow[j] = old[j];
+    }
+    if (t < nr) {
+      const int i = r0 + t;
+      s_f[t] = (i == p && p != k) ? old[k] : own[(size_t)t * na + k];
+    }
+    __syncthreads();
+    for (int e = t; e < nr * na; e += blockDim.x) {
+      const int ii = e / na, j = e - ii * na;
+      const int i = r0 + ii;
+      float* Mi = own + (size_t)ii * na;
+      if (i == k) {
+        Mi[j] = prow[j];
+      } else {
+        const float base = (i == p && p != k) ? orow[j] : Mi[j];
+        Mi[j] = (j == k ? 0.0f : base) - s_f[ii] * prow[j];
+      }
+    }
+    __syncthreads();
+    if (k + 1 < na) publish(k + 1, buf ^ 1);
+    cluster.sync();  // publications visible; every block is done reading this step's
+  }
+  // undo the column swaps (k_gj_unswap) on the own rows, write them out
+  for (int q = t; q < nr; q += blockDim.x) {
+    float* row = own + (size_t)q * na;
+    for (int k = na - 1; k >= 0; --k) {
+      const int pk = perm_s[k];
+      if (pk != k) {
+        const float a = row[k];
+        row[k] = row[pk];
+        row[pk] = a;
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = t; e < nr * na; e += blockDim.x) out[(size_t)r0 * na + e] = own[e];
+  if (t == 0 && s_sing) *flag = 1;
+}
+
+__global__ void k_coarse_gemv32(int n, int na, const int* __restrict__ act, const int* __restrict__ pos,
+                                const float* __restrict__ inv, const float* __restrict__ b,
+                                float* __restrict__ x) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp < na) {
+    const float* row = inv + (size_t)warp * na;
+    float s = 0.0f;
+    for (int j = lane; j < na; j += 32) s += row[j] * b[act[j]];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) x[act[warp]] = s;
+  } else {
+    const int t = (warp - na) * 32 + lane;
+    if (t < n && pos[t] < 0) x[t] = b[t];
+  }
+}
+
+void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
+  n = A.n_rows;
+  int na_ = 0;
+  for (int i = 0; i < n; ++i)
+    for (int b = 0; b < A.mask.nb; ++b)
+      if (i >= A.mask.start[b] && i < A.mask.end[b] && i < A.mask.active_end[b]) ++na_;
+  const int R = (na_ + kGjCluster - 1) / kGjCluster;
+  const size_t smem = (size_t(R) + 6) * na_ * sizeof(float) + size_t(na_) * sizeof(int);
+  if (na_ == 0 || R > 128 || smem > kGjClusterSmem) {
+    build(c, A);  // large: the FP64 inverse, rounded
+    inv32.ensure(size_t(na) * na);
+    if (na) {
+      k_d2f<<<grid_for(c, (long long)na * na), 256, 0, c->stream>>>((long long)na * na, inv.p, inv32.p);
+      PM_CHECK_LAUNCH();
+      c->kernel_launches++;
+    }
+    has32 = true;
+    return;
+  }
+  prepare(c, A);  // act, pos, the dense active block in inv (FP64)
+  inv32.ensure(size_t(na) * na);
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_gj_cluster32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(kGjClusterSmem));
+  });
+  PM_CUDA(attr_err);
+  k_gj_cluster32<<<kGjCluster, kGjClusterThreads, smem, c->stream>>>(na, R, inv.p, inv32.p, flag.p);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+  int h_flag = 0;
+  PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  if (h_flag) throw Error(PM_E_BREAKDOWN, "coarse matrix is singular (zero pivot)");
+  has64 = false;  // inv holds the active block, not its inverse
+  has32 = true;
+}
+
+void DenseInverse::solve32(pm_ctx* c, const float* b, float* x) {
+  if (!has32) throw Error(PM_E_INVALID, "coarse FP32 inverse used before build32");
+  const long long threads = (long long)(na + (n + 31) / 32) * 32;
+  k_coarse_gemv32<<<nblocks(threads, 256), 256, 0, c->stream>>>(n, na, act.p, pos.p, inv32.p, b, x);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+void DenseInverse::prepare(pm_ctx* c, const DevCsr& A) {
   n = A.n_rows;
   std::vector<int> h_act, h_pos(n, -1);
   for (int i = 0; i < n; ++i) {
@@ -1151,11 +1355,20 @@ void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
   perm.ensure(std::max(na, 1));
   flag.ensure(1);
   PM_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c->stream));
+  has64 = has32 = false;
   if (na == 0) return;
   k_dense_fill<<<nblocks(na, 128), 128, 0, c->stream>>>(na, act.p, pos.p, A.row_ptr.p, A.cols.p,
                                                         A.vals.p, inv.p);
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
+}
+
+void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
+  prepare(c, A);
+  if (na == 0) {
+    has64 = true;
+    return;
+  }
   int coop = 0, per_sm = 0;
   PM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
   PM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
@@ -1223,6 +1436,7 @@ void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
   PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   PM_CUDA(cudaStreamSynchronize(c->stream));
   if (h_flag) throw Error(PM_E_BREAKDOWN, "coarse matrix is singular (zero pivot)");
+  has64 = true;
 }
 
 // tmp_a = b_a - sum over non-active columns of A_{a,j} b_j

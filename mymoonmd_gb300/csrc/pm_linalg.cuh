@@ -127,7 +127,19 @@ struct DenseInverse {
   // arg-max values and positions ([2][blocks])
   DBuf<double> pub_rows, pub_v;
   DBuf<int> pub_i;
+  // FP32 inverse for the mixed-precision cycle (build32); has64/has32: which
+  // inverse holds the current matrix
+  DBuf<float> inv32;
+  bool has64 = false, has32 = false;
   void build(pm_ctx* c, const DevCsr& A);
+  // act, pos and the dense active block (FP64) in inv
+  void prepare(pm_ctx* c, const DevCsr& A);
+  // the FP32 inverse: Gauss-Jordan in FP32 on one thread-block cluster when
+  // the active block fits its distributed shared memory, else the FP64
+  // inverse rounded to FP32
+  void build32(pm_ctx* c, const DevCsr& A);
+  // x_a = inv32 b_a, x_n = b_n for a right-hand side with zero non-actives
+  void solve32(pm_ctx* c, const float* b, float* x);
   // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active);
   // rhs_nonactive_zero skips the b_n correction (the multigrid coarse rhs has
   // its non-actives reset to zero)

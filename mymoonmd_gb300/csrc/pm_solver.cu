@@ -122,6 +122,8 @@ void Multigrid::set_mixed(pm_ctx* c, bool on) {
       const bool nodal = lv.smoother == SM_NODAL_VANKA || lv.smoother == SM_NODAL_VANKA_JACOBI;
       if (vanka) lv.vanka->factor(c, lv.proj->csr, false);
       if (nodal) lv.nodal->factor(c, lv.proj->csr, false);
+      // the mixed cycle built only the FP32 coarse inverse
+      if (lv.smoother == SM_DIRECT && !lv.coarse.has64) lv.coarse.build(c, lv.proj ? lv.proj->csr : lv.A->csr);
     }
     fp64_smoothers = true;
   }
@@ -181,8 +183,11 @@ void Multigrid::update(pm_ctx* c) {
     lv.alt.ensure(n);
     lv.defect.ensure(n);
     if (lv.smoother == SM_DIRECT) {
-      // DirectSolver factorises get_combined_matrix (with the pressure projection)
-      lv.coarse.build(c, lv.proj ? lv.proj->csr : A);
+      // DirectSolver factorises get_combined_matrix (with the pressure projection);
+      // the mixed cycle solves with an FP32 inverse (the FP64 one is made on a
+      // fallback to FP64)
+      if (mixed) lv.coarse.build32(c, lv.proj ? lv.proj->csr : A);
+      else lv.coarse.build(c, lv.proj ? lv.proj->csr : A);
       if (mixed) {
         lv.coarse_rhs64.ensure(n);
         lv.coarse_sol64.ensure(n);
@@ -239,9 +244,7 @@ void Multigrid::coarse_solve(pm_ctx* c) {
   const DevCsr& A = lv.A->csr;
   if (mixed) {
     // the coarse rhs comes from the restriction with its non-actives reset
-    vcvt_f2d(c, A.n_rows, lv.rhs32.p, lv.coarse_rhs64.p);
-    lv.coarse.solve(c, A, lv.coarse_rhs64.p, lv.coarse_sol64.p, true);
-    vcvt_d2f(c, A.n_rows, lv.coarse_sol64.p, lv.cur32);
+    lv.coarse.solve32(c, lv.rhs32.p, lv.cur32);
   } else {
     // the coarse rhs comes from the restriction with its non-actives reset
     lv.coarse.solve(c, A, lv.rhs.p, lv.cur, true);
@@ -798,6 +801,7 @@ size_t pm_solver::layout_signature() const {
     mix(lv.rhs.p); mix(lv.sol.p); mix(lv.alt.p); mix(lv.defect.p);
     mix(lv.rhs32.p); mix(lv.sol32.p); mix(lv.alt32.p); mix(lv.defect32.p);
     mix(lv.coarse.inv.p); mix(lv.coarse.act.p); mix(lv.coarse.pos.p); mix(lv.coarse.tmp.p);
+    mix(lv.coarse.inv32.p);
     mix(lv.coarse_rhs64.p); mix(lv.coarse_sol64.p);
   }
   mix(work.p); mix(gm.p); mix(flags.p);

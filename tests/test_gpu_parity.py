@@ -233,6 +233,21 @@ def test_reassembled_problem_solves_like_a_fresh_one(ctx, precision):
     fresh.close()
 
 
+@pytest.mark.parametrize("case", ["q1_2d", "q2_2d", "q2_3d", "q2_3d_root3"])
+def test_mixed_cycle_with_fp32_coarse_inverse_matches_oracle_cycle(ctx, case):
+    """the mixed form's cycle (FP32 smoothing, transfer and coarse solve with the
+    FP32 inverse from the one-cluster Gauss-Jordan) against the FP64 oracle
+    cycle: agreement to FP32 accuracy (1e-4 relative in the max norm)"""
+    nl = CASES[case][3]
+    disc, prob, ora = make_pair(ctx, case, mg_db(nl, precision="mixed"))
+    prob.solve()
+    ora.build_mg(2, 2, 0.8, 1.0, "V")
+    z = np.random.default_rng(17).standard_normal(ora.finest.n_dofs)
+    rd = m.DeviceVector(ctx, z.size)
+    prob.solver().apply_preconditioner(m.DeviceVector.from_numpy(ctx, z), rd)
+    assert rel(rd.numpy(), ora.mg_apply(z)) <= 1e-4
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("cycle", ["V", "W"])
 def test_jacobi_zero_start_gives_the_full_sweeps_bits(ctx, precision, cycle):
