@@ -91,6 +91,12 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->sell_shape64 = value;
     return PM_OK;
   }
+  if (std::string(key) == "coarse_cluster") {
+    if (value != 1 && value != 2 && value != 4 && value != 8)
+      return fail(c, PM_E_INVALID, "coarse_cluster is 1, 2, 4 or 8");
+    c->coarse_cluster = value;
+    return PM_OK;
+  }
   if (std::string(key) == "jacobi_zero_start") {
     c->jacobi_zero_start = value != 0;
     return PM_OK;

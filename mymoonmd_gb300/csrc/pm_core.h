@@ -123,6 +123,9 @@ struct pm_ctx {
   // first Jacobi sweep from an exactly zero iterate as a diagonal scaling
   // (option "jacobi_zero_start"; same bits as the full sweep)
   bool jacobi_zero_start = true;
+  // thread blocks of the FP32 coarse Gauss-Jordan cluster (option
+  // "coarse_cluster": 1, 2, 4 or 8; more when the matrix does not fit)
+  int coarse_cluster = 8;
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

@@ -1130,18 +1130,19 @@ __global__ void __launch_bounds__(256) k_gj_rows(int na, int R, double* __restri
 
 constexpr size_t kGjRowsSmem = 160 * 1024;  // dynamic shared memory cap of k_gj_rows
 
-// Gauss-Jordan inverse in FP32 on one cluster of kGjCluster thread blocks:
-// block r keeps positions [r R, r R + R) in its shared memory, and the blocks
-// read each other's published rows through distributed shared memory. Per
-// column one cluster barrier: after step k every block publishes its pivot
-// candidate for column k+1 (arg-max value, position and the row, double
-// buffered) and the owner of position k+1 publishes that row; at step k+1
-// every block picks the pivot from the candidates (the rule of k_gj_pivot:
-// largest |a|, smallest position on ties), copies the pivot row and the old
-// row k+1 and eliminates its own rows. The column swaps are undone on the
-// rows in shared memory before they are written out.
+// Gauss-Jordan inverse in FP32 on one cluster of CS thread blocks (CS = 1: a
+// single block): block r keeps positions [r R, r R + R) in its shared memory.
+// Per column one cluster barrier. Before it, every block pushes its pivot
+// candidate for the next column (arg-max value and position) into every
+// block's candidate table, keeps the candidate row in its own double-buffered
+// publication slot, and the owner of the next position pushes that row into
+// every block's old-row buffer. After it, every block picks the pivot from its
+// local table (the rule of k_gj_pivot: largest |a|, smallest position on
+// ties), reads the pivot row from the winner's slot (the one remote read of
+// the step) and eliminates its own rows, thread tx on column tx for the rows
+// ty, ty + G, ... . The column swaps are undone on the rows in shared memory
+// before they are written out.
 constexpr int kGjCluster = 8;
-constexpr int kGjClusterThreads = 512;
 constexpr size_t kGjClusterSmem = 220 * 1024;
 
 __device__ __forceinline__ void gj_merge32(float& v, int& i, float v2, int i2) {
@@ -1151,25 +1152,30 @@ __device__ __forceinline__ void gj_merge32(float& v, int& i, float v2, int i2) {
   }
 }
 
-__global__ void __cluster_dims__(kGjCluster, 1, 1) __launch_bounds__(kGjClusterThreads)
+template <int NT>
+__global__ void __launch_bounds__(NT)
 k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ out, int* __restrict__ flag) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) float gjc_smem[];
-  __shared__ float cand_v[2];
-  __shared__ int cand_i[2];
-  __shared__ float s_f[128];  // multipliers of the own rows (R <= 128)
+  __shared__ float cand_v[2][kGjCluster];
+  __shared__ int cand_i[2][kGjCluster];
+  __shared__ float s_f[256];  // multipliers of the own rows (R <= 256)
   __shared__ int s_p, s_src, s_cand, s_sing;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int CS = int(cluster.num_blocks());
   const int rank = int(cluster.block_rank());
   const int r0 = min(na, rank * R), r1 = min(na, r0 + R), nr = r1 - r0;
+  // column-major thread layout of the elimination: CW threads per row pass
+  const int na32 = (na + 31) & ~31;
+  const int G = max(1, NT / na32), CW = NT / G;
+  const int tx = t % CW, ty = t / CW;
   float* own = gjc_smem;                    // [R][na]
   float* pubrow = own + (size_t)R * na;     // [2][na] pivot candidate for the next column
-  float* pubold = pubrow + 2 * (size_t)na;  // [2][na] the row at the next position (its owner)
-  float* prow = pubold + 2 * (size_t)na;    // scaled pivot row of the step
-  float* orow = prow + na;                  // row k before the step
-  int* perm_s = reinterpret_cast<int*>(orow + na);  // pivot positions
-  for (int e = t; e < nr * na; e += blockDim.x) own[e] = float(M[(size_t)r0 * na + e]);
+  float* oldrow = pubrow + 2 * (size_t)na;  // [2][na] the row at the next position (pushed by its owner)
+  float* prow = oldrow + 2 * (size_t)na;    // scaled pivot row of the step
+  int* perm_s = reinterpret_cast<int*>(prow + na);  // pivot positions
+  for (int e = t; e < nr * na; e += NT) own[e] = float(M[(size_t)r0 * na + e]);
   if (t == 0) s_sing = 0;
   __syncthreads();
   auto publish = [&](int col, int buf) {
@@ -1184,17 +1190,20 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
         const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
         gj_merge32(v, i, v2, i2);
       }
-      if (lane == 0) {
-        cand_v[buf] = v;
-        cand_i[buf] = i;
-        s_cand = i < na ? i - r0 : -1;
+      if (lane < CS) {  // into every block's candidate table
+        cluster.map_shared_rank(&cand_v[buf][0], lane)[rank] = v;
+        cluster.map_shared_rank(&cand_i[buf][0], lane)[rank] = i;
       }
+      if (lane == 0) s_cand = i < na ? i - r0 : -1;
     }
     __syncthreads();
     if (s_cand >= 0)
-      for (int j = t; j < na; j += blockDim.x) pubrow[(size_t)buf * na + j] = own[(size_t)s_cand * na + j];
-    if (col >= r0 && col < r1)
-      for (int j = t; j < na; j += blockDim.x) pubold[(size_t)buf * na + j] = own[(size_t)(col - r0) * na + j];
+      for (int j = t; j < na; j += NT) pubrow[(size_t)buf * na + j] = own[(size_t)s_cand * na + j];
+    if (col >= r0 && col < r1)  // the old row of the next step, into every block
+      for (int q = 0; q < CS; ++q) {
+        float* dst = cluster.map_shared_rank(oldrow, q) + (size_t)buf * na;
+        for (int j = t; j < na; j += NT) dst[j] = own[(size_t)(col - r0) * na + j];
+      }
   };
   publish(0, 0);
   cluster.sync();
@@ -1203,11 +1212,9 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
     if (warp == 0) {  // the pivot: the same reduction in every block
       float v = -1.0f;
       int i = na;
-      if (lane < kGjCluster) {
-        const float* rv = cluster.map_shared_rank(cand_v, lane);
-        const int* ri = cluster.map_shared_rank(cand_i, lane);
-        v = rv[buf];
-        i = ri[buf];
+      if (lane < CS) {
+        v = cand_v[buf][lane];
+        i = cand_i[buf][lane];
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -1225,28 +1232,28 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
     }
     __syncthreads();
     const int p = s_p;
-    const int owner_k = k / R;
-    const float* old = cluster.map_shared_rank(pubold, owner_k) + (size_t)buf * na;
+    const float* old = oldrow + (size_t)buf * na;
     const float* src = s_src < 0 ? old : cluster.map_shared_rank(pubrow, s_src) + (size_t)buf * na;
     const float pv = s_src < 0 ? 1.0f : src[k];
-    for (int j = t; j < na; j += blockDim.x) {
-      prow[j] = (j == k ? 1.0f : src[j]) / pv;
-      orow[j] = old[j];
-    }
+    for (int j = t; j < na; j += NT) prow[j] = (j == k ? 1.0f : src[j]) / pv;
     if (t < nr) {
       const int i = r0 + t;
       s_f[t] = (i == p && p != k) ? old[k] : own[(size_t)t * na + k];
     }
     __syncthreads();
-    for (int e = t; e < nr * na; e += blockDim.x) {
-      const int ii = e / na, j = e - ii * na;
-      const int i = r0 + ii;
-      float* Mi = own + (size_t)ii * na;
-      if (i == k) {
-        Mi[j] = prow[j];
-      } else {
-        const float base = (i == p && p != k) ? orow[j] : Mi[j];
-        Mi[j] = (j == k ? 0.0f : base) - s_f[ii] * prow[j];
+    for (int j = tx; j < na; j += CW) {
+      const float pj = prow[j], oj = old[j];
+      const bool jk = j == k;
+      for (int ii = ty; ii < nr; ii += G) {  // the row index is the same across a warp
+        const int i = r0 + ii;
+        float* Mij = own + (size_t)ii * na + j;
+        if (i != k && i != p) {
+          *Mij = (jk ? 0.0f : *Mij) - s_f[ii] * pj;
+        } else if (i == k) {
+          *Mij = pj;
+        } else {  // i == p != k: the old row k moves here
+          *Mij = (jk ? 0.0f : oj) - s_f[ii] * pj;
+        }
       }
     }
     __syncthreads();
@@ -1254,7 +1261,7 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
     cluster.sync();  // publications visible; every block is done reading this step's
   }
   // undo the column swaps (k_gj_unswap) on the own rows, write them out
-  for (int q = t; q < nr; q += blockDim.x) {
+  for (int q = t; q < nr; q += NT) {
     float* row = own + (size_t)q * na;
     for (int k = na - 1; k >= 0; --k) {
       const int pk = perm_s[k];
@@ -1266,7 +1273,7 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
     }
   }
   __syncthreads();
-  for (int e = t; e < nr * na; e += blockDim.x) out[(size_t)r0 * na + e] = own[e];
+  for (int e = t; e < nr * na; e += NT) out[(size_t)r0 * na + e] = own[e];
   if (t == 0 && s_sing) *flag = 1;
 }
 
@@ -1293,9 +1300,16 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
   for (int i = 0; i < n; ++i)
     for (int b = 0; b < A.mask.nb; ++b)
       if (i >= A.mask.start[b] && i < A.mask.end[b] && i < A.mask.active_end[b]) ++na_;
-  const int R = (na_ + kGjCluster - 1) / kGjCluster;
-  const size_t smem = (size_t(R) + 6) * na_ * sizeof(float) + size_t(na_) * sizeof(int);
-  if (na_ == 0 || R > 128 || smem > kGjClusterSmem) {
+  // one block when the whole active block fits its shared memory, else a
+  // cluster of kGjCluster blocks
+  auto smem_for = [&](int R) { return (size_t(R) + 5) * na_ * sizeof(float) + size_t(na_) * sizeof(int); };
+  int cs = std::max(1, std::min(kGjCluster, c->coarse_cluster)), R = (na_ + cs - 1) / cs;
+  while (cs < kGjCluster && smem_for(R) > kGjClusterSmem) {
+    cs *= 2;
+    R = (na_ + cs - 1) / cs;
+  }
+  const size_t smem = smem_for(R);
+  if (na_ == 0 || R > 256 || smem > kGjClusterSmem) {
     build(c, A);  // large: the FP64 inverse, rounded
     inv32.ensure(size_t(na) * na);
     if (na) {
@@ -1311,12 +1325,31 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(k_gj_cluster32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    attr_err = cudaFuncSetAttribute(k_gj_cluster32<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(kGjClusterSmem));
+    if (attr_err == cudaSuccess)
+      attr_err = cudaFuncSetAttribute(k_gj_cluster32<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(kGjClusterSmem));
   });
   PM_CUDA(attr_err);
-  k_gj_cluster32<<<kGjCluster, kGjClusterThreads, smem, c->stream>>>(na, R, inv.p, inv32.p, flag.p);
-  PM_CHECK_LAUNCH();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(cs));
+  cfg.blockDim = dim3(cs <= 2 ? 1024u : 512u);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = unsigned(cs);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const double* Mp = inv.p;
+  float* outp = inv32.p;
+  int* fl = flag.p;
+  int na_arg = na, R_arg = R;
+  if (cs <= 2) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<1024>, na_arg, R_arg, Mp, outp, fl));
+  else PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<512>, na_arg, R_arg, Mp, outp, fl));
   c->kernel_launches++;
   int h_flag = 0;
   PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));

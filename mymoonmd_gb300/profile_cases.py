@@ -3,6 +3,10 @@
     python -m mymoonmd_gb300.profile_cases request [--precision mixed|fp64]
         one warm-up request, then one request (assembly + solve) of the 3D Q2
         32^3 convection-diffusion workload (274,625 DOFs, 4 levels)
+    python -m mymoonmd_gb300.profile_cases request2d [--precision mixed|fp64] [--cluster 1|2|4|8]
+        the same for the 2D Q1 128^2 workload (16,641 DOFs, 4 levels), with the
+        host wall time of each request; --cluster: thread blocks of the FP32
+        coarse Gauss-Jordan (request3d_cluster: the 3D workload the same way)
     python -m mymoonmd_gb300.profile_cases spmv
         the finest 32^3 Q2 matrix: two FP64 and two FP32 SpMV launches
     python -m mymoonmd_gb300.profile_cases sliced
@@ -54,11 +58,24 @@ def problem(ctx, precision="mixed", n_levels=4):
     return disc, m.ConvectionDiffusion(ctx, disc, cf, _db(precision), quad_points=3)
 
 
+def problem2d(ctx, precision="mixed"):
+    """the 2D Q1 128^2 convection-diffusion workload (16,641 DOFs, 4 levels,
+    FGMRES(20), to 1e-10)"""
+    disc = m.Discretization(m.GEO_SQUARE_QUAD, 1, 7, 4, m.KIND_CD, 1)
+    cf = m.cd_coeffs(0.1, (1.0, 0.0, 0.0), 0.0, True)
+    db = _db(precision)
+    db["gmres_restart"] = 20
+    db["residual_reduction"] = 1e-10
+    return disc, m.ConvectionDiffusion(ctx, disc, cf, db, quad_points=3)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["request", "spmv", "assembly", "stokes", "sliced"])
+    ap.add_argument("case", choices=["request", "request2d", "request3d_cluster", "spmv", "assembly", "stokes",
+                                     "sliced"])
     ap.add_argument("--shapes", default="0,140,141,180,240,241,280,440,441,480,481,840,841,881")
     ap.add_argument("--pdl", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--cluster", type=int, default=8, choices=[1, 2, 4, 8])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
     ap.add_argument("--coarse", default="nodal_vanka_jacobi")
@@ -81,6 +98,21 @@ def main() -> None:
             prob.assemble()
             prob.solve()
         print("stokes", args.precision, args.smoother, args.coarse, "iterations", prob.last_info()[0])
+        prob.close()
+        ctx.close()
+        return
+    if args.case in ("request2d", "request3d_cluster"):
+        import time
+        ctx.set_option("coarse_cluster", args.cluster)
+        disc, prob = problem2d(ctx, args.precision) if args.case == "request2d" else problem(ctx, args.precision)
+        for _ in range(3):
+            t0 = time.perf_counter()
+            prob.reset_solution()
+            prob.assemble()
+            prob.solve()
+            ctx.synchronize()
+            print(f"{args.case} {args.precision} cluster {args.cluster}: {(time.perf_counter() - t0) * 1e3:.3f} ms, "
+                  f"{prob.last_info()[0]} iterations", flush=True)
         prob.close()
         ctx.close()
         return
