@@ -1354,7 +1354,18 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
   int h_flag = 0;
   PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   PM_CUDA(cudaStreamSynchronize(c->stream));
-  if (h_flag) throw Error(PM_E_BREAKDOWN, "coarse matrix is singular (zero pivot)");
+  if (h_flag) {
+    // no FP32 pivot (a singular matrix, or values outside the FP32 range): the
+    // FP64 inverse decides (and throws if the matrix is singular), rounded
+    build(c, A);
+    if (na) {
+      k_d2f<<<grid_for(c, (long long)na * na), 256, 0, c->stream>>>((long long)na * na, inv.p, inv32.p);
+      PM_CHECK_LAUNCH();
+      c->kernel_launches++;
+    }
+    has32 = true;
+    return;
+  }
   has64 = false;  // inv holds the active block, not its inverse
   has32 = true;
 }

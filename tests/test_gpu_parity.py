@@ -392,31 +392,51 @@ def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
     assert np.array_equal(out[0][1], out[1][1])
 
 
-FALLBACK_CASES = [(3, 16, 2, 1e-2, (0.8, 0.6, 0.0)), (2, 64, 2, 5e-3, (0.8, 0.0)), (3, 24, 1, 3e-3, (0.0, 0.6, 0.8)),
-                  (2, 128, 1, 4e-3, (0.48, -0.64)), (3, 16, 2, 2e-3, (0.5, 0.5, 0.5))]
-
-
-@pytest.mark.parametrize("dim,cells,elem,eps,b", FALLBACK_CASES)
-def test_mixed_form_with_fallback_converges_where_fp64_does(ctx, dim, cells, elem, eps, b):
-    """convection-dominated requests of the batched stream's kind: the FP32
-    multigrid may stall; the mixed form then switches the multigrid to FP64
-    (gpu_mixed_fallback, on by default) and must still reach the 1e-8 FP64
-    residual wherever the FP64 form does, with the same solution"""
+def _cd_case(dim, cells, elem, eps, b):
     from mymoonmd_gb300 import workloads as wl
     rq = wl.cd_request(dim, cells, elem, eps, b)
     disc = m.Discretization(rq["geometry"], rq["root_n"], rq["n_refine"], rq["n_levels"], m.KIND_CD, elem)
-    cf = m.cd_coeffs(eps, rq["b"], 0.0, True)
-    out = {}
-    for precision in ("fp64", "mixed"):
-        db = mg_db(rq["n_levels"], restart=30, reduction=1e-8, precision=precision)
-        db["max_n_iterations"] = 300
-        prob = m.ConvectionDiffusion(ctx, disc, cf, db)
-        prob.assemble()
-        prob.solve()
-        out[precision] = (prob.solution(), *prob.last_info())
-    sol64, it64, res64, init64 = out["fp64"]
-    if not res64 <= 1e-8 * init64:
-        pytest.skip("the FP64 form does not converge on this case either")
-    solm, itm, resm, initm = out["mixed"]
-    assert resm <= 1e-8 * initm, (itm, it64)
+    return rq, disc, m.cd_coeffs(eps, rq["b"], 0.0, True)
+
+
+def _solve(ctx, disc, cf, n_levels, precision, fallback=1):
+    db = mg_db(n_levels, restart=30, reduction=1e-8, precision=precision)
+    db["max_n_iterations"] = 100
+    db["gpu_mixed_fallback"] = fallback
+    prob = m.ConvectionDiffusion(ctx, disc, cf, db)
+    prob.assemble()
+    prob.solve()
+    out = (prob.solution(), *prob.last_info(), prob.solver().residual_history())
+    prob.close()
+    return out
+
+
+def test_mixed_form_switches_to_fp64_when_the_residual_stalls(ctx):
+    """a slowly converging request of the batched stream (3D Q1 16^3, eps 5.2e-3):
+    its residual is not halved within 10 iterations, so the mixed form switches
+    the multigrid to FP64 (gpu_mixed_fallback) and goes on from the current
+    Krylov basis; it reaches the 1e-8 FP64 residual like the FP64 form, and its
+    residual history leaves the one without the switch"""
+    rq, disc, cf = _cd_case(3, 16, 1, 5.21e-3, (-0.06, -0.13, 0.21))
+    sol64, it64, res64, init64, _ = _solve(ctx, disc, cf, rq["n_levels"], "fp64")
+    solm, itm, resm, initm, histm = _solve(ctx, disc, cf, rq["n_levels"], "mixed")
+    soln, itn, resn, initn, histn = _solve(ctx, disc, cf, rq["n_levels"], "mixed", fallback=0)
+    assert res64 <= 1e-8 * init64 and resm <= 1e-8 * initm
+    assert abs(itm - it64) <= 2, (itm, it64)
+    k = min(histm.size, histn.size)
+    assert histm.size != histn.size or not np.array_equal(histm[:k], histn[:k])
     assert rel(solm, sol64) <= 1e-6
+
+
+def test_mixed_form_restarts_in_fp64_after_an_fp32_overflow(ctx):
+    """diffusion 1e40 (2D Q1 32^2): the FP64 system is fine, its FP32 copy
+    overflows, so the first FP32 cycle gives a non-finite residual; the mixed
+    form discards that Krylov cycle and restarts from the same iterate with the
+    FP64 multigrid (the FP64 coarse inverse is made then): the FP64 form's
+    iterates, one iteration later"""
+    rq, disc, cf = _cd_case(2, 32, 1, 1e40, (1.0, 0.0))
+    sol64, it64, res64, init64, _ = _solve(ctx, disc, cf, rq["n_levels"], "fp64")
+    solm, itm, resm, initm, _ = _solve(ctx, disc, cf, rq["n_levels"], "mixed")
+    assert res64 <= 1e-8 * init64 and resm <= 1e-8 * initm
+    assert itm == it64 + 1
+    assert rel(solm, sol64) <= 1e-12
