@@ -176,6 +176,7 @@ def large_spmv(ctx, m, np, hbm_peak):
     prob.assemble()
     A = prob.matrix(-1)
     A.make_fp32()
+    A.make_sliced64()
     n = A.n_rows
     x, y = m.DeviceVector(ctx, n), m.DeviceVector(ctx, n)
     x32, y32 = m.DeviceVector(ctx, n, np.float32), m.DeviceVector(ctx, n, np.float32)

@@ -135,6 +135,11 @@ int pm_matrix_get_diagonal(pm_matrix* A, double* diag_dev);
 /* FP32 copy of the values for the mixed-precision preconditioner, and its SpMV
  * y = A32*x (FP32 values, vectors and accumulation). */
 int pm_matrix_make_fp32(pm_matrix* A);
+/* Sliced-ELL copy of the FP64 values for the context's "fp64_sliced_spmv"
+ * shape (no reference counterpart): FP64 SpMV-family launches on A use it from
+ * then on; writers of the values keep it current. Solvers make it in their
+ * update. */
+int pm_matrix_make_sliced64(pm_matrix* A);
 int pm_matrix_apply_f32(pm_matrix* A, const float* x_dev, float* y_dev);
 /* Launch shape of the CSR kernels of this matrix (no reference counterpart;
  * tuning only): lanes per row (1, 2, 4, 8, 16, 32) and entries per lane per chunk

@@ -98,6 +98,7 @@ _SIGS = {
     "pm_matrix_apply": (i32, [vp, vp, vp]),
     "pm_matrix_get_diagonal": (i32, [vp, vp]),
     "pm_matrix_make_fp32": (i32, [vp]),
+    "pm_matrix_make_sliced64": (i32, [vp]),
     "pm_matrix_apply_f32": (i32, [vp, vp, vp]),
     "pm_matrix_set_kernel": (i32, [vp, i32, i32]),
     "pm_matrix_bench_apply": (i32, [vp, i32, vp, vp, i32, C.POINTER(C.c_float), pf64]),

@@ -236,6 +236,9 @@ class FEMatrix:
     def make_fp32(self) -> None:
         check(lib.pm_matrix_make_fp32(self.handle), self.ctx.handle)
 
+    def make_sliced64(self) -> None:
+        check(lib.pm_matrix_make_sliced64(self.handle), self.ctx.handle)
+
     def apply_f32(self, x: DeviceVector, y: DeviceVector) -> None:
         check(lib.pm_matrix_apply_f32(self.handle, x.ptr, y.ptr), self.ctx.handle)
 

@@ -331,6 +331,14 @@ int pm_matrix_make_fp32(pm_matrix* A) {
   PM_CATCH(A->ctx)
 }
 
+int pm_matrix_make_sliced64(pm_matrix* A) {
+  if (!A) return PM_E_INVALID;
+  PM_TRY
+  A->csr.make_sliced64(A->ctx);
+  return PM_OK;
+  PM_CATCH(A->ctx)
+}
+
 int pm_matrix_apply_f32(pm_matrix* A, const float* x, float* y) {
   if (!A || !x || !y) return PM_E_INVALID;
   PM_TRY

@@ -168,6 +168,7 @@ def main() -> None:
         prob.assemble()
         A = prob.matrix(-1)
         A.make_fp32()
+        A.make_sliced64()
         n = A.n_rows
         x = m.DeviceVector.from_numpy(ctx, np.random.default_rng(0).standard_normal(n))
         y = m.DeviceVector(ctx, n)
