@@ -567,66 +567,110 @@ __global__ void __launch_bounds__(256) k_cgs_update(int n, int nk, double* __res
 constexpr int kCgsFused = 32;
 constexpr int kCgsChunk = 8;
 
-template <int CH>
-__device__ __forceinline__ void block_partials_multi(double (&acc)[CH], double* red, double* __restrict__ part,
-                                                     int k0, int nk) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+// Reduce-scatter of W accumulators over the lanes of a warp by recursive
+// halving (W = 32: offsets 16..1, afterwards lane l holds the warp's sum of
+// accumulator l); W - 1 FP64 additions per lane instead of 5 W for a
+// butterfly on every accumulator, which on GB300's FP64 pipe cost as much as
+// the projections themselves
+template <int W>
+__device__ __forceinline__ double warp_halving(double (&a)[W], int lane) {
 #pragma unroll
-  for (int u = 0; u < CH; ++u) {
-    double v = acc[u];
+  for (int o = W / 2; o >= 1; o >>= 1) {
+    const bool hi = (lane & o) != 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp * CH + u] = v;
+    for (int j = 0; j < o; ++j) {
+      const double keep = hi ? a[o + j] : a[j];
+      const double send = hi ? a[j] : a[o + j];
+      a[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
   }
+  return a[0];
+}
+
+// the block's partial sums of NK accumulators (NK = 16 or 32) into
+// part[k * kRedBlocks + block], k < nk
+template <int NK>
+__device__ __forceinline__ void block_partials_multi(double (&acc)[NK], double* red, double* __restrict__ part,
+                                                     int nk) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if constexpr (NK == 16) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], 16);
+  }
+  const double v = warp_halving<NK>(acc, lane);  // lane l (mod NK): accumulator l
+  if (lane < NK) red[warp * NK + lane] = v;
   __syncthreads();
   const int k = threadIdx.x;
-  if (k < CH && k0 + k < nk) {
+  if (k < NK && k < nk) {
     double sum = 0.0;
-    for (int w = 0; w < nw; ++w) sum += red[w * CH + k];
-    part[(size_t)(k0 + k) * kRedBlocks + blockIdx.x] = sum;
+    for (int w = 0; w < nw; ++w) sum += red[w * NK + k];
+    part[(size_t)k * kRedBlocks + blockIdx.x] = sum;
   }
   __syncthreads();
 }
 
-// partials of <r, V_k>, k < nk, CH projections per sweep
-template <int CH>
-__global__ void __launch_bounds__(256, 2) k_mdot(int n, int nk, const double* __restrict__ r,
-                                              const double* __restrict__ V, size_t ld, double* __restrict__ part) {
-  __shared__ double red[8 * CH];
-  for (int k0 = 0; k0 < nk; k0 += CH) {
-    double acc[CH];
+// Per basis chunk c (8 vectors) f(c, rem) with rem = nk - 8c >= 1: exactly
+// min(8, rem) loads and FMAs; the bodies run full chunks unpredicated and the
+// last partial chunk predicated (uniform tests). The loop is unrolled, so c is
+// a constant in every body and the accumulator indices stay static.
+template <int NK, class F>
+__device__ __forceinline__ void cgs_chunks(int nk, F&& f) {
 #pragma unroll
-    for (int u = 0; u < CH; ++u) acc[u] = 0.0;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
-      const double ri = r[idx];
-      double v[CH];
+  for (int c = 0; c < NK / kCgsChunk; ++c)
+    if (c * kCgsChunk < nk) f(c, nk - c * kCgsChunk);
+}
+
+// acc[8c + u] += ri * V_{8c+u}(idx) for the chunk's vectors
+template <int NK>
+__device__ __forceinline__ void cgs_dot_chunk(double (&acc)[NK], int c, int rem, double ri, int idx,
+                                              const double* __restrict__ V, size_t ld) {
+  if (rem >= kCgsChunk) {
+    double v[kCgsChunk];
 #pragma unroll
-      for (int u = 0; u < CH; ++u) v[u] = k0 + u < nk ? V[(size_t)(k0 + u) * ld + idx] : 0.0;
+    for (int u = 0; u < kCgsChunk; ++u) v[u] = V[(size_t)(c * kCgsChunk + u) * ld + idx];
 #pragma unroll
-      for (int u = 0; u < CH; ++u) acc[u] += ri * v[u];
-    }
-    block_partials_multi<CH>(acc, red, part, k0, nk);
+    for (int u = 0; u < kCgsChunk; ++u) acc[c * kCgsChunk + u] += ri * v[u];
+  } else {
+#pragma unroll
+    for (int u = 0; u < kCgsChunk; ++u)
+      if (u < rem) acc[c * kCgsChunk + u] += ri * V[(size_t)(c * kCgsChunk + u) * ld + idx];
   }
+}
+
+// partials of <r, V_k>, k < nk <= NK, in one sweep
+template <int NK>
+__global__ void __launch_bounds__(256, 2) k_mdot(int n, int nk, const double* __restrict__ r,
+                                                 const double* __restrict__ V, size_t ld, double* __restrict__ part) {
+  __shared__ double red[8 * NK];
+  double acc[NK];
+#pragma unroll
+  for (int u = 0; u < NK; ++u) acc[u] = 0.0;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const double ri = r[idx];
+    cgs_chunks<NK>(nk, [&](int c, int rem) { cgs_dot_chunk<NK>(acc, c, rem, ri, idx, V, ld); });
+  }
+  block_partials_multi<NK>(acc, red, part, nk);
 }
 
 // ri -= sum_k h[k] V_k(idx) in k order (the operations of k_cgs_update)
 template <int NK>
 __device__ __forceinline__ double cgs_update_entry(double ri, int idx, int nk, const double* __restrict__ V,
                                                    size_t ld, const double* hs) {
+  cgs_chunks<NK>(nk, [&](int c, int rem) {
+    double v[kCgsChunk];
+    if (rem >= kCgsChunk) {
 #pragma unroll
-  for (int c = 0; c < NK / kCgsChunk; ++c) {
-    if (c * kCgsChunk < nk) {
-      double v[kCgsChunk];
+      for (int u = 0; u < kCgsChunk; ++u) v[u] = V[(size_t)(c * kCgsChunk + u) * ld + idx];
 #pragma unroll
-      for (int u = 0; u < kCgsChunk; ++u) {
-        const int k = c * kCgsChunk + u;
-        v[u] = k < nk ? V[(size_t)k * ld + idx] : 0.0;
-      }
+      for (int u = 0; u < kCgsChunk; ++u) ri -= hs[c * kCgsChunk + u] * v[u];
+    } else {
+#pragma unroll
+      for (int u = 0; u < kCgsChunk; ++u) v[u] = u < rem ? V[(size_t)(c * kCgsChunk + u) * ld + idx] : 0.0;
 #pragma unroll
       for (int u = 0; u < kCgsChunk; ++u)
-        if (c * kCgsChunk + u < nk) ri -= hs[c * kCgsChunk + u] * v[u];
+        if (u < rem) ri -= hs[c * kCgsChunk + u] * v[u];
     }
-  }
+  });
   return ri;
 }
 
@@ -645,21 +689,9 @@ __global__ void __launch_bounds__(256, 2) k_cgs_update_mdot(int n, int nk, doubl
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const double ri = cgs_update_entry<NK>(r[idx], idx, nk, V, ld, hs);
     r[idx] = ri;
-#pragma unroll
-    for (int c = 0; c < NK / kCgsChunk; ++c) {
-      if (c * kCgsChunk < nk) {
-        double v[kCgsChunk];
-#pragma unroll
-        for (int u = 0; u < kCgsChunk; ++u) {
-          const int k = c * kCgsChunk + u;
-          v[u] = k < nk ? V[(size_t)k * ld + idx] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < kCgsChunk; ++u) acc[c * kCgsChunk + u] += ri * v[u];
-      }
-    }
+    cgs_chunks<NK>(nk, [&](int c, int rem) { cgs_dot_chunk<NK>(acc, c, rem, ri, idx, V, ld); });
   }
-  block_partials_multi<NK>(acc, red, part, 0, nk);
+  block_partials_multi<NK>(acc, red, part, nk);
 }
 
 // r -= sum_k h[k] V_k, then the block's partial sum of |r_new|^2
@@ -935,7 +967,8 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
           // two classical Gram-Schmidt passes in three sweeps over the basis;
           // H(:,i) = h1 + h2, |r|^2 partials into partA
           const int nk = i + 1;
-          k_mdot<16><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
+          if (nk <= 16) k_mdot<16><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
+          else k_mdot<kCgsFused><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
           k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i, nullptr);
           if (nk <= 16) k_cgs_update_mdot<16><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
           else k_cgs_update_mdot<kCgsFused><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
