@@ -97,6 +97,12 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->coarse_cluster = value;
     return PM_OK;
   }
+  if (std::string(key) == "coarse_threads") {
+    if (value != 0 && value != 256 && value != 512 && value != 1024)
+      return fail(c, PM_E_INVALID, "coarse_threads is 0, 256, 512 or 1024");
+    c->coarse_threads = value;
+    return PM_OK;
+  }
   if (std::string(key) == "jacobi_zero_start") {
     c->jacobi_zero_start = value != 0;
     return PM_OK;

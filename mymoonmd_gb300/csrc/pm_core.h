@@ -126,6 +126,7 @@ struct pm_ctx {
   // thread blocks of the FP32 coarse Gauss-Jordan cluster (option
   // "coarse_cluster": 1, 2, 4 or 8; more when the matrix does not fit)
   int coarse_cluster = 8;
+  int coarse_threads = 0;  // threads per block of it (option "coarse_threads"; 0 = by cluster size)
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)

@@ -1330,11 +1330,16 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
     if (attr_err == cudaSuccess)
       attr_err = cudaFuncSetAttribute(k_gj_cluster32<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       int(kGjClusterSmem));
+    if (attr_err == cudaSuccess)
+      attr_err = cudaFuncSetAttribute(k_gj_cluster32<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(kGjClusterSmem));
   });
   PM_CUDA(attr_err);
+  // measured on GB300 (225 and 343 active rows): 8 blocks of 1024 threads
+  const int nt = c->coarse_threads > 0 ? c->coarse_threads : 1024;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(unsigned(cs));
-  cfg.blockDim = dim3(cs <= 2 ? 1024u : 512u);
+  cfg.blockDim = dim3(unsigned(nt));
   cfg.dynamicSmemBytes = smem;
   cfg.stream = c->stream;
   cudaLaunchAttribute attr[1];
@@ -1348,8 +1353,9 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
   float* outp = inv32.p;
   int* fl = flag.p;
   int na_arg = na, R_arg = R;
-  if (cs <= 2) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<1024>, na_arg, R_arg, Mp, outp, fl));
-  else PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<512>, na_arg, R_arg, Mp, outp, fl));
+  if (nt == 1024) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<1024>, na_arg, R_arg, Mp, outp, fl));
+  else if (nt == 512) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<512>, na_arg, R_arg, Mp, outp, fl));
+  else PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<256>, na_arg, R_arg, Mp, outp, fl));
   c->kernel_launches++;
   int h_flag = 0;
   PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));

@@ -76,6 +76,7 @@ def main() -> None:
     ap.add_argument("--shapes", default="0,140,141,180,240,241,280,440,441,480,481,840,841,881")
     ap.add_argument("--pdl", type=int, default=1, choices=[0, 1])
     ap.add_argument("--cluster", type=int, default=8, choices=[1, 2, 4, 8])
+    ap.add_argument("--threads", type=int, default=0, choices=[0, 256, 512, 1024])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
     ap.add_argument("--coarse", default="nodal_vanka_jacobi")
@@ -104,6 +105,7 @@ def main() -> None:
     if args.case in ("request2d", "request3d_cluster"):
         import time
         ctx.set_option("coarse_cluster", args.cluster)
+        ctx.set_option("coarse_threads", args.threads)
         disc, prob = problem2d(ctx, args.precision) if args.case == "request2d" else problem(ctx, args.precision)
         for _ in range(3):
             t0 = time.perf_counter()
@@ -111,7 +113,8 @@ def main() -> None:
             prob.assemble()
             prob.solve()
             ctx.synchronize()
-            print(f"{args.case} {args.precision} cluster {args.cluster}: {(time.perf_counter() - t0) * 1e3:.3f} ms, "
+            print(f"{args.case} {args.precision} cluster {args.cluster} threads {args.threads}: "
+                  f"{(time.perf_counter() - t0) * 1e3:.3f} ms, "
                   f"{prob.last_info()[0]} iterations", flush=True)
         prob.close()
         ctx.close()
