@@ -97,6 +97,11 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->coarse_cluster = value;
     return PM_OK;
   }
+  if (std::string(key) == "sliced_min_entries") {
+    if (value < 0) return fail(c, PM_E_INVALID, "sliced_min_entries is >= 0");
+    c->sell_min_avg = value;
+    return PM_OK;
+  }
   if (std::string(key) == "coarse_threads") {
     if (value != 0 && value != 256 && value != 512 && value != 1024)
       return fail(c, PM_E_INVALID, "coarse_threads is 0, 256, 512 or 1024");
@@ -873,6 +878,8 @@ int pm_problem_assemble(pm_problem* p) {
     double* r = (l == nl - 1) ? p->rhs.p : p->rhs_coarse.p;
     assemble_cd_level(c, p->alev[l], D.dim(), D.elem, p->qn, p->coeffs, p->ref, p->mats[l]->csr, r,
                       p->K.p, p->F.p);
+    // the coarse factorisation overlaps the assembly of the finer levels
+    if (l == 0 && nl > 1 && p->solver->use_mg) p->solver->mg.start_coarse(c);
   }
   // copy_nonactive(rhs -> solution) (ConvectionDiffusion.C:343)
   const DevCsr& top = p->mats.back()->csr;

@@ -91,6 +91,10 @@ struct DBuf {
 struct pm_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // second stream for work that overlaps the main stream (the coarse-grid
+  // factorisation during the assembly of the finer levels)
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_event = nullptr;
   int num_sms = 0;
   std::string last_error;
   int verbosity = 1;
@@ -118,6 +122,9 @@ struct pm_ctx {
   // FP64 SpMV-family launches by the sliced-ELL kernel (same encoding; the
   // layout's lanes must equal those of the FP32 shape when both are used)
   int sell_shape64 = 441;
+  // matrices with more entries per row than this on average get sliced copies
+  // (option "sliced_min_entries")
+  int sell_min_avg = 16;
   // sliced-ELL launches with programmatic stream serialization (option "pdl")
   bool pdl = true;
   // first Jacobi sweep from an exactly zero iterate as a diagonal scaling

@@ -15,6 +15,8 @@ void ctx_init(pm_ctx* c, int device) {
   c->device = device;
   PM_CUDA(cudaSetDevice(device));
   PM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  PM_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  PM_CUDA(cudaEventCreateWithFlags(&c->side_event, cudaEventDisableTiming));
   PM_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
   PM_CUDA(cudaMallocHost(&c->host_scalars, 64 * sizeof(double)));
   c->dev_scalars.alloc(256);
@@ -41,6 +43,11 @@ void ctx_destroy(pm_ctx* c) {
   c->dev_error.release();
   if (c->host_scalars) cudaFreeHost(c->host_scalars);
   c->host_scalars = nullptr;
+  if (c->side) cudaStreamSynchronize(c->side);
+  if (c->side_event) cudaEventDestroy(c->side_event);
+  if (c->side) cudaStreamDestroy(c->side);
+  c->side_event = nullptr;
+  c->side = nullptr;
   if (c->stream) cudaStreamDestroy(c->stream);
   c->stream = nullptr;
 }
@@ -289,7 +296,7 @@ void DevCsr::values_changed(pm_ctx* c) {
 
 void DevCsr::make_sliced64(pm_ctx* c) {
   const int want = c->sell_shape64 / 100;
-  if (want <= 0 || nnz <= 16 * int64_t(n_rows)) return;
+  if (want <= 0 || nnz <= c->sell_min_avg * int64_t(n_rows)) return;
   if (sell_lanes == 0) build_sell(c, want);
   if (sell_lanes != want || !sell_entries) return;
   if (!sell_vals64.p) sell_vals64.ensure(size_t(sell_entries));
@@ -297,10 +304,10 @@ void DevCsr::make_sliced64(pm_ctx* c) {
 }
 
 void DevCsr::make_fp32(pm_ctx* c) {
-  // the sliced copy: rows of more than 16 entries on average (the operators
-  // whose FP32 SpMV streams many bytes per row); laid out once per lane count
+  // the sliced copy: matrices with more than sell_min_avg entries per row on
+  // average; laid out once per lane count
   const int want = c->sell_shape / 100;
-  if (want > 0 && want != sell_lanes && nnz > 16 * int64_t(n_rows)) build_sell(c, want);
+  if (want > 0 && want != sell_lanes && nnz > c->sell_min_avg * int64_t(n_rows)) build_sell(c, want);
   if (sell_lanes && sell_entries) {
     k_sell_fill<float><<<grid_for(c, sell_entries), 256, 0, c->stream>>>(sell_entries, sell_src.p, vals.p,
                                                                        sell_vals.p);
@@ -1295,6 +1302,12 @@ __global__ void k_coarse_gemv32(int n, int na, const int* __restrict__ act, cons
 }
 
 void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
+  launch32(c, A, c->stream);
+  complete32(c, A);
+}
+
+void DenseInverse::launch32(pm_ctx* c, const DevCsr& A, cudaStream_t s) {
+  pending32 = false;
   n = A.n_rows;
   int na_ = 0;
   for (int i = 0; i < n; ++i)
@@ -1320,6 +1333,13 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
     has32 = true;
     return;
   }
+  // the preparation and the kernel on stream s (restored on every exit)
+  struct StreamSwap {
+    pm_ctx* c;
+    cudaStream_t saved;
+    StreamSwap(pm_ctx* c_, cudaStream_t s_) : c(c_), saved(c_->stream) { c->stream = s_; }
+    ~StreamSwap() { c->stream = saved; }
+  } swap(c, s);
   prepare(c, A);  // act, pos, the dense active block in inv (FP64)
   inv32.ensure(size_t(na) * na);
   static std::once_flag once;
@@ -1341,7 +1361,7 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
   cfg.gridDim = dim3(unsigned(cs));
   cfg.blockDim = dim3(unsigned(nt));
   cfg.dynamicSmemBytes = smem;
-  cfg.stream = c->stream;
+  cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = unsigned(cs);
@@ -1357,11 +1377,20 @@ void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
   else if (nt == 512) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<512>, na_arg, R_arg, Mp, outp, fl));
   else PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<256>, na_arg, R_arg, Mp, outp, fl));
   c->kernel_launches++;
+  if (!done_event) PM_CUDA(cudaEventCreateWithFlags(&done_event, cudaEventDisableTiming));
+  PM_CUDA(cudaEventRecord(done_event, s));
+  pending32 = true;
+}
+
+void DenseInverse::complete32(pm_ctx* c, const DevCsr& A) {
+  if (!pending32) return;  // done at launch (large matrices) or nothing queued
+  pending32 = false;
   int h_flag = 0;
+  PM_CUDA(cudaStreamWaitEvent(c->stream, done_event, 0));
   PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   PM_CUDA(cudaStreamSynchronize(c->stream));
   if (h_flag) {
-    // no FP32 pivot (a singular matrix, or values outside the FP32 range): the
+    // no FP32 pivot (a singular matrix, or values beyond the FP32 range): the
     // FP64 inverse decides (and throws if the matrix is singular), rounded
     build(c, A);
     if (na) {

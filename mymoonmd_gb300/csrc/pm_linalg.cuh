@@ -138,6 +138,14 @@ struct DenseInverse {
   // the active block fits its distributed shared memory, else the FP64
   // inverse rounded to FP32
   void build32(pm_ctx* c, const DevCsr& A);
+  // build32 in two halves: launch32 queues the factorisation on the stream s
+  // (no host synchronisation; the large-matrix path runs build() at once),
+  // complete32 waits for it, checks the pivot flag and falls back to the FP64
+  // inverse if needed
+  void launch32(pm_ctx* c, const DevCsr& A, cudaStream_t s);
+  void complete32(pm_ctx* c, const DevCsr& A);
+  bool pending32 = false;   // launch32 queued, complete32 not yet run
+  cudaEvent_t done_event = nullptr;  // recorded after the queued factorisation
   // x_a = inv32 b_a, x_n = b_n for a right-hand side with zero non-actives
   void solve32(pm_ctx* c, const float* b, float* x);
   // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active);

@@ -130,6 +130,15 @@ void Multigrid::set_mixed(pm_ctx* c, bool on) {
   mixed = on;
 }
 
+void Multigrid::start_coarse(pm_ctx* c) {
+  if (levels.size() < 2 || !levels[0].A || levels[0].proj) return;
+  if (!mixed_cfg || smoother_coarse != SM_DIRECT) return;
+  // the side stream starts after the assembly queued so far on the main one
+  PM_CUDA(cudaEventRecord(c->side_event, c->stream));
+  PM_CUDA(cudaStreamWaitEvent(c->side, c->side_event, 0));
+  levels[0].coarse.launch32(c, levels[0].A->csr, c->side);
+}
+
 void Multigrid::update(pm_ctx* c) {
   mixed = mixed_cfg;
   fp64_smoothers = !mixed;
@@ -186,7 +195,8 @@ void Multigrid::update(pm_ctx* c) {
       // DirectSolver factorises get_combined_matrix (with the pressure projection);
       // the mixed cycle solves with an FP32 inverse (the FP64 one is made on a
       // fallback to FP64)
-      if (mixed) lv.coarse.build32(c, lv.proj ? lv.proj->csr : A);
+      if (mixed && lv.coarse.pending32) lv.coarse.complete32(c, A);  // queued by start_coarse
+      else if (mixed) lv.coarse.build32(c, lv.proj ? lv.proj->csr : A);
       else lv.coarse.build(c, lv.proj ? lv.proj->csr : A);
       if (mixed) {
         lv.coarse_rhs64.ensure(n);
@@ -331,6 +341,9 @@ void Multigrid::prolongate_from(pm_ctx* c, int l) {
 
 void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol, bool rhs_nonactive_zero) {
   if (!ready) throw Error(PM_E_INVALID, "multigrid used before update()");
+  // a factorisation queued by a new assembly (a caller applying the cycle
+  // without the update that follows an assembly): wait for it
+  if (levels[0].coarse.pending32) levels[0].coarse.complete32(c, levels[0].A->csr);
   const int L = int(levels.size());
   const int finest = L - 1;
   MGLevel& top = levels[finest];

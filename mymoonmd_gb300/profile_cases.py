@@ -77,6 +77,7 @@ def main() -> None:
     ap.add_argument("--pdl", type=int, default=1, choices=[0, 1])
     ap.add_argument("--cluster", type=int, default=8, choices=[1, 2, 4, 8])
     ap.add_argument("--threads", type=int, default=0, choices=[0, 256, 512, 1024])
+    ap.add_argument("--min-entries", type=int, default=16, help="sliced_min_entries option")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
     ap.add_argument("--coarse", default="nodal_vanka_jacobi")
@@ -84,6 +85,7 @@ def main() -> None:
     args = ap.parse_args()
     ctx = m.Context(0)
     ctx.set_option("pdl", args.pdl)
+    ctx.set_option("sliced_min_entries", args.min_entries)
     if args.case == "stokes":
         db = _db(args.precision)
         db["multigrid_n_levels"] = 3
