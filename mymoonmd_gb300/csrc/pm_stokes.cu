@@ -680,8 +680,12 @@ static __device__ __forceinline__ int find_sorted(const int* a, int n, int key) 
 
 // one block per pressure DOF: the velocity block of the patch from the
 // projected matrix (non-zero entries only, as the reference copies them),
-// inverted by Gauss-Jordan with partial pivoting in shared memory; then
-// t_k = A^{-1} bt_k and the Schur complement S
+// inverted in place by Gauss-Jordan in shared memory; then t_k = A^{-1} bt_k
+// and the Schur complement S. No pivoting: the block is the velocity
+// stiffness of the patch nodes (symmetric positive definite on the active
+// nodes) with unit rows for Dirichlet nodes, so every leading block is
+// nonsingular; a zero pivot still raises the flag. The reference's LAPACK LU
+// pivots; the two inverses agree to rounding.
 template <class T>
 __global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int* __restrict__ vptr,
                                                       const int* __restrict__ vidx,
@@ -707,16 +711,12 @@ __global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int*
   __shared__ T cdiag;
   const int t = threadIdx.x;
   for (int a = t; a < m; a += blockDim.x) nodes[a] = vidx[vptr[i] + a];
-  for (int e = t; e < m * ld; e += blockDim.x) {
-    M[e] = T(0);
-    Inv[e] = T(0);
-  }
+  for (int e = t; e < m * ld; e += blockDim.x) M[e] = T(0);
   for (int e = t; e < 6 * m; e += blockDim.x) bt[e] = T(0);
   if (t == 0) cdiag = T(0);
   __syncthreads();
   const int prow = 3 * nu + i;
   for (int a = t; a < m; a += blockDim.x) {
-    Inv[a * ld + a] = T(1);
     const int r = nodes[a];
     for (int k = rp[r]; k < rp[r + 1]; ++k) {
       const T val = v[k];
@@ -747,47 +747,29 @@ __global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int*
     }
   }
   __syncthreads();
+  T* pr = Inv;  // the scaled pivot row of the step
+  const int lane = t & 31, wid = t >> 5, nw = int(blockDim.x >> 5);
   for (int k = 0; k < m; ++k) {
-    if (t == 0) {
-      int p = k;
-      T best = fabs(M[k * ld + k]);
-      for (int r = k + 1; r < m; ++r)
-        if (fabs(M[r * ld + k]) > best) {
-          best = fabs(M[r * ld + k]);
-          p = r;
-        }
-      piv_row = p;
-      if (!(best > T(0))) atomicExch(flag, 1);
-    }
-    __syncthreads();
-    const int p = piv_row;
-    if (p != k)
-      for (int j = t; j < m; j += blockDim.x) {
-        T x0 = M[k * ld + j];
-        M[k * ld + j] = M[p * ld + j];
-        M[p * ld + j] = x0;
-        T x1 = Inv[k * ld + j];
-        Inv[k * ld + j] = Inv[p * ld + j];
-        Inv[p * ld + j] = x1;
-      }
-    __syncthreads();
-    const T pv = M[k * ld + k] != T(0) ? M[k * ld + k] : T(1);
+    const T pv = M[k * ld + k];
+    if (t == 0 && !(pv != T(0))) atomicExch(flag, 1);
+    const T piv = pv != T(0) ? pv : T(1);
+    for (int j = t; j < m; j += blockDim.x) pr[j] = (j == k ? T(1) : M[k * ld + j]) / piv;
     for (int r = t; r < m; r += blockDim.x) colk[r] = M[r * ld + k];
     __syncthreads();
-    for (int j = t; j < m; j += blockDim.x) {
-      M[k * ld + j] /= pv;
-      Inv[k * ld + j] /= pv;
-    }
-    __syncthreads();
-    for (int e = t; e < m * m; e += blockDim.x) {
-      const int r = e / m, j = e % m;
-      if (r == k) continue;
+    // warps over rows, lanes over columns: row k becomes the scaled pivot row,
+    // the others lose their column-k multiple of it (column k: -f / pv)
+    for (int r = wid; r < m; r += nw) {
       const T f = colk[r];
-      M[r * ld + j] -= f * M[k * ld + j];
-      Inv[r * ld + j] -= f * Inv[k * ld + j];
+      T* Mr = M + r * ld;
+      if (r == k) {
+        for (int j = lane; j < m; j += 32) Mr[j] = pr[j];
+      } else {
+        for (int j = lane; j < m; j += 32) Mr[j] = (j == k ? T(0) : Mr[j]) - f * pr[j];
+      }
     }
     __syncthreads();
   }
+  Inv = M;  // the inverse, in place
   // t_k = Inv bt_k
   for (int e = t; e < 3 * m; e += blockDim.x) {
     const int comp = e / m, a = e % m;
