@@ -81,9 +81,11 @@ int pm_version(void);
  *   slices of 32/L rows, padded to the slice's longest row) is laid out when
  *   the FP32 values are made (pm_matrix_make_fp32, the multigrid update) for
  *   the shape's L. Shapes with the same L give the same bits;
- *   "pdl" 0|1 - sliced-ELL launches with programmatic stream serialization:
- *   a sweep loads its slice layout and first values while the previous
- *   kernel finishes, and waits for it before reading vectors (default 1);
+ *   "pdl" 0|1|2 - launches with programmatic stream serialization: 1 the
+ *   sliced-ELL sweeps (a sweep loads its slice layout and first values while
+ *   the previous kernel finishes, and waits for it before reading vectors), 2
+ *   also the vector, conversion and Krylov kernels (default 1: on GB300 the
+ *   3D Q2 request took 26.9 ms with 1, 27.6 ms with 0, 28.3 ms with 2);
  *   "fp64_sliced_spmv" 0|441|481|841 - the same for FP64 values (the Krylov
  *   SpMV, the FP64 multigrid); used when its L equals the layout's (default 441);
  *   "jacobi_zero_start" 0|1 - the first damped Jacobi sweep of a multigrid level

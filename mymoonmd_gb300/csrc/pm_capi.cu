@@ -113,7 +113,8 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     return PM_OK;
   }
   if (std::string(key) == "pdl") {
-    c->pdl = value != 0;
+    if (value < 0 || value > 2) return fail(c, PM_E_INVALID, "pdl is 0, 1 or 2");
+    c->pdl = value;
     return PM_OK;
   }
   if (std::string(key) == "probe_epilogue") {

@@ -125,8 +125,9 @@ struct pm_ctx {
   // matrices with more entries per row than this on average get sliced copies
   // (option "sliced_min_entries")
   int sell_min_avg = 16;
-  // sliced-ELL launches with programmatic stream serialization (option "pdl")
-  bool pdl = true;
+  // launches with programmatic stream serialization (option "pdl"): 0 none,
+  // 1 the sliced-ELL sweeps, 2 also the vector, conversion and Krylov kernels
+  int pdl = 1;
   // first Jacobi sweep from an exactly zero iterate as a diagonal scaling
   // (option "jacobi_zero_start"; same bits as the full sweep)
   bool jacobi_zero_start = true;

@@ -257,11 +257,13 @@ void DevCsr::set_blocks(int nb, const int* lengths, const int* actives) {
 }
 
 __global__ void k_d2f(long long n, const double* __restrict__ x, float* __restrict__ y) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] = float(x[i]);
 }
 __global__ void k_f2d(long long n, const float* __restrict__ x, double* __restrict__ y) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] = double(x[i]);
@@ -368,11 +370,12 @@ size_t DevCsr::spmv_bytes(int eb, bool read_y) const {
 template <class TV, class TX, class TA, int G, int EPI>
 static void launch_gu(pm_ctx* c, int U, int grid, int n, const int* rp, const int* ci, const TV* v,
                       const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
+  const dim3 gr(grid), bl(256);
   switch (U) {
-    case 2: csr_kernel<TV, TX, TA, G, 2, EPI><<<grid, 256, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    case 4: csr_kernel<TV, TX, TA, G, 4, EPI><<<grid, 256, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    case 16: csr_kernel<TV, TX, TA, G, 16, EPI><<<grid, 256, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    default: csr_kernel<TV, TX, TA, G, 8, EPI><<<grid, 256, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 2: launch_pdl(c, csr_kernel<TV, TX, TA, G, 2, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 4: launch_pdl(c, csr_kernel<TV, TX, TA, G, 4, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 16: launch_pdl(c, csr_kernel<TV, TX, TA, G, 16, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    default: launch_pdl(c, csr_kernel<TV, TX, TA, G, 8, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
   }
 }
 
@@ -399,8 +402,6 @@ static void launch_epi(pm_ctx* c, int G, int U, int n, const int* rp, const int*
     case 16: launch_gu<TV, TX, TA, 16, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
     default: launch_gu<TV, TX, TA, 32, EPI>(c, U, grid, n, rp, ci, v, x, y, b, d, alpha, mg); break;
   }
-  PM_CHECK_LAUNCH();
-  c->kernel_launches++;
 }
 
 static cudaEvent_t probe_event(pm_ctx* c) {
@@ -477,7 +478,7 @@ static void launch_sell_epi(pm_ctx* c, const DevCsr& A, const T* x, T* y, const 
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = c->pdl ? 1 : 0;
+  cfg.numAttrs = c->pdl >= 1 ? 1 : 0;
   PM_CUDA(cudaLaunchKernelEx(&cfg, sell_kernel<T, L, U, P, EPI>, A.n_slices, (const int*)A.sell_perm.p,
                              (const int*)A.sell_off.p, (const int*)A.sell_cols.p, sell_values<T>(A), x, y, b, d,
                              alpha, m));
@@ -720,49 +721,52 @@ double dot_host(pm_ctx* c, int n, const double* x, const double* y) {
 
 template <class T>
 __global__ void k_copy(long long n, const T* __restrict__ x, T* __restrict__ y) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] = x[i];
 }
 __global__ void k_set(long long n, double* __restrict__ y, double v) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] = v;
 }
 __global__ void k_scale(long long n, double* __restrict__ y, double a) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] *= a;
 }
 __global__ void k_axpy(long long n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] += a * x[i];
 }
 __global__ void k_axpby(long long n, double a, const double* __restrict__ x, double b,
                         double* __restrict__ y) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] = a * x[i] + b * y[i];
 }
 __global__ void k_div(long long n, const double* __restrict__ d, double* __restrict__ y) {
+  pdl_enter();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] /= d[i];
 }
 template <class T>
 __global__ void k_init_sol(int n, BlockMask m, const T* __restrict__ rhs, T* __restrict__ sol) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     sol[i] = row_is_active(m, i) ? T(0) : rhs[i];
 }
 
 #define PM_LAUNCH1D(kern, n, ...)                                                     \
   do {                                                                                \
-    if ((n) > 0) {                                                                    \
-      kern<<<grid_for(c, (n)), 256, 0, c->stream>>>(__VA_ARGS__);                     \
-      PM_CHECK_LAUNCH();                                                              \
-      c->kernel_launches++;                                                           \
-    }                                                                                 \
+    if ((n) > 0) launch_pdl(c, kern, dim3(grid_for(c, (n))), dim3(256), 0, __VA_ARGS__); \
   } while (0)
 
 void vcopy(pm_ctx* c, int n, const double* x, double* y) { PM_LAUNCH1D(k_copy<double>, n, n, x, y); }
@@ -777,6 +781,7 @@ void vdiv(pm_ctx* c, int n, const double* d, double* y) { PM_LAUNCH1D(k_div, n, 
 void vcvt_d2f(pm_ctx* c, int n, const double* x, float* y) { PM_LAUNCH1D(k_d2f, n, n, x, y); }
 void vcvt_f2d(pm_ctx* c, int n, const float* x, double* y) { PM_LAUNCH1D(k_f2d, n, n, x, y); }
 __global__ void k_copy_nonactive(int n, BlockMask m, const double* __restrict__ src, double* __restrict__ dst) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     if (!row_is_active(m, i)) dst[i] = src[i];
 }
@@ -809,6 +814,7 @@ void init_solution32(pm_ctx* c, int n, const BlockMask& m, const float* rhs, flo
 // x + w q with x = +0)
 template <class T>
 __global__ void k_jacobi_zero(int n, const T* __restrict__ b, const T* __restrict__ d, T w, T* __restrict__ x) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     x[i] = fmadd(w, (b[i] - T(0)) / d[i], T(0));
 }
@@ -1287,6 +1293,7 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
 __global__ void k_coarse_gemv32(int n, int na, const int* __restrict__ act, const int* __restrict__ pos,
                                 const float* __restrict__ inv, const float* __restrict__ b,
                                 float* __restrict__ x) {
+  pdl_enter();
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp < na) {
@@ -1408,9 +1415,8 @@ void DenseInverse::complete32(pm_ctx* c, const DevCsr& A) {
 void DenseInverse::solve32(pm_ctx* c, const float* b, float* x) {
   if (!has32) throw Error(PM_E_INVALID, "coarse FP32 inverse used before build32");
   const long long threads = (long long)(na + (n + 31) / 32) * 32;
-  k_coarse_gemv32<<<nblocks(threads, 256), 256, 0, c->stream>>>(n, na, act.p, pos.p, inv32.p, b, x);
-  PM_CHECK_LAUNCH();
-  c->kernel_launches++;
+  launch_pdl(c, k_coarse_gemv32, dim3(nblocks(threads, 256)), dim3(256), 0, n, na, (const int*)act.p,
+             (const int*)pos.p, (const float*)inv32.p, b, x);
 }
 
 void DenseInverse::prepare(pm_ctx* c, const DevCsr& A) {

@@ -7,6 +7,26 @@
 
 namespace pm {
 
+// Launch with programmatic stream serialization (when the context's pdl
+// option is on): the kernel may start while the previous kernel on the stream
+// finishes; it must begin with pdl_enter() (or load only data no earlier
+// kernel writes before pdl_wait()).
+template <class... KArgs, class... Args>
+inline void launch_pdl(pm_ctx* c, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = c->pdl >= 2 ? 1 : 0;
+  PM_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+  c->kernel_launches++;
+}
+
 // device CSR with optional FP32 copy of the values
 struct DevCsr {
   int n_rows = 0, n_cols = 0, n_active = 0;

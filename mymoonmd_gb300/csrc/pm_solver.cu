@@ -395,8 +395,15 @@ void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol, bool rhs_nonact
       defect(c, level);
       MGLevel& crs = levels[level - 1];
       const int nc = crs.A->csr.n_rows;
-      if (mixed) PM_CUDA(cudaMemsetAsync(crs.cur32, 0, sizeof(float) * nc, c->stream));
-      else PM_CUDA(cudaMemsetAsync(crs.cur, 0, sizeof(double) * nc, c->stream));
+      // the coarse iterate starts at zero; the reset is skipped where the
+      // level's first step writes every entry without reading it (a Jacobi
+      // sweep from zero, the direct coarse solve)
+      const bool written = (level - 1 > 0 && crs.smoother == SM_JACOBI && n_pre >= 1 && c->jacobi_zero_start) ||
+                           (level - 1 == 0 && crs.smoother == SM_DIRECT);
+      if (!written) {
+        if (mixed) PM_CUDA(cudaMemsetAsync(crs.cur32, 0, sizeof(float) * nc, c->stream));
+        else PM_CUDA(cudaMemsetAsync(crs.cur, 0, sizeof(double) * nc, c->stream));
+      }
       zero[level - 1] = 1;
       restrict_to(c, level);
       level -= 1;
@@ -467,6 +474,7 @@ __global__ void __launch_bounds__(256) k_fg_normalize(int n, int ldh, int i, con
                                                       double* __restrict__ v,
                                                       const double* __restrict__ part_in,
                                                       double* __restrict__ H, int* __restrict__ flag) {
+  pdl_enter();
   __shared__ double sh[256];
   const double hn = sqrt(sum_partials(part_in, sh));
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -537,6 +545,7 @@ __global__ void __launch_bounds__(256) k_multidot(int n, int nk, const double* _
 __global__ void __launch_bounds__(256) k_reduce_proj(const double* __restrict__ part, double* __restrict__ h,
                                                      const double* __restrict__ hsum, double* __restrict__ H,
                                                      int ldh, int col, const int* __restrict__ guard) {
+  pdl_enter();
   __shared__ double sh[256];
   const int k = blockIdx.x;
   if (guarded(guard)) {  // uniform for the whole grid
@@ -654,6 +663,7 @@ __device__ __forceinline__ void cgs_dot_chunk(double (&acc)[NK], int c, int rem,
 template <int NK>
 __global__ void __launch_bounds__(256, 2) k_mdot(int n, int nk, const double* __restrict__ r,
                                                  const double* __restrict__ V, size_t ld, double* __restrict__ part) {
+  pdl_enter();
   __shared__ double red[8 * NK];
   double acc[NK];
 #pragma unroll
@@ -692,6 +702,7 @@ template <int NK>
 __global__ void __launch_bounds__(256, 2) k_cgs_update_mdot(int n, int nk, double* __restrict__ r,
                                                             const double* __restrict__ V, size_t ld,
                                                             const double* __restrict__ h, double* __restrict__ part) {
+  pdl_enter();
   __shared__ double hs[NK];
   __shared__ double red[8 * NK];
   if (threadIdx.x < NK) hs[threadIdx.x] = int(threadIdx.x) < nk ? h[threadIdx.x] : 0.0;
@@ -711,6 +722,7 @@ __global__ void __launch_bounds__(256, 2) k_cgs_update_mdot(int n, int nk, doubl
 __global__ void __launch_bounds__(256, 2) k_cgs_update_norm(int n, int nk, double* __restrict__ r,
                                                          const double* __restrict__ V, size_t ld,
                                                          const double* __restrict__ h, double* __restrict__ part) {
+  pdl_enter();
   constexpr int NK = kCgsFused;
   __shared__ double hs[NK];
   __shared__ double red[8];
@@ -766,6 +778,7 @@ __device__ void app_rot(double& dx, double& dy, double cs, double sn) {
 
 __global__ void k_fg_givens(int ldh, int i, double* __restrict__ H, double* __restrict__ cs,
                             double* __restrict__ sn, double* __restrict__ s, double* __restrict__ resid) {
+  pdl_enter();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double* col = H + (size_t)ldh * i;
   for (int k = 0; k < i; ++k) app_rot(col[k], col[k + 1], cs[k], sn[k]);
@@ -853,7 +866,7 @@ size_t pm_solver::layout_signature() const {
   mix(ctx->partials.p); mix(ctx->host_scalars);
   h ^= size_t(restart) * 31 + size_t(work_n);
   h = h * 1099511628211ull ^ (size_t(ctx->sell_shape) * 2 + size_t(ctx->bulk_spmv));
-  h = h * 1099511628211ull ^ (size_t(ctx->sell_shape64) * 4 + size_t(ctx->pdl) * 2 + size_t(ctx->jacobi_zero_start));
+  h = h * 1099511628211ull ^ (size_t(ctx->sell_shape64) * 8 + size_t(ctx->pdl) * 2 + size_t(ctx->jacobi_zero_start));
   return h;
 }
 
@@ -980,15 +993,18 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
           // two classical Gram-Schmidt passes in three sweeps over the basis;
           // H(:,i) = h1 + h2, |r|^2 partials into partA
           const int nk = i + 1;
-          if (nk <= 16) k_mdot<16><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
-          else k_mdot<kCgsFused><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part);
-          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i, nullptr);
-          if (nk <= 16) k_cgs_update_mdot<16><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
-          else k_cgs_update_mdot<kCgsFused><<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part);
-          k_reduce_proj<<<nk, 256, 0, c->stream>>>(cgs_part, h2, h1, H, ldh, i, nullptr);
-          k_cgs_update_norm<<<kRedBlocks, 256, 0, c->stream>>>(n, nk, r, V, ld, h2, partA);
-          PM_CHECK_LAUNCH();
-          c->kernel_launches += 5;
+          const dim3 rb(kRedBlocks), t256(256);
+          const double* Vc = V;
+          const double* nul = nullptr;
+          const int* inul = nullptr;
+          if (nk <= 16) launch_pdl(c, k_mdot<16>, rb, t256, 0, n, nk, (const double*)r, Vc, ld, cgs_part);
+          else launch_pdl(c, k_mdot<kCgsFused>, rb, t256, 0, n, nk, (const double*)r, Vc, ld, cgs_part);
+          launch_pdl(c, k_reduce_proj, dim3(nk), t256, 0, (const double*)cgs_part, h1, nul, H, ldh, i, inul);
+          if (nk <= 16) launch_pdl(c, k_cgs_update_mdot<16>, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h1, cgs_part);
+          else launch_pdl(c, k_cgs_update_mdot<kCgsFused>, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h1, cgs_part);
+          launch_pdl(c, k_reduce_proj, dim3(nk), t256, 0, (const double*)cgs_part, h2, (const double*)h1, H, ldh, i,
+                     inul);
+          launch_pdl(c, k_cgs_update_norm, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h2, partA);
         } else if (cgs2) {
           // two passes of classical Gram-Schmidt; H(:,i) = h1 + h2. With the
           // conditional variant the second pass runs only when the first lost
@@ -1023,11 +1039,9 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
             std::swap(pin, pout);
           }
         }
-        k_fg_normalize<<<grid, 256, 0, c->stream>>>(n, ldh, i, r, V + ld * (i + 1), pin, H, flags.p);
-        PM_CHECK_LAUNCH();
-        k_fg_givens<<<1, 32, 0, c->stream>>>(ldh, i, H, cs, sn, s, dres);
-        PM_CHECK_LAUNCH();
-        c->kernel_launches += 2;
+        launch_pdl(c, k_fg_normalize, dim3(grid), dim3(256), 0, n, ldh, i, (const double*)r, V + ld * (i + 1),
+                   (const double*)pin, H, flags.p);
+        launch_pdl(c, k_fg_givens, dim3(1), dim3(32), 0, ldh, i, H, cs, sn, s, dres);
         PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         PM_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(c->host_scalars + 1), flags.p, sizeof(int),
                                 cudaMemcpyDeviceToHost, c->stream));

@@ -53,6 +53,12 @@ __device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
 // has completed and its writes are visible (a no-op without the attribute).
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// the start of a kernel launched by launch_pdl that reads nothing before the
+// previous kernel has completed
+__device__ __forceinline__ void pdl_enter() {
+  pdl_trigger();
+  pdl_wait();
+}
 
 // G lanes per row, U entries per lane per chunk: a lane first issues its U
 // value and U column loads, then its U gathers of x, then the U products, so
@@ -63,7 +69,7 @@ csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ 
            const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
            const TX* __restrict__ b, const TX* __restrict__ diag, const TX* __restrict__ xold,
            TA alpha, BlockMask mask) {
-  pdl_trigger();
+  pdl_enter();
   if (guarded(mask.guard)) {  // uniform for the whole grid
     // a skipped Jacobi sweep leaves the iterate as it is (the caller swaps
     // the two iterate buffers after every sweep)

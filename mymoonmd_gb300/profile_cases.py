@@ -74,7 +74,7 @@ def main() -> None:
     ap.add_argument("case", choices=["request", "request2d", "request3d_cluster", "spmv", "assembly", "stokes",
                                      "sliced"])
     ap.add_argument("--shapes", default="0,140,141,180,240,241,280,440,441,480,481,840,841,881")
-    ap.add_argument("--pdl", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--pdl", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--cluster", type=int, default=8, choices=[1, 2, 4, 8])
     ap.add_argument("--threads", type=int, default=0, choices=[0, 256, 512, 1024])
     ap.add_argument("--min-entries", type=int, default=16, help="sliced_min_entries option")
