@@ -1449,6 +1449,29 @@ void DenseInverse::prepare(pm_ctx* c, const DevCsr& A) {
 }
 
 void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
+  launch64(c, A, c->stream);
+  complete64(c);
+}
+
+void DenseInverse::complete64(pm_ctx* c) {
+  if (!pending64) return;
+  pending64 = false;
+  int h_flag = 0;
+  PM_CUDA(cudaStreamWaitEvent(c->stream, done_event, 0));
+  PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  if (h_flag) throw Error(PM_E_BREAKDOWN, "coarse matrix is singular (zero pivot)");
+  has64 = true;
+}
+
+void DenseInverse::launch64(pm_ctx* c, const DevCsr& A, cudaStream_t s) {
+  pending64 = false;
+  struct StreamSwap {
+    pm_ctx* c;
+    cudaStream_t saved;
+    StreamSwap(pm_ctx* c_, cudaStream_t s_) : c(c_), saved(c_->stream) { c->stream = s_; }
+    ~StreamSwap() { c->stream = saved; }
+  } swap(c, s);
   prepare(c, A);
   if (na == 0) {
     has64 = true;
@@ -1517,11 +1540,9 @@ void DenseInverse::build(pm_ctx* c, const DevCsr& A) {
   k_gj_unswap<<<nblocks(na, 128), 128, 0, c->stream>>>(na, inv.p, perm.p);
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
-  int h_flag = 0;
-  PM_CUDA(cudaMemcpyAsync(&h_flag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  PM_CUDA(cudaStreamSynchronize(c->stream));
-  if (h_flag) throw Error(PM_E_BREAKDOWN, "coarse matrix is singular (zero pivot)");
-  has64 = true;
+  if (!done_event) PM_CUDA(cudaEventCreateWithFlags(&done_event, cudaEventDisableTiming));
+  PM_CUDA(cudaEventRecord(done_event, s));
+  pending64 = true;
 }
 
 // tmp_a = b_a - sum over non-active columns of A_{a,j} b_j

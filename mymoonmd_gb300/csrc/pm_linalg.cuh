@@ -165,6 +165,10 @@ struct DenseInverse {
   void launch32(pm_ctx* c, const DevCsr& A, cudaStream_t s);
   void complete32(pm_ctx* c, const DevCsr& A);
   bool pending32 = false;   // launch32 queued, complete32 not yet run
+  // build in two halves, the same way (FP64 inverse)
+  void launch64(pm_ctx* c, const DevCsr& A, cudaStream_t s);
+  void complete64(pm_ctx* c);
+  bool pending64 = false;
   cudaEvent_t done_event = nullptr;  // recorded after the queued factorisation
   // x_a = inv32 b_a, x_n = b_n for a right-hand side with zero non-actives
   void solve32(pm_ctx* c, const float* b, float* x);

@@ -132,11 +132,12 @@ void Multigrid::set_mixed(pm_ctx* c, bool on) {
 
 void Multigrid::start_coarse(pm_ctx* c) {
   if (levels.size() < 2 || !levels[0].A || levels[0].proj) return;
-  if (!mixed_cfg || smoother_coarse != SM_DIRECT) return;
+  if (smoother_coarse != SM_DIRECT) return;
   // the side stream starts after the assembly queued so far on the main one
   PM_CUDA(cudaEventRecord(c->side_event, c->stream));
   PM_CUDA(cudaStreamWaitEvent(c->side, c->side_event, 0));
-  levels[0].coarse.launch32(c, levels[0].A->csr, c->side);
+  if (mixed_cfg) levels[0].coarse.launch32(c, levels[0].A->csr, c->side);
+  else levels[0].coarse.launch64(c, levels[0].A->csr, c->side);
 }
 
 void Multigrid::update(pm_ctx* c) {
@@ -197,6 +198,7 @@ void Multigrid::update(pm_ctx* c) {
       // fallback to FP64)
       if (mixed && lv.coarse.pending32) lv.coarse.complete32(c, A);  // queued by start_coarse
       else if (mixed) lv.coarse.build32(c, lv.proj ? lv.proj->csr : A);
+      else if (lv.coarse.pending64) lv.coarse.complete64(c);
       else lv.coarse.build(c, lv.proj ? lv.proj->csr : A);
       if (mixed) {
         lv.coarse_rhs64.ensure(n);
@@ -344,6 +346,7 @@ void Multigrid::apply(pm_ctx* c, const double* rhs, double* sol, bool rhs_nonact
   // a factorisation queued by a new assembly (a caller applying the cycle
   // without the update that follows an assembly): wait for it
   if (levels[0].coarse.pending32) levels[0].coarse.complete32(c, levels[0].A->csr);
+  if (levels[0].coarse.pending64) levels[0].coarse.complete64(c);
   const int L = int(levels.size());
   const int finest = L - 1;
   MGLevel& top = levels[finest];

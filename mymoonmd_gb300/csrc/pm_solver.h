@@ -72,9 +72,10 @@ struct Multigrid {
 
   void configure(const Params& p);
   void update(pm_ctx* c);                                  // Multigrid::update
-  // queue the coarse direct solver's FP32 factorisation on the context's side
-  // stream as soon as the coarsest matrix is assembled (the mixed form with a
-  // direct coarse solve on a plain system matrix); update() completes it
+  // queue the coarse direct solver's factorisation (FP32 in the mixed form,
+  // else FP64) on the context's side stream as soon as the coarsest matrix is
+  // assembled (a direct coarse solve on a plain system matrix); update()
+  // completes it
   void start_coarse(pm_ctx* c);
   // Iteration_multigrid::apply; rhs_nonactive_zero: the caller guarantees
   // exact zeros in the non-active entries of rhs (FGMRES basis vectors whose
