@@ -168,6 +168,14 @@ int pm_scal(pm_ctx* ctx, int n, double a, double* x_dev);
  * src/Multigrid/Multigrid.C:422-514), e.g.
  *   solver_type: iterative       iterative_solver_type: fgmres
  *   preconditioner: multigrid    residual_reduction: 1e-8
+ * Implemented: iterative_solver_type fgmres (right_gmres), cg, bi_cgstab,
+ * jacobi, sor, ssor; preconditioner no_preconditioner, jacobi, sor, ssor,
+ * multigrid; multigrid_smoother(_coarse) jacobi, sor, ssor, cell_vanka,
+ * cell_vanka_jacobi, nodal_vanka, nodal_vanka_jacobi, direct_solve (coarse).
+ * SOR and SSOR (TMatrix::sor_sweep, src/Matrix/Matrix.C:943, omega =
+ * sor_omega) sweep the rows in multicolour order: a greedy colouring of the
+ * matrix graph in row order, rows grouped by colour; rows of one colour are
+ * updated in parallel, which equals the sequential sweep over that order.
  * New keys (no reference counterpart):
  *   gpu_precision {fp64, mixed}: mixed = FP32 multigrid inside FP64 FGMRES;
  *   gpu_mixed_fallback {1, 0}: in the mixed form, the multigrid switches to

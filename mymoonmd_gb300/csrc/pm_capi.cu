@@ -459,8 +459,10 @@ int pm_solver_create(pm_ctx* c, const char* params, pm_solver** out) {
     s->gram_schmidt = p.str("gpu_gram_schmidt", s->mixed ? "cgs2" : "mgs");
     if (s->gram_schmidt != "mgs" && s->gram_schmidt != "cgs2" && s->gram_schmidt != "cgs2_cond")
       throw Error(PM_E_INVALID, "gpu_gram_schmidt is mgs, cgs2 or cgs2_cond");
-    if (s->prec != "no_preconditioner" && s->prec != "jacobi" && s->prec != "multigrid")
+    if (s->prec != "no_preconditioner" && s->prec != "jacobi" && s->prec != "multigrid" && s->prec != "sor" &&
+        s->prec != "ssor")
       throw Error(PM_E_UNSUPPORTED, "preconditioner '" + s->prec + "' is not implemented on the GPU");
+    s->sor_omega = p.num("sor_omega", 1.5);
     s->use_mg = s->solver_type == "iterative" && s->prec == "multigrid";
     if (s->use_mg) {
       s->mg.configure(p);
@@ -540,8 +542,14 @@ int pm_solver_update_matrix(pm_solver* s, pm_matrix* A) {
   } else {
     A->csr.make_sliced64(s->ctx);
   }
-  if (!s->use_mg && (s->prec == "jacobi" || s->method == "jacobi")) {
-    A->csr.make_diag(s->ctx);
+  const bool sor = s->solver_type == "iterative" &&
+                   (s->prec == "sor" || s->prec == "ssor" || s->method == "sor" || s->method == "ssor");
+  if ((!s->use_mg && (s->prec == "jacobi" || s->method == "jacobi")) || sor) A->csr.make_diag(s->ctx);
+  if (sor) {
+    // the colour order of the sweeps (Iteration_sor as a solver or as the
+    // preconditioner)
+    s->sor.build(s->ctx, A->csr);
+    pm::sor_check_diagonal(s->ctx, A->csr);
   }
   PM_CUDA(cudaStreamSynchronize(s->ctx->stream));
   return PM_OK;

@@ -825,6 +825,115 @@ void jacobi_from_zero32(pm_ctx* c, int n, const float* b, const float* d, float 
   PM_LAUNCH1D(k_jacobi_zero<float>, n, n, b, d, w, x);
 }
 
+// ------------------------------------------------------------ SOR ----------
+void SorColours::build(pm_ctx* c, const DevCsr& A) {
+  if (key == A.row_ptr.p && key_nnz == A.nnz) return;
+  const int n = A.n_rows;
+  if (A.n_cols != n) throw Error(PM_E_INVALID, "SOR needs a square matrix");
+  std::vector<int> rp(static_cast<size_t>(n) + 1), ci(static_cast<size_t>(A.nnz));
+  PM_CUDA(cudaMemcpyAsync(rp.data(), A.row_ptr.p, rp.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (A.nnz)
+    PM_CUDA(cudaMemcpyAsync(ci.data(), A.cols.p, ci.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  // the transposed pattern: rows k that store column i
+  std::vector<int> tp(static_cast<size_t>(n) + 1, 0), tc(ci.size());
+  for (int k : ci) tp[size_t(k) + 1]++;
+  for (int i = 0; i < n; ++i) tp[size_t(i) + 1] += tp[size_t(i)];
+  std::vector<int> fill(tp.begin(), tp.end() - 1);
+  for (int i = 0; i < n; ++i)
+    for (int k = rp[size_t(i)]; k < rp[size_t(i) + 1]; ++k) tc[size_t(fill[size_t(ci[size_t(k)])]++)] = i;
+  std::vector<int> colour(static_cast<size_t>(n), -1), stamp;
+  int n_col = 0;
+  for (int i = 0; i < n; ++i) {
+    auto mark = [&](int j) {
+      if (j < i && j != i) {
+        const int cj = colour[size_t(j)];
+        if (cj >= int(stamp.size())) stamp.resize(size_t(cj) + 1, -1);
+        stamp[size_t(cj)] = i;
+      }
+    };
+    for (int k = rp[size_t(i)]; k < rp[size_t(i) + 1]; ++k) mark(ci[size_t(k)]);
+    for (int k = tp[size_t(i)]; k < tp[size_t(i) + 1]; ++k) mark(tc[size_t(k)]);
+    int cc = 0;
+    while (cc < int(stamp.size()) && stamp[size_t(cc)] == i) ++cc;
+    colour[size_t(i)] = cc;
+    n_col = std::max(n_col, cc + 1);
+  }
+  ptr.assign(size_t(n_col) + 1, 0);
+  for (int i = 0; i < n; ++i) ptr[size_t(colour[size_t(i)]) + 1]++;
+  for (int k = 0; k < n_col; ++k) ptr[size_t(k) + 1] += ptr[size_t(k)];
+  std::vector<int> order(static_cast<size_t>(n)), pos(ptr.begin(), ptr.end() - 1);
+  for (int i = 0; i < n; ++i) order[size_t(pos[size_t(colour[size_t(i)])]++)] = i;
+  rows.upload(order, c->stream);
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  key = A.row_ptr.p;
+  key_nnz = A.nnz;
+}
+
+void sor_check_diagonal(pm_ctx* c, const DevCsr& A) {
+  if (!A.diag.p) throw Error(PM_E_INVALID, "SOR check without diagonal");
+  std::vector<double> d(static_cast<size_t>(A.n_rows));
+  if (!d.empty())
+    PM_CUDA(cudaMemcpyAsync(d.data(), A.diag.p, d.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  for (double v : d)
+    if (v == 0.0) throw Error(PM_E_INVALID, "There is a zero on the diagonal. You can not use `sor` in this case");
+}
+
+// x_row += omega (b_row - sum_k a_row,k x_k) / d_row for the rows of one
+// colour, G lanes per row (they do not couple, so x is updated in place)
+template <class T, int G>
+__global__ void __launch_bounds__(256) k_sor_rows(int cnt, const int* __restrict__ rows, const int* __restrict__ rp,
+                                                  const int* __restrict__ ci, const T* __restrict__ v,
+                                                  const T* __restrict__ d, const T* __restrict__ b, T* x, T omega,
+                                                  const int* __restrict__ guard) {
+  if (guarded(guard)) return;  // uniform for the whole grid
+  const int lane = threadIdx.x & (G - 1);
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const bool valid = q < cnt;
+  const int row = valid ? __ldg(rows + q) : 0;
+  const int beg = valid ? __ldg(rp + row) : 0;
+  const int end = valid ? __ldg(rp + row + 1) : 0;
+  T s = T(0);
+  for (int k = beg + lane; k < end; k += G) s += __ldg(v + k) * x[__ldg(ci + k)];
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, G);
+  if (valid && lane == 0) x[row] = x[row] + omega * (b[row] - s) / d[row];
+}
+
+template <class T>
+static void sor_sweep_t(pm_ctx* c, const DevCsr& A, const T* vals, const T* diag, const SorColours& col, const T* b,
+                        T* x, T omega, bool backward) {
+  if (!diag) throw Error(PM_E_INVALID, "SOR sweep without diagonal");
+  if (col.ptr.empty() || col.key != A.row_ptr.p) throw Error(PM_E_INVALID, "SOR sweep without the matrix's colours");
+  const int nc = int(col.ptr.size()) - 1;
+  const bool wide = A.nnz > 16 * int64_t(A.n_rows);
+  for (int q = 0; q < nc; ++q) {
+    const int k = backward ? nc - 1 - q : q;
+    const int cnt = col.ptr[size_t(k) + 1] - col.ptr[size_t(k)];
+    if (!cnt) continue;
+    const int* rows = col.rows.p + col.ptr[size_t(k)];
+    if (wide)
+      k_sor_rows<T, 8><<<nblocks((long long)cnt * 8, 256), 256, 0, c->stream>>>(
+          cnt, rows, A.row_ptr.p, A.cols.p, vals, diag, b, x, omega, c->guard);
+    else
+      k_sor_rows<T, 4><<<nblocks((long long)cnt * 4, 256), 256, 0, c->stream>>>(
+          cnt, rows, A.row_ptr.p, A.cols.p, vals, diag, b, x, omega, c->guard);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
+}
+
+void sor_sweep(pm_ctx* c, const DevCsr& A, const SorColours& col, const double* b, double* x, double omega,
+               bool backward) {
+  sor_sweep_t<double>(c, A, A.vals.p, A.diag.p, col, b, x, omega, backward);
+}
+void sor_sweep32(pm_ctx* c, const DevCsr& A, const SorColours& col, const float* b, float* x, float omega,
+                 bool backward) {
+  if (!A.vals32.p) throw Error(PM_E_INVALID, "matrix has no FP32 copy");
+  sor_sweep_t<float>(c, A, A.vals32.p, A.diag32.p, col, b, x, omega, backward);
+}
+
 // ------------------------------------------------------- dense inverse ------
 __global__ void k_dense_fill(int na, const int* __restrict__ act, const int* __restrict__ pos,
                              const int* __restrict__ rp, const int* __restrict__ ci,

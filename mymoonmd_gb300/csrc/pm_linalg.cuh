@@ -129,6 +129,30 @@ void copy_nonactive(pm_ctx* c, int n, const BlockMask& m, const double* src, dou
 // *flag := 1 if some non-active entry of x is not zero (the caller clears it)
 void nonactive_nonzero(pm_ctx* c, const BlockMask& m, const double* x, int* flag);
 
+// Multicolour order of the SOR / SSOR sweeps (TMatrix::sor_sweep,
+// src/Matrix/Matrix.C:943-1031, visits the rows in order): a greedy colouring
+// of the matrix graph (rows i and j adjacent when a_ij or a_ji is stored), in
+// row order, each row taking the smallest colour none of its already coloured
+// neighbours has. Rows of one colour do not couple, so a colour is updated in
+// parallel and the sweep equals the sequential one over the rows ordered by
+// colour.
+struct SorColours {
+  DBuf<int> rows;        // rows grouped by colour, increasing within a colour
+  std::vector<int> ptr;  // colour k: rows[ptr[k], ptr[k+1])
+  const int* key = nullptr;  // the structure (row pointer array) it was built for
+  int64_t key_nnz = -1;
+  void build(pm_ctx* c, const DevCsr& A);  // once per structure
+};
+// one SOR sweep x += omega D^-1 (b - A x), row by row in colour order
+// (backward: colours in reverse), FP64 or on the FP32 copy
+// TMatrix::sor_sweep refuses a zero on the diagonal (src/Matrix/Matrix.C:956-961);
+// reads the diagonal made by make_diag
+void sor_check_diagonal(pm_ctx* c, const DevCsr& A);
+void sor_sweep(pm_ctx* c, const DevCsr& A, const SorColours& col, const double* b, double* x, double omega,
+               bool backward);
+void sor_sweep32(pm_ctx* c, const DevCsr& A, const SorColours& col, const float* b, float* x, float omega,
+                 bool backward);
+
 // dense inverse of the active block of a small CSR matrix (Gauss-Jordan with
 // partial pivoting on the device); used by the coarse-grid direct solve
 struct DenseInverse {

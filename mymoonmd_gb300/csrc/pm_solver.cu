@@ -92,6 +92,10 @@ static int smoother_code(const std::string& s) {
   if (s == "nodal_vanka" || s == "nodal_vanka_store") return SM_NODAL_VANKA;
   // additive nodal Vanka (the CELL_JACOBI treatment on nodal patches)
   if (s == "nodal_vanka_jacobi") return SM_NODAL_VANKA_JACOBI;
+  // SOR / SSOR in multicolour order (the sequential sweep over the rows
+  // ordered by colour)
+  if (s == "sor") return SM_SOR;
+  if (s == "ssor") return SM_SSOR;
   throw Error(PM_E_UNSUPPORTED, "multigrid smoother '" + s + "' is not implemented on the GPU");
 }
 
@@ -99,6 +103,7 @@ void Multigrid::configure(const Params& p) {
   n_pre = int(p.integer("multigrid_n_pre_smooth", 1));
   n_post = int(p.integer("multigrid_n_post_smooth", 1));
   jacobi_damp = p.num("jacobi_damp", 1.0);
+  sor_omega = p.num("sor_omega", 1.5);
   vanka_damp = p.num("multigrid_vanka_damp_factor", 1.0);
   correction_damp = p.num("multigrid_correction_damp_factor", 1.0);
   coarse_residual = p.num("multigrid_coarse_residual", 0.1);
@@ -164,7 +169,12 @@ void Multigrid::update(pm_ctx* c) {
     if (lv.proj) lv.proj->refresh(c, A, mixed);
     if (vanka) lv.vanka->factor(c, lv.proj->csr, mixed);
     if (nodal) lv.nodal->factor(c, lv.proj->csr, mixed);
-    if (lv.smoother == SM_JACOBI) A.make_diag(c);
+    const bool sor = lv.smoother == SM_SOR || lv.smoother == SM_SSOR;
+    if (lv.smoother == SM_JACOBI || sor) A.make_diag(c);
+    if (sor) {
+      lv.sor.build(c, A);
+      sor_check_diagonal(c, A);
+    }
     A.make_sliced64(c);  // FP64 sweeps, defects and the Krylov SpMV on the sliced copy
     const int n = A.n_rows;
     if (l < L - 1) {
@@ -219,6 +229,16 @@ void Multigrid::smooth(pm_ctx* c, int l) {
     } else {
       csr_apply(c, A, EPI_JACOBI, lv.cur, lv.oth, lv.rhs.p, jacobi_damp);
       std::swap(lv.cur, lv.oth);
+    }
+  } else if (lv.smoother == SM_SOR || lv.smoother == SM_SSOR) {
+    // SORSmoother::smooth: one sweep of Iteration_sor::apply_smoother on the
+    // current iterate (SSOR: forward, then backward)
+    if (mixed) {
+      sor_sweep32(c, A, lv.sor, lv.rhs32.p, lv.cur32, float(sor_omega), false);
+      if (lv.smoother == SM_SSOR) sor_sweep32(c, A, lv.sor, lv.rhs32.p, lv.cur32, float(sor_omega), true);
+    } else {
+      sor_sweep(c, A, lv.sor, lv.rhs.p, lv.cur, sor_omega, false);
+      if (lv.smoother == SM_SSOR) sor_sweep(c, A, lv.sor, lv.rhs.p, lv.cur, sor_omega, true);
     }
   } else if (lv.smoother == SM_DIRECT) {
     coarse_solve(c);
@@ -864,7 +884,12 @@ size_t pm_solver::layout_signature() const {
     mix(lv.coarse.inv.p); mix(lv.coarse.act.p); mix(lv.coarse.pos.p); mix(lv.coarse.tmp.p);
     mix(lv.coarse.inv32.p);
     mix(lv.coarse_rhs64.p); mix(lv.coarse_sol64.p);
+    mix(lv.sor.rows.p);
+    h ^= lv.sor.ptr.size();
   }
+  // the SOR preconditioner's colours (a new structure gives new launches)
+  mix(sor.rows.p);
+  h ^= sor.ptr.size() * 977;
   mix(work.p); mix(gm.p); mix(flags.p);
   mix(ctx->partials.p); mix(ctx->host_scalars);
   h ^= size_t(restart) * 31 + size_t(work_n);
@@ -904,6 +929,11 @@ void pm_solver::precondition(const double* z, double* r, bool z_nonactive_zero) 
     // Iteration_jacobi::apply: r = z / diag
     vcopy(ctx, n, z, r);
     vdiv(ctx, n, A->csr.diag.p, r);
+  } else if (prec == "sor" || prec == "ssor") {
+    // Iteration_sor::apply (src/Solver/Iteration_sor.C:75): r = 0, one sweep
+    vset(ctx, n, r, 0.0);
+    sor_sweep(ctx, A->csr, sor, z, r, sor_omega, false);
+    if (prec == "ssor") sor_sweep(ctx, A->csr, sor, z, r, sor_omega, true);
   } else {
     vcopy(ctx, n, z, r);
   }
@@ -1236,6 +1266,28 @@ void pm_solver::jacobi_iter(const double* rhs, double* sol) {
   }
 }
 
+// Iteration_sor::iterate (src/Solver/Iteration_sor.C:24-60): one (S)SOR sweep
+// per iteration in the colour order, then the defect for the stopping test
+void pm_solver::sor_iter(const double* rhs, double* sol, bool symmetric) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  ensure_work(1, n);
+  double* r = work.p;
+  csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+  double normb = std::sqrt(dot_host(c, n, rhs, rhs));
+  if (normb == 0.0) normb = 1.0;
+  double resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+  if (converged(resid, 0)) return;
+  for (unsigned i = 1; i <= (unsigned long)max_it; ++i) {
+    sor_sweep(c, M, sor, rhs, sol, sor_omega, false);
+    if (symmetric) sor_sweep(c, M, sor, rhs, sol, sor_omega, true);
+    csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+    resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+    if (converged(resid, i)) return;
+  }
+}
+
 void pm_solver::solve(const double* rhs, double* sol) {
   if (!A) throw Error(PM_E_INVALID, "Solver::solve called before update_matrix");
   history.clear();
@@ -1253,5 +1305,6 @@ void pm_solver::solve(const double* rhs, double* sol) {
   else if (method == "cg") cg(rhs, sol);
   else if (method == "bi_cgstab") bicgstab(rhs, sol);
   else if (method == "jacobi") jacobi_iter(rhs, sol);
+  else if (method == "sor" || method == "ssor") sor_iter(rhs, sol, method == "ssor");
   else throw Error(PM_E_UNSUPPORTED, "iterative_solver_type '" + method + "' is not implemented on the GPU");
 }

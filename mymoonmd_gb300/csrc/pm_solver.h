@@ -30,7 +30,8 @@ struct Params {
 
 enum Smoother {
   SM_JACOBI = 0, SM_DIRECT = 1, SM_CELL_VANKA = 2, SM_CELL_VANKA_JACOBI = 3, SM_NONE = 4,
-  SM_NODAL_VANKA = 5, SM_NODAL_VANKA_JACOBI = 6
+  SM_NODAL_VANKA = 5, SM_NODAL_VANKA_JACOBI = 6,
+  SM_SOR = 7, SM_SSOR = 8  // SORSmoother (src/Multigrid/SORSmoother.C), forward / forward + backward
 };
 enum Dir { DIR_DUMMY = 0, DIR_DOWN = 1, DIR_UP = 2, DIR_END = 3 };
 
@@ -47,6 +48,7 @@ struct MGLevel {
   int smoother = SM_JACOBI;
   DenseInverse coarse;
   DBuf<double> coarse_rhs64, coarse_sol64;
+  SorColours sor;  // the level's multicolour SOR order
   // saddle point levels: the projected combined matrix (Vanka, direct solve)
   // and the cell Vanka data; owned by the problem
   ProjectedMatrix* proj = nullptr;
@@ -61,7 +63,7 @@ struct Multigrid {
   std::vector<MGLevel> levels;  // 0 = coarsest
   std::vector<int> control;
   int n_pre = 1, n_post = 1;
-  double jacobi_damp = 1.0, correction_damp = 1.0, coarse_residual = 0.1, vanka_damp = 1.0;
+  double jacobi_damp = 1.0, correction_damp = 1.0, coarse_residual = 0.1, vanka_damp = 1.0, sor_omega = 1.5;
   int coarse_max_it = 10;
   int smoother = SM_JACOBI, smoother_coarse = SM_DIRECT;
   std::string cycle_type = "V";
@@ -128,6 +130,9 @@ struct pm_solver {
   bool use_mg = false;
   pm::DenseInverse direct;
   bool direct_ready = false;
+  // "sor" / "ssor" preconditioner (Iteration_sor, src/Solver/Iteration_sor.C)
+  pm::SorColours sor;
+  double sor_omega = 1.5;
   // Krylov work space
   pm::DBuf<double> work;  // vectors
   size_t work_n = 0;
@@ -156,4 +161,5 @@ struct pm_solver {
   void cg(const double* rhs, double* sol);
   void bicgstab(const double* rhs, double* sol);
   void jacobi_iter(const double* rhs, double* sol);
+  void sor_iter(const double* rhs, double* sol, bool symmetric);
 };

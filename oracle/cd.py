@@ -10,6 +10,10 @@ import numpy as np
 
 from . import build as _build
 from . import refsetup
+from . import sor as _sor
+
+# smoother codes of orc_mg (oracle.c)
+SMOOTHERS = {"jacobi": 0, "direct_solve": 1, "sor": 5, "ssor": 6}
 
 _lib = None
 
@@ -38,6 +42,12 @@ def lib() -> C.CDLL:
                                        C.POINTER(i32), C.POINTER(f64), vp, i32, C.POINTER(i32)]
         L.orc_prolongate_flat.argtypes = [i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]
         L.orc_restrict_flat.argtypes = [i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]
+        L.orc_sor_sweep.argtypes = [i32, vp, vp, vp, vp, vp, f64, vp, i32]
+        L.orc_sor_sweep.restype = i32
+        L.orc_mg_set_sor.argtypes = [vp, i32, vp, f64]
+        L.orc_mg_set_smoothers.argtypes = [vp, i32, i32, f64]
+        L.orc_krylov_solve_sor.argtypes = [i32, i32, vp, vp, vp, vp, vp, i32, vp, f64, f64, f64, i32, i32, i32, vp,
+                                           vp, C.POINTER(i32), C.POINTER(f64), vp, i32, C.POINTER(i32)]
         L.orc_lu_factor.argtypes = [i32, vp, vp]
         L.orc_lu_solve.argtypes = [i32, vp, vp, vp]
         _lib = L
@@ -58,6 +68,51 @@ def apply_scaled_add(rp, ci, v, active, x, y, a):
     x = np.ascontiguousarray(x, dtype=np.float64)
     lib().orc_apply_scaled_add(rp.size - 1, _p(act), _p(rp), _p(ci), _p(v), _p(x), _p(y), a)
     return y
+
+
+def sor_sweep(rp, ci, v, b, x, omega, order, flag):
+    """TMatrix::sor_sweep (src/Matrix/Matrix.C:943-1031) over the rows in
+    `order` (flag 0 forward, 1 backward, 2 forward then backward); returns the
+    new x"""
+    x = np.array(x, dtype=np.float64, copy=True)
+    rp = np.ascontiguousarray(rp, dtype=np.int32)
+    ci = np.ascontiguousarray(ci, dtype=np.int32)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    order = np.ascontiguousarray(order, dtype=np.int32)
+    if lib().orc_sor_sweep(rp.size - 1, _p(rp), _p(ci), _p(v), _p(b), _p(x), omega, _p(order), flag) != 0:
+        raise ValueError("There is a zero on the diagonal. You can not use `sor` in this case")
+    return x
+
+
+def sor_iterate(rp, ci, v, active, rhs, sol, omega, order, flag, tol, reduction, max_it, min_it=0,
+                divergence=1e10, stagnation=1e10):
+    """Iteration_sor::iterate (src/Solver/Iteration_sor.C:24-60) with the
+    stopping test of IterativeMethod::converged (include/Solver/IterativeMethod.h:81-135);
+    returns (solution, iterations, residual, history)"""
+    x = np.array(sol, dtype=np.float64, copy=True)
+    r = apply_scaled_add(rp, ci, v, active, x, rhs, -1.0)
+    normb = float(np.linalg.norm(rhs)) or 1.0
+    hist = []
+
+    def converged(res, it):
+        hist.append(res)
+        init, prev = hist[0], hist[-2] if len(hist) > 1 else hist[0]
+        if res > divergence * init:
+            raise RuntimeError("solver divergence")
+        conv = (res < tol or res < reduction * init or res > stagnation * prev) and (it > min_it or min_it == 0)
+        return conv or it == max_it
+
+    res = float(np.linalg.norm(r)) / normb
+    if converged(res, 0):
+        return x, 0, res, np.array(hist)
+    for i in range(1, max_it + 1):
+        x = sor_sweep(rp, ci, v, rhs, x, omega, order, flag)
+        r = apply_scaled_add(rp, ci, v, active, x, rhs, -1.0)
+        res = float(np.linalg.norm(r)) / normb
+        if converged(res, i):
+            return x, i, res, np.array(hist)
+    return x, max_it, res, np.array(hist)
 
 
 def transfer(dim: int, k: int, coarse_level, fine_level, vec: np.ndarray, prolongate: bool) -> np.ndarray:
@@ -125,8 +180,14 @@ class OracleCD:
         a[: lv.n_active] = 1
         return a
 
+    def sor_order(self, l: int = -1) -> np.ndarray:
+        """the row order of the multicolour SOR sweep of level l"""
+        lv = self.levels[l]
+        return _sor.colour_order(_sor.greedy_colouring(lv.row_ptr, lv.cols))
+
     def build_mg(self, n_pre=2, n_post=2, jacobi_damp=0.8, correction_damp=1.0, cycle="V",
-                 coarse_direct=True, coarse_max_it=10, coarse_residual=0.1, n_mg_levels=None):
+                 coarse_direct=True, coarse_max_it=10, coarse_residual=0.1, n_mg_levels=None,
+                 smoother="jacobi", coarse_smoother=None, sor_omega=1.5):
         L = lib()
         if self._mg:
             L.orc_mg_destroy(self._mg)
@@ -152,6 +213,15 @@ class OracleCD:
             keep += [fd, cd, fv, cv, par]
             L.orc_mg_set_transfer(mg, l, self.dim, self.elem, fl.n_cells, fl.nloc, _p(fd), _p(cd), _p(par),
                                   _p(fv), _p(cv), fl.n_dofs, cl.n_dofs)
+        coarse = coarse_smoother or ("direct_solve" if coarse_direct else smoother)
+        if smoother != "jacobi" or coarse not in ("direct_solve", "jacobi"):
+            L.orc_mg_set_smoothers(mg, SMOOTHERS[smoother], SMOOTHERS[coarse], 1.0)
+        for l in range(nl):
+            code = coarse if l == 0 else smoother
+            if code in ("sor", "ssor"):
+                order = self.sor_order(off + l)
+                keep.append(order)
+                L.orc_mg_set_sor(mg, l, _p(order), sor_omega)
         if L.orc_mg_finalize(mg) != 0:
             raise RuntimeError("oracle coarse factorisation failed")
         self._mg = mg
@@ -165,8 +235,13 @@ class OracleCD:
         return r
 
     def solve(self, method: str = "fgmres", tol: float = 0.0, reduction: float = 1e-8, max_it: int = 100,
-              min_it: int = 0, restart: int = 20, use_mg: bool = True, sol0=None):
-        """returns (solution, iterations, residual, history, status)"""
+              min_it: int = 0, restart: int = 20, use_mg: bool = True, sol0=None, sor: str | None = None,
+              sor_omega: float = 1.5):
+        """returns (solution, iterations, residual, history, status); sor = "sor" or
+        "ssor" preconditions with one (S)SOR sweep in colour order instead of the
+        multigrid"""
+        if sor is not None:
+            return self._solve_sor(method, tol, reduction, max_it, min_it, restart, sol0, sor, sor_omega)
         lv = self.finest
         act = self.active()
         rhs = self.rhs[-1]
@@ -180,6 +255,32 @@ class OracleCD:
                                     self._mg if use_mg else None, tol, reduction, max_it, min_it, restart,
                                     _p(rhs), _p(sol), C.byref(it), C.byref(res), _p(hist), hist.size,
                                     C.byref(nh))
+        return sol, it.value, res.value, hist[: nh.value].copy(), st
+
+    def sor_iterate(self, sor="sor", tol=0.0, reduction=1e-8, max_it=100, sor_omega=1.5):
+        """iterative_solver_type sor / ssor on the finest level in colour order;
+        the start has the rhs's non-active entries"""
+        lv = self.finest
+        rhs = self.rhs[-1]
+        sol = np.zeros(lv.n_dofs)
+        sol[lv.n_active:] = rhs[lv.n_active:]
+        return sor_iterate(lv.row_ptr, lv.cols, self.vals[-1], self.active(), rhs, sol, sor_omega,
+                           self.sor_order(-1), {"sor": 0, "ssor": 2}[sor], tol, reduction, max_it)
+
+    def _solve_sor(self, method, tol, reduction, max_it, min_it, restart, sol0, sor, sor_omega):
+        lv = self.finest
+        act = self.active()
+        rhs = self.rhs[-1]
+        sol = np.zeros(lv.n_dofs) if sol0 is None else np.array(sol0, dtype=np.float64)
+        sol[lv.n_active:] = rhs[lv.n_active:]
+        order = self.sor_order(-1)
+        it, res, nh = C.c_int(), C.c_double(), C.c_int()
+        hist = np.zeros(100000)
+        st = lib().orc_krylov_solve_sor({"fgmres": 0, "cg": 1, "bi_cgstab": 2}[method], lv.n_dofs, _p(act),
+                                        _p(lv.row_ptr), _p(lv.cols), _p(self.vals[-1]), None,
+                                        {"sor": 0, "ssor": 2}[sor], _p(order), sor_omega, tol, reduction, max_it,
+                                        min_it, restart, _p(rhs), _p(sol), C.byref(it), C.byref(res), _p(hist),
+                                        hist.size, C.byref(nh))
         return sol, it.value, res.value, hist[: nh.value].copy(), st
 
     def close(self):

@@ -529,9 +529,38 @@ typedef struct {
   int n_colors;
   const int* n_freeze;
   void* store; /* stored local factorisations */
+  const int* sor_order; /* rows in the order of the SOR sweep (NULL: 0..n-1) */
 } orc_level;
 
-enum { SM_JAC = 0, SM_DIR = 1, SM_VANKA = 2, SM_VANKA_JAC = 3, SM_VANKA_COLOR = 4 };
+enum { SM_JAC = 0, SM_DIR = 1, SM_VANKA = 2, SM_VANKA_JAC = 3, SM_VANKA_COLOR = 4, SM_SOR = 5, SM_SSOR = 6 };
+
+/* TMatrix::sor_sweep (src/Matrix/Matrix.C:943-1031): for every row in turn,
+ * s = b_row - sum_k a_row,k x_k (left to right), x_row += omega s / a_row,row;
+ * flag 0 forward, 1 backward, 2 forward then backward (SSOR). The rows are
+ * visited in `order` (NULL: the natural order, the reference's); the GPU's
+ * multicolour sweep is this sweep in colour order. Returns -1 on a zero
+ * diagonal entry (the reference throws). */
+int orc_sor_sweep(int n, const int* rp, const int* ci, const double* v, const double* b, double* x, double omega,
+                  const int* order, int flag) {
+  double* diag = (double*)calloc((size_t)n, sizeof(double));
+  for (int i = 0; i < n; ++i)
+    for (int k = rp[i]; k < rp[i + 1]; ++k)
+      if (ci[k] == i) diag[i] = v[k];
+  for (int i = 0; i < n; ++i)
+    if (diag[i] == 0.0) { free(diag); return -1; }
+  for (int sweep = 0; sweep < (flag == 2 ? 2 : 1); ++sweep) {
+    const int backward = flag == 1 || (flag == 2 && sweep == 1);
+    for (int r = 0; r < n; ++r) {
+      const int q = backward ? n - 1 - r : r;
+      const int row = order ? order[q] : q;
+      double s = b[row];
+      for (int k = rp[row]; k < rp[row + 1]; ++k) s -= v[k] * x[ci[k]];
+      x[row] = x[row] + omega * s / diag[row];
+    }
+  }
+  free(diag);
+  return 0;
+}
 
 void* orc_vanka_store_create(int n_patches);
 void orc_vanka_store_destroy(void* st);
@@ -540,7 +569,7 @@ typedef struct {
   int n_levels;
   orc_level* lv;
   int n_pre, n_post, coarse_max_it, cycle; /* cycle: 0 V, 1 W, 2 F */
-  double jacobi_damp, correction_damp, coarse_residual, vanka_damp;
+  double jacobi_damp, correction_damp, coarse_residual, vanka_damp, sor_omega;
   int coarse_direct;
   int smoother, smoother_coarse;
   int* control;
@@ -575,6 +604,7 @@ orc_mg* orc_mg_create(int n_levels, int n_pre, int n_post, double jacobi_damp, d
   m->smoother = SM_JAC;
   m->smoother_coarse = coarse_direct ? SM_DIR : SM_JAC;
   m->vanka_damp = 1.0;
+  m->sor_omega = 1.5;
   int* rec = (int*)malloc(sizeof(int) * (size_t)n_levels);
   for (int i = 0; i < n_levels; ++i) rec[i] = cycle == 0 ? 1 : 2;
   rec[n_levels - 1] = 1;
@@ -614,6 +644,13 @@ void orc_mg_set_smoothers(orc_mg* m, int fine, int coarse, double vanka_damp) {
   m->smoother_coarse = coarse;
   m->coarse_direct = coarse == SM_DIR;
   m->vanka_damp = vanka_damp;
+}
+
+/* SOR / SSOR smoother: the row order of level l's sweeps and the
+ * overrelaxation parameter (sor_omega) */
+void orc_mg_set_sor(orc_mg* m, int l, const int* order, double omega) {
+  m->lv[l].sor_order = order;
+  m->sor_omega = omega;
 }
 
 /* saddle point level: projected combined matrix (get_combined_matrix) and the
@@ -710,6 +747,12 @@ static void smooth(orc_mg* m, int l) {
     orc_vanka_sweep_var(code == SM_VANKA ? 0 : code == SM_VANKA_JAC ? 1 : 2, L->n_patches, L->patch_ptr, L->patch, L->n, L->vrp,
                     L->vci, L->vv, L->rhs, L->sol, m->vanka_damp, L->color_ptr, L->color_cells, L->n_colors,
                     L->n_freeze, L->store);
+    return;
+  }
+  if (code == SM_SOR || code == SM_SSOR) {
+    /* SORSmoother::smooth (src/Multigrid/SORSmoother.C:29): one sweep of
+     * Iteration_sor::apply_smoother, SOR forward (0) or SSOR (2) */
+    orc_sor_sweep(L->n, L->rp, L->ci, L->v, L->rhs, L->sol, m->sor_omega, L->sor_order, code == SM_SOR ? 0 : 2);
     return;
   }
   /* JacobiSmoother::smooth */
@@ -813,6 +856,10 @@ typedef struct {
   const int *rp, *ci;
   const double* v;
   orc_mg* mg; /* NULL: no preconditioner */
+  /* SOR / SSOR preconditioner (Iteration_sor::apply): sor_flag 0 or 2, -1 none */
+  int sor_flag;
+  const int* sor_order;
+  double sor_omega;
 } orc_system;
 
 static void sys_apply_scaled_add(const orc_system* s, const double* x, double* y, double a) {
@@ -820,7 +867,11 @@ static void sys_apply_scaled_add(const orc_system* s, const double* x, double* y
 }
 static void prec_apply(const orc_system* s, const double* z, double* r) {
   if (s->mg) orc_mg_apply(s->mg, z, r);
-  else memcpy(r, z, sizeof(double) * (size_t)s->n);
+  else if (s->sor_flag >= 0) {
+    /* Iteration_sor::apply (src/Solver/Iteration_sor.C:75): r = 0, one sweep */
+    memset(r, 0, sizeof(double) * (size_t)s->n);
+    orc_sor_sweep(s->n, s->rp, s->ci, s->v, z, r, s->sor_omega, s->sor_order, s->sor_flag);
+  } else memcpy(r, z, sizeof(double) * (size_t)s->n);
 }
 
 static void gen_rot(double dx, double dy, double* cs, double* sn) {
@@ -994,11 +1045,28 @@ int orc_bicgstab(const orc_system* s, orc_krylov* k, const double* rhs, double* 
 }
 
 /* flat entry point for ctypes: solver 0 fgmres, 1 cg, 2 bicgstab */
+int orc_krylov_solve_sor(int method, int n, const unsigned char* active, const int* rp, const int* ci,
+                         const double* v, orc_mg* mg, int sor_flag, const int* sor_order, double sor_omega,
+                         double tol, double reduction, int max_it, int min_it, int restart, const double* rhs,
+                         double* sol, int* iterations, double* residual, double* history, int cap_history,
+                         int* n_history);
+
 int orc_krylov_solve(int method, int n, const unsigned char* active, const int* rp, const int* ci,
                      const double* v, orc_mg* mg, double tol, double reduction, int max_it, int min_it,
                      int restart, const double* rhs, double* sol, int* iterations, double* residual,
                      double* history, int cap_history, int* n_history) {
-  orc_system s = {n, active, rp, ci, v, mg};
+  return orc_krylov_solve_sor(method, n, active, rp, ci, v, mg, -1, NULL, 0.0, tol, reduction, max_it, min_it,
+                              restart, rhs, sol, iterations, residual, history, cap_history, n_history);
+}
+
+/* the same with the SOR (sor_flag 0) or SSOR (2) preconditioner when mg is
+ * NULL; the sweeps visit the rows in sor_order */
+int orc_krylov_solve_sor(int method, int n, const unsigned char* active, const int* rp, const int* ci,
+                         const double* v, orc_mg* mg, int sor_flag, const int* sor_order, double sor_omega,
+                         double tol, double reduction, int max_it, int min_it, int restart, const double* rhs,
+                         double* sol, int* iterations, double* residual, double* history, int cap_history,
+                         int* n_history) {
+  orc_system s = {n, active, rp, ci, v, mg, sor_flag, sor_order, sor_omega};
   orc_krylov k;
   memset(&k, 0, sizeof(k));
   k.tol = tol; k.reduction = reduction; k.divergence = 1e10; k.stagnation = 1e10;
