@@ -244,15 +244,25 @@ int pm_disc_prolongation(const pm_disc* d, int level, int* row_ptr, int* cols, d
 
 /* ------------------------------------------------------------ assembly --- */
 /* Coefficients of the convection-diffusion problem
- *   -eps Laplace(u) + b.grad(u) + c u = f, u = 0 on the boundary,
- * with f from the manufactured solution u = prod_d sin(pi x_d)
- * (manufactured = 1) or f = f_const (manufactured = 0). */
+ *   -eps Laplace(u) + b.grad(u) + c u = f, u = g on the boundary:
+ *   manufactured = 1: f from the exact solution u = prod_d sin(pi x_d), g = 0
+ *     (Example_CD2D/3D sine examples);
+ *   manufactured = 0: f = f_const, g = 0;
+ *   manufactured = 2: f from the quadratic exact solution
+ *     u = poly[0] + poly[1] x + poly[2] y + poly[3] z + poly[4] x^2 + poly[5] y^2
+ *         + poly[6] z^2 + poly[7] xy + poly[8] xz + poly[9] yz,
+ *     g = u at the Dirichlet DOFs (the point values of the Lagrange nodal
+ *     functionals, Assemble3D.C:640-665). The examples test_p0 / test_p1 /
+ *     test_p2 of Example_CD3D.C:164-193 (exact solution in Q1 / Q2).
+ * poly is read only with manufactured = 2 (a caller built against a header
+ * without it passes the smaller struct safely with 0 or 1). */
 typedef struct pm_cd_coeffs {
   double eps;
   double b[3];
   double c;
   int manufactured;
   double f_const;
+  double poly[10];
 } pm_cd_coeffs;
 
 /* Assemble2D / Assemble3D with LocalAssembling (ConvDiff Galerkin,

@@ -37,7 +37,7 @@ class PmError(RuntimeError):
 
 class CdCoeffs(C.Structure):
     _fields_ = [("eps", C.c_double), ("b", C.c_double * 3), ("c", C.c_double),
-                ("manufactured", C.c_int), ("f_const", C.c_double)]
+                ("manufactured", C.c_int), ("f_const", C.c_double), ("poly", C.c_double * 10)]
 
 
 class Request(C.Structure):

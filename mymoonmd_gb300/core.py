@@ -410,14 +410,20 @@ class Discretization:
 
 
 def cd_coeffs(eps: float, b=(0.0, 0.0, 0.0), c: float = 0.0, manufactured: bool = True,
-              f_const: float = 0.0) -> CdCoeffs:
+              f_const: float = 0.0, poly=None) -> CdCoeffs:
+    """poly: the ten coefficients of a quadratic exact solution (1, x, y, z, x^2,
+    y^2, z^2, xy, xz, yz); f and the Dirichlet values then come from it"""
     cf = CdCoeffs()
+    if poly is not None:
+        p = list(poly) + [0.0] * (10 - len(poly))
+        for i in range(10):
+            cf.poly[i] = p[i]
     cf.eps = eps
     bb = list(b) + [0.0] * (3 - len(b))
     for i in range(3):
         cf.b[i] = bb[i]
     cf.c = c
-    cf.manufactured = 1 if manufactured else 0
+    cf.manufactured = 2 if poly is not None else (1 if manufactured else 0)
     cf.f_const = f_const
     return cf
 

@@ -96,8 +96,47 @@ void build_qk_tables(int dim, int k, int qn, RefTables& t) {
 // -------------------------------------------------------------- kernels ----
 struct CdCoef {
   double eps, b0, b1, b2, c, fconst;
-  int manufactured;
+  int manufactured;  // 0: f = fconst; 1: sine exact solution; 2: quadratic exact solution
+  double poly[10];   // 1, x, y, z, x^2, y^2, z^2, xy, xz, yz
 };
+
+static CdCoef make_coef(const pm_cd_coeffs& cf) {
+  CdCoef k{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured, {}};
+  if (cf.manufactured == 2)
+    for (int i = 0; i < 10; ++i) k.poly[i] = cf.poly[i];
+  return k;
+}
+
+// value of the quadratic exact solution (x[2] = 0 in 2D)
+__host__ __device__ __forceinline__ double poly_u(const double* p, const double* x) {
+  double u = p[0];
+  u += p[1] * x[0];
+  u += p[2] * x[1];
+  u += p[3] * x[2];
+  u += p[4] * x[0] * x[0];
+  u += p[5] * x[1] * x[1];
+  u += p[6] * x[2] * x[2];
+  u += p[7] * x[0] * x[1];
+  u += p[8] * x[0] * x[2];
+  u += p[9] * x[1] * x[2];
+  return u;
+}
+
+// f = -eps Lap u + b.grad u + c u of the quadratic exact solution, in the
+// order of the sine branch (the examples' BilinearCoeffs)
+__device__ __forceinline__ double poly_rhs(const CdCoef& k, int dim, const double* xin) {
+  const double x[3] = {xin[0], xin[1], dim == 3 ? xin[2] : 0.0};
+  const double* p = k.poly;
+  const double u = poly_u(p, x);
+  const double ux = p[1] + 2 * p[4] * x[0] + p[7] * x[1] + p[8] * x[2];
+  const double uy = p[2] + 2 * p[5] * x[1] + p[7] * x[0] + p[9] * x[2];
+  const double uz = p[3] + 2 * p[6] * x[2] + p[8] * x[0] + p[9] * x[1];
+  const double lap = dim == 3 ? 2 * (p[4] + p[5] + p[6]) : 2 * (p[4] + p[5]);
+  double f = -k.eps * lap;
+  f += k.b0 * ux + k.b1 * uy + (dim == 3 ? k.b2 * uz : 0.0);
+  f += k.c * u;
+  return f;
+}
 
 // affine map of cell `cell`: origin and Jacobian columns (QuadAffin/HexaAffin)
 template <int DIM>
@@ -121,6 +160,7 @@ __device__ __forceinline__ void affine_map(const double* __restrict__ v, double*
 
 __device__ __forceinline__ double rhs_value(const CdCoef& k, int dim, const double* x) {
   if (!k.manufactured) return k.fconst;
+  if (k.manufactured == 2) return poly_rhs(k, dim, x);
   const double p = 3.14159265358979323846;
   // exact solution u = prod sin(pi x_d): values, gradient, Laplacian
   double s[3], co[3];
@@ -150,6 +190,7 @@ __device__ __forceinline__ double rhs_value(const CdCoef& k, int dim, const doub
 // the same right-hand side with sin(pi x) and cos(pi x) from one sincospi call
 __device__ __forceinline__ double rhs_value_pi(const CdCoef& k, int dim, const double* x) {
   if (!k.manufactured) return k.fconst;
+  if (k.manufactured == 2) return poly_rhs(k, dim, x);
   const double p = 3.14159265358979323846;
   double s[3], co[3];
   for (int d = 0; d < dim; ++d) sincospi(x[d], &s[d], &co[d]);
@@ -442,10 +483,30 @@ static void launch_elem(pm_ctx* c, int n_cells, const double* verts, const doubl
   c->kernel_launches++;
 }
 
+// Dirichlet values g = u(node) of the quadratic exact solution at the
+// non-active DOFs (their rows are unit rows; the gather left their rhs 0)
+__global__ void k_dirichlet_poly(int nb, int n_active, const double* __restrict__ xyz, CdCoef co,
+                                 double* __restrict__ rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  rhs[n_active + i] = poly_u(co.poly, x);
+}
+
+void launch_dirichlet_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs) {
+  const int nb = int(L.bnd_xyz.n / 3);
+  if (cf.manufactured != 2 || nb == 0) return;
+  k_dirichlet_poly<<<(nb + 255) / 256, 256, 0, c->stream>>>(nb, L.n_active, L.bnd_xyz.p, make_coef(cf), rhs);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
 void DevAssemblyLevel::upload(pm_ctx* c, const DiscLevel& L, int dim, int nvc) {
   n_cells = L.n_cells;
   nloc = L.space.nloc;
   n_dofs = L.sys.n_rows;
+  n_active = L.sys.n_active;
+  bnd_xyz.upload(L.bnd_xyz, c->stream);
   verts.upload(L.verts, c->stream);
   gat_ptr.upload(L.gat_ptr, c->stream);
   gat_idx.upload(L.gat_idx, c->stream);
@@ -464,7 +525,7 @@ void DevAssemblyLevel::scratch_sizes(size_t& k_elems, size_t& f_elems) const {
 void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, int qn,
                        const pm_cd_coeffs& cf, const DevRefTables& rt, DevCsr& A, double* rhs,
                        double* K, double* F) {
-  CdCoef co{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured};
+  const CdCoef co = make_coef(cf);
   const int k = elem;
   const double* T = rt.tensors.p;
   if (!c->assembly_quadrature_loop && T) {
@@ -500,6 +561,7 @@ void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, 
       n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
   PM_CHECK_LAUNCH();
   c->kernel_launches += nd ? 3 : 2;
+  launch_dirichlet_values(c, L, cf, rhs);
   A.values_changed(c);
 }
 
@@ -580,7 +642,7 @@ namespace pm {
 // element kernels of assemble_cd_level, for the allocation-free entry point
 static void noalloc_elements(pm_ctx* c, const DevAssemblyLevel& L, int dim, int k, int qn,
                              const pm_cd_coeffs& cf, const DevRefTables& rt, double* K, double* F) {
-  CdCoef co{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured};
+  const CdCoef co = make_coef(cf);
   if (dim == 2 && k == 1 && qn == 3) launch_elem<2, 4, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 2 && k == 1 && qn == 2) launch_elem<2, 4, 4, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 2 && k == 2 && qn == 3) launch_elem<2, 9, 9, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
@@ -643,6 +705,7 @@ extern "C" int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coef
       return PM_E_CUDA;
     }
     c->kernel_launches += nd ? 3 : 2;
+    pm::launch_dirichlet_values(c, L, coeffs ? *coeffs : p->coeffs, rhs_dev);
     return PM_OK;
   } catch (const pm::Error& e) {
     c->last_error = e.what();

@@ -29,12 +29,17 @@ void build_ref_tensors(const RefTables& t, std::vector<double>& out);
 
 // device copy of one level's assembly inputs
 struct DevAssemblyLevel {
-  int n_cells = 0, nloc = 0, n_dofs = 0;
+  int n_cells = 0, nloc = 0, n_dofs = 0, n_active = 0;
   DBuf<double> verts;
+  DBuf<double> bnd_xyz;  // coordinates of the non-active DOFs (3 per DOF)
   DBuf<int> gat_ptr, gat_idx, rgat_ptr, rgat_idx, diag_pos;
   void upload(pm_ctx* c, const DiscLevel& L, int dim, int nvc);
   void scratch_sizes(size_t& k_elems, size_t& f_elems) const;
 };
+
+// Dirichlet values of the quadratic exact solution (manufactured = 2) into the
+// non-active entries of rhs; nothing for the other coefficient kinds
+void launch_dirichlet_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs);
 
 // assemble matrix values and right-hand side of one level; K and F are scratch
 // arrays of n_cells*nloc*nloc and n_cells*nloc doubles

@@ -283,6 +283,17 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
     std::vector<char> act(L.space.n_dofs, 0);
     for (int i = 0; i < L.space.n_active; ++i) act[i] = 1;
     build_gather(L, L.space.nloc, L.space.dofmap, act);
+    const int dim = D->h.dim;
+    // lattice coordinates to physical ones the way cell_vertices converts them
+    const int64_t S = D->h.scale;
+    const double inv = 1.0 / double(S);
+    const bool pow2 = (S & (S - 1)) == 0;
+    L.bnd_xyz.assign(size_t(L.space.n_dofs - L.space.n_active) * 3, 0.0);
+    for (int i = L.space.n_active; i < L.space.n_dofs; ++i)
+      for (int d = 0; d < dim; ++d) {
+        const double v = double(L.space.node[size_t(i) * dim + d]);
+        L.bnd_xyz[size_t(i - L.space.n_active) * 3 + d] = pow2 ? v * inv : v / double(S);
+      }
     L.n_blocks = 1;
     L.block_len[0] = L.space.n_dofs;
     L.block_active[0] = L.space.n_active;

@@ -26,6 +26,10 @@ struct DiscLevel {
   std::vector<int> rgat_ptr, rgat_idx;
   // Dirichlet rows: CSR position of the diagonal entry
   std::vector<int> diag_pos;
+  // convection-diffusion: physical coordinates (x, y, z; z = 0 in 2D) of the
+  // non-active DOFs n_active .. n_dofs-1, the points of the nodal functionals
+  // the Dirichlet values are taken at
+  std::vector<double> bnd_xyz;
   // prolongation to the next finer level (rows of the finer level)
   pmsetup::Csr P;
   // Stokes block layout of the combined vector [u1 | u2 | u3 | p]

@@ -42,6 +42,12 @@ def lib() -> C.CDLL:
                                        C.POINTER(i32), C.POINTER(f64), vp, i32, C.POINTER(i32)]
         L.orc_prolongate_flat.argtypes = [i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]
         L.orc_restrict_flat.argtypes = [i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]
+        L.orc_assemble_cd_poly.argtypes = [i32, i32, i32, i32, vp, i32, vp, i32, i32, vp, vp, f64, vp, f64,
+                                           i32, f64, vp, vp, vp]
+        L.orc_poly_u.argtypes = [vp, vp]
+        L.orc_poly_u.restype = f64
+        L.orc_poly_rhs.argtypes = [i32, vp, f64, vp, f64, vp]
+        L.orc_poly_rhs.restype = f64
         L.orc_sor_sweep.argtypes = [i32, vp, vp, vp, vp, vp, f64, vp, i32]
         L.orc_sor_sweep.restype = i32
         L.orc_mg_set_sor.argtypes = [vp, i32, vp, f64]
@@ -140,7 +146,9 @@ class OracleCD:
 
     def __init__(self, geometry: int, root_n: int, n_refine: int, n_levels: int, elem: int,
                  eps: float, b=(0.0, 0.0, 0.0), c: float = 0.0, quad_points: int = 3,
-                 manufactured: bool = True, f_const: float = 0.0):
+                 manufactured: bool = True, f_const: float = 0.0, poly=None):
+        """poly: ten coefficients (1, x, y, z, x^2, y^2, z^2, xy, xz, yz) of a
+        quadratic exact solution; f and the Dirichlet values then come from it"""
         self.geometry = geometry
         self.dim = 2 if geometry == refsetup.GEO_SQUARE_QUAD else 3
         self.elem = elem
@@ -149,10 +157,17 @@ class OracleCD:
         self.b = np.array(list(b) + [0.0] * (3 - len(b)), dtype=np.float64)
         self.qn = quad_points
         self.manufactured, self.f_const = manufactured, f_const
+        self.poly = None if poly is None else np.array(list(poly) + [0.0] * (10 - len(poly)), dtype=np.float64)
         self.vals = []
         self.rhs = []
         self._mg = None
         self._keep = []
+
+    def exact(self, x) -> float:
+        """the quadratic exact solution at one point"""
+        X = np.zeros(3)
+        X[: len(x)] = x
+        return lib().orc_poly_u(_p(self.poly), _p(X))
 
     @property
     def finest(self):
@@ -166,11 +181,18 @@ class OracleCD:
             rhs = np.zeros(lv.n_dofs, dtype=np.float64)
             verts = np.ascontiguousarray(lv.verts, dtype=np.float64)
             dm = np.ascontiguousarray(lv.dofmap, dtype=np.int32)
-            rc = L.orc_assemble_cd(self.dim, self.elem, self.qn, lv.n_cells, _p(verts), lv.nloc, _p(dm),
-                                   lv.n_dofs, lv.n_active, _p(lv.row_ptr), _p(lv.cols), self.eps, _p(self.b),
-                                   self.c, int(self.manufactured), self.f_const, _p(vals), _p(rhs))
+            manuf = 2 if self.poly is not None else int(self.manufactured)
+            rc = L.orc_assemble_cd_poly(self.dim, self.elem, self.qn, lv.n_cells, _p(verts), lv.nloc, _p(dm),
+                                        lv.n_dofs, lv.n_active, _p(lv.row_ptr), _p(lv.cols), self.eps,
+                                        _p(self.b), self.c, manuf, self.f_const,
+                                        None if self.poly is None else _p(self.poly), _p(vals), _p(rhs))
             if rc != 0:
                 raise RuntimeError(f"oracle assembly failed ({rc})")
+            if self.poly is not None:
+                # Dirichlet values: point values of the exact solution at the
+                # nodes of the non-active DOFs (Assemble3D.C:640-665)
+                for i in range(lv.n_active, lv.n_dofs):
+                    rhs[i] = self.exact(lv.node_coords[i])
             self.vals.append(vals)
             self.rhs.append(rhs)
 

@@ -134,9 +134,40 @@ static int qk_eval(int dim, int k, const double* xi, double* phi, double* dx, do
 
 /* exact solution u = prod sin(pi x_d) and f = -eps*Lap u + b.grad u + c u in
  * the order of the example callbacks (include/Examples/CD_2D/SineLaplace.h) */
+/* quadratic exact solution u = p0 + p1 x + p2 y + p3 z + p4 x^2 + p5 y^2 +
+ * p6 z^2 + p7 xy + p8 xz + p9 yz (the test_p0 / test_p1 / test_p2 examples of
+ * src/Examples/Example_CD3D.C:164-193 are of this form) */
+double orc_poly_u(const double* p, const double* x) {
+  double u = p[0];
+  u += p[1] * x[0];
+  u += p[2] * x[1];
+  u += p[3] * x[2];
+  u += p[4] * x[0] * x[0];
+  u += p[5] * x[1] * x[1];
+  u += p[6] * x[2] * x[2];
+  u += p[7] * x[0] * x[1];
+  u += p[8] * x[0] * x[2];
+  u += p[9] * x[1] * x[2];
+  return u;
+}
+
+double orc_poly_rhs(int dim, const double* xin, double eps, const double* b, double c, const double* p) {
+  const double x[3] = {xin[0], xin[1], dim == 3 ? xin[2] : 0.0};
+  const double u = orc_poly_u(p, x);
+  const double ux = p[1] + 2 * p[4] * x[0] + p[7] * x[1] + p[8] * x[2];
+  const double uy = p[2] + 2 * p[5] * x[1] + p[7] * x[0] + p[9] * x[2];
+  const double uz = p[3] + 2 * p[6] * x[2] + p[8] * x[0] + p[9] * x[1];
+  const double lap = dim == 3 ? 2 * (p[4] + p[5] + p[6]) : 2 * (p[4] + p[5]);
+  double f = -eps * lap;
+  f += b[0] * ux + b[1] * uy + (dim == 3 ? b[2] * uz : 0.0);
+  f += c * u;
+  return f;
+}
+
 static double rhs_f(int dim, const double* x, double eps, const double* b, double c, int manuf,
-                    double fconst) {
+                    double fconst, const double* poly) {
   if (!manuf) return fconst;
+  if (manuf == 2) return orc_poly_rhs(dim, x, eps, b, c, poly);
   const double p = 3.14159265358979323846;
   double u, ux, uy, uz = 0, lap;
   if (dim == 2) {
@@ -163,10 +194,27 @@ static double rhs_f(int dim, const double* x, double eps, const double* b, doubl
  * BilinearAssembleGalerkin<d> (ConvDiff.C:1794-1856). Affine cells: QuadAffin
  * (src/FE/QuadAffin.C:614) / HexaAffin (src/FE/HexaAffin.C:858).
  * verts: n_cells * nv * dim; dofmap: n_cells * nloc. vals / rhs are reset. */
+int orc_assemble_cd_poly(int dim, int k, int qn, int n_cells, const double* verts, int nloc,
+                         const int* dofmap, int n_rows, int n_active, const int* rp, const int* ci,
+                         double eps, const double* b, double c, int manuf, double fconst, const double* poly,
+                         double* vals, double* rhs);
+
 int orc_assemble_cd(int dim, int k, int qn, int n_cells, const double* verts, int nloc,
                     const int* dofmap, int n_rows, int n_active, const int* rp, const int* ci,
                     double eps, const double* b, double c, int manuf, double fconst, double* vals,
                     double* rhs) {
+  if (manuf == 2) return -2; /* the polynomial needs orc_assemble_cd_poly */
+  return orc_assemble_cd_poly(dim, k, qn, n_cells, verts, nloc, dofmap, n_rows, n_active, rp, ci, eps, b, c,
+                              manuf, fconst, NULL, vals, rhs);
+}
+
+/* the same; manuf = 2 takes f from the quadratic exact solution `poly` (its
+ * Dirichlet values are set by the caller: the non-active rhs entries stay 0) */
+int orc_assemble_cd_poly(int dim, int k, int qn, int n_cells, const double* verts, int nloc,
+                         const int* dofmap, int n_rows, int n_active, const int* rp, const int* ci,
+                         double eps, const double* b, double c, int manuf, double fconst, const double* poly,
+                         double* vals, double* rhs) {
+  if (manuf == 2 && !poly) return -2;
   double xq[3 * MAXQ], wq[MAXQ];
   const int nq = gauss_rule(dim, qn, xq, wq);
   if (nq < 0) return -1;
@@ -224,7 +272,7 @@ int orc_assemble_cd(int dim, int k, int qn, int n_cells, const double* verts, in
       double X[3] = {x0[0], x0[1], dim == 3 ? x0[2] : 0.0};
       for (int d = 0; d < dim; ++d)
         for (int a = 0; a < dim; ++a) X[d] += J[d][a] * xq[3 * q + a];
-      const double f = rhs_f(dim, X, eps, b, c, manuf, fconst);
+      const double f = rhs_f(dim, X, eps, b, c, manuf, fconst, poly);
       const double Mult = wq[q] * adet;
       double ux[MAXNB], uy[MAXNB], uz[MAXNB];
       for (int i = 0; i < nloc; ++i) {

@@ -67,3 +67,28 @@ def test_noalloc_assembly_rejects_levels_beyond_its_scratch():
         prob.close()
     finally:
         ctx.close()
+
+
+def test_noalloc_assembly_writes_the_dirichlet_values():
+    """the quadratic exact-solution example (x^2 + yz, example -3 of
+    test/cd3d_solvers_test.c++): the Dirichlet rows of the right-hand side get
+    the exact solution's values, as in the allocating assembly"""
+    ctx = m.Context(0)
+    try:
+        disc = m.Discretization(m.GEO_CUBE_HEXA, 1, 2, 2, m.KIND_CD, 2)
+        cf = m.cd_coeffs(1.0, (4.0, 3.0, 2.0), 1.0, True, poly=[0, 0, 0, 0, 1.0, 0, 0, 0, 0, 1.0])
+        prob = m.ConvectionDiffusion(ctx, disc, cf, "solver_type: direct\n", quad_points=3)
+        info = disc.level_info(1)
+        rp, ci = disc.structure(1)
+        A = m.FEMatrix.from_csr(ctx, rp, ci, None, n_active=info["n_active"])
+        rhs = m.DeviceVector(ctx, info["n_dofs"])
+        m.assemble_cd(ctx, disc, 1, cf, 3, A, rhs)
+        vals = m.DeviceVector(ctx, info["nnz"])
+        r = m.DeviceVector(ctx, info["n_dofs"])
+        prob.assemble_level_noalloc(1, vals, r, cf)
+        assert rel(vals.numpy(), A.values()) <= TOL
+        assert rel(r.numpy(), rhs.numpy()) <= TOL
+        assert np.abs(r.numpy()[info["n_active"]:]).max() > 0.5
+        prob.close()
+    finally:
+        ctx.close()
