@@ -254,8 +254,11 @@ int pm_disc_prolongation(const pm_disc* d, int level, int* row_ptr, int* cols, d
  *     g = u at the Dirichlet DOFs (the point values of the Lagrange nodal
  *     functionals, Assemble3D.C:640-665). The examples test_p0 / test_p1 /
  *     test_p2 of Example_CD3D.C:164-193 (exact solution in Q1 / Q2).
- * poly is read only with manufactured = 2 (a caller built against a header
- * without it passes the smaller struct safely with 0 or 1). */
+ *     With manufactured = 2, poly_src (same monomials) is added to f: the time
+ *     derivative of a time-dependent exact solution (zero for stationary
+ *     problems).
+ * poly and poly_src are read only with manufactured = 2 (a caller built
+ * against a header without them passes the smaller struct safely with 0 or 1). */
 typedef struct pm_cd_coeffs {
   double eps;
   double b[3];
@@ -263,6 +266,7 @@ typedef struct pm_cd_coeffs {
   int manufactured;
   double f_const;
   double poly[10];
+  double poly_src[10];
 } pm_cd_coeffs;
 
 /* Assemble2D / Assemble3D with LocalAssembling (ConvDiff Galerkin,
@@ -327,6 +331,34 @@ int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* coeffs, const double*
 /* Solver statistics of the problem's last solve. */
 int pm_problem_last_info(const pm_problem* p, int* iterations, double* residual,
                          double* initial_residual);
+
+/* ------------------------------------------- time-dependent problem ------ */
+/* TimeConvectionDiffusion<d> (src/System/TimeConvectionDiffusion.C) with
+ * TimeDiscretization (src/TimeDiscRoutines/TimeDiscretizations.C):
+ * backward_euler, crank_nicolson, bdf_two. params: the solver keys of
+ * pm_problem_create_cd plus time_discretization, time_step_length,
+ * time_start, time_end. poly_time (20 doubles or NULL): P1, P2 of the exact
+ * solution u = P0 + t P1 + t^2 P2 with coeffs->manufactured = 2 (P0 =
+ * coeffs->poly); f and the Dirichlet values follow from u at the current time.
+ * The time loop of the reference's test programs
+ * (test/tcd3d_solvers_test.c++:76-92) reads:
+ *   pm_tcd_assemble_initial_time(s);
+ *   while (time < time_end - 1e-10) { pm_tcd_next_step(s); pm_tcd_assemble(s); pm_tcd_solve(s); } */
+typedef struct pm_tcd pm_tcd;
+int pm_tcd_create(pm_ctx* ctx, const pm_disc* d, const pm_cd_coeffs* coeffs, const double* poly_time,
+                  int quad_points, const char* params, pm_tcd** out);
+void pm_tcd_destroy(pm_tcd* s);
+/* assemble_initial_time: stiffness, mass, rhs; solution = initial condition */
+int pm_tcd_assemble_initial_time(pm_tcd* s);
+/* current_step_++, set_time_disc_parameters, current_time += tau */
+int pm_tcd_next_step(pm_tcd* s);
+/* assemble: stiffness and rhs at the current time, time-discrete rhs, system matrices */
+int pm_tcd_assemble(pm_tcd* s);
+/* solve, then reset_linear_matrices and the old solutions */
+int pm_tcd_solve(pm_tcd* s);
+int pm_tcd_state(const pm_tcd* s, double* time, int* step);
+/* the underlying problem: solution, matrices, solver statistics */
+int pm_tcd_problem(pm_tcd* s, pm_problem** out);
 
 /* ---------------------------------------------------------------------------
  * Request executor (no reference counterpart: the batched stream and the

@@ -37,7 +37,8 @@ class PmError(RuntimeError):
 
 class CdCoeffs(C.Structure):
     _fields_ = [("eps", C.c_double), ("b", C.c_double * 3), ("c", C.c_double),
-                ("manufactured", C.c_int), ("f_const", C.c_double), ("poly", C.c_double * 10)]
+                ("manufactured", C.c_int), ("f_const", C.c_double), ("poly", C.c_double * 10),
+                ("poly_src", C.c_double * 10)]
 
 
 class Request(C.Structure):
@@ -139,6 +140,14 @@ _SIGS = {
     "pm_problem_solution_dev": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "pm_problem_run_host": (i32, [vp, C.POINTER(CdCoeffs), vp, vp]),
     "pm_problem_last_info": (i32, [vp, pi32, pf64, pf64]),
+    "pm_tcd_create": (i32, [vp, vp, C.POINTER(CdCoeffs), vp, i32, C.c_char_p, C.POINTER(vp)]),
+    "pm_tcd_destroy": (None, [vp]),
+    "pm_tcd_assemble_initial_time": (i32, [vp]),
+    "pm_tcd_next_step": (i32, [vp]),
+    "pm_tcd_assemble": (i32, [vp]),
+    "pm_tcd_solve": (i32, [vp]),
+    "pm_tcd_state": (i32, [vp, pf64, pi32]),
+    "pm_tcd_problem": (i32, [vp, C.POINTER(vp)]),
     "pm_server_create": (i32, [i32, i32, C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
     "pm_server_destroy": (None, [vp]),
     "pm_server_submit": (i32, [vp, C.POINTER(Request)]),

@@ -410,14 +410,18 @@ class Discretization:
 
 
 def cd_coeffs(eps: float, b=(0.0, 0.0, 0.0), c: float = 0.0, manufactured: bool = True,
-              f_const: float = 0.0, poly=None) -> CdCoeffs:
+              f_const: float = 0.0, poly=None, poly_src=None) -> CdCoeffs:
     """poly: the ten coefficients of a quadratic exact solution (1, x, y, z, x^2,
-    y^2, z^2, xy, xz, yz); f and the Dirichlet values then come from it"""
+    y^2, z^2, xy, xz, yz); f and the Dirichlet values then come from it;
+    poly_src (same monomials) is added to f"""
     cf = CdCoeffs()
     if poly is not None:
         p = list(poly) + [0.0] * (10 - len(poly))
+        q = [] if poly_src is None else list(poly_src)
+        q = q + [0.0] * (10 - len(q))
         for i in range(10):
             cf.poly[i] = p[i]
+            cf.poly_src[i] = q[i]
     cf.eps = eps
     bb = list(b) + [0.0] * (3 - len(b))
     for i in range(3):
@@ -515,6 +519,71 @@ class ConvectionDiffusion:
         except Exception:
             pass
 
+
+
+class TimeConvectionDiffusion(ConvectionDiffusion):
+    """TimeConvectionDiffusion<d> on one GPU (src/System/TimeConvectionDiffusion.C)
+    with TimeDiscretization's backward_euler, crank_nicolson and bdf_two. The
+    database carries the solver keys and time_discretization,
+    time_step_length, time_start, time_end. poly_time = (P1, P2) makes the
+    exact solution u = P0 + t P1 + t^2 P2 (P0 = the coefficients' poly).
+
+    The time loop of the reference's tests:
+        tcd.assemble_initial_time()
+        while tcd.current_time < tcd.end_time - 1e-10:
+            tcd.next_time_step(); tcd.assemble(); tcd.solve()
+    """
+
+    def __init__(self, ctx: Context, disc: Discretization, coeffs: CdCoeffs, db, quad_points: int = 0,
+                 poly_time=None):
+        self.ctx = ctx
+        self.disc = disc
+        self.coeffs = coeffs
+        text = _db_text(db)
+        pt = None
+        if poly_time is not None:
+            p1, p2 = [list(v) + [0.0] * (10 - len(v)) for v in poly_time]
+            pt = np.ascontiguousarray(p1 + p2, dtype=np.float64)
+        self._pt = pt
+        h = C.c_void_p()
+        check(lib.pm_tcd_create(ctx.handle, disc.handle, C.byref(coeffs), None if pt is None else _ptr(pt),
+                                quad_points, text.encode(), C.byref(h)), ctx.handle)
+        self.tcd = h
+        ph = C.c_void_p()
+        check(lib.pm_tcd_problem(self.tcd, C.byref(ph)))
+        self.handle = ph
+        prm = dict(line.split(":", 1) for line in text.splitlines() if ":" in line)
+        self.end_time = float(prm.get("time_end", 1.0))
+
+    def assemble_initial_time(self) -> None:
+        check(lib.pm_tcd_assemble_initial_time(self.tcd), self.ctx.handle)
+
+    def next_time_step(self) -> None:
+        check(lib.pm_tcd_next_step(self.tcd), self.ctx.handle)
+
+    def assemble(self) -> None:
+        check(lib.pm_tcd_assemble(self.tcd), self.ctx.handle)
+
+    def solve(self) -> None:
+        check(lib.pm_tcd_solve(self.tcd), self.ctx.handle)
+
+    @property
+    def current_time(self) -> float:
+        t, k = C.c_double(), C.c_int()
+        check(lib.pm_tcd_state(self.tcd, C.byref(t), C.byref(k)))
+        return t.value
+
+    @property
+    def current_step(self) -> int:
+        t, k = C.c_double(), C.c_int()
+        check(lib.pm_tcd_state(self.tcd, C.byref(t), C.byref(k)))
+        return k.value
+
+    def close(self) -> None:
+        if self.tcd and self.ctx.handle:
+            lib.pm_tcd_destroy(self.tcd)
+        self.tcd = None
+        self.handle = None
 
 class StokesProblem(ConvectionDiffusion):
     """NavierStokes<3> for the Stokes problem (P2/P1 on tetrahedra) on one GPU:

@@ -98,12 +98,16 @@ struct CdCoef {
   double eps, b0, b1, b2, c, fconst;
   int manufactured;  // 0: f = fconst; 1: sine exact solution; 2: quadratic exact solution
   double poly[10];   // 1, x, y, z, x^2, y^2, z^2, xy, xz, yz
+  double src[10];    // added to f (time derivative of the exact solution)
 };
 
 static CdCoef make_coef(const pm_cd_coeffs& cf) {
-  CdCoef k{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured, {}};
+  CdCoef k{cf.eps, cf.b[0], cf.b[1], cf.b[2], cf.c, cf.f_const, cf.manufactured, {}, {}};
   if (cf.manufactured == 2)
-    for (int i = 0; i < 10; ++i) k.poly[i] = cf.poly[i];
+    for (int i = 0; i < 10; ++i) {
+      k.poly[i] = cf.poly[i];
+      k.src[i] = cf.poly_src[i];
+    }
   return k;
 }
 
@@ -135,6 +139,7 @@ __device__ __forceinline__ double poly_rhs(const CdCoef& k, int dim, const doubl
   double f = -k.eps * lap;
   f += k.b0 * ux + k.b1 * uy + (dim == 3 ? k.b2 * uz : 0.0);
   f += k.c * u;
+  f += poly_u(k.src, x);
   return f;
 }
 
@@ -492,6 +497,8 @@ __global__ void k_dirichlet_poly(int nb, int n_active, const double* __restrict_
   const double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
   rhs[n_active + i] = poly_u(co.poly, x);
 }
+
+double poly_value_host(const double* p, const double* x) { return poly_u(p, x); }
 
 void launch_dirichlet_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs) {
   const int nb = int(L.bnd_xyz.n / 3);

@@ -37,6 +37,10 @@ struct DevAssemblyLevel {
   void scratch_sizes(size_t& k_elems, size_t& f_elems) const;
 };
 
+// value of the quadratic polynomial p (1, x, y, z, x^2, y^2, z^2, xy, xz, yz)
+// at x (the evaluation the device kernels use)
+double poly_value_host(const double* p, const double* x);
+
 // Dirichlet values of the quadratic exact solution (manufactured = 2) into the
 // non-active entries of rhs; nothing for the other coefficient kinds
 void launch_dirichlet_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs);

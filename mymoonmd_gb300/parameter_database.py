@@ -56,6 +56,16 @@ _GPU_DEFAULTS: dict[str, tuple[Any, tuple | None]] = {
     "gpu_mixed_fallback": (1, (0, 1)),
 }
 
+# TimeDiscretization::default_TimeDiscretization_database
+# (src/TimeDiscRoutines/TimeDiscretizations.C:23-56); fractional_step is not
+# implemented on the GPU
+_TIME_DEFAULTS: dict[str, tuple[Any, tuple | None]] = {
+    "time_start": (0.0, None),
+    "time_end": (1.0, None),
+    "time_step_length": (0.05, None),
+    "time_discretization": ("backward_euler", ("backward_euler", "crank_nicolson", "bdf_two")),
+}
+
 
 class ParameterDatabase:
     """Typed key/value store; unknown keys may be added with `add`."""
@@ -129,6 +139,10 @@ class ParameterDatabase:
     @staticmethod
     def default_gpu_database() -> "ParameterDatabase":
         return ParameterDatabase._from(_GPU_DEFAULTS, "gpu database")
+
+    @staticmethod
+    def default_time_database() -> "ParameterDatabase":
+        return ParameterDatabase._from(_TIME_DEFAULTS, "default time discretization database")
 
     @staticmethod
     def solve_path_database() -> "ParameterDatabase":

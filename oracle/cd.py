@@ -46,7 +46,7 @@ def lib() -> C.CDLL:
                                            i32, f64, vp, vp, vp]
         L.orc_poly_u.argtypes = [vp, vp]
         L.orc_poly_u.restype = f64
-        L.orc_poly_rhs.argtypes = [i32, vp, f64, vp, f64, vp]
+        L.orc_poly_rhs.argtypes = [i32, vp, f64, vp, f64, vp, vp]
         L.orc_poly_rhs.restype = f64
         L.orc_sor_sweep.argtypes = [i32, vp, vp, vp, vp, vp, f64, vp, i32]
         L.orc_sor_sweep.restype = i32
@@ -146,9 +146,10 @@ class OracleCD:
 
     def __init__(self, geometry: int, root_n: int, n_refine: int, n_levels: int, elem: int,
                  eps: float, b=(0.0, 0.0, 0.0), c: float = 0.0, quad_points: int = 3,
-                 manufactured: bool = True, f_const: float = 0.0, poly=None):
+                 manufactured: bool = True, f_const: float = 0.0, poly=None, poly_src=None):
         """poly: ten coefficients (1, x, y, z, x^2, y^2, z^2, xy, xz, yz) of a
-        quadratic exact solution; f and the Dirichlet values then come from it"""
+        quadratic exact solution; f and the Dirichlet values then come from it;
+        poly_src (same monomials) is added to f"""
         self.geometry = geometry
         self.dim = 2 if geometry == refsetup.GEO_SQUARE_QUAD else 3
         self.elem = elem
@@ -157,7 +158,11 @@ class OracleCD:
         self.b = np.array(list(b) + [0.0] * (3 - len(b)), dtype=np.float64)
         self.qn = quad_points
         self.manufactured, self.f_const = manufactured, f_const
-        self.poly = None if poly is None else np.array(list(poly) + [0.0] * (10 - len(poly)), dtype=np.float64)
+        self.poly = None
+        if poly is not None:
+            src = [] if poly_src is None else list(poly_src)
+            self.poly = np.array(list(poly) + [0.0] * (10 - len(poly)) + src + [0.0] * (10 - len(src)),
+                                 dtype=np.float64)
         self.vals = []
         self.rhs = []
         self._mg = None

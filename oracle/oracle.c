@@ -151,7 +151,8 @@ double orc_poly_u(const double* p, const double* x) {
   return u;
 }
 
-double orc_poly_rhs(int dim, const double* xin, double eps, const double* b, double c, const double* p) {
+double orc_poly_rhs(int dim, const double* xin, double eps, const double* b, double c, const double* p,
+                    const double* src) {
   const double x[3] = {xin[0], xin[1], dim == 3 ? xin[2] : 0.0};
   const double u = orc_poly_u(p, x);
   const double ux = p[1] + 2 * p[4] * x[0] + p[7] * x[1] + p[8] * x[2];
@@ -161,13 +162,14 @@ double orc_poly_rhs(int dim, const double* xin, double eps, const double* b, dou
   double f = -eps * lap;
   f += b[0] * ux + b[1] * uy + (dim == 3 ? b[2] * uz : 0.0);
   f += c * u;
+  if (src) f += orc_poly_u(src, x);
   return f;
 }
 
 static double rhs_f(int dim, const double* x, double eps, const double* b, double c, int manuf,
                     double fconst, const double* poly) {
   if (!manuf) return fconst;
-  if (manuf == 2) return orc_poly_rhs(dim, x, eps, b, c, poly);
+  if (manuf == 2) return orc_poly_rhs(dim, x, eps, b, c, poly, poly ? poly + 10 : NULL);
   const double p = 3.14159265358979323846;
   double u, ux, uy, uz = 0, lap;
   if (dim == 2) {
@@ -208,8 +210,10 @@ int orc_assemble_cd(int dim, int k, int qn, int n_cells, const double* verts, in
                               manuf, fconst, NULL, vals, rhs);
 }
 
-/* the same; manuf = 2 takes f from the quadratic exact solution `poly` (its
- * Dirichlet values are set by the caller: the non-active rhs entries stay 0) */
+/* the same; manuf = 2 takes f from the quadratic exact solution poly[0..9]
+ * plus the source polynomial poly[10..19] (the time derivative of a
+ * time-dependent exact solution); the Dirichlet values are set by the
+ * caller: the non-active rhs entries stay 0 */
 int orc_assemble_cd_poly(int dim, int k, int qn, int n_cells, const double* verts, int nloc,
                          const int* dofmap, int n_rows, int n_active, const int* rp, const int* ci,
                          double eps, const double* b, double c, int manuf, double fconst, const double* poly,

@@ -49,7 +49,7 @@ def test_polynomial_rhs_equals_the_examples_formula(example):
     rng = np.random.default_rng(example + 10)
     for x in rng.random((20, 3)):
         x = np.ascontiguousarray(x)
-        f = ocd.lib().orc_poly_rhs(3, ocd._p(x), eps, ocd._p(bb), c, ocd._p(p))
+        f = ocd.lib().orc_poly_rhs(3, ocd._p(x), eps, ocd._p(bb), c, ocd._p(p), None)
         assert abs(f - reference_rhs(example, *x)) <= 1e-14 * max(1.0, abs(f))
 
 
