@@ -20,6 +20,11 @@
         one warm-up request, then one request of the 3D Stokes P2/P1 workload
         (24^3 cubes x 6 tetrahedra, 368,572 DOFs, 3 levels, V(1,1) Vanka);
         --cubes 12 runs the 12^3 mesh of the same family
+    python -m mymoonmd_gb300.profile_cases tcd [--precision mixed|fp64] [--scheme ...]
+        time-dependent convection-diffusion on the 3D Q2 32^3 mesh (4 levels,
+        the request's solver): initial assembly, then 6 time steps of 0.01
+        (the first is a warm-up), each assembly + time-discrete rhs + system
+        matrices + solve + reset, timed with CUDA events
 
 Each case prints what it ran; device memory stays below 2 GB.
 """
@@ -72,7 +77,8 @@ def problem2d(ctx, precision="mixed"):
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["request", "request2d", "request3d_cluster", "spmv", "assembly", "stokes",
-                                     "sliced"])
+                                     "sliced", "tcd"])
+    ap.add_argument("--scheme", default="crank_nicolson", choices=["backward_euler", "crank_nicolson", "bdf_two"])
     ap.add_argument("--shapes", default="0,140,141,180,240,241,280,440,441,480,481,840,841,881")
     ap.add_argument("--pdl", type=int, default=1, choices=[0, 1, 2])
     ap.add_argument("--cluster", type=int, default=8, choices=[1, 2, 4, 8])
@@ -86,6 +92,30 @@ def main() -> None:
     ctx = m.Context(0)
     ctx.set_option("pdl", args.pdl)
     ctx.set_option("sliced_min_entries", args.min_entries)
+    if args.case == "tcd":
+        db = _db(args.precision)
+        db.merge(ParameterDatabase.default_time_database())
+        db["time_discretization"] = args.scheme
+        db["time_step_length"] = 0.01
+        db["time_end"] = 0.06
+        disc = m.Discretization(m.GEO_CUBE_HEXA, 1, 5, 4, m.KIND_CD, 2)
+        cf = m.cd_coeffs(1e-2, (1.0, 0.5, 0.25), 0.0, True)
+        tcd = m.TimeConvectionDiffusion(ctx, disc, cf, db, quad_points=3)
+        tcd.assemble_initial_time()
+        times, its = [], []
+        while tcd.current_time < 0.06 - 1e-10:
+            ctx.time_begin()
+            tcd.next_time_step()
+            tcd.assemble()
+            tcd.solve()
+            times.append(ctx.time_end())
+            its.append(tcd.last_info()[0])
+        steady = times[1:]
+        print(f"tcd {args.scheme} {args.precision}: {np.mean(steady):.2f} ms per time step "
+              f"(min {min(steady):.2f}, {len(steady)} steps after a warm-up), FGMRES iterations {its}")
+        tcd.close()
+        ctx.close()
+        return
     if args.case == "stokes":
         db = _db(args.precision)
         db["multigrid_n_levels"] = 3
