@@ -1288,6 +1288,28 @@ void pm_solver::sor_iter(const double* rhs, double* sol, bool symmetric) {
   }
 }
 
+// Iteration_richardson::iterate (src/Solver/Iteration_richardson.C:24-110):
+// x += damping * P^{-1}(b - A x) with the configured preconditioner
+void pm_solver::richardson(const double* rhs, double* sol) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  ensure_work(2, n);
+  double *r = work.p, *z = r + work_n;
+  double normb = std::sqrt(dot_host(c, n, rhs, rhs));
+  if (normb == 0.0) normb = 1.0;
+  csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+  double resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+  if (converged(resid, 0)) return;
+  for (unsigned i = 1; i <= (unsigned long)max_it; ++i) {
+    precondition(r, z, false);
+    vaxpy(c, n, damping, z, sol);
+    csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+    resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+    if (converged(resid, i)) return;
+  }
+}
+
 void pm_solver::solve(const double* rhs, double* sol) {
   if (!A) throw Error(PM_E_INVALID, "Solver::solve called before update_matrix");
   history.clear();
@@ -1306,5 +1328,6 @@ void pm_solver::solve(const double* rhs, double* sol) {
   else if (method == "bi_cgstab") bicgstab(rhs, sol);
   else if (method == "jacobi") jacobi_iter(rhs, sol);
   else if (method == "sor" || method == "ssor") sor_iter(rhs, sol, method == "ssor");
+  else if (method == "richardson") richardson(rhs, sol);
   else throw Error(PM_E_UNSUPPORTED, "iterative_solver_type '" + method + "' is not implemented on the GPU");
 }

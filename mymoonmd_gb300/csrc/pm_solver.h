@@ -162,4 +162,5 @@ struct pm_solver {
   void bicgstab(const double* rhs, double* sol);
   void jacobi_iter(const double* rhs, double* sol);
   void sor_iter(const double* rhs, double* sol, bool symmetric);
+  void richardson(const double* rhs, double* sol);
 };

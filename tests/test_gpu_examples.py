@@ -29,6 +29,16 @@ def solver_db(name, precision="fp64"):
     if name == "direct":
         db["solver_type"] = "direct"
         return db
+    if name == "jacobi":
+        # set_solver_globals("jacobi"), test/cd3d_solvers_test.c++:75-84
+        db["solver_type"] = "iterative"
+        db["iterative_solver_type"] = "richardson"
+        db["preconditioner"] = "jacobi"
+        db["residual_tolerance"] = 1e-10
+        db["residual_reduction"] = 0.0
+        db["max_n_iterations"] = 1000
+        db["min_n_iterations"] = 5
+        return db
     db["solver_type"] = "iterative"
     db["iterative_solver_type"] = "fgmres"
     db["preconditioner"] = "multigrid"
@@ -68,7 +78,7 @@ def test_polynomial_example_assembly_matches_oracle(ctx, example):
     prob.close()
 
 
-@pytest.mark.parametrize("solver,tol", [("multigrid", 1e-12), ("direct", 1e-13)])
+@pytest.mark.parametrize("solver,tol", [("multigrid", 1e-12), ("direct", 1e-13), ("jacobi", 1e-8)])
 @pytest.mark.parametrize("example", [-1, -2, -3])
 def test_cd3d_solvers_polynomial_examples_solved_exactly(ctx, example, solver, tol):
     disc, cf, prob, ora = gpu_example(ctx, example, solver_db(solver))

@@ -124,7 +124,8 @@ def test_sor_iteration_matches_oracle(ctx, method):
     assert rel(prob.solution(), sol) <= 1e-10
 
 
-@pytest.mark.parametrize("method", ["fgmres", "right_gmres", "cg", "bi_cgstab", "jacobi", "sor", "ssor"])
+@pytest.mark.parametrize("method", ["fgmres", "right_gmres", "cg", "bi_cgstab", "jacobi", "sor", "ssor",
+                                    "richardson"])
 def test_reference_test_system_with_ssor_preconditioner(ctx, method):
     """test/iterative_solver_test.c++:104-160: the 7x7 block system with
     preconditioner ssor and sor_omega 1.25; error <= 100 * residual_tolerance"""
