@@ -795,6 +795,10 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
     p->disc = d;
     p->kind = KIND_STOKES;
     p->nu = nu;
+    // Example_NSE3D's "example" key: -3 is the polynomial solution in P2 / P1
+    p->stokes_example = int(Params::parse(params ? params : "").integer("example", 0));
+    if (p->stokes_example != 0 && p->stokes_example != -3)
+      throw Error(PM_E_UNSUPPORTED, "Stokes example must be 0 (manufactured) or -3 (test_u_2_p_1)");
     const Disc& D = *d->d;
     const int nl = int(D.levels.size());
     p->stab.upload(c);
@@ -876,7 +880,8 @@ int pm_problem_assemble(pm_problem* p) {
     // NavierStokes<3>::assemble_linear_terms for the Stokes problem
     for (int l = 0; l < nl; ++l) {
       double* r = (l == nl - 1) ? p->rhs.p : p->rhs_coarse.p;
-      assemble_stokes_level(c, p->slev[l], p->stab, p->nu, p->mats[l]->csr, r, p->K.p, p->F.p);
+      assemble_stokes_level(c, p->slev[l], p->stab, p->nu, p->mats[l]->csr, r, p->K.p, p->F.p,
+                            p->stokes_example);
     }
     const DevCsr& top = p->mats.back()->csr;
     copy_nonactive(c, top.n_rows, top.mask, p->rhs.p, p->sol.p);

@@ -82,6 +82,21 @@ static inline int stokes_pos(int c, int m, int k) {
   return -1;
 }
 
+// physical coordinates of the non-active DOFs of L.space (lattice coordinates
+// converted the way cell_vertices converts them)
+static void fill_bnd_xyz(const Hierarchy& h, DiscLevel& L) {
+  const int dim = h.dim;
+  const int64_t S = h.scale;
+  const double inv = 1.0 / double(S);
+  const bool pow2 = (S & (S - 1)) == 0;
+  L.bnd_xyz.assign(size_t(L.space.n_dofs - L.space.n_active) * 3, 0.0);
+  for (int i = L.space.n_active; i < L.space.n_dofs; ++i)
+    for (int d = 0; d < dim; ++d) {
+      const double v = double(L.space.node[size_t(i) * dim + d]);
+      L.bnd_xyz[size_t(i - L.space.n_active) * 3 + d] = pow2 ? v * inv : v / double(S);
+    }
+}
+
 static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L) {
   L.space = build_space(h, lvl, EL_P2, BND_DIRICHLET);
   L.pspace = build_space(h, lvl, EL_P1, BND_NEUMANN);
@@ -266,6 +281,7 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
       L.n_cells = D->h.levels[first + l].n_cells;
       L.verts = cell_vertices(D->h, first + l);
       build_stokes_level(D->h, first + l, L);
+      fill_bnd_xyz(D->h, L);
     }
     for (int l = 0; l + 1 < n_levels; ++l) build_stokes_transfer(D->h, D->levels[l], D->levels[l + 1]);
     return D;
@@ -283,17 +299,7 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
     std::vector<char> act(L.space.n_dofs, 0);
     for (int i = 0; i < L.space.n_active; ++i) act[i] = 1;
     build_gather(L, L.space.nloc, L.space.dofmap, act);
-    const int dim = D->h.dim;
-    // lattice coordinates to physical ones the way cell_vertices converts them
-    const int64_t S = D->h.scale;
-    const double inv = 1.0 / double(S);
-    const bool pow2 = (S & (S - 1)) == 0;
-    L.bnd_xyz.assign(size_t(L.space.n_dofs - L.space.n_active) * 3, 0.0);
-    for (int i = L.space.n_active; i < L.space.n_dofs; ++i)
-      for (int d = 0; d < dim; ++d) {
-        const double v = double(L.space.node[size_t(i) * dim + d]);
-        L.bnd_xyz[size_t(i - L.space.n_active) * 3 + d] = pow2 ? v * inv : v / double(S);
-      }
+    fill_bnd_xyz(D->h, L);
     L.n_blocks = 1;
     L.block_len[0] = L.space.n_dofs;
     L.block_active[0] = L.space.n_active;

@@ -26,9 +26,9 @@ struct DiscLevel {
   std::vector<int> rgat_ptr, rgat_idx;
   // Dirichlet rows: CSR position of the diagonal entry
   std::vector<int> diag_pos;
-  // convection-diffusion: physical coordinates (x, y, z; z = 0 in 2D) of the
-  // non-active DOFs n_active .. n_dofs-1, the points of the nodal functionals
-  // the Dirichlet values are taken at
+  // physical coordinates (x, y, z; z = 0 in 2D) of the non-active DOFs
+  // n_active .. n_dofs-1 of `space` (for Stokes the velocity component space),
+  // the points of the nodal functionals the Dirichlet values are taken at
   std::vector<double> bnd_xyz;
   // prolongation to the next finer level (rows of the finer level)
   pmsetup::Csr P;

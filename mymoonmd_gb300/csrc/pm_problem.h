@@ -14,6 +14,7 @@ struct pm_problem {
   int kind = 0;  // 0 convection-diffusion, 1 Stokes
   pm_cd_coeffs coeffs{};
   double nu = 1.0;  // Stokes viscosity
+  int stokes_example = 0;  // 0: manufactured sine velocity; -3: polynomial (test_u_2_p_1)
   int qn = 3;
   std::vector<pm::DevStokesLevel> slev;
   pm::DevStokesTables stab;

@@ -117,10 +117,20 @@ void DevStokesLevel::upload(pm_ctx* c, const DiscLevel& L) {
   rgat_ptr.upload(L.rgat_ptr, c->stream);
   rgat_idx.upload(L.rgat_idx, c->stream);
   diag_pos.upload(L.diag_pos, c->stream);
+  nvel = L.block_len[0];
+  nvel_active = L.block_active[0];
+  bnd_xyz.upload(L.bnd_xyz, c->stream);
 }
 
 // right-hand side f = -nu Lap u + grad p of the manufactured Stokes solution
-__device__ void stokes_f(double nu, const double* x, double* f) {
+__device__ void stokes_f(double nu, const double* x, double* f, int example) {
+  if (example == -3) {
+    // u = (y^2, xz, -y^2): Lap u = (2, 0, -2); grad p = (1, 1, 1)
+    f[0] = -nu * 2.0 + 1.0;
+    f[1] = -nu * 0.0 + 1.0;
+    f[2] = -nu * -2.0 + 1.0;
+    return;
+  }
   const double p = 3.14159265358979323846;
   double S[3], S1[3], S2[3], S3[3];
   for (int d = 0; d < 3; ++d) {
@@ -146,7 +156,7 @@ __device__ void stokes_f(double nu, const double* x, double* f) {
 template <int CHUNK>
 __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* __restrict__ verts,
                                                      const double* __restrict__ tab, double nu,
-                                                     double* __restrict__ K, double* __restrict__ F) {
+                                                     double* __restrict__ K, double* __restrict__ F, int example) {
   __shared__ double cS[CHUNK][6];
   __shared__ double cB[CHUNK][9];
   __shared__ double geo[CHUNK][13];
@@ -202,7 +212,7 @@ __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* 
       x[d] = s;
     }
     double f[3];
-    stokes_f(nu, x, f);
+    stokes_f(nu, x, f, example);
     const double m = tab[kOffW + q] * geo[cl][12];
     for (int d = 0; d < 3; ++d) fq[cl][q][d] = m * f[d];
   }
@@ -245,11 +255,24 @@ __global__ void k_unit_diag(int n, const int* __restrict__ pos, double* __restri
   if (i < n) vals[pos[i]] = 1.0;
 }
 
+// Dirichlet values of example -3 at the non-active velocity DOFs of the three
+// components ([u1 | u2 | u3 | p] layout)
+__global__ void k_stokes_dirichlet(int nb, int nvel, int nact, const double* __restrict__ xyz,
+                                   double* __restrict__ rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  rhs[nact + i] = y * y;
+  rhs[nvel + nact + i] = x * z;
+  rhs[2 * nvel + nact + i] = -y * y;
+}
+
 void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu,
-                           DevCsr& A, double* rhs, double* K, double* F) {
+                           DevCsr& A, double* rhs, double* K, double* F, int example) {
   constexpr int CHUNK = 32;
+  if (example != 0 && example != -3) throw Error(PM_E_UNSUPPORTED, "Stokes example must be 0 or -3");
   k_elem_stokes<CHUNK><<<(L.n_cells + CHUNK - 1) / CHUNK, 256, 0, c->stream>>>(L.n_cells, L.verts.p, t.data.p,
-                                                                              nu, K, F);
+                                                                              nu, K, F, example);
   PM_CHECK_LAUNCH();
   const int nnz = int(A.nnz);
   const int g = std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16));
@@ -264,6 +287,12 @@ void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTa
   k_gather_stokes<<<gr, 256, 0, c->stream>>>(L.n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
   PM_CHECK_LAUNCH();
   c->kernel_launches += nd ? 4 : 3;
+  const int nb = L.nvel - L.nvel_active;
+  if (example == -3 && nb > 0) {
+    k_stokes_dirichlet<<<(nb + 255) / 256, 256, 0, c->stream>>>(nb, L.nvel, L.nvel_active, L.bnd_xyz.p, rhs);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
   A.values_changed(c);
 }
 

@@ -15,7 +15,9 @@ struct DevStokesTables {
 // device copy of one Stokes level's assembly inputs
 struct DevStokesLevel {
   int n_cells = 0, n = 0;
+  int nvel = 0, nvel_active = 0;  // DOFs and active DOFs of one velocity component
   DBuf<double> verts;
+  DBuf<double> bnd_xyz;  // coordinates of the non-active velocity DOFs
   DBuf<int> gat_ptr, gat_idx, rgat_ptr, rgat_idx, diag_pos;
   void upload(pm_ctx* c, const DiscLevel& L);
 };
@@ -23,9 +25,12 @@ struct DevStokesLevel {
 // element matrices (220 doubles per cell) and element right-hand sides (34)
 // of -nu Lap u + grad p = f, div u = 0 with f from the manufactured
 // velocity u = curl(psi (1,1,1)), psi = (sin pi x sin pi y sin pi z)^2 and
-// pressure p = x + y + z - 3/2; then gather into the combined CSR
+// pressure p = x + y + z - 3/2 (example 0), or from the polynomial solution
+// u = (y^2, xz, -y^2), p = x + y + z - 3/2 of the reference's example -3
+// (include/Examples/NSE_3D/test_u_2_p_1.h, u in P2, p in P1) with its
+// Dirichlet values u(node); then gather into the combined CSR
 void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu,
-                           DevCsr& A, double* rhs, double* K, double* F);
+                           DevCsr& A, double* rhs, double* K, double* F, int example = 0);
 
 // get_combined_submatrix: the combined matrix with the first pressure row
 // replaced by the unit row (pressure projection, all-Dirichlet velocity)

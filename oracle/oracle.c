@@ -1345,7 +1345,15 @@ void orc_vanka_sweep(int type, int n_patches, const int* patch, int n, const int
  * ([u1 | u2 | u3 | p] numbering). Right-hand side of the manufactured
  * solution u = curl(psi (1,1,1)), psi = (sin pi x sin pi y sin pi z)^2,
  * p = x + y + z - 3/2. */
-static void stokes_f(double nu, const double* x, double* f) {
+static void stokes_f(double nu, const double* x, double* f, int example) {
+  if (example == -3) {
+    /* include/Examples/NSE_3D/test_u_2_p_1.h: u = (y^2, xz, -y^2),
+     * p = x + y + z - 3/2: f = -nu Lap u + grad p */
+    f[0] = -nu * 2.0 + 1.0;
+    f[1] = -nu * 0.0 + 1.0;
+    f[2] = -nu * -2.0 + 1.0;
+    return;
+  }
   const double p = 3.14159265358979323846;
   double S[3], S1[3], S2[3], S3[3];
   for (int d = 0; d < 3; ++d) {
@@ -1394,8 +1402,19 @@ static int add_entry(const int* rp, const int* ci, double* vals, int row, int co
   return -1;
 }
 
+int orc_assemble_stokes_ex(int n_cells, const double* verts, double nu, const int* cdof, int n_rows,
+                           const unsigned char* active, const int* rp, const int* ci, double* vals, double* rhs,
+                           int example);
 int orc_assemble_stokes(int n_cells, const double* verts, double nu, const int* cdof, int n_rows,
                         const unsigned char* active, const int* rp, const int* ci, double* vals, double* rhs) {
+  return orc_assemble_stokes_ex(n_cells, verts, nu, cdof, n_rows, active, rp, ci, vals, rhs, 0);
+}
+
+/* the same for example 0 (manufactured) or -3 (polynomial; the Dirichlet
+ * values are set by the caller) */
+int orc_assemble_stokes_ex(int n_cells, const double* verts, double nu, const int* cdof, int n_rows,
+                           const unsigned char* active, const int* rp, const int* ci, double* vals, double* rhs,
+                           int example) {
   memset(vals, 0, sizeof(double) * (size_t)rp[n_rows]);
   memset(rhs, 0, sizeof(double) * (size_t)n_rows);
   for (int cell = 0; cell < n_cells; ++cell) {
@@ -1432,7 +1451,7 @@ int orc_assemble_stokes(int n_cells, const double* verts, double nu, const int* 
       double X[3];
       for (int d = 0; d < 3; ++d) X[d] = v[d] + J[d][0] * xi + J[d][1] * et + J[d][2] * ze;
       double f[3];
-      stokes_f(nu, X, f);
+      stokes_f(nu, X, f, example);
       const double Mult = P4W[q] * adet;
       for (int i = 0; i < 10; ++i)
         for (int j = 0; j < 10; ++j) A[i][j] += Mult * nu * (ux[i] * ux[j] + uy[i] * uy[j] + uz[i] * uz[j]);

@@ -46,6 +46,8 @@ def lib() -> C.CDLL:
         vp, i32, f64 = C.c_void_p, C.c_int, C.c_double
         L.orc_assemble_stokes.argtypes = [i32, vp, f64, vp, i32, vp, vp, vp, vp, vp]
         L.orc_assemble_stokes.restype = i32
+        L.orc_assemble_stokes_ex.argtypes = [i32, vp, f64, vp, i32, vp, vp, vp, vp, vp, i32]
+        L.orc_assemble_stokes_ex.restype = i32
         L.orc_vanka_sweep.argtypes = [i32, i32, vp, i32, vp, vp, vp, vp, vp, f64, vp, vp, i32, vp]
         L.orc_mg_set_smoothers.argtypes = [vp, i32, i32, f64]
         L.orc_mg_set_vanka.argtypes = [vp, i32, vp, vp, vp, vp, i32, vp, vp, i32, vp, vp]
@@ -227,9 +229,13 @@ def vanka_sweep(kind: str, lv: StokesLevel, pvals: np.ndarray, b: np.ndarray, x:
 class OracleStokes:
     """NavierStokes<3> (Stokes, Laplace form) restated on the CPU."""
 
-    def __init__(self, root_n: int, n_refine: int, n_levels: int, nu: float = 1.0):
+    def __init__(self, root_n: int, n_refine: int, n_levels: int, nu: float = 1.0, example: int = 0):
+        """example 0: the manufactured sine velocity; -3: the polynomial
+        solution u = (y^2, xz, -y^2), p = x + y + z - 3/2 of
+        include/Examples/NSE_3D/test_u_2_p_1.h with its Dirichlet values"""
         self.levels = stokes_levels(root_n, n_refine, n_levels)
         self.nu = nu
+        self.example = example
         self.vals, self.pvals, self.rhs = [], [], []
         self._mg = None
         self._keep = []
@@ -244,10 +250,16 @@ class OracleStokes:
         for lv in self.levels:
             vals = np.zeros(lv.cols.size)
             rhs = np.zeros(lv.n)
-            rc = L.orc_assemble_stokes(lv.n_cells, _p(lv.verts), self.nu, _p(lv.cdof), lv.n, _p(lv.active),
-                                       _p(lv.row_ptr), _p(lv.cols), _p(vals), _p(rhs))
+            rc = L.orc_assemble_stokes_ex(lv.n_cells, _p(lv.verts), self.nu, _p(lv.cdof), lv.n, _p(lv.active),
+                                          _p(lv.row_ptr), _p(lv.cols), _p(vals), _p(rhs), self.example)
             if rc != 0:
                 raise RuntimeError(f"oracle Stokes assembly failed ({rc})")
+            if self.example == -3:
+                # Dirichlet values: the exact velocity at the non-active nodes
+                X = lv.ucoords[lv.nu_active:] / lv.ucoords.max()
+                x, y, z = X[:, 0], X[:, 1], X[:, 2]
+                for b, val in enumerate((y * y, x * z, -y * y)):
+                    rhs[b * lv.nu + lv.nu_active: (b + 1) * lv.nu] = val
             self.vals.append(vals)
             self.pvals.append(np.ascontiguousarray(lv.project(vals)))
             self.rhs.append(rhs)
