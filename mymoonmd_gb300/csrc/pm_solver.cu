@@ -1310,6 +1310,65 @@ void pm_solver::richardson(const double* rhs, double* sol) {
   }
 }
 
+// Iteration_cgs::iterate (src/Solver/Iteration_cgs.C:22-110): conjugate
+// gradient squared with right preconditioning
+void pm_solver::cgs(const double* rhs, double* sol) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  ensure_work(9, n);
+  double* r = work.p;
+  double* rt = r + work_n;
+  double* p = rt + work_n;
+  double* ph = p + work_n;
+  double* q = ph + work_n;
+  double* u = q + work_n;
+  double* uh = u + work_n;
+  double* qh = uh + work_n;
+  double* vh = qh + work_n;
+  csr_apply(c, M, EPI_DEFECT, sol, r, rhs, 1.0);
+  vcopy(c, n, r, rt);
+  double normb = std::sqrt(dot_host(c, n, rhs, rhs));
+  if (normb == 0.0) normb = 1.0;
+  double resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+  if (converged(resid, 0)) return;
+  double rho_2 = 0.0;
+  for (unsigned i = 1; i <= (unsigned long)max_it; ++i) {
+    const double rho_1 = dot_host(c, n, rt, r);
+    if (rho_1 == 0.0) {
+      last_it = int(i);
+      last_res = std::sqrt(dot_host(c, n, r, r)) / normb;
+      return;
+    }
+    if (i == 1) {
+      vcopy(c, n, r, u);
+      vcopy(c, n, u, p);
+    } else {
+      const double beta = rho_1 / rho_2;
+      vcopy(c, n, q, u);
+      vscale(c, n, u, beta);
+      vaxpy(c, n, 1.0, r, u);     // u = beta q + r
+      vscale(c, n, p, beta);
+      vaxpy(c, n, 1.0, q, p);
+      vscale(c, n, p, beta);
+      vaxpy(c, n, 1.0, u, p);     // p = beta (beta p + q) + u
+    }
+    precondition(p, ph);
+    csr_apply(c, M, EPI_SET, ph, vh, nullptr, 1.0);
+    const double alpha = rho_1 / dot_host(c, n, rt, vh);
+    vcopy(c, n, u, q);
+    vaxpy(c, n, -alpha, vh, q);   // q = u - alpha vhat
+    vaxpy(c, n, 1.0, q, u);       // u = u + q
+    precondition(u, uh);
+    vaxpy(c, n, alpha, uh, sol);
+    csr_apply(c, M, EPI_SET, uh, qh, nullptr, 1.0);
+    vaxpy(c, n, -alpha, qh, r);   // r += -alpha qhat
+    rho_2 = rho_1;
+    resid = std::sqrt(dot_host(c, n, r, r)) / normb;
+    if (converged(resid, i)) return;
+  }
+}
+
 void pm_solver::solve(const double* rhs, double* sol) {
   if (!A) throw Error(PM_E_INVALID, "Solver::solve called before update_matrix");
   history.clear();
@@ -1329,5 +1388,6 @@ void pm_solver::solve(const double* rhs, double* sol) {
   else if (method == "jacobi") jacobi_iter(rhs, sol);
   else if (method == "sor" || method == "ssor") sor_iter(rhs, sol, method == "ssor");
   else if (method == "richardson") richardson(rhs, sol);
+  else if (method == "cgs") cgs(rhs, sol);
   else throw Error(PM_E_UNSUPPORTED, "iterative_solver_type '" + method + "' is not implemented on the GPU");
 }

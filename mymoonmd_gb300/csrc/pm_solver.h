@@ -163,4 +163,5 @@ struct pm_solver {
   void jacobi_iter(const double* rhs, double* sol);
   void sor_iter(const double* rhs, double* sol, bool symmetric);
   void richardson(const double* rhs, double* sol);
+  void cgs(const double* rhs, double* sol);
 };
