@@ -170,7 +170,8 @@ int pm_scal(pm_ctx* ctx, int n, double a, double* x_dev);
  *   preconditioner: multigrid    residual_reduction: 1e-8
  * Implemented: iterative_solver_type fgmres (right_gmres), cg, bi_cgstab,
  * jacobi, sor, ssor, richardson (x += damping_factor P^-1 (b - A x),
- * src/Solver/Iteration_richardson.C), cgs (src/Solver/Iteration_cgs.C); preconditioner no_preconditioner, jacobi, sor, ssor,
+ * src/Solver/Iteration_richardson.C), cgs (src/Solver/Iteration_cgs.C),
+ * left_gmres (Iteration_gmres::left_gmres, preconditioned residual); preconditioner no_preconditioner, jacobi, sor, ssor,
  * multigrid; multigrid_smoother(_coarse) jacobi, sor, ssor, cell_vanka,
  * cell_vanka_jacobi, nodal_vanka, nodal_vanka_jacobi, direct_solve (coarse).
  * SOR and SSOR (TMatrix::sor_sweep, src/Matrix/Matrix.C:943, omega =

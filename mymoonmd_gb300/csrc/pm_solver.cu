@@ -1369,6 +1369,86 @@ void pm_solver::cgs(const double* rhs, double* sol) {
   }
 }
 
+// Iteration_gmres::left_gmres (src/Solver/Iteration_gmres.C:173-268): GMRES on
+// P^{-1} A with the preconditioned residual as the stopping quantity; the
+// Arnoldi step is the reference's modified Gram-Schmidt (v_k scaled by h,
+// subtracted, scaled back), host Givens rotations
+void pm_solver::left_gmres(const double* rhs, double* sol) {
+  pm_ctx* c = ctx;
+  const DevCsr& M = A->csr;
+  const int n = M.n_rows;
+  const int m = int(restart);
+  ensure_work(size_t(m) + 4, n);
+  double* a = work.p;
+  double* w = a + work_n;
+  double* r = w + work_n;
+  auto V = [&](int k) { return r + size_t(k + 1) * work_n; };
+  std::vector<double> Hm(size_t(m + 1) * size_t(m + 1), 0.0), s(size_t(m) + 1), cs(size_t(m) + 1),
+      sn(size_t(m) + 1);
+  auto Hij = [&](int i, int j) -> double& { return Hm[size_t(i) * size_t(m + 1) + size_t(j)]; };
+  auto gen = [](double dx, double dy, double& c_, double& s_) {
+    if (dy == 0.0) { c_ = 1.0; s_ = 0.0; }
+    else if (std::fabs(dy) > std::fabs(dx)) { const double t = dx / dy; s_ = 1.0 / std::sqrt(1.0 + t * t); c_ = t * s_; }
+    else { const double t = dy / dx; c_ = 1.0 / std::sqrt(1.0 + t * t); s_ = t * c_; }
+  };
+  auto app = [](double& dx, double& dy, double c_, double s_) {
+    const double t = c_ * dx + s_ * dy;
+    dy = -s_ * dx + c_ * dy;
+    dx = t;
+  };
+  // x += sum_k y_k v_k with H y = s (upper triangular, rows 0..k)
+  auto update = [&](int k) {
+    std::vector<double> y(s.begin(), s.end());
+    for (int i = k; i >= 0; --i) {
+      y[size_t(i)] /= Hij(i, i);
+      for (int j = i - 1; j >= 0; --j) y[size_t(j)] -= Hij(j, i) * y[size_t(i)];
+    }
+    for (int j = 0; j <= k; ++j) vaxpy(c, n, y[size_t(j)], V(j), sol);
+  };
+  csr_apply(c, M, EPI_DEFECT, sol, a, rhs, 1.0);
+  precondition(a, r);
+  double resid = std::sqrt(dot_host(c, n, r, r));
+  double beta = resid;
+  if (converged(resid, 0)) return;
+  unsigned j = 1;
+  while (j <= (unsigned long)max_it) {
+    vcopy(c, n, r, V(0));
+    vscale(c, n, V(0), 1.0 / beta);
+    std::fill(s.begin(), s.end(), 0.0);
+    s[0] = beta;
+    for (int i = 0; i < m && j <= (unsigned long)max_it; ++i, ++j) {
+      csr_apply(c, M, EPI_SET, V(i), a, nullptr, 1.0);
+      precondition(a, w);
+      for (int k = 0; k <= i; ++k) {
+        const double h = dot_host(c, n, w, V(k));
+        Hij(k, i) = h;
+        if (h != 0.0) {
+          vscale(c, n, V(k), h);
+          vaxpy(c, n, -1.0, V(k), w);
+          vscale(c, n, V(k), 1.0 / h);
+        }
+      }
+      Hij(i + 1, i) = std::sqrt(dot_host(c, n, w, w));
+      vcopy(c, n, w, V(i + 1));
+      vscale(c, n, V(i + 1), 1.0 / Hij(i + 1, i));
+      for (int k = 0; k < i; ++k) app(Hij(k, i), Hij(k + 1, i), cs[size_t(k)], sn[size_t(k)]);
+      gen(Hij(i, i), Hij(i + 1, i), cs[size_t(i)], sn[size_t(i)]);
+      app(Hij(i, i), Hij(i + 1, i), cs[size_t(i)], sn[size_t(i)]);
+      app(s[size_t(i)], s[size_t(i) + 1], cs[size_t(i)], sn[size_t(i)]);
+      resid = std::fabs(s[size_t(i) + 1]);
+      if (converged(resid, j)) {
+        update(i);
+        return;
+      }
+    }
+    update(m - 1);
+    csr_apply(c, M, EPI_DEFECT, sol, a, rhs, 1.0);
+    precondition(a, r);
+    beta = std::sqrt(dot_host(c, n, r, r));
+    if (converged(resid, j)) return;
+  }
+}
+
 void pm_solver::solve(const double* rhs, double* sol) {
   if (!A) throw Error(PM_E_INVALID, "Solver::solve called before update_matrix");
   history.clear();
@@ -1389,5 +1469,6 @@ void pm_solver::solve(const double* rhs, double* sol) {
   else if (method == "sor" || method == "ssor") sor_iter(rhs, sol, method == "ssor");
   else if (method == "richardson") richardson(rhs, sol);
   else if (method == "cgs") cgs(rhs, sol);
+  else if (method == "left_gmres") left_gmres(rhs, sol);
   else throw Error(PM_E_UNSUPPORTED, "iterative_solver_type '" + method + "' is not implemented on the GPU");
 }

@@ -164,4 +164,5 @@ struct pm_solver {
   void sor_iter(const double* rhs, double* sol, bool symmetric);
   void richardson(const double* rhs, double* sol);
   void cgs(const double* rhs, double* sol);
+  void left_gmres(const double* rhs, double* sol);
 };

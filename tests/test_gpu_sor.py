@@ -125,7 +125,7 @@ def test_sor_iteration_matches_oracle(ctx, method):
 
 
 @pytest.mark.parametrize("method", ["fgmres", "right_gmres", "cg", "bi_cgstab", "jacobi", "sor", "ssor",
-                                    "richardson", "cgs"])
+                                    "richardson", "cgs", "left_gmres"])
 def test_reference_test_system_with_ssor_preconditioner(ctx, method):
     """test/iterative_solver_test.c++:104-160: the 7x7 block system with
     preconditioner ssor and sor_omega 1.25; error <= 100 * residual_tolerance"""
@@ -162,11 +162,13 @@ def test_sor_on_a_zero_diagonal_is_refused(ctx):
 
 
 @pytest.mark.parametrize("prec", ["jacobi", "ssor"])
-def test_cgs_solution_matches_oracle(ctx, prec):
-    """iterative_solver_type cgs (Iteration_cgs::iterate) on the 2D Q1 case to a
-    1e-10 reduction: the solution agrees with the oracle's FGMRES solution to
-    a 1e-12 reduction within 1e-8"""
-    disc, prob, ora = make_pair(ctx, "q1_2d", krylov_db("cgs", prec, 1.2, 1e-10, 500))
+@pytest.mark.parametrize("method", ["cgs", "left_gmres"])
+def test_cgs_and_left_gmres_solutions_match_oracle(ctx, method, prec):
+    """iterative_solver_type cgs (Iteration_cgs::iterate) and left_gmres
+    (Iteration_gmres::left_gmres, preconditioned residual) on the 2D Q1 case
+    to a 1e-10 reduction: the solution agrees with the oracle's FGMRES
+    solution to a 1e-12 reduction within 1e-8"""
+    disc, prob, ora = make_pair(ctx, "q1_2d", krylov_db(method, prec, 1.2, 1e-10, 500))
     prob.solve()
     it, res, init = prob.last_info()
     assert res <= 1e-10 * init and it < 500
