@@ -1,0 +1,116 @@
+"""Generate the golden fixtures that pin the solve path against the reference
+itself (ParMooN compiled by oracle/ref/build_ref.py; run where the reference
+sources are present).
+
+For each case the reference's own ConvectionDiffusion<d> (driver
+oracle/ref/ref_cd.C) builds the mesh hierarchy, the FE spaces and the CSR
+structures, assembles every multigrid level and solves with FGMRES +
+multigrid. The fixture keeps, per level:
+  * SHA-256 digests of GlobalNumbers (cell order, BeginIndex = c * nloc), the
+    CSR row pointers and column indices and the cell vertex coordinates - the
+    bit-exact contract;
+  * the assembled entries and the right-hand side: in full for the small cases,
+    as a fixed sample (SAMPLES indices) plus the largest magnitude for the
+    full-size ones;
+and for the solve: the FGMRES iteration count, the initial and final residual
+of the reference's LoopInfo and the solution (full or sampled).
+
+    python tests/golden/make_ref_fixtures.py            # all cases
+    python tests/golden/make_ref_fixtures.py cd3d_q2_8  # one case
+"""
+from __future__ import annotations
+
+import hashlib
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT / "oracle" / "ref"))
+
+SAMPLES = 4096
+
+# name: (dim, n_refine, element order, levels, eps, b, quadrature degree 2 x
+#        order (1) or the default 3 x order (0), restart, residual reduction, full arrays)
+CASES = {
+    # 3D Q2 32^3 convection-diffusion, 4 levels, FGMRES(30), 1e-8, Gauss 3x3x3
+    "cd3d_q2_32": (3, 5, 2, 4, 1e-2, (1.0, 0.5, 0.25), 1, 30, 1e-8, False),
+    # 2D Q1 128^2 convection-diffusion, 4 levels, FGMRES(20), 1e-10, Gauss 3x3
+    "cd2d_q1_128": (2, 7, 1, 4, 0.1, (1.0, 0.0, 0.0), 0, 20, 1e-10, False),
+    # smaller cases (the last three with every array in full)
+    "cd3d_q2_8": (3, 3, 2, 3, 0.1, (1.0, 0.5, 0.25), 1, 30, 1e-10, False),
+    "cd3d_q2_4": (3, 2, 2, 2, 0.1, (1.0, 0.5, 0.25), 1, 30, 1e-10, True),
+    "cd3d_q1_8": (3, 3, 1, 3, 0.05, (0.3, -1.0, 0.5), 1, 30, 1e-10, True),
+    "cd2d_q2_16": (2, 4, 2, 3, 0.02, (1.0, 0.5, 0.0), 1, 20, 1e-10, True),
+}
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def sample_idx(n: int) -> np.ndarray:
+    if n <= SAMPLES:
+        return np.arange(n, dtype=np.int64)
+    rng = np.random.default_rng(n)
+    return np.unique(np.concatenate([np.linspace(0, n - 1, SAMPLES // 2).astype(np.int64),
+                                     rng.integers(0, n, SAMPLES // 2)]))
+
+
+def run_case(name: str) -> None:
+    import build_ref
+    dim, nref, order, nlev, eps, b, quad_linear, restart, reduction, full = CASES[name]
+    exe = build_ref.link_program(str(dim), build_ref.HERE / "ref_cd.C", build_ref.OUT / f"ref_cd{dim}d")
+    with tempfile.TemporaryDirectory() as tmp:
+        cmd = [str(exe), tmp, str(nref), str(order), str(nlev), repr(eps), *map(repr, b), str(quad_linear),
+               "fgmres_mg", str(restart), repr(reduction)]
+        subprocess.run(cmd, check=True, capture_output=True)
+        meta = {}
+        for line in Path(tmp, "meta.txt").read_text().splitlines():
+            k, v = line.split(None, 1)
+            meta[k] = v
+        out: dict[str, np.ndarray] = {
+            "config": np.array([dim, nref, order, nlev, quad_linear, restart], dtype=np.int64),
+            "coeffs": np.array([eps, *b, reduction], dtype=np.float64),
+            "iterations": np.array(int(meta["iterations"])),
+            "initial_residual": np.array(float(meta["initial_residual"])),
+            "final_residual": np.array(float(meta["final_residual"])),
+        }
+        for rl in range(nlev):
+            lvl = nlev - 1 - rl  # 0 = coarsest, as the library counts levels
+            info = meta[f"L{rl}"].split()
+            kv = dict(zip(info[0::2], map(int, info[1::2])))
+            rd = lambda n, t: np.fromfile(Path(tmp, f"L{rl}_{n}"), dtype=t)
+            dm, rows, cols = rd("dofmap.i32", np.int32), rd("rows.i32", np.int32), rd("cols.i32", np.int32)
+            verts, vals, rhs = rd("verts.f64", np.float64), rd("vals.f64", np.float64), rd("rhs.f64", np.float64)
+            p = f"L{lvl}_"
+            out[p + "sizes"] = np.array([kv["cells"], kv["nloc"], kv["n_dofs"], kv["active"], kv["nnz"]], np.int64)
+            out[p + "digests"] = np.array([digest(dm), digest(rows), digest(cols), digest(verts)])
+            for key, arr in (("vals", vals), ("rhs", rhs)):
+                out[p + key + "_max"] = np.array(np.abs(arr).max())
+                if full:
+                    out[p + key] = arr
+                else:
+                    idx = sample_idx(arr.size)
+                    out[p + key + "_idx"] = idx
+                    out[p + key] = arr[idx]
+            if full:
+                out[p + "dofmap"], out[p + "rows"], out[p + "cols"] = dm, rows, cols
+        sol = np.fromfile(Path(tmp, "solution.f64"), dtype=np.float64)
+        out["solution_max"] = np.array(np.abs(sol).max())
+        if full:
+            out["solution"] = sol
+        else:
+            idx = sample_idx(sol.size)
+            out["solution_idx"], out["solution"] = idx, sol[idx]
+    np.savez_compressed(HERE / f"ref_{name}.npz", **out)
+    print(f"{name}: {int(out['iterations'])} iterations, final residual {float(out['final_residual']):.3e}")
+
+
+if __name__ == "__main__":
+    for n in (sys.argv[1:] or list(CASES)):
+        run_case(n)

@@ -1,0 +1,61 @@
+"""Loading the fixtures made by the compiled reference (tests/golden/ref_*.npz,
+generated by tests/golden/make_ref_fixtures.py) and mapping their
+configuration onto the library's and the oracle's arguments."""
+from __future__ import annotations
+
+import hashlib
+from pathlib import Path
+
+import numpy as np
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+# the reference's quadrature rule of a tensor element of order k:
+# degree = (2 if INTERNAL_PROBLEM_LINEAR else 3) * k, then
+# QF{Quad,Hexa}FromDegree (src/FE/FEDatabase2D.C:1629-1647,
+# src/FE/FEDatabase3D.C:977-994): degree 0-2 Gauss2, 3-5 Gauss3, 6-7 Gauss4
+_POINTS = {0: 2, 1: 2, 2: 2, 3: 3, 4: 3, 5: 3, 6: 4, 7: 4}
+
+
+def names() -> list[str]:
+    return sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_*.npz"))
+
+
+class RefCase:
+    def __init__(self, name: str):
+        self.name = name
+        self.z = np.load(GOLDEN / f"ref_{name}.npz")
+        dim, nref, order, nlev, quad_linear, restart = (int(v) for v in self.z["config"])
+        eps, b1, b2, b3, reduction = (float(v) for v in self.z["coeffs"])
+        self.dim, self.n_refine, self.order, self.n_levels = dim, nref, order, nlev
+        self.restart, self.reduction = restart, reduction
+        self.eps, self.b = eps, (b1, b2, b3)
+        self.quad_points = _POINTS[(2 if quad_linear else 3) * order]
+        self.geometry = 0 if dim == 2 else 1  # unit square (quads) / unit cube (hexahedra)
+        self.iterations = int(self.z["iterations"])
+        self.initial_residual = float(self.z["initial_residual"])
+        self.final_residual = float(self.z["final_residual"])
+
+    def has(self, key: str) -> bool:
+        return key in self.z.files
+
+    def level(self, l: int) -> dict:
+        p = f"L{l}_"
+        d = {k[len(p):]: self.z[k] for k in self.z.files if k.startswith(p)}
+        cells, nloc, n_dofs, active, nnz = (int(v) for v in d["sizes"])
+        d.update(cells=cells, nloc=nloc, n_dofs=n_dofs, active=active, nnz=nnz)
+        return d
+
+    def compare(self, key_prefix: str, got_full: np.ndarray, level: int | None = None) -> float:
+        """largest difference of `got_full` to the reference's entries (full or
+        sampled), relative to the reference's largest magnitude"""
+        pre = f"L{level}_" if level is not None else ""
+        ref = self.z[pre + key_prefix]
+        idx_key = pre + key_prefix + "_idx"
+        got = got_full[self.z[idx_key]] if idx_key in self.z.files else got_full
+        assert got.shape == ref.shape, (got.shape, ref.shape)
+        return float(np.abs(got - ref).max() / float(self.z[pre + key_prefix + "_max"]))
+
+
+def digest(a: np.ndarray, dtype) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=dtype).tobytes()).hexdigest()
