@@ -320,10 +320,6 @@ def run_ours(args, w, rank, world, local, pg):
     A.bench_apply(x32, y32, 5, fp32=True)
     msr, br = A.bench_apply(x32, y32, 50, fp32=True)
     ctx.set_option("fp32_sliced_spmv", SLICED_DEFAULT)
-    ctx.set_option("fp32_bulk_spmv", 1)
-    A.bench_apply(x32, y32, 5, fp32=True)
-    msb, bb = A.bench_apply(x32, y32, 50, fp32=True)
-    ctx.set_option("fp32_bulk_spmv", 0)
     big = None if stokes or args.no_large_spmv else large_spmv(ctx, m, np, hbm_peak)
 
     if rank != 0:
@@ -369,8 +365,7 @@ def run_ours(args, w, rank, world, local, pg):
                  "fp64_frac": round(b64 / (ms64 / 1e3) / 1e9 / hbm_peak, 3),
                  "fp32_frac": round(b32 / (ms32 / 1e3) / 1e9 / hbm_peak, 3),
                  "fp32_row_group_gbs": round(br / (msr / 1e3) / 1e9, 1),
-                 "fp32_bulk_copy_gbs": round(bb / (msb / 1e3) / 1e9, 1),
-                 "note": "fp32: the sliced-ELL kernel (library default); row_group and bulk_copy: the CSR kernels"},
+                 "note": "fp32: the sliced-ELL kernel (library default); row_group: the CSR kernel"},
         "spmv_4x_l2": big,
         "e2e": {"value": round(world * K / (e2e_ms / 1e3), 3), "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

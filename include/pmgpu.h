@@ -68,10 +68,6 @@ int pm_version(void);
  *   4 restriction, 5 prolongation add; -1 = all);
  *   "probe_precision" 0|4|8 - only launches whose matrix values have this
  *   size in bytes (0 = all);
- *   "fp32_bulk_spmv" 0|1 - FP32 SpMV-family launches on full matrices by the
- *   bulk-copy kernel (row chunks streamed into shared memory with
- *   cp.async.bulk) or by the per-row-group kernel (default 0); both give the
- *   same bits;
  *   "fp32_sliced_spmv" 0|100 L + 10 U + P - FP32 SpMV-family launches on
  *   matrices with more than 16 entries per row by the sliced-ELL kernel: L
  *   lanes per row (1, 2, 4, 8), U steps in flight (4, 8), P = 1 issues the next
@@ -81,11 +77,10 @@ int pm_version(void);
  *   slices of 32/L rows, padded to the slice's longest row) is laid out when
  *   the FP32 values are made (pm_matrix_make_fp32, the multigrid update) for
  *   the shape's L. Shapes with the same L give the same bits;
- *   "pdl" 0|1|2 - launches with programmatic stream serialization: 1 the
- *   sliced-ELL sweeps (a sweep loads its slice layout and first values while
- *   the previous kernel finishes, and waits for it before reading vectors), 2
- *   also the vector, conversion and Krylov kernels (default 1: on GB300 the
- *   3D Q2 request took 26.9 ms with 1, 27.6 ms with 0, 28.3 ms with 2);
+ *   "pdl" 0|1 - launches of the sliced-ELL sweeps with programmatic stream
+ *   serialization (a sweep loads its slice layout and first values while the
+ *   previous kernel finishes, and waits for it before reading vectors; default
+ *   1: on GB300 the 3D Q2 request took 26.9 ms with 1, 27.6 ms with 0);
  *   "fp64_sliced_spmv" 0|441|481|841 - the same for FP64 values (the Krylov
  *   SpMV, the FP64 multigrid); used when its L equals the layout's (default 441);
  *   "jacobi_zero_start" 0|1 - the first damped Jacobi sweep of a multigrid level
@@ -290,7 +285,10 @@ int pm_assemble_cd(pm_ctx* ctx, const pm_disc* d, int level, const pm_cd_coeffs*
  * levels needing more than 4 Mi doubles (n_cells*nloc*(nloc+1)) are rejected
  * with PM_E_INVALID. The first call on a device looks the array up and should
  * come before any stream capture; calls that overlap on the GPU race on the
- * shared array. coeffs == NULL keeps the problem's coefficients. */
+ * shared array. coeffs == NULL keeps the problem's coefficients. The element
+ * kernels are those pm_assemble_cd runs under the same context options, so
+ * both entry points give the same bits. Stokes problems are refused with
+ * PM_E_UNSUPPORTED. */
 int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coeffs* coeffs, double* vals_dev,
                            double* rhs_dev);
 

@@ -529,11 +529,14 @@ void DevAssemblyLevel::scratch_sizes(size_t& k_elems, size_t& f_elems) const {
   f_elems = size_t(n_cells) * nloc;
 }
 
-void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, int qn,
-                       const pm_cd_coeffs& cf, const DevRefTables& rt, DevCsr& A, double* rhs,
-                       double* K, double* F) {
+// Element matrices and element right-hand sides of one level into K and F: by
+// the reference-tensor contraction (default) or, with the context option
+// assembly_quadrature_loop, by the per-quadrature-point loop. Shared by
+// pm_assemble_cd / pm_problem_assemble and the allocation-free entry point,
+// so both give the same bits.
+void launch_cd_elements(pm_ctx* c, const DevAssemblyLevel& L, int dim, int k, int qn,
+                        const pm_cd_coeffs& cf, const DevRefTables& rt, double* K, double* F) {
   const CdCoef co = make_coef(cf);
-  const int k = elem;
   const double* T = rt.tensors.p;
   if (!c->assembly_quadrature_loop && T) {
     if (dim == 2 && k == 1 && qn == 3) launch_elem_tensor<2, 4, 9>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
@@ -554,6 +557,12 @@ void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, 
   else if (dim == 3 && k == 2 && qn == 3) launch_elem<3, 27, 27, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 3 && k == 2 && qn == 4) launch_elem<3, 27, 64, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else throw Error(PM_E_UNSUPPORTED, "element / quadrature combination not compiled");
+}
+
+void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, int qn,
+                       const pm_cd_coeffs& cf, const DevRefTables& rt, DevCsr& A, double* rhs,
+                       double* K, double* F) {
+  launch_cd_elements(c, L, dim, elem, qn, cf, rt, K, F);
   const int nnz = int(A.nnz);
   k_gather<<<std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16)), 256, 0, c->stream>>>(
       nnz, L.gat_ptr.p, L.gat_idx.p, K, A.vals.p);
@@ -645,22 +654,6 @@ static int noalloc_scratch(int device, double** out, std::string& err) {
   return PM_OK;
 }
 
-namespace pm {
-// element kernels of assemble_cd_level, for the allocation-free entry point
-static void noalloc_elements(pm_ctx* c, const DevAssemblyLevel& L, int dim, int k, int qn,
-                             const pm_cd_coeffs& cf, const DevRefTables& rt, double* K, double* F) {
-  const CdCoef co = make_coef(cf);
-  if (dim == 2 && k == 1 && qn == 3) launch_elem<2, 4, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else if (dim == 2 && k == 1 && qn == 2) launch_elem<2, 4, 4, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else if (dim == 2 && k == 2 && qn == 3) launch_elem<2, 9, 9, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else if (dim == 2 && k == 2 && qn == 4) launch_elem<2, 9, 16, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else if (dim == 3 && k == 1 && qn == 2) launch_elem<3, 8, 8, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else if (dim == 3 && k == 1 && qn == 3) launch_elem<3, 8, 27, 2>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else if (dim == 3 && k == 2 && qn == 3) launch_elem<3, 27, 27, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else if (dim == 3 && k == 2 && qn == 4) launch_elem<3, 27, 64, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
-  else throw Error(PM_E_UNSUPPORTED, "element / quadrature combination not compiled");
-}
-}  // namespace pm
 
 /* Assembly of one level of a convection-diffusion problem into caller-owned
  * device arrays, with no device allocation (see the comment block above).
@@ -679,6 +672,10 @@ extern "C" int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coef
   if (!p || !vals_dev || !rhs_dev) return PM_E_INVALID;
   pm_ctx* c = p->ctx;
   try {
+    if (p->kind != 0) {
+      c->last_error = "pm_assemble_cd_noalloc: convection-diffusion problems only";
+      return PM_E_UNSUPPORTED;
+    }
     if (level < 0 || level >= int(p->alev.size())) {
       c->last_error = "level out of range";
       return PM_E_INVALID;
@@ -697,7 +694,7 @@ extern "C" int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coef
     double* K = scratch;
     double* F = scratch + kn;
     const pm::Disc& D = *p->disc->d;
-    pm::noalloc_elements(c, L, D.dim(), D.elem, p->qn, coeffs ? *coeffs : p->coeffs, p->ref, K, F);
+    pm::launch_cd_elements(c, L, D.dim(), D.elem, p->qn, coeffs ? *coeffs : p->coeffs, p->ref, K, F);
     const int nnz = int(p->mats[level]->csr.nnz);
     pm::k_gather<<<std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16)), 256, 0, c->stream>>>(
         nnz, L.gat_ptr.p, L.gat_idx.p, K, vals_dev);

@@ -45,6 +45,11 @@ double poly_value_host(const double* p, const double* x);
 // non-active entries of rhs; nothing for the other coefficient kinds
 void launch_dirichlet_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs);
 
+// element matrices and element right-hand sides of one level into K and F, by
+// the kernel the context's assembly_quadrature_loop option selects
+void launch_cd_elements(pm_ctx* c, const DevAssemblyLevel& L, int dim, int k, int qn,
+                        const pm_cd_coeffs& cf, const DevRefTables& rt, double* K, double* F);
+
 // assemble matrix values and right-hand side of one level; K and F are scratch
 // arrays of n_cells*nloc*nloc and n_cells*nloc doubles
 void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, int qn,

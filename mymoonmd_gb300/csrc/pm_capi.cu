@@ -73,10 +73,6 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->assembly_quadrature_loop = value != 0;
     return PM_OK;
   }
-  if (std::string(key) == "fp32_bulk_spmv") {
-    c->bulk_spmv = value != 0;
-    return PM_OK;
-  }
   if (std::string(key) == "fp32_sliced_spmv") {
     static const int shapes[] = {0, 140, 141, 180, 240, 241, 280, 440, 441, 480, 481, 840, 841, 881};
     if (std::find(std::begin(shapes), std::end(shapes), value) == std::end(shapes))
@@ -113,7 +109,7 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     return PM_OK;
   }
   if (std::string(key) == "pdl") {
-    if (value < 0 || value > 2) return fail(c, PM_E_INVALID, "pdl is 0, 1 or 2");
+    if (value < 0 || value > 1) return fail(c, PM_E_INVALID, "pdl is 0 or 1");
     c->pdl = value;
     return PM_OK;
   }
@@ -355,7 +351,6 @@ int pm_matrix_apply_f32(pm_matrix* A, const float* x, float* y) {
   if (!A || !x || !y) return PM_E_INVALID;
   PM_TRY
   csr_apply32(A->ctx, A->csr, EPI_SET, x, y, nullptr, 1.0f);
-  check_device_error(A->ctx);
   return PM_OK;
   PM_CATCH(A->ctx)
 }
@@ -560,7 +555,6 @@ int pm_solver_solve(pm_solver* s, const double* rhs, double* sol) {
   if (!s || !rhs || !sol) return fail(s ? s->ctx : nullptr, PM_E_INVALID, "null argument");
   PM_TRY
   s->solve(rhs, sol);
-  check_device_error(s->ctx);
   return PM_OK;
   PM_CATCH(s->ctx)
 }
@@ -575,7 +569,6 @@ int pm_solver_solve_host(pm_solver* s, const double* rhs_h, double* sol_h, int n
   x.upload(sol_h, n, c->stream);
   s->solve(r.p, x.p);
   x.download(sol_h, c->stream);
-  check_device_error(c);
   return PM_OK;
   PM_CATCH(s->ctx)
 }
@@ -601,7 +594,6 @@ int pm_solver_apply_preconditioner(pm_solver* s, const double* z, double* r) {
   PM_TRY
   if (!s->A) throw Error(PM_E_INVALID, "preconditioner used before update_matrix");
   s->precondition(z, r);
-  check_device_error(s->ctx);
   return PM_OK;
   PM_CATCH(s->ctx)
 }
@@ -916,7 +908,6 @@ int pm_problem_solve(pm_problem* p) {
     p->solver_ready = true;
   }
   p->solver->solve(p->rhs.p, p->sol.p);
-  check_device_error(p->ctx);
   return PM_OK;
   PM_CATCH(p->ctx)
 }

@@ -113,8 +113,6 @@ struct pm_ctx {
   // while set (nullptr = none): a set flag turns those launches into no-ops
   const int* guard = nullptr;
   // set by kernels whose bounded waits gave up (checked after each solve)
-  pm::DBuf<int> dev_error;
-  bool bulk_spmv = false;  // FP32 SpMV by the bulk-copy kernel where a matrix allows it
   // FP32 SpMV by the sliced-ELL kernel: 0 = off, else 100 L + 10 U + P (L lanes
   // per row, U steps in flight, P = 1: next steps' loads issued before the
   // current gathers); the matrix copies are laid out for L in make_fp32
@@ -125,8 +123,8 @@ struct pm_ctx {
   // matrices with more entries per row than this on average get sliced copies
   // (option "sliced_min_entries")
   int sell_min_avg = 16;
-  // launches with programmatic stream serialization (option "pdl"): 0 none,
-  // 1 the sliced-ELL sweeps, 2 also the vector, conversion and Krylov kernels
+  // launches of the sliced-ELL sweeps with programmatic stream serialization
+  // (option "pdl": 0 off, 1 on)
   int pdl = 1;
   // first Jacobi sweep from an exactly zero iterate as a diagonal scaling
   // (option "jacobi_zero_start"; same bits as the full sweep)

@@ -22,25 +22,12 @@ void ctx_init(pm_ctx* c, int device) {
   c->dev_scalars.alloc(256);
   c->partials.alloc(4 * kRedBlocks);
   c->n_partials = kRedBlocks;
-  c->dev_error.alloc(1);
-  PM_CUDA(cudaMemsetAsync(c->dev_error.p, 0, sizeof(int), c->stream));
-}
-
-void check_device_error(pm_ctx* c) {
-  int h = 0;
-  PM_CUDA(cudaMemcpyAsync(&h, c->dev_error.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  PM_CUDA(cudaStreamSynchronize(c->stream));
-  if (h) {
-    PM_CUDA(cudaMemsetAsync(c->dev_error.p, 0, sizeof(int), c->stream));
-    throw Error(PM_E_TIMEOUT, "a bounded wait of a bulk-copy SpMV kernel gave up");
-  }
 }
 
 void ctx_destroy(pm_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->dev_scalars.release();
   c->partials.release();
-  c->dev_error.release();
   if (c->host_scalars) cudaFreeHost(c->host_scalars);
   c->host_scalars = nullptr;
   if (c->side) cudaStreamSynchronize(c->side);
@@ -69,8 +56,8 @@ void DevCsr::upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int*
   n_active = na;
   nnz = rp[nr];
   row_ptr.upload(rp, size_t(nr) + 1, c->stream);
-  // column indices readable up to nnz rounded up to 4 entries (bulk copies
-  // move 16-byte aligned spans); the tail holds zeros
+  // column indices readable up to nnz rounded up to 4 entries; the tail holds
+  // zeros
   cols.alloc(size_t(nnz4()));
   if (nnz) PM_CUDA(cudaMemcpyAsync(cols.p, ci, size_t(nnz) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   if (nnz4() > nnz)
@@ -96,28 +83,7 @@ void DevCsr::upload(pm_ctx* c, int nr, int nc, int na, const int* rp, const int*
   n_rblocks = rb.empty() ? 0 : int(rb.size()) - 1;
   if (n_rblocks) rblock.upload(rb, c->stream);
   else rblock.release();
-  std::vector<int> ch = build_bulk_chunks(nr, rp, kBulkEntries);
-  n_chunks = ch.empty() ? 0 : int(ch.size()) - 1;
-  if (n_chunks) chunk_rows.upload(ch, c->stream);
-  else chunk_rows.release();
   set_single_block();
-}
-
-std::vector<int> build_bulk_chunks(int n_rows, const int* rp, int max_entries) {
-  std::vector<int> ch;
-  if (n_rows <= 0) return ch;
-  ch.push_back(0);
-  int r0 = 0;
-  auto span = [&](int a, int b) { return ((rp[b] + 3) & ~3) - (rp[a] & ~3); };
-  for (int i = 0; i < n_rows; ++i) {
-    if (span(i, i + 1) > max_entries) return std::vector<int>();  // a row alone does not fit
-    if (span(r0, i + 1) > max_entries) {
-      ch.push_back(i);
-      r0 = i;
-    }
-  }
-  ch.push_back(n_rows);
-  return ch;
 }
 
 std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int max_rows) {
@@ -372,10 +338,10 @@ static void launch_gu(pm_ctx* c, int U, int grid, int n, const int* rp, const in
                       const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
   const dim3 gr(grid), bl(256);
   switch (U) {
-    case 2: launch_pdl(c, csr_kernel<TV, TX, TA, G, 2, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    case 4: launch_pdl(c, csr_kernel<TV, TX, TA, G, 4, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    case 16: launch_pdl(c, csr_kernel<TV, TX, TA, G, 16, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
-    default: launch_pdl(c, csr_kernel<TV, TX, TA, G, 8, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 2: launch_k(c, csr_kernel<TV, TX, TA, G, 2, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 4: launch_k(c, csr_kernel<TV, TX, TA, G, 4, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    case 16: launch_k(c, csr_kernel<TV, TX, TA, G, 16, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
+    default: launch_k(c, csr_kernel<TV, TX, TA, G, 8, EPI>, gr, bl, 0, n, rp, ci, v, x, y, b, d, x, alpha, m); break;
   }
 }
 
@@ -424,39 +390,6 @@ static double epi_bytes(const DevCsr& A, int epi, int eb, int n) {
   if (epi == EPI_DEFECT) rows_vec += 1.0;                      // b read
   if (epi == EPI_JACOBI) rows_vec += 2.0;                      // b and diag read
   return double(A.nnz) * (eb + 4) + double(n + 1) * 4 + double(A.n_cols) * eb + double(n) * eb * rows_vec;
-}
-
-// the bulk-copy FP32 kernel: persistent grid, two 32 KB buffers per block
-template <int G, int U, int EPI>
-static void launch_bulk_g(pm_ctx* c, const DevCsr& A, const float* vals, const float* x, float* y, const float* b,
-                          const float* d, float alpha, const BlockMask& m) {
-  constexpr size_t smem = 4 * size_t(kBulkEntries) * 4 + 2 * sizeof(uint64_t);
-  // per instantiation, once per process (several host threads may launch)
-  static std::once_flag once;
-  static int per_sm = 1;
-  static cudaError_t init_err = cudaSuccess;
-  std::call_once(once, [&] {
-    init_err = cudaFuncSetAttribute(csr_bulk_kernel<G, U, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    int bps = 0;
-    if (init_err == cudaSuccess)
-      init_err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, csr_bulk_kernel<G, U, EPI>, 256, smem);
-    per_sm = std::max(1, bps);
-  });
-  PM_CUDA(init_err);
-  const int grid = std::max(1, std::min(A.n_chunks, c->num_sms * per_sm));
-  csr_bulk_kernel<G, U, EPI><<<grid, 256, smem, c->stream>>>(A.n_chunks, A.chunk_rows.p, A.row_ptr.p, A.cols.p, vals,
-                                                         x, y, b, d, alpha, m, c->dev_error.p);
-}
-
-template <int EPI>
-static void launch_bulk(pm_ctx* c, const DevCsr& A, const float* vals, const float* x, float* y, const float* b,
-                        const float* d, float alpha, const BlockMask& m) {
-  BlockMask mg = m;
-  mg.guard = c->guard;
-  if (A.lanes32 == 4) launch_bulk_g<4, 4, EPI>(c, A, vals, x, y, b, d, alpha, mg);
-  else launch_bulk_g<8, 16, EPI>(c, A, vals, x, y, b, d, alpha, mg);
-  PM_CHECK_LAUNCH();
-  c->kernel_launches++;
 }
 
 template <class T>
@@ -570,38 +503,10 @@ static void csr_dispatch(pm_ctx* c, const DevCsr& A, const TV* vals, const TX* d
     }
   }
   if constexpr (sizeof(TV) == 4) {
-    if (!(c->bulk_spmv && A.bulk32 && A.n_chunks > 0) && c->sell_shape > 0 && A.sell_lanes == c->sell_shape / 100 &&
+    if (c->sell_shape > 0 && A.sell_lanes == c->sell_shape / 100 &&
         A.n_slices > 0 && n == A.n_rows) {
       launch_sell(c, A, epi, reinterpret_cast<const float*>(x), reinterpret_cast<float*>(y),
                   reinterpret_cast<const float*>(b), reinterpret_cast<const float*>(diag), float(alpha));
-      if (probe) {
-        cudaEvent_t e1 = probe_event(c);
-        PM_CUDA(cudaEventRecord(e1, c->stream));
-        c->probe_events.push_back(e1);
-      }
-      return;
-    }
-  }
-  // the bulk kernel exists for the two FP32 launch shapes the matrices choose
-  const bool bulk = sizeof(TV) == 4 && c->bulk_spmv && A.bulk32 && A.n_chunks > 0 && n == A.n_rows &&
-                    ((G == 4 && U == 4) || (G == 8 && U == 16));
-  if constexpr (sizeof(TV) == 4) {
-    if (bulk) {
-      const float* fv = reinterpret_cast<const float*>(vals);
-      const float* fx = reinterpret_cast<const float*>(x);
-      float* fy = reinterpret_cast<float*>(y);
-      const float* fb = reinterpret_cast<const float*>(b);
-      const float* fd = reinterpret_cast<const float*>(diag);
-      const float fa = float(alpha);
-      switch (epi) {
-        case EPI_AXPY: launch_bulk<EPI_AXPY>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
-        case EPI_SET: launch_bulk<EPI_SET>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
-        case EPI_DEFECT: launch_bulk<EPI_DEFECT>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
-        case EPI_JACOBI: launch_bulk<EPI_JACOBI>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
-        case EPI_RESTRICT: launch_bulk<EPI_RESTRICT>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
-        case EPI_PROLONG: launch_bulk<EPI_PROLONG>(c, A, fv, fx, fy, fb, fd, fa, A.mask); break;
-        default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
-      }
       if (probe) {
         cudaEvent_t e1 = probe_event(c);
         PM_CUDA(cudaEventRecord(e1, c->stream));
@@ -766,7 +671,7 @@ __global__ void k_init_sol(int n, BlockMask m, const T* __restrict__ rhs, T* __r
 
 #define PM_LAUNCH1D(kern, n, ...)                                                     \
   do {                                                                                \
-    if ((n) > 0) launch_pdl(c, kern, dim3(grid_for(c, (n))), dim3(256), 0, __VA_ARGS__); \
+    if ((n) > 0) launch_k(c, kern, dim3(grid_for(c, (n))), dim3(256), 0, __VA_ARGS__); \
   } while (0)
 
 void vcopy(pm_ctx* c, int n, const double* x, double* y) { PM_LAUNCH1D(k_copy<double>, n, n, x, y); }
@@ -1524,7 +1429,7 @@ void DenseInverse::complete32(pm_ctx* c, const DevCsr& A) {
 void DenseInverse::solve32(pm_ctx* c, const float* b, float* x) {
   if (!has32) throw Error(PM_E_INVALID, "coarse FP32 inverse used before build32");
   const long long threads = (long long)(na + (n + 31) / 32) * 32;
-  launch_pdl(c, k_coarse_gemv32, dim3(nblocks(threads, 256)), dim3(256), 0, n, na, (const int*)act.p,
+  launch_k(c, k_coarse_gemv32, dim3(nblocks(threads, 256)), dim3(256), 0, n, na, (const int*)act.p,
              (const int*)pos.p, (const float*)inv32.p, b, x);
 }
 

@@ -7,23 +7,14 @@
 
 namespace pm {
 
-// Launch with programmatic stream serialization (when the context's pdl
-// option is on): the kernel may start while the previous kernel on the stream
-// finishes; it must begin with pdl_enter() (or load only data no earlier
-// kernel writes before pdl_wait()).
+// Plain launch on the context's stream, counted. The vector and Krylov
+// kernels launched this way begin with pdl_enter(): its trigger lets a
+// following sliced-ELL sweep (launched with programmatic stream
+// serialization) load its slice layout while they run.
 template <class... KArgs, class... Args>
-inline void launch_pdl(pm_ctx* c, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = c->stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = c->pdl >= 2 ? 1 : 0;
-  PM_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+inline void launch_k(pm_ctx* c, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+  kern<<<grid, block, smem, c->stream>>>(static_cast<KArgs>(args)...);
+  PM_CHECK_LAUNCH();
   c->kernel_launches++;
 }
 
@@ -40,11 +31,6 @@ struct DevCsr {
   DBuf<int> rblock;
   int n_rblocks = 0;
   bool stream = true;  // use the streaming kernel when row blocks exist
-  // chunks of consecutive rows for the bulk-copy FP32 kernel (empty when a
-  // row's aligned span exceeds a buffer); bulk32 selects that kernel
-  DBuf<int> chunk_rows;
-  int n_chunks = 0;
-  bool bulk32 = true;
   int64_t nnz4() const { return (nnz + 3) & ~int64_t(3); }
   // sliced-ELL copy of the FP32 values (sell_kernel): built by make_fp32 for
   // matrices with more than 16 entries per row when the context asks for it;
@@ -84,16 +70,11 @@ int choose_lanes(double avg_nnz_per_row);
 constexpr int kStreamNnz = 2048;  // entries per row block of the streaming kernel
 // greedy row blocks over a host row-pointer array; empty if a row is too long
 std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int max_rows);
-// chunks of consecutive rows whose 4-entry aligned span holds at most
-// max_entries entries; empty if one row alone does not fit
-std::vector<int> build_bulk_chunks(int n_rows, const int* rp, int max_entries);
 // sliced-ELL layout (see sell_kernel) of a host CSR structure with `lanes`
 // lanes per row and sorting windows of `window` rows; false if the padded
 // layout would exceed 2^31 - 1 entries
 bool build_sell_layout(int n_rows, const int* rp, const int* ci, int lanes, int window, std::vector<int>& perm,
                        std::vector<int>& off, std::vector<int>& cols, std::vector<int>& src);
-// reads and clears the context's device error flag; throws PM_E_TIMEOUT if set
-void check_device_error(pm_ctx* c);
 
 // y := epilogue(A x); see pm_spmv.cuh for the epilogue meanings
 void csr_apply(pm_ctx* c, const DevCsr& A, int epi, const double* x, double* y, const double* b,

@@ -178,6 +178,9 @@ void pm_server::worker(int index) {
     if (rc == PM_OK && entry) {
       const int64_t before = pm::g_thread_dev_bytes;
       if (rq.kind == 1) {
+        // the cached problem serves every viscosity of its set-up: the
+        // assembly below takes this request's nu
+        entry->p->nu = rq.nu;
         rc = pm_problem_reset_solution(entry->p);
         if (rc == PM_OK) rc = pm_problem_assemble(entry->p);
         if (rc == PM_OK) rc = pm_problem_solve(entry->p);

@@ -868,7 +868,7 @@ size_t pm_solver::layout_signature() const {
   // the sliced copies are chosen per launch by the context's kernel options
   auto mix_csr = [&mix](const DevCsr& M) {
     mix(M.vals.p); mix(M.vals32.p); mix(M.diag.p); mix(M.diag32.p);
-    mix(M.row_ptr.p); mix(M.cols.p); mix(M.rblock.p); mix(M.chunk_rows.p);
+    mix(M.row_ptr.p); mix(M.cols.p); mix(M.rblock.p);
     mix(M.sell_perm.p); mix(M.sell_off.p); mix(M.sell_cols.p); mix(M.sell_vals.p); mix(M.sell_vals64.p);
   };
   mix(A);
@@ -893,7 +893,7 @@ size_t pm_solver::layout_signature() const {
   mix(work.p); mix(gm.p); mix(flags.p);
   mix(ctx->partials.p); mix(ctx->host_scalars);
   h ^= size_t(restart) * 31 + size_t(work_n);
-  h = h * 1099511628211ull ^ (size_t(ctx->sell_shape) * 2 + size_t(ctx->bulk_spmv));
+  h = h * 1099511628211ull ^ size_t(ctx->sell_shape);
   h = h * 1099511628211ull ^ (size_t(ctx->sell_shape64) * 8 + size_t(ctx->pdl) * 2 + size_t(ctx->jacobi_zero_start));
   return h;
 }
@@ -1030,14 +1030,14 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
           const double* Vc = V;
           const double* nul = nullptr;
           const int* inul = nullptr;
-          if (nk <= 16) launch_pdl(c, k_mdot<16>, rb, t256, 0, n, nk, (const double*)r, Vc, ld, cgs_part);
-          else launch_pdl(c, k_mdot<kCgsFused>, rb, t256, 0, n, nk, (const double*)r, Vc, ld, cgs_part);
-          launch_pdl(c, k_reduce_proj, dim3(nk), t256, 0, (const double*)cgs_part, h1, nul, H, ldh, i, inul);
-          if (nk <= 16) launch_pdl(c, k_cgs_update_mdot<16>, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h1, cgs_part);
-          else launch_pdl(c, k_cgs_update_mdot<kCgsFused>, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h1, cgs_part);
-          launch_pdl(c, k_reduce_proj, dim3(nk), t256, 0, (const double*)cgs_part, h2, (const double*)h1, H, ldh, i,
+          if (nk <= 16) launch_k(c, k_mdot<16>, rb, t256, 0, n, nk, (const double*)r, Vc, ld, cgs_part);
+          else launch_k(c, k_mdot<kCgsFused>, rb, t256, 0, n, nk, (const double*)r, Vc, ld, cgs_part);
+          launch_k(c, k_reduce_proj, dim3(nk), t256, 0, (const double*)cgs_part, h1, nul, H, ldh, i, inul);
+          if (nk <= 16) launch_k(c, k_cgs_update_mdot<16>, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h1, cgs_part);
+          else launch_k(c, k_cgs_update_mdot<kCgsFused>, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h1, cgs_part);
+          launch_k(c, k_reduce_proj, dim3(nk), t256, 0, (const double*)cgs_part, h2, (const double*)h1, H, ldh, i,
                      inul);
-          launch_pdl(c, k_cgs_update_norm, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h2, partA);
+          launch_k(c, k_cgs_update_norm, rb, t256, 0, n, nk, r, Vc, ld, (const double*)h2, partA);
         } else if (cgs2) {
           // two passes of classical Gram-Schmidt; H(:,i) = h1 + h2. With the
           // conditional variant the second pass runs only when the first lost
@@ -1072,9 +1072,9 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
             std::swap(pin, pout);
           }
         }
-        launch_pdl(c, k_fg_normalize, dim3(grid), dim3(256), 0, n, ldh, i, (const double*)r, V + ld * (i + 1),
+        launch_k(c, k_fg_normalize, dim3(grid), dim3(256), 0, n, ldh, i, (const double*)r, V + ld * (i + 1),
                    (const double*)pin, H, flags.p);
-        launch_pdl(c, k_fg_givens, dim3(1), dim3(32), 0, ldh, i, H, cs, sn, s, dres);
+        launch_k(c, k_fg_givens, dim3(1), dim3(32), 0, ldh, i, H, cs, sn, s, dres);
         PM_CUDA(cudaMemcpyAsync(c->host_scalars, dres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         PM_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(c->host_scalars + 1), flags.p, sizeof(int),
                                 cudaMemcpyDeviceToHost, c->stream));

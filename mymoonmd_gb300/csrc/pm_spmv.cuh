@@ -53,7 +53,7 @@ __device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
 // has completed and its writes are visible (a no-op without the attribute).
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-// the start of a kernel launched by launch_pdl that reads nothing before the
+// the start of a kernel launched by launch_k that reads nothing before the
 // previous kernel has completed
 __device__ __forceinline__ void pdl_enter() {
   pdl_trigger();
@@ -214,178 +214,6 @@ csr_stream_kernel(const int* __restrict__ rblock, const int* __restrict__ row_pt
   }
 }
 
-
-// ------------------------------------------------------------------------
-// Bulk-copy CSR kernel for FP32 values. A persistent grid walks chunks of
-// consecutive rows whose entries (4-entry aligned span) fit one buffer. One
-// thread streams the next chunk's values and column indices into shared
-// memory with cp.async.bulk (completion counted on an mbarrier) while the
-// block computes the current chunk: G lanes per row, each lane summing the
-// entries beg+lane, beg+lane+G, ... in rounds of U (gathers first), then the
-// same shuffle tree as csr_kernel<.., G, U, ..>, so the results are
-// bit-identical to it. The
-// arrays must be readable up to nnz rounded up to a multiple of 4 entries.
-namespace bulk {
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_init_fence() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: false after the iteration limit (the caller records an error)
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < (1 << 22); ++i)
-    if (mbar_test(bar, parity)) return true;
-  return false;
-}
-
-}  // namespace bulk
-
-constexpr int kBulkEntries = 4096;  // entries per buffer: 16 KB values + 16 KB indices
-
-template <int G, int U, int EPI>
-__global__ void __launch_bounds__(256)
-csr_bulk_kernel(int n_chunks, const int* __restrict__ chunk_rows, const int* __restrict__ row_ptr,
-                const int* __restrict__ cols, const float* __restrict__ vals, const float* __restrict__ x,
-                float* __restrict__ y, const float* __restrict__ b, const float* __restrict__ diag, float alpha,
-                BlockMask mask, int* __restrict__ err) {
-  extern __shared__ __align__(128) unsigned char bulk_smem[];
-  float* sv = reinterpret_cast<float*>(bulk_smem);                       // [2][kBulkEntries]
-  int* sc = reinterpret_cast<int*>(bulk_smem + 2 * kBulkEntries * 4);     // [2][kBulkEntries]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(bulk_smem + 4 * kBulkEntries * 4);  // [2]
-  __shared__ int s_failed;
-  const int t = threadIdx.x;
-  if (guarded(mask.guard)) {  // uniform for the whole grid
-    if (EPI == EPI_JACOBI) {
-      const int n = chunk_rows[n_chunks];
-      for (int i = blockIdx.x * blockDim.x + t; i < n; i += gridDim.x * blockDim.x) y[i] = x[i];
-    }
-    return;
-  }
-  if (t == 0) {
-    bulk::mbar_init(&bar[0]);
-    bulk::mbar_init(&bar[1]);
-    bulk::mbar_init_fence();
-    s_failed = 0;
-  }
-  __syncthreads();
-  unsigned issued = 0u, phase = 0u;  // per buffer bit: copy in flight; parity of its next wait
-  auto issue = [&](int c, int buf) {
-    const int s4 = __ldg(row_ptr + __ldg(chunk_rows + c)) & ~3;
-    const int e4 = (__ldg(row_ptr + __ldg(chunk_rows + c + 1)) + 3) & ~3;
-    const uint32_t bytes = uint32_t(e4 - s4) * 4u;
-    bulk::proxy_fence();
-    bulk::mbar_expect(&bar[buf], 2u * bytes);
-    bulk::copy_g2s(sv + buf * kBulkEntries, vals + s4, bytes, &bar[buf]);
-    bulk::copy_g2s(sc + buf * kBulkEntries, cols + s4, bytes, &bar[buf]);
-  };
-  if (t == 0 && int(blockIdx.x) < n_chunks) {
-    issue(blockIdx.x, 0);
-    issued |= 1u;
-  }
-  const int lane = t & (G - 1);
-  int it = 0;
-  for (int c = blockIdx.x; c < n_chunks; c += gridDim.x, ++it) {
-    const int buf = it & 1;
-    const int cn = c + gridDim.x;
-    if (t == 0 && cn < n_chunks && !s_failed) {
-      issue(cn, buf ^ 1);  // that buffer was released by the barrier closing the last iteration
-      issued |= 2u >> buf;
-    }
-    if (t == 0) {
-      if (!bulk::mbar_wait(&bar[buf], (phase >> buf) & 1u)) {
-        s_failed = 1;
-        atomicExch(err, 1);
-      }
-      issued &= ~(1u << buf);
-      phase ^= 1u << buf;
-    }
-    __syncthreads();
-    if (s_failed) break;
-    const int r0 = __ldg(chunk_rows + c), r1 = __ldg(chunk_rows + c + 1);
-    const int s4 = __ldg(row_ptr + r0) & ~3;
-    const float* V = sv + buf * kBulkEntries - s4;
-    const int* Cc = sc + buf * kBulkEntries - s4;
-    for (int rb = r0; rb < r1; rb += 256 / G) {
-      const int row = rb + t / G;
-      const bool valid = row < r1;
-      const int beg = valid ? __ldg(row_ptr + row) : 0;
-      const int end = valid ? __ldg(row_ptr + row + 1) : 0;
-      float pre_b = 0.f, pre_d = 1.f, pre_x = 0.f, pre_y = 0.f;
-      if (valid && lane == 0) {
-        if constexpr (EPI == EPI_AXPY || EPI == EPI_PROLONG) pre_y = y[row];
-        if constexpr (EPI == EPI_DEFECT || EPI == EPI_JACOBI) pre_b = __ldg(b + row);
-        if constexpr (EPI == EPI_JACOBI) {
-          pre_d = __ldg(diag + row);
-          pre_x = __ldg(x + row);
-        }
-      }
-      // U entries per lane per round, all gathers issued before the products
-      // (the order and the zero padding of csr_kernel<.., G, U, ..>)
-      float s = 0.f;
-      for (int base = beg; base < end; base += G * U) {
-        float vv[U], xv[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int k = base + u * G + lane;
-          const bool in = k < end;
-          vv[u] = in ? V[k] : 0.f;
-          xv[u] = __ldg(x + (in ? Cc[k] : 0));
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) s += vv[u] * xv[u];
-      }
-#pragma unroll
-      for (int off = G / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, G);
-      if (valid && lane == 0) {
-        if constexpr (EPI == EPI_AXPY) {
-          y[row] = pre_y + alpha * s;
-        } else if constexpr (EPI == EPI_SET) {
-          y[row] = s;
-        } else if constexpr (EPI == EPI_DEFECT) {
-          y[row] = pre_b - s;
-        } else if constexpr (EPI == EPI_JACOBI) {
-          const float d = (pre_b - s) / pre_d;
-          y[row] = pre_x + alpha * d;
-        } else if constexpr (EPI == EPI_RESTRICT) {
-          y[row] = row_is_active(mask, row) ? s : 0.f;
-        } else if constexpr (EPI == EPI_PROLONG) {
-          if (row_is_active(mask, row)) y[row] = pre_y + alpha * s;
-        }
-      }
-    }
-    __syncthreads();  // buffer `buf` may be refilled now
-  }
-  // leave no copy in flight (bounded)
-  if (t == 0)
-    for (int q = 0; q < 2; ++q)
-      if (((issued >> q) & 1u) && !bulk::mbar_wait(&bar[q], (phase >> q) & 1u)) atomicExch(err, 1);
-}
 
 // Sliced-ELL copy of an FP32 matrix (SELL-C-sigma, C = 32/L rows per slice).
 // Rows are sorted by length, longest first (ties in row order), inside windows

@@ -3,19 +3,8 @@
     python -m mymoonmd_gb300.profile_cases request [--precision mixed|fp64]
         one warm-up request, then one request (assembly + solve) of the 3D Q2
         32^3 convection-diffusion workload (274,625 DOFs, 4 levels)
-    python -m mymoonmd_gb300.profile_cases request2d [--precision mixed|fp64] [--cluster 1|2|4|8]
-        the same for the 2D Q1 128^2 workload (16,641 DOFs, 4 levels), with the
-        host wall time of each request; --cluster: thread blocks of the FP32
-        coarse Gauss-Jordan (request3d_cluster: the 3D workload the same way)
     python -m mymoonmd_gb300.profile_cases spmv
         the finest 32^3 Q2 matrix: two FP64 and two FP32 SpMV launches
-    python -m mymoonmd_gb300.profile_cases sliced
-        the request above once per SpMV kernel shape (option fp32_sliced_spmv,
-        or fp64_sliced_spmv with --precision fp64: 0 = row groups, else
-        sliced-ELL shapes): request time, iterations, and the finest-level
-        Jacobi sweep and defect bandwidths from the launch probe
-    python -m mymoonmd_gb300.profile_cases assembly
-        one assembly of the four 32^3 Q2 levels
     python -m mymoonmd_gb300.profile_cases stokes [--precision ...] [--smoother ...] [--coarse ...]
         one warm-up request, then one request of the 3D Stokes P2/P1 workload
         (24^3 cubes x 6 tetrahedra, 368,572 DOFs, 3 levels, V(1,1) Vanka);
@@ -63,35 +52,16 @@ def problem(ctx, precision="mixed", n_levels=4):
     return disc, m.ConvectionDiffusion(ctx, disc, cf, _db(precision), quad_points=3)
 
 
-def problem2d(ctx, precision="mixed"):
-    """the 2D Q1 128^2 convection-diffusion workload (16,641 DOFs, 4 levels,
-    FGMRES(20), to 1e-10)"""
-    disc = m.Discretization(m.GEO_SQUARE_QUAD, 1, 7, 4, m.KIND_CD, 1)
-    cf = m.cd_coeffs(0.1, (1.0, 0.0, 0.0), 0.0, True)
-    db = _db(precision)
-    db["gmres_restart"] = 20
-    db["residual_reduction"] = 1e-10
-    return disc, m.ConvectionDiffusion(ctx, disc, cf, db, quad_points=3)
-
-
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["request", "request2d", "request3d_cluster", "spmv", "assembly", "stokes",
-                                     "sliced", "tcd"])
+    ap.add_argument("case", choices=["request", "spmv", "stokes", "tcd"])
     ap.add_argument("--scheme", default="crank_nicolson", choices=["backward_euler", "crank_nicolson", "bdf_two"])
-    ap.add_argument("--shapes", default="0,140,141,180,240,241,280,440,441,480,481,840,841,881")
-    ap.add_argument("--pdl", type=int, default=1, choices=[0, 1, 2])
-    ap.add_argument("--cluster", type=int, default=8, choices=[1, 2, 4, 8])
-    ap.add_argument("--threads", type=int, default=0, choices=[0, 256, 512, 1024])
-    ap.add_argument("--min-entries", type=int, default=16, help="sliced_min_entries option")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
     ap.add_argument("--coarse", default="nodal_vanka_jacobi")
     ap.add_argument("--cubes", type=int, default=24, choices=[12, 24])
     args = ap.parse_args()
     ctx = m.Context(0)
-    ctx.set_option("pdl", args.pdl)
-    ctx.set_option("sliced_min_entries", args.min_entries)
     if args.case == "tcd":
         db = _db(args.precision)
         db.merge(ParameterDatabase.default_time_database())
@@ -134,71 +104,13 @@ def main() -> None:
         prob.close()
         ctx.close()
         return
-    if args.case in ("request2d", "request3d_cluster"):
-        import time
-        ctx.set_option("coarse_cluster", args.cluster)
-        ctx.set_option("coarse_threads", args.threads)
-        disc, prob = problem2d(ctx, args.precision) if args.case == "request2d" else problem(ctx, args.precision)
-        for _ in range(3):
-            t0 = time.perf_counter()
-            prob.reset_solution()
-            prob.assemble()
-            prob.solve()
-            ctx.synchronize()
-            print(f"{args.case} {args.precision} cluster {args.cluster} threads {args.threads}: "
-                  f"{(time.perf_counter() - t0) * 1e3:.3f} ms, "
-                  f"{prob.last_info()[0]} iterations", flush=True)
-        prob.close()
-        ctx.close()
-        return
     disc, prob = problem(ctx, args.precision)
-    if args.case == "sliced":
-        import time
-        nnz = prob.matrix(-1).nnz
-        fp64 = args.precision == "fp64"
-        opt = "fp64_sliced_spmv" if fp64 else "fp32_sliced_spmv"
-        for shape in [int(v) for v in args.shapes.split(",")]:
-            ctx.set_option(opt, shape)
-            for _ in range(2):  # lays out the sliced copies, captures the graphs
-                prob.reset_solution()
-                prob.assemble()
-                prob.solve()
-            ctx.synchronize()
-            t0 = time.perf_counter()
-            for _ in range(3):
-                prob.reset_solution()
-                prob.assemble()
-                prob.solve()
-            ctx.synchronize()
-            ms = (time.perf_counter() - t0) / 3 * 1e3
-            its = prob.last_info()[0]
-            bw = {}
-            for epi in (3, 2):  # Jacobi sweep, defect
-                ctx.set_option("probe_epilogue", epi)
-                ctx.set_option("probe_precision", 8 if fp64 else 4)
-                ctx.probe(nnz)
-                prob.reset_solution()
-                prob.assemble()
-                prob.solve()
-                n, pms, pb = ctx.probe_result()
-                ctx.probe(0)
-                bw[epi] = (pb / pms / 1e6 if pms > 0 else 0.0, n)
-            ctx.set_option("probe_epilogue", -1)
-            ctx.set_option("probe_precision", 0)
-            print(f"shape {shape:3d}: request {ms:7.2f} ms, {its} iterations, finest Jacobi "
-                  f"{bw[3][0]:6.0f} GB/s ({bw[3][1]} launches), defect {bw[2][0]:6.0f} GB/s ({bw[2][1]})",
-                  flush=True)
-        ctx.set_option(opt, 441 if fp64 else 481)
-    elif args.case == "request":
+    if args.case == "request":
         for _ in range(2):
             prob.reset_solution()
             prob.assemble()
             prob.solve()
         print("request", args.precision, "iterations", prob.last_info()[0])
-    elif args.case == "assembly":
-        prob.assemble()
-        ctx.synchronize()
-        print("assembly of 4 levels")
     else:
         prob.assemble()
         A = prob.matrix(-1)
@@ -211,18 +123,7 @@ def main() -> None:
         y32 = m.DeviceVector(ctx, n, np.float32)
         ms, b = A.bench_apply(x, y, 2)
         ms32, b32 = A.bench_apply(x32, y32, 2, fp32=True)
-        for shape in [int(v) for v in args.shapes.split(",")]:
-            ctx.set_option("fp32_sliced_spmv", shape)
-            A.make_fp32()  # lays out the sliced copy for the shape's lanes per row
-            A.bench_apply(x32, y32, 1, fp32=True)
-            mss, bs = A.bench_apply(x32, y32, 2, fp32=True)
-            print(f"fp32 sliced shape {shape}: {bs / mss / 1e6:.0f} GB/s")
-        ctx.set_option("fp32_sliced_spmv", 0)
-        ctx.set_option("fp32_bulk_spmv", 1)
-        msb, bb = A.bench_apply(x32, y32, 2, fp32=True)
-        ctx.set_option("fp32_bulk_spmv", 0)
-        print(f"spmv fp64 {b / ms / 1e6:.0f} GB/s, fp32 {b32 / ms32 / 1e6:.0f} GB/s, "
-              f"fp32 bulk-copy kernel {bb / msb / 1e6:.0f} GB/s (2 launches each)")
+        print(f"spmv fp64 {b / ms / 1e6:.0f} GB/s, fp32 {b32 / ms32 / 1e6:.0f} GB/s (2 launches each)")
     prob.close()
     ctx.close()
 

@@ -362,36 +362,6 @@ def test_multigrid_iterative_coarse_level_matches_oracle(ctx, coarse_residual):
     assert rel(rd.numpy(), ora.mg_apply(z)) <= 1e-11
 
 
-@pytest.mark.parametrize("case", ["q1_2d", "q2_3d"])
-def test_fp32_bulk_kernel_gives_the_row_group_kernels_bits(ctx, case):
-    """the bulk-copy FP32 kernel sums each row in the order of the per-row-group
-    kernel with the same lanes: identical results, for the SpMV and for a whole
-    mixed-precision multigrid application (Jacobi sweeps, defects, transfer)"""
-    nl = CASES[case][3]
-    disc, prob, ora = make_pair(ctx, case, mg_db(nl, precision="mixed"))
-    prob.solve()
-    A = prob.matrix(-1)
-    n = ora.finest.n_dofs
-    rng = np.random.default_rng(9)
-    x = m.DeviceVector.from_numpy(ctx, rng.standard_normal(n).astype(np.float32))
-    z = m.DeviceVector.from_numpy(ctx, rng.standard_normal(n))
-    out = {}
-    try:
-        ctx.set_option("fp32_sliced_spmv", 0)  # the row-group kernel is the comparison
-        for flag in (1, 0):
-            ctx.set_option("fp32_bulk_spmv", flag)
-            y = m.DeviceVector(ctx, n, np.float32)
-            A.apply_f32(x, y)
-            r = m.DeviceVector(ctx, n)
-            prob.solver().apply_preconditioner(z, r)
-            out[flag] = (y.numpy(), r.numpy())
-    finally:
-        ctx.set_option("fp32_bulk_spmv", 0)  # the library defaults
-        ctx.set_option("fp32_sliced_spmv", 481)
-    assert np.array_equal(out[0][0], out[1][0])
-    assert np.array_equal(out[0][1], out[1][1])
-
-
 def _cd_case(dim, cells, elem, eps, b):
     from mymoonmd_gb300 import workloads as wl
     rq = wl.cd_request(dim, cells, elem, eps, b)

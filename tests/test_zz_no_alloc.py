@@ -5,8 +5,9 @@ pm_assemble_cd_noalloc is for callers that cannot call cudaMalloc when they
 assemble - for instance a serving worker that must not stall requests already
 running on the GPU with an allocation, or a host that reserved all device memory
 up front. It keeps its scratch in a static device array of 32 MiB, so it must
-give the same matrix and right-hand side as the allocating path, call after
-call, and refuse levels whose scratch would not fit.
+give the same matrix and right-hand side as the allocating path (the same
+element kernels: the same bits), call after call, agree with the oracle's
+element loop, and refuse levels whose scratch would not fit.
 
 This file is collected last so that a failure here comes after every other test
 has run; it creates its own context and passes alone in a fresh process too.
@@ -15,6 +16,7 @@ import numpy as np
 import pytest
 
 import mymoonmd_gb300 as m
+from oracle import cd as ocd
 
 pytestmark = pytest.mark.gpu
 
@@ -26,12 +28,17 @@ def rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-def test_noalloc_assembly_matches_allocating_assembly_twice():
+@pytest.mark.parametrize("quadrature_loop", [0, 1])
+def test_noalloc_assembly_matches_allocating_assembly_twice(quadrature_loop):
     ctx = m.Context(0)
     try:
+        # both entry points run the element kernel this option selects
+        ctx.set_option("assembly_quadrature_loop", quadrature_loop)
         disc = m.Discretization(m.GEO_CUBE_HEXA, 1, 3, 3, m.KIND_CD, 2)  # 8^3 Q2, 3 levels
         cf = m.cd_coeffs(0.05, (1.0, 0.5, 0.25), 0.3, True)
         prob = m.ConvectionDiffusion(ctx, disc, cf, "solver_type: direct\n", quad_points=3)
+        ora = ocd.OracleCD(m.GEO_CUBE_HEXA, 1, 3, 3, 2, 0.05, (1.0, 0.5, 0.25), 0.3, 3)
+        ora.assemble()
         for level in range(disc.n_levels):
             info = disc.level_info(level)
             rp, ci = disc.structure(level)
@@ -43,8 +50,27 @@ def test_noalloc_assembly_matches_allocating_assembly_twice():
                 vals = m.DeviceVector(ctx, info["nnz"])
                 r = m.DeviceVector(ctx, info["n_dofs"])
                 prob.assemble_level_noalloc(level, vals, r, cf)
-                assert rel(vals.numpy(), ref_vals) <= TOL
-                assert rel(r.numpy(), ref_rhs) <= TOL
+                got_vals, got_rhs = vals.numpy(), r.numpy()
+                assert np.array_equal(got_vals, ref_vals)
+                assert np.array_equal(got_rhs, ref_rhs)
+                # and the oracle's element loop, within the assembly tolerance
+                assert rel(got_vals, ora.vals[level]) <= TOL
+                assert rel(got_rhs, ora.rhs[level]) <= TOL
+        prob.close()
+    finally:
+        ctx.close()
+
+
+def test_noalloc_assembly_refuses_stokes_problems():
+    ctx = m.Context(0)
+    try:
+        disc = m.Discretization(m.GEO_CUBE_TETRA, 1, 1, 2, m.KIND_STOKES, 12)
+        prob = m.StokesProblem(ctx, disc, 1.0, "solver_type: direct\n")
+        info = disc.level_info(1)
+        vals = m.DeviceVector(ctx, info["nnz"])
+        r = m.DeviceVector(ctx, info["n_dofs"])
+        with pytest.raises(m.PmError, match="convection-diffusion only"):
+            prob.assemble_level_noalloc(1, vals, r)
         prob.close()
     finally:
         ctx.close()
