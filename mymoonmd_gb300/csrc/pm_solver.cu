@@ -47,6 +47,9 @@ std::string Params::str(const std::string& k, const std::string& def) const {
 double Params::num(const std::string& k, double def) const {
   auto it = kv.find(k);
   if (it == kv.end()) return def;
+  // ParameterDatabase::write prints bool parameters as true / false
+  if (it->second == "true") return 1.0;
+  if (it->second == "false") return 0.0;
   char* end = nullptr;
   double v = strtod(it->second.c_str(), &end);
   if (end == it->second.c_str()) throw Error(PM_E_INVALID, "parameter " + k + " is not a number");

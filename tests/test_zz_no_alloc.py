@@ -69,7 +69,7 @@ def test_noalloc_assembly_refuses_stokes_problems():
         info = disc.level_info(1)
         vals = m.DeviceVector(ctx, info["nnz"])
         r = m.DeviceVector(ctx, info["n_dofs"])
-        with pytest.raises(m.PmError, match="convection-diffusion only"):
+        with pytest.raises(m.PmError, match="convection-diffusion problems only"):
             prob.assemble_level_noalloc(1, vals, r)
         prob.close()
     finally:
