@@ -331,6 +331,20 @@ int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* coeffs, const double*
 /* Solver statistics of the problem's last solve. */
 int pm_problem_last_info(const pm_problem* p, int* iterations, double* residual,
                          double* initial_residual);
+/* Batched solve (no reference counterpart; the reference solves one system
+ * per Solver::solve, src/Solver/Solver.C:415): n_problems assembled
+ * convection-diffusion problems of one set-up (the same pm_disc) and one
+ * context, solved by FGMRES(m <= 32) with the multigrid preconditioner (damped
+ * Jacobi smoothing, direct coarse solve) in lockstep, at most `slots` (<= 16)
+ * at a time: every kernel of an Arnoldi step and of the V-cycle runs once for
+ * all slots. Problems join at restart-cycle boundaries and leave when their
+ * residual test passes; each problem's iterates are those of its lone
+ * pm_problem_solve, bit for bit, except that the mixed form keeps its FP32
+ * cycle throughout (the lone solve may switch to FP64 when the residual
+ * stalls). status_out (n_problems, or NULL): per problem PM_OK, PM_E_MAXIT,
+ * PM_E_DIVERGED or PM_E_BREAKDOWN; pm_problem_last_info and the solution
+ * vectors hold each problem's result. */
+int pm_problem_solve_batched(pm_problem* const* probs, int n_problems, int slots, int* status_out);
 
 /* ------------------------------------------- time-dependent problem ------ */
 /* TimeConvectionDiffusion<d> (src/System/TimeConvectionDiffusion.C) with

@@ -8,6 +8,6 @@ from .parameter_database import ParameterDatabase  # noqa: F401
 from .core import (  # noqa: F401
     GEO_CUBE_HEXA, GEO_CUBE_TETRA, GEO_SQUARE_QUAD, KIND_CD, KIND_STOKES, Context, ConvectionDiffusion,
     DeviceVector, Discretization, FEMatrix, PinnedArray, PmError, Server, Solver, StokesProblem,
-    TimeConvectionDiffusion, assemble_cd, cd_coeffs)
+    TimeConvectionDiffusion, assemble_cd, cd_coeffs, solve_batched)
 
 __version__ = "0.1.0"

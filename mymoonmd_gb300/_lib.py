@@ -140,6 +140,7 @@ _SIGS = {
     "pm_problem_solution_dev": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "pm_problem_run_host": (i32, [vp, C.POINTER(CdCoeffs), vp, vp]),
     "pm_problem_last_info": (i32, [vp, pi32, pf64, pf64]),
+    "pm_problem_solve_batched": (i32, [vp, i32, i32, pi32]),
     "pm_tcd_create": (i32, [vp, vp, C.POINTER(CdCoeffs), vp, i32, C.c_char_p, C.POINTER(vp)]),
     "pm_tcd_destroy": (None, [vp]),
     "pm_tcd_assemble_initial_time": (i32, [vp]),

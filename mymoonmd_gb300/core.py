@@ -521,6 +521,18 @@ class ConvectionDiffusion:
 
 
 
+def solve_batched(problems, slots: int = 8) -> list:
+    """pm_problem_solve_batched: assembled ConvectionDiffusion problems of one
+    set-up and one context solved together, at most `slots` in lockstep (every
+    kernel of an Arnoldi step runs once for all of them). Returns the status of
+    each problem; last_info() and solution() hold each result."""
+    n = len(problems)
+    arr = (C.c_void_p * n)(*[p.handle for p in problems])
+    st = (C.c_int * n)()
+    check(lib.pm_problem_solve_batched(arr, n, slots, st), problems[0].ctx.handle)
+    return list(st)
+
+
 class TimeConvectionDiffusion(ConvectionDiffusion):
     """TimeConvectionDiffusion<d> on one GPU (src/System/TimeConvectionDiffusion.C)
     with TimeDiscretization's backward_euler, crank_nicolson and bdf_two. The

@@ -112,7 +112,6 @@ struct pm_ctx {
   // device flag passed to the SpMV-family and Vanka launches of this context
   // while set (nullptr = none): a set flag turns those launches into no-ops
   const int* guard = nullptr;
-  // set by kernels whose bounded waits gave up (checked after each solve)
   // FP32 SpMV by the sliced-ELL kernel: 0 = off, else 100 L + 10 U + P (L lanes
   // per row, U steps in flight, P = 1: next steps' loads issued before the
   // current gathers); the matrix copies are laid out for L in make_fp32

@@ -1609,3 +1609,328 @@ void DenseInverse::solve(pm_ctx* c, const DevCsr& A, const double* b, double* x,
 }
 
 }  // namespace pm
+
+// ---------------------------------------------------------------------------
+// Batched launches (pm_batch.h): the same operation for the slots of a batch
+// in one launch (the slot is blockIdx.x in the SpMV family, blockIdx.y
+// elsewhere). The SpMV family runs csr_body / sell_body,
+// the other kernels restate the single-problem loops line for line, so each
+// slot gets the bits a lone launch gives.
+#include "pm_batch.h"
+
+namespace pm {
+
+// SpMV-family launches: bt.vals holds two pointers per slot, the sliced-ELL
+// values [2 s] and the CSR values [2 s + 1]; bt.aux the slot's diagonal
+template <class TV, class TX, class TA, int G, int U, int EPI>
+__global__ void __launch_bounds__(256)
+csr_batch_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+                 const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
+                 const TX* __restrict__ b, const TX* __restrict__ diag, TA alpha, BlockMask mask, Batch bt) {
+  const int s = blockIdx.x;
+  if (!bt.on[s]) return;
+  const TV* v = bt.vals ? static_cast<const TV*>(bt.vals[2 * s + 1]) : vals;
+  const TX* d = bt.aux ? static_cast<const TX*>(bt.aux[s]) : diag;
+  const TX* xs = slot_ptr(x, bt, s);
+  csr_body<TV, TX, TA, G, U, EPI>(n_rows, row_ptr, cols, v, xs, slot_ptr(y, bt, s), slot_ptr(b, bt, s), d, xs,
+                                  alpha, mask, blockIdx.y, gridDim.y);
+}
+
+template <class T, int L, int U, bool PIPE, int EPI>
+__global__ void __launch_bounds__(128)
+sell_batch_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ soff,
+                  const int* __restrict__ scols, const T* __restrict__ svals, const T* __restrict__ x,
+                  T* __restrict__ y, const T* __restrict__ b, const T* __restrict__ diag, T alpha, BlockMask mask,
+                  Batch bt) {
+  const int s = blockIdx.x;
+  if (!bt.on[s]) return;
+  const T* v = bt.vals ? static_cast<const T*>(bt.vals[2 * s]) : svals;
+  const T* d = bt.aux ? static_cast<const T*>(bt.aux[s]) : diag;
+  sell_body<T, L, U, PIPE, EPI>(n_slices, perm, soff, scols, v, slot_ptr(x, bt, s), slot_ptr(y, bt, s),
+                                slot_ptr(b, bt, s), d, alpha, mask, blockIdx.y);
+}
+
+template <class T, int L, int U, bool P, int EPI>
+static void launch_sell_batch_epi(pm_ctx* c, const DevCsr& A, int ns, const Batch& bt, const T* x, T* y, const T* b,
+                                  const T* d, T alpha, const BlockMask& m) {
+  cudaLaunchConfig_t cfg = {};
+  if (nblocks(A.n_slices, 4) > 65535) throw Error(PM_E_UNSUPPORTED, "batched launch: too many row blocks");
+  cfg.gridDim = dim3(unsigned(ns), unsigned(nblocks(A.n_slices, 4)));
+  cfg.blockDim = dim3(128);
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = c->pdl >= 1 ? 1 : 0;
+  PM_CUDA(cudaLaunchKernelEx(&cfg, sell_batch_kernel<T, L, U, P, EPI>, A.n_slices, (const int*)A.sell_perm.p,
+                             (const int*)A.sell_off.p, (const int*)A.sell_cols.p, sell_values<T>(A), x, y, b, d,
+                             alpha, m, bt));
+  c->kernel_launches++;
+}
+
+template <class T, int L, int U, bool P>
+static void launch_sell_batch(pm_ctx* c, const DevCsr& A, int ns, const Batch& bt, int epi, const T* x, T* y,
+                              const T* b, const T* d, T alpha, const BlockMask& m) {
+  switch (epi) {
+    case EPI_AXPY: launch_sell_batch_epi<T, L, U, P, EPI_AXPY>(c, A, ns, bt, x, y, b, d, alpha, m); break;
+    case EPI_SET: launch_sell_batch_epi<T, L, U, P, EPI_SET>(c, A, ns, bt, x, y, b, d, alpha, m); break;
+    case EPI_DEFECT: launch_sell_batch_epi<T, L, U, P, EPI_DEFECT>(c, A, ns, bt, x, y, b, d, alpha, m); break;
+    case EPI_JACOBI: launch_sell_batch_epi<T, L, U, P, EPI_JACOBI>(c, A, ns, bt, x, y, b, d, alpha, m); break;
+    case EPI_RESTRICT: launch_sell_batch_epi<T, L, U, P, EPI_RESTRICT>(c, A, ns, bt, x, y, b, d, alpha, m); break;
+    case EPI_PROLONG: launch_sell_batch_epi<T, L, U, P, EPI_PROLONG>(c, A, ns, bt, x, y, b, d, alpha, m); break;
+    default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
+  }
+}
+
+template <class TV, class TX, class TA, int G, int U>
+static void launch_csr_batch_gu(pm_ctx* c, int ns, const Batch& bt, int epi, int n, const DevCsr& A, const TV* v,
+                                const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
+  if (nblocks((long long)n * G, 256) > 65535) throw Error(PM_E_UNSUPPORTED, "batched launch: too many row blocks");
+  const dim3 gr = dim3(unsigned(ns), unsigned(nblocks((long long)n * G, 256))), bl = dim3(256);
+  const int* rp = A.row_ptr.p;
+  const int* ci = A.cols.p;
+  switch (epi) {
+    case EPI_AXPY: csr_batch_kernel<TV, TX, TA, G, U, EPI_AXPY><<<gr, bl, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, alpha, m, bt); break;
+    case EPI_SET: csr_batch_kernel<TV, TX, TA, G, U, EPI_SET><<<gr, bl, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, alpha, m, bt); break;
+    case EPI_DEFECT: csr_batch_kernel<TV, TX, TA, G, U, EPI_DEFECT><<<gr, bl, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, alpha, m, bt); break;
+    case EPI_JACOBI: csr_batch_kernel<TV, TX, TA, G, U, EPI_JACOBI><<<gr, bl, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, alpha, m, bt); break;
+    case EPI_RESTRICT: csr_batch_kernel<TV, TX, TA, G, U, EPI_RESTRICT><<<gr, bl, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, alpha, m, bt); break;
+    case EPI_PROLONG: csr_batch_kernel<TV, TX, TA, G, U, EPI_PROLONG><<<gr, bl, 0, c->stream>>>(n, rp, ci, v, x, y, b, d, alpha, m, bt); break;
+    default: throw Error(PM_E_INVALID, "unknown SpMV epilogue");
+  }
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+// the launch shapes DevCsr::upload picks: FP64 four lanes x four or eight
+// loads, FP32 four x four or eight x sixteen
+template <class TV, class TX, class TA>
+static void launch_csr_batch(pm_ctx* c, int ns, const Batch& bt, int epi, int n, const DevCsr& A, const TV* v,
+                             const TX* x, TX* y, const TX* b, const TX* d, TA alpha, const BlockMask& m) {
+  const bool fp32 = sizeof(TV) == 4;
+  const int G = fp32 ? A.lanes32 : A.lanes;
+  const int U = fp32 ? A.unroll32 : A.unroll;
+  if (G == 4 && U == 4) launch_csr_batch_gu<TV, TX, TA, 4, 4>(c, ns, bt, epi, n, A, v, x, y, b, d, alpha, m);
+  else if (G == 4 && U == 8) launch_csr_batch_gu<TV, TX, TA, 4, 8>(c, ns, bt, epi, n, A, v, x, y, b, d, alpha, m);
+  else if (G == 8 && U == 16) launch_csr_batch_gu<TV, TX, TA, 8, 16>(c, ns, bt, epi, n, A, v, x, y, b, d, alpha, m);
+  else throw Error(PM_E_UNSUPPORTED, "batched CSR launch shape " + std::to_string(G) + "x" + std::to_string(U));
+}
+
+void csr_apply_batch(pm_ctx* c, const DevCsr& A, int ns, const Batch& bt, int epi, const double* x, double* y,
+                     const double* b, double alpha) {
+  const int n = A.n_rows;
+  if (n <= 0) return;
+  if (A.stream && A.n_rblocks > 0) throw Error(PM_E_UNSUPPORTED, "batched launch of the streaming CSR kernel");
+  if (c->sell_shape64 > 0 && A.sell64_ok && A.sell_lanes == c->sell_shape64 / 100 && A.n_slices > 0) {
+    switch (c->sell_shape64) {
+      case 441: launch_sell_batch<double, 4, 4, true>(c, A, ns, bt, epi, x, y, b, A.diag.p, alpha, A.mask); break;
+      case 481: launch_sell_batch<double, 4, 8, true>(c, A, ns, bt, epi, x, y, b, A.diag.p, alpha, A.mask); break;
+      case 841: launch_sell_batch<double, 8, 4, true>(c, A, ns, bt, epi, x, y, b, A.diag.p, alpha, A.mask); break;
+      default: throw Error(PM_E_INVALID, "unknown FP64 sliced SpMV shape");
+    }
+    PM_CHECK_LAUNCH();
+    return;
+  }
+  launch_csr_batch<double, double, double>(c, ns, bt, epi, n, A, A.vals.p, x, y, b, A.diag.p, alpha, A.mask);
+}
+
+void csr_apply32_batch(pm_ctx* c, const DevCsr& A, int ns, const Batch& bt, int epi, const float* x, float* y,
+                       const float* b, float alpha) {
+  const int n = A.n_rows;
+  if (n <= 0) return;
+  if (A.stream && A.n_rblocks > 0) throw Error(PM_E_UNSUPPORTED, "batched launch of the streaming CSR kernel");
+  if (c->sell_shape > 0 && A.sell_lanes == c->sell_shape / 100 && A.n_slices > 0) {
+    switch (c->sell_shape) {
+      case 441: launch_sell_batch<float, 4, 4, true>(c, A, ns, bt, epi, x, y, b, A.diag32.p, alpha, A.mask); break;
+      case 481: launch_sell_batch<float, 4, 8, true>(c, A, ns, bt, epi, x, y, b, A.diag32.p, alpha, A.mask); break;
+      case 841: launch_sell_batch<float, 8, 4, true>(c, A, ns, bt, epi, x, y, b, A.diag32.p, alpha, A.mask); break;
+      case 881: launch_sell_batch<float, 8, 8, true>(c, A, ns, bt, epi, x, y, b, A.diag32.p, alpha, A.mask); break;
+      default: throw Error(PM_E_UNSUPPORTED, "batched launch of sliced shape " + std::to_string(c->sell_shape));
+    }
+    PM_CHECK_LAUNCH();
+    return;
+  }
+  launch_csr_batch<float, float, float>(c, ns, bt, epi, n, A, A.vals32.p, x, y, b, A.diag32.p, alpha, A.mask);
+}
+
+__global__ void kb_copy(long long n, const double* __restrict__ x, double* __restrict__ y, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  x = slot_ptr(x, bt);
+  y = slot_ptr(y, bt);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = x[i];
+}
+__global__ void kb_d2f(long long n, const double* __restrict__ x, float* __restrict__ y, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  x = slot_ptr(x, bt);
+  y = slot_ptr(y, bt);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = float(x[i]);
+}
+__global__ void kb_f2d(long long n, const float* __restrict__ x, double* __restrict__ y, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  x = slot_ptr(x, bt);
+  y = slot_ptr(y, bt);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = double(x[i]);
+}
+template <class T>
+__global__ void kb_init_sol(int n, BlockMask m, const T* __restrict__ rhs, T* __restrict__ sol, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  rhs = slot_ptr(rhs, bt);
+  sol = slot_ptr(sol, bt);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    sol[i] = row_is_active(m, i) ? T(0) : rhs[i];
+}
+template <class T>
+__global__ void kb_jacobi_zero(int n, const T* __restrict__ b, T w, T* __restrict__ x, Batch bt) {
+  const int s = blockIdx.y;
+  if (!bt.on[s]) return;
+  const T* d = static_cast<const T*>(bt.aux[s]);
+  b = slot_ptr(b, bt);
+  x = slot_ptr(x, bt);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = fmadd(w, (b[i] - T(0)) / d[i], T(0));
+}
+
+#define PM_LAUNCH_BATCH(kern, ns, n, ...)                                                       \
+  do {                                                                                          \
+    if ((n) > 0) {                                                                              \
+      kern<<<dim3(unsigned(grid_for(c, (n))), unsigned(ns)), 256, 0, c->stream>>>(__VA_ARGS__); \
+      PM_CHECK_LAUNCH();                                                                        \
+      c->kernel_launches++;                                                                     \
+    }                                                                                           \
+  } while (0)
+
+void vcopy_batch(pm_ctx* c, int ns, const Batch& bt, int n, const double* x, double* y) {
+  PM_LAUNCH_BATCH(kb_copy, ns, n, n, x, y, bt);
+}
+void vcvt_d2f_batch(pm_ctx* c, int ns, const Batch& bt, int n, const double* x, float* y) {
+  PM_LAUNCH_BATCH(kb_d2f, ns, n, n, x, y, bt);
+}
+void vcvt_f2d_batch(pm_ctx* c, int ns, const Batch& bt, int n, const float* x, double* y) {
+  PM_LAUNCH_BATCH(kb_f2d, ns, n, n, x, y, bt);
+}
+template <class T>
+void init_solution_batch(pm_ctx* c, int ns, const Batch& bt, int n, const BlockMask& m, const T* rhs, T* sol) {
+  PM_LAUNCH_BATCH(kb_init_sol<T>, ns, n, n, m, rhs, sol, bt);
+}
+template void init_solution_batch<float>(pm_ctx*, int, const Batch&, int, const BlockMask&, const float*, float*);
+template void init_solution_batch<double>(pm_ctx*, int, const Batch&, int, const BlockMask&, const double*, double*);
+template <class T>
+void jacobi_from_zero_batch(pm_ctx* c, int ns, const Batch& bt, int n, const T* b, T w, T* x) {
+  PM_LAUNCH_BATCH(kb_jacobi_zero<T>, ns, n, n, b, w, x, bt);
+}
+template void jacobi_from_zero_batch<float>(pm_ctx*, int, const Batch&, int, const float*, float, float*);
+template void jacobi_from_zero_batch<double>(pm_ctx*, int, const Batch&, int, const double*, double, double*);
+
+// the coarse-grid inverse of slot s is bt.aux[s]; act / pos are the same for
+// every slot (one set-up)
+__global__ void kb_coarse_gemv32(int n, int na, const int* __restrict__ act, const int* __restrict__ pos,
+                                 const float* __restrict__ b, float* __restrict__ x, Batch bt) {
+  const int s = blockIdx.y;
+  if (!bt.on[s]) return;
+  const float* inv = static_cast<const float*>(bt.aux[s]);
+  b = slot_ptr(b, bt);
+  x = slot_ptr(x, bt);
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp < na) {
+    const float* row = inv + (size_t)warp * na;
+    float sum = 0.0f;
+    for (int j = lane; j < na; j += 32) sum += row[j] * b[act[j]];
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+    if (lane == 0) x[act[warp]] = sum;
+  } else {
+    const int t = (warp - na) * 32 + lane;
+    if (t < n && pos[t] < 0) x[t] = b[t];
+  }
+}
+// the FP64 coarse solve of a right-hand side with zero non-actives (the
+// gather form of k_coarse_gemv)
+__global__ void kb_coarse_gemv(int n, int na, const int* __restrict__ act, const int* __restrict__ pos,
+                               const double* __restrict__ b, double* __restrict__ x, Batch bt) {
+  const int s = blockIdx.y;
+  if (!bt.on[s]) return;
+  const double* inv = static_cast<const double*>(bt.aux[s]);
+  b = slot_ptr(b, bt);
+  x = slot_ptr(x, bt);
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp < na) {
+    const double* row = inv + (size_t)warp * na;
+    double sum = 0.0;
+    for (int j = lane; j < na; j += 32) sum += row[j] * b[act[j]];
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+    if (lane == 0) x[act[warp]] = sum;
+  } else {
+    const int t = (warp - na) * 32 + lane;
+    if (t < n && pos[t] < 0) x[t] = b[t];
+  }
+}
+
+void coarse_solve32_batch(pm_ctx* c, int ns, const Batch& bt, const DenseInverse& inv0, const float* b, float* x) {
+  const long long threads = (long long)(inv0.na + (inv0.n + 31) / 32) * 32;
+  kb_coarse_gemv32<<<dim3(unsigned(nblocks(threads, 256)), unsigned(ns)), 256, 0, c->stream>>>(
+      inv0.n, inv0.na, inv0.act.p, inv0.pos.p, b, x, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+void coarse_solve_batch(pm_ctx* c, int ns, const Batch& bt, const DenseInverse& inv0, const double* b, double* x) {
+  const long long threads = (long long)(inv0.na + (inv0.n + 31) / 32) * 32;
+  kb_coarse_gemv<<<dim3(unsigned(nblocks(threads, 256)), unsigned(ns)), 256, 0, c->stream>>>(
+      inv0.n, inv0.na, inv0.act.p, inv0.pos.p, b, x, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+__global__ void __launch_bounds__(256) kb_dot_partials(int n, const double* __restrict__ x,
+                                                       const double* __restrict__ y, double* __restrict__ part,
+                                                       Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  x = slot_ptr(x, bt);
+  y = slot_ptr(y, bt);
+  part = slot_ptr(part, bt);
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += x[i] * y[i];
+  double r = block_sum(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+__global__ void kb_finish_sum(const double* __restrict__ part, int np, double* out, int take_sqrt, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  part = slot_ptr(part, bt);
+  out = slot_ptr(out, bt);
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  double r = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = take_sqrt ? sqrt(r) : r;
+}
+void dot_partials_batch(pm_ctx* c, int ns, const Batch& bt, int n, const double* x, const double* y, double* part) {
+  kb_dot_partials<<<dim3(kRedBlocks, unsigned(ns)), kRedThreads, 0, c->stream>>>(n, x, y, part, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+void finish_sum_batch(pm_ctx* c, int ns, const Batch& bt, const double* part, double* out, bool take_sqrt) {
+  kb_finish_sum<<<dim3(1, unsigned(ns)), 256, 0, c->stream>>>(part, kRedBlocks, out, take_sqrt ? 1 : 0, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+__global__ void kb_nonactive_nonzero(BlockMask m, const double* __restrict__ x, int* __restrict__ flag, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  x = slot_ptr(x, bt);
+  flag = slot_ptr(flag, bt);
+  for (int b = 0; b < m.nb; ++b)
+    for (int i = m.active_end[b] + blockIdx.x * blockDim.x + threadIdx.x; i < m.end[b]; i += gridDim.x * blockDim.x)
+      if (x[i] != 0.0) *flag = 1;
+}
+void nonactive_nonzero_batch(pm_ctx* c, int ns, const Batch& bt, const BlockMask& m, const double* x, int* flag) {
+  kb_nonactive_nonzero<<<dim3(kRedBlocks, unsigned(ns)), 256, 0, c->stream>>>(m, x, flag, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+}  // namespace pm

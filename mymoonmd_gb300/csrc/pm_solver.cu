@@ -13,6 +13,7 @@
 #include <sstream>
 
 #include "pm_solver.h"
+#include "pm_batch.h"
 
 namespace pm {
 
@@ -496,7 +497,7 @@ __global__ void __launch_bounds__(256) k_fg_mgs(int n, int ldh, int k, int i, do
 }
 
 // H(i+1,i) = |r|; v_{i+1} = r * (1/H(i+1,i))
-__global__ void __launch_bounds__(256) k_fg_normalize(int n, int ldh, int i, const double* __restrict__ r,
+__device__ __forceinline__ void fg_normalize_body(int n, int ldh, int i, const double* __restrict__ r,
                                                       double* __restrict__ v,
                                                       const double* __restrict__ part_in,
                                                       double* __restrict__ H, int* __restrict__ flag) {
@@ -511,9 +512,15 @@ __global__ void __launch_bounds__(256) k_fg_normalize(int n, int ldh, int i, con
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x)
     v[idx] = r[idx] * sc;
 }
+__global__ void __launch_bounds__(256) k_fg_normalize(int n, int ldh, int i, const double* __restrict__ r,
+                                                      double* __restrict__ v,
+                                                      const double* __restrict__ part_in,
+                                                      double* __restrict__ H, int* __restrict__ flag) {
+  fg_normalize_body(n, ldh, i, r, v, part_in, H, flag);
+}
 
 // beta = |r|; v_0 = r * (1/beta); s = (beta, 0, ...)
-__global__ void __launch_bounds__(256) k_fg_start(int n, int m, const double* __restrict__ r,
+__device__ __forceinline__ void fg_start_body(int n, int m, const double* __restrict__ r,
                                                   double* __restrict__ v0,
                                                   const double* __restrict__ part_in,
                                                   double* __restrict__ s, double* __restrict__ beta_out) {
@@ -526,6 +533,12 @@ __global__ void __launch_bounds__(256) k_fg_start(int n, int m, const double* __
   const double sc = 1.0 / beta;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x)
     v0[idx] = r[idx] * sc;
+}
+__global__ void __launch_bounds__(256) k_fg_start(int n, int m, const double* __restrict__ r,
+                                                  double* __restrict__ v0,
+                                                  const double* __restrict__ part_in,
+                                                  double* __restrict__ s, double* __restrict__ beta_out) {
+  fg_start_body(n, m, r, v0, part_in, s, beta_out);
 }
 
 // Classical Gram-Schmidt with one re-orthogonalisation (CGS2), the batched
@@ -568,7 +581,7 @@ __global__ void __launch_bounds__(256) k_multidot(int n, int nk, const double* _
 // h[k] = sum of the partials of projection k (one block per k); with hsum,
 // also H(k, col) = hsum[k] + h[k]
 // guard set (second pass skipped): h[k] = 0 and H(k, col) = hsum[k]
-__global__ void __launch_bounds__(256) k_reduce_proj(const double* __restrict__ part, double* __restrict__ h,
+__device__ __forceinline__ void reduce_proj_body(const double* __restrict__ part, double* __restrict__ h,
                                                      const double* __restrict__ hsum, double* __restrict__ H,
                                                      int ldh, int col, const int* __restrict__ guard) {
   pdl_enter();
@@ -586,6 +599,11 @@ __global__ void __launch_bounds__(256) k_reduce_proj(const double* __restrict__ 
     h[k] = s;
     if (hsum) H[k + (size_t)ldh * col] = hsum[k] + s;
   }
+}
+__global__ void __launch_bounds__(256) k_reduce_proj(const double* __restrict__ part, double* __restrict__ h,
+                                                     const double* __restrict__ hsum, double* __restrict__ H,
+                                                     int ldh, int col, const int* __restrict__ guard) {
+  reduce_proj_body(part, h, hsum, H, ldh, col, guard);
 }
 
 // r -= sum_k h[k] V_k, subtracted in k order
@@ -687,7 +705,7 @@ __device__ __forceinline__ void cgs_dot_chunk(double (&acc)[NK], int c, int rem,
 
 // partials of <r, V_k>, k < nk <= NK, in one sweep
 template <int NK>
-__global__ void __launch_bounds__(256, 2) k_mdot(int n, int nk, const double* __restrict__ r,
+__device__ __forceinline__ void mdot_body(int n, int nk, const double* __restrict__ r,
                                                  const double* __restrict__ V, size_t ld, double* __restrict__ part) {
   pdl_enter();
   __shared__ double red[8 * NK];
@@ -699,6 +717,11 @@ __global__ void __launch_bounds__(256, 2) k_mdot(int n, int nk, const double* __
     cgs_chunks<NK>(nk, [&](int c, int rem) { cgs_dot_chunk<NK>(acc, c, rem, ri, idx, V, ld); });
   }
   block_partials_multi<NK>(acc, red, part, nk);
+}
+template <int NK>
+__global__ void __launch_bounds__(256, 2) k_mdot(int n, int nk, const double* __restrict__ r,
+                                                 const double* __restrict__ V, size_t ld, double* __restrict__ part) {
+  mdot_body<NK>(n, nk, r, V, ld, part);
 }
 
 // ri -= sum_k h[k] V_k(idx) in k order (the operations of k_cgs_update)
@@ -725,7 +748,7 @@ __device__ __forceinline__ double cgs_update_entry(double ri, int idx, int nk, c
 
 // r -= sum_k h[k] V_k, then the partials of <r_new, V_k> (nk <= NK)
 template <int NK>
-__global__ void __launch_bounds__(256, 2) k_cgs_update_mdot(int n, int nk, double* __restrict__ r,
+__device__ __forceinline__ void cgs_update_mdot_body(int n, int nk, double* __restrict__ r,
                                                             const double* __restrict__ V, size_t ld,
                                                             const double* __restrict__ h, double* __restrict__ part) {
   pdl_enter();
@@ -743,9 +766,15 @@ __global__ void __launch_bounds__(256, 2) k_cgs_update_mdot(int n, int nk, doubl
   }
   block_partials_multi<NK>(acc, red, part, nk);
 }
+template <int NK>
+__global__ void __launch_bounds__(256, 2) k_cgs_update_mdot(int n, int nk, double* __restrict__ r,
+                                                            const double* __restrict__ V, size_t ld,
+                                                            const double* __restrict__ h, double* __restrict__ part) {
+  cgs_update_mdot_body<NK>(n, nk, r, V, ld, h, part);
+}
 
 // r -= sum_k h[k] V_k, then the block's partial sum of |r_new|^2
-__global__ void __launch_bounds__(256, 2) k_cgs_update_norm(int n, int nk, double* __restrict__ r,
+__device__ __forceinline__ void cgs_update_norm_body(int n, int nk, double* __restrict__ r,
                                                          const double* __restrict__ V, size_t ld,
                                                          const double* __restrict__ h, double* __restrict__ part) {
   pdl_enter();
@@ -769,6 +798,11 @@ __global__ void __launch_bounds__(256, 2) k_cgs_update_norm(int n, int nk, doubl
     for (int w = 0; w < int(blockDim.x >> 5); ++w) sum += red[w];
     part[blockIdx.x] = sum;
   }
+}
+__global__ void __launch_bounds__(256, 2) k_cgs_update_norm(int n, int nk, double* __restrict__ r,
+                                                         const double* __restrict__ V, size_t ld,
+                                                         const double* __restrict__ h, double* __restrict__ part) {
+  cgs_update_norm_body(n, nk, r, V, ld, h, part);
 }
 
 // DGKS test after the first classical Gram-Schmidt pass: the second pass is
@@ -802,7 +836,7 @@ __device__ void app_rot(double& dx, double& dy, double cs, double sn) {
   dx = t;
 }
 
-__global__ void k_fg_givens(int ldh, int i, double* __restrict__ H, double* __restrict__ cs,
+__device__ __forceinline__ void fg_givens_body(int ldh, int i, double* __restrict__ H, double* __restrict__ cs,
                             double* __restrict__ sn, double* __restrict__ s, double* __restrict__ resid) {
   pdl_enter();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -813,9 +847,13 @@ __global__ void k_fg_givens(int ldh, int i, double* __restrict__ H, double* __re
   app_rot(s[i], s[i + 1], cs[i], sn[i]);
   *resid = fabs(s[i + 1]);
 }
+__global__ void k_fg_givens(int ldh, int i, double* __restrict__ H, double* __restrict__ cs,
+                            double* __restrict__ sn, double* __restrict__ s, double* __restrict__ resid) {
+  fg_givens_body(ldh, i, H, cs, sn, s, resid);
+}
 
 // Update (src/Solver/Iteration_gmres.C:152): back-solve H y = s
-__global__ void k_fg_backsolve(int ldh, int k, const double* __restrict__ H,
+__device__ __forceinline__ void fg_backsolve_body(int ldh, int k, const double* __restrict__ H,
                                const double* __restrict__ s, double* __restrict__ y) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   for (int i = 0; i <= k; ++i) y[i] = s[i];
@@ -824,9 +862,13 @@ __global__ void k_fg_backsolve(int ldh, int k, const double* __restrict__ H,
     for (int j = i - 1; j >= 0; --j) y[j] -= H[j + (size_t)ldh * i] * y[i];
   }
 }
+__global__ void k_fg_backsolve(int ldh, int k, const double* __restrict__ H,
+                               const double* __restrict__ s, double* __restrict__ y) {
+  fg_backsolve_body(ldh, k, H, s, y);
+}
 
 // x += sum_j y_j z_j  (accumulated in j order, then added)
-__global__ void __launch_bounds__(256) k_fg_combine(int n, int k, const double* __restrict__ Z, size_t ldz,
+__device__ __forceinline__ void fg_combine_body(int n, int k, const double* __restrict__ Z, size_t ldz,
                                                     const double* __restrict__ y, double* __restrict__ x) {
   __shared__ double ys[64];
   for (int j = threadIdx.x; j <= k; j += blockDim.x) ys[j] = y[j];
@@ -836,6 +878,127 @@ __global__ void __launch_bounds__(256) k_fg_combine(int n, int k, const double* 
     for (int j = 0; j <= k; ++j) acc += ys[j] * Z[(size_t)j * ldz + idx];
     x[idx] += acc;
   }
+}
+__global__ void __launch_bounds__(256) k_fg_combine(int n, int k, const double* __restrict__ Z, size_t ldz,
+                                                    const double* __restrict__ y, double* __restrict__ x) {
+  fg_combine_body(n, k, Z, ldz, y, x);
+}
+
+
+// ---- batched FGMRES launches (pm_batch.h): every pointer is slot 0's and
+// moves by bt.stride to the slot blockIdx.y; the bodies are the kernels' own
+#define PM_SLOT(p) (p) = slot_ptr((p), bt)
+
+__global__ void __launch_bounds__(256) kb_fg_start(int n, int m, const double* __restrict__ r, double* __restrict__ v0,
+                                                   const double* __restrict__ part_in, double* __restrict__ s,
+                                                   double* __restrict__ beta_out, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(r); PM_SLOT(v0); PM_SLOT(part_in); PM_SLOT(s); PM_SLOT(beta_out);
+  fg_start_body(n, m, r, v0, part_in, s, beta_out);
+}
+template <int NK>
+__global__ void __launch_bounds__(256, 2) kb_mdot(int n, int nk, const double* __restrict__ r,
+                                                  const double* __restrict__ V, size_t ld, double* __restrict__ part,
+                                                  Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(r); PM_SLOT(V); PM_SLOT(part);
+  mdot_body<NK>(n, nk, r, V, ld, part);
+}
+__global__ void __launch_bounds__(256) kb_reduce_proj(const double* __restrict__ part, double* __restrict__ h,
+                                                      const double* __restrict__ hsum, double* __restrict__ H, int ldh,
+                                                      int col, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(part); PM_SLOT(h); PM_SLOT(hsum); PM_SLOT(H);
+  reduce_proj_body(part, h, hsum, H, ldh, col, nullptr);
+}
+template <int NK>
+__global__ void __launch_bounds__(256, 2) kb_cgs_update_mdot(int n, int nk, double* __restrict__ r,
+                                                             const double* __restrict__ V, size_t ld,
+                                                             const double* __restrict__ h, double* __restrict__ part,
+                                                             Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(r); PM_SLOT(V); PM_SLOT(h); PM_SLOT(part);
+  cgs_update_mdot_body<NK>(n, nk, r, V, ld, h, part);
+}
+__global__ void __launch_bounds__(256, 2) kb_cgs_update_norm(int n, int nk, double* __restrict__ r,
+                                                             const double* __restrict__ V, size_t ld,
+                                                             const double* __restrict__ h, double* __restrict__ part,
+                                                             Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(r); PM_SLOT(V); PM_SLOT(h); PM_SLOT(part);
+  cgs_update_norm_body(n, nk, r, V, ld, h, part);
+}
+__global__ void __launch_bounds__(256) kb_fg_normalize(int n, int ldh, int i, const double* __restrict__ r,
+                                                       double* __restrict__ v, const double* __restrict__ part_in,
+                                                       double* __restrict__ H, int* __restrict__ flag, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(r); PM_SLOT(v); PM_SLOT(part_in); PM_SLOT(H); PM_SLOT(flag);
+  fg_normalize_body(n, ldh, i, r, v, part_in, H, flag);
+}
+__global__ void kb_fg_givens(int ldh, int i, double* __restrict__ H, double* __restrict__ cs, double* __restrict__ sn,
+                             double* __restrict__ s, double* __restrict__ resid, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(H); PM_SLOT(cs); PM_SLOT(sn); PM_SLOT(s); PM_SLOT(resid);
+  fg_givens_body(ldh, i, H, cs, sn, s, resid);
+}
+__global__ void kb_fg_backsolve(int ldh, int k, const double* __restrict__ H, const double* __restrict__ s,
+                                double* __restrict__ y, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(H); PM_SLOT(s); PM_SLOT(y);
+  fg_backsolve_body(ldh, k, H, s, y);
+}
+__global__ void __launch_bounds__(256) kb_fg_combine(int n, int k, const double* __restrict__ Z, size_t ldz,
+                                                     const double* __restrict__ y, double* __restrict__ x, Batch bt) {
+  if (!bt.on[blockIdx.y]) return;
+  PM_SLOT(Z); PM_SLOT(y); PM_SLOT(x);
+  fg_combine_body(n, k, Z, ldz, y, x);
+}
+#undef PM_SLOT
+
+void fg_start_batch(pm_ctx* c, int ns, const Batch& bt, int n, int m, const double* r, double* v0,
+                    const double* part, double* s, double* beta_out) {
+  kb_fg_start<<<dim3(kRedBlocks, unsigned(ns)), 256, 0, c->stream>>>(n, m, r, v0, part, s, beta_out, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+// the fused CGS2 branch of pm_solver::fgmres for i + 1 <= kCgsFused
+void fg_cgs2_batch(pm_ctx* c, int ns, const Batch& bt, int n, int i, int ldh, double* r, const double* V, size_t ld,
+                   double* cgs_part, double* h1, double* h2, double* H, double* part_norm) {
+  const int nk = i + 1;
+  if (nk > kCgsFused) throw Error(PM_E_UNSUPPORTED, "batched FGMRES needs gmres_restart <= 32");
+  const dim3 rb = dim3(kRedBlocks, unsigned(ns)), pk = dim3(unsigned(nk), unsigned(ns)), t256 = dim3(256);
+  if (nk <= 16) kb_mdot<16><<<rb, t256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part, bt);
+  else kb_mdot<kCgsFused><<<rb, t256, 0, c->stream>>>(n, nk, r, V, ld, cgs_part, bt);
+  kb_reduce_proj<<<pk, t256, 0, c->stream>>>(cgs_part, h1, nullptr, H, ldh, i, bt);
+  if (nk <= 16) kb_cgs_update_mdot<16><<<rb, t256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part, bt);
+  else kb_cgs_update_mdot<kCgsFused><<<rb, t256, 0, c->stream>>>(n, nk, r, V, ld, h1, cgs_part, bt);
+  kb_reduce_proj<<<pk, t256, 0, c->stream>>>(cgs_part, h2, h1, H, ldh, i, bt);
+  kb_cgs_update_norm<<<rb, t256, 0, c->stream>>>(n, nk, r, V, ld, h2, part_norm, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 5;
+}
+
+void fg_normalize_batch(pm_ctx* c, int ns, const Batch& bt, int n, int ldh, int i, const double* r, double* v,
+                        const double* part, double* H, int* flag) {
+  kb_fg_normalize<<<dim3(kRedBlocks, unsigned(ns)), 256, 0, c->stream>>>(n, ldh, i, r, v, part, H, flag, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+void fg_givens_batch(pm_ctx* c, int ns, const Batch& bt, int ldh, int i, double* H, double* cs, double* sn, double* s,
+                     double* resid) {
+  kb_fg_givens<<<dim3(1, unsigned(ns)), 32, 0, c->stream>>>(ldh, i, H, cs, sn, s, resid, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+void fg_update_batch(pm_ctx* c, int ns, const Batch& bt, int n, int ldh, int k, const double* H, const double* s,
+                     double* y, const double* Z, size_t ldz, double* x) {
+  kb_fg_backsolve<<<dim3(1, unsigned(ns)), 32, 0, c->stream>>>(ldh, k, H, s, y, bt);
+  kb_fg_combine<<<dim3(unsigned(grid_blocks_for(n)), unsigned(ns)), 256, 0, c->stream>>>(n, k, Z, ldz, y, x, bt);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 2;
 }
 
 }  // namespace pm

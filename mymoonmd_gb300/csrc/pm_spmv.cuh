@@ -64,21 +64,21 @@ __device__ __forceinline__ void pdl_enter() {
 // value and U column loads, then its U gathers of x, then the U products, so
 // that every lane keeps U independent DRAM requests in flight.
 template <class TV, class TX, class TA, int G, int U, int EPI>
-__global__ void __launch_bounds__(256)
-csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ cols,
-           const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
-           const TX* __restrict__ b, const TX* __restrict__ diag, const TX* __restrict__ xold,
-           TA alpha, BlockMask mask) {
+__device__ __forceinline__ void
+csr_body(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+         const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
+         const TX* __restrict__ b, const TX* __restrict__ diag, const TX* __restrict__ xold,
+         TA alpha, const BlockMask& mask, int bx, int gx) {
   pdl_enter();
   if (guarded(mask.guard)) {  // uniform for the whole grid
     // a skipped Jacobi sweep leaves the iterate as it is (the caller swaps
     // the two iterate buffers after every sweep)
     if (EPI == EPI_JACOBI)
-      for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_rows; i += gridDim.x * blockDim.x) y[i] = xold[i];
+      for (int i = bx * blockDim.x + threadIdx.x; i < n_rows; i += gx * blockDim.x) y[i] = xold[i];
     return;
   }
   const int lane = threadIdx.x & (G - 1);
-  const int row = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int row = (bx * blockDim.x + threadIdx.x) / G;
   const bool valid = row < n_rows;  // whole groups share a row: no early exit before the shuffles
   const int beg = valid ? __ldg(row_ptr + row) : 0;
   const int end = valid ? __ldg(row_ptr + row + 1) : 0;
@@ -132,6 +132,16 @@ csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ 
   } else if constexpr (EPI == EPI_PROLONG) {
     if (row_is_active(mask, row)) y[row] = TX(TA(pre_y) + alpha * s);
   }
+}
+
+template <class TV, class TX, class TA, int G, int U, int EPI>
+__global__ void __launch_bounds__(256)
+csr_kernel(int n_rows, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+           const TV* __restrict__ vals, const TX* __restrict__ x, TX* __restrict__ y,
+           const TX* __restrict__ b, const TX* __restrict__ diag, const TX* __restrict__ xold,
+           TA alpha, BlockMask mask) {
+  csr_body<TV, TX, TA, G, U, EPI>(n_rows, row_ptr, cols, vals, x, y, b, diag, xold, alpha, mask, blockIdx.x,
+                                  gridDim.x);
 }
 
 // Row-block streaming variant. Block b owns the consecutive rows
@@ -240,14 +250,14 @@ template <>
 __device__ __forceinline__ double fmadd<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 template <class T, int L, int U, bool PIPE, int EPI>
-__global__ void __launch_bounds__(128)
-sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ soff,
-            const int* __restrict__ scols, const T* __restrict__ svals, const T* __restrict__ x,
-            T* __restrict__ y, const T* __restrict__ b, const T* __restrict__ diag, T alpha,
-            BlockMask mask) {
+__device__ __forceinline__ void
+sell_body(int n_slices, const int* __restrict__ perm, const int* __restrict__ soff,
+          const int* __restrict__ scols, const T* __restrict__ svals, const T* __restrict__ x,
+          T* __restrict__ y, const T* __restrict__ b, const T* __restrict__ diag, T alpha,
+          const BlockMask& mask, int bx) {
   constexpr int C = 32 / L;
   pdl_trigger();
-  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int s = bx * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (s >= n_slices) return;  // whole warps leave: the shuffles below stay full-warp
   const int lane = threadIdx.x & 31;
   const int p = lane % C, sub = lane / C;
@@ -334,6 +344,15 @@ sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ 
   } else if constexpr (EPI == EPI_PROLONG) {
     if (row_is_active(mask, row)) y[row] = pre_y + alpha * acc;
   }
+}
+
+template <class T, int L, int U, bool PIPE, int EPI>
+__global__ void __launch_bounds__(128)
+sell_kernel(int n_slices, const int* __restrict__ perm, const int* __restrict__ soff,
+            const int* __restrict__ scols, const T* __restrict__ svals, const T* __restrict__ x,
+            T* __restrict__ y, const T* __restrict__ b, const T* __restrict__ diag, T alpha,
+            BlockMask mask) {
+  sell_body<T, L, U, PIPE, EPI>(n_slices, perm, soff, scols, svals, x, y, b, diag, alpha, mask, blockIdx.x);
 }
 
 }  // namespace pm
