@@ -68,6 +68,9 @@ int pm_version(void);
  *   4 restriction, 5 prolongation add; -1 = all);
  *   "probe_precision" 0|4|8 - only launches whose matrix values have this
  *   size in bytes (0 = all);
+ *   "probe_nodal" 0|1 - the launch probe brackets instead the residual and
+ *   local-solve pair of every colour of the multiplicative nodal Vanka
+ *   sweeps (counted as one launch, with the pair's algorithmic bytes);
  *   "fp32_sliced_spmv" 0|100 L + 10 U + P - FP32 SpMV-family launches on
  *   matrices with more than 16 entries per row by the sliced-ELL kernel: L
  *   lanes per row (1, 2, 4, 8), U steps in flight (4, 8), P = 1 issues the next

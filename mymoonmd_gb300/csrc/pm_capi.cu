@@ -117,6 +117,10 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->probe_epilogue = value;
     return PM_OK;
   }
+  if (std::string(key) == "probe_nodal") {
+    c->probe_nodal = value != 0;
+    return PM_OK;
+  }
   if (std::string(key) == "probe_precision") {
     if (value != 0 && value != 4 && value != 8) return fail(c, PM_E_INVALID, "probe_precision is 0, 4 or 8");
     c->probe_precision = value;

@@ -135,6 +135,9 @@ struct pm_ctx {
   int64_t probe_nnz = 0;
   int probe_epilogue = -1;  // only launches with this epilogue (-1 = all)
   int probe_precision = 0;  // only launches with values of this size in bytes (0 = all)
+  // launch probe of the multiplicative nodal Vanka sweeps: events around the
+  // residual + local-solve pair of every colour (option "probe_nodal")
+  int probe_nodal = 0;
   std::vector<cudaEvent_t> probe_events;  // start/end pairs
   std::vector<double> probe_bytes;        // algorithmic bytes of each probed launch
   std::vector<cudaEvent_t> probe_pool;

@@ -370,7 +370,7 @@ static void launch_epi(pm_ctx* c, int G, int U, int n, const int* rp, const int*
   }
 }
 
-static cudaEvent_t probe_event(pm_ctx* c) {
+cudaEvent_t probe_event(pm_ctx* c) {
   if (!c->probe_pool.empty()) {
     cudaEvent_t e = c->probe_pool.back();
     c->probe_pool.pop_back();

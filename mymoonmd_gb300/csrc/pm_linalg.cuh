@@ -76,6 +76,9 @@ std::vector<int> build_row_blocks(int n_rows, const int* rp, int max_nnz, int ma
 bool build_sell_layout(int n_rows, const int* rp, const int* ci, int lanes, int window, std::vector<int>& perm,
                        std::vector<int>& off, std::vector<int>& cols, std::vector<int>& src);
 
+// an event for the launch probe (from the context's pool)
+cudaEvent_t probe_event(pm_ctx* c);
+
 // y := epilogue(A x); see pm_spmv.cuh for the epilogue meanings
 void csr_apply(pm_ctx* c, const DevCsr& A, int epi, const double* x, double* y, const double* b,
                double alpha, int n_rows_override = -1);

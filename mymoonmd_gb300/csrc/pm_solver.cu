@@ -1246,7 +1246,7 @@ void pm_solver::fgmres(const double* rhs, double* sol) {
                                 cudaMemcpyDeviceToHost, c->stream));
       };
       // the probe brackets launches with events one by one: no graphs then
-      const bool graphs = use_graphs && c->probe_nnz == 0;
+      const bool graphs = use_graphs && c->probe_nnz == 0 && !c->probe_nodal;
       // one graph per Arnoldi index and multigrid precision
       const int gi = i + ((use_mg && !mg.mixed && mg.mixed_cfg) ? m : 0);
       if (graphs) {

@@ -690,6 +690,20 @@ void DevNodalVanka::setup(pm_ctx* c, const DiscLevel& L) {
     for (int i = 0; i < np; ++i) cp[fill[color[i]]++] = i;
   }
   color_patches.upload(cp, c->stream);
+  color_entries.assign(n_colors, 0);
+  color_rows.assign(n_colors, 0);
+  color_nodes.assign(n_colors, 0);
+  color_msq.assign(n_colors, 0);
+  for (int i = 0; i < np; ++i) {
+    const int k = color[i], m = vp[i + 1] - vp[i];
+    auto row_len = [&](int g) { return int64_t(S.row_ptr[g + 1] - S.row_ptr[g]); };
+    for (int d = 0; d < 3; ++d)
+      for (int t = vp[i]; t < vp[i + 1]; ++t) color_entries[k] += row_len(d * nu + vi[t]);
+    color_entries[k] += row_len(3 * nu + i);
+    color_rows[k] += 3 * m + 1;
+    color_nodes[k] += m;
+    color_msq[k] += int64_t(m) * m;
+  }
   flag.ensure(1);
 }
 
@@ -1028,11 +1042,27 @@ static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T
     const int beg = nv.color_ptr[k], cnt = nv.color_ptr[k + 1] - beg;
     if (!cnt) continue;
     const int* pts = nv.color_patches.p + beg;
+    if (c->probe_nodal) {
+      cudaEvent_t e0 = probe_event(c);
+      PM_CUDA(cudaEventRecord(e0, c->stream));
+      c->probe_events.push_back(e0);
+      // algorithmic bytes of the pair: the rows' values, column indices and
+      // gathered x, b, the local residuals written and read back, the
+      // inverses (m^2), t and b vectors (6 m), 1/S, and x read and written
+      const double eb = double(sizeof(T));
+      c->probe_bytes.push_back(double(nv.color_entries[k]) * (2 * eb + 4) + double(nv.color_rows[k]) * 5 * eb +
+                               double(nv.color_msq[k]) * eb + double(nv.color_nodes[k]) * 6 * eb + double(cnt) * eb);
+    }
     k_nodal_rhs<T><<<cnt, 512, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
                                                         V.cols.p, vals, b, x, rloc);
     k_nodal_local<T><<<cnt, 512, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
                                                           tb, sinv, nullptr, rloc, nullptr, x, damp);
     c->kernel_launches += 2;
+    if (c->probe_nodal) {
+      cudaEvent_t e1 = probe_event(c);
+      PM_CUDA(cudaEventRecord(e1, c->stream));
+      c->probe_events.push_back(e1);
+    }
   }
   PM_CHECK_LAUNCH();
 }

@@ -100,6 +100,10 @@ struct DevNodalVanka {
   DBuf<float> sinv32;
   DBuf<int> inc_ptr, inc_idx, count;  // per combined DOF: positions in the local storage
   std::vector<int> color_ptr;          // host: colour ranges into color_patches
+  // host, per colour: matrix entries of the patches' rows, the rows (3 m + 1
+  // per patch), the velocity nodes m and the inverse entries m^2 (the launch
+  // probe's algorithmic bytes)
+  std::vector<int64_t> color_entries, color_rows, color_nodes, color_msq;
   DBuf<int> color_patches;
   DBuf<double> sol;  // local corrections / residuals: patch i at 3 vptr[i] + i, 3 n_i + 1 entries
   DBuf<float> sol32;
