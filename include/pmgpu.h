@@ -226,6 +226,19 @@ int pm_solver_apply_preconditioner(pm_solver* s, const double* z_dev, double* r_
  *       1 Stokes P2/P1 Taylor-Hood on tetrahedra (elem ignored). */
 int pm_disc_create(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
                    pm_disc** out);
+/* pm_disc_create with Neumann conditions on some sides of the unit square
+ * (convection-diffusion, geometry 0): bit s of neumann_sides marks side s in
+ * the numbering of UnitSquare's boundary components (Default_UnitSquare):
+ * 0 y=0, 1 x=1, 2 y=1, 3 x=0; the other sides stay Dirichlet. The example's
+ * BoundCondition (e.g. include/Examples/CD_2D/SineLaplace.h: side 1 Neumann)
+ * in mask form. DOFs are numbered inner, Neumann, Dirichlet, each in order of
+ * first touch (TFESpace2D::ConstructSpace); a DOF is Neumann when every side it
+ * lies on is, so corners next to a Dirichlet side are Dirichlet. Neumann DOFs
+ * are active. Assembly adds the boundary integral of the exact solution's flux
+ * eps grad u . n over the Neumann edges (Assemble2D.C:716-757); with a constant
+ * right-hand side (no exact solution) the Neumann data are zero. */
+int pm_disc_create_bc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
+                      int neumann_sides, pm_disc** out);
 void pm_disc_destroy(pm_disc* d);
 /* per level (0 = coarsest kept level): cells, local DOFs per cell, DOFs,
  * active DOFs and nnz of the level matrix (space 0 = velocity/scalar,
@@ -331,6 +344,17 @@ int pm_problem_solution_dev(pm_problem* p, double** sol_dev, double** rhs_dev);
  * finest-level solution copied back into sol_host. */
 int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* coeffs, const double* const* level_verts,
                         double* sol_host);
+/* Errors of the finest-level solution against the exact solution of the
+ * problem's coefficients, as ConvectionDiffusion<d>::output computes them
+ * (src/System/ConvectionDiffusion.C:213-283 with conv_diff_l2_h1_linf_error,
+ * src/AssembleRoutines/ConvDiff.C:2134-2185): errors[0] L2, errors[1]
+ * H1-semi, errors[2] SD (eps |grad e|^2 + c e^2 + delta (b . grad e)^2 with
+ * the SUPG delta of the reference's default parameters), errors[3] L_inf over
+ * the quadrature points, on the assembly's quadrature rule (the rule
+ * TFEDatabase{2,3}D::GetOrig picks). With a constant right-hand side the exact
+ * solution is zero and these are norms of the solution. Convection-diffusion
+ * problems only. */
+int pm_problem_errors(pm_problem* p, double* errors);
 /* Solver statistics of the problem's last solve. */
 int pm_problem_last_info(const pm_problem* p, int* iterations, double* residual,
                          double* initial_residual);

@@ -117,6 +117,7 @@ _SIGS = {
     "pm_solver_residual_history": (i32, [vp, vp, i32, pi32]),
     "pm_solver_apply_preconditioner": (i32, [vp, vp, vp]),
     "pm_disc_create": (i32, [i32, i32, i32, i32, i32, i32, C.POINTER(vp)]),
+    "pm_disc_create_bc": (i32, [i32, i32, i32, i32, i32, i32, i32, C.POINTER(vp)]),
     "pm_disc_destroy": (None, [vp]),
     "pm_disc_level_info": (i32, [vp, i32, i32, pi32, pi32, pi32, pi32, C.POINTER(i64)]),
     "pm_disc_dofmap": (i32, [vp, i32, i32, vp]),
@@ -139,6 +140,7 @@ _SIGS = {
     "pm_problem_solver": (i32, [vp, C.POINTER(vp)]),
     "pm_problem_solution_dev": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "pm_problem_run_host": (i32, [vp, C.POINTER(CdCoeffs), vp, vp]),
+    "pm_problem_errors": (i32, [vp, vp]),
     "pm_problem_last_info": (i32, [vp, pi32, pf64, pf64]),
     "pm_problem_solve_batched": (i32, [vp, i32, i32, pi32]),
     "pm_tcd_create": (i32, [vp, vp, C.POINTER(CdCoeffs), vp, i32, C.c_char_p, C.POINTER(vp)]),

@@ -349,12 +349,14 @@ class Discretization:
     """Mesh hierarchy + FE spaces + structures + transfer (host set-up)."""
 
     def __init__(self, geometry: int, root_n: int, n_refine: int, n_levels: int, kind: int = KIND_CD,
-                 elem: int = 1):
+                 elem: int = 1, neumann_sides: int = 0):
+        """neumann_sides: bit mask of the unit square's sides (0 y=0, 1 x=1,
+        2 y=1, 3 x=0) with Neumann conditions; the others are Dirichlet"""
         h = C.c_void_p()
-        check(lib.pm_disc_create(geometry, root_n, n_refine, n_levels, kind, elem, C.byref(h)))
+        check(lib.pm_disc_create_bc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides, C.byref(h)))
         self.handle = h
         self.geometry, self.root_n, self.n_refine, self.n_levels = geometry, root_n, n_refine, n_levels
-        self.kind, self.elem = kind, elem
+        self.kind, self.elem, self.neumann_sides = kind, elem, neumann_sides
         self.dim = 2 if geometry == GEO_SQUARE_QUAD else 3
 
     def level_info(self, level: int, space: int = 0) -> dict:
@@ -498,6 +500,13 @@ class ConvectionDiffusion:
         it, res, init = C.c_int(), C.c_double(), C.c_double()
         check(lib.pm_problem_last_info(self.handle, C.byref(it), C.byref(res), C.byref(init)))
         return it.value, res.value, init.value
+
+    def errors(self) -> tuple[float, float, float, float]:
+        """(L2, H1-semi, SD, L_inf) errors of the solution against the exact
+        solution, as ConvectionDiffusion<d>::output computes them"""
+        out = np.zeros(4, dtype=np.float64)
+        check(lib.pm_problem_errors(self.handle, _ptr(out)), self.ctx.handle)
+        return tuple(float(v) for v in out)
 
     def run_host(self, coeffs: Optional[CdCoeffs], level_verts, sol_out: np.ndarray) -> None:
         """one request end to end from host memory (pm_problem_run_host)"""

@@ -500,6 +500,271 @@ __global__ void k_dirichlet_poly(int nb, int n_active, const double* __restrict_
 
 double poly_value_host(const double* p, const double* x) { return poly_u(p, x); }
 
+// Exact solution of the coefficient kind and its gradient at x: the sine
+// solution prod sin(pi x_d), the quadratic polynomial, or zero when the
+// right-hand side is a constant (the examples without a known solution set
+// their Exact to zero). out = (u, u_x, u_y, u_z).
+__device__ __forceinline__ void exact_value(const CdCoef& k, int dim, const double* xin, double* out) {
+  const double x[3] = {xin[0], xin[1], dim == 3 ? xin[2] : 0.0};
+  out[0] = out[1] = out[2] = out[3] = 0.0;
+  if (k.manufactured == 2) {
+    const double* p = k.poly;
+    out[0] = poly_u(p, x);
+    out[1] = p[1] + 2 * p[4] * x[0] + p[7] * x[1] + p[8] * x[2];
+    out[2] = p[2] + 2 * p[5] * x[1] + p[7] * x[0] + p[9] * x[2];
+    out[3] = dim == 3 ? p[3] + 2 * p[6] * x[2] + p[8] * x[0] + p[9] * x[1] : 0.0;
+  } else if (k.manufactured == 1) {
+    const double pi = 3.14159265358979323846;
+    double s[3], co[3];
+    for (int d = 0; d < dim; ++d) {
+      s[d] = sin(pi * x[d]);
+      co[d] = cos(pi * x[d]);
+    }
+    if (dim == 2) {
+      out[0] = s[0] * s[1];
+      out[1] = pi * co[0] * s[1];
+      out[2] = pi * s[0] * co[1];
+    } else {
+      out[0] = s[0] * s[1] * s[2];
+      out[1] = pi * co[0] * s[1] * s[2];
+      out[2] = pi * s[0] * co[1] * s[2];
+      out[3] = pi * s[0] * s[1] * co[2];
+    }
+  }
+}
+
+// Neumann boundary integral (Assemble2D.C:716-757): for every edge on a
+// Neumann side, rhs_i += sum_l g(x_l) hE w_l phi_i(xi_l) over the line Gauss
+// rule of degree 2k (Gauss2 for Q1, Gauss3 for Q2), hE half the edge length,
+// xi_l on edge m of [-1,1]^2 (vertex m to m+1, BaseFunct2D.C:87-118), only for
+// active DOFs. g = eps grad u . n is the Neumann datum of the exact solution
+// (SineLaplace's BoundValue on x = 1). One thread per DOF on a Neumann edge
+// adds its edges in cell order, so the sum is deterministic.
+struct LineRule {
+  int n;
+  double z[4], w[4];
+};
+
+template <int K>
+__global__ void k_neumann_rhs(int nt, const int* __restrict__ dof, const int* __restrict__ ptr,
+                              const int* __restrict__ cell, const int* __restrict__ code,
+                              const double* __restrict__ verts, CdCoef co, LineRule lr,
+                              double* __restrict__ rhs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const int g = dof[t];
+  double acc = rhs[g];
+  for (int e = ptr[t]; e < ptr[t + 1]; ++e) {
+    const int c = cell[e], cd = code[e];
+    const int m = cd & 3, side = (cd >> 2) & 3, loc = cd >> 4;
+    const int m1 = (m + 1) & 3;
+    const double* v = verts + size_t(c) * 8;
+    const double ax = v[2 * m], ay = v[2 * m + 1], bx = v[2 * m1], by = v[2 * m1 + 1];
+    const double hE = sqrt((bx - ax) * (bx - ax) + (by - ay) * (by - ay)) / 2;
+    // reference vertices (-1,-1) (1,-1) (1,1) (-1,1)
+    const double r0x = (m == 1 || m == 2) ? 1.0 : -1.0, r0y = m >= 2 ? 1.0 : -1.0;
+    const double r1x = (m1 == 1 || m1 == 2) ? 1.0 : -1.0, r1y = m1 >= 2 ? 1.0 : -1.0;
+    const int a = loc % (K + 1), b = loc / (K + 1);
+    for (int l = 0; l < lr.n; ++l) {
+      const double f = 0.5 * (lr.z[l] + 1.0);
+      const double xi = r0x + f * (r1x - r0x), eta = r0y + f * (r1y - r0y);
+      double lx[3], ly[3];
+      if (K == 1) {
+        lx[0] = 0.5 * (1.0 - xi); lx[1] = 0.5 * (1.0 + xi);
+        ly[0] = 0.5 * (1.0 - eta); ly[1] = 0.5 * (1.0 + eta);
+      } else {
+        lx[0] = 0.5 * xi * (xi - 1.0); lx[1] = 1.0 - xi * xi; lx[2] = 0.5 * xi * (xi + 1.0);
+        ly[0] = 0.5 * eta * (eta - 1.0); ly[1] = 1.0 - eta * eta; ly[2] = 0.5 * eta * (eta + 1.0);
+      }
+      const double x[3] = {ax + f * (bx - ax), ay + f * (by - ay), 0.0};
+      double u[4];
+      exact_value(co, 2, x, u);
+      // outward normals of the sides y=0, x=1, y=1, x=0
+      const double gn = side == 0 ? -u[2] : side == 1 ? u[1] : side == 2 ? u[2] : -u[1];
+      double sv = co.eps * gn;
+      sv *= hE * lr.w[l];
+      acc += sv * (lx[a] * ly[b]);
+    }
+  }
+  rhs[g] = acc;
+}
+
+void launch_neumann_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs) {
+  const int nt = int(L.nm_dof.n);
+  // homogeneous Neumann data when the solution is not known (constant f)
+  if (nt == 0 || cf.manufactured == 0) return;
+  const int k = L.nloc == 9 ? 2 : 1;
+  std::vector<double> z, w;
+  gauss1d(k + 1, z, w);
+  LineRule lr{};
+  lr.n = k + 1;
+  for (int l = 0; l < lr.n; ++l) {
+    lr.z[l] = z[l];
+    lr.w[l] = w[l];
+  }
+  const CdCoef co = make_coef(cf);
+  const int grid = (nt + 127) / 128;
+  if (k == 1)
+    k_neumann_rhs<1><<<grid, 128, 0, c->stream>>>(nt, L.nm_dof.p, L.nm_ptr.p, L.nm_cell.p, L.nm_code.p,
+                                                   L.verts.p, co, lr, rhs);
+  else
+    k_neumann_rhs<2><<<grid, 128, 0, c->stream>>>(nt, L.nm_dof.p, L.nm_ptr.p, L.nm_cell.p, L.nm_code.p,
+                                                   L.verts.p, co, lr, rhs);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+// Error functional of ConvectionDiffusion<d>::output (ConvectionDiffusion.C:213-283):
+// TFEFunction{2,3}D::GetErrors (FEFunction2D.C:318-575, FEFunction3D.C:80-245)
+// with conv_diff_l2_h1_linf_error (ConvDiff.C:2134-2185). Per cell and
+// quadrature point, e = u_h - u, w = weight |det J|:
+//   L2^2 += w e^2,  H1^2 += w |grad e|^2,  L_inf = max |e|,
+//   SD^2 += w (eps |grad e|^2 + c e^2 + delta (b . grad e)^2)
+// with the SUPG parameter delta of Compute_SDFEM_delta (ConvDiff.C:273-360)
+// at the reference's defaults (SDFEM_TYPE 2, DELTA0 1, polynomial degree 1,
+// CELL_MEASURE 0: hK = cell diameter). One thread per cell; each block sums
+// its cells by a fixed tree into one partial, a second kernel sums the
+// partials in a fixed order: the result does not depend on scheduling.
+template <int DIM, int NB, int NQ>
+__global__ void __launch_bounds__(128) k_cd_errors(int n_cells, const double* __restrict__ verts,
+                                                   const int* __restrict__ dofmap, const double* __restrict__ u,
+                                                   const double* __restrict__ ref, CdCoef co,
+                                                   double* __restrict__ partial) {
+  constexpr int NV = DIM == 2 ? 4 : 8;
+  __shared__ double red[4][128];
+  const int cell = blockIdx.x * 128 + threadIdx.x;
+  double loc[4] = {0.0, 0.0, 0.0, 0.0};
+  if (cell < n_cells) {
+    const double* v = verts + size_t(cell) * NV * DIM;
+    double x0[3] = {0, 0, 0}, J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    affine_map<DIM>(v, x0, J);
+    double G[3][3] = {{0}}, det;
+    if (DIM == 2) {
+      det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      const double r = 1.0 / det;
+      G[0][0] = J[1][1] * r;  G[0][1] = -J[1][0] * r;
+      G[1][0] = -J[0][1] * r; G[1][1] = J[0][0] * r;
+    } else {
+      det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+            J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+            J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      const double r = 1.0 / det;
+      G[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * r;
+      G[0][1] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) * r;
+      G[0][2] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * r;
+      G[1][0] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * r;
+      G[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+      G[1][2] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * r;
+      G[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+      G[2][1] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) * r;
+      G[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    }
+    const double adet = fabs(det);
+    // cell diameter: the largest distance between two vertices
+    double hk2 = 0.0;
+    for (int i = 0; i < NV; ++i)
+      for (int j = i + 1; j < NV; ++j) {
+        double s = 0.0;
+        for (int d = 0; d < DIM; ++d) s += (v[i * DIM + d] - v[j * DIM + d]) * (v[i * DIM + d] - v[j * DIM + d]);
+        hk2 = fmax(hk2, s);
+      }
+    const double hK = sqrt(hk2);
+    const double bv[3] = {co.b0, co.b1, DIM == 3 ? co.b2 : 0.0};
+    const double eps = fabs(co.eps) < 1e-20 ? 1e-20 : co.eps;
+    const double norm_b = sqrt(bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]);
+    double delta = 0.0;
+    if (norm_b > 0) {
+      const double alpha = norm_b * hK / (2 * eps);
+      delta = hK * (1 / tanh(alpha) - 1 / alpha) / (2 * norm_b);
+    }
+    double uc[NB];
+    for (int i = 0; i < NB; ++i) uc[i] = u[dofmap[size_t(cell) * NB + i]];
+    const double* phi = ref;
+    const double* dphi = ref + NQ * NB;
+    const double* w = ref + 4 * NQ * NB;
+    const double* xi = w + NQ;
+    for (int q = 0; q < NQ; ++q) {
+      double val = 0.0, dr[3] = {0.0, 0.0, 0.0};
+      for (int i = 0; i < NB; ++i) {
+        val += uc[i] * phi[q * NB + i];
+        for (int a = 0; a < DIM; ++a) dr[a] += uc[i] * dphi[(a * NQ + q) * NB + i];
+      }
+      double grad[3] = {0.0, 0.0, 0.0};
+      for (int d = 0; d < DIM; ++d)
+        for (int a = 0; a < DIM; ++a) grad[d] += G[d][a] * dr[a];
+      double x[3];
+      for (int d = 0; d < DIM; ++d) {
+        double s = x0[d];
+        for (int a = 0; a < DIM; ++a) s += J[d][a] * xi[q * 3 + a];
+        x[d] = s;
+      }
+      double ex[4];
+      exact_value(co, DIM, x, ex);
+      const double wq = w[q] * adet;
+      const double e0 = val - ex[0];
+      const double e1 = grad[0] - ex[1], e2 = grad[1] - ex[2], e3 = DIM == 3 ? grad[2] - ex[3] : 0.0;
+      loc[0] += wq * e0 * e0;
+      loc[1] += wq * (e1 * e1 + e2 * e2 + e3 * e3);
+      const double e4 = bv[0] * e1 + bv[1] * e2 + bv[2] * e3;
+      loc[2] += wq * (co.eps * (e1 * e1 + e2 * e2 + e3 * e3) + co.c * e0 * e0 + delta * e4 * e4);
+      loc[3] = fmax(loc[3], fabs(e0));
+    }
+  }
+  for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = loc[k];
+  __syncthreads();
+  for (int s = 64; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+      red[3][threadIdx.x] = fmax(red[3][threadIdx.x], red[3][threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) partial[size_t(blockIdx.x) * 4 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(256) k_cd_errors_finish(int nparts, const double* __restrict__ partial,
+                                                          double* __restrict__ out) {
+  __shared__ double red[4][256];
+  double loc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < nparts; i += 256) {
+    for (int k = 0; k < 3; ++k) loc[k] += partial[size_t(i) * 4 + k];
+    loc[3] = fmax(loc[3], partial[size_t(i) * 4 + 3]);
+  }
+  for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = loc[k];
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+      red[3][threadIdx.x] = fmax(red[3][threadIdx.x], red[3][threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) out[threadIdx.x] = sqrt(red[threadIdx.x][0]);
+  if (threadIdx.x == 3) out[3] = red[3][0];
+}
+
+int error_blocks(int n_cells) { return (n_cells + 127) / 128; }
+
+void launch_cd_errors(pm_ctx* c, int dim, int k, int qn, int n_cells, const double* verts, const int* dofmap,
+                      const double* u, const DevRefTables& rt, const pm_cd_coeffs& cf, double* partial,
+                      double* out) {
+  const CdCoef co = make_coef(cf);
+  const int grid = error_blocks(n_cells);
+  if (dim == 2 && k == 1 && qn == 2) k_cd_errors<2, 4, 4><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (dim == 2 && k == 1 && qn == 3) k_cd_errors<2, 4, 9><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (dim == 2 && k == 2 && qn == 3) k_cd_errors<2, 9, 9><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (dim == 2 && k == 2 && qn == 4) k_cd_errors<2, 9, 16><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (dim == 3 && k == 1 && qn == 3) k_cd_errors<3, 8, 27><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (dim == 3 && k == 1 && qn == 2) k_cd_errors<3, 8, 8><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (dim == 3 && k == 2 && qn == 4) k_cd_errors<3, 27, 64><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (dim == 3 && k == 2 && qn == 3) k_cd_errors<3, 27, 27><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else throw Error(PM_E_UNSUPPORTED, "error functional: element / quadrature combination not compiled");
+  PM_CHECK_LAUNCH();
+  k_cd_errors_finish<<<1, 256, 0, c->stream>>>(grid, partial, out);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 2;
+}
+
 void launch_dirichlet_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs) {
   const int nb = int(L.bnd_xyz.n / 3);
   if (cf.manufactured != 2 || nb == 0) return;
@@ -520,6 +785,10 @@ void DevAssemblyLevel::upload(pm_ctx* c, const DiscLevel& L, int dim, int nvc) {
   rgat_ptr.upload(L.rgat_ptr, c->stream);
   rgat_idx.upload(L.rgat_idx, c->stream);
   diag_pos.upload(L.diag_pos, c->stream);
+  nm_dof.upload(L.nm_dof, c->stream);
+  nm_ptr.upload(L.nm_ptr, c->stream);
+  nm_cell.upload(L.nm_cell, c->stream);
+  nm_code.upload(L.nm_code, c->stream);
   (void)dim;
   (void)nvc;
 }
@@ -578,6 +847,7 @@ void assemble_cd_level(pm_ctx* c, const DevAssemblyLevel& L, int dim, int elem, 
   PM_CHECK_LAUNCH();
   c->kernel_launches += nd ? 3 : 2;
   launch_dirichlet_values(c, L, cf, rhs);
+  launch_neumann_values(c, L, cf, rhs);
   A.values_changed(c);
 }
 
@@ -710,6 +980,7 @@ extern "C" int pm_assemble_cd_noalloc(pm_problem* p, int level, const pm_cd_coef
     }
     c->kernel_launches += nd ? 3 : 2;
     pm::launch_dirichlet_values(c, L, coeffs ? *coeffs : p->coeffs, rhs_dev);
+    pm::launch_neumann_values(c, L, coeffs ? *coeffs : p->coeffs, rhs_dev);
     return PM_OK;
   } catch (const pm::Error& e) {
     c->last_error = e.what();

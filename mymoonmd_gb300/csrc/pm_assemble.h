@@ -33,6 +33,7 @@ struct DevAssemblyLevel {
   DBuf<double> verts;
   DBuf<double> bnd_xyz;  // coordinates of the non-active DOFs (3 per DOF)
   DBuf<int> gat_ptr, gat_idx, rgat_ptr, rgat_idx, diag_pos;
+  DBuf<int> nm_dof, nm_ptr, nm_cell, nm_code;  // Neumann boundary integral plan
   void upload(pm_ctx* c, const DiscLevel& L, int dim, int nvc);
   void scratch_sizes(size_t& k_elems, size_t& f_elems) const;
 };
@@ -44,6 +45,20 @@ double poly_value_host(const double* p, const double* x);
 // Dirichlet values of the quadratic exact solution (manufactured = 2) into the
 // non-active entries of rhs; nothing for the other coefficient kinds
 void launch_dirichlet_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs);
+
+// Neumann boundary integrals of the exact solution's flux eps grad u . n added
+// to the active entries of rhs on the Neumann edges; nothing without Neumann
+// sides or for a constant right-hand side (homogeneous Neumann data)
+void launch_neumann_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coeffs& cf, double* rhs);
+
+// L2, H1-semi, SD and L_inf errors of the FE function u (dofmap: n_cells x
+// nloc) against the exact solution of cf, over the tensor Gauss rule with qn
+// points per direction; partial holds error_blocks(n_cells) * 4 doubles, out
+// receives the four errors (device pointers)
+int error_blocks(int n_cells);
+void launch_cd_errors(pm_ctx* c, int dim, int k, int qn, int n_cells, const double* verts, const int* dofmap,
+                      const double* u, const DevRefTables& rt, const pm_cd_coeffs& cf, double* partial,
+                      double* out);
 
 // element matrices and element right-hand sides of one level into K and F, by
 // the kernel the context's assembly_quadrature_loop option selects

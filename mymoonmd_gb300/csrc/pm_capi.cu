@@ -614,6 +614,22 @@ int pm_disc_create(int geometry, int root_n, int n_refine, int n_levels, int kin
   PM_CATCH(nullptr)
 }
 
+int pm_disc_create_bc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
+                      int neumann_sides, pm_disc** out) {
+  if (!out) return fail(nullptr, PM_E_INVALID, "null argument");
+  PM_TRY
+  auto* d = new pm_disc();
+  try {
+    d->d = build_disc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides);
+  } catch (...) {
+    delete d;
+    throw;
+  }
+  *out = d;
+  return PM_OK;
+  PM_CATCH(nullptr)
+}
+
 void pm_disc_destroy(pm_disc* d) { delete d; }
 
 static const DiscLevel* disc_level(const pm_disc* d, int level) {
@@ -987,6 +1003,34 @@ int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* cf, const double* con
   rc = pm_problem_solve(p);
   if (rc != PM_OK) return rc;
   p->sol.download(sol_host, c->stream);
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  return PM_OK;
+  PM_CATCH(p->ctx)
+}
+
+int pm_problem_errors(pm_problem* p, double* errors) {
+  if (!p || !errors) return PM_E_INVALID;
+  PM_TRY
+  if (p->kind != KIND_CD) throw Error(PM_E_UNSUPPORTED, "pm_problem_errors: convection-diffusion problems only");
+  pm_ctx* c = p->ctx;
+  const Disc& D = *p->disc->d;
+  const DiscLevel& top = D.levels.back();
+  // TFEFunction{2,3}D::GetErrors evaluate on the rule TFEDatabase{2,3}D::GetOrig
+  // picks, the assembly's (degree N_terms x k, FEDatabase2D.C:1718-1790,
+  // FEDatabase3D.C:1129-1163)
+  const int qn = p->qn;
+  if (p->err_qn != qn) {
+    RefTables t;
+    build_qk_tables(D.dim(), D.elem, qn, t);
+    p->err_ref.upload(c, t);
+    p->err_dofmap.upload(top.space.dofmap, c->stream);
+    p->err_out.alloc(4);
+    p->err_qn = qn;
+  }
+  if (size_t(error_blocks(top.n_cells)) * 4 > p->F.n) throw Error(PM_E_INVALID, "error partials exceed the scratch");
+  launch_cd_errors(c, D.dim(), D.elem, qn, top.n_cells, p->alev.back().verts.p, p->err_dofmap.p, p->sol.p,
+                   p->err_ref, p->coeffs, p->F.p, p->err_out.p);
+  p->err_out.download(errors, c->stream);
   PM_CUDA(cudaStreamSynchronize(c->stream));
   return PM_OK;
   PM_CATCH(p->ctx)

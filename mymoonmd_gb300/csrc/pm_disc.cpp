@@ -256,7 +256,43 @@ static void build_stokes_transfer(const Hierarchy& h, DiscLevel& Lc, const DiscL
   }
 }
 
-std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem) {
+// The Neumann plan of one level: for every active DOF on a Neumann edge the
+// edges that integrate into its right-hand side entry (only the local DOFs on
+// the edge: the others vanish there).
+static void build_neumann_plan(const Hierarchy& h, DiscLevel& L, int neumann_sides) {
+  L.nm_dof.clear();
+  L.nm_ptr.assign(1, 0);
+  L.nm_cell.clear();
+  L.nm_code.clear();
+  const std::vector<NeumannEdge> edges = neumann_edges(h, L.level_in_hierarchy, neumann_sides);
+  if (edges.empty()) return;
+  const int nloc = L.space.nloc, k = nloc == 9 ? 2 : 1;
+  // local DOF (a, b) of a tensor element lies on edge m of [-1,1]^2 when
+  // b = 0 (m 0), a = k (m 1), b = k (m 2), a = 0 (m 3)
+  auto on_edge = [k](int loc, int m) {
+    const int a = loc % (k + 1), b = loc / (k + 1);
+    return m == 0 ? b == 0 : m == 1 ? a == k : m == 2 ? b == k : a == 0;
+  };
+  std::vector<std::vector<std::pair<int, int>>> per(L.space.n_dofs);
+  for (const NeumannEdge& e : edges)
+    for (int loc = 0; loc < nloc; ++loc) {
+      if (!on_edge(loc, e.edge)) continue;
+      const int g = L.space.dofmap[size_t(e.cell) * nloc + loc];
+      if (g < L.space.n_active) per[g].push_back({e.cell, e.edge | (e.side << 2) | (loc << 4)});
+    }
+  for (int g = 0; g < L.space.n_dofs; ++g) {
+    if (per[g].empty()) continue;
+    L.nm_dof.push_back(g);
+    for (auto& pc : per[g]) {
+      L.nm_cell.push_back(pc.first);
+      L.nm_code.push_back(pc.second);
+    }
+    L.nm_ptr.push_back(int(L.nm_cell.size()));
+  }
+}
+
+std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
+                                 int neumann_sides) {
   if (n_levels < 1 || n_levels > n_refine + 1)
     throw std::invalid_argument("multigrid levels must be between 1 and refinements + 1");
   auto D = std::make_unique<Disc>();
@@ -266,6 +302,9 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
   D->n_refine = n_refine;
   D->n_levels = n_levels;
   D->elem = elem;
+  if (neumann_sides < 0 || neumann_sides > 15 || (neumann_sides && (kind != KIND_CD || geometry != GEO_SQUARE_QUAD)))
+    throw std::invalid_argument("Neumann sides (a mask of 4 bits) apply to convection-diffusion on the unit square");
+  D->neumann_sides = neumann_sides;
   if (kind == KIND_CD) {
     if (geometry == GEO_CUBE_TETRA) throw std::invalid_argument("convection-diffusion uses quadrilaterals or hexahedra");
     if (elem != EL_Q1 && elem != EL_Q2) throw std::invalid_argument("convection-diffusion elements are Q1 or Q2");
@@ -293,13 +332,14 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
     DiscLevel& L = D->levels[l];
     L.level_in_hierarchy = first + l;
     L.n_cells = D->h.levels[first + l].n_cells;
-    L.space = build_space(D->h, first + l, elem, BND_DIRICHLET);
+    L.space = build_space(D->h, first + l, elem, BND_DIRICHLET, neumann_sides);
     L.sys = build_structure(L.space, L.n_cells);
     L.verts = cell_vertices(D->h, first + l);
     std::vector<char> act(L.space.n_dofs, 0);
     for (int i = 0; i < L.space.n_active; ++i) act[i] = 1;
     build_gather(L, L.space.nloc, L.space.dofmap, act);
     fill_bnd_xyz(D->h, L);
+    build_neumann_plan(D->h, L, neumann_sides);
     L.n_blocks = 1;
     L.block_len[0] = L.space.n_dofs;
     L.block_active[0] = L.space.n_active;

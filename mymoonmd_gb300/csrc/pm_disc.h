@@ -30,6 +30,10 @@ struct DiscLevel {
   // n_active .. n_dofs-1 of `space` (for Stokes the velocity component space),
   // the points of the nodal functionals the Dirichlet values are taken at
   std::vector<double> bnd_xyz;
+  // Neumann boundary integral plan (2D): the active DOFs that lie on a
+  // Neumann edge (ascending) and, per DOF, its (cell, code) pairs in cell
+  // order; code = edge | side << 2 | local DOF << 4
+  std::vector<int> nm_dof, nm_ptr, nm_cell, nm_code;
   // prolongation to the next finer level (rows of the finer level)
   pmsetup::Csr P;
   // Stokes block layout of the combined vector [u1 | u2 | u3 | p]
@@ -53,13 +57,15 @@ struct DiscLevel {
 struct Disc {
   int kind = KIND_CD;
   int geometry = 0, root_n = 1, n_refine = 0, n_levels = 1, elem = 1;
+  int neumann_sides = 0;  // 2D convection-diffusion: sides with Neumann conditions
   pmsetup::Hierarchy h;
   std::vector<DiscLevel> levels;  // 0 = coarsest kept level
   int dim() const { return h.dim; }
   int nvc() const { return h.nvc; }
 };
 
-std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem);
+std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
+                                 int neumann_sides = 0);
 
 }  // namespace pm
 

@@ -27,5 +27,11 @@ struct pm_problem {
   pm::DBuf<double> K, F, rhs, sol, rhs_coarse;
   pm_solver* solver = nullptr;
   bool solver_ready = false;
+  // error functional: reference tables of its quadrature rule, the finest
+  // level's dofmap and the four results (set up by the first pm_problem_errors)
+  int err_qn = 0;
+  pm::DevRefTables err_ref;
+  pm::DBuf<int> err_dofmap;
+  pm::DBuf<double> err_out;
   ~pm_problem();
 };

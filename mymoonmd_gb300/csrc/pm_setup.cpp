@@ -212,20 +212,35 @@ static void cell_nodes(int geometry, int elem, const int64_t* v, int64_t* out) {
   }
 }
 
-Space build_space(const Hierarchy& h, int level, int elem, int boundary) {
+int square_sides(int64_t S, const int64_t* x) {
+  int m = 0;
+  if (x[1] == 0) m |= SIDE_Y0;
+  if (x[0] == S) m |= SIDE_X1;
+  if (x[1] == S) m |= SIDE_Y1;
+  if (x[0] == 0) m |= SIDE_X0;
+  return m;
+}
+
+Space build_space(const Hierarchy& h, int level, int elem, int boundary, int neumann_sides) {
   const Level& L = h.levels.at(level);
   const int dim = h.dim, nvc = h.nvc;
+  if (neumann_sides && (dim != 2 || boundary != BND_DIRICHLET))
+    throw std::invalid_argument("Neumann sides are supported on the unit square with Dirichlet elsewhere");
   Space s;
   s.elem = elem;
   s.boundary = boundary;
+  s.neumann_sides = neumann_sides;
   s.nloc = space_nloc(h.geometry, elem);
   const int64_t S = h.scale, W = S + 1;
   size_t lattice = size_t(W) * W * (dim == 3 ? W : 1);
-  // provisional number per lattice point: -1 unseen, >=0 inner, <=-2 boundary
+  // provisional number per lattice point: -1 unseen, >= 0 class-local number
+  // (class in cls)
   std::vector<int> mark(lattice, -1);
+  std::vector<char> cls(lattice, 0);
   s.dofmap.resize(size_t(L.n_cells) * s.nloc);
-  int n_inner = 0, n_bnd = 0;
-  std::vector<int64_t> inner_nodes, bnd_nodes;
+  std::vector<int> dof_key(size_t(L.n_cells) * s.nloc);
+  int count[3] = {0, 0, 0};  // inner, Neumann, Dirichlet (or all-boundary)
+  std::vector<int64_t> cls_nodes[3];
   std::vector<int64_t> nodes(size_t(s.nloc) * dim);
   for (int c = 0; c < L.n_cells; ++c) {
     cell_nodes(h.geometry, elem, &L.vtx[size_t(c) * nvc * dim], nodes.data());
@@ -236,24 +251,45 @@ Space build_space(const Hierarchy& h, int level, int elem, int boundary) {
       if (mk == -1) {
         bool on_bnd = false;
         for (int d = 0; d < dim; ++d) on_bnd |= (x[d] == 0 || x[d] == S);
+        int k = 0;
         if (on_bnd) {
-          mk = -2 - n_bnd++;
-          bnd_nodes.insert(bnd_nodes.end(), x, x + dim);
-        } else {
-          mk = n_inner++;
-          inner_nodes.insert(inner_nodes.end(), x, x + dim);
+          k = 2;
+          if (neumann_sides) {
+            const int sides = square_sides(S, x);
+            if ((sides & neumann_sides) == sides) k = 1;
+          }
         }
+        cls[key] = char(k);
+        mk = count[k]++;
+        cls_nodes[k].insert(cls_nodes[k].end(), x, x + dim);
       }
       s.dofmap[size_t(c) * s.nloc + m] = mk;
+      dof_key[size_t(c) * s.nloc + m] = cls[key];
     }
   }
-  for (auto& d : s.dofmap)
-    if (d <= -2) d = n_inner + (-2 - d);
-  s.n_dofs = n_inner + n_bnd;
-  s.n_active = boundary == BND_DIRICHLET ? n_inner : s.n_dofs;
-  s.node = inner_nodes;
-  s.node.insert(s.node.end(), bnd_nodes.begin(), bnd_nodes.end());
+  const int base[3] = {0, count[0], count[0] + count[1]};
+  for (size_t i = 0; i < s.dofmap.size(); ++i) s.dofmap[i] += base[dof_key[i]];
+  s.n_dofs = count[0] + count[1] + count[2];
+  s.n_neumann = count[1];
+  s.n_active = boundary == BND_DIRICHLET ? count[0] + count[1] : s.n_dofs;
+  s.node = cls_nodes[0];
+  for (int k = 1; k < 3; ++k) s.node.insert(s.node.end(), cls_nodes[k].begin(), cls_nodes[k].end());
   return s;
+}
+
+std::vector<NeumannEdge> neumann_edges(const Hierarchy& h, int level, int neumann_sides) {
+  std::vector<NeumannEdge> out;
+  if (!neumann_sides || h.dim != 2) return out;
+  const Level& L = h.levels.at(level);
+  for (int c = 0; c < L.n_cells; ++c) {
+    const int64_t* v = &L.vtx[size_t(c) * 8];
+    for (int m = 0; m < 4; ++m) {
+      const int common = square_sides(h.scale, v + 2 * m) & square_sides(h.scale, v + 2 * ((m + 1) % 4));
+      for (int sd = 0; sd < 4; ++sd)
+        if ((common >> sd) & (neumann_sides >> sd) & 1) out.push_back({c, m, sd});
+    }
+  }
+  return out;
 }
 
 static void dof_cells(const Space& s, int n_cells, std::vector<int>& ptr, std::vector<int>& cells) {

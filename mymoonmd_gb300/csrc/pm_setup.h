@@ -40,6 +40,8 @@ struct Level {
 struct Space {
   int elem = 0, nloc = 0, n_dofs = 0, n_active = 0;
   int boundary = BND_DIRICHLET;
+  int neumann_sides = 0;  // 2D sides with Neumann conditions (bit s: side s)
+  int n_neumann = 0;      // Neumann DOFs n_active - n_neumann .. n_active-1
   std::vector<int> dofmap;   // n_cells * nloc  (GlobalNumbers, BeginIndex = c*nloc)
   std::vector<int64_t> node; // n_dofs * dim lattice coordinates of each DOF
 };
@@ -64,10 +66,32 @@ int element_dim(int elem);
 // regularly n_refine times, keeping every level.
 Hierarchy build_hierarchy(int geometry, int root_n, int n_refine);
 
+// Sides of the unit square as the boundary components of UnitSquare number
+// them (Default_UnitSquare): 0 y=0, 1 x=1, 2 y=1, 3 x=0.
+enum SquareSide { SIDE_Y0 = 1, SIDE_X1 = 2, SIDE_Y1 = 4, SIDE_X0 = 8 };
+
+// Bit mask of the square's sides that lattice point x lies on (0 inside).
+int square_sides(int64_t scale, const int64_t* x);
+
 // Numbers the DOFs of `elem` on one level: inner DOFs in order of first touch
 // (cells in collection order, local DOFs in local order), then boundary DOFs of
 // the given kind in the same order. Dirichlet DOFs are non-active.
-Space build_space(const Hierarchy& h, int level, int elem, int boundary);
+//
+// With boundary == BND_DIRICHLET and a non-zero neumann_sides (2D only) the
+// sides in the mask carry Neumann conditions: DOFs whose every side is a
+// Neumann side are numbered after the inner DOFs and stay active, the rest of
+// the boundary (the corners between a Neumann and a Dirichlet side among
+// them) after those, non-active: inner, Neumann, Dirichlet, each in order of
+// first touch (TFESpace2D::ConstructSpace, src/FE/FESpace2D.C).
+Space build_space(const Hierarchy& h, int level, int elem, int boundary, int neumann_sides = 0);
+
+// Boundary edges of one 2D level on the Neumann sides: for each, the cell,
+// the local edge m (vertices m and m+1 mod 4) and the side, in cell order then
+// edge order.
+struct NeumannEdge {
+  int cell, edge, side;
+};
+std::vector<NeumannEdge> neumann_edges(const Hierarchy& h, int level, int neumann_sides);
 
 // Square CSR pattern of one space: active rows couple to every DOF of every
 // cell containing them, rows sorted ascending; non-active rows hold only the

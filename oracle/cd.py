@@ -141,19 +141,55 @@ def transfer(dim: int, k: int, coarse_level, fine_level, vec: np.ndarray, prolon
     return out
 
 
+def _gauss(n: int):
+    """Gauss-Legendre points and weights on [-1, 1]"""
+    return np.polynomial.legendre.leggauss(n)
+
+
+def _lag1d(k: int, x: np.ndarray):
+    """Lagrange basis of degree k on the nodes -1, (0,) 1 and its derivative"""
+    if k == 1:
+        return [0.5 * (1 - x), 0.5 * (1 + x)], [np.full_like(x, -0.5), np.full_like(x, 0.5)]
+    return ([0.5 * x * (x - 1), 1 - x * x, 0.5 * x * (x + 1)], [x - 0.5, -2 * x, x + 0.5])
+
+
+def _qk_values(k: int, d: int, xi: np.ndarray):
+    """values (points, nb) and reference derivatives (d, points, nb) of the
+    lexicographic Qk basis at reference points xi (points, d)"""
+    L = [_lag1d(k, xi[:, a]) for a in range(d)]
+    vals, ders = [], [[] for _ in range(d)]
+    idx = [(a, b, 0) for b in range(k + 1) for a in range(k + 1)] if d == 2 else \
+        [(a, b, c) for c in range(k + 1) for b in range(k + 1) for a in range(k + 1)]
+    for t in idx:
+        v = np.ones(xi.shape[0])
+        for a in range(d):
+            v = v * L[a][0][t[a]]
+        vals.append(v)
+        for da in range(d):
+            g = np.ones(xi.shape[0])
+            for a in range(d):
+                g = g * (L[a][1][t[a]] if a == da else L[a][0][t[a]])
+            ders[da].append(g)
+    return np.stack(vals, axis=1), np.stack([np.stack(dd, axis=1) for dd in ders])
+
+
 class OracleCD:
     """ConvectionDiffusion<d> restated on the CPU over a multigrid hierarchy."""
 
     def __init__(self, geometry: int, root_n: int, n_refine: int, n_levels: int, elem: int,
                  eps: float, b=(0.0, 0.0, 0.0), c: float = 0.0, quad_points: int = 3,
-                 manufactured: bool = True, f_const: float = 0.0, poly=None, poly_src=None):
+                 manufactured: bool = True, f_const: float = 0.0, poly=None, poly_src=None,
+                 neumann_sides: int = 0):
         """poly: ten coefficients (1, x, y, z, x^2, y^2, z^2, xy, xz, yz) of a
         quadratic exact solution; f and the Dirichlet values then come from it;
-        poly_src (same monomials) is added to f"""
+        poly_src (same monomials) is added to f. neumann_sides: bit mask of the
+        unit square's sides (0 y=0, 1 x=1, 2 y=1, 3 x=0) with Neumann data
+        eps grad u . n of the exact solution"""
         self.geometry = geometry
         self.dim = 2 if geometry == refsetup.GEO_SQUARE_QUAD else 3
         self.elem = elem
-        self.levels = refsetup.cd_levels(geometry, root_n, n_refine, n_levels, elem)
+        self.neumann_sides = neumann_sides
+        self.levels = refsetup.cd_levels(geometry, root_n, n_refine, n_levels, elem, neumann_sides)
         self.eps, self.c = eps, c
         self.b = np.array(list(b) + [0.0] * (3 - len(b)), dtype=np.float64)
         self.qn = quad_points
@@ -198,8 +234,125 @@ class OracleCD:
                 # nodes of the non-active DOFs (Assemble3D.C:640-665)
                 for i in range(lv.n_active, lv.n_dofs):
                     rhs[i] = self.exact(lv.node_coords[i])
+            if self.neumann_sides and (self.manufactured or self.poly is not None):
+                self._neumann_rhs(lv, rhs)
             self.vals.append(vals)
             self.rhs.append(rhs)
+
+    def exact_grad(self, x: np.ndarray) -> np.ndarray:
+        """(u, u_x, u_y[, u_z]) of the exact solution at points x (n, dim);
+        zero for a constant right-hand side"""
+        n, d = x.shape
+        out = np.zeros((n, 1 + d))
+        if self.poly is not None:
+            X = np.zeros((n, 3))
+            X[:, :d] = x
+            p = self.poly
+            out[:, 0] = (p[0] + p[1] * X[:, 0] + p[2] * X[:, 1] + p[3] * X[:, 2] + p[4] * X[:, 0] ** 2 +
+                         p[5] * X[:, 1] ** 2 + p[6] * X[:, 2] ** 2 + p[7] * X[:, 0] * X[:, 1] +
+                         p[8] * X[:, 0] * X[:, 2] + p[9] * X[:, 1] * X[:, 2])
+            g = [p[1] + 2 * p[4] * X[:, 0] + p[7] * X[:, 1] + p[8] * X[:, 2],
+                 p[2] + 2 * p[5] * X[:, 1] + p[7] * X[:, 0] + p[9] * X[:, 2],
+                 p[3] + 2 * p[6] * X[:, 2] + p[8] * X[:, 0] + p[9] * X[:, 1]]
+            for a in range(d):
+                out[:, 1 + a] = g[a]
+        elif self.manufactured:
+            s, c = np.sin(np.pi * x), np.cos(np.pi * x)
+            out[:, 0] = np.prod(s, axis=1)
+            for a in range(d):
+                t = np.pi * c[:, a]
+                for b in range(d):
+                    if b != a:
+                        t = t * s[:, b]
+                out[:, 1 + a] = t
+        return out
+
+    def _neumann_rhs(self, lv, rhs: np.ndarray) -> None:
+        """boundary integral of Assemble2D (src/AssembleRoutines/Assemble2D.C:716-757):
+        for each edge m (vertex m to m+1) of a cell on a Neumann side and each
+        line Gauss point zeta_l (degree 2k: k+1 points),
+        rhs_i += g(x_l) hE w_l phi_i(xi_l) for active DOFs i, hE = |edge| / 2,
+        xi_l on edge m of [-1,1]^2 (src/FE/BaseFunct2D.C:87-118),
+        g = eps grad u . n (SineLaplace's BoundValue on x = 1)"""
+        k = self.elem
+        z, w = np.polynomial.legendre.leggauss(k + 1)
+        ref = np.array([[-1.0, -1.0], [1.0, -1.0], [1.0, 1.0], [-1.0, 1.0]])
+        normal = {0: (0.0, -1.0), 1: (1.0, 0.0), 2: (0.0, 1.0), 3: (-1.0, 0.0)}
+        S = lv.scale
+        for c in range(lv.n_cells):
+            vl = lv.verts_lattice[c]
+            for m in range(4):
+                m1 = (m + 1) % 4
+                ss = refsetup.square_sides(vl[[m, m1]], S)
+                common = int(ss[0] & ss[1])
+                for side in range(4):
+                    if not (common >> side) & (self.neumann_sides >> side) & 1:
+                        continue
+                    a, b = lv.verts[c, m], lv.verts[c, m1]
+                    hE = np.sqrt(((b - a) ** 2).sum()) / 2
+                    f = 0.5 * (z + 1.0)
+                    xi = ref[m][None, :] + f[:, None] * (ref[m1] - ref[m])[None, :]
+                    x = a[None, :] + f[:, None] * (b - a)[None, :]
+                    g = self.eps * (self.exact_grad(x)[:, 1:] @ np.array(normal[side]))
+                    phi = _qk_values(k, 2, xi)[0]          # (points, nloc)
+                    contrib = (g * hE * w)[:, None] * phi
+                    for loc in range(lv.nloc):
+                        dof = lv.dofmap[c, loc]
+                        if dof < lv.n_active:
+                            rhs[dof] += contrib[:, loc].sum()
+
+    def errors(self, sol: np.ndarray) -> np.ndarray:
+        """(L2, H1-semi, SD, L_inf) of ConvectionDiffusion<d>::output
+        (src/System/ConvectionDiffusion.C:213-283): TFEFunction{2,3}D::GetErrors
+        (src/FE/FEFunction2D.C:318-575, FEFunction3D.C:80-245) on the rule
+        that GetOrig picks (src/FE/FEDatabase2D.C:1718-1790: degree N_terms x
+        k, the assembly's rule) with
+        conv_diff_l2_h1_linf_error (src/AssembleRoutines/ConvDiff.C:2134-2185)
+        and the SUPG delta of Compute_SDFEM_delta (ConvDiff.C:273-360) at
+        SDFEM_TYPE 2, DELTA0 1, polynomial degree 1, hK = cell diameter"""
+        lv = self.finest
+        d, k = self.dim, self.elem
+        qn = self.qn
+        x1, w1 = _gauss(qn)
+        if d == 2:
+            xi = np.array([[x1[a], x1[b]] for b in range(qn) for a in range(qn)])
+            wq = np.array([w1[a] * w1[b] for b in range(qn) for a in range(qn)])
+        else:
+            xi = np.array([[x1[a], x1[b], x1[c]] for c in range(qn) for b in range(qn) for a in range(qn)])
+            wq = np.array([w1[a] * w1[b] * w1[c] for c in range(qn) for b in range(qn) for a in range(qn)])
+        phi, dphi = _qk_values(k, d, xi)                  # (nq, nb), (d, nq, nb)
+        v = lv.verts                                       # (n_cells, nv, d)
+        if d == 2:
+            x0 = (v[:, 1] + v[:, 3]) / 2
+            J = np.stack([(v[:, 1] - v[:, 0]) / 2, (v[:, 3] - v[:, 0]) / 2], axis=2)
+        else:
+            x0 = (v[:, 1] + v[:, 3] + v[:, 4] - v[:, 0]) / 2
+            J = np.stack([(v[:, 1] - v[:, 0]) / 2, (v[:, 3] - v[:, 0]) / 2, (v[:, 4] - v[:, 0]) / 2], axis=2)
+        det = np.linalg.det(J)
+        G = np.linalg.inv(J).transpose(0, 2, 1)          # J^{-T}
+        uc = sol[lv.dofmap]                                # (n_cells, nb)
+        val = uc @ phi.T                                   # (n_cells, nq)
+        dref = np.stack([uc @ dphi[a].T for a in range(d)], axis=2)   # (n_cells, nq, d)
+        grad = np.einsum("cda,cqa->cqd", G, dref)
+        x = x0[:, None, :] + np.einsum("cda,qa->cqd", J, xi)
+        ex = self.exact_grad(x.reshape(-1, d)).reshape(lv.n_cells, -1, 1 + d)
+        w = wq[None, :] * np.abs(det)[:, None]
+        e0 = val - ex[:, :, 0]
+        eg = grad - ex[:, :, 1:]
+        diam = np.sqrt(((v[:, :, None, :] - v[:, None, :, :]) ** 2).sum(axis=3)).max(axis=(1, 2))
+        b = self.b[:d]
+        nb_ = np.sqrt((b ** 2).sum())
+        eps = self.eps if abs(self.eps) >= 1e-20 else 1e-20
+        if nb_ > 0:
+            alpha = nb_ * diam / (2 * eps)
+            delta = diam * (1 / np.tanh(alpha) - 1 / alpha) / (2 * nb_)
+        else:
+            delta = np.zeros(lv.n_cells)
+        e4 = eg @ b
+        l2 = (w * e0 ** 2).sum()
+        h1 = (w * (eg ** 2).sum(axis=2)).sum()
+        sd = (w * (self.eps * (eg ** 2).sum(axis=2) + self.c * e0 ** 2 + delta[:, None] * e4 ** 2)).sum()
+        return np.array([np.sqrt(l2), np.sqrt(h1), np.sqrt(sd), np.abs(e0).max()])
 
     def active(self, l: int = -1) -> np.ndarray:
         lv = self.levels[l]

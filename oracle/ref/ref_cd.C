@@ -16,6 +16,10 @@
 //   QUAD_LINEAR 1 sets INTERNAL_PROBLEM_LINEAR (quadrature degree 2 x the
 //   element degree, e.g. Gauss3 for Q2), 0 keeps the default (3 x);
 //   SOLVER fgmres_mg | direct | none (assemble only).
+//   optional EXAMPLE: the reference's own example of that number
+//   (Example_CD2D/3D from the database, e.g. 0 = SineLaplace in 2D, whose
+//   boundary part 1 is a Neumann boundary) instead of the sine problem above;
+//   the errors of ConvectionDiffusion::output are dumped as well.
 #include <BaseCell.h>
 #include <ConvectionDiffusion.h>
 #include <Vertex.h>
@@ -130,6 +134,7 @@ int main(int argc, char** argv) {
   const std::string solver = argv[10];
   const int restart = std::atoi(argv[11]);
   const double reduction = std::atof(argv[12]);
+  const int builtin_example = argc > 13 ? std::atoi(argv[13]) : -1;
 
   Output::setVerbosity(1);
   TDatabase database;
@@ -142,6 +147,15 @@ int main(int argc, char** argv) {
   db.merge(Solver<>::default_solver_database());
   db.merge(Multigrid::default_multigrid_database());
   db.merge(ParameterDatabase::default_output_database());
+#ifdef __2D__
+  db.merge(Example2D::default_example_database());
+#else
+  db.merge(Example3D::default_example_database());
+#endif
+  if (builtin_example >= 0) {
+    db["example"] = builtin_example;
+    db["output_compute_errors"] = true;
+  }
   db["problem_type"] = 1;
 #ifdef __2D__
   db.add("boundary_file", "Default_UnitSquare", "");
@@ -175,7 +189,7 @@ int main(int argc, char** argv) {
 
   TDomain domain(db);
   domain.refine_and_get_hierarchy_of_collections(db);
-  RefCD cd(domain, db, make_example());
+  RefCD cd(domain, db, builtin_example >= 0 ? Example(db) : make_example());
   cd.assemble();
 
   std::FILE* meta = std::fopen((out + "/meta.txt").c_str(), "w");
@@ -236,6 +250,11 @@ int main(int argc, char** argv) {
                    info.get_previous_residual());
     }
     std::fprintf(meta, "solve_seconds %.6f\n", t);
+    if (builtin_example >= 0) {
+      cd.output();
+      std::fprintf(meta, "errors %.17g %.17g %.17g %.17g\n", cd.get_L2_error(), cd.get_H1_semi_error(),
+                   cd.get_SD_error(), cd.get_L_inf_error());
+    }
   }
   std::fclose(meta);
   return 0;

@@ -16,7 +16,11 @@ numbering and CSR patterns of ParMooN's solve path, restated with numpy.
                  class when it meets its representative, inner classes first
                  and Dirichlet classes after them. On a conforming mesh a class
                  is a geometric node, so the result is first-touch order over
-                 (cell, local DOF), inner nodes, then boundary nodes.
+                 (cell, local DOF), inner nodes, then boundary nodes. With
+                 Neumann sides (2D, SineLaplace's BoundCondition) the boundary
+                 splits into Neumann nodes (all their sides Neumann, active)
+                 numbered before the Dirichlet nodes (TFESpace2D::ConstructSpace,
+                 src/FE/FESpace2D.C).
   structure    : TStructure(space) (src/Matrix/Structure.C:829-1283), Sort (:2681)
 """
 from __future__ import annotations
@@ -113,8 +117,16 @@ def local_nodes(geometry: int, elem: int, v: np.ndarray) -> np.ndarray:
     return np.stack([(v[:, a] + v[:, b]) // 2 for a, b in pairs], axis=1)
 
 
-def number_dofs(nodes: np.ndarray, scale: int, dirichlet: bool = True):
-    """first-touch numbering, inner nodes first; returns (dofmap, n_dofs, n_active, coords)"""
+def square_sides(c: np.ndarray, scale: int) -> np.ndarray:
+    """bit mask of the unit square's sides (0 y=0, 1 x=1, 2 y=1, 3 x=0, the
+    boundary components of UnitSquare) that each lattice point lies on"""
+    return ((c[:, 1] == 0) * 1 + (c[:, 0] == scale) * 2 + (c[:, 1] == scale) * 4 +
+            (c[:, 0] == 0) * 8).astype(np.int64)
+
+
+def number_dofs(nodes: np.ndarray, scale: int, dirichlet: bool = True, neumann_sides: int = 0):
+    """first-touch numbering, inner nodes first, then Neumann nodes (active),
+    then Dirichlet nodes; returns (dofmap, n_dofs, n_active, coords)"""
     n_cells, nloc, dim = nodes.shape
     flat = nodes.reshape(-1, dim)
     w = scale + 1
@@ -123,15 +135,21 @@ def number_dofs(nodes: np.ndarray, scale: int, dirichlet: bool = True):
     order = np.argsort(first, kind="stable")           # unique nodes in first-touch order
     ucoord = flat[first]
     on_bnd = np.any((ucoord == 0) | (ucoord == scale), axis=1)
+    neumann = np.zeros(uniq.size, dtype=bool)
+    if neumann_sides:
+        sides = square_sides(ucoord, scale)
+        neumann = on_bnd & ((sides & neumann_sides) == sides)
     inner = order[~on_bnd[order]]
-    bnd = order[on_bnd[order]]
+    neu = order[neumann[order]]
+    bnd = order[(on_bnd & ~neumann)[order]]
     number = np.empty(uniq.size, dtype=np.int64)
     number[inner] = np.arange(inner.size)
-    number[bnd] = inner.size + np.arange(bnd.size)
+    number[neu] = inner.size + np.arange(neu.size)
+    number[bnd] = inner.size + neu.size + np.arange(bnd.size)
     dofmap = number[inv].reshape(n_cells, nloc).astype(np.int32)
     coords = np.empty((uniq.size, dim), dtype=np.int64)
     coords[number] = ucoord
-    n_active = inner.size if dirichlet else uniq.size
+    n_active = inner.size + neu.size if dirichlet else uniq.size
     return dofmap, uniq.size, n_active, coords
 
 
@@ -156,24 +174,26 @@ def structure(dofmap: np.ndarray, n_dofs: int, n_active: int):
 
 
 class Level:
-    def __init__(self, geometry, elem, verts_lattice, parent, scale):
+    def __init__(self, geometry, elem, verts_lattice, parent, scale, neumann_sides=0):
         self.verts_lattice = verts_lattice
+        self.scale = scale
         self.parent = None if parent is None else parent.astype(np.int32)
         self.n_cells = verts_lattice.shape[0]
         inv = 1.0 / scale if (scale & (scale - 1)) == 0 else None
         self.verts = (verts_lattice * inv if inv is not None else verts_lattice / scale).astype(np.float64)
         nodes = local_nodes(geometry, elem, verts_lattice)
-        self.dofmap, self.n_dofs, self.n_active, self.coords = number_dofs(nodes, scale)
+        self.dofmap, self.n_dofs, self.n_active, self.coords = number_dofs(nodes, scale,
+                                                                           neumann_sides=neumann_sides)
         self.nloc = self.dofmap.shape[1]
         self.row_ptr, self.cols = structure(self.dofmap, self.n_dofs, self.n_active)
         self.node_coords = self.coords / scale
 
 
-def cd_levels(geometry: int, root_n: int, n_refine: int, n_levels: int, elem: int):
+def cd_levels(geometry: int, root_n: int, n_refine: int, n_levels: int, elem: int, neumann_sides: int = 0):
     """the kept multigrid levels (coarsest first) of a convection-diffusion set-up"""
     meshes, parents, scale = hierarchy(geometry, root_n, n_refine)
     first = n_refine + 1 - n_levels
     out = []
     for l in range(first, n_refine + 1):
-        out.append(Level(geometry, elem, meshes[l], parents[l], scale))
+        out.append(Level(geometry, elem, meshes[l], parents[l], scale, neumann_sides))
     return out

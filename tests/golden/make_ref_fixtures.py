@@ -15,6 +15,11 @@ multigrid. The fixture keeps, per level:
 and for the solve: the FGMRES iteration count, the initial and final residual
 of the reference's LoopInfo and the solution (full or sampled).
 
+The sine_* cases run the reference's own SineLaplace example (Example_CD2D
+number 0, include/Examples/CD_2D/SineLaplace.h: u = sin(pi x) sin(pi y),
+eps = 1, Neumann boundary on x = 1) instead of the driver's sine problem, and
+keep the L2, H1-semi, SD and L_inf errors of ConvectionDiffusion::output.
+
     python tests/golden/make_ref_fixtures.py            # all cases
     python tests/golden/make_ref_fixtures.py cd3d_q2_8  # one case
 """
@@ -35,7 +40,8 @@ sys.path.insert(0, str(ROOT / "oracle" / "ref"))
 SAMPLES = 4096
 
 # name: (dim, n_refine, element order, levels, eps, b, quadrature degree 2 x
-#        order (1) or the default 3 x order (0), restart, residual reduction, full arrays)
+#        order (1) or the default 3 x order (0), restart, residual reduction, full arrays
+#        [, the reference's example number])
 CASES = {
     # 3D Q2 32^3 convection-diffusion, 4 levels, FGMRES(30), 1e-8, Gauss 3x3x3
     "cd3d_q2_32": (3, 5, 2, 4, 1e-2, (1.0, 0.5, 0.25), 1, 30, 1e-8, False),
@@ -46,6 +52,12 @@ CASES = {
     "cd3d_q2_4": (3, 2, 2, 2, 0.1, (1.0, 0.5, 0.25), 1, 30, 1e-10, True),
     "cd3d_q1_8": (3, 3, 1, 3, 0.05, (0.3, -1.0, 0.5), 1, 30, 1e-10, True),
     "cd2d_q2_16": (2, 4, 2, 3, 0.02, (1.0, 0.5, 0.0), 1, 20, 1e-10, True),
+    # SineLaplace with its Neumann side: the 4 x 4 mesh of test/cd2d_test.c++
+    # (2 refinements of UnitSquare) and larger meshes
+    "sine_q1_4": (2, 2, 1, 2, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-12, True, 0),
+    "sine_q2_4": (2, 2, 2, 2, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-12, True, 0),
+    "sine_q1_64": (2, 6, 1, 4, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-10, False, 0),
+    "sine_q2_32": (2, 5, 2, 3, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-10, False, 0),
 }
 
 
@@ -63,11 +75,12 @@ def sample_idx(n: int) -> np.ndarray:
 
 def run_case(name: str) -> None:
     import build_ref
-    dim, nref, order, nlev, eps, b, quad_linear, restart, reduction, full = CASES[name]
+    dim, nref, order, nlev, eps, b, quad_linear, restart, reduction, full = CASES[name][:10]
+    example = CASES[name][10] if len(CASES[name]) > 10 else -1
     exe = build_ref.link_program(str(dim), build_ref.HERE / "ref_cd.C", build_ref.OUT / f"ref_cd{dim}d")
     with tempfile.TemporaryDirectory() as tmp:
         cmd = [str(exe), tmp, str(nref), str(order), str(nlev), repr(eps), *map(repr, b), str(quad_linear),
-               "fgmres_mg", str(restart), repr(reduction)]
+               "fgmres_mg", str(restart), repr(reduction)] + ([str(example)] if example >= 0 else [])
         subprocess.run(cmd, check=True, capture_output=True)
         meta = {}
         for line in Path(tmp, "meta.txt").read_text().splitlines():
@@ -79,7 +92,10 @@ def run_case(name: str) -> None:
             "iterations": np.array(int(meta["iterations"])),
             "initial_residual": np.array(float(meta["initial_residual"])),
             "final_residual": np.array(float(meta["final_residual"])),
+            "example": np.array(example, dtype=np.int64),
         }
+        if example >= 0:
+            out["errors"] = np.array([float(v) for v in meta["errors"].split()])
         for rl in range(nlev):
             lvl = nlev - 1 - rl  # 0 = coarsest, as the library counts levels
             info = meta[f"L{rl}"].split()

@@ -32,6 +32,10 @@ class RefCase:
         self.eps, self.b = eps, (b1, b2, b3)
         self.quad_points = _POINTS[(2 if quad_linear else 3) * order]
         self.geometry = 0 if dim == 2 else 1  # unit square (quads) / unit cube (hexahedra)
+        # the reference's own example (0 = SineLaplace, Neumann side x = 1) or -1
+        self.example = int(self.z["example"]) if "example" in self.z.files else -1
+        self.neumann_sides = 2 if self.example == 0 else 0
+        self.errors = self.z["errors"] if "errors" in self.z.files else None
         self.iterations = int(self.z["iterations"])
         self.initial_residual = float(self.z["initial_residual"])
         self.final_residual = float(self.z["final_residual"])

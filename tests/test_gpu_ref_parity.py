@@ -14,7 +14,10 @@ assembled and solved on the GPU through the C ABI:
   FP64 FGMRES)                          error against the reference's solution is
                                         stated and held to 1e-7
 Cases include the 2D Q1 128^2 workload (16,641 DOFs) and the 3D Q2 32^3
-workload (274,625 DOFs, 15.8 M nonzeros, 82 iterations in the reference).
+workload (274,625 DOFs, 15.8 M nonzeros, 82 iterations in the reference), and
+the reference's SineLaplace example with its Neumann side (sine_*: Neumann
+boundary integral in the right-hand side, and the L2 / H1-semi / SD / L_inf
+errors of ConvectionDiffusion::output within 1e-10 / h of the reference's).
 """
 import numpy as np
 import pytest
@@ -47,7 +50,8 @@ def db_for(rc: RefCase, precision: str) -> m.ParameterDatabase:
 
 
 def make(ctx, rc: RefCase, precision: str):
-    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order)
+    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order,
+                            neumann_sides=rc.neumann_sides)
     cf = m.cd_coeffs(rc.eps, rc.b[:rc.dim], 0.0, True)
     return disc, m.ConvectionDiffusion(ctx, disc, cf, db_for(rc, precision), quad_points=rc.quad_points)
 
@@ -66,6 +70,11 @@ def test_gpu_assembly_and_fp64_solve_match_the_reference(ctx, name):
         assert abs(its - rc.iterations) <= 1, (name, its, rc.iterations)
         assert abs(init - rc.initial_residual) <= 1e-12 * rc.initial_residual, (init, rc.initial_residual)
         assert rc.compare("solution", prob.solution()) <= 1e-10
+        if rc.errors is not None:
+            # ConvectionDiffusion::output's errors of the SineLaplace cases: the
+            # solutions agree to 1e-10, so the errors agree to that over h
+            tol = 1e-10 * float(rc.z["solution_max"]) * 2 ** rc.n_refine
+            assert np.abs(np.array(prob.errors()) - rc.errors).max() <= tol, (prob.errors(), rc.errors)
     finally:
         prob.close()
         disc.close()

@@ -11,7 +11,11 @@ ConvectionDiffusion<d>::assemble and ::solve with FGMRES + multigrid).
   * the oracle's element loop reproduces the reference's assembled entries and
     right-hand sides within 1e-13 (relative to the largest entry), and its
     FGMRES + multigrid solve takes the reference's iteration count with a
-    solution within 1e-10.
+    solution within 1e-10;
+  * on the reference's SineLaplace example (Neumann boundary on x = 1) the
+    oracle's error functional gives the reference's L2 / H1-semi / SD / L_inf
+    errors of the same solution, and the oracle's own solutions reproduce the
+    golden errors of test/cd2d_test.c++:91-98 within its 1e-11.
 """
 import numpy as np
 import pytest
@@ -24,7 +28,8 @@ from ref_fixtures import RefCase, digest, names
 @pytest.mark.parametrize("name", names())
 def test_setup_is_bit_identical_to_the_reference(name):
     rc = RefCase(name)
-    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order)
+    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order,
+                            neumann_sides=rc.neumann_sides)
     try:
         for l in range(rc.n_levels):
             ref = rc.level(l)
@@ -43,7 +48,7 @@ def test_setup_is_bit_identical_to_the_reference(name):
 def test_oracle_reproduces_the_reference_assembly_and_solve(name):
     rc = RefCase(name)
     ora = ocd.OracleCD(rc.geometry, 1, rc.n_refine, rc.n_levels, rc.order, rc.eps, rc.b[:rc.dim], 0.0,
-                       rc.quad_points)
+                       rc.quad_points, neumann_sides=rc.neumann_sides)
     ora.assemble()
     for l in range(rc.n_levels):
         assert rc.compare("vals", ora.vals[l], l) <= 1e-13, (name, l)
@@ -55,4 +60,30 @@ def test_oracle_reproduces_the_reference_assembly_and_solve(name):
     # the initial residual |b - A x0| of the reference's LoopInfo
     assert abs(hist[0] - rc.initial_residual) <= 1e-12 * rc.initial_residual
     assert rc.compare("solution", sol) <= 1e-10
+    if rc.errors is not None:
+        if rc.has("solution") and not rc.has("solution_idx"):
+            # the functional alone, on the reference's own solution
+            assert np.allclose(ora.errors(rc.z["solution"]), rc.errors, rtol=1e-13, atol=0), name
+        assert np.allclose(ora.errors(sol), rc.errors, rtol=1e-9, atol=0), (ora.errors(sol), rc.errors)
+    ora.close()
+
+
+# test/cd2d_test.c++:91-98: SineLaplace on UnitSquare after 2 refinements,
+# errors L2, H1-semi, SD, L_inf; the test's tolerance is 1e-11 (:42)
+CD2D_GOLDEN = {1: (0.030136750989447, 0.50136473756928, 0.50136473756928, 0.086620472046938),
+               2: (0.0019271846609828, 0.050971302154831, 0.050971302154831, 0.0033739148851507)}
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_oracle_reproduces_the_cd2d_test_golden_errors(order):
+    """the W-cycle multigrid run of cd2d_test (2 levels, 2+2 Jacobi with the
+    default damping 1, direct coarse solve, residual_tolerance 1e-13) on the
+    oracle"""
+    ora = ocd.OracleCD(0, 1, 2, 2, order, 1.0, (0.0, 0.0), 0.0, 3 if order == 1 else 4, neumann_sides=2)
+    ora.assemble()
+    ora.build_mg(2, 2, 1.0, 1.0, "W")
+    sol, its, res, hist, st = ora.solve("fgmres", 1e-13, 0.0, 1000, 0, 20)
+    assert st == 0 and res <= 1e-13
+    err = ora.errors(sol)
+    assert np.abs(err - np.array(CD2D_GOLDEN[order])).max() <= 1e-11, err
     ora.close()
