@@ -1172,22 +1172,27 @@ constexpr size_t kGjRowsSmem = 160 * 1024;  // dynamic shared memory cap of k_gj
 constexpr int kGjCluster = 8;
 constexpr size_t kGjClusterSmem = 220 * 1024;
 
-__device__ __forceinline__ void gj_merge32(float& v, int& i, float v2, int i2) {
+template <class T>
+__device__ __forceinline__ void gj_merge(T& v, int& i, T v2, int i2) {
   if (v2 > v || (v2 == v && i2 < i)) {
     v = v2;
     i = i2;
   }
 }
 
-template <int NT>
+// T = float: the mixed cycle's inverse; T = double: the FP64 inverse, written
+// in place over the dense block M (every block reads its rows of M before the
+// first cluster barrier and writes them after the last one)
+template <class T, int NT>
 __global__ void __launch_bounds__(NT)
-k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ out, int* __restrict__ flag) {
+k_gj_cluster(int na, int R, const double* M, T* out, int* __restrict__ flag) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
-  extern __shared__ __align__(16) float gjc_smem[];
-  __shared__ float cand_v[2][kGjCluster];
+  extern __shared__ __align__(16) unsigned char gjc_raw[];
+  T* gjc_smem = reinterpret_cast<T*>(gjc_raw);
+  __shared__ T cand_v[2][kGjCluster];
   __shared__ int cand_i[2][kGjCluster];
-  __shared__ float s_f[256];  // multipliers of the own rows (R <= 256)
+  __shared__ T s_f[256];  // multipliers of the own rows (R <= 256)
   __shared__ int s_p, s_src, s_cand, s_sing;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int CS = int(cluster.num_blocks());
@@ -1197,25 +1202,25 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
   const int na32 = (na + 31) & ~31;
   const int G = max(1, NT / na32), CW = NT / G;
   const int tx = t % CW, ty = t / CW;
-  float* own = gjc_smem;                    // [R][na]
-  float* pubrow = own + (size_t)R * na;     // [2][na] pivot candidate for the next column
-  float* oldrow = pubrow + 2 * (size_t)na;  // [2][na] the row at the next position (pushed by its owner)
-  float* prow = oldrow + 2 * (size_t)na;    // scaled pivot row of the step
+  T* own = gjc_smem;                    // [R][na]
+  T* pubrow = own + (size_t)R * na;     // [2][na] pivot candidate for the next column
+  T* oldrow = pubrow + 2 * (size_t)na;  // [2][na] the row at the next position (pushed by its owner)
+  T* prow = oldrow + 2 * (size_t)na;    // scaled pivot row of the step
   int* perm_s = reinterpret_cast<int*>(prow + na);  // pivot positions
-  for (int e = t; e < nr * na; e += NT) own[e] = float(M[(size_t)r0 * na + e]);
+  for (int e = t; e < nr * na; e += NT) own[e] = T(M[(size_t)r0 * na + e]);
   if (t == 0) s_sing = 0;
   __syncthreads();
   auto publish = [&](int col, int buf) {
     if (warp == 0) {
-      float v = -1.0f;
+      T v = -T(1.0);
       int i = na;
       for (int q = lane; q < nr; q += 32)
-        if (r0 + q >= col) gj_merge32(v, i, fabsf(own[(size_t)q * na + col]), r0 + q);
+        if (r0 + q >= col) gj_merge<T>(v, i, fabs(own[(size_t)q * na + col]), r0 + q);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const T v2 = __shfl_xor_sync(0xffffffffu, v, o);
         const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
-        gj_merge32(v, i, v2, i2);
+        gj_merge<T>(v, i, v2, i2);
       }
       if (lane < CS) {  // into every block's candidate table
         cluster.map_shared_rank(&cand_v[buf][0], lane)[rank] = v;
@@ -1228,7 +1233,7 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
       for (int j = t; j < na; j += NT) pubrow[(size_t)buf * na + j] = own[(size_t)s_cand * na + j];
     if (col >= r0 && col < r1)  // the old row of the next step, into every block
       for (int q = 0; q < CS; ++q) {
-        float* dst = cluster.map_shared_rank(oldrow, q) + (size_t)buf * na;
+        T* dst = cluster.map_shared_rank(oldrow, q) + (size_t)buf * na;
         for (int j = t; j < na; j += NT) dst[j] = own[(size_t)(col - r0) * na + j];
       }
   };
@@ -1237,7 +1242,7 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
   for (int k = 0; k < na; ++k) {
     const int buf = k & 1;
     if (warp == 0) {  // the pivot: the same reduction in every block
-      float v = -1.0f;
+      T v = -T(1.0);
       int i = na;
       if (lane < CS) {
         v = cand_v[buf][lane];
@@ -1245,12 +1250,12 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const T v2 = __shfl_xor_sync(0xffffffffu, v, o);
         const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
-        gj_merge32(v, i, v2, i2);
+        gj_merge<T>(v, i, v2, i2);
       }
       if (lane == 0) {
-        const bool singular = !(v > 0.0f);
+        const bool singular = !(v > T(0.0));
         s_p = singular ? k : i;
         s_src = singular ? -1 : i / R;  // -1: the pivot row is the old row k
         perm_s[k] = s_p;
@@ -1259,27 +1264,27 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
     }
     __syncthreads();
     const int p = s_p;
-    const float* old = oldrow + (size_t)buf * na;
-    const float* src = s_src < 0 ? old : cluster.map_shared_rank(pubrow, s_src) + (size_t)buf * na;
-    const float pv = s_src < 0 ? 1.0f : src[k];
-    for (int j = t; j < na; j += NT) prow[j] = (j == k ? 1.0f : src[j]) / pv;
+    const T* old = oldrow + (size_t)buf * na;
+    const T* src = s_src < 0 ? old : cluster.map_shared_rank(pubrow, s_src) + (size_t)buf * na;
+    const T pv = s_src < 0 ? T(1.0) : src[k];
+    for (int j = t; j < na; j += NT) prow[j] = (j == k ? T(1.0) : src[j]) / pv;
     if (t < nr) {
       const int i = r0 + t;
       s_f[t] = (i == p && p != k) ? old[k] : own[(size_t)t * na + k];
     }
     __syncthreads();
     for (int j = tx; j < na; j += CW) {
-      const float pj = prow[j], oj = old[j];
+      const T pj = prow[j], oj = old[j];
       const bool jk = j == k;
       for (int ii = ty; ii < nr; ii += G) {  // the row index is the same across a warp
         const int i = r0 + ii;
-        float* Mij = own + (size_t)ii * na + j;
+        T* Mij = own + (size_t)ii * na + j;
         if (i != k && i != p) {
-          *Mij = (jk ? 0.0f : *Mij) - s_f[ii] * pj;
+          *Mij = (jk ? T(0.0) : *Mij) - s_f[ii] * pj;
         } else if (i == k) {
           *Mij = pj;
         } else {  // i == p != k: the old row k moves here
-          *Mij = (jk ? 0.0f : oj) - s_f[ii] * pj;
+          *Mij = (jk ? T(0.0) : oj) - s_f[ii] * pj;
         }
       }
     }
@@ -1289,11 +1294,11 @@ k_gj_cluster32(int na, int R, const double* __restrict__ M, float* __restrict__ 
   }
   // undo the column swaps (k_gj_unswap) on the own rows, write them out
   for (int q = t; q < nr; q += NT) {
-    float* row = own + (size_t)q * na;
+    T* row = own + (size_t)q * na;
     for (int k = na - 1; k >= 0; --k) {
       const int pk = perm_s[k];
       if (pk != k) {
-        const float a = row[k];
+        const T a = row[k];
         row[k] = row[pk];
         row[pk] = a;
       }
@@ -1320,6 +1325,34 @@ __global__ void k_coarse_gemv32(int n, int na, const int* __restrict__ act, cons
     const int t = (warp - na) * 32 + lane;
     if (t < n && pos[t] < 0) x[t] = b[t];
   }
+}
+
+// the mixed cycle's coarse solve with the FP64 inverse: FP32 right-hand
+// side and iterate, FP64 inverse entries and FP64 accumulation (the split
+// of the outer solve: FP64 for the coarse-grid direct solve)
+__global__ void k_coarse_gemv_mixed(int n, int na, const int* __restrict__ act, const int* __restrict__ pos,
+                                    const double* __restrict__ inv, const float* __restrict__ b,
+                                    float* __restrict__ x) {
+  pdl_enter();
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp < na) {
+    const double* row = inv + (size_t)warp * na;
+    double s = 0.0;
+    for (int j = lane; j < na; j += 32) s = fma(row[j], double(b[act[j]]), s);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) x[act[warp]] = float(s);
+  } else {
+    const int t = (warp - na) * 32 + lane;
+    if (t < n && pos[t] < 0) x[t] = b[t];
+  }
+}
+
+void DenseInverse::solve_mixed(pm_ctx* c, const float* b, float* x) {
+  if (!has64) throw Error(PM_E_INVALID, "coarse solve before the FP64 inverse was built");
+  const long long threads = (long long)na * 32 + n;
+  launch_k(c, k_coarse_gemv_mixed, dim3(nblocks(threads, 256)), dim3(256), 0, n, na, (const int*)act.p,
+           (const int*)pos.p, (const double*)inv.p, b, x);
 }
 
 void DenseInverse::build32(pm_ctx* c, const DevCsr& A) {
@@ -1366,13 +1399,13 @@ void DenseInverse::launch32(pm_ctx* c, const DevCsr& A, cudaStream_t s) {
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(k_gj_cluster32<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    attr_err = cudaFuncSetAttribute(k_gj_cluster<float, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(kGjClusterSmem));
     if (attr_err == cudaSuccess)
-      attr_err = cudaFuncSetAttribute(k_gj_cluster32<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      attr_err = cudaFuncSetAttribute(k_gj_cluster<float, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       int(kGjClusterSmem));
     if (attr_err == cudaSuccess)
-      attr_err = cudaFuncSetAttribute(k_gj_cluster32<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      attr_err = cudaFuncSetAttribute(k_gj_cluster<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       int(kGjClusterSmem));
   });
   PM_CUDA(attr_err);
@@ -1394,9 +1427,9 @@ void DenseInverse::launch32(pm_ctx* c, const DevCsr& A, cudaStream_t s) {
   float* outp = inv32.p;
   int* fl = flag.p;
   int na_arg = na, R_arg = R;
-  if (nt == 1024) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<1024>, na_arg, R_arg, Mp, outp, fl));
-  else if (nt == 512) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<512>, na_arg, R_arg, Mp, outp, fl));
-  else PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster32<256>, na_arg, R_arg, Mp, outp, fl));
+  if (nt == 1024) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster<float, 1024>, na_arg, R_arg, Mp, outp, fl));
+  else if (nt == 512) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster<float, 512>, na_arg, R_arg, Mp, outp, fl));
+  else PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster<float, 256>, na_arg, R_arg, Mp, outp, fl));
   c->kernel_launches++;
   if (!done_event) PM_CUDA(cudaEventCreateWithFlags(&done_event, cudaEventDisableTiming));
   PM_CUDA(cudaEventRecord(done_event, s));
@@ -1490,6 +1523,58 @@ void DenseInverse::launch64(pm_ctx* c, const DevCsr& A, cudaStream_t s) {
   if (na == 0) {
     has64 = true;
     return;
+  }
+  // Gauss-Jordan on one thread-block cluster when the active block fits its
+  // distributed shared memory (cluster barriers per column instead of grid
+  // barriers; the same pivot rule), in place
+  {
+    auto smem_for = [&](int R) { return (size_t(R) + 5) * na * sizeof(double) + size_t(na) * sizeof(int); };
+    int cs = std::max(1, std::min(kGjCluster, c->coarse_cluster)), R = (na + cs - 1) / cs;
+    while (cs < kGjCluster && smem_for(R) > kGjClusterSmem) {
+      cs *= 2;
+      R = (na + cs - 1) / cs;
+    }
+    const size_t smem = smem_for(R);
+    if (R <= 256 && smem <= kGjClusterSmem) {
+      static std::once_flag once;
+      static cudaError_t attr_err = cudaSuccess;
+      std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(k_gj_cluster<double, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(kGjClusterSmem));
+        if (attr_err == cudaSuccess)
+          attr_err = cudaFuncSetAttribute(k_gj_cluster<double, 512>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGjClusterSmem));
+        if (attr_err == cudaSuccess)
+          attr_err = cudaFuncSetAttribute(k_gj_cluster<double, 256>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(kGjClusterSmem));
+      });
+      PM_CUDA(attr_err);
+      const int nt = c->coarse_threads > 0 ? c->coarse_threads : 1024;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(unsigned(cs));
+      cfg.blockDim = dim3(unsigned(nt));
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = unsigned(cs);
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      const double* Mp = inv.p;
+      double* outp = inv.p;
+      int* fl = flag.p;
+      int na_arg = na, R_arg = R;
+      if (nt == 1024) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster<double, 1024>, na_arg, R_arg, Mp, outp, fl));
+      else if (nt == 512) PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster<double, 512>, na_arg, R_arg, Mp, outp, fl));
+      else PM_CUDA(cudaLaunchKernelEx(&cfg, k_gj_cluster<double, 256>, na_arg, R_arg, Mp, outp, fl));
+      c->kernel_launches++;
+      if (!done_event) PM_CUDA(cudaEventCreateWithFlags(&done_event, cudaEventDisableTiming));
+      PM_CUDA(cudaEventRecord(done_event, s));
+      pending64 = true;
+      return;
+    }
   }
   int coop = 0, per_sm = 0;
   PM_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));

@@ -180,6 +180,8 @@ struct DenseInverse {
   cudaEvent_t done_event = nullptr;  // recorded after the queued factorisation
   // x_a = inv32 b_a, x_n = b_n for a right-hand side with zero non-actives
   void solve32(pm_ctx* c, const float* b, float* x);
+  // the same with the FP64 inverse: FP32 vectors, FP64 products and sums
+  void solve_mixed(pm_ctx* c, const float* b, float* x);
   // x_a = inv (b_a - A_{a,n} b_n), x_n = b_n  (a: active rows, n: non-active);
   // rhs_nonactive_zero skips the b_n correction (the multigrid coarse rhs has
   // its non-actives reset to zero)

@@ -120,6 +120,9 @@ void Multigrid::configure(const Params& p) {
   if (type != "standard") throw Error(PM_E_UNSUPPORTED, "only standard multigrid is implemented");
   mixed = p.str("gpu_precision", "fp64") == "mixed";
   mixed_cfg = mixed;
+  const std::string cp = p.str("gpu_mixed_coarse", "fp32");
+  if (cp != "fp32" && cp != "fp64") throw Error(PM_E_INVALID, "gpu_mixed_coarse is fp32 or fp64");
+  coarse64 = cp == "fp64";
 }
 
 void Multigrid::set_mixed(pm_ctx* c, bool on) {
@@ -145,7 +148,7 @@ void Multigrid::start_coarse(pm_ctx* c) {
   // the side stream starts after the assembly queued so far on the main one
   PM_CUDA(cudaEventRecord(c->side_event, c->stream));
   PM_CUDA(cudaStreamWaitEvent(c->side, c->side_event, 0));
-  if (mixed_cfg) levels[0].coarse.launch32(c, levels[0].A->csr, c->side);
+  if (mixed_cfg && !coarse64) levels[0].coarse.launch32(c, levels[0].A->csr, c->side);
   else levels[0].coarse.launch64(c, levels[0].A->csr, c->side);
 }
 
@@ -210,8 +213,8 @@ void Multigrid::update(pm_ctx* c) {
       // DirectSolver factorises get_combined_matrix (with the pressure projection);
       // the mixed cycle solves with an FP32 inverse (the FP64 one is made on a
       // fallback to FP64)
-      if (mixed && lv.coarse.pending32) lv.coarse.complete32(c, A);  // queued by start_coarse
-      else if (mixed) lv.coarse.build32(c, lv.proj ? lv.proj->csr : A);
+      if (mixed && !coarse64 && lv.coarse.pending32) lv.coarse.complete32(c, A);  // queued by start_coarse
+      else if (mixed && !coarse64) lv.coarse.build32(c, lv.proj ? lv.proj->csr : A);
       else if (lv.coarse.pending64) lv.coarse.complete64(c);
       else lv.coarse.build(c, lv.proj ? lv.proj->csr : A);
       if (mixed) {
@@ -278,7 +281,9 @@ void Multigrid::smooth_from_zero(pm_ctx* c, int l) {
 void Multigrid::coarse_solve(pm_ctx* c) {
   MGLevel& lv = levels[0];
   const DevCsr& A = lv.A->csr;
-  if (mixed) {
+  if (mixed && coarse64) {
+    lv.coarse.solve_mixed(c, lv.rhs32.p, lv.cur32);
+  } else if (mixed) {
     // the coarse rhs comes from the restriction with its non-actives reset
     lv.coarse.solve32(c, lv.rhs32.p, lv.cur32);
   } else {

@@ -69,6 +69,9 @@ struct Multigrid {
   std::string cycle_type = "V";
   bool mixed = false;       // the precision the cycle runs in now
   bool mixed_cfg = false;   // the precision the database asked for
+  // mixed form: the coarse direct solve with the FP64 inverse (FP32 vectors,
+  // FP64 products and sums) instead of an FP32 inverse (gpu_mixed_coarse)
+  bool coarse64 = false;
   bool fp64_smoothers = false;  // FP64 Vanka factors exist for the current matrices
   bool ready = false;
 

@@ -3,8 +3,9 @@ allowed values for the solve path.
 
 Defaults follow Solver<>::default_solver_database (src/Solver/Solver.C:21-115)
 and Multigrid::default_multigrid_database (src/Multigrid/Multigrid.C:422-514).
-New keys with defaults here: `gpu_precision` (fp64 | mixed) and `gpu_mixed_fallback`
-(0 | 1); `gpu_gram_schmidt` and `gpu_cuda_graphs` can be added with `add`.
+New keys with defaults here: `gpu_precision` (fp64 | mixed), `gpu_mixed_fallback`
+(0 | 1) and `gpu_mixed_coarse` (fp32 | fp64); `gpu_gram_schmidt` and `gpu_cuda_graphs` can be
+added with `add`.
 """
 from __future__ import annotations
 
@@ -54,6 +55,9 @@ _GPU_DEFAULTS: dict[str, tuple[Any, tuple | None]] = {
     # mixed form: the multigrid switches to FP64 for the rest of a solve when
     # the FP64 residual falls by less than half over 10 FGMRES iterations
     "gpu_mixed_fallback": (1, (0, 1)),
+    # mixed form: the coarse direct solve with an FP32 inverse or with the
+    # FP64 inverse (FP32 vectors in and out, FP64 products and sums)
+    "gpu_mixed_coarse": ("fp32", ("fp32", "fp64")),
 }
 
 # TimeDiscretization::default_TimeDiscretization_database

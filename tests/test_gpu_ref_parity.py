@@ -96,3 +96,30 @@ def test_gpu_mixed_form_error_against_the_reference(ctx, name):
     finally:
         prob.close()
         disc.close()
+
+
+@pytest.mark.parametrize("name", ["cd2d_q1_128", "cd3d_q2_32"])
+def test_gpu_mixed_form_with_the_fp64_coarse_solve(ctx, name):
+    """gpu_mixed_coarse = fp64: the mixed cycle's coarse direct solve uses the
+    FP64 inverse (FP32 vectors, FP64 products and sums). It takes the
+    iterations of the FP32-inverse cycle (within one) and stays within the
+    mixed form's 1e-7 of the reference's solution."""
+    rc = RefCase(name)
+    its = {}
+    for coarse in ("fp32", "fp64"):
+        disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order)
+        db = db_for(rc, "mixed")
+        db["gpu_mixed_coarse"] = coarse
+        prob = m.ConvectionDiffusion(ctx, disc, m.cd_coeffs(rc.eps, rc.b[:rc.dim], 0.0, True), db,
+                                     quad_points=rc.quad_points)
+        try:
+            prob.assemble()
+            prob.solve()
+            it, res, init = prob.last_info()
+            assert res <= rc.reduction * init
+            assert rc.compare("solution", prob.solution()) <= 1e-7
+            its[coarse] = it
+        finally:
+            prob.close()
+            disc.close()
+    assert abs(its["fp64"] - its["fp32"]) <= 1, its
