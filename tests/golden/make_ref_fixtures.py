@@ -20,6 +20,14 @@ number 0, include/Examples/CD_2D/SineLaplace.h: u = sin(pi x) sin(pi y),
 eps = 1, Neumann boundary on x = 1) instead of the driver's sine problem, and
 keep the L2, H1-semi, SD and L_inf errors of ConvectionDiffusion::output.
 
+The stokes_* cases run the driver oracle/ref/ref_stokes.C: the reference's
+NavierStokes<3> as a Stokes problem with P2/P1 elements on
+Default_UnitCube_Tetra and its example -3 (test_u_2_p_1). Per level: digests
+of the cell vertices and of the velocity and pressure GlobalNumbers, and the
+combined matrix of BlockFEMatrix::get_combined_matrix (the pressure
+projection applied, exact zeros removed) with the right-hand side; on the
+smallest mesh also the direct solve's solution.
+
     python tests/golden/make_ref_fixtures.py            # all cases
     python tests/golden/make_ref_fixtures.py cd3d_q2_8  # one case
 """
@@ -58,6 +66,13 @@ CASES = {
     "sine_q2_4": (2, 2, 2, 2, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-12, True, 0),
     "sine_q1_64": (2, 6, 1, 4, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-10, False, 0),
     "sine_q2_32": (2, 5, 2, 3, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-10, False, 0),
+}
+
+
+# name: (refinements of Default_UnitCube_Tetra, levels, full arrays, direct solve)
+STOKES_CASES = {
+    "stokes_p2p1_4": (2, 2, True, True),
+    "stokes_p2p1_8": (3, 3, False, False),
 }
 
 
@@ -127,6 +142,51 @@ def run_case(name: str) -> None:
     print(f"{name}: {int(out['iterations'])} iterations, final residual {float(out['final_residual']):.3e}")
 
 
+def run_stokes_case(name: str) -> None:
+    import build_ref
+    nref, nlev, full, direct = STOKES_CASES[name]
+    exe = build_ref.link_program("3", build_ref.HERE / "ref_stokes.C", build_ref.OUT / "ref_stokes3d")
+    out: dict[str, np.ndarray] = {"config": np.array([nref, nlev], dtype=np.int64)}
+    with tempfile.TemporaryDirectory() as tmp:
+        subprocess.run([str(exe), tmp, str(nref), str(nlev), "none"], check=True, capture_output=True)
+        meta = {}
+        for line in Path(tmp, "meta.txt").read_text().splitlines():
+            k, v = line.split(None, 1)
+            meta[k] = v
+        for rl in range(nlev):
+            lvl = nlev - 1 - rl
+            info = meta[f"L{rl}"].split()
+            kv = dict(zip(info[0::2], map(int, info[1::2])))
+            rd = lambda n, t: np.fromfile(Path(tmp, f"L{rl}_{n}"), dtype=t)
+            udm, pdm, verts = rd("u_dofmap.i32", np.int32), rd("p_dofmap.i32", np.int32), rd("verts.f64", np.float64)
+            rows, cols, vals, rhs = (rd("rows.i32", np.int32), rd("cols.i32", np.int32), rd("vals.f64", np.float64),
+                                     rd("rhs.f64", np.float64))
+            p = f"L{lvl}_"
+            out[p + "sizes"] = np.array([kv["cells"], kv["u_n_dofs"], kv["u_active"], kv["p_n_dofs"], kv["p_active"],
+                                         kv["nnz"]], np.int64)
+            out[p + "digests"] = np.array([digest(udm), digest(pdm), digest(verts)])
+            out[p + "vals_max"] = np.array(np.abs(vals).max())
+            out[p + "rhs_max"] = np.array(np.abs(rhs).max())
+            out[p + "rhs"] = rhs
+            if full:
+                out[p + "rows"], out[p + "cols"], out[p + "vals"] = rows, cols, vals
+            else:
+                # a fixed sample of the combined matrix's entries as (row, column, value)
+                idx = sample_idx(vals.size)
+                row_of = np.repeat(np.arange(rows.size - 1, dtype=np.int32), np.diff(rows))
+                out[p + "sample_rows"], out[p + "sample_cols"] = row_of[idx], cols[idx]
+                out[p + "sample_vals"] = vals[idx]
+    if direct:
+        with tempfile.TemporaryDirectory() as tmp:
+            subprocess.run([str(exe), tmp, str(nref), "1", "direct"], check=True, capture_output=True)
+            out["solution"] = np.fromfile(Path(tmp, "solution.f64"), dtype=np.float64)
+    np.savez_compressed(HERE / f"ref_{name}.npz", **out)
+    print(f"{name}: {nlev} levels" + (", direct solution" if direct else ""))
+
+
 if __name__ == "__main__":
-    for n in (sys.argv[1:] or list(CASES)):
-        run_case(n)
+    for n in (sys.argv[1:] or list(CASES) + list(STOKES_CASES)):
+        if n in STOKES_CASES:
+            run_stokes_case(n)
+        else:
+            run_case(n)

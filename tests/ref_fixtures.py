@@ -18,7 +18,12 @@ _POINTS = {0: 2, 1: 2, 2: 2, 3: 3, 4: 3, 5: 3, 6: 4, 7: 4}
 
 
 def names() -> list[str]:
-    return sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_*.npz"))
+    """the convection-diffusion cases"""
+    return sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_*.npz") if not p.stem.startswith("ref_stokes"))
+
+
+def stokes_names() -> list[str]:
+    return sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_stokes*.npz"))
 
 
 class RefCase:
@@ -63,3 +68,52 @@ class RefCase:
 
 def digest(a: np.ndarray, dtype) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, dtype=dtype).tobytes()).hexdigest()
+
+
+class StokesRefCase:
+    """a Stokes fixture: NavierStokes<3> (Stokes, P2/P1, example -3) of the
+    reference on Default_UnitCube_Tetra"""
+
+    def __init__(self, name: str):
+        self.name = name
+        self.z = np.load(GOLDEN / f"ref_{name}.npz")
+        self.n_refine, self.n_levels = (int(v) for v in self.z["config"])
+
+    def has(self, key: str) -> bool:
+        return key in self.z.files
+
+    def level(self, l: int) -> dict:
+        p = f"L{l}_"
+        d = {k[len(p):]: self.z[k] for k in self.z.files if k.startswith(p)}
+        cells, nu, nua, np_, npa, nnz = (int(v) for v in d["sizes"])
+        d.update(cells=cells, nu=nu, nu_active=nua, np=np_, np_active=npa, nnz=nnz)
+        return d
+
+    def compare_matrix(self, l: int, rp: np.ndarray, ci: np.ndarray, vals: np.ndarray) -> float:
+        """largest difference between the reference's combined matrix of level
+        l (pressure projection applied, exact zeros removed) and the given
+        projected CSR matrix, relative to the reference's largest entry; the
+        given matrix's entries outside the reference's pattern count as
+        differences from zero"""
+        d = self.level(l)
+        n = rp.size - 1
+        ours_row = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp))
+        ours_key = ours_row * n + ci
+        if "rows" in d:
+            ref_row = np.repeat(np.arange(d["rows"].size - 1, dtype=np.int64), np.diff(d["rows"]))
+            ref_key, ref_val = ref_row * n + d["cols"], d["vals"]
+            # every entry of ours: the reference's value or zero
+            pos = np.searchsorted(ref_key, ours_key)
+            pos_c = np.minimum(pos, ref_key.size - 1)
+            hit = ref_key[pos_c] == ours_key
+            diff_ours = np.abs(vals - np.where(hit, ref_val[pos_c], 0.0)).max()
+        else:
+            ref_key = d["sample_rows"].astype(np.int64) * n + d["sample_cols"]
+            ref_val = d["sample_vals"]
+            diff_ours = 0.0
+        # every entry of the reference: ours must hold it
+        pos = np.searchsorted(ours_key, ref_key)
+        pos_c = np.minimum(pos, ours_key.size - 1)
+        assert np.all(ours_key[pos_c] == ref_key), "an entry of the reference is outside the pattern"
+        diff_ref = np.abs(vals[pos_c] - ref_val).max()
+        return float(max(diff_ours, diff_ref) / float(d["vals_max"]))

@@ -12,6 +12,11 @@ ConvectionDiffusion<d>::assemble and ::solve with FGMRES + multigrid).
     right-hand sides within 1e-13 (relative to the largest entry), and its
     FGMRES + multigrid solve takes the reference's iteration count with a
     solution within 1e-10;
+  * Stokes P2/P1 (the reference's NavierStokes<3> as a Stokes problem on
+    Default_UnitCube_Tetra, example -3): the library's velocity and pressure
+    numbering and cell vertices are bit-identical on every level; the oracle's
+    projected matrices equal the reference's combined matrices within 1e-13 and
+    its direct solution the reference's (velocity 1e-12, mean-free pressure);
   * on the reference's SineLaplace example (Neumann boundary on x = 1) the
     oracle's error functional gives the reference's L2 / H1-semi / SD / L_inf
     errors of the same solution, and the oracle's own solutions reproduce the
@@ -22,7 +27,8 @@ import pytest
 
 import mymoonmd_gb300 as m
 from oracle import cd as ocd
-from ref_fixtures import RefCase, digest, names
+from oracle import stokes as ost
+from ref_fixtures import RefCase, StokesRefCase, digest, names, stokes_names
 
 
 @pytest.mark.parametrize("name", names())
@@ -86,4 +92,45 @@ def test_oracle_reproduces_the_cd2d_test_golden_errors(order):
     assert st == 0 and res <= 1e-13
     err = ora.errors(sol)
     assert np.abs(err - np.array(CD2D_GOLDEN[order])).max() <= 1e-11, err
+    ora.close()
+
+
+
+@pytest.mark.parametrize("name", stokes_names())
+def test_stokes_setup_is_bit_identical_to_the_reference(name):
+    rc = StokesRefCase(name)
+    disc = m.Discretization(m.GEO_CUBE_TETRA, 1, rc.n_refine, rc.n_levels, m.KIND_STOKES, 12)
+    try:
+        for l in range(rc.n_levels):
+            ref = rc.level(l)
+            iu, ip = disc.level_info(l, 0), disc.level_info(l, 1)
+            assert (iu["n_cells"], iu["n_dofs"], iu["n_active"], ip["n_dofs"], ip["n_active"]) == \
+                (ref["cells"], ref["nu"], ref["nu_active"], ref["np"], ref["np_active"]), (name, l)
+            got = [digest(disc.dofmap(l, 0), np.int32), digest(disc.dofmap(l, 1), np.int32),
+                   digest(disc.cell_vertices(l), np.float64)]
+            assert got == [str(s) for s in ref["digests"]], (name, l)
+    finally:
+        disc.close()
+
+
+@pytest.mark.parametrize("name", stokes_names())
+def test_oracle_stokes_assembly_matches_the_reference(name):
+    rc = StokesRefCase(name)
+    ora = ost.OracleStokes(1, rc.n_refine, rc.n_levels, 1.0, example=-3)
+    ora.assemble()
+    for l, lv in enumerate(ora.levels):
+        assert rc.compare_matrix(l, lv.vrow_ptr, lv.vcols, ora.pvals[l]) <= 1e-13, (name, l)
+        ref_rhs = rc.level(l)["rhs"]
+        assert np.abs(ora.rhs[l] - ref_rhs).max() <= 1e-13 * float(rc.level(l)["rhs_max"]), (name, l)
+    if rc.has("solution"):
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spla
+        lv = ora.finest
+        A = sp.csr_matrix((ora.pvals[-1], lv.vcols, lv.vrow_ptr), shape=(lv.n, lv.n))
+        x = spla.spsolve(A.tocsc(), ora.rhs[-1])
+        ref = rc.z["solution"]
+        nu3 = 3 * lv.nu
+        assert np.abs(x[:nu3] - ref[:nu3]).max() <= 1e-12 * np.abs(ref[:nu3]).max()
+        p, pr = x[nu3:], ref[nu3:]
+        assert np.abs((p - p.mean()) - (pr - pr.mean())).max() <= 1e-10
     ora.close()
