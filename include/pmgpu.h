@@ -239,6 +239,16 @@ int pm_disc_create(int geometry, int root_n, int n_refine, int n_levels, int kin
  * right-hand side (no exact solution) the Neumann data are zero. */
 int pm_disc_create_bc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
                       int neumann_sides, pm_disc** out);
+/* pm_disc_create_bc with the heavy part of the set-up on the context's GPU:
+ * for convection-diffusion levels the CSR structure (TStructure(space),
+ * src/Matrix/Structure.C:829-1283, sorted) and the assembly gather plans come
+ * from one stable radix sort of the element entries by (row, column) instead
+ * of the host construction. The result is the same discretisation, array for
+ * array (refinement, numbering and transfer stay on the host). The context's
+ * stream is synchronised; temporary device memory of about 40 bytes per
+ * element-matrix entry of the finest level is freed before the call returns. */
+int pm_disc_create_device(pm_ctx* ctx, int geometry, int root_n, int n_refine, int n_levels, int kind,
+                          int elem, int neumann_sides, pm_disc** out);
 void pm_disc_destroy(pm_disc* d);
 /* per level (0 = coarsest kept level): cells, local DOFs per cell, DOFs,
  * active DOFs and nnz of the level matrix (space 0 = velocity/scalar,

@@ -118,6 +118,7 @@ _SIGS = {
     "pm_solver_apply_preconditioner": (i32, [vp, vp, vp]),
     "pm_disc_create": (i32, [i32, i32, i32, i32, i32, i32, C.POINTER(vp)]),
     "pm_disc_create_bc": (i32, [i32, i32, i32, i32, i32, i32, i32, C.POINTER(vp)]),
+    "pm_disc_create_device": (i32, [vp, i32, i32, i32, i32, i32, i32, i32, C.POINTER(vp)]),
     "pm_disc_destroy": (None, [vp]),
     "pm_disc_level_info": (i32, [vp, i32, i32, pi32, pi32, pi32, pi32, C.POINTER(i64)]),
     "pm_disc_dofmap": (i32, [vp, i32, i32, vp]),

@@ -349,11 +349,18 @@ class Discretization:
     """Mesh hierarchy + FE spaces + structures + transfer (host set-up)."""
 
     def __init__(self, geometry: int, root_n: int, n_refine: int, n_levels: int, kind: int = KIND_CD,
-                 elem: int = 1, neumann_sides: int = 0):
+                 elem: int = 1, neumann_sides: int = 0, ctx: Optional["Context"] = None):
         """neumann_sides: bit mask of the unit square's sides (0 y=0, 1 x=1,
-        2 y=1, 3 x=0) with Neumann conditions; the others are Dirichlet"""
+        2 y=1, 3 x=0) with Neumann conditions; the others are Dirichlet.
+        ctx: build the structure and the gather plans on that context's GPU
+        (pm_disc_create_device); the same discretisation as without"""
         h = C.c_void_p()
-        check(lib.pm_disc_create_bc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides, C.byref(h)))
+        if ctx is not None:
+            check(lib.pm_disc_create_device(ctx.handle, geometry, root_n, n_refine, n_levels, kind, elem,
+                                            neumann_sides, C.byref(h)), ctx.handle)
+        else:
+            check(lib.pm_disc_create_bc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides,
+                                        C.byref(h)))
         self.handle = h
         self.geometry, self.root_n, self.n_refine, self.n_levels = geometry, root_n, n_refine, n_levels
         self.kind, self.elem, self.neumann_sides = kind, elem, neumann_sides

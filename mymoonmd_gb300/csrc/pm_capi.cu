@@ -9,6 +9,7 @@
 #include "pm_assemble.h"
 #include "pm_disc.h"
 #include "pm_problem.h"
+#include "pm_devsetup.h"
 #include "pm_solver.h"
 
 using namespace pm;
@@ -630,6 +631,23 @@ int pm_disc_create_bc(int geometry, int root_n, int n_refine, int n_levels, int 
   PM_CATCH(nullptr)
 }
 
+int pm_disc_create_device(pm_ctx* c, int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
+                          int neumann_sides, pm_disc** out) {
+  if (!c || !out) return fail(c, PM_E_INVALID, "null argument");
+  PM_TRY
+  auto* d = new pm_disc();
+  try {
+    d->d = build_disc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides,
+                      [c](DiscLevel& L) { device_level_structure(c, L); });
+  } catch (...) {
+    delete d;
+    throw;
+  }
+  *out = d;
+  return PM_OK;
+  PM_CATCH(c)
+}
+
 void pm_disc_destroy(pm_disc* d) { delete d; }
 
 static const DiscLevel* disc_level(const pm_disc* d, int level) {
@@ -904,8 +922,10 @@ int pm_problem_assemble(pm_problem* p) {
     double* r = (l == nl - 1) ? p->rhs.p : p->rhs_coarse.p;
     assemble_cd_level(c, p->alev[l], D.dim(), D.elem, p->qn, p->coeffs, p->ref, p->mats[l]->csr, r,
                       p->K.p, p->F.p);
-    // the coarse factorisation overlaps the assembly of the finer levels
-    if (l == 0 && nl > 1 && p->solver->use_mg) p->solver->mg.start_coarse(c);
+    // the coarse factorisation overlaps the assembly of the finer levels; the
+    // multigrid's coarsest level is disc level nl - (multigrid levels)
+    if (p->solver->use_mg && l == nl - int(p->solver->mg.levels.size()) && l + 1 < nl)
+      p->solver->mg.start_coarse(c);
   }
   // copy_nonactive(rhs -> solution) (ConvectionDiffusion.C:343)
   const DevCsr& top = p->mats.back()->csr;

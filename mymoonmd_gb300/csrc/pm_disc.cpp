@@ -292,7 +292,7 @@ static void build_neumann_plan(const Hierarchy& h, DiscLevel& L, int neumann_sid
 }
 
 std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
-                                 int neumann_sides) {
+                                 int neumann_sides, const std::function<void(DiscLevel&)>& device_structure) {
   if (n_levels < 1 || n_levels > n_refine + 1)
     throw std::invalid_argument("multigrid levels must be between 1 and refinements + 1");
   auto D = std::make_unique<Disc>();
@@ -333,11 +333,15 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
     L.level_in_hierarchy = first + l;
     L.n_cells = D->h.levels[first + l].n_cells;
     L.space = build_space(D->h, first + l, elem, BND_DIRICHLET, neumann_sides);
-    L.sys = build_structure(L.space, L.n_cells);
     L.verts = cell_vertices(D->h, first + l);
-    std::vector<char> act(L.space.n_dofs, 0);
-    for (int i = 0; i < L.space.n_active; ++i) act[i] = 1;
-    build_gather(L, L.space.nloc, L.space.dofmap, act);
+    if (device_structure) {
+      device_structure(L);
+    } else {
+      L.sys = build_structure(L.space, L.n_cells);
+      std::vector<char> act(L.space.n_dofs, 0);
+      for (int i = 0; i < L.space.n_active; ++i) act[i] = 1;
+      build_gather(L, L.space.nloc, L.space.dofmap, act);
+    }
     fill_bnd_xyz(D->h, L);
     build_neumann_plan(D->h, L, neumann_sides);
     L.n_blocks = 1;

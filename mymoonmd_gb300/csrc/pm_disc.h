@@ -2,6 +2,7 @@
 // its FE space(s), system CSR pattern, gather plans for the device assembly and
 // the prolongation to the next finer level.
 #pragma once
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -64,8 +65,12 @@ struct Disc {
   int nvc() const { return h.nvc; }
 };
 
+// device_structure (optional): builds a convection-diffusion level's `sys`,
+// gather plans and diag_pos from its space in place of the host construction
+// (the GPU set-up, pm_devsetup.cu); the results are the same arrays
 std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
-                                 int neumann_sides = 0);
+                                 int neumann_sides = 0,
+                                 const std::function<void(DiscLevel&)>& device_structure = nullptr);
 
 }  // namespace pm
 

@@ -127,7 +127,9 @@ struct pm_server {
   std::atomic<bool> pressure{false};
   std::atomic<int64_t> committed_view{0};
 
-  std::shared_ptr<SharedSetup> setup_for(const SetupKey& k) {
+  // the set-up of k (built once; convection-diffusion structures on the
+  // caller's GPU when a context is given)
+  std::shared_ptr<SharedSetup> setup_for(const SetupKey& k, pm_ctx* ctx = nullptr) {
     std::shared_ptr<SharedSetup> s;
     {
       std::lock_guard<std::mutex> g(setup_mu);
@@ -137,7 +139,10 @@ struct pm_server {
     }
     std::lock_guard<std::mutex> g(s->mu);
     if (s->status < 0) {
-      s->status = pm_disc_create(k.geometry, k.root_n, k.n_refine, k.n_levels, k.kind, k.elem, &s->disc);
+      s->status = ctx && k.kind == 0
+                      ? pm_disc_create_device(ctx, k.geometry, k.root_n, k.n_refine, k.n_levels, k.kind, k.elem, 0,
+                                              &s->disc)
+                      : pm_disc_create(k.geometry, k.root_n, k.n_refine, k.n_levels, k.kind, k.elem, &s->disc);
       if (s->status != PM_OK) s->error = pm_last_error(nullptr);
     }
     return s;
@@ -284,7 +289,7 @@ void Lane::run() {
     std::vector<Job> deferred;
     for (auto& job : taken) {
       const auto t0 = Clock::now();
-      if (!setup) setup = S.setup_for(key);
+      if (!setup) setup = S.setup_for(key, ctx);
       if (setup->status != PM_OK) {
         fail_job(job, setup->status, setup->error);
         std::lock_guard<std::mutex> g(S.mu);
@@ -536,7 +541,7 @@ void pm_server::worker(int index) {
       entry = &it->second;
       res.cache_hit = 1;
     } else {
-      auto setup = setup_for(key);
+      auto setup = setup_for(key, ctx);
       if (setup->status != PM_OK) {
         rc = setup->status;
       } else {

@@ -1,0 +1,87 @@
+"""The set-up on the GPU (pm_disc_create_device): the CSR structure and the
+assembly gather plans of every convection-diffusion level come from one
+stable radix sort of the element entries instead of the host construction.
+The discretisation must be the same array for array: structure, numbering,
+prolongations, and - through the gather plans - the assembled matrices and
+right-hand sides, bit for bit."""
+import numpy as np
+import pytest
+
+import mymoonmd_gb300 as m
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    (m.GEO_SQUARE_QUAD, 2, 5, 3, 1, 0),   # 2D Q1 64^2 on a 2x2 root mesh
+    (m.GEO_SQUARE_QUAD, 1, 4, 3, 2, 2),   # 2D Q2 16^2, Neumann side x = 1
+    (m.GEO_CUBE_HEXA, 1, 3, 3, 1, 0),     # 3D Q1 8^3
+    (m.GEO_CUBE_HEXA, 1, 4, 3, 2, 0),     # 3D Q2 16^3
+]
+
+
+def db():
+    d = m.ParameterDatabase.solve_path_database()
+    d["solver_type"] = "iterative"
+    d["iterative_solver_type"] = "fgmres"
+    d["preconditioner"] = "multigrid"
+    d["residual_tolerance"] = 0.0
+    d["residual_reduction"] = 1e-10
+    d["multigrid_smoother"] = "jacobi"
+    d["jacobi_damp"] = 0.8
+    return d
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_device_setup_equals_the_host_setup(ctx, case):
+    geo, root, nref, nlev, elem, neumann = case
+    host = m.Discretization(geo, root, nref, nlev, m.KIND_CD, elem, neumann_sides=neumann)
+    dev = m.Discretization(geo, root, nref, nlev, m.KIND_CD, elem, neumann_sides=neumann, ctx=ctx)
+    probs = []
+    try:
+        for l in range(nlev):
+            assert host.level_info(l) == dev.level_info(l)
+            for a, b in zip(host.structure(l), dev.structure(l)):
+                assert np.array_equal(a, b), l
+            assert np.array_equal(host.dofmap(l), dev.dofmap(l))
+            if l + 1 < nlev:
+                for a, b in zip(host.prolongation(l)[:3], dev.prolongation(l)[:3]):
+                    assert np.array_equal(a, b)
+        dim_b = (1.0, 0.5, 0.25) if geo == m.GEO_CUBE_HEXA else (1.0, 0.5)
+        cf = m.cd_coeffs(0.05, dim_b, 0.0, True)
+        for d in (host, dev):
+            p = m.ConvectionDiffusion(ctx, d, cf, db())
+            p.assemble()
+            probs.append(p)
+        for l in range(nlev):
+            assert np.array_equal(probs[0].matrix(l).values(), probs[1].matrix(l).values()), l
+        assert np.array_equal(probs[0].rhs(), probs[1].rhs())
+        for p in probs:
+            p.solve()
+        assert np.array_equal(probs[0].solution(), probs[1].solution())
+    finally:
+        for p in probs:
+            p.close()
+        host.close()
+        dev.close()
+
+
+def test_device_setup_time_of_the_32cube_q2_hierarchy(ctx):
+    """the set-up of the 3D Q2 32^3 workload (4 levels): host construction
+    against the GPU one (timings printed; the GPU one must be faster)"""
+    import time
+    t0 = time.perf_counter()
+    host = m.Discretization(m.GEO_CUBE_HEXA, 1, 5, 4, m.KIND_CD, 2)
+    t1 = time.perf_counter()
+    dev = m.Discretization(m.GEO_CUBE_HEXA, 1, 5, 4, m.KIND_CD, 2, ctx=ctx)  # warm-up of the sort kernels
+    dev.close()
+    t2 = time.perf_counter()
+    dev = m.Discretization(m.GEO_CUBE_HEXA, 1, 5, 4, m.KIND_CD, 2, ctx=ctx)
+    t3 = time.perf_counter()
+    try:
+        for a, b in zip(host.structure(3), dev.structure(3)):
+            assert np.array_equal(a, b)
+        print(f"32^3 Q2 set-up: host {t1 - t0:.3f} s, GPU {t3 - t2:.3f} s")
+        assert t3 - t2 < t1 - t0
+    finally:
+        host.close()
+        dev.close()

@@ -410,3 +410,21 @@ def test_mixed_form_restarts_in_fp64_after_an_fp32_overflow(ctx):
     assert res64 <= 1e-8 * init64 and resm <= 1e-8 * initm
     assert itm == it64 + 1
     assert rel(solm, sol64) <= 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_multigrid_on_fewer_levels_than_the_discretisation_keeps(ctx, precision):
+    """multigrid_n_levels = 2 on a discretisation of 3 levels: the cycle runs on
+    the two finest levels, and the coarse direct solve factorises the middle
+    level once that level is assembled (not the unused coarsest one)"""
+    disc, prob, ora = make_pair(ctx, "q1_2d", mg_db(2, precision=precision))
+    prob.solve()
+    it, res, init = prob.last_info()
+    ora.build_mg(2, 2, 0.8, 1.0, "V", n_mg_levels=2)
+    sol, oit, ores, hist, st = ora.solve("fgmres", 0.0, 1e-10, 200, 0, 20)
+    assert st == 0 and res < 1e-10 * init
+    if precision == "fp64":
+        assert abs(it - oit) <= 1, (it, oit)
+    assert rel(prob.solution(), sol) <= (1e-10 if precision == "fp64" else 1e-7)
+    prob.close()
+    disc.close()
