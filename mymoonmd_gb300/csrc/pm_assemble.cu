@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "pm_assemble.h"
+#include "pm_tetra.h"
 
 namespace pm {
 
@@ -93,6 +94,42 @@ void build_qk_tables(int dim, int k, int qn, RefTables& t) {
       }
 }
 
+// P1 / P2 tables on a tetrahedral rule: qn = 11 (P4Tetra) or 15 (P5Tetra)
+// points; the same layout as build_qk_tables (dim 3)
+void build_pk_tables(int elem, int qn, RefTables& t) {
+  if (qn != kP4n && qn != kP5n) throw Error(PM_E_UNSUPPORTED, "tetrahedral rules with 11 or 15 points");
+  const double* X = qn == kP4n ? kP4x : kP5x;
+  const double* Y = qn == kP4n ? kP4y : kP5y;
+  const double* Z = qn == kP4n ? kP4z : kP5z;
+  const double* W = qn == kP4n ? kP4w : kP5w;
+  t.dim = 3;
+  t.nb = elem == 12 ? 10 : 4;
+  t.nq = qn;
+  t.w.assign(W, W + qn);
+  t.xi.assign(size_t(qn) * 3, 0.0);
+  t.phi.assign(size_t(qn) * t.nb, 0.0);
+  t.dphi.assign(size_t(3) * qn * t.nb, 0.0);
+  for (int q = 0; q < qn; ++q) {
+    t.xi[q * 3 + 0] = X[q];
+    t.xi[q * 3 + 1] = Y[q];
+    t.xi[q * 3 + 2] = Z[q];
+    double v[10], dx[10], dy[10], dz[10];
+    if (elem == 12) p2_eval(X[q], Y[q], Z[q], v, dx, dy, dz);
+    else p1_eval(X[q], Y[q], Z[q], v, dx, dy, dz);
+    for (int i = 0; i < t.nb; ++i) {
+      t.phi[size_t(q) * t.nb + i] = v[i];
+      t.dphi[(size_t(0) * qn + q) * t.nb + i] = dx[i];
+      t.dphi[(size_t(1) * qn + q) * t.nb + i] = dy[i];
+      t.dphi[(size_t(2) * qn + q) * t.nb + i] = dz[i];
+    }
+  }
+}
+
+void build_element_tables(int dim, int elem, int qn, RefTables& t) {
+  if (elem == 11 || elem == 12) build_pk_tables(elem, qn, t);
+  else build_qk_tables(dim, elem, qn, t);
+}
+
 // -------------------------------------------------------------- kernels ----
 struct CdCoef {
   double eps, b0, b1, b2, c, fconst;
@@ -143,10 +180,19 @@ __device__ __forceinline__ double poly_rhs(const CdCoef& k, int dim, const doubl
   return f;
 }
 
-// affine map of cell `cell`: origin and Jacobian columns (QuadAffin/HexaAffin)
-template <int DIM>
+// affine map of cell `cell`: origin and Jacobian columns (QuadAffin/HexaAffin;
+// TetraAffin, src/FE/TetraAffin.C: x = v0 + [v1-v0, v2-v0, v3-v0] xi on the
+// unit simplex, when NV = 4 in 3D)
+template <int DIM, int NV = DIM == 2 ? 4 : 8>
 __device__ __forceinline__ void affine_map(const double* __restrict__ v, double* x0, double J[3][3]) {
-  if (DIM == 2) {
+  if (DIM == 3 && NV == 4) {
+    for (int d = 0; d < 3; ++d) {
+      x0[d] = v[d];
+      J[d][0] = v[3 + d] - v[d];
+      J[d][1] = v[6 + d] - v[d];
+      J[d][2] = v[9 + d] - v[d];
+    }
+  } else if (DIM == 2) {
     // vertices 0,1,3: xc0 = (x1+x3)/2, xc1 = (x1-x0)/2, xc2 = (x3-x0)/2
     for (int d = 0; d < 2; ++d) {
       x0[d] = (v[2 + d] + v[6 + d]) * 0.5;
@@ -221,12 +267,11 @@ __device__ __forceinline__ double rhs_value_pi(const CdCoef& k, int dim, const d
 // One group of TPC threads per cell, CPB cells per block. Shared memory per
 // cell: A[q][i][4] = Mult_q (eps dphi_i, phi_i), B[q][j][4] = (dphi_j, b.dphi_j + c phi_j);
 // K_ij = sum_q sum_d A[q][i][d] B[q][j][d].
-template <int DIM, int NB, int NQ, int CPB>
+template <int DIM, int NB, int NQ, int CPB, int NV = DIM == 2 ? 4 : 8>
 __global__ void __launch_bounds__(256) k_elem_cd(int n_cells, const double* __restrict__ verts,
                                                  const double* __restrict__ ref, CdCoef co,
                                                  double* __restrict__ K, double* __restrict__ F) {
   extern __shared__ double smem[];
-  constexpr int NV = DIM == 2 ? 4 : 8;
   constexpr int TPC = 256 / CPB;
   const int slot = threadIdx.x / TPC;
   const int t = threadIdx.x % TPC;
@@ -240,7 +285,7 @@ __global__ void __launch_bounds__(256) k_elem_cd(int n_cells, const double* __re
   const double* xi = w + NQ;
   const bool valid = cell < n_cells;
   double x0[3] = {0, 0, 0}, J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-  if (valid) affine_map<DIM>(verts + (size_t)cell * NV * DIM, x0, J);
+  if (valid) affine_map<DIM, NV>(verts + (size_t)cell * NV * DIM, x0, J);
   // inverse transpose and |det J|
   double G[3][3], det;
   if (DIM == 2) {
@@ -328,12 +373,11 @@ __global__ void __launch_bounds__(256) k_elem_cd(int n_cells, const double* __re
 // computed once per element type). This is the same quadrature applied in a
 // different summation order: NT FMAs per entry instead of 4 per quadrature
 // point. The right-hand side keeps the per-point loop (f varies in the cell).
-template <int DIM, int NB, int NQ, int CHUNK>
+template <int DIM, int NB, int NQ, int CHUNK, int NV = DIM == 2 ? 4 : 8>
 __global__ void __launch_bounds__(256) k_elem_cd_tensor(int n_cells, const double* __restrict__ verts,
                                                         const double* __restrict__ ref,
                                                         const double* __restrict__ T, CdCoef co,
                                                         double* __restrict__ K, double* __restrict__ F) {
-  constexpr int NV = DIM == 2 ? 4 : 8;
   constexpr int NT = DIM * (DIM + 1) / 2 + DIM + 1;
   __shared__ double coef[CHUNK][NT];
   __shared__ double fq[CHUNK][NQ];
@@ -347,7 +391,7 @@ __global__ void __launch_bounds__(256) k_elem_cd_tensor(int n_cells, const doubl
   double x0[3] = {0, 0, 0}, J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
   // per-cell coefficients (one thread per cell)
   if (t < nc) {
-    affine_map<DIM>(verts + (size_t)(c0 + t) * NV * DIM, x0, J);
+    affine_map<DIM, NV>(verts + (size_t)(c0 + t) * NV * DIM, x0, J);
     double G[3][3] = {{0}}, det;
     if (DIM == 2) {
       det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
@@ -451,12 +495,12 @@ void build_ref_tensors(const RefTables& t, std::vector<double>& out) {
     }
 }
 
-template <int DIM, int NB, int NQ>
+template <int DIM, int NB, int NQ, int NV = DIM == 2 ? 4 : 8>
 static void launch_elem_tensor(pm_ctx* c, int n_cells, const double* verts, const double* ref,
                                const double* T, const CdCoef& co, double* K, double* F) {
   constexpr int CHUNK = 64;
   const int grid = (n_cells + CHUNK - 1) / CHUNK;
-  k_elem_cd_tensor<DIM, NB, NQ, CHUNK><<<grid, 256, 0, c->stream>>>(n_cells, verts, ref, T, co, K, F);
+  k_elem_cd_tensor<DIM, NB, NQ, CHUNK, NV><<<grid, 256, 0, c->stream>>>(n_cells, verts, ref, T, co, K, F);
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
 }
@@ -476,11 +520,11 @@ __global__ void k_set_unit(int n, const int* __restrict__ pos, double* __restric
   if (i < n) vals[pos[i]] = 1.0;
 }
 
-template <int DIM, int NB, int NQ, int CPB>
+template <int DIM, int NB, int NQ, int CPB, int NV = DIM == 2 ? 4 : 8>
 static void launch_elem(pm_ctx* c, int n_cells, const double* verts, const double* ref,
                         const CdCoef& co, double* K, double* F) {
   const size_t sm = size_t(CPB) * (2 * NQ * NB * 4 + NQ) * sizeof(double);
-  auto kern = k_elem_cd<DIM, NB, NQ, CPB>;
+  auto kern = k_elem_cd<DIM, NB, NQ, CPB, NV>;
   if (sm > 48 * 1024) PM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
   const int grid = (n_cells + CPB - 1) / CPB;
   kern<<<grid, 256, sm, c->stream>>>(n_cells, verts, ref, co, K, F);
@@ -625,19 +669,18 @@ void launch_neumann_values(pm_ctx* c, const DevAssemblyLevel& L, const pm_cd_coe
 // CELL_MEASURE 0: hK = cell diameter). One thread per cell; each block sums
 // its cells by a fixed tree into one partial, a second kernel sums the
 // partials in a fixed order: the result does not depend on scheduling.
-template <int DIM, int NB, int NQ>
+template <int DIM, int NB, int NQ, int NV = DIM == 2 ? 4 : 8>
 __global__ void __launch_bounds__(128) k_cd_errors(int n_cells, const double* __restrict__ verts,
                                                    const int* __restrict__ dofmap, const double* __restrict__ u,
                                                    const double* __restrict__ ref, CdCoef co,
                                                    double* __restrict__ partial) {
-  constexpr int NV = DIM == 2 ? 4 : 8;
   __shared__ double red[4][128];
   const int cell = blockIdx.x * 128 + threadIdx.x;
   double loc[4] = {0.0, 0.0, 0.0, 0.0};
   if (cell < n_cells) {
     const double* v = verts + size_t(cell) * NV * DIM;
     double x0[3] = {0, 0, 0}, J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    affine_map<DIM>(v, x0, J);
+    affine_map<DIM, NV>(v, x0, J);
     double G[3][3] = {{0}}, det;
     if (DIM == 2) {
       det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
@@ -758,6 +801,10 @@ void launch_cd_errors(pm_ctx* c, int dim, int k, int qn, int n_cells, const doub
   else if (dim == 3 && k == 1 && qn == 2) k_cd_errors<3, 8, 8><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
   else if (dim == 3 && k == 2 && qn == 4) k_cd_errors<3, 27, 64><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
   else if (dim == 3 && k == 2 && qn == 3) k_cd_errors<3, 27, 27><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (k == 11 && qn == 11) k_cd_errors<3, 4, 11, 4><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (k == 11 && qn == 15) k_cd_errors<3, 4, 15, 4><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (k == 12 && qn == 11) k_cd_errors<3, 10, 11, 4><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
+  else if (k == 12 && qn == 15) k_cd_errors<3, 10, 15, 4><<<grid, 128, 0, c->stream>>>(n_cells, verts, dofmap, u, rt.data.p, co, partial);
   else throw Error(PM_E_UNSUPPORTED, "error functional: element / quadrature combination not compiled");
   PM_CHECK_LAUNCH();
   k_cd_errors_finish<<<1, 256, 0, c->stream>>>(grid, partial, out);
@@ -816,6 +863,10 @@ void launch_cd_elements(pm_ctx* c, const DevAssemblyLevel& L, int dim, int k, in
     else if (dim == 3 && k == 1 && qn == 3) launch_elem_tensor<3, 8, 27>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
     else if (dim == 3 && k == 2 && qn == 3) launch_elem_tensor<3, 27, 27>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
     else if (dim == 3 && k == 2 && qn == 4) launch_elem_tensor<3, 27, 64>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (k == 11 && qn == 11) launch_elem_tensor<3, 4, 11, 4>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (k == 11 && qn == 15) launch_elem_tensor<3, 4, 15, 4>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (k == 12 && qn == 11) launch_elem_tensor<3, 10, 11, 4>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
+    else if (k == 12 && qn == 15) launch_elem_tensor<3, 10, 15, 4>(c, L.n_cells, L.verts.p, rt.data.p, T, co, K, F);
     else throw Error(PM_E_UNSUPPORTED, "element / quadrature combination not compiled");
   } else if (dim == 2 && k == 1 && qn == 3) launch_elem<2, 4, 9, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 2 && k == 1 && qn == 2) launch_elem<2, 4, 4, 16>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
@@ -825,6 +876,10 @@ void launch_cd_elements(pm_ctx* c, const DevAssemblyLevel& L, int dim, int k, in
   else if (dim == 3 && k == 1 && qn == 3) launch_elem<3, 8, 27, 2>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 3 && k == 2 && qn == 3) launch_elem<3, 27, 27, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else if (dim == 3 && k == 2 && qn == 4) launch_elem<3, 27, 64, 1>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (k == 11 && qn == 11) launch_elem<3, 4, 11, 16, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (k == 11 && qn == 15) launch_elem<3, 4, 15, 16, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (k == 12 && qn == 11) launch_elem<3, 10, 11, 4, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
+  else if (k == 12 && qn == 15) launch_elem<3, 10, 15, 4, 4>(c, L.n_cells, L.verts.p, rt.data.p, co, K, F);
   else throw Error(PM_E_UNSUPPORTED, "element / quadrature combination not compiled");
 }
 

@@ -13,6 +13,11 @@ struct RefTables {
   std::vector<double> w, xi, phi, dphi;
 };
 void build_qk_tables(int dim, int k, int qn, RefTables& t);
+// P1 (elem 11) / P2 (elem 12) on a tetrahedral rule of qn = 11 or 15 points
+void build_pk_tables(int elem, int qn, RefTables& t);
+// the tables of `elem` (Qk: k = 1, 2 on qn Gauss points per direction; Pk on
+// tetrahedra: elem 11, 12 on a rule of qn points)
+void build_element_tables(int dim, int elem, int qn, RefTables& t);
 
 struct DevRefTables {
   int nb = 0, nq = 0, nt = 0;

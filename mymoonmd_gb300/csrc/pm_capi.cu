@@ -712,9 +712,13 @@ int pm_disc_prolongation(const pm_disc* d, int level, int* rp, int* ci, double* 
 // --------------------------------------------------------------- assembly --
 static int default_quad_points(const Disc& D) {
   // ParMooN picks degree N_terms * polynomial degree (FEDatabase3D.C:1153-1207);
-  // for convection-diffusion (N_terms = 3): Q1 -> Gauss3, Q2 -> Gauss4 in 3D
+  // for convection-diffusion (N_terms = 3): Q1 -> Gauss3, Q2 -> Gauss4; on
+  // tetrahedra P1 (degree 3) -> P4Tetra (11 points), P2 (degree 6) ->
+  // P5Tetra (15 points)
+  if (D.elem == pmsetup::EL_P1) return 11;
+  if (D.elem == pmsetup::EL_P2) return 15;
   if (D.elem == 1) return 3;
-  return D.dim() == 3 ? 4 : 4;
+  return 4;
 }
 
 int pm_assemble_cd(pm_ctx* c, const pm_disc* d, int level, const pm_cd_coeffs* cf, int qn,
@@ -727,7 +731,7 @@ int pm_assemble_cd(pm_ctx* c, const pm_disc* d, int level, const pm_cd_coeffs* c
     throw Error(PM_E_INVALID, "matrix does not have the level's CSR pattern");
   if (qn == 0) qn = default_quad_points(*d->d);
   RefTables t;
-  build_qk_tables(d->d->dim(), d->d->elem, qn, t);
+  build_element_tables(d->d->dim(), d->d->elem, qn, t);
   DevRefTables rt;
   rt.upload(c, t);
   DevAssemblyLevel dl;
@@ -756,7 +760,7 @@ int pm_problem_create_cd(pm_ctx* c, const pm_disc* d, const pm_cd_coeffs* cf, in
     const Disc& D = *d->d;
     p->qn = qn ? qn : default_quad_points(D);
     RefTables t;
-    build_qk_tables(D.dim(), D.elem, p->qn, t);
+    build_element_tables(D.dim(), D.elem, p->qn, t);
     p->ref.upload(c, t);
     size_t kmax = 0, fmax = 0;
     const int nl = int(D.levels.size());
@@ -1041,7 +1045,7 @@ int pm_problem_errors(pm_problem* p, double* errors) {
   const int qn = p->qn;
   if (p->err_qn != qn) {
     RefTables t;
-    build_qk_tables(D.dim(), D.elem, qn, t);
+    build_element_tables(D.dim(), D.elem, qn, t);
     p->err_ref.upload(c, t);
     p->err_dofmap.upload(top.space.dofmap, c->stream);
     p->err_out.alloc(4);

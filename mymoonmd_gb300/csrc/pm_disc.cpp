@@ -306,8 +306,11 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
     throw std::invalid_argument("Neumann sides (a mask of 4 bits) apply to convection-diffusion on the unit square");
   D->neumann_sides = neumann_sides;
   if (kind == KIND_CD) {
-    if (geometry == GEO_CUBE_TETRA) throw std::invalid_argument("convection-diffusion uses quadrilaterals or hexahedra");
-    if (elem != EL_Q1 && elem != EL_Q2) throw std::invalid_argument("convection-diffusion elements are Q1 or Q2");
+    const bool tet = geometry == GEO_CUBE_TETRA;
+    if (!tet && elem != EL_Q1 && elem != EL_Q2)
+      throw std::invalid_argument("convection-diffusion on quadrilaterals or hexahedra uses Q1 or Q2");
+    if (tet && elem != EL_P1 && elem != EL_P2)
+      throw std::invalid_argument("convection-diffusion on tetrahedra uses P1 or P2");
   } else {
     if (geometry != GEO_CUBE_TETRA) throw std::invalid_argument("Stokes P2/P1 uses the tetrahedral unit cube");
     D->elem = EL_P2;

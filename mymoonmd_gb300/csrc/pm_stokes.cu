@@ -17,54 +17,12 @@
 #include <vector>
 
 #include "pm_stokes.h"
+#include "pm_tetra.h"
 
 namespace pm {
 
 // ------------------------------------------------------------- tables ------
-static const double kP4w[11] = {-.0131555555555555555555555555556, .00762222222222222222222222222222,
-                                .00762222222222222222222222222222, .00762222222222222222222222222222,
-                                .00762222222222222222222222222222, .0248888888888888888888888888889,
-                                .0248888888888888888888888888889, .0248888888888888888888888888889,
-                                .0248888888888888888888888888889, .0248888888888888888888888888889,
-                                .0248888888888888888888888888889};
-static const double kP4x[11] = {.25, .0714285714285714285714285714286, .785714285714285714285714285714,
-                                .0714285714285714285714285714286, .0714285714285714285714285714286,
-                                .399403576166799204996102147462, .399403576166799204996102147462,
-                                .100596423833200795003897852538, .100596423833200795003897852538,
-                                .100596423833200795003897852538, .399403576166799204996102147462};
-static const double kP4y[11] = {.25, .0714285714285714285714285714286, .0714285714285714285714285714286,
-                                .785714285714285714285714285714, .0714285714285714285714285714286,
-                                .399403576166799204996102147462, .100596423833200795003897852538,
-                                .399403576166799204996102147462, .100596423833200795003897852538,
-                                .399403576166799204996102147462, .100596423833200795003897852538};
-static const double kP4z[11] = {.25, .0714285714285714285714285714286, .0714285714285714285714285714286,
-                                .0714285714285714285714285714286, .785714285714285714285714285714,
-                                .100596423833200795003897852538, .399403576166799204996102147462,
-                                .399403576166799204996102147462, .399403576166799204996102147462,
-                                .100596423833200795003897852538, .100596423833200795003897852538};
-
-// C_T_P2_3D values and derivatives (include/FE3D/BF_C_T_P2_3D.h)
-static void p2_eval(double x, double y, double z, double* v, double* dx, double* dy, double* dz) {
-  v[0] = 1 - 3 * x - 3 * y - 3 * z + 2 * x * x + 4 * x * y + 4 * x * z + 2 * y * y + 4 * y * z + 2 * z * z;
-  v[1] = 4 * x - 4 * x * x - 4 * x * y - 4 * x * z;
-  v[2] = -x + 2 * x * x;
-  v[3] = 4 * y - 4 * x * y - 4 * y * y - 4 * y * z;
-  v[4] = 4 * x * y;
-  v[5] = -y + 2 * y * y;
-  v[6] = 4 * z - 4 * x * z - 4 * y * z - 4 * z * z;
-  v[7] = 4 * x * z;
-  v[8] = 4 * y * z;
-  v[9] = -z + 2 * z * z;
-  const double g0 = -3 + 4 * x + 4 * y + 4 * z;
-  const double dxs[10] = {g0, 4 - 8 * x - 4 * y - 4 * z, -1 + 4 * x, -4 * y, 4 * y, 0, -4 * z, 4 * z, 0, 0};
-  const double dys[10] = {g0, -4 * x, 0, 4 - 4 * x - 8 * y - 4 * z, 4 * x, -1 + 4 * y, -4 * z, 0, 4 * z, 0};
-  const double dzs[10] = {g0, -4 * x, 0, -4 * y, 0, 0, 4 - 4 * x - 4 * y - 8 * z, 4 * x, 4 * y, -1 + 4 * z};
-  for (int i = 0; i < 10; ++i) {
-    dx[i] = dxs[i];
-    dy[i] = dys[i];
-    dz[i] = dzs[i];
-  }
-}
+// the P4Tetra rule and the P2 basis: pm_tetra.h
 
 // layout: S[6][100] | D[3][40] | phi2[11][10] | w[11] | xi[11][3]
 static constexpr int kOffS = 0, kOffD = 600, kOffPhi = 720, kOffW = 830, kOffXi = 841, kTabSize = 874;

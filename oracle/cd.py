@@ -173,6 +173,52 @@ def _qk_values(k: int, d: int, xi: np.ndarray):
     return np.stack(vals, axis=1), np.stack([np.stack(dd, axis=1) for dd in ders])
 
 
+# the reference's tetrahedral rules (src/QuadFormulas/QuadFormulaTetra.C,
+# P4Exact / P5Exact), points in its order, weights summing to 1/6
+def _tet_rule(n: int):
+    """(x, y, z, w) of the P4Tetra (11 points) or P5Tetra (15 points) rule"""
+    if n == 11:
+        a, b = 0.399403576166799204996102147462, 0.100596423833200795003897852538
+        t1, t2 = 0.0714285714285714285714285714286, 0.785714285714285714285714285714
+        x = [.25, t1, t2, t1, t1, a, a, b, b, b, a]
+        y = [.25, t1, t1, t2, t1, a, b, a, b, a, b]
+        z = [.25, t1, t1, t1, t2, b, a, a, a, b, b]
+        w = [-.0131555555555555555555555555556] + [.00762222222222222222222222222222] * 4 + \
+            [.0248888888888888888888888888889] * 6
+    elif n == 15:
+        a, b = 0.066550153573664298239880464226303, 0.43344984642633570176011953577370
+        e, g = 1 / 11, 8 / 11
+        x = [1 / 3, 1 / 3, 0, 1 / 3, .25, e, e, g, e, a, b, b, a, a, b]
+        y = [1 / 3, 0, 1 / 3, 1 / 3, .25, e, g, e, e, b, a, b, a, b, a]
+        z = [0, 1 / 3, 1 / 3, 1 / 3, .25, g, e, e, e, b, b, a, b, a, a]
+        w = [0.0060267857142857142857142857142857] * 4 + [0.030283678097089175806376972557730] + \
+            [0.011645249086028969410893609144338] * 4 + [0.010949141561386459345643019112407] * 6
+    else:
+        raise ValueError("tetrahedral rules with 11 or 15 points")
+    return np.array(x), np.array(y), np.array(z), np.array(w)
+
+
+def _pk_values(elem: int, x, y, z):
+    """P1 (11) / P2 (12) basis values (nq, nb) and reference derivatives
+    (3, nq, nb) in local DOF order (C_T_P1_3D, C_T_P2_3D)"""
+    one, zero = np.ones_like(x), np.zeros_like(x)
+    if elem == 11:
+        v = [1 - x - y - z, x, y, z]
+        dx = [-one, one, zero, zero]
+        dy = [-one, zero, one, zero]
+        dz = [-one, zero, zero, one]
+    else:
+        g0 = -3 + 4 * x + 4 * y + 4 * z
+        v = [1 - 3 * x - 3 * y - 3 * z + 2 * x * x + 4 * x * y + 4 * x * z + 2 * y * y + 4 * y * z + 2 * z * z,
+             4 * x - 4 * x * x - 4 * x * y - 4 * x * z, -x + 2 * x * x, 4 * y - 4 * x * y - 4 * y * y - 4 * y * z,
+             4 * x * y, -y + 2 * y * y, 4 * z - 4 * x * z - 4 * y * z - 4 * z * z, 4 * x * z, 4 * y * z,
+             -z + 2 * z * z]
+        dx = [g0, 4 - 8 * x - 4 * y - 4 * z, -1 + 4 * x, -4 * y, 4 * y, zero, -4 * z, 4 * z, zero, zero]
+        dy = [g0, -4 * x, zero, 4 - 4 * x - 8 * y - 4 * z, 4 * x, -1 + 4 * y, -4 * z, zero, 4 * z, zero]
+        dz = [g0, -4 * x, zero, -4 * y, zero, zero, 4 - 4 * x - 4 * y - 8 * z, 4 * x, 4 * y, -1 + 4 * z]
+    return np.stack(v, axis=1), np.stack([np.stack(dx, axis=1), np.stack(dy, axis=1), np.stack(dz, axis=1)])
+
+
 class OracleCD:
     """ConvectionDiffusion<d> restated on the CPU over a multigrid hierarchy."""
 
@@ -214,10 +260,68 @@ class OracleCD:
     def finest(self):
         return self.levels[-1]
 
+    def _assemble_tetra(self, lv):
+        """ConvectionDiffusion's Galerkin element loop on tetrahedra (P1 / P2 on
+        the P4Tetra / P5Tetra rule, src/AssembleRoutines/Assemble3D.C:228-470 with
+        BilinearAssembleGalerkin, src/AssembleRoutines/ConvDiff.C:1794-1856, on
+        TetraAffin): per cell K_ij += w |det J| (eps grad phi_i . grad phi_j
+        + (b . grad phi_j) phi_i + c phi_j phi_i), F_i += w |det J| f phi_i,
+        added to the active rows; non-active rows keep their unit diagonal and
+        the Dirichlet value"""
+        X, Y, Z, W = _tet_rule(self.qn)
+        phi, dphi = _pk_values(self.elem, X, Y, Z)            # (nq, nb), (3, nq, nb)
+        v = lv.verts                                           # (cells, 4, 3)
+        J = np.stack([v[:, 1] - v[:, 0], v[:, 2] - v[:, 0], v[:, 3] - v[:, 0]], axis=2)
+        det = np.linalg.det(J)
+        G = np.linalg.inv(J).transpose(0, 2, 1)
+        grad = np.einsum("cda,aqi->cqid", G, dphi)             # (cells, nq, nb, 3)
+        w = W[None, :] * np.abs(det)[:, None]                  # (cells, nq)
+        b = self.b
+        conv = grad @ b                                        # (cells, nq, nb)
+        K = (self.eps * np.einsum("cq,cqid,cqjd->cij", w, grad, grad)
+             + np.einsum("cq,qi,cqj->cij", w, phi, conv)
+             + self.c * np.einsum("cq,qi,qj->cij", w, phi, phi))
+        xq = v[:, 0][:, None, :] + np.einsum("cda,qa->cqd", J, np.stack([X, Y, Z], axis=1))
+        ex = self.exact_grad(xq.reshape(-1, 3))
+        if self.poly is not None:
+            pp, ps = np.ascontiguousarray(self.poly[:10]), np.ascontiguousarray(self.poly[10:])
+            f = np.array([lib().orc_poly_rhs(3, _p(np.ascontiguousarray(x)), self.eps, _p(self.b), self.c,
+                                             _p(pp), _p(ps))
+                          for x in xq.reshape(-1, 3)])
+        elif self.manufactured:
+            s_ = np.sin(np.pi * xq.reshape(-1, 3))
+            lap = -3 * np.pi ** 2 * np.prod(s_, axis=1)
+            f = -self.eps * lap + ex[:, 1:] @ b + self.c * ex[:, 0]
+        else:
+            f = np.full(xq.shape[0] * xq.shape[1], self.f_const)
+        F = np.einsum("cq,cq,qi->ci", w, f.reshape(xq.shape[0], -1), phi)
+        vals = np.zeros(lv.cols.size)
+        rhs = np.zeros(lv.n_dofs)
+        dm = lv.dofmap
+        rows = np.repeat(dm, dm.shape[1], axis=1).ravel()
+        cols = np.tile(dm, (1, dm.shape[1])).ravel()
+        act = rows < lv.n_active
+        key_pat = np.repeat(np.arange(lv.n_dofs, dtype=np.int64), np.diff(lv.row_ptr)) * lv.n_dofs + lv.cols
+        pos = np.searchsorted(key_pat, rows[act].astype(np.int64) * lv.n_dofs + cols[act])
+        np.add.at(vals, pos, K.ravel()[act])
+        ra = dm.ravel() < lv.n_active
+        np.add.at(rhs, dm.ravel()[ra], F.ravel()[ra])
+        for i in range(lv.n_active, lv.n_dofs):
+            vals[lv.row_ptr[i]] = 1.0
+        return vals, rhs
+
     def assemble(self) -> None:
         L = lib()
         self.vals, self.rhs = [], []
         for lv in self.levels:
+            if self.geometry == refsetup.GEO_CUBE_TETRA:
+                vals, rhs = self._assemble_tetra(lv)
+                if self.poly is not None:
+                    for i in range(lv.n_active, lv.n_dofs):
+                        rhs[i] = self.exact(lv.node_coords[i])
+                self.vals.append(vals)
+                self.rhs.append(rhs)
+                continue
             vals = np.zeros(lv.cols.size, dtype=np.float64)
             rhs = np.zeros(lv.n_dofs, dtype=np.float64)
             verts = np.ascontiguousarray(lv.verts, dtype=np.float64)

@@ -16,6 +16,8 @@
 //   QUAD_LINEAR 1 sets INTERNAL_PROBLEM_LINEAR (quadrature degree 2 x the
 //   element degree, e.g. Gauss3 for Q2), 0 keeps the default (3 x);
 //   SOLVER fgmres_mg | direct | none (assemble only).
+//   optional GEOMETRY (after EXAMPLE; 3D only): tetra for Default_UnitCube_Tetra
+//   (P1 / P2 for ANSATZ_ORDER 1 / 2), hexa (default) for Default_UnitCube_Hexa.
 //   optional EXAMPLE: the reference's own example of that number
 //   (Example_CD2D/3D from the database, e.g. 0 = SineLaplace in 2D, whose
 //   boundary part 1 is a Neumann boundary) instead of the sine problem above;
@@ -135,6 +137,7 @@ int main(int argc, char** argv) {
   const int restart = std::atoi(argv[11]);
   const double reduction = std::atof(argv[12]);
   const int builtin_example = argc > 13 ? std::atoi(argv[13]) : -1;
+  const std::string geometry = argc > 14 ? argv[14] : "hexa";
 
   Output::setVerbosity(1);
   TDatabase database;
@@ -162,7 +165,7 @@ int main(int argc, char** argv) {
   db.add("geo_file", "UnitSquare", "");
 #else
   db.add("boundary_file", "Default_UnitCube", "");
-  db.add("geo_file", "Default_UnitCube_Hexa", "");
+  db.add("geo_file", geometry == "tetra" ? "Default_UnitCube_Tetra" : "Default_UnitCube_Hexa", "");
 #endif
   db.add("refinement_n_initial_steps", n_refine, "");
   if (solver == "direct" || solver == "none") {

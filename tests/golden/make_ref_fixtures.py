@@ -49,7 +49,7 @@ SAMPLES = 4096
 
 # name: (dim, n_refine, element order, levels, eps, b, quadrature degree 2 x
 #        order (1) or the default 3 x order (0), restart, residual reduction, full arrays
-#        [, the reference's example number])
+#        [, the reference's example number (-1: the sine problem) [, "tetra"]])
 CASES = {
     # 3D Q2 32^3 convection-diffusion, 4 levels, FGMRES(30), 1e-8, Gauss 3x3x3
     "cd3d_q2_32": (3, 5, 2, 4, 1e-2, (1.0, 0.5, 0.25), 1, 30, 1e-8, False),
@@ -66,6 +66,10 @@ CASES = {
     "sine_q2_4": (2, 2, 2, 2, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-12, True, 0),
     "sine_q1_64": (2, 6, 1, 4, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-10, False, 0),
     "sine_q2_32": (2, 5, 2, 3, 1.0, (0.0, 0.0, 0.0), 0, 20, 1e-10, False, 0),
+    # P1 / P2 on Default_UnitCube_Tetra (the tetrahedral half of test/cd3d_solvers_test.c++)
+    "tet_p1_8": (3, 3, 1, 3, 0.1, (1.0, 0.5, 0.25), 0, 30, 1e-10, True, -1, "tetra"),
+    "tet_p2_4": (3, 2, 2, 2, 0.1, (1.0, 0.5, 0.25), 0, 30, 1e-10, True, -1, "tetra"),
+    "tet_p2_16": (3, 4, 2, 3, 0.05, (1.0, 0.5, 0.25), 0, 30, 1e-10, False, -1, "tetra"),
 }
 
 
@@ -92,17 +96,21 @@ def run_case(name: str) -> None:
     import build_ref
     dim, nref, order, nlev, eps, b, quad_linear, restart, reduction, full = CASES[name][:10]
     example = CASES[name][10] if len(CASES[name]) > 10 else -1
+    geometry = CASES[name][11] if len(CASES[name]) > 11 else ("square" if dim == 2 else "hexa")
     exe = build_ref.link_program(str(dim), build_ref.HERE / "ref_cd.C", build_ref.OUT / f"ref_cd{dim}d")
     with tempfile.TemporaryDirectory() as tmp:
         cmd = [str(exe), tmp, str(nref), str(order), str(nlev), repr(eps), *map(repr, b), str(quad_linear),
-               "fgmres_mg", str(restart), repr(reduction)] + ([str(example)] if example >= 0 else [])
+               "fgmres_mg", str(restart), repr(reduction)] + ([str(example)] if example >= 0 or geometry == "tetra" else [])
+        if geometry == "tetra":
+            cmd.append("tetra")
         subprocess.run(cmd, check=True, capture_output=True)
         meta = {}
         for line in Path(tmp, "meta.txt").read_text().splitlines():
             k, v = line.split(None, 1)
             meta[k] = v
         out: dict[str, np.ndarray] = {
-            "config": np.array([dim, nref, order, nlev, quad_linear, restart], dtype=np.int64),
+            "config": np.array([dim, nref, order, nlev, quad_linear, restart,
+                                {"square": 0, "hexa": 1, "tetra": 2}[geometry]], dtype=np.int64),
             "coeffs": np.array([eps, *b, reduction], dtype=np.float64),
             "iterations": np.array(int(meta["iterations"])),
             "initial_residual": np.array(float(meta["initial_residual"])),

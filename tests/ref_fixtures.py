@@ -30,13 +30,23 @@ class RefCase:
     def __init__(self, name: str):
         self.name = name
         self.z = np.load(GOLDEN / f"ref_{name}.npz")
-        dim, nref, order, nlev, quad_linear, restart = (int(v) for v in self.z["config"])
+        cfg = [int(v) for v in self.z["config"]]
+        dim, nref, order, nlev, quad_linear, restart = cfg[:6]
         eps, b1, b2, b3, reduction = (float(v) for v in self.z["coeffs"])
         self.dim, self.n_refine, self.order, self.n_levels = dim, nref, order, nlev
         self.restart, self.reduction = restart, reduction
         self.eps, self.b = eps, (b1, b2, b3)
-        self.quad_points = _POINTS[(2 if quad_linear else 3) * order]
-        self.geometry = 0 if dim == 2 else 1  # unit square (quads) / unit cube (hexahedra)
+        # unit square (quads) / unit cube (hexahedra) / unit cube (tetrahedra)
+        self.geometry = cfg[6] if len(cfg) > 6 else (0 if dim == 2 else 1)
+        if self.geometry == 2:
+            # P1 / P2 (library elements 11 / 12); QFTetraFromDegree: degree 3 -> P4Tetra
+            # (11 points), 6 -> P5Tetra (15 points); 2 x order: P2Tetra / P4Tetra
+            self.elem = 10 + order
+            degree = (2 if quad_linear else 3) * order
+            self.quad_points = 11 if degree in (3, 4) else 15 if degree in (5, 6) else 4
+        else:
+            self.elem = order
+            self.quad_points = _POINTS[(2 if quad_linear else 3) * order]
         # the reference's own example (0 = SineLaplace, Neumann side x = 1) or -1
         self.example = int(self.z["example"]) if "example" in self.z.files else -1
         self.neumann_sides = 2 if self.example == 0 else 0

@@ -50,7 +50,7 @@ def db_for(rc: RefCase, precision: str) -> m.ParameterDatabase:
 
 
 def make(ctx, rc: RefCase, precision: str):
-    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order,
+    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.elem,
                             neumann_sides=rc.neumann_sides)
     cf = m.cd_coeffs(rc.eps, rc.b[:rc.dim], 0.0, True)
     return disc, m.ConvectionDiffusion(ctx, disc, cf, db_for(rc, precision), quad_points=rc.quad_points)
@@ -107,7 +107,7 @@ def test_gpu_mixed_form_with_the_fp64_coarse_solve(ctx, name):
     rc = RefCase(name)
     its = {}
     for coarse in ("fp32", "fp64"):
-        disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order)
+        disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.elem)
         db = db_for(rc, "mixed")
         db["gpu_mixed_coarse"] = coarse
         prob = m.ConvectionDiffusion(ctx, disc, m.cd_coeffs(rc.eps, rc.b[:rc.dim], 0.0, True), db,

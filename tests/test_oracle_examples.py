@@ -31,9 +31,16 @@ def reference_rhs(example, x, y, z):
     return -1.0 * 2 + 4 * 2 * x + 3 * z + 2 * y + 1 * (x * x + y * z)
 
 
-def oracle_example(example, n_levels=2):
+def oracle_example(example, n_levels=2, tetra=False):
+    """hexahedra (Q1 / Q2, Gauss3) or, with tetra, the tetrahedral unit cube
+    Default_UnitCube_Tetra (P1 / P2 on the reference's default rules P4Tetra /
+    P5Tetra), two refinements"""
     elem, eps, b, c, poly = EXAMPLES[example]
-    o = ocd.OracleCD(1, 1, 2, n_levels, elem, eps=eps, b=b, c=c, quad_points=3, poly=poly)
+    if tetra:
+        o = ocd.OracleCD(2, 1, 2, n_levels, 10 + elem, eps=eps, b=b, c=c, quad_points=11 if elem == 1 else 15,
+                         poly=poly)
+    else:
+        o = ocd.OracleCD(1, 1, 2, n_levels, elem, eps=eps, b=b, c=c, quad_points=3, poly=poly)
     o.assemble()
     return o
 
@@ -53,9 +60,12 @@ def test_polynomial_rhs_equals_the_examples_formula(example):
         assert abs(f - reference_rhs(example, *x)) <= 1e-14 * max(1.0, abs(f))
 
 
+@pytest.mark.parametrize("tetra", [False, True])
 @pytest.mark.parametrize("example", [-1, -2, -3])
-def test_cd3d_solvers_polynomial_examples_are_solved_exactly(example):
-    o = oracle_example(example)
+def test_cd3d_solvers_polynomial_examples_are_solved_exactly(example, tetra):
+    """both halves of test/cd3d_solvers_test.c++: hexahedra (Q1, Q1, Q2) and
+    tetrahedra (P1, P1, P2)"""
+    o = oracle_example(example, tetra=tetra)
     lv = o.finest
     o.build_mg(3, 3, 0.8, 0.8, "W", smoother="sor", sor_omega=1.5)
     sol, it, res, hist, st = o.solve("fgmres", 1e-15, 0.0, 100, 0, 20)

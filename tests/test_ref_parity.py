@@ -34,7 +34,7 @@ from ref_fixtures import RefCase, StokesRefCase, digest, names, stokes_names
 @pytest.mark.parametrize("name", names())
 def test_setup_is_bit_identical_to_the_reference(name):
     rc = RefCase(name)
-    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.order,
+    disc = m.Discretization(rc.geometry, 1, rc.n_refine, rc.n_levels, m.KIND_CD, rc.elem,
                             neumann_sides=rc.neumann_sides)
     try:
         for l in range(rc.n_levels):
@@ -53,7 +53,7 @@ def test_setup_is_bit_identical_to_the_reference(name):
 @pytest.mark.parametrize("name", [n for n in names() if n != "cd3d_q2_32"])
 def test_oracle_reproduces_the_reference_assembly_and_solve(name):
     rc = RefCase(name)
-    ora = ocd.OracleCD(rc.geometry, 1, rc.n_refine, rc.n_levels, rc.order, rc.eps, rc.b[:rc.dim], 0.0,
+    ora = ocd.OracleCD(rc.geometry, 1, rc.n_refine, rc.n_levels, rc.elem, rc.eps, rc.b[:rc.dim], 0.0,
                        rc.quad_points, neumann_sides=rc.neumann_sides)
     ora.assemble()
     for l in range(rc.n_levels):
