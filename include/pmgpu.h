@@ -334,16 +334,57 @@ void pm_problem_destroy(pm_problem* p);
  * (multigrid_smoother cell_vanka | cell_vanka_jacobi, VankaSmoother.C). */
 int pm_problem_create_stokes(pm_ctx* ctx, const pm_disc* d, double nu, const char* params,
                              pm_problem** out);
-/* ConvectionDiffusion::assemble (src/System/ConvectionDiffusion.C:174) */
+/* The Navier-Stokes problem (NavierStokes<3> with problem_type 5, the
+ * convective form, NSTYPE 4, LAPLACETYPE 0, Galerkin) is the same handle,
+ * created with "problem_type: 5" and "example: -3" in params (the reference's
+ * example -3, include/Examples/NSE_3D/test_u_2_p_1.h, whose body force holds
+ * the convective term; nu = 1 / reynolds_number). Its assembly uses the
+ * P5Tetra rule (degree 3 x 2 for nonlinear problems, FEDatabase3D.C:1153-1219)
+ * and adds the convective term (u . grad u_j, phi_i) of each level's current
+ * velocity to A11, A22 and A33 (NSNonlinearTerm_convective,
+ * src/AssembleRoutinesSaddle/NSE_local_assembling_routines.C). */
+/* ConvectionDiffusion::assemble (src/System/ConvectionDiffusion.C:174);
+ * NavierStokes::assemble_linear_terms (src/System/NavierStokes.C:407) for a
+ * Stokes / Navier-Stokes problem */
 int pm_problem_assemble(pm_problem* p);
+/* NavierStokes::assemble_nonlinear_term (src/System/NavierStokes.C:573): the
+ * finest velocity restricted to every coarser level
+ * (GridTransfer::RestrictFunctionRepeatedly, src/Multigrid/GridTransfer.C:1506;
+ * per coarse cell the L2 projection of its children's values, averaged over
+ * the cells of each DOF) and the velocity blocks of every level reassembled
+ * with the convective term of that level's velocity. Navier-Stokes only. */
+int pm_problem_assemble_nonlinear(pm_problem* p);
+/* NavierStokes::compute_residuals (src/System/NavierStokes.C:820): d = rhs -
+ * A x on the finest level, the pressure part of d projected into L2_0; out[0]
+ * = |d_u1| + |d_u2| + |d_u3| (impuls: BlockVector::norm over blocks sums the
+ * blocks' 2-norms, src/Matrix/BlockVector.C:293), out[1] = |d_p| (mass),
+ * out[2] = the full residual sqrt(out[0]^2 + out[1]^2). Stokes or
+ * Navier-Stokes problems. */
+int pm_problem_residuals(pm_problem* p, double* out);
+/* The nonlinear loop of the reference's test/nse3d_solvers_test.c++:
+ * stop_it(0); then solve / assemble_nonlinear_term / stop_it(k) until stop_it
+ * (src/System/NavierStokes.C:753) says so, with the params keys
+ * nonlinloop_maxit (100), nonlinloop_minit (1), nonlinloop_epsilon (1e-10),
+ * nonlinloop_damping_factor (1.0), nonlinloop_slowfactor (1e10),
+ * nonlinloop_scale_epsilon_with_size and nonlinloop_residual_relative_to_rhs
+ * (false). Call after pm_problem_assemble. residuals (3 doubles per step,
+ * steps 0..n_steps, at most max_records steps, or NULL) receives the impuls,
+ * mass and full residual of every stop_it; n_steps the number of solves. */
+int pm_problem_solve_nonlinear(pm_problem* p, int max_records, double* residuals, int* n_steps);
 /* ConvectionDiffusion::solve (src/System/ConvectionDiffusion.C:191). Like the
- * reference, the solve starts from the current solution vector. */
+ * reference, the solve starts from the current solution vector. For a Stokes /
+ * Navier-Stokes problem NavierStokes::solve (src/System/NavierStokes.C:878):
+ * afterwards the pressure is projected into L2_0 (TFEFunction3D::
+ * project_into_L20, src/FE/FEFunction3D.C:1678). */
 int pm_problem_solve(pm_problem* p);
 /* Zero initial guess for the next request (the state after construction,
  * ConvectionDiffusion.C:73). */
 int pm_problem_reset_solution(pm_problem* p);
 int pm_problem_size(const pm_problem* p, int* n_dofs, int* n_active);
 int pm_problem_get_solution(const pm_problem* p, double* sol_host);
+/* the finest-level solution vector from host memory (an initial guess or a
+ * given velocity for the nonlinear assembly: NavierStokes::get_solution()) */
+int pm_problem_set_solution(pm_problem* p, const double* sol_host);
 int pm_problem_get_rhs(const pm_problem* p, double* rhs_host);
 int pm_problem_matrix(pm_problem* p, int level, pm_matrix** out);
 int pm_problem_solver(pm_problem* p, pm_solver** out);

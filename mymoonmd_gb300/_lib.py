@@ -137,11 +137,15 @@ _SIGS = {
     "pm_problem_size": (i32, [vp, pi32, pi32]),
     "pm_problem_get_solution": (i32, [vp, vp]),
     "pm_problem_get_rhs": (i32, [vp, vp]),
+    "pm_problem_set_solution": (i32, [vp, vp]),
     "pm_problem_matrix": (i32, [vp, i32, C.POINTER(vp)]),
     "pm_problem_solver": (i32, [vp, C.POINTER(vp)]),
     "pm_problem_solution_dev": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "pm_problem_run_host": (i32, [vp, C.POINTER(CdCoeffs), vp, vp]),
     "pm_problem_errors": (i32, [vp, vp]),
+    "pm_problem_assemble_nonlinear": (i32, [vp]),
+    "pm_problem_residuals": (i32, [vp, vp]),
+    "pm_problem_solve_nonlinear": (i32, [vp, i32, vp, pi32]),
     "pm_problem_last_info": (i32, [vp, pi32, pf64, pf64]),
     "pm_problem_solve_batched": (i32, [vp, i32, i32, pi32]),
     "pm_tcd_create": (i32, [vp, vp, C.POINTER(CdCoeffs), vp, i32, C.c_char_p, C.POINTER(vp)]),

@@ -480,6 +480,12 @@ class ConvectionDiffusion:
         check(lib.pm_problem_get_solution(self.handle, _ptr(out)), self.ctx.handle)
         return out
 
+    def set_solution(self, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.size != self.size()[0]:
+            raise ValueError("solution of the wrong length")
+        check(lib.pm_problem_set_solution(self.handle, _ptr(x)), self.ctx.handle)
+
     def rhs(self) -> np.ndarray:
         out = np.empty(self.size()[0], dtype=np.float64)
         check(lib.pm_problem_get_rhs(self.handle, _ptr(out)), self.ctx.handle)
@@ -614,9 +620,12 @@ class TimeConvectionDiffusion(ConvectionDiffusion):
         self.handle = None
 
 class StokesProblem(ConvectionDiffusion):
-    """NavierStokes<3> for the Stokes problem (P2/P1 on tetrahedra) on one GPU:
-    assemble() and solve() as NavierStokes::assemble_linear_terms / solve
-    (src/System/NavierStokes.C:407, 878). Vector layout [u1 | u2 | u3 | p]."""
+    """NavierStokes<3> (P2/P1 on tetrahedra) on one GPU: the Stokes problem, or
+    with "problem_type": 5 in the database the Navier-Stokes problem in
+    convective form (nu = 1 / Reynolds number; example -3). assemble() and
+    solve() as NavierStokes::assemble_linear_terms / solve
+    (src/System/NavierStokes.C:407, 878), the pressure of the solution projected
+    into L2_0. Vector layout [u1 | u2 | u3 | p]."""
 
     def __init__(self, ctx: Context, disc: Discretization, nu: float, db):
         self.ctx = ctx
@@ -632,6 +641,34 @@ class StokesProblem(ConvectionDiffusion):
         lv = self.disc.n_levels - 1
         v, p = self.disc.level_info(lv, 0), self.disc.level_info(lv, 1)
         return v["n_dofs"], v["n_active"], p["n_dofs"]
+
+    def assemble_linear_terms(self) -> None:
+        """NavierStokes::assemble_linear_terms (the same as assemble())"""
+        self.assemble()
+
+    def assemble_nonlinear_term(self) -> None:
+        """NavierStokes::assemble_nonlinear_term (src/System/NavierStokes.C:573):
+        the finest velocity restricted to every level, the velocity blocks
+        reassembled with the convective term (problem_type 5 only)"""
+        check(lib.pm_problem_assemble_nonlinear(self.handle), self.ctx.handle)
+
+    def residuals(self) -> tuple[float, float, float]:
+        """NavierStokes::compute_residuals: (impuls, mass, full) residual of the
+        current solution, the pressure defect projected into L2_0"""
+        out = np.zeros(3)
+        check(lib.pm_problem_residuals(self.handle, out.ctypes.data_as(C.c_void_p)), self.ctx.handle)
+        return float(out[0]), float(out[1]), float(out[2])
+
+    def solve_nonlinear(self, max_records: int = 1000) -> np.ndarray:
+        """The nonlinear loop of test/nse3d_solvers_test.c++ (stop_it(0), then
+        solve / assemble_nonlinear_term / stop_it(k)) with the nonlinloop_*
+        keys of the problem's database; call after assemble(). Returns the
+        (impuls, mass, full) residuals of steps 0..n (n solves)."""
+        res = np.zeros((max_records, 3))
+        n = C.c_int()
+        check(lib.pm_problem_solve_nonlinear(self.handle, max_records, res.ctypes.data_as(C.c_void_p),
+                                             C.byref(n)), self.ctx.handle)
+        return res[: min(n.value + 1, max_records)].copy()
 
 
 class Server:

@@ -1,6 +1,7 @@
 // extern "C" entry points (include/pmgpu.h). Every call catches the library's
 // exceptions and turns them into status codes plus a per-context message.
 #include <algorithm>
+#include <deque>
 #include <cstring>
 #include <iterator>
 #include <new>
@@ -833,9 +834,18 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
     p->stokes_example = int(Params::parse(params ? params : "").integer("example", 0));
     if (p->stokes_example != 0 && p->stokes_example != -3)
       throw Error(PM_E_UNSUPPORTED, "Stokes example must be 0 (manufactured) or -3 (test_u_2_p_1)");
+    // problem_type 3 Stokes, 5 Navier-Stokes (ParameterDatabase "problem_type")
+    p->problem_type = int(Params::parse(params ? params : "").integer("problem_type", 3));
+    if (p->problem_type != 3 && p->problem_type != 5)
+      throw Error(PM_E_UNSUPPORTED, "problem_type must be 3 (Stokes) or 5 (Navier-Stokes)");
+    if (p->problem_type == 5 && p->stokes_example != -3)
+      throw Error(PM_E_UNSUPPORTED, "the Navier-Stokes problem is implemented for example -3 (test_u_2_p_1)");
+    p->params_text = params ? params : "";
     const Disc& D = *d->d;
     const int nl = int(D.levels.size());
-    p->stab.upload(c);
+    // the rule of the assembly: degree 2 x 2 for the linear (Stokes) problem,
+    // 3 x 2 for the nonlinear one (FEDatabase3D.C:1153-1219)
+    p->stab.upload(c, p->problem_type == 5 ? 15 : 11);
     size_t kmax = 0, fmax = 0;
     p->slev.resize(nl);
     const Params pre = Params::parse(params ? params : "");
@@ -872,6 +882,25 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
     p->sol.alloc(n);
     p->rhs_coarse.alloc(n);
     PM_CUDA(cudaMemsetAsync(p->sol.p, 0, sizeof(double) * n, c->stream));
+    p->defect.alloc(n);
+    p->res2.alloc(4);
+    if (p->problem_type == 5) {
+      // velocities of the coarser levels (zero until the first restriction)
+      size_t cmax = 0;
+      p->ulev.resize(nl);
+      for (int l = 0; l + 1 < nl; ++l) {
+        p->slev[l].set_children(c, D.h.levels[D.levels[l + 1].level_in_hierarchy], D.levels[l]);
+        p->ulev[l].alloc(size_t(3) * p->slev[l].nvel);
+        PM_CUDA(cudaMemsetAsync(p->ulev[l].p, 0, p->ulev[l].bytes(), c->stream));
+        cmax = std::max(cmax, size_t(p->slev[l].n_cells) * 30);
+      }
+      if (nl > 1) {
+        std::vector<double> q;
+        build_p2_restriction(D.h, q);
+        p->rq.upload(q, c->stream);
+        p->cellval.alloc(cmax);
+      }
+    }
     std::string text = params ? params : "";
     Params prm = Params::parse(text.c_str());
     if (prm.str("preconditioner", "") == "multigrid" && !prm.has("multigrid_n_levels"))
@@ -911,11 +940,17 @@ int pm_problem_assemble(pm_problem* p) {
   const Disc& D = *p->disc->d;
   const int nl = int(D.levels.size());
   if (p->kind == KIND_STOKES) {
-    // NavierStokes<3>::assemble_linear_terms for the Stokes problem
+    // NavierStokes<3>::assemble_linear_terms (NavierStokes.C:407-570); for the
+    // Navier-Stokes problem NavierStokesAll holds the convective term of each
+    // level's current velocity (zero before the first solve)
     for (int l = 0; l < nl; ++l) {
       double* r = (l == nl - 1) ? p->rhs.p : p->rhs_coarse.p;
-      assemble_stokes_level(c, p->slev[l], p->stab, p->nu, p->mats[l]->csr, r, p->K.p, p->F.p,
-                            p->stokes_example);
+      if (p->problem_type == 5)
+        assemble_nse_level(c, p->slev[l], p->stab, p->nu, p->mats[l]->csr, l == nl - 1 ? p->sol.p : p->ulev[l].p,
+                           r, p->K.p, p->F.p);
+      else
+        assemble_stokes_level(c, p->slev[l], p->stab, p->nu, p->mats[l]->csr, r, p->K.p, p->F.p,
+                              p->stokes_example);
     }
     const DevCsr& top = p->mats.back()->csr;
     copy_nonactive(c, top.n_rows, top.mask, p->rhs.p, p->sol.p);
@@ -952,6 +987,109 @@ int pm_problem_solve(pm_problem* p) {
     p->solver_ready = true;
   }
   p->solver->solve(p->rhs.p, p->sol.p);
+  // NavierStokes::solve (NavierStokes.C:910-912): with the pressure projection
+  // (all-Dirichlet velocity) the pressure is moved into L2_0
+  if (p->kind == KIND_STOKES) project_pressure_l20(p->ctx, p->slev.back(), p->sol.p + 3 * size_t(p->slev.back().nvel));
+  return PM_OK;
+  PM_CATCH(p->ctx)
+}
+
+int pm_problem_assemble_nonlinear(pm_problem* p) {
+  if (!p) return PM_E_INVALID;
+  PM_TRY
+  if (p->kind != KIND_STOKES || p->problem_type != 5)
+    throw Error(PM_E_INVALID, "assemble_nonlinear_term needs a Navier-Stokes problem (problem_type 5)");
+  pm_ctx* c = p->ctx;
+  const int nl = int(p->slev.size());
+  // RestrictFunctionRepeatedly: finest -> coarsest, each from the one above
+  for (int l = nl - 2; l >= 0; --l) {
+    const double* uf = (l == nl - 2) ? p->sol.p : p->ulev[l + 1].p;
+    restrict_velocity(c, p->slev[l], p->slev[l + 1], p->rq.p, uf, p->ulev[l].p, p->cellval.p);
+  }
+  for (int l = 0; l < nl; ++l)
+    assemble_nse_level(c, p->slev[l], p->stab, p->nu, p->mats[l]->csr, l == nl - 1 ? p->sol.p : p->ulev[l].p,
+                       nullptr, p->K.p, p->F.p);
+  p->solver_ready = false;
+  return PM_OK;
+  PM_CATCH(p->ctx)
+}
+
+int pm_problem_residuals(pm_problem* p, double* out) {
+  if (!p || !out) return PM_E_INVALID;
+  PM_TRY
+  if (p->kind != KIND_STOKES) throw Error(PM_E_INVALID, "residuals of a convection-diffusion problem");
+  pm_ctx* c = p->ctx;
+  nse_residuals(c, p->slev.back(), p->mats.back()->csr, p->rhs.p, p->sol.p, p->defect.p, p->res2.p);
+  double h[4];
+  PM_CUDA(cudaMemcpyAsync(h, p->res2.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  PM_CUDA(cudaStreamSynchronize(c->stream));
+  // BlockVector::norm(blocks) (src/Matrix/BlockVector.C:293) sums the blocks'
+  // 2-norms; Residuals(imR, maR) takes the squares of the two sums
+  out[0] = std::sqrt(h[0]) + std::sqrt(h[1]) + std::sqrt(h[2]);
+  out[1] = std::sqrt(h[3]);
+  out[2] = std::sqrt(out[0] * out[0] + out[1] * out[1]);
+  return PM_OK;
+  PM_CATCH(p->ctx)
+}
+
+int pm_problem_solve_nonlinear(pm_problem* p, int max_records, double* residuals, int* n_steps) {
+  if (!p) return PM_E_INVALID;
+  PM_TRY
+  if (p->kind != KIND_STOKES || p->problem_type != 5)
+    throw Error(PM_E_INVALID, "the nonlinear loop needs a Navier-Stokes problem (problem_type 5)");
+  pm_ctx* c = p->ctx;
+  const Params prm = Params::parse(p->params_text.c_str());
+  const long max_it = prm.integer("nonlinloop_maxit", 100);
+  const long min_it = prm.integer("nonlinloop_minit", 1);
+  double limit = prm.num("nonlinloop_epsilon", 1e-10);
+  const double damping = prm.num("nonlinloop_damping_factor", 1.0);
+  const double slow = prm.num("nonlinloop_slowfactor", 1e10);
+  auto flag = [&](const char* k) {
+    const std::string v = prm.str(k, "false");
+    return v == "true" || v == "1";
+  };
+  const int n = p->mats.back()->csr.n_rows;
+  if (flag("nonlinloop_scale_epsilon_with_size")) limit *= std::sqrt(double(n));
+  // old_residuals: FixedSizeQueue<10, Residuals>, filled with 1e10 at the start
+  std::deque<double> old(10, 1e10);
+  double initial_rhs_norm = 0.0;
+  pm::DBuf<double> prev;
+  if (damping != 1.0) prev.alloc(n);
+  int k = 0;
+  auto record = [&](const double* r) {
+    if (residuals && k < max_records)
+      for (int i = 0; i < 3; ++i) residuals[3 * k + i] = r[i];
+  };
+  // NavierStokes::stop_it (NavierStokes.C:753-816)
+  auto stop_it = [&](int it) {
+    double r[3];
+    int rc = pm_problem_residuals(p, r);
+    if (rc != PM_OK) throw Error(rc, c->last_error);
+    record(r);
+    old.push_back(r[2]);
+    old.pop_front();
+    if (it == 0) initial_rhs_norm = std::sqrt(dot_host(c, n, p->rhs.p, p->rhs.p));
+    if (it < min_it) return false;
+    const bool slow_conv = r[2] >= slow * old.front();
+    double lim = limit;
+    if (flag("nonlinloop_residual_relative_to_rhs")) lim *= initial_rhs_norm;
+    return r[2] <= lim || it == max_it || slow_conv;
+  };
+  stop_it(0);
+  for (k = 1;; ++k) {
+    if (damping != 1.0) vcopy(c, n, p->sol.p, prev.p);
+    int rc = pm_problem_solve(p);
+    if (rc != PM_OK) return rc;
+    if (damping != 1.0) {
+      // x = w x_new + (1 - w) x_old, then the pressure back into L2_0
+      vaxpby(c, n, 1.0 - damping, prev.p, damping, p->sol.p);
+      project_pressure_l20(c, p->slev.back(), p->sol.p + 3 * size_t(p->slev.back().nvel));
+    }
+    rc = pm_problem_assemble_nonlinear(p);
+    if (rc != PM_OK) return rc;
+    if (stop_it(k)) break;
+  }
+  if (n_steps) *n_steps = k;
   return PM_OK;
   PM_CATCH(p->ctx)
 }
@@ -975,6 +1113,15 @@ int pm_problem_get_solution(const pm_problem* p, double* out) {
   if (!p || !out) return PM_E_INVALID;
   PM_TRY
   p->sol.download(out, p->ctx->stream);
+  PM_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  return PM_OK;
+  PM_CATCH(p->ctx)
+}
+
+int pm_problem_set_solution(pm_problem* p, const double* in) {
+  if (!p || !in) return PM_E_INVALID;
+  PM_TRY
+  PM_CUDA(cudaMemcpyAsync(p->sol.p, in, p->sol.bytes(), cudaMemcpyHostToDevice, p->ctx->stream));
   PM_CUDA(cudaStreamSynchronize(p->ctx->stream));
   return PM_OK;
   PM_CATCH(p->ctx)

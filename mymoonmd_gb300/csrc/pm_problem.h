@@ -2,6 +2,7 @@
 // level matrices, assembly inputs, right-hand side, solution and solver.
 #pragma once
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "pm_assemble.h"
@@ -15,6 +16,12 @@ struct pm_problem {
   pm_cd_coeffs coeffs{};
   double nu = 1.0;  // Stokes viscosity
   int stokes_example = 0;  // 0: manufactured sine velocity; -3: polynomial (test_u_2_p_1)
+  int problem_type = 3;    // Stokes kind: 3 Stokes, 5 Navier-Stokes (convective form)
+  // Navier-Stokes: restricted velocities of the coarser levels, the P2
+  // restriction matrices, scratch, the defect and its blocks' squared norms
+  std::vector<pm::DBuf<double>> ulev;
+  pm::DBuf<double> rq, cellval, defect, res2;
+  std::string params_text;  // the creation parameters (nonlinloop_* keys)
   int qn = 3;
   std::vector<pm::DevStokesLevel> slev;
   pm::DevStokesTables stab;

@@ -22,30 +22,41 @@
 namespace pm {
 
 // ------------------------------------------------------------- tables ------
-// the P4Tetra rule and the P2 basis: pm_tetra.h
+// the P4Tetra / P5Tetra rules and the P2 basis: pm_tetra.h
 
-// layout: S[6][100] | D[3][40] | phi2[11][10] | w[11] | xi[11][3]
-static constexpr int kOffS = 0, kOffD = 600, kOffPhi = 720, kOffW = 830, kOffXi = 841, kTabSize = 874;
+// layout: S[6][100] | D[3][40] | phi2[qn][10] | w[qn] | xi[qn][3] | C[3][10][10][10]
+static constexpr int kOffS = 0, kOffD = 600, kOffPhi = 720;
+__host__ __device__ constexpr int tab_off_w(int qn) { return kOffPhi + 10 * qn; }
+__host__ __device__ constexpr int tab_off_xi(int qn) { return tab_off_w(qn) + qn; }
+__host__ __device__ constexpr int tab_off_c(int qn) { return tab_off_xi(qn) + 3 * qn; }
+__host__ __device__ constexpr int tab_size(int qn) { return tab_off_c(qn) + 3000; }
 
-void DevStokesTables::upload(pm_ctx* c) {
-  std::vector<double> t(kTabSize, 0.0);
-  double phi[11][10], d[3][11][10], psi[11][4];
-  for (int q = 0; q < 11; ++q) {
-    p2_eval(kP4x[q], kP4y[q], kP4z[q], phi[q], d[0][q], d[1][q], d[2][q]);
-    psi[q][0] = 1 - kP4x[q] - kP4y[q] - kP4z[q];
-    psi[q][1] = kP4x[q];
-    psi[q][2] = kP4y[q];
-    psi[q][3] = kP4z[q];
+void DevStokesTables::upload(pm_ctx* c, int nq) {
+  if (nq != kP4n && nq != kP5n) throw Error(PM_E_UNSUPPORTED, "Stokes tables: 11 or 15 quadrature points");
+  qn = nq;
+  const double* qw = nq == kP4n ? kP4w : kP5w;
+  const double* qx = nq == kP4n ? kP4x : kP5x;
+  const double* qy = nq == kP4n ? kP4y : kP5y;
+  const double* qz = nq == kP4n ? kP4z : kP5z;
+  std::vector<double> t(tab_size(nq), 0.0);
+  std::vector<double> phi(nq * 10), d(3 * nq * 10), psi(nq * 4);
+  for (int q = 0; q < nq; ++q) {
+    p2_eval(qx[q], qy[q], qz[q], &phi[q * 10], &d[(0 * nq + q) * 10], &d[(1 * nq + q) * 10], &d[(2 * nq + q) * 10]);
+    psi[q * 4 + 0] = 1 - qx[q] - qy[q] - qz[q];
+    psi[q * 4 + 1] = qx[q];
+    psi[q * 4 + 2] = qy[q];
+    psi[q * 4 + 3] = qz[q];
   }
+  auto D = [&](int a, int q, int i) { return d[(a * nq + q) * 10 + i]; };
   int k = 0;
   for (int a = 0; a < 3; ++a)
     for (int b = a; b < 3; ++b, ++k)
       for (int i = 0; i < 10; ++i)
         for (int j = 0; j < 10; ++j) {
           double s = 0.0;
-          for (int q = 0; q < 11; ++q) {
-            s += kP4w[q] * d[a][q][i] * d[b][q][j];
-            if (a != b) s += kP4w[q] * d[b][q][i] * d[a][q][j];
+          for (int q = 0; q < nq; ++q) {
+            s += qw[q] * D(a, q, i) * D(b, q, j);
+            if (a != b) s += qw[q] * D(b, q, i) * D(a, q, j);
           }
           t[kOffS + k * 100 + i * 10 + j] = s;
         }
@@ -53,16 +64,26 @@ void DevStokesTables::upload(pm_ctx* c) {
     for (int i = 0; i < 4; ++i)
       for (int j = 0; j < 10; ++j) {
         double s = 0.0;
-        for (int q = 0; q < 11; ++q) s += kP4w[q] * psi[q][i] * d[a][q][j];
+        for (int q = 0; q < nq; ++q) s += qw[q] * psi[q * 4 + i] * D(a, q, j);
         t[kOffD + a * 40 + i * 10 + j] = s;
       }
-  for (int q = 0; q < 11; ++q) {
-    for (int i = 0; i < 10; ++i) t[kOffPhi + q * 10 + i] = phi[q][i];
-    t[kOffW + q] = kP4w[q];
-    t[kOffXi + q * 3 + 0] = kP4x[q];
-    t[kOffXi + q * 3 + 1] = kP4y[q];
-    t[kOffXi + q * 3 + 2] = kP4z[q];
+  for (int q = 0; q < nq; ++q) {
+    for (int i = 0; i < 10; ++i) t[kOffPhi + q * 10 + i] = phi[q * 10 + i];
+    t[tab_off_w(nq) + q] = qw[q];
+    t[tab_off_xi(nq) + q * 3 + 0] = qx[q];
+    t[tab_off_xi(nq) + q * 3 + 1] = qy[q];
+    t[tab_off_xi(nq) + q * 3 + 2] = qz[q];
   }
+  // C[a][i][j][k]: test function i, ansatz function j (derivative a), velocity
+  // basis function k
+  for (int a = 0; a < 3; ++a)
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j)
+        for (int l = 0; l < 10; ++l) {
+          double s = 0.0;
+          for (int q = 0; q < nq; ++q) s += qw[q] * phi[q * 10 + i] * D(a, q, j) * phi[q * 10 + l];
+          t[tab_off_c(nq) + a * 1000 + i * 100 + j * 10 + l] = s;
+        }
   data.upload(t, c->stream);
 }
 
@@ -77,16 +98,60 @@ void DevStokesLevel::upload(pm_ctx* c, const DiscLevel& L) {
   diag_pos.upload(L.diag_pos, c->stream);
   nvel = L.block_len[0];
   nvel_active = L.block_active[0];
+  np = L.block_len[3];
   bnd_xyz.upload(L.bnd_xyz, c->stream);
+  udof.upload(L.space.dofmap, c->stream);
+  // pressure integral weights: the P1 integral over a cell is |K| / 4 times
+  // the sum of its vertex values
+  std::vector<double> w(np, 0.0);
+  measure = 0.0;
+  for (int cell = 0; cell < n_cells; ++cell) {
+    const double* v = L.verts.data() + size_t(cell) * 12;
+    double J[3][3];
+    for (int d = 0; d < 3; ++d)
+      for (int a = 0; a < 3; ++a) J[d][a] = v[3 * (a + 1) + d] - v[d];
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    const double vol = std::fabs(det) / 6.0;
+    measure += vol;
+    for (int k = 0; k < 4; ++k) w[L.pspace.dofmap[size_t(cell) * 4 + k]] += vol / 4.0;
+  }
+  pweight.upload(w, c->stream);
+}
+
+void DevStokesLevel::set_children(pm_ctx* c, const pmsetup::Level& fine, const DiscLevel& L) {
+  std::vector<int> ch(size_t(n_cells) * 8, -1);
+  for (int f = 0; f < fine.n_cells; ++f) {
+    const int par = fine.parent[f], j = fine.child_no[f];
+    if (par < 0 || par >= n_cells || j < 0 || j >= 8) throw Error(PM_E_INVALID, "tetrahedral refinement: bad parent");
+    ch[size_t(par) * 8 + j] = f;
+  }
+  for (int v : ch)
+    if (v < 0) throw Error(PM_E_INVALID, "tetrahedral refinement: a cell without 8 children");
+  children.upload(ch, c->stream);
+  std::vector<int> ip(nvel + 1, 0), ix(size_t(n_cells) * 10);
+  for (int e = 0; e < n_cells * 10; ++e) ip[L.space.dofmap[e] + 1]++;
+  for (int d = 0; d < nvel; ++d) ip[d + 1] += ip[d];
+  std::vector<int> fill(ip.begin(), ip.end() - 1);
+  for (int e = 0; e < n_cells * 10; ++e) ix[fill[L.space.dofmap[e]]++] = e;  // cell order
+  vinc_ptr.upload(ip, c->stream);
+  vinc_idx.upload(ix, c->stream);
 }
 
 // right-hand side f = -nu Lap u + grad p of the manufactured Stokes solution
-__device__ void stokes_f(double nu, const double* x, double* f, int example) {
+// (example 0 / -3); with `convective` the example -3 body force of the
+// Navier-Stokes equations, which adds (u . grad) u
+__device__ void stokes_f(double nu, const double* x, double* f, int example, bool convective = false) {
   if (example == -3) {
-    // u = (y^2, xz, -y^2): Lap u = (2, 0, -2); grad p = (1, 1, 1)
-    f[0] = -nu * 2.0 + 1.0;
-    f[1] = -nu * 0.0 + 1.0;
-    f[2] = -nu * -2.0 + 1.0;
+    // u = (y^2, xz, -y^2): Lap u = (2, 0, -2); grad p = (1, 1, 1);
+    // (u . grad) u = (2xyz, y^2 z - x y^2, -2xyz)
+    const double X = x[0], Y = x[1], Z = x[2];
+    const double c0 = convective ? 2.0 * X * Y * Z : 0.0;
+    const double c1 = convective ? Y * Y * Z - X * Y * Y : 0.0;
+    f[0] = -nu * 2.0 + c0 + 1.0;
+    f[1] = -nu * 0.0 + c1 + 1.0;
+    f[2] = -nu * -2.0 - c0 + 1.0;
     return;
   }
   const double p = 3.14159265358979323846;
@@ -111,14 +176,23 @@ __device__ void stokes_f(double nu, const double* x, double* f, int example) {
   f[2] = -nu * (lx - ly) + 1.0;
 }
 
-template <int CHUNK>
+// one block per CHUNK cells: per-cell geometry factors, then the element
+// matrix as contractions of the reference tensors (A part: stiffness and,
+// with a velocity u, the convective term; B part) and, with F, the element
+// right-hand side on the NQ-point rule
+template <int CHUNK, int NQ>
 __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* __restrict__ verts,
                                                      const double* __restrict__ tab, double nu,
-                                                     double* __restrict__ K, double* __restrict__ F, int example) {
+                                                     double* __restrict__ K, double* __restrict__ F, int example,
+                                                     bool convective_f, const double* __restrict__ u,
+                                                     const int* __restrict__ udof, int nvel) {
+  constexpr int kW = tab_off_w(NQ), kXi = tab_off_xi(NQ), kC = tab_off_c(NQ);
   __shared__ double cS[CHUNK][6];
   __shared__ double cB[CHUNK][9];
   __shared__ double geo[CHUNK][13];
-  __shared__ double fq[CHUNK][11][3];
+  __shared__ double cG[CHUNK][9];
+  __shared__ double cV[CHUNK][30];  // |det J| sum_d G[d][a] u_d,k
+  __shared__ double fq[CHUNK][NQ][3];
   const int c0 = blockIdx.x * CHUNK;
   const int nc = min(CHUNK, n_cells - c0);
   const int t = threadIdx.x;
@@ -134,7 +208,7 @@ __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* 
                        J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
                        J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
     const double r = 1.0 / det;
-    double G[3][3];
+    double G[3][3];  // J^{-T}: d_k phi = sum_a G[k][a] dhat_a phi
     G[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * r;
     G[0][1] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) * r;
     G[0][2] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * r;
@@ -153,7 +227,10 @@ __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* 
         cS[t][k++] = nu * adet * s;
       }
     for (int kk = 0; kk < 3; ++kk)
-      for (int a = 0; a < 3; ++a) cB[t][kk * 3 + a] = -adet * G[kk][a];
+      for (int a = 0; a < 3; ++a) {
+        cB[t][kk * 3 + a] = -adet * G[kk][a];
+        cG[t][kk * 3 + a] = adet * G[kk][a];
+      }
     for (int d = 0; d < 3; ++d) {
       geo[t][d] = v[d];
       for (int a = 0; a < 3; ++a) geo[t][3 + d * 3 + a] = J[d][a];
@@ -161,18 +238,29 @@ __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* 
     geo[t][12] = adet;
   }
   __syncthreads();
-  for (int e = t; e < nc * 11; e += blockDim.x) {
-    const int cl = e / 11, q = e % 11;
-    double x[3];
-    for (int d = 0; d < 3; ++d) {
-      double s = geo[cl][d];
-      for (int a = 0; a < 3; ++a) s += geo[cl][3 + d * 3 + a] * tab[kOffXi + q * 3 + a];
-      x[d] = s;
+  if (u) {
+    for (int e = t; e < nc * 30; e += blockDim.x) {
+      const int cl = e / 30, ak = e % 30, a = ak / 10, k = ak % 10;
+      const int g = udof[(size_t)(c0 + cl) * 10 + k];
+      double s = 0.0;
+      for (int d = 0; d < 3; ++d) s += cG[cl][d * 3 + a] * u[(size_t)d * nvel + g];
+      cV[cl][ak] = s;
     }
-    double f[3];
-    stokes_f(nu, x, f, example);
-    const double m = tab[kOffW + q] * geo[cl][12];
-    for (int d = 0; d < 3; ++d) fq[cl][q][d] = m * f[d];
+  }
+  if (F) {
+    for (int e = t; e < nc * NQ; e += blockDim.x) {
+      const int cl = e / NQ, q = e % NQ;
+      double x[3];
+      for (int d = 0; d < 3; ++d) {
+        double s = geo[cl][d];
+        for (int a = 0; a < 3; ++a) s += geo[cl][3 + d * 3 + a] * tab[kXi + q * 3 + a];
+        x[d] = s;
+      }
+      double f[3];
+      stokes_f(nu, x, f, example, convective_f);
+      const double m = tab[kW + q] * geo[cl][12];
+      for (int d = 0; d < 3; ++d) fq[cl][q][d] = m * f[d];
+    }
   }
   __syncthreads();
   for (int e = t; e < nc * 220; e += blockDim.x) {
@@ -181,6 +269,17 @@ __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* 
     if (p < 100) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) s = fma(cS[cl][k], __ldg(tab + kOffS + k * 100 + p), s);
+      if (u) {
+        // N_ij = sum_a sum_k V[a][k] C[a][i][j][k], p = i * 10 + j
+        double nsum = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const double* Ca = tab + kC + a * 1000 + p * 10;
+#pragma unroll
+          for (int k = 0; k < 10; ++k) nsum = fma(cV[cl][a * 10 + k], __ldg(Ca + k), nsum);
+        }
+        s += nsum;
+      }
     } else {
       const int kk = (p - 100) / 40, ij = (p - 100) % 40;
 #pragma unroll
@@ -188,14 +287,16 @@ __global__ void __launch_bounds__(256) k_elem_stokes(int n_cells, const double* 
     }
     K[(size_t)(c0 + cl) * 220 + p] = s;
   }
-  for (int e = t; e < nc * 34; e += blockDim.x) {
-    const int cl = e / 34, m = e % 34;
-    double s = 0.0;
-    if (m < 30) {
-      const int comp = m / 10, i = m % 10;
-      for (int q = 0; q < 11; ++q) s += fq[cl][q][comp] * tab[kOffPhi + q * 10 + i];
+  if (F) {
+    for (int e = t; e < nc * 34; e += blockDim.x) {
+      const int cl = e / 34, m = e % 34;
+      double s = 0.0;
+      if (m < 30) {
+        const int comp = m / 10, i = m % 10;
+        for (int q = 0; q < NQ; ++q) s += fq[cl][q][comp] * tab[kOffPhi + q * 10 + i];
+      }
+      F[(size_t)(c0 + cl) * 34 + m] = s;
     }
-    F[(size_t)(c0 + cl) * 34 + m] = s;
   }
 }
 
@@ -225,13 +326,23 @@ __global__ void k_stokes_dirichlet(int nb, int nvel, int nact, const double* __r
   rhs[2 * nvel + nact + i] = -y * y;
 }
 
-void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu,
-                           DevCsr& A, double* rhs, double* K, double* F, int example) {
+static void launch_elem_stokes(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu,
+                               double* K, double* F, int example, bool convective_f, const double* u) {
   constexpr int CHUNK = 32;
-  if (example != 0 && example != -3) throw Error(PM_E_UNSUPPORTED, "Stokes example must be 0 or -3");
-  k_elem_stokes<CHUNK><<<(L.n_cells + CHUNK - 1) / CHUNK, 256, 0, c->stream>>>(L.n_cells, L.verts.p, t.data.p,
-                                                                              nu, K, F, example);
+  const int g = (L.n_cells + CHUNK - 1) / CHUNK;
+  if (t.qn == kP4n)
+    k_elem_stokes<CHUNK, kP4n><<<g, 256, 0, c->stream>>>(L.n_cells, L.verts.p, t.data.p, nu, K, F, example,
+                                                          convective_f, u, L.udof.p, L.nvel);
+  else
+    k_elem_stokes<CHUNK, kP5n><<<g, 256, 0, c->stream>>>(L.n_cells, L.verts.p, t.data.p, nu, K, F, example,
+                                                          convective_f, u, L.udof.p, L.nvel);
   PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+// element storage -> matrix values (and right-hand side)
+static void gather_stokes(pm_ctx* c, const DevStokesLevel& L, DevCsr& A, double* rhs, const double* K,
+                          const double* F, int example) {
   const int nnz = int(A.nnz);
   const int g = std::max(1, std::min((nnz + 255) / 256, c->num_sms * 16));
   k_gather_stokes<<<g, 256, 0, c->stream>>>(nnz, L.gat_ptr.p, L.gat_idx.p, K, A.vals.p);
@@ -241,17 +352,235 @@ void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTa
     k_unit_diag<<<(nd + 255) / 256, 256, 0, c->stream>>>(nd, L.diag_pos.p, A.vals.p);
     PM_CHECK_LAUNCH();
   }
-  const int gr = std::max(1, std::min((L.n + 255) / 256, c->num_sms * 16));
-  k_gather_stokes<<<gr, 256, 0, c->stream>>>(L.n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
-  PM_CHECK_LAUNCH();
-  c->kernel_launches += nd ? 4 : 3;
-  const int nb = L.nvel - L.nvel_active;
-  if (example == -3 && nb > 0) {
-    k_stokes_dirichlet<<<(nb + 255) / 256, 256, 0, c->stream>>>(nb, L.nvel, L.nvel_active, L.bnd_xyz.p, rhs);
+  c->kernel_launches += nd ? 2 : 1;
+  if (rhs) {
+    const int gr = std::max(1, std::min((L.n + 255) / 256, c->num_sms * 16));
+    k_gather_stokes<<<gr, 256, 0, c->stream>>>(L.n, L.rgat_ptr.p, L.rgat_idx.p, F, rhs);
     PM_CHECK_LAUNCH();
     c->kernel_launches++;
+    const int nb = L.nvel - L.nvel_active;
+    if (example == -3 && nb > 0) {
+      k_stokes_dirichlet<<<(nb + 255) / 256, 256, 0, c->stream>>>(nb, L.nvel, L.nvel_active, L.bnd_xyz.p, rhs);
+      PM_CHECK_LAUNCH();
+      c->kernel_launches++;
+    }
   }
   A.values_changed(c);
+}
+
+void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu,
+                           DevCsr& A, double* rhs, double* K, double* F, int example) {
+  if (example != 0 && example != -3) throw Error(PM_E_UNSUPPORTED, "Stokes example must be 0 or -3");
+  launch_elem_stokes(c, L, t, nu, K, F, example, false, nullptr);
+  gather_stokes(c, L, A, rhs, K, F, example);
+}
+
+void assemble_nse_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu, DevCsr& A,
+                        const double* u, double* rhs, double* K, double* F) {
+  launch_elem_stokes(c, L, t, nu, K, rhs ? F : nullptr, -3, true, u);
+  gather_stokes(c, L, A, rhs, K, F, -3);
+}
+
+// ------------------------------------------------------ restriction --------
+void build_p2_restriction(const pmsetup::Hierarchy& h, std::vector<double>& q) {
+  if (h.geometry != pmsetup::GEO_CUBE_TETRA || h.levels.size() < 2)
+    throw Error(PM_E_INVALID, "P2 restriction needs a refined tetrahedral hierarchy");
+  const pmsetup::Level& L0 = h.levels[0];
+  const pmsetup::Level& L1 = h.levels[1];
+  const double s = 1.0 / double(h.scale);
+  auto vtx = [&](const pmsetup::Level& L, int cell, int v, int d) {
+    return double(L.vtx[(size_t(cell) * 4 + v) * 3 + d]) * s;
+  };
+  // parent 0: x = v0 + J xi
+  double J[3][3], Ji[3][3];
+  for (int d = 0; d < 3; ++d)
+    for (int a = 0; a < 3; ++a) J[d][a] = vtx(L0, 0, a + 1, d) - vtx(L0, 0, 0, d);
+  const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                     J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                     J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+  Ji[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) / det;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+  Ji[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) / det;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+  Ji[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) / det;
+  Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+  Ji[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) / det;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  // mass matrix of the parent's basis on the reference cell (P4Tetra: exact)
+  double G[10][10] = {};
+  double phi[10], dx[10], dy[10], dz[10];
+  for (int qq = 0; qq < kP4n; ++qq) {
+    p2_eval(kP4x[qq], kP4y[qq], kP4z[qq], phi, dx, dy, dz);
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j) G[i][j] += kP4w[qq] * phi[i] * phi[j];
+  }
+  q.assign(8 * 100, 0.0);
+  int found = 0;
+  for (int f = 0; f < L1.n_cells; ++f) {
+    if (L1.parent[f] != 0) continue;
+    const int ch = L1.child_no[f];
+    ++found;
+    // child vertices in the parent's reference coordinates
+    double xi[4][3];
+    for (int v = 0; v < 4; ++v)
+      for (int a = 0; a < 3; ++a) {
+        double sum = 0.0;
+        for (int d = 0; d < 3; ++d) sum += Ji[a][d] * (vtx(L1, f, v, d) - vtx(L0, 0, 0, d));
+        xi[v][a] = sum;
+      }
+    double Jc[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) Jc[a][b] = xi[b + 1][a] - xi[0][a];
+    const double dc = std::fabs(Jc[0][0] * (Jc[1][1] * Jc[2][2] - Jc[1][2] * Jc[2][1]) -
+                                Jc[0][1] * (Jc[1][0] * Jc[2][2] - Jc[1][2] * Jc[2][0]) +
+                                Jc[0][2] * (Jc[1][0] * Jc[2][1] - Jc[1][1] * Jc[2][0]));
+    // R[k][l] = (parent k, child l) over the child (P4Tetra on the child)
+    double R[10][10] = {};
+    double phc[10], php[10];
+    for (int qq = 0; qq < kP4n; ++qq) {
+      p2_eval(kP4x[qq], kP4y[qq], kP4z[qq], phc, dx, dy, dz);
+      double pt[3];
+      for (int a = 0; a < 3; ++a)
+        pt[a] = xi[0][a] + Jc[a][0] * kP4x[qq] + Jc[a][1] * kP4y[qq] + Jc[a][2] * kP4z[qq];
+      p2_eval(pt[0], pt[1], pt[2], php, dx, dy, dz);
+      for (int k = 0; k < 10; ++k)
+        for (int l = 0; l < 10; ++l) R[k][l] += kP4w[qq] * dc * php[k] * phc[l];
+    }
+    // Q = G^{-1} R by Gauss-Jordan with partial pivoting
+    double M[10][20];
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j) {
+        M[i][j] = G[i][j];
+        M[i][10 + j] = R[i][j];
+      }
+    for (int k = 0; k < 10; ++k) {
+      int pr = k;
+      for (int i = k + 1; i < 10; ++i)
+        if (std::fabs(M[i][k]) > std::fabs(M[pr][k])) pr = i;
+      for (int j = 0; j < 20; ++j) std::swap(M[k][j], M[pr][j]);
+      const double pv = M[k][k];
+      for (int j = 0; j < 20; ++j) M[k][j] /= pv;
+      for (int i = 0; i < 10; ++i) {
+        if (i == k) continue;
+        const double fct = M[i][k];
+        for (int j = 0; j < 20; ++j) M[i][j] -= fct * M[k][j];
+      }
+    }
+    for (int k = 0; k < 10; ++k)
+      for (int l = 0; l < 10; ++l) q[size_t(ch) * 100 + k * 10 + l] = M[k][10 + l];
+  }
+  if (found != 8) throw Error(PM_E_INVALID, "P2 restriction: the root cell has no 8 children");
+}
+
+// one thread per (coarse cell, component, coarse local DOF): sum over the
+// children j (in order) of sum_l Q_j[k][l] u(child j, l)
+__global__ void k_restrict_cells(int n_coarse, const int* __restrict__ children, const int* __restrict__ fdof,
+                                 const double* __restrict__ q, const double* __restrict__ uf, int nvf,
+                                 double* __restrict__ cellval) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_coarse * 30) return;
+  const int cell = e / 30, comp = (e % 30) / 10, k = e % 10;
+  double acc = 0.0;
+  for (int j = 0; j < 8; ++j) {
+    const int f = children[(size_t)cell * 8 + j];
+    const int* fd = fdof + (size_t)f * 10;
+    const double* Q = q + j * 100 + k * 10;
+    double s = 0.0;
+    for (int l = 0; l < 10; ++l) s += Q[l] * uf[(size_t)comp * nvf + fd[l]];
+    acc += s;
+  }
+  cellval[e] = acc;
+}
+
+// coarse DOF d: the cell values at its positions, in cell order, averaged
+__global__ void k_restrict_average(int nvc, const int* __restrict__ ip, const int* __restrict__ ix,
+                                   const double* __restrict__ cellval, double* __restrict__ uc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 3 * nvc) return;
+  const int comp = e / nvc, d = e % nvc;
+  double s = 0.0;
+  for (int t = ip[d]; t < ip[d + 1]; ++t) {
+    const int pos = ix[t];
+    s += cellval[(size_t)(pos / 10) * 30 + comp * 10 + pos % 10];
+  }
+  const int cnt = ip[d + 1] - ip[d];
+  uc[e] = cnt ? s / double(cnt) : 0.0;
+}
+
+void restrict_velocity(pm_ctx* c, const DevStokesLevel& coarse, const DevStokesLevel& fine, const double* q,
+                       const double* u_fine, double* u_coarse, double* cellval) {
+  if (!coarse.children.p) throw Error(PM_E_INVALID, "restriction: the coarse level has no children map");
+  const int nw = coarse.n_cells * 30;
+  k_restrict_cells<<<(nw + 255) / 256, 256, 0, c->stream>>>(coarse.n_cells, coarse.children.p, fine.udof.p, q,
+                                                            u_fine, fine.nvel, cellval);
+  PM_CHECK_LAUNCH();
+  const int nd = 3 * coarse.nvel;
+  k_restrict_average<<<(nd + 255) / 256, 256, 0, c->stream>>>(coarse.nvel, coarse.vinc_ptr.p, coarse.vinc_idx.p,
+                                                              cellval, u_coarse);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 2;
+}
+
+// ------------------------------------------- pressure projection, residuals --
+// one block: the weighted sum in a fixed order, then p -= sum / measure
+__global__ void __launch_bounds__(1024) k_project_l20(int np, const double* __restrict__ w, double measure,
+                                                       double* __restrict__ p) {
+  __shared__ double red[32];
+  __shared__ double mean;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += w[i] * p[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int k = 0; k < int(blockDim.x >> 5); ++k) tot += red[k];
+    mean = tot / measure;
+  }
+  __syncthreads();
+  const double m = mean;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) p[i] -= m;
+}
+
+void project_pressure_l20(pm_ctx* c, const DevStokesLevel& L, double* p) {
+  k_project_l20<<<1, 1024, 0, c->stream>>>(L.np, L.pweight.p, L.measure, p);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
+}
+
+// one block: the squared norms of the blocks [0, nv), [nv, 2 nv), [2 nv, 3 nv)
+// and [3 nv, n), each summed in a fixed order
+__global__ void __launch_bounds__(1024) k_block_norms(int nv, int n, const double* __restrict__ d,
+                                                       double* __restrict__ out4) {
+  __shared__ double red[4][32];
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = d[i];
+    const int b = min(i / nv, 3);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] += (k == b) ? v * v : 0.0;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = a[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double s = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+    out4[threadIdx.x] = s;
+  }
+}
+
+void nse_residuals(pm_ctx* c, const DevStokesLevel& L, const DevCsr& A, const double* rhs, const double* x,
+                   double* d, double* out4) {
+  csr_apply(c, A, EPI_DEFECT, x, d, rhs, 1.0);
+  project_pressure_l20(c, L, d + 3 * size_t(L.nvel));
+  k_block_norms<<<1, 1024, 0, c->stream>>>(L.nvel, L.n, d, out4);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches++;
 }
 
 // --------------------------------------------------- projected matrix ------

@@ -6,20 +6,37 @@
 
 namespace pm {
 
-// reference-element data of P2/P1 on the P4Tetra rule (11 points)
+// reference-element data of P2/P1 on a tetrahedral rule: P4Tetra (11 points)
+// for the Stokes problem, P5Tetra (15 points) for the Navier-Stokes problem
+// (FEDatabase3D.C:1153-1219: degree 2 x 2 for linear problems, 3 x 2
+// otherwise)
 struct DevStokesTables {
-  DBuf<double> data;  // S (6 x 100), D (3 x 40), phi2 (11 x 10), w (11), xi (11 x 3)
-  void upload(pm_ctx* c);
+  int qn = 11;
+  // S (6 x 100), D (3 x 40), phi2 (qn x 10), w (qn), xi (qn x 3), and the
+  // convection tensor C[a][i][j][k] = sum_q w phi_i d_a phi_j phi_k (3 x 1000)
+  DBuf<double> data;
+  void upload(pm_ctx* c, int qn = 11);
 };
 
 // device copy of one Stokes level's assembly inputs
 struct DevStokesLevel {
   int n_cells = 0, n = 0;
   int nvel = 0, nvel_active = 0;  // DOFs and active DOFs of one velocity component
+  int np = 0;                     // pressure DOFs
   DBuf<double> verts;
   DBuf<double> bnd_xyz;  // coordinates of the non-active velocity DOFs
   DBuf<int> gat_ptr, gat_idx, rgat_ptr, rgat_idx, diag_pos;
+  DBuf<int> udof;        // velocity GlobalNumbers (n_cells x 10)
+  // P1 pressure: integral weights (sum over the cells of a DOF of |K| / 4)
+  // and the measure of the domain, for the projection into L2_0
+  DBuf<double> pweight;
+  double measure = 0.0;
+  // restriction of a velocity from the next finer level (coarse levels):
+  // the 8 children of each cell, and per velocity DOF its (cell * 10 + k)
+  // positions in cell order
+  DBuf<int> children, vinc_ptr, vinc_idx;
   void upload(pm_ctx* c, const DiscLevel& L);
+  void set_children(pm_ctx* c, const pmsetup::Level& fine, const DiscLevel& L);
 };
 
 // element matrices (220 doubles per cell) and element right-hand sides (34)
@@ -31,6 +48,41 @@ struct DevStokesLevel {
 // Dirichlet values u(node); then gather into the combined CSR
 void assemble_stokes_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu,
                            DevCsr& A, double* rhs, double* K, double* F, int example = 0);
+
+// Navier-Stokes (problem_type 5, convective form, NSTYPE 4, LAPLACETYPE 0):
+// NavierStokesAll / NavierStokesNL of src/AssembleRoutinesSaddle/
+// NSE_local_assembling_routines.C with NSNonlinearTerm_convective, which adds
+//   N_ij = sum_q w |det J| (u . grad phi_j) phi_i
+// to each of A11, A22, A33 for the current velocity u = [u1 | u2 | u3] of the
+// level (nullptr: u = 0). With rhs == nullptr only the matrix is assembled
+// (assemble_nonlinear_term, NavierStokes.C:573-750); otherwise also the
+// right-hand side of the reference's example -3, whose body force holds the
+// convective term: f = -nu Lap u + (u . grad) u + grad p.
+void assemble_nse_level(pm_ctx* c, const DevStokesLevel& L, const DevStokesTables& t, double nu, DevCsr& A,
+                        const double* u, double* rhs, double* K, double* F);
+
+// the restriction matrices of P2 on the 8 children of the regular tetrahedral
+// refinement (TFEDatabase3D::GetRestrictionMatrix3D, FEDatabase3D.C:1771-1890):
+// Q_j = G^{-1} R_j, G the mass matrix of the parent's basis, R_j the products
+// of the parent's and child j's basis over child j; 8 x 10 x 10, Q_j[k][l]
+void build_p2_restriction(const pmsetup::Hierarchy& h, std::vector<double>& q);
+
+// GridTransfer::RestrictFunction (src/Multigrid/GridTransfer.C:1218-1501) of
+// the three velocity components from `fine` to `coarse`: per coarse cell the
+// sum over its children of Q_j times the child's values, then each coarse DOF
+// the average over its cells. cellval: coarse n_cells x 30 doubles scratch
+void restrict_velocity(pm_ctx* c, const DevStokesLevel& coarse, const DevStokesLevel& fine, const double* q,
+                       const double* u_fine, double* u_coarse, double* cellval);
+
+// TFEFunction3D::project_into_L20 (src/FE/FEFunction3D.C:1678) of a P1
+// pressure: p -= (integral of p) / measure
+void project_pressure_l20(pm_ctx* c, const DevStokesLevel& L, double* p);
+
+// NavierStokes::compute_residuals (NavierStokes.C:820-870): d = rhs - A x,
+// the pressure part of d projected into L2_0, then the squared norms of the
+// blocks u1, u2, u3, p of d into out4[0..3] (device)
+void nse_residuals(pm_ctx* c, const DevStokesLevel& L, const DevCsr& A, const double* rhs, const double* x,
+                   double* d, double* out4);
 
 // get_combined_submatrix: the combined matrix with the first pressure row
 // replaced by the unit row (pressure projection, all-Dirichlet velocity)

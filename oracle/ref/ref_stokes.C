@@ -15,19 +15,33 @@
 // (BlockFEMatrix::get_combined_matrix) and the right-hand side; with SOLVER
 // direct, the direct solve's solution of the finest level.
 //
-// usage: ref_stokes OUTDIR N_REFINE N_LEVELS SOLVER
-//   SOLVER direct (one level) | none (assemble only; N_LEVELS levels)
+// usage: ref_stokes OUTDIR N_REFINE N_LEVELS SOLVER [MODE RE EPS MAXIT]
+//   SOLVER direct (one level) | none (assemble only; N_LEVELS levels) |
+//          mg (FGMRES with a nodal Vanka multigrid, N_LEVELS levels)
+//   MODE stokes (default) | nse: the Navier-Stokes problem (problem_type 5,
+//   convective form) with the reference's own example -3 (whose coefficients
+//   hold the convective term) at Reynolds number RE, run as the reference's
+//   nse3d_solvers_test runs it (assemble_linear_terms, stop_it(0), then
+//   solve / assemble_nonlinear_term / stop_it(k) until stop_it says so, with
+//   nonlinloop_epsilon EPS and nonlinloop_maxit MAXIT); dumps the residuals
+//   of every nonlinear step, the linear iterations of every solve, the final
+//   solution and get_errors(). With SOLVER none, MODE nse sets the finest
+//   solution to u_b[i] = sin(0.7 i + 1.3 b + 0.1) (velocity component b, DOF
+//   i; pressure 0) and calls assemble_nonlinear_term once, then dumps every
+//   level as above plus every level's (restricted) velocity.
 #include <BaseCell.h>
 #include <Database.h>
 #include <Domain.h>
 #include <Example_NSE3D.h>
 #include <FEDatabase3D.h>
 #include <LocalAssembling.h>
+#include <LoopInfo.h>
 #include <Multigrid.h>
 #include <NavierStokes.h>
 #include <Solver.h>
 #include <Vertex.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -78,6 +92,7 @@ struct RefStokes : public NavierStokes<3> {
   RefStokes(const TDomain& dom, const ParameterDatabase& db, const Example_NSE3D& ex)
       : NavierStokes<3>(dom, db, ex) {}
   using NavierStokes<3>::systems;
+  using NavierStokes<3>::solver;
 };
 
 void dump_space(const std::string& pre, const TFESpace3D& space, std::FILE* meta, const char* name) {
@@ -97,13 +112,17 @@ void dump_space(const std::string& pre, const TFESpace3D& space, std::FILE* meta
 
 int main(int argc, char** argv) {
   if (argc < 5) {
-    std::fprintf(stderr, "usage: %s OUTDIR N_REFINE N_LEVELS SOLVER\n", argv[0]);
+    std::fprintf(stderr, "usage: %s OUTDIR N_REFINE N_LEVELS SOLVER [MODE RE EPS MAXIT]\n", argv[0]);
     return 2;
   }
   const std::string out = argv[1];
   const size_t n_refine = size_t(std::atoi(argv[2]));
   const size_t n_levels = size_t(std::atoi(argv[3]));
   const std::string solver = argv[4];
+  const bool nse_mode = argc > 5 && std::string(argv[5]) == "nse";
+  const double reynolds = argc > 6 ? std::atof(argv[6]) : 1.0;
+  const double nl_eps = argc > 7 ? std::atof(argv[7]) : 1e-10;
+  const size_t nl_maxit = argc > 8 ? size_t(std::atoi(argv[8])) : 10;
 
   Output::setVerbosity(1);
   TDatabase database;
@@ -114,8 +133,14 @@ int main(int argc, char** argv) {
   db.merge(ParameterDatabase::default_nonlinit_database());
   db.merge(LocalAssembling3D::default_local_assembling_database());
   db.merge(Example_NSE3D::default_example_database());
-  db["problem_type"].set<size_t>(3);
+  db["problem_type"].set<size_t>(nse_mode ? 5 : 3);
   db["example"] = -3;
+  if (nse_mode) {
+    db["nse_nonlinear_form"] = "convective";
+    db["reynolds_number"] = reynolds;
+    db["nonlinloop_epsilon"] = nl_eps;
+    db["nonlinloop_maxit"] = nl_maxit;
+  }
   db["space_discretization_type"] = "galerkin";
   db.add("boundary_file", "Default_UnitCube", "");
   db.add("geo_file", "Default_UnitCube_Tetra", "");
@@ -130,18 +155,73 @@ int main(int argc, char** argv) {
     db["multigrid_n_levels"] = n_levels;
     db["multigrid_smoother"] = "nodal_vanka";
     db["multigrid_smoother_coarse"] = "direct_solve";
+    if (solver == "mg") {
+      db["gmres_restart"] = size_t(20);
+      db["max_n_iterations"] = size_t(100);
+      db["residual_tolerance"] = 1e-12;
+      db["residual_reduction"] = 0.0;
+      db["multigrid_cycle_type"] = "V";
+      db["multigrid_n_pre_smooth"] = size_t(1);
+      db["multigrid_n_post_smooth"] = size_t(1);
+      db["multigrid_vanka_damp_factor"] = 1.0;
+      db["multigrid_correction_damp_factor"] = 1.0;
+    }
   }
   TDatabase::ParamDB->VELOCITY_SPACE = 2;
   TDatabase::ParamDB->PRESSURE_SPACE = -4711;
   TDatabase::ParamDB->NSTYPE = 4;
   TDatabase::ParamDB->LAPLACETYPE = 0;
-  TDatabase::ParamDB->FLOW_PROBLEM_TYPE = 3;
+  TDatabase::ParamDB->FLOW_PROBLEM_TYPE = nse_mode ? 5 : 3;
+  TDatabase::ParamDB->SC_NONLIN_ITE_TYPE_SADDLE = 0;
   check_parameters_consistency_NSE(db);
 
   TDomain domain(db);
   domain.refine_and_get_hierarchy_of_collections(db);
-  RefStokes nse(domain, db, make_example());
+  RefStokes nse(domain, db, nse_mode ? Example_NSE3D(db) : make_example());
   nse.assemble_linear_terms();
+
+  if (nse_mode && solver != "none") {
+    // the nonlinear loop of the reference's nse3d_solvers_test
+    std::FILE* meta = std::fopen((out + "/meta.txt").c_str(), "w");
+    std::fprintf(meta, "n_refine %zu\nlevels %zu\n", n_refine, nse.systems.size());
+    nse.stop_it(0);
+    std::fprintf(meta, "res 0 %.17g %.17g %.17g\n", nse.get_impuls_residual(), nse.get_mass_residual(),
+                 nse.get_full_residual());
+    for (unsigned k = 1;; ++k) {
+      nse.solve();
+      const unsigned lin = solver == "mg" ? nse.solver.get_solver_loop_info().get_n_previous_iterations() : 0;
+      nse.assemble_nonlinear_term();
+      const bool stop = nse.stop_it(k);
+      std::fprintf(meta, "res %u %.17g %.17g %.17g\nlin %u %u\n", k, nse.get_impuls_residual(),
+                   nse.get_mass_residual(), nse.get_full_residual(), k, lin);
+      if (stop) break;
+    }
+    nse.output();
+    const auto e = nse.get_errors();
+    std::fprintf(meta, "errors");
+    for (double v : e) std::fprintf(meta, " %.17g", v);
+    std::fprintf(meta, "\n");
+    const auto& s = nse.systems.front();
+    dump(out + "/solution.f64", s.solution.get_entries(), s.solution.length());
+    std::fclose(meta);
+    return 0;
+  }
+  if (nse_mode) {
+    // a fixed finest velocity, restricted to every level by the nonlinear
+    // assembly
+    auto& f = nse.systems.front().solution;
+    for (int b = 0; b < 3; ++b) {
+      double* u = f.block(b);
+      for (size_t i = 0; i < f.length(b); ++i) u[i] = std::sin(0.7 * double(i) + 1.3 * b + 0.1);
+    }
+    nse.assemble_nonlinear_term();
+    int level = 0;
+    for (auto& s : nse.systems) {
+      dump(out + "/L" + std::to_string(level) + "_velocity.f64", s.solution.get_entries(),
+           3 * s.solution.length(0));
+      ++level;
+    }
+  }
 
   std::FILE* meta = std::fopen((out + "/meta.txt").c_str(), "w");
   std::fprintf(meta, "n_refine %zu\nlevels %zu\n", n_refine, nse.systems.size());

@@ -28,6 +28,17 @@ combined matrix of BlockFEMatrix::get_combined_matrix (the pressure
 projection applied, exact zeros removed) with the right-hand side; on the
 smallest mesh also the direct solve's solution.
 
+The nse_* cases run the same driver in its Navier-Stokes mode: problem_type 5,
+the convective form and the reference's own example -3 (whose coefficients
+hold the convective term) at a Reynolds number, through the nonlinear loop of
+the reference's test/nse3d_solvers_test.c++ (assemble_linear_terms,
+stop_it(0), then solve / assemble_nonlinear_term / stop_it(k)). They keep the
+impuls, mass and full residual of every nonlinear step, the FGMRES iterations
+of every solve (multigrid cases), the final solution and get_errors(). The
+nse_*_nl case instead sets a fixed finest velocity, calls
+assemble_nonlinear_term once and keeps every level's restricted velocity and
+combined matrix (the convective term and GridTransfer::RestrictFunction).
+
     python tests/golden/make_ref_fixtures.py            # all cases
     python tests/golden/make_ref_fixtures.py cd3d_q2_8  # one case
 """
@@ -77,6 +88,15 @@ CASES = {
 STOKES_CASES = {
     "stokes_p2p1_4": (2, 2, True, True),
     "stokes_p2p1_8": (3, 3, False, False),
+}
+
+# name: (refinements, levels, solver (direct | mg | none), Reynolds number,
+#        nonlinloop_epsilon, nonlinloop_maxit)
+NSE_CASES = {
+    "nse_p2p1_4": (2, 1, "direct", 1.0, 1e-10, 10),
+    "nse_p2p1_4_re100": (2, 1, "direct", 100.0, 1e-10, 30),
+    "nse_p2p1_8_mg": (3, 3, "mg", 10.0, 1e-10, 10),
+    "nse_p2p1_8_nl": (3, 3, "none", 1.0, 1e-10, 10),
 }
 
 
@@ -192,9 +212,60 @@ def run_stokes_case(name: str) -> None:
     print(f"{name}: {nlev} levels" + (", direct solution" if direct else ""))
 
 
+def run_nse_case(name: str) -> None:
+    import build_ref
+    nref, nlev, solver, re, eps, maxit = NSE_CASES[name]
+    exe = build_ref.link_program("3", build_ref.HERE / "ref_stokes.C", build_ref.OUT / "ref_stokes3d")
+    out: dict[str, np.ndarray] = {"config": np.array([nref, nlev, maxit], dtype=np.int64),
+                                  "params": np.array([re, eps]), "solver": np.array(solver)}
+    with tempfile.TemporaryDirectory() as tmp:
+        subprocess.run([str(exe), tmp, str(nref), str(nlev), solver, "nse", repr(re), repr(eps), str(maxit)],
+                       check=True, capture_output=True)
+        lines = Path(tmp, "meta.txt").read_text().splitlines()
+        if solver == "none":
+            for rl in range(nlev):
+                lvl = nlev - 1 - rl
+                info = next(l for l in lines if l.startswith(f"L{rl} ")).split()[1:]
+                kv = dict(zip(info[0::2], map(int, info[1::2])))
+                rd = lambda n, t: np.fromfile(Path(tmp, f"L{rl}_{n}"), dtype=t)
+                rows, cols, vals = rd("rows.i32", np.int32), rd("cols.i32", np.int32), rd("vals.f64", np.float64)
+                p = f"L{lvl}_"
+                out[p + "sizes"] = np.array([kv["cells"], kv["u_n_dofs"], kv["u_active"], kv["p_n_dofs"], kv["nnz"]],
+                                            np.int64)
+                out[p + "velocity"] = rd("velocity.f64", np.float64)
+                out[p + "vals_max"] = np.array(np.abs(vals).max())
+                if lvl == 0:
+                    out[p + "rows"], out[p + "cols"], out[p + "vals"] = rows, cols, vals
+                else:
+                    idx = sample_idx(vals.size)
+                    row_of = np.repeat(np.arange(rows.size - 1, dtype=np.int32), np.diff(rows))
+                    out[p + "sample_rows"], out[p + "sample_cols"] = row_of[idx], cols[idx]
+                    out[p + "sample_vals"] = vals[idx]
+        else:
+            res = [list(map(float, l.split()[2:])) for l in lines if l.startswith("res ")]
+            lin = [int(l.split()[2]) for l in lines if l.startswith("lin ")]
+            out["residuals"] = np.array(res)
+            # the solver's LoopInfo counts iterations over all solves
+            out["linear_iterations"] = np.diff(np.array([0] + lin, dtype=np.int64))
+            out["errors"] = np.array([float(v) for v in next(l for l in lines if l.startswith("errors")).split()[1:]])
+            sol = np.fromfile(Path(tmp, "solution.f64"), dtype=np.float64)
+            if sol.size <= 4 * SAMPLES:
+                out["solution"] = sol
+            else:
+                idx = sample_idx(sol.size)
+                out["solution_idx"], out["solution"] = idx, sol[idx]
+    np.savez_compressed(HERE / f"ref_{name}.npz", **out)
+    if "residuals" in out:
+        print(f"{name}: {len(out['residuals']) - 1} nonlinear steps, residual {out['residuals'][-1][2]:.3e}")
+    else:
+        print(f"{name}: {nlev} levels after one nonlinear assembly")
+
+
 if __name__ == "__main__":
-    for n in (sys.argv[1:] or list(CASES) + list(STOKES_CASES)):
+    for n in (sys.argv[1:] or list(CASES) + list(STOKES_CASES) + list(NSE_CASES)):
         if n in STOKES_CASES:
             run_stokes_case(n)
+        elif n in NSE_CASES:
+            run_nse_case(n)
         else:
             run_case(n)

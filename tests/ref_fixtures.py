@@ -19,11 +19,18 @@ _POINTS = {0: 2, 1: 2, 2: 2, 3: 3, 4: 3, 5: 3, 6: 4, 7: 4}
 
 def names() -> list[str]:
     """the convection-diffusion cases"""
-    return sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_*.npz") if not p.stem.startswith("ref_stokes"))
+    return sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_*.npz")
+                  if not p.stem.startswith(("ref_stokes", "ref_nse")))
 
 
 def stokes_names() -> list[str]:
     return sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_stokes*.npz"))
+
+
+def nse_names(solver: str | None = None) -> list[str]:
+    """the Navier-Stokes cases (of one solver: direct, mg or none)"""
+    out = sorted(p.stem[len("ref_"):] for p in GOLDEN.glob("ref_nse*.npz"))
+    return [n for n in out if solver is None or NseRefCase(n).solver == solver]
 
 
 class RefCase:
@@ -127,3 +134,40 @@ class StokesRefCase:
         assert np.all(ours_key[pos_c] == ref_key), "an entry of the reference is outside the pattern"
         diff_ref = np.abs(vals[pos_c] - ref_val).max()
         return float(max(diff_ours, diff_ref) / float(d["vals_max"]))
+
+
+class NseRefCase(StokesRefCase):
+    """a Navier-Stokes fixture: NavierStokes<3> (problem_type 5, convective
+    form, example -3) of the reference through the nonlinear loop of
+    test/nse3d_solvers_test.c++ (solver direct or mg: residuals of every step,
+    linear iterations, solution, errors), or one assemble_nonlinear_term with
+    a fixed finest velocity (solver none: every level's matrix and velocity)"""
+
+    def __init__(self, name: str):
+        self.name = name
+        self.z = np.load(GOLDEN / f"ref_{name}.npz")
+        self.n_refine, self.n_levels, self.maxit = (int(v) for v in self.z["config"])
+        self.reynolds, self.epsilon = (float(v) for v in self.z["params"])
+        self.solver = str(self.z["solver"])
+
+    def level(self, l: int) -> dict:
+        p = f"L{l}_"
+        d = {k[len(p):]: self.z[k] for k in self.z.files if k.startswith(p)}
+        cells, nu, nua, np_, nnz = (int(v) for v in d["sizes"])
+        d.update(cells=cells, nu=nu, nu_active=nua, np=np_, nnz=nnz)
+        return d
+
+    def fixed_velocity(self, nu: int, n: int) -> np.ndarray:
+        """the finest solution the nonlinear assembly case starts from:
+        u_b[i] = sin(0.7 i + 1.3 b + 0.1), pressure 0"""
+        x = np.zeros(n)
+        i = np.arange(nu)
+        for b in range(3):
+            x[b * nu:(b + 1) * nu] = np.sin(0.7 * i + 1.3 * b + 0.1)
+        return x
+
+    def full_solution(self, n: int):
+        """(indices, values) of the stored solution"""
+        if "solution_idx" in self.z.files:
+            return self.z["solution_idx"], self.z["solution"]
+        return np.arange(n), self.z["solution"]
