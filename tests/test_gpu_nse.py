@@ -79,8 +79,9 @@ def test_gpu_nonlinear_assembly_matches_the_oracle_after_a_solve(ctx):
             v, ref = prob.matrix(l).values(), o.vals[l]
             assert np.abs(v - ref).max() <= 1e-13 * np.abs(ref).max(), l
         g, r = prob.residuals(), o.residuals()
-        assert abs(g[0] - r[0]) <= 1e-10 * r[0] + 1e-14
-        assert abs(g[1] - r[1]) <= 1e-10 * max(r[1], 1e-12)
+        # the mass residual after a solve is at rounding level (about 1e-13)
+        assert abs(g[0] - r[0]) <= 1e-10 * r[0] + 1e-13
+        assert abs(g[1] - r[1]) <= 1e-10 * r[1] + 1e-13
     finally:
         prob.close()
         disc.close()
