@@ -55,6 +55,18 @@ WORKLOADS = {
                                   "pressure DOFs), FGMRES(30) + MG V(1,1) nodal Vanka (colour order, damping "
                                   "0.8), 3 levels, coarse level: additive nodal Vanka, at most 10 sweeps down "
                                   "to a 0.1 residual, to 1e-8"),
+    # Navier-Stokes (convective form) at Reynolds number 10 on the same mesh:
+    # the reference's example -3 of test/nse3d_solvers_test.c++; one request =
+    # assemble_linear_terms + the Picard loop to a 1e-10 nonlinear residual
+    "nse3d_p2p1_24": dict(kind="nse", geometry=2, root_n=3, n_refine=3, n_levels=3, elem=12, nu=0.1,
+                          restart=30, reduction=1e-8, smoother="nodal_vanka", coarse="nodal_vanka_jacobi",
+                          damp=0.8, pre=1, post=1, nl_epsilon=1e-10, nl_maxit=30,
+                          sample=dict(root_n=3, n_refine=1, n_levels=1),
+                          desc="3D Navier-Stokes P2/P1 (convective form, Picard), Reynolds number 10, "
+                               "24^3 cubes x 6 tetrahedra (352,947 velocity + 15,625 pressure DOFs), "
+                               "example -3 of the reference's NSE test; each nonlinear step FGMRES(30) + "
+                               "MG V(1,1) nodal Vanka (colour order, damping 0.8), 3 levels, to 1e-8 "
+                               "relative; nonlinear loop to a 1e-10 residual"),
 }
 
 
@@ -76,6 +88,11 @@ def solver_db(w, precision):
     db["multigrid_n_pre_smooth"] = w.get("pre", 2)
     db["multigrid_n_post_smooth"] = w.get("post", 2)
     db["gpu_precision"] = precision
+    if w.get("kind") == "nse":
+        db.add("example", -3)
+        db.add("problem_type", 5)
+        db.add("nonlinloop_epsilon", w["nl_epsilon"])
+        db.add("nonlinloop_maxit", w["nl_maxit"])
     return db
 
 
@@ -205,7 +222,8 @@ def run_ours(args, w, rank, world, local, pg):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
 
     ctx = m.Context(local)
-    stokes = w.get("kind") == "stokes"
+    nse = w.get("kind") == "nse"
+    stokes = w.get("kind") in ("stokes", "nse")
     disc = m.Discretization(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"],
                             m.KIND_STOKES if stokes else m.KIND_CD, w["elem"])
     cf = None if stokes else m.cd_coeffs(w["eps"], w["b"], 0.0, True)
@@ -219,20 +237,27 @@ def run_ours(args, w, rank, world, local, pg):
             return m.StokesProblem(ctx, disc, w["nu"], solver_db(w, precision))
         return m.ConvectionDiffusion(ctx, disc, cf, solver_db(w, precision), quad_points=w["quad"])
 
+    def solve(prob):
+        # a Navier-Stokes request runs the nonlinear loop
+        if nse:
+            return len(prob.solve_nonlinear()) - 1
+        prob.solve()
+        return 1
+
     results = {}
     for precision in ("fp64", "mixed"):
         prob = make_problem(precision)
         for _ in range(args.warmup):
             prob.reset_solution()
             prob.assemble()
-            prob.solve()
+            solve(prob)
         # phase split of one request (device time)
         prob.reset_solution()
         ctx.time_begin()
         prob.assemble()
         asm_ms = ctx.time_end()
         ctx.time_begin()
-        prob.solve()
+        nl_steps = solve(prob)
         solve_ms = ctx.time_end()
         its = []
         step_ms = []
@@ -248,7 +273,7 @@ def run_ours(args, w, rank, world, local, pg):
             ctx_t = time.perf_counter()
             prob.reset_solution()
             prob.assemble()
-            prob.solve()
+            solve(prob)
             step_ms.append((time.perf_counter() - ctx_t) * 1e3)
             its.append(prob.last_info()[0])
         dev_ms = ctx.time_end()
@@ -273,7 +298,7 @@ def run_ours(args, w, rank, world, local, pg):
             for _ in range(min(args.steps, 3)):
                 prob.reset_solution()
                 prob.assemble()
-                prob.solve()
+                solve(prob)
             probe = ctx.probe_result()
             ctx.probe(0)
             ctx.set_option("probe_nodal", 0)
@@ -283,6 +308,7 @@ def run_ours(args, w, rank, world, local, pg):
         ms = max_over_ranks(pg, dev_ms)
         results[precision] = dict(ms=ms, wall=wall, its=its, step_ms=step_ms, launches=launches,
                                   clocks=clocks, probe=probe, info=prob.last_info(), solution=prob.solution(),
+                                  nl_steps=nl_steps,
                                   split={"assembly_ms": round(asm_ms, 3), "solve_ms": round(solve_ms, 3)})
         if precision == "mixed":
             keep_prob = prob
@@ -356,11 +382,15 @@ def run_ours(args, w, rank, world, local, pg):
                    "l2": "inputs larger than L2: finest FP64 matrix "
                          f"{(nnz * 12 + n_dofs * 4) / 1e6:.0f} MB > 126 MB L2",
                    "smoother": w.get("smoother", "jacobi"),
-                   "step": "assembly of all levels + FGMRES/MG solve to "
-                           f"{w['reduction']:g} relative FP64 residual"},
+                   "step": ("assemble_linear_terms + Picard loop (per step: FGMRES/MG solve to "
+                            f"{w['reduction']:g} relative, restriction of the velocity, assembly of the "
+                            f"convective term on all levels) to a {w.get('nl_epsilon', 0):g} nonlinear residual"
+                            if nse else "assembly of all levels + FGMRES/MG solve to "
+                            f"{w['reduction']:g} relative FP64 residual")},
         "dofs_per_s": round(solves_s * n_dofs, 1),
         "fgmres_iterations": mixed["its"][-1],
         "final_relative_residual": mixed["info"][1] / mixed["info"][2],
+        "nonlinear_steps": {"mixed": mixed["nl_steps"], "fp64": fp64["nl_steps"]} if nse else None,
         "phase_ms": mixed["split"],
         "fp64": {"value": round(fp64_solves_s, 3), "unit": "solves/s", "ms_per_step": round(fp64["ms"] / K, 3),
                  "fgmres_iterations": fp64["its"][-1], "dofs_per_s": round(fp64_solves_s * n_dofs, 1),
@@ -426,6 +456,15 @@ def _oracle_solve(wname):
     """one oracle (CPU) request: assembly of all levels + FGMRES/MG solve"""
     from oracle import cd as ocd
     w = WORKLOADS[wname]
+    if w.get("kind") == "nse":
+        # the bounded sample: the nonlinear loop with the direct solver on the
+        # 6^3 mesh of the family
+        from oracle import nse as onse
+        smp = w["sample"]
+        o = onse.OracleNSE(smp["root_n"], smp["n_refine"], smp["n_levels"], 1.0 / w["nu"])
+        t0 = time.perf_counter()
+        hist = o.run(w["nl_epsilon"], w["nl_maxit"])
+        return time.perf_counter() - t0, len(hist) - 1, 0, o.levels[-1].n
     if w.get("kind") == "stokes":
         # the bounded sample: the same family on the 12^3 mesh (three levels)
         from oracle import stokes as ost
@@ -458,6 +497,11 @@ def cpu_baseline(w, n_dofs):
                           f"of the same workload by the C restatement in oracle/, single thread, {dt:.1f} s"}
     # a smaller mesh of the same family, scaled by the DOF ratio (work per
     # request grows at least linearly with the DOFs, so this overstates the CPU)
+    if w.get("kind") == "nse":
+        return {"value": round(n_sample / n_dofs / dt, 6), "unit": "solves/s", "cores": 1, "kind": "port",
+                "sample": f"one full nonlinear request on the 6^3 mesh of the same family ({n_sample} DOFs, "
+                          f"{it} Picard steps with a sparse direct solve each, {dt:.1f} s, oracle/nse.py "
+                          f"on scipy), scaled by {n_sample}/{n_dofs} DOFs"}
     return {"value": round(n_sample / n_dofs / dt, 6), "unit": "solves/s", "cores": 1, "kind": "port",
             "sample": f"one full request on the 12^3 mesh of the same family ({n_sample} DOFs, {it} "
                       f"iterations, {dt:.1f} s single thread, C restatement in oracle/), scaled by "
@@ -485,13 +529,23 @@ def run_reference(args, w, rank, world):
         dt = time.perf_counter() - t0
     value = steps * cores / dt
     scale_note = ""
-    if w.get("kind") == "stokes":
-        # the CPU runs the 12^3 mesh of the family; scaled to the 24^3 workload by DOFs
+    if w.get("kind") in ("stokes", "nse"):
+        # the CPU runs a smaller mesh of the family; scaled to the 24^3 workload by DOFs
         import mymoonmd_gb300 as m
         d = m.Discretization(w["geometry"], w["root_n"], w["n_refine"], w["n_levels"], m.KIND_STOKES, w["elem"])
         n_full = 3 * d.level_info(w["n_levels"] - 1)["n_dofs"] + d.level_info(w["n_levels"] - 1, 1)["n_dofs"]
         value *= n_sample / n_full
-        scale_note = f"; requests on the 12^3 mesh ({n_sample} DOFs) scaled by {n_sample}/{n_full} DOFs"
+        scale_note = (f"; requests on the {'6' if w.get('kind') == 'nse' else '12'}^3 mesh ({n_sample} DOFs) "
+                      f"scaled by {n_sample}/{n_full} DOFs")
+    last = its[-1] if its else 0
+    if w.get("kind") == "nse":
+        what = (f"nonlinear requests ({last} Picard steps with a sparse direct solve each, the restatement "
+                "oracle/nse.py on scipy)")
+    else:
+        what = (f"requests (assembly + FGMRES/MG, {last} iterations), C restatement in oracle/ (the "
+                "reference is compiled from its sources where they are present, which is not this "
+                "machine; its own solve of the 3D Q2 32^3 request takes about the restatement's time on "
+                "one core, 19.4 s on a 2.7 GHz x86 core)")
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "solves/s", "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": round(dt / steps * 1e3, 1), "higher_is_better": True,
@@ -500,12 +554,7 @@ def run_reference(args, w, rank, world):
         "config": {"workload": w["desc"], "parallelism": f"{cores} independent CPU requests per step"},
         "cpu_baseline": {"value": round(value, 5), "unit": "solves/s", "cores": cores, "kind": "port",
                          "sample": f"{steps} step(s) (of {args.steps} requested) of {cores} concurrent full "
-                                   f"requests (assembly + FGMRES/MG, {its[-1] if its else 0} iterations), "
-                                   "one per host core, C restatement in oracle/ (the reference is "
-                                   "compiled from its sources where they are present, which is not this "
-                                   "machine; its own solve of the 3D Q2 32^3 request takes about the "
-                                   "restatement's time on one core, 19.4 s on a 2.7 GHz x86 core)"
-                                   + scale_note},
+                                   + what + ", one per host core" + scale_note},
         "e2e": {"value": round(value, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

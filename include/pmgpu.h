@@ -391,8 +391,9 @@ int pm_problem_solver(pm_problem* p, pm_solver** out);
 int pm_problem_solution_dev(pm_problem* p, double** sol_dev, double** rhs_dev);
 /* One request end to end from host memory: new coefficients, the cell vertex
  * coordinates of every kept level (level_verts[l], NULL = keep the current
- * geometry) copied to the device, assembly of all levels, solve, and the
- * finest-level solution copied back into sol_host. */
+ * geometry) copied to the device, assembly of all levels, solve (for a
+ * Navier-Stokes problem the nonlinear loop of pm_problem_solve_nonlinear), and
+ * the finest-level solution copied back into sol_host. */
 int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* coeffs, const double* const* level_verts,
                         double* sol_host);
 /* Errors of the finest-level solution against the exact solution of the

@@ -1171,7 +1171,9 @@ int pm_problem_run_host(pm_problem* p, const pm_cd_coeffs* cf, const double* con
   PM_CUDA(cudaMemsetAsync(p->sol.p, 0, p->sol.bytes(), c->stream));
   int rc = pm_problem_assemble(p);
   if (rc != PM_OK) return rc;
-  rc = pm_problem_solve(p);
+  // a Navier-Stokes request runs the nonlinear loop
+  rc = (p->kind == KIND_STOKES && p->problem_type == 5) ? pm_problem_solve_nonlinear(p, 0, nullptr, nullptr)
+                                                        : pm_problem_solve(p);
   if (rc != PM_OK) return rc;
   p->sol.download(sol_host, c->stream);
   PM_CUDA(cudaStreamSynchronize(c->stream));
