@@ -71,6 +71,12 @@ int pm_version(void);
  *   "probe_nodal" 0|1 - the launch probe brackets instead the residual and
  *   local-solve pair of every colour of the multiplicative nodal Vanka
  *   sweeps (counted as one launch, with the pair's algorithmic bytes);
+ *   "nodal_sliced" 0|4|8 - the local residuals of a colour of the
+ *   multiplicative nodal Vanka sweep by one sliced-ELL launch over a copy of
+ *   its patches' rows with 4 or 8 lanes per row (8, default; 1 = 4; the copy
+ *   holds every patch row once, laid out when a problem sets up its
+ *   smoothers, values refreshed with the Vanka factors) or by one block per
+ *   patch over the CSR rows (0);
  *   "fp32_sliced_spmv" 0|100 L + 10 U + P - FP32 SpMV-family launches on
  *   matrices with more than 16 entries per row by the sliced-ELL kernel: L
  *   lanes per row (1, 2, 4, 8), U steps in flight (4, 8), P = 1 issues the next

@@ -123,6 +123,13 @@ int pm_ctx_set_option(pm_ctx* c, const char* key, int value) {
     c->probe_nodal = value != 0;
     return PM_OK;
   }
+  if (std::string(key) == "nodal_sliced") {
+    if (value != 0 && value != 1 && value != 4 && value != 8)
+      return fail(c, PM_E_INVALID, "nodal_sliced is 0, 1, 4 or 8");
+    if (value == 1) value = 4;
+    c->nodal_sliced = value;
+    return PM_OK;
+  }
   if (std::string(key) == "probe_precision") {
     if (value != 0 && value != 4 && value != 8) return fail(c, PM_E_INVALID, "probe_precision is 0, 4 or 8");
     c->probe_precision = value;

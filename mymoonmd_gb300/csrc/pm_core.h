@@ -138,6 +138,11 @@ struct pm_ctx {
   // launch probe of the multiplicative nodal Vanka sweeps: events around the
   // residual + local-solve pair of every colour (option "probe_nodal")
   int probe_nodal = 0;
+  // local residuals of the multiplicative nodal Vanka sweep from the
+  // per-colour sliced copy of the patch rows with 4 or 8 lanes per row, or
+  // from the CSR rows, one block per patch (0) (option "nodal_sliced"; read
+  // when a problem lays out its smoothers)
+  int nodal_sliced = 8;
   std::vector<cudaEvent_t> probe_events;  // start/end pairs
   std::vector<double> probe_bytes;        // algorithmic bytes of each probed launch
   std::vector<cudaEvent_t> probe_pool;

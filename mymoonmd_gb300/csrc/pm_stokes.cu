@@ -14,6 +14,7 @@
 // VankaSmoother::smooth (src/Multigrid/VankaSmoother.C:110-292).
 #include <algorithm>
 #include <cmath>
+#include <numeric>
 #include <vector>
 
 #include "pm_stokes.h"
@@ -894,6 +895,123 @@ void DevVanka::sweep_colored32(pm_ctx* c, const DevCsr& V, const float* b, float
 // ------------------------------------------------------- nodal Vanka -------
 namespace pm {
 
+void DevNodalVanka::build_row_slices(pm_ctx* c, const pmsetup::Csr& S, int p0, const std::vector<int>& vp,
+                                     const std::vector<int>& vi, const std::vector<int>& cp) {
+  rs_ok = false;
+  rs_lanes = 0;
+  const int Lanes = c->nodal_sliced == 8 ? 8 : 4, C = 32 / Lanes;
+  if (c->nodal_sliced == 0) return;
+  // the projected structure: row p0 holds only its diagonal
+  auto row_len = [&](int g) { return g == p0 ? 1 : S.row_ptr[g + 1] - S.row_ptr[g]; };
+  auto proj_start = [&](int g) {  // first entry of row g in the projected arrays
+    const int64_t shift = g > p0 ? int64_t(S.row_ptr[p0 + 1] - S.row_ptr[p0]) - 1 : 0;
+    return int64_t(S.row_ptr[g]) - shift;
+  };
+  const size_t n_slots = size_t(3) * vi.size() + size_t(np);
+  std::vector<int> slot_row(n_slots);
+  for (int i = 0; i < np; ++i) {
+    const int m = vp[i + 1] - vp[i];
+    const size_t off = 3 * size_t(vp[i]) + i;
+    for (int e = 0; e < 3 * m; ++e) slot_row[off + e] = (e / m) * nu + vi[vp[i] + e % m];
+    slot_row[off + 3 * m] = 3 * nu + i;
+  }
+  const int ncol = int(color_ptr.size()) - 1;
+  std::vector<int> perm, soff{0}, cols, src;
+  color_slice.assign(size_t(ncol) + 1, 0);
+  std::vector<int> rows;
+  int64_t total = 0;
+  for (int k = 0; k < ncol; ++k) {
+    rows.clear();
+    for (int t = color_ptr[k]; t < color_ptr[k + 1]; ++t) {
+      const int i = cp[t], m = vp[i + 1] - vp[i];
+      const int off = 3 * vp[i] + i;
+      for (int e = 0; e <= 3 * m; ++e) rows.push_back(off + e);
+    }
+    // longest rows first (ties in slot order): slices of similar rows
+    std::stable_sort(rows.begin(), rows.end(),
+                     [&](int a, int b) { return row_len(slot_row[a]) > row_len(slot_row[b]); });
+    const int nsl = int((rows.size() + C - 1) / C);
+    for (int sl = 0; sl < nsl; ++sl) {
+      int width = 0;
+      for (int q = 0; q < C; ++q) {
+        const size_t r = size_t(sl) * C + q;
+        perm.push_back(r < rows.size() ? rows[r] : -1);
+        if (r < rows.size()) width = std::max(width, row_len(slot_row[rows[r]]));
+      }
+      const int T = (width + Lanes - 1) / Lanes;
+      if (total + int64_t(32) * T > int64_t(0x7fffffff)) return;  // the residual kernel stays
+      cols.resize(size_t(total) + size_t(32) * T);
+      src.resize(size_t(total) + size_t(32) * T);
+      for (int q = 0; q < C; ++q) {
+        const size_t r = size_t(sl) * C + q;
+        const int g = r < rows.size() ? slot_row[rows[r]] : -1;
+        const int len = g >= 0 ? row_len(g) : 0;
+        const int64_t base = g >= 0 ? proj_start(g) : 0;
+        auto col_of = [&](int j) { return g == p0 ? p0 : S.cols[S.row_ptr[g] + j]; };
+        const int pad = len > 0 ? col_of(len - 1) : 0;
+        for (int t = 0; t < T; ++t)
+          for (int sub = 0; sub < Lanes; ++sub) {
+            const int j = t * Lanes + sub;
+            const size_t at = size_t(total) + size_t(t) * 32 + size_t(sub) * C + q;
+            cols[at] = j < len ? col_of(j) : pad;
+            src[at] = j < len ? int(base + j) : -1;
+          }
+      }
+      total += int64_t(32) * T;
+      soff.push_back(int(total));
+    }
+    color_slice[size_t(k) + 1] = color_slice[size_t(k)] + nsl;
+  }
+  rs_perm.upload(perm, c->stream);
+  rs_off.upload(soff, c->stream);
+  rs_cols.upload(cols, c->stream);
+  rs_src.upload(src, c->stream);
+  bslot.upload(slot_row, c->stream);
+  PM_CUDA(cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
+  rs_entries = total;
+  rs_lanes = Lanes;
+  rs_ok = true;
+}
+
+// the periodic lattice colouring of the nodal patches (see setup); false if
+// the pressure nodes are not on a 3D lattice or two patches of one colour
+// share a velocity node
+static bool lattice_colours(const pmsetup::Space& ps, const std::vector<int>& vp, const std::vector<int>& vi,
+                            std::vector<int>& color, int& n_colors) {
+  const int np = int(vp.size()) - 1;
+  if (np <= 0 || ps.node.size() != size_t(np) * 3) return false;
+  int64_t spacing = 0;
+  for (int64_t v : ps.node) spacing = std::gcd(spacing, v < 0 ? -v : v);
+  if (spacing <= 0) return false;
+  std::vector<int> raw(np);
+  for (int i = 0; i < np; ++i) {
+    int col = 0, mult = 1;
+    for (int d = 0; d < 3; ++d) {
+      const int64_t k = ps.node[size_t(i) * 3 + d] / spacing;
+      col += int(((k % 3) + 3) % 3) * mult;
+      mult *= 3;
+    }
+    raw[i] = col;
+  }
+  // check: no velocity node in two patches of one colour
+  int nmax = 0;
+  for (int v : vi) nmax = std::max(nmax, v + 1);
+  std::vector<int> mark(size_t(nmax) * 27, 0);
+  for (int i = 0; i < np; ++i)
+    for (int t = vp[i]; t < vp[i + 1]; ++t) {
+      int& m = mark[size_t(vi[t]) * 27 + raw[i]];
+      if (m) return false;
+      m = 1;
+    }
+  int remap[27];
+  bool used[27] = {};
+  for (int i = 0; i < np; ++i) used[raw[i]] = true;
+  n_colors = 0;
+  for (int k = 0; k < 27; ++k) remap[k] = used[k] ? n_colors++ : -1;
+  for (int i = 0; i < np; ++i) color[i] = remap[raw[i]];
+  return true;
+}
+
 void DevNodalVanka::setup(pm_ctx* c, const DiscLevel& L) {
   nu = L.space.n_dofs;
   np = L.pspace.n_dofs;
@@ -942,8 +1060,12 @@ void DevNodalVanka::setup(pm_ctx* c, const DiscLevel& L) {
   inc_ptr.upload(ip, c->stream);
   inc_idx.upload(ix, c->stream);
   count.upload(cnt, c->stream);
-  // greedy colouring in pressure-DOF order: patches of one colour share no
-  // velocity node (and so no DOF)
+  // colouring: patches of one colour share no velocity node (and so no DOF).
+  // On the vertex lattice of the unit-cube meshes the patches of two pressure
+  // vertices share a node only when the vertices are at most two lattice
+  // steps apart in every direction, so (i mod 3) + 3 (j mod 3) + 9 (k mod 3)
+  // is a colouring with 27 colours of equal size; it is checked and used where
+  // it holds, the greedy colouring in pressure-DOF order otherwise
   std::vector<int> np_ptr(nu + 1, 0), np_idx(vi.size());
   for (int v : vi) np_ptr[v + 1]++;
   for (int v = 0; v < nu; ++v) np_ptr[v + 1] += np_ptr[v];
@@ -954,19 +1076,21 @@ void DevNodalVanka::setup(pm_ctx* c, const DiscLevel& L) {
   }
   std::vector<int> color(np, -1), seen;
   int n_colors = 0;
-  for (int i = 0; i < np; ++i) {
-    seen.assign(n_colors + 1, 0);
-    for (int t = vp[i]; t < vp[i + 1]; ++t) {
-      const int v = vi[t];
-      for (int e = np_ptr[v]; e < np_ptr[v + 1]; ++e) {
-        const int j = np_idx[e];
-        if (j < i) seen[color[j]] = 1;
+  if (!lattice_colours(L.pspace, vp, vi, color, n_colors)) {
+    for (int i = 0; i < np; ++i) {
+      seen.assign(n_colors + 1, 0);
+      for (int t = vp[i]; t < vp[i + 1]; ++t) {
+        const int v = vi[t];
+        for (int e = np_ptr[v]; e < np_ptr[v + 1]; ++e) {
+          const int j = np_idx[e];
+          if (j < i) seen[color[j]] = 1;
+        }
       }
+      int col = 0;
+      while (col < n_colors && seen[col]) ++col;
+      color[i] = col;
+      if (col == n_colors) ++n_colors;
     }
-    int col = 0;
-    while (col < n_colors && seen[col]) ++col;
-    color[i] = col;
-    if (col == n_colors) ++n_colors;
   }
   color_ptr.assign(n_colors + 1, 0);
   for (int i = 0; i < np; ++i) color_ptr[color[i] + 1]++;
@@ -977,6 +1101,7 @@ void DevNodalVanka::setup(pm_ctx* c, const DiscLevel& L) {
     for (int i = 0; i < np; ++i) cp[fill[color[i]]++] = i;
   }
   color_patches.upload(cp, c->stream);
+  build_row_slices(c, S, L.pressure_row0, vp, vi, cp);
   color_entries.assign(n_colors, 0);
   color_rows.assign(n_colors, 0);
   color_nodes.assign(n_colors, 0);
@@ -1134,6 +1259,14 @@ __global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int*
 }
 
 template <class T>
+__global__ void k_fill_rows(int64_t n, const int* __restrict__ src, const double* __restrict__ v, T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int k = src[i];
+    out[i] = k >= 0 ? T(v[k]) : T(0);
+  }
+}
+
+template <class T>
 static size_t nodal_factor_smem(int m) {
   return sizeof(T) * (size_t(2) * m * (m + 1) + 10 * size_t(m) + 32) + sizeof(int) * size_t(m);
 }
@@ -1161,6 +1294,21 @@ void DevNodalVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
   }
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
+  if (rs_ok) {
+    // the sliced rows take the projected matrix's values (FP32: rounded FP64)
+    const int g = int(std::max<int64_t>(1, std::min<int64_t>((rs_entries + 255) / 256, int64_t(c->num_sms) * 8)));
+    if (fp32) {
+      rs_vals32.ensure(size_t(rs_entries));
+      bloc32.ensure(sol32.n);
+      k_fill_rows<float><<<g, 256, 0, c->stream>>>(rs_entries, rs_src.p, V.vals.p, rs_vals32.p);
+    } else {
+      rs_vals.ensure(size_t(rs_entries));
+      bloc.ensure(sol.n);
+      k_fill_rows<double><<<g, 256, 0, c->stream>>>(rs_entries, rs_src.p, V.vals.p, rs_vals.p);
+    }
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
   int h = 0;
   PM_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   PM_CUDA(cudaStreamSynchronize(c->stream));
@@ -1171,91 +1319,127 @@ void DevNodalVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
 
 namespace pm {
 
-// one block of 512 threads per patch: local residual (gathered from the
-// global residual r or read from rloc), w_k = A^{-1} r_k for the three
-// components (four threads per row, each summing a quarter of the columns of
-// A^{-1}, combined in a fixed order), the pressure from the Schur complement,
-// u_k = w_k - t_k p; the damped correction is written to the local storage
-// (additive sweep) or added into x (colour sweep)
+// one block of 256 threads per patch (four patches resident per SM, so that
+// the few hundred patches of a colour run in one wave): local residual
+// (gathered from the global residual r or read from rloc), w_k = A^{-1} r_k
+// for the three components (four threads per row, each over a quarter of the
+// columns of A^{-1}, its loads issued twelve at a time, combined in a fixed
+// order), the pressure from the Schur complement, u_k = w_k - t_k p; the
+// damped correction is written to the local storage (additive sweep) or
+// added into x (colour sweep). Every load that does not depend on the local
+// solve (t_k, b_k, 1/S, the node indices and, in the colour sweep, the
+// patch's x values, which no other patch of the colour writes) is issued
+// before the first barrier.
+constexpr int kLocalThreads = 256;
 template <class T>
-__global__ void __launch_bounds__(512) k_nodal_local(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
+__global__ void __launch_bounds__(kLocalThreads, 4) k_nodal_local(const int* __restrict__ guard, int cnt, const int* __restrict__ patches, int nu,
                                                      const int* __restrict__ vptr, const int* __restrict__ vidx,
                                                      const int64_t* __restrict__ aoff, const T* __restrict__ ainv,
                                                      const T* __restrict__ tb, const T* __restrict__ sinv,
                                                      const T* __restrict__ r, const T* __restrict__ rloc,
                                                      T* __restrict__ out, T* __restrict__ x, T damp) {
   if (guarded(guard)) return;  // uniform for the whole grid
-  constexpr int P = 4, R = 128;  // threads per row, rows per pass
+  constexpr int NT = kLocalThreads, P = 4, R = NT / P;  // threads per row, rows per pass
+  constexpr int CH = 12;  // loads of A^{-1} in flight per thread (two rounds for up to 96 nodes)
+  constexpr int E = (3 * kNodalMaxNodes + NT - 1) / NT;  // velocity unknowns per thread
   __shared__ T rl[3 * kNodalMaxNodes + 1];
   __shared__ T w[3 * kNodalMaxNodes];
   __shared__ T part[P][3][R];
-  __shared__ T red[16];
+  __shared__ T red[NT / 32];
   const int idx = blockIdx.x;
   if (idx >= cnt) return;
   const int t = threadIdx.x;
   const int i = patches ? patches[idx] : idx;
-  const int m = vptr[i + 1] - vptr[i];
-  const int* nodes = vidx + vptr[i];
-  const size_t off = 3 * size_t(vptr[i]) + i;
-  for (int e = t; e < 3 * m + 1; e += blockDim.x) {
+  const int v0 = vptr[i];
+  const int m = vptr[i + 1] - v0;
+  const int* nodes = vidx + v0;
+  const size_t off = 3 * size_t(v0) + i;
+  const int rows3 = 3 * m;
+  // loads independent of the solve: thread t owns the velocity unknowns
+  // t, t + NT, ... (3m <= 288)
+  const T* tt = tb + 6 * size_t(v0);
+  T ttv[E], bbv[E], xv[E];
+  int g[E];
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int e = t + k * NT;
+    ttv[k] = bbv[k] = xv[k] = T(0);
+    g[k] = 0;
+    if (e < rows3) {
+      ttv[k] = tt[e];
+      bbv[k] = tt[rows3 + e];
+      g[k] = (e / m) * nu + nodes[e % m];
+      if (x) xv[k] = x[g[k]];
+    }
+  }
+  const T si = sinv[i];
+  T xp = T(0);
+  if (x && t == 0) xp = x[3 * nu + i];
+  for (int e = t; e <= rows3; e += NT) {
     T val;
     if (rloc) {
       val = rloc[off + e];
     } else {
-      const int g = e < 3 * m ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
-      val = r[g];
+      const int gg = e < rows3 ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
+      val = r[gg];
     }
     rl[e] = val;
   }
   __syncthreads();
   const T* A = ainv + aoff[i];
-  const int q = t / R;        // column quarter
-  const int lr = t % R;       // row within the pass
+  const int q = t / R;   // column quarter
+  const int lr = t % R;  // row within the pass
   const int qlen = (m + P - 1) / P;
   const int b0 = q * qlen, b1 = min(m, b0 + qlen);
   for (int a0 = 0; a0 < m; a0 += R) {
     const int a = a0 + lr;
     T s0 = T(0), s1 = T(0), s2 = T(0);
-    if (a < m) {
-#pragma unroll 4
-      for (int bb = b0; bb < b1; ++bb) {
-        const T qv = A[size_t(bb) * m + a];
-        s0 += qv * rl[bb];
-        s1 += qv * rl[m + bb];
-        s2 += qv * rl[2 * m + bb];
+    for (int c0 = b0; c0 < b1; c0 += CH) {
+      T av[CH];
+#pragma unroll
+      for (int u = 0; u < CH; ++u) av[u] = (a < m && c0 + u < b1) ? A[size_t(c0 + u) * m + a] : T(0);
+#pragma unroll
+      for (int u = 0; u < CH; ++u) {
+        if (c0 + u < b1) {
+          s0 += av[u] * rl[c0 + u];
+          s1 += av[u] * rl[m + c0 + u];
+          s2 += av[u] * rl[2 * m + c0 + u];
+        }
       }
     }
     part[q][0][lr] = s0;
     part[q][1][lr] = s1;
     part[q][2][lr] = s2;
     __syncthreads();
-    if (t < R && a < m) {
-      for (int k = 0; k < 3; ++k) w[k * m + a] = ((part[0][k][t] + part[1][k][t]) + part[2][k][t]) + part[3][k][t];
+    for (int e = t; e < 3 * R; e += NT) {
+      const int k = e / R, rr = e % R, aa = a0 + rr;
+      if (aa < m) w[k * m + aa] = ((part[0][k][rr] + part[1][k][rr]) + part[2][k][rr]) + part[3][k][rr];
     }
     __syncthreads();
   }
-  const T* tt = tb + 6 * size_t(vptr[i]);
-  const T* bb = tt + 3 * m;
   T d = T(0);
-  for (int e = t; e < 3 * m; e += blockDim.x) d += bb[e] * w[e];
+#pragma unroll
+  for (int k = 0; k < E; ++k)
+    if (t + k * NT < rows3) d += bbv[k] * w[t + k * NT];
   for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
   if ((t & 31) == 0) red[t >> 5] = d;
   __syncthreads();
-  if (t == 0) {
-    T sum = T(0);
-    for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
-    red[0] = sum;
+  T dsum = T(0);
+#pragma unroll
+  for (int k = 0; k < NT / 32; ++k) dsum += red[k];
+  const T p = si * (rl[rows3] - dsum);
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int e = t + k * NT;
+    if (e < rows3) {
+      const T u = damp * (w[e] - ttv[k] * p);
+      if (x) x[g[k]] = xv[k] + u;
+      else out[off + e] = u;
+    }
   }
-  __syncthreads();
-  const T p = sinv[i] * (rl[3 * m] - red[0]);
-  for (int e = t; e < 3 * m; e += blockDim.x) {
-    const T u = damp * (w[e] - tt[e] * p);
-    if (x) x[(e / m) * nu + nodes[e % m]] += u;
-    else out[off + e] = u;
-  }
   if (t == 0) {
-    if (x) x[3 * nu + i] += damp * p;
-    else out[off + 3 * m] = damp * p;
+    if (x) x[3 * nu + i] = xp + damp * p;
+    else out[off + rows3] = damp * p;
   }
 }
 
@@ -1313,7 +1497,7 @@ static void nodal_jacobi(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T*
                          T* sol, const T* b, T* x, T* r, T damp) {
   if constexpr (sizeof(T) == 8) csr_apply(c, V, EPI_DEFECT, x, r, b, 1.0);
   else csr_apply32(c, V, EPI_DEFECT, x, r, b, 1.0f);
-  k_nodal_local<T><<<nv.np, 512, 0, c->stream>>>(c->guard, nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
+  k_nodal_local<T><<<nv.np, kLocalThreads, 0, c->stream>>>(c->guard, nv.np, nullptr, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p,
                                                           ainv, tb, sinv, r, nullptr, sol, nullptr, damp);
   const int g = std::max(1, std::min((nv.n + 255) / 256, c->num_sms * 16));
   k_vanka_average<T><<<g, 256, 0, c->stream>>>(c->guard, nv.n, nv.inc_ptr.p, nv.inc_idx.p, nv.count.p, sol, x);
@@ -1321,10 +1505,37 @@ static void nodal_jacobi(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T*
   c->kernel_launches += 2;
 }
 
+// bloc[slot] = b[global row of the slot]
+template <class T>
+__global__ void k_gather_slots(const int* __restrict__ guard, int n, const int* __restrict__ rows,
+                               const T* __restrict__ b, T* __restrict__ out) {
+  if (guarded(guard)) return;  // uniform for the whole grid
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = b[rows[i]];
+}
+
 template <class T>
 static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T* vals, const T* ainv, const T* tb,
                           const T* sinv, T* rloc, const T* b, T* x, T damp) {
   const int ncol = int(nv.color_ptr.size()) - 1;
+  const T* rsv = nullptr;
+  T* bl = nullptr;
+  if constexpr (sizeof(T) == 4) {
+    rsv = nv.rs_vals32.p;
+    bl = nv.bloc32.p;
+  } else {
+    rsv = nv.rs_vals.p;
+    bl = nv.bloc.p;
+  }
+  const bool sliced = nv.rs_ok && rsv && bl && c->nodal_sliced != 0;
+  BlockMask mg{};
+  mg.guard = c->guard;
+  if (sliced) {
+    const int n = int(nv.bslot.n);
+    const int g = std::max(1, std::min((n + 255) / 256, c->num_sms * 8));
+    k_gather_slots<T><<<g, 256, 0, c->stream>>>(c->guard, n, nv.bslot.p, b, bl);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+  }
   for (int k = 0; k < ncol; ++k) {
     const int beg = nv.color_ptr[k], cnt = nv.color_ptr[k + 1] - beg;
     if (!cnt) continue;
@@ -1340,9 +1551,20 @@ static void nodal_colored(pm_ctx* c, DevNodalVanka& nv, const DevCsr& V, const T
       c->probe_bytes.push_back(double(nv.color_entries[k]) * (2 * eb + 4) + double(nv.color_rows[k]) * 5 * eb +
                                double(nv.color_msq[k]) * eb + double(nv.color_nodes[k]) * 6 * eb + double(cnt) * eb);
     }
-    k_nodal_rhs<T><<<cnt, 512, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
-                                                        V.cols.p, vals, b, x, rloc);
-    k_nodal_local<T><<<cnt, 512, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
+    if (sliced) {
+      // the colour's local residuals as one sliced SpMV: rloc[slot] = bloc[slot] - (V x)[row]
+      const int s0 = nv.color_slice[k], ns = nv.color_slice[k + 1] - s0;
+      if (nv.rs_lanes == 8)
+        sell_kernel<T, 8, 8, true, EPI_DEFECT><<<(ns + 3) / 4, 128, 0, c->stream>>>(
+            ns, nv.rs_perm.p + size_t(s0) * 4, nv.rs_off.p + s0, nv.rs_cols.p, rsv, x, rloc, bl, nullptr, T(0), mg);
+      else
+        sell_kernel<T, 4, 8, true, EPI_DEFECT><<<(ns + 3) / 4, 128, 0, c->stream>>>(
+            ns, nv.rs_perm.p + size_t(s0) * 8, nv.rs_off.p + s0, nv.rs_cols.p, rsv, x, rloc, bl, nullptr, T(0), mg);
+    } else {
+      k_nodal_rhs<T><<<cnt, 512, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, V.row_ptr.p,
+                                                  V.cols.p, vals, b, x, rloc);
+    }
+    k_nodal_local<T><<<cnt, kLocalThreads, 0, c->stream>>>(c->guard, cnt, pts, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, ainv,
                                                           tb, sinv, nullptr, rloc, nullptr, x, damp);
     c->kernel_launches += 2;
     if (c->probe_nodal) {

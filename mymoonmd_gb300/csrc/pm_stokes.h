@@ -160,7 +160,22 @@ struct DevNodalVanka {
   DBuf<double> sol;  // local corrections / residuals: patch i at 3 vptr[i] + i, 3 n_i + 1 entries
   DBuf<float> sol32;
   DBuf<int> flag;
+  // the rows of every patch as a sliced-ELL copy of the projected matrix,
+  // colour by colour (the layout of the sliced SpMV, four lanes per row):
+  // the local residuals of one colour are one SpMV-shaped launch over its
+  // slices, rs_perm mapping each sliced row to its slot in the local storage.
+  // Slices of colour k: color_slice[k] .. color_slice[k+1]. bslot: the global
+  // row of each slot (the smoother's right-hand side gathered once per sweep)
+  bool rs_ok = false;
+  int rs_lanes = 0;  // lanes per row of the copy (4 or 8)
+  std::vector<int> color_slice;
+  int64_t rs_entries = 0;
+  DBuf<int> rs_perm, rs_off, rs_cols, rs_src, bslot;
+  DBuf<float> rs_vals32, bloc32;
+  DBuf<double> rs_vals, bloc;
   void setup(pm_ctx* c, const DiscLevel& L);
+  void build_row_slices(pm_ctx* c, const pmsetup::Csr& S, int p0, const std::vector<int>& vp,
+                        const std::vector<int>& vi, const std::vector<int>& cp);
   void factor(pm_ctx* c, const DevCsr& V, bool fp32);
   // additive sweep: x += average of damp * local corrections from one residual
   void sweep_jacobi(pm_ctx* c, const DevCsr& V, const double* b, double* x, double* r, double damp);

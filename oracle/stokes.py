@@ -179,11 +179,37 @@ def _greedy_colours(members: list, n_shared: int):
     return (np.cumsum(cp).astype(np.int32), np.argsort(color, kind="stable").astype(np.int32), n_colors)
 
 
+def _lattice_colours(members: list, n_shared: int, coords: np.ndarray):
+    """the periodic colouring (i mod 3) + 3 (j mod 3) + 9 (k mod 3) of patches
+    whose anchors lie on a lattice (coords: integer lattice coordinates of each
+    patch's anchor), or None where two patches of one colour share an entry
+    of `members`; colours in ascending order, patches in patch order inside"""
+    spacing = int(np.gcd.reduce(coords.ravel().astype(np.int64)))
+    if spacing <= 0:
+        return None
+    ijk = coords.astype(np.int64) // spacing
+    color = (ijk[:, 0] % 3) + 3 * (ijk[:, 1] % 3) + 9 * (ijk[:, 2] % 3)
+    owner = np.full((27, n_shared), False)
+    for p, mem in enumerate(members):
+        if owner[color[p], mem].any():
+            return None
+        owner[color[p], mem] = True
+    used = np.unique(color)
+    remap = np.full(27, -1)
+    remap[used] = np.arange(used.size)
+    color = remap[color]
+    n_colors = int(used.size)
+    cp = np.zeros(n_colors + 1, dtype=np.int64)
+    np.add.at(cp, color + 1, 1)
+    return (np.cumsum(cp).astype(np.int32), np.argsort(color, kind="stable").astype(np.int32), n_colors)
+
+
 def nodal_patches(lv: "StokesLevel"):
     """VankaType::NODAL patches (VankaSmoother::set_up_pressure_patches /
     set_up_velocity_patches, src/Multigrid/VankaSmoother.C:302-420): pressure
     DOF i with the velocity nodes in row i of the coupling block B1, all three
-    components; returns (ptr, dofs, colour_ptr, colour_patches, n_colours)"""
+    components; returns (ptr, dofs, colour_ptr, colour_patches, n_colours) with
+    the library's colouring of the patches for the colour-ordered sweep"""
     if getattr(lv, "_nodal", None) is None:
         nu, rp, ci = lv.nu, lv.row_ptr, lv.cols
         vel, dofs, ptr = [], [], [0]
@@ -194,7 +220,10 @@ def nodal_patches(lv: "StokesLevel"):
             vel.append(vn)
             dofs.append(np.concatenate([vn + k * nu for k in range(3)] + [np.array([r])]))
             ptr.append(ptr[-1] + dofs[-1].size)
-        cptr, cpat, nc = _greedy_colours(vel, nu)
+        # the library's colouring: periodic on the vertex lattice where that is
+        # conflict-free (27 colours of equal size), greedy otherwise
+        lat = _lattice_colours(vel, nu, lv.pcoords)
+        cptr, cpat, nc = lat if lat is not None else _greedy_colours(vel, nu)
         lv._nodal = (np.array(ptr, dtype=np.int32), np.ascontiguousarray(np.concatenate(dofs), dtype=np.int32),
                      cptr, cpat, nc)
     return lv._nodal

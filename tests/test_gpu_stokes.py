@@ -203,3 +203,37 @@ def test_stokes_workload_multigrid_matches_oracle(ctx):
     rd = m.DeviceVector(ctx, z.size)
     prob.solver().apply_preconditioner(zd, rd)
     assert rel(rd.numpy(), ora.mg_apply(z)) <= 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nodal_sweep_sliced_rows_match_the_patch_rows(ctx, precision):
+    """the colour's local residuals from the sliced copy of the patch rows
+    (nodal_sliced 4, the default, or 8 lanes per row) and from the CSR rows,
+    one block per patch (nodal_sliced 0): one multigrid cycle within rounding
+    (1e-12 FP64, 1e-5 FP32) and the same FGMRES iterations"""
+    db = stokes_db(3, "nodal_vanka", 0.8, coarse="nodal_vanka_jacobi", max_it=100, reduction=1e-8,
+                   precision=precision)
+    db["multigrid_coarse_max_n_iterations"] = 10
+    db["multigrid_coarse_residual"] = 0.1
+    out = {}
+    try:
+        for sliced in (4, 8, 0):
+            ctx.set_option("nodal_sliced", sliced)
+            disc = m.Discretization(m.GEO_CUBE_TETRA, 2, 3, 3, m.KIND_STOKES, 12)
+            prob = m.StokesProblem(ctx, disc, 1.0, db)
+            prob.assemble()
+            prob.solve()
+            z = np.random.default_rng(5).standard_normal(prob.size()[0])
+            zd = m.DeviceVector.from_numpy(ctx, z)
+            rd = m.DeviceVector(ctx, z.size)
+            prob.solver().apply_preconditioner(zd, rd)
+            out[sliced] = (prob.last_info()[0], prob.solution(), rd.numpy())
+            prob.close()
+            disc.close()
+    finally:
+        ctx.set_option("nodal_sliced", 8)
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    for lanes in (4, 8):
+        assert rel(out[lanes][2], out[0][2]) <= tol
+        assert abs(out[lanes][0] - out[0][0]) <= (0 if precision == "fp64" else 1)
+        assert rel(out[lanes][1], out[0][1]) <= 1e-7

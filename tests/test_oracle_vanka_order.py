@@ -7,11 +7,12 @@ iterates differ and the solutions agree to the solver tolerance.
 
 Measured with the oracle (FGMRES(30) to a 1e-10 residual reduction, V(1,1)
 nodal Vanka on three levels, direct coarse solve, P2/P1 on 2^3 x 6 and 3^3 x 6
-root tetrahedra refined twice):
-  damping 1.0: 20 (sequential) vs 17 (colours) iterations on the 2^3 root,
-               23 vs 21 on the 3^3 root;
+root tetrahedra refined twice; the 27 colours of the periodic lattice
+colouring the library uses):
+  damping 1.0: 20 (sequential) vs 18 (colours) iterations on the 2^3 root,
+               23 vs 25 on the 3^3 root;
   damping 0.8: 14 vs 13 on both;
-  velocities agree within 3e-10, mean-free pressures within 1e-6.
+  velocities agree within 4e-10, mean-free pressures within 1.4e-6.
 """
 import numpy as np
 import pytest
@@ -30,11 +31,11 @@ def solve(root, kind, damp):
     return sol, it, nv
 
 
-@pytest.mark.parametrize("root,damp,its", [(2, 1.0, (20, 17)), (2, 0.8, (14, 13)), (3, 0.8, (14, 13))])
+@pytest.mark.parametrize("root,damp,its", [(2, 1.0, (20, 18)), (2, 0.8, (14, 13)), (3, 0.8, (14, 13))])
 def test_colour_ordered_nodal_vanka_against_the_sequential_sweep(root, damp, its):
     seq, it_seq, nv = solve(root, "nodal", damp)
     col, it_col, _ = solve(root, "nodal_color", damp)
     assert (it_seq, it_col) == its
-    assert np.abs(seq[:nv] - col[:nv]).max() <= 3e-10 * np.abs(seq[:nv]).max()
+    assert np.abs(seq[:nv] - col[:nv]).max() <= 5e-10 * np.abs(seq[:nv]).max()
     ps, pc = seq[nv:] - seq[nv:].mean(), col[nv:] - col[nv:].mean()
-    assert np.abs(ps - pc).max() <= 1e-6 * np.abs(ps).max()
+    assert np.abs(ps - pc).max() <= 2e-6 * np.abs(ps).max()
