@@ -1141,7 +1141,7 @@ static __device__ __forceinline__ int find_sorted(const int* a, int n, int key) 
 // nodes) with unit rows for Dirichlet nodes, so every leading block is
 // nonsingular; a zero pivot still raises the flag. The reference's LAPACK LU
 // pivots; the two inverses agree to rounding.
-template <class T>
+template <class T, int TR>
 __global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int* __restrict__ vptr,
                                                       const int* __restrict__ vidx,
                                                       const int64_t* __restrict__ aoff,
@@ -1162,33 +1162,72 @@ __global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int*
   T* tk = colk + m;      // 3 m: t_k = A^{-1} bt_k
   T* red = tk + 3 * m;   // 32
   int* nodes = reinterpret_cast<int*>(red + 32);
-  __shared__ int piv_row;
   __shared__ T cdiag;
+  // rows of the patch's nodes (component 0): start, and the prefix of their
+  // lengths, so that the block reads all their entries as one flat range;
+  // jpos: position of the coupling to the patch pressure in the row (the rows
+  // of components 1 and 2 of a node hold it at the same position)
+  __shared__ int rstart[kNodalMaxNodes], rofs[kNodalMaxNodes + 1], jpos[kNodalMaxNodes];
   const int t = threadIdx.x;
-  for (int a = t; a < m; a += blockDim.x) nodes[a] = vidx[vptr[i] + a];
+  for (int a = t; a < m; a += blockDim.x) {
+    const int r = vidx[vptr[i] + a];
+    nodes[a] = r;
+    const int r0 = rp[r], r1 = rp[r + 1];
+    rstart[a] = r0;
+    rofs[a + 1] = r1 - r0;
+    jpos[a] = -1;
+  }
   for (int e = t; e < m * ld; e += blockDim.x) M[e] = T(0);
   for (int e = t; e < 6 * m; e += blockDim.x) bt[e] = T(0);
-  if (t == 0) cdiag = T(0);
+  if (t == 0) {
+    cdiag = T(0);
+    rofs[0] = 0;
+  }
+  __syncthreads();
+  if (t == 0)
+    for (int a = 0; a < m; ++a) rofs[a + 1] += rofs[a];
   __syncthreads();
   const int prow = 3 * nu + i;
-  for (int a = t; a < m; a += blockDim.x) {
-    const int r = nodes[a];
-    for (int k = rp[r]; k < rp[r + 1]; ++k) {
-      const T val = v[k];
-      if (val == T(0)) continue;
-      const int col = ci[k];
-      if (col < nu) {
-        const int b = find_sorted(nodes, m, col);
-        if (b >= 0) M[a * ld + b] = val;
-      } else if (col == prow) {
-        bt[a] = val;
+  const int total = rofs[m];
+  constexpr int UF = 4;  // entries in flight per thread
+  for (int f0 = t; f0 < total; f0 += UF * int(blockDim.x)) {
+    T val[UF];
+    int col[UF], row[UF], pos[UF];
+#pragma unroll
+    for (int u = 0; u < UF; ++u) {
+      const int f = f0 + u * int(blockDim.x);
+      row[u] = -1;
+      if (f < total) {
+        int lo = 0, hi = m;  // the row a with rofs[a] <= f < rofs[a + 1]
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (rofs[mid] <= f) lo = mid;
+          else hi = mid;
+        }
+        row[u] = lo;
+        pos[u] = f - rofs[lo];
+        const int k = rstart[lo] + pos[u];
+        val[u] = v[k];
+        col[u] = ci[k];
       }
     }
-    for (int comp = 1; comp < 3; ++comp) {
-      const int rr = comp * nu + r;
-      const int k = find_sorted(ci + rp[rr], rp[rr + 1] - rp[rr], prow);
-      if (k >= 0) bt[comp * m + a] = v[rp[rr] + k];
+#pragma unroll
+    for (int u = 0; u < UF; ++u) {
+      if (row[u] < 0) continue;
+      const int a = row[u];
+      if (col[u] == prow) {
+        jpos[a] = pos[u];
+        bt[a] = val[u];
+      } else if (val[u] != T(0) && col[u] < nu) {
+        const int b = find_sorted(nodes, m, col[u]);
+        if (b >= 0) M[a * ld + b] = val[u];
+      }
     }
+  }
+  __syncthreads();
+  for (int e = t; e < 2 * m; e += blockDim.x) {
+    const int comp = 1 + e / m, a = e % m;
+    if (jpos[a] >= 0) bt[comp * m + a] = v[rp[comp * nu + nodes[a]] + jpos[a]];
   }
   for (int k = rp[prow] + t; k < rp[prow + 1]; k += blockDim.x) {
     const T val = v[k];
@@ -1202,28 +1241,80 @@ __global__ void __launch_bounds__(256) k_nodal_factor(int np, int nu, const int*
     }
   }
   __syncthreads();
-  T* pr = Inv;  // the scaled pivot row of the step
-  const int lane = t & 31, wid = t >> 5, nw = int(blockDim.x >> 5);
+  // Gauss-Jordan on register tiles: thread (tr, tc) of a 16 x 16 grid holds
+  // the entries (tr + 16 i, tc + 16 j), i, j < TR (the launch picks TR for the
+  // level's largest patch). Per column k the owners of row k and
+  // of column k publish them (double-buffered by the parity of k, so one
+  // barrier per column suffices), then every thread scales the pivot row for
+  // its columns by the pivot's reciprocal and updates its tile: row k becomes
+  // the scaled pivot row, the others lose their column-k multiple of it
+  // (column k: -f / pv).
+  constexpr int TD = 16;  // TR x TR entries per thread: m <= 16 TR
+  __shared__ T rowb[2][kNodalMaxNodes], colb[2][kNodalMaxNodes];
+  const int tr = t / TD, tc = t % TD;
+  T reg[TR][TR];
+#pragma unroll
+  for (int ir = 0; ir < TR; ++ir)
+#pragma unroll
+    for (int jc = 0; jc < TR; ++jc) {
+      const int r = tr + TD * ir, j = tc + TD * jc;
+      reg[ir][jc] = (r < m && j < m) ? M[r * ld + j] : T(0);
+    }
   for (int k = 0; k < m; ++k) {
-    const T pv = M[k * ld + k];
-    if (t == 0 && !(pv != T(0))) atomicExch(flag, 1);
-    const T piv = pv != T(0) ? pv : T(1);
-    for (int j = t; j < m; j += blockDim.x) pr[j] = (j == k ? T(1) : M[k * ld + j]) / piv;
-    for (int r = t; r < m; r += blockDim.x) colk[r] = M[r * ld + k];
-    __syncthreads();
-    // warps over rows, lanes over columns: row k becomes the scaled pivot row,
-    // the others lose their column-k multiple of it (column k: -f / pv)
-    for (int r = wid; r < m; r += nw) {
-      const T f = colk[r];
-      T* Mr = M + r * ld;
-      if (r == k) {
-        for (int j = lane; j < m; j += 32) Mr[j] = pr[j];
-      } else {
-        for (int j = lane; j < m; j += 32) Mr[j] = (j == k ? T(0) : Mr[j]) - f * pr[j];
-      }
+    T* rk = rowb[k & 1];
+    T* ck = colb[k & 1];
+    const int kb = k / TD, km = k % TD;
+    if (tr == km) {
+#pragma unroll
+      for (int ir = 0; ir < TR; ++ir)
+        if (ir == kb)
+#pragma unroll
+          for (int jc = 0; jc < TR; ++jc) {
+            const int j = tc + TD * jc;
+            if (j < m) rk[j] = reg[ir][jc];
+          }
+    }
+    if (tc == km) {
+#pragma unroll
+      for (int jc = 0; jc < TR; ++jc)
+        if (jc == kb)
+#pragma unroll
+          for (int ir = 0; ir < TR; ++ir) {
+            const int r = tr + TD * ir;
+            if (r < m) ck[r] = reg[ir][jc];
+          }
     }
     __syncthreads();
+    const T pv = ck[k];
+    if (t == 0 && !(pv != T(0))) atomicExch(flag, 1);
+    const T rpiv = T(1) / (pv != T(0) ? pv : T(1));
+    T prj[TR];
+#pragma unroll
+    for (int jc = 0; jc < TR; ++jc) {
+      const int j = tc + TD * jc;
+      prj[jc] = j < m ? (j == k ? rpiv : rk[j] * rpiv) : T(0);
+    }
+#pragma unroll
+    for (int ir = 0; ir < TR; ++ir) {
+      const int r = tr + TD * ir;
+      if (r >= m) continue;
+      const T f = ck[r];
+#pragma unroll
+      for (int jc = 0; jc < TR; ++jc) {
+        const int j = tc + TD * jc;
+        if (r == k) reg[ir][jc] = prj[jc];
+        else reg[ir][jc] = (j == k ? T(0) : reg[ir][jc]) - f * prj[jc];
+      }
+    }
   }
+#pragma unroll
+  for (int ir = 0; ir < TR; ++ir)
+#pragma unroll
+    for (int jc = 0; jc < TR; ++jc) {
+      const int r = tr + TD * ir, j = tc + TD * jc;
+      if (r < m && j < m) M[r * ld + j] = reg[ir][jc];
+    }
+  __syncthreads();
   Inv = M;  // the inverse, in place
   // t_k = Inv bt_k
   for (int e = t; e < 3 * m; e += blockDim.x) {
@@ -1271,6 +1362,25 @@ static size_t nodal_factor_smem(int m) {
   return sizeof(T) * (size_t(2) * m * (m + 1) + 10 * size_t(m) + 32) + sizeof(int) * size_t(m);
 }
 
+template <class T, int TR>
+static void launch_nodal_factor_tr(pm_ctx* c, DevNodalVanka& nv, const int* rp, const int* ci, const T* v, T* ainv,
+                                   T* tb, T* sinv) {
+  const size_t sm = nodal_factor_smem<T>(nv.max_nodes);
+  PM_CUDA(cudaFuncSetAttribute(k_nodal_factor<T, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+  k_nodal_factor<T, TR><<<nv.np, 256, sm, c->stream>>>(nv.np, nv.nu, nv.vptr.p, nv.vidx.p, nv.aoff.p, rp, ci, v, ainv,
+                                                        tb, sinv, nv.flag.p);
+}
+
+// the register tile of the factor kernel covers 16 TR rows and columns
+template <class T>
+static void launch_nodal_factor(pm_ctx* c, DevNodalVanka& nv, const int* rp, const int* ci, const T* v, T* ainv,
+                                T* tb, T* sinv) {
+  static_assert(kNodalMaxNodes <= 96, "register tiles cover at most 96 nodes");
+  if (nv.max_nodes <= 64) launch_nodal_factor_tr<T, 4>(c, nv, rp, ci, v, ainv, tb, sinv);
+  else if (nv.max_nodes <= 80) launch_nodal_factor_tr<T, 5>(c, nv, rp, ci, v, ainv, tb, sinv);
+  else launch_nodal_factor_tr<T, 6>(c, nv, rp, ci, v, ainv, tb, sinv);
+}
+
 void DevNodalVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
   PM_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c->stream));
   if (fp32) {
@@ -1278,19 +1388,13 @@ void DevNodalVanka::factor(pm_ctx* c, const DevCsr& V, bool fp32) {
     tb32.ensure(size_t(6) * vidx.n);
     sinv32.ensure(np);
     sol32.ensure(size_t(3) * vidx.n + np);
-    const size_t sm = nodal_factor_smem<float>(max_nodes);
-    PM_CUDA(cudaFuncSetAttribute(k_nodal_factor<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
-    k_nodal_factor<float><<<np, 256, sm, c->stream>>>(np, nu, vptr.p, vidx.p, aoff.p, V.row_ptr.p, V.cols.p,
-                                                     V.vals32.p, ainv32.p, tb32.p, sinv32.p, flag.p);
+    launch_nodal_factor<float>(c, *this, V.row_ptr.p, V.cols.p, V.vals32.p, ainv32.p, tb32.p, sinv32.p);
   } else {
     ainv.ensure(size_t(ainv_len));
     tb.ensure(size_t(6) * vidx.n);
     sinv.ensure(np);
     sol.ensure(size_t(3) * vidx.n + np);
-    const size_t sm = nodal_factor_smem<double>(max_nodes);
-    PM_CUDA(cudaFuncSetAttribute(k_nodal_factor<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
-    k_nodal_factor<double><<<np, 256, sm, c->stream>>>(np, nu, vptr.p, vidx.p, aoff.p, V.row_ptr.p, V.cols.p,
-                                                      V.vals.p, ainv.p, tb.p, sinv.p, flag.p);
+    launch_nodal_factor<double>(c, *this, V.row_ptr.p, V.cols.p, V.vals.p, ainv.p, tb.p, sinv.p);
   }
   PM_CHECK_LAUNCH();
   c->kernel_launches++;
