@@ -1442,10 +1442,10 @@ __global__ void __launch_bounds__(kLocalThreads, 4) k_nodal_local(const int* __r
                                                      const T* __restrict__ tb, const T* __restrict__ sinv,
                                                      const T* __restrict__ r, const T* __restrict__ rloc,
                                                      T* __restrict__ out, T* __restrict__ x, T damp) {
-  if (guarded(guard)) return;  // uniform for the whole grid
   constexpr int NT = kLocalThreads, P = 4, R = NT / P;  // threads per row, rows per pass
   constexpr int CH = 12;  // loads of A^{-1} in flight per thread (two rounds for up to 96 nodes)
   constexpr int E = (3 * kNodalMaxNodes + NT - 1) / NT;  // velocity unknowns per thread
+  static_assert(3 * kNodalMaxNodes + 1 <= 2 * NT, "the local residual takes two loads per thread");
   __shared__ T rl[3 * kNodalMaxNodes + 1];
   __shared__ T w[3 * kNodalMaxNodes];
   __shared__ T part[P][3][R];
@@ -1453,13 +1453,26 @@ __global__ void __launch_bounds__(kLocalThreads, 4) k_nodal_local(const int* __r
   const int idx = blockIdx.x;
   if (idx >= cnt) return;
   const int t = threadIdx.x;
+  // the loads run ahead in dependent rounds (patch, then its offsets, then
+  // its operands and the first columns of A^{-1}); the guard is tested
+  // before the first store (uniform for the whole grid)
+  const int gflag = guard ? *(volatile const int*)guard : 0;
   const int i = patches ? patches[idx] : idx;
   const int v0 = vptr[i];
   const int m = vptr[i + 1] - v0;
+  const T si = sinv[i];
+  const T* A = ainv + aoff[i];
   const int* nodes = vidx + v0;
   const size_t off = 3 * size_t(v0) + i;
   const int rows3 = 3 * m;
-  // loads independent of the solve: thread t owns the velocity unknowns
+  const int q = t / R;   // column quarter
+  const int lr = t % R;  // row within the pass
+  const int qlen = (m + P - 1) / P;
+  const int b0 = q * qlen, b1 = min(m, b0 + qlen);
+  T av[CH];  // the first chunk of the first pass
+#pragma unroll
+  for (int u = 0; u < CH; ++u) av[u] = (lr < m && b0 + u < b1) ? A[size_t(b0 + u) * m + lr] : T(0);
+  // operands independent of the solve: thread t owns the velocity unknowns
   // t, t + NT, ... (3m <= 288)
   const T* tt = tb + 6 * size_t(v0);
   T ttv[E], bbv[E], xv[E];
@@ -1476,32 +1489,35 @@ __global__ void __launch_bounds__(kLocalThreads, 4) k_nodal_local(const int* __r
       if (x) xv[k] = x[g[k]];
     }
   }
-  const T si = sinv[i];
   T xp = T(0);
   if (x && t == 0) xp = x[3 * nu + i];
-  for (int e = t; e <= rows3; e += NT) {
-    T val;
-    if (rloc) {
-      val = rloc[off + e];
-    } else {
-      const int gg = e < rows3 ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
-      val = r[gg];
+  T rv[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int e = t + k * NT;
+    rv[k] = T(0);
+    if (e <= rows3) {
+      if (rloc) {
+        rv[k] = rloc[off + e];
+      } else {
+        const int gg = e < rows3 ? (e / m) * nu + nodes[e % m] : 3 * nu + i;
+        rv[k] = r[gg];
+      }
     }
-    rl[e] = val;
   }
+  if (gflag) return;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (t + k * NT <= rows3) rl[t + k * NT] = rv[k];
   __syncthreads();
-  const T* A = ainv + aoff[i];
-  const int q = t / R;   // column quarter
-  const int lr = t % R;  // row within the pass
-  const int qlen = (m + P - 1) / P;
-  const int b0 = q * qlen, b1 = min(m, b0 + qlen);
   for (int a0 = 0; a0 < m; a0 += R) {
     const int a = a0 + lr;
     T s0 = T(0), s1 = T(0), s2 = T(0);
     for (int c0 = b0; c0 < b1; c0 += CH) {
-      T av[CH];
+      if (a0 > 0 || c0 > b0) {
 #pragma unroll
-      for (int u = 0; u < CH; ++u) av[u] = (a < m && c0 + u < b1) ? A[size_t(c0 + u) * m + a] : T(0);
+        for (int u = 0; u < CH; ++u) av[u] = (a < m && c0 + u < b1) ? A[size_t(c0 + u) * m + a] : T(0);
+      }
 #pragma unroll
       for (int u = 0; u < CH; ++u) {
         if (c0 + u < b1) {
