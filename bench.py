@@ -411,9 +411,10 @@ def run_ours(args, w, rank, world, local, pg):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": mixed["launches"],
         "roofline": {"bound": "hbm",
-                     "kernel": ("k_nodal_rhs<float> + k_nodal_local<float>: one colour of the multiplicative "
-                                "nodal Vanka sweep in FP32 (local residuals of the colour's patches, then their "
-                                "Schur-complement local solves and the update; all colours of both fine levels)"
+                     "kernel": ("sell_kernel<float,8,8,PIPE,EPI_DEFECT> on the patch rows + k_nodal_local<float>: "
+                                "one colour of the multiplicative nodal Vanka sweep in FP32 (local residuals of the "
+                                "colour's patches from their sliced rows, then their Schur-complement local solves "
+                                "and the update; all colours of both fine levels)"
                                 if stokes else
                                 "sell_kernel<4,8,PIPE,EPI_JACOBI>: finest-level damped Jacobi sweep in FP32 "
                                 "on the sliced-ELL copy (the largest share of a mixed request's GPU time)"),
