@@ -245,12 +245,16 @@ int pm_disc_create(int geometry, int root_n, int n_refine, int n_levels, int kin
  * right-hand side (no exact solution) the Neumann data are zero. */
 int pm_disc_create_bc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
                       int neumann_sides, pm_disc** out);
-/* pm_disc_create_bc with the heavy part of the set-up on the context's GPU:
- * for convection-diffusion levels the CSR structure (TStructure(space),
- * src/Matrix/Structure.C:829-1283, sorted) and the assembly gather plans come
- * from one stable radix sort of the element entries by (row, column) instead
- * of the host construction. The result is the same discretisation, array for
- * array (refinement, numbering and transfer stay on the host). The context's
+/* pm_disc_create_bc with the set-up on the context's GPU: the regular
+ * refinement of the root mesh (the RefQuadRegDesc / RefHexaRegDesc /
+ * RefTetraRegDesc children, one thread per child cell), the first-touch DOF
+ * numbering of every kept convection-diffusion level (TFESpace{2,3}D::
+ * ConstructSpace: two radix sorts, of the local DOF positions by node and of
+ * the distinct nodes by class and first touch) and its CSR structure
+ * (TStructure(space), src/Matrix/Structure.C:829-1283, sorted) with the
+ * assembly gather plans (one stable radix sort of the element entries by
+ * (row, column)). The result is the same discretisation, array for array;
+ * the grid transfer and the Stokes numbering stay on the host. The context's
  * stream is synchronised; temporary device memory of about 40 bytes per
  * element-matrix entry of the finest level is freed before the call returns. */
 int pm_disc_create_device(pm_ctx* ctx, int geometry, int root_n, int n_refine, int n_levels, int kind,

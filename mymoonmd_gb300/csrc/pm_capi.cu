@@ -645,8 +645,13 @@ int pm_disc_create_device(pm_ctx* c, int geometry, int root_n, int n_refine, int
   PM_TRY
   auto* d = new pm_disc();
   try {
-    d->d = build_disc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides,
-                      [c](DiscLevel& L) { device_level_structure(c, L); });
+    SetupParts parts;
+    parts.hierarchy = [c](int g, int r, int n) { return device_hierarchy(c, g, r, n); };
+    parts.space = [c](const pmsetup::Hierarchy& h, int level, int elem_, int bnd, int ns) {
+      return device_space(c, h, level, elem_, bnd, ns);
+    };
+    parts.structure = [c](DiscLevel& L) { device_level_structure(c, L); };
+    d->d = build_disc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides, &parts);
   } catch (...) {
     delete d;
     throw;

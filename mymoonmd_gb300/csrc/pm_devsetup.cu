@@ -16,9 +16,20 @@
 // The right-hand side plan is the same with keys = row and values = the
 // positions cell * nloc + m. The results equal the host construction
 // (pm_disc.cpp) entry for entry.
+//
+// The mesh hierarchy and the DOF numbering come from the GPU as well: regular
+// refinement one thread per child cell with the refinement tables of the host
+// set-up (pm_refine_tables.h), and the first-touch numbering (inner DOFs,
+// then Neumann, then Dirichlet, each in order of first touch over the cells
+// in collection order and their local DOFs in local order,
+// TFESpace{2,3}D::ConstructSpace) by two stable radix sorts: the local DOF
+// positions t = cell * nloc + m by the lattice key of their node (the first
+// item of each key run is the node's first touch), then the distinct nodes by
+// (class, first touch), whose order is the numbering.
 #include <cub/cub.cuh>
 
 #include "pm_devsetup.h"
+#include "pm_refine_tables.h"
 
 namespace pm {
 
@@ -111,6 +122,178 @@ __global__ void k_fill_rhs(long long total, int n, const unsigned int* __restric
 
 __global__ void k_set_tail(int* __restrict__ p, int from, int to, int value) {
   for (int i = from + blockIdx.x * blockDim.x + threadIdx.x; i < to; i += gridDim.x * blockDim.x) p[i] = value;
+}
+
+// ------------------------------------------------------------ refinement --
+struct RefineTables {
+  int quad_child[4][4], quad_new[5][4];
+  int hex_child[8][8], hex_new[19][8];
+  int tet_child[8][4], tet_new[6][2];
+};
+
+RefineTables refine_tables() {
+  RefineTables t{};
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) t.quad_child[a][b] = pmsetup::kQuadChild[a][b];
+  for (int a = 0; a < 5; ++a)
+    for (int b = 0; b < 4; ++b) t.quad_new[a][b] = pmsetup::kQuadNew[a][b];
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b) t.hex_child[a][b] = pmsetup::kHexChild[a][b];
+  for (int a = 0; a < 19; ++a)
+    for (int b = 0; b < 8; ++b) t.hex_new[a][b] = pmsetup::kHexNew[a][b];
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 4; ++b) t.tet_child[a][b] = pmsetup::kTetChild[a][b];
+  for (int a = 0; a < 6; ++a)
+    for (int b = 0; b < 2; ++b) t.tet_new[a][b] = pmsetup::kTetNew[a][b];
+  return t;
+}
+
+// one thread per child cell: its vertices from the parent's (a parent vertex,
+// or the mean of the parent vertices a new vertex averages), in the child's
+// vertex order; children of a cell are consecutive (cell order, child order)
+__global__ void k_refine(int geometry, int n_coarse, int nvc, int dim, const long long* __restrict__ cv,
+                         long long* __restrict__ fv, int* __restrict__ parent, int* __restrict__ child_no,
+                         RefineTables T) {
+  const int nchild = dim == 2 ? 4 : 8;
+  const long long total = (long long)n_coarse * nchild;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int c = int(t / nchild), ch = int(t % nchild);
+    const long long* pv = cv + (long long)c * nvc * dim;
+    long long* out = fv + t * nvc * dim;
+    for (int v = 0; v < nvc; ++v) {
+      const int idx = geometry == pmsetup::GEO_SQUARE_QUAD ? T.quad_child[ch][v]
+                      : geometry == pmsetup::GEO_CUBE_HEXA ? T.hex_child[ch][v]
+                                                           : T.tet_child[ch][v];
+      for (int d = 0; d < dim; ++d) {
+        long long val;
+        if (idx < nvc) {
+          val = pv[idx * dim + d];
+        } else {
+          const int n = idx - nvc;
+          if (geometry == pmsetup::GEO_SQUARE_QUAD) {
+            long long sum = 0;
+            int cnt = 0;
+            for (int q = 0; q < 4 && T.quad_new[n][q] >= 0; ++q, ++cnt) sum += pv[T.quad_new[n][q] * 2 + d];
+            val = sum / cnt;
+          } else if (geometry == pmsetup::GEO_CUBE_HEXA) {
+            long long sum = 0;
+            int cnt = 0;
+            for (; cnt < 8 && T.hex_new[n][cnt] >= 0; ++cnt) sum += pv[T.hex_new[n][cnt] * 3 + d];
+            val = sum / cnt;
+          } else {
+            val = (pv[T.tet_new[n][0] * 3 + d] + pv[T.tet_new[n][1] * 3 + d]) / 2;
+          }
+        }
+        out[v * dim + d] = val;
+      }
+    }
+    parent[t] = c;
+    child_no[t] = ch;
+  }
+}
+
+// ------------------------------------------------------------- numbering --
+// lattice coordinates of local DOF m of a cell (cell_nodes of the host set-up)
+__device__ void node_of(int geometry, int elem, const long long* v, int m, long long* x) {
+  if (geometry == pmsetup::GEO_SQUARE_QUAD) {
+    const int k = elem == pmsetup::EL_Q2 ? 2 : 1;
+    const int a = m % (k + 1), b = m / (k + 1);
+    for (int d = 0; d < 2; ++d) x[d] = v[d] + (v[2 + d] - v[d]) * a / k + (v[6 + d] - v[d]) * b / k;
+  } else if (geometry == pmsetup::GEO_CUBE_HEXA) {
+    const int k = elem == pmsetup::EL_Q2 ? 2 : 1;
+    const int a = m % (k + 1), b = (m / (k + 1)) % (k + 1), cc = m / ((k + 1) * (k + 1));
+    for (int d = 0; d < 3; ++d)
+      x[d] = v[d] + (v[3 + d] - v[d]) * a / k + (v[9 + d] - v[d]) * b / k + (v[12 + d] - v[d]) * cc / k;
+  } else if (elem == pmsetup::EL_P1) {
+    for (int d = 0; d < 3; ++d) x[d] = v[m * 3 + d];
+  } else {
+    // v0, m01, v1, m02, m12, v2, m03, m13, m23, v3
+    const int pa[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3}, pb[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+    for (int d = 0; d < 3; ++d) x[d] = (v[pa[m] * 3 + d] + v[pb[m] * 3 + d]) / 2;
+  }
+}
+
+// class of a node: 0 inner, 1 Neumann (every side it lies on is a Neumann
+// side, 2D), 2 other boundary
+__device__ int node_class(int dim, long long S, int neumann_sides, const long long* x) {
+  bool on_bnd = false;
+  for (int d = 0; d < dim; ++d) on_bnd |= (x[d] == 0 || x[d] == S);
+  if (!on_bnd) return 0;
+  if (neumann_sides) {
+    int sides = 0;
+    if (x[1] == 0) sides |= pmsetup::SIDE_Y0;
+    if (x[0] == S) sides |= pmsetup::SIDE_X1;
+    if (x[1] == S) sides |= pmsetup::SIDE_Y1;
+    if (x[0] == 0) sides |= pmsetup::SIDE_X0;
+    if ((sides & neumann_sides) == sides) return 1;
+  }
+  return 2;
+}
+
+__global__ void k_node_keys(int geometry, int elem, int nvc, int dim, int nloc, long long nt, long long W,
+                            const long long* __restrict__ vtx, unsigned long long* __restrict__ key,
+                            int* __restrict__ val) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nt;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long c = t / nloc;
+    const int m = int(t % nloc);
+    long long x[3] = {0, 0, 0};
+    node_of(geometry, elem, vtx + c * nvc * dim, m, x);
+    key[t] = (unsigned long long)(x[0] + W * (x[1] + (dim == 3 ? W * x[2] : 0)));
+    val[t] = int(t);
+  }
+}
+
+__global__ void k_key_heads(long long nt, const unsigned long long* __restrict__ key, int* __restrict__ head) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nt;
+       i += (long long)gridDim.x * blockDim.x)
+    head[i] = (i == 0 || key[i] != key[i - 1]) ? 1 : 0;
+}
+
+// per distinct node g (run head i, gid[i] = g + 1): (class, first touch)
+__global__ void k_distinct(long long nt, int dim, long long W, long long S, int neumann_sides,
+                           const unsigned long long* __restrict__ key, const int* __restrict__ val,
+                           const int* __restrict__ head, const int* __restrict__ gid,
+                           unsigned long long* __restrict__ ukey, unsigned long long* __restrict__ order_key,
+                           int* __restrict__ order_val) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nt;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (!head[i]) continue;
+    const int g = gid[i] - 1;
+    const unsigned long long k = key[i];
+    long long x[3];
+    x[0] = (long long)(k % (unsigned long long)W);
+    x[1] = (long long)((k / (unsigned long long)W) % (unsigned long long)W);
+    x[2] = dim == 3 ? (long long)(k / ((unsigned long long)W * W)) : 0;
+    ukey[g] = k;
+    order_key[g] = ((unsigned long long)node_class(dim, S, neumann_sides, x) << 32) | (unsigned)val[i];
+    order_val[g] = g;
+  }
+}
+
+// number[g] = position of node g in (class, first touch) order; its
+// coordinates at that position; the first position of each class
+__global__ void k_number(int U, int dim, long long W, const unsigned long long* __restrict__ order_key,
+                         const int* __restrict__ order_g, const unsigned long long* __restrict__ ukey,
+                         int* __restrict__ number, long long* __restrict__ node, int* __restrict__ class_first) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < U; p += gridDim.x * blockDim.x) {
+    const int g = order_g[p];
+    number[g] = p;
+    const unsigned long long k = ukey[g];
+    node[(long long)p * dim + 0] = (long long)(k % (unsigned long long)W);
+    node[(long long)p * dim + 1] = (long long)((k / (unsigned long long)W) % (unsigned long long)W);
+    if (dim == 3) node[(long long)p * dim + 2] = (long long)(k / ((unsigned long long)W * W));
+    const int cls = int(order_key[p] >> 32);
+    if (p == 0 || int(order_key[p - 1] >> 32) != cls) class_first[cls] = p;
+  }
+}
+
+__global__ void k_dofmap(long long nt, const int* __restrict__ val, const int* __restrict__ gid,
+                         const int* __restrict__ number, int* __restrict__ dofmap) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nt;
+       i += (long long)gridDim.x * blockDim.x)
+    dofmap[val[i]] = number[gid[i] - 1];
 }
 
 int bits_for(unsigned long long v) {
@@ -221,6 +404,128 @@ void device_level_structure(pm_ctx* c, DiscLevel& L) {
   for (int i = na; i <= n; ++i) rp[size_t(i)] = int(valid);
   L.rgat_ptr = std::move(rp);
   L.rgat_idx = std::move(ri);
+}
+
+pmsetup::Hierarchy device_hierarchy(pm_ctx* c, int geometry, int root_n, int n_refine) {
+  pmsetup::Hierarchy h = pmsetup::root_hierarchy(geometry, root_n, n_refine);
+  const int dim = h.dim, nvc = h.nvc, nchild = dim == 2 ? 4 : 8;
+  cudaStream_t st = c->stream;
+  const RefineTables T = refine_tables();
+  static_assert(sizeof(long long) == sizeof(int64_t), "lattice coordinates are 64-bit");
+  DBuf<long long> cur;
+  cur.upload(reinterpret_cast<const long long*>(h.levels[0].vtx.data()), h.levels[0].vtx.size(), st);
+  for (int r = 0; r < n_refine; ++r) {
+    const int nc = h.levels.back().n_cells;
+    if ((long long)nc * nchild >= (1LL << 31)) throw Error(PM_E_INVALID, "mesh too large for the device refinement");
+    pmsetup::Level fine;
+    fine.n_cells = nc * nchild;
+    const size_t nv = size_t(fine.n_cells) * nvc * dim;
+    DBuf<long long> fv(nv);
+    DBuf<int> parent(size_t(fine.n_cells)), child(size_t(fine.n_cells));
+    const int grid = std::max(1, std::min((fine.n_cells + 255) / 256, c->num_sms * 8));
+    k_refine<<<grid, 256, 0, st>>>(geometry, nc, nvc, dim, cur.p, fv.p, parent.p, child.p, T);
+    PM_CHECK_LAUNCH();
+    c->kernel_launches++;
+    fine.vtx.resize(nv);
+    fine.parent.resize(size_t(fine.n_cells));
+    fine.child_no.resize(size_t(fine.n_cells));
+    PM_CUDA(cudaMemcpyAsync(fine.vtx.data(), fv.p, nv * sizeof(long long), cudaMemcpyDeviceToHost, st));
+    PM_CUDA(cudaMemcpyAsync(fine.parent.data(), parent.p, fine.parent.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+    PM_CUDA(cudaMemcpyAsync(fine.child_no.data(), child.p, fine.child_no.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                            st));
+    PM_CUDA(cudaStreamSynchronize(st));
+    h.levels.push_back(std::move(fine));
+    cur = std::move(fv);
+  }
+  return h;
+}
+
+pmsetup::Space device_space(pm_ctx* c, const pmsetup::Hierarchy& h, int level, int elem, int boundary,
+                            int neumann_sides) {
+  const pmsetup::Level& L = h.levels.at(size_t(level));
+  const int dim = h.dim, nvc = h.nvc;
+  if (neumann_sides && (dim != 2 || boundary != pmsetup::BND_DIRICHLET))
+    throw Error(PM_E_INVALID, "Neumann sides are supported on the unit square with Dirichlet elsewhere");
+  pmsetup::Space s;
+  s.elem = elem;
+  s.boundary = boundary;
+  s.neumann_sides = neumann_sides;
+  s.nloc = pmsetup::space_nloc(h.geometry, elem);
+  const long long S = h.scale, W = S + 1;
+  const long long nt = (long long)L.n_cells * s.nloc;
+  if (nt >= (1LL << 31)) throw Error(PM_E_INVALID, "level too large for the device numbering");
+  cudaStream_t st = c->stream;
+  const int grid = std::max(1, std::min(int((nt + 255) / 256), c->num_sms * 8));
+  DBuf<long long> vtx;
+  vtx.upload(reinterpret_cast<const long long*>(L.vtx.data()), L.vtx.size(), st);
+  // local DOF positions sorted by the lattice key of their node (stable: a
+  // run's first item is the node's first touch)
+  DBuf<unsigned long long> key_in(static_cast<size_t>(nt)), key_out(static_cast<size_t>(nt));
+  DBuf<int> val_in(static_cast<size_t>(nt)), val_out(static_cast<size_t>(nt));
+  k_node_keys<<<grid, 256, 0, st>>>(h.geometry, elem, nvc, dim, s.nloc, nt, W, vtx.p, key_in.p, val_in.p);
+  PM_CHECK_LAUNCH();
+  const unsigned long long kmax = (unsigned long long)W * W * (dim == 3 ? (unsigned long long)W : 1ULL);
+  const int end_bit = bits_for(kmax);
+  size_t tb = 0, sb = 0;
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key_in.p, key_out.p, val_in.p, val_out.p, int(nt), 0, end_bit,
+                                          st));
+  DBuf<int> head(static_cast<size_t>(nt)), gid(static_cast<size_t>(nt));
+  PM_CUDA(cub::DeviceScan::InclusiveSum(nullptr, sb, head.p, gid.p, int(nt), st));
+  DBuf<unsigned char> tmp(std::max(tb, sb));
+  tb = tmp.n;
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, key_in.p, key_out.p, val_in.p, val_out.p, int(nt), 0, end_bit,
+                                          st));
+  k_key_heads<<<grid, 256, 0, st>>>(nt, key_out.p, head.p);
+  PM_CHECK_LAUNCH();
+  sb = tmp.n;
+  PM_CUDA(cub::DeviceScan::InclusiveSum(tmp.p, sb, head.p, gid.p, int(nt), st));
+  int U = 0;
+  PM_CUDA(cudaMemcpyAsync(&U, gid.p + nt - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaStreamSynchronize(st));
+  // the distinct nodes in (class, first touch) order
+  DBuf<unsigned long long> ukey(static_cast<size_t>(U)), okey_in(static_cast<size_t>(U)),
+      okey_out(static_cast<size_t>(U));
+  DBuf<int> oval_in(static_cast<size_t>(U)), oval_out(static_cast<size_t>(U));
+  k_distinct<<<grid, 256, 0, st>>>(nt, dim, W, S, neumann_sides, key_out.p, val_out.p, head.p, gid.p, ukey.p,
+                                   okey_in.p, oval_in.p);
+  PM_CHECK_LAUNCH();
+  size_t ob = 0;
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, ob, okey_in.p, okey_out.p, oval_in.p, oval_out.p, U, 0, 34, st));
+  if (ob > tmp.n) tmp.alloc(ob);
+  ob = tmp.n;
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, ob, okey_in.p, okey_out.p, oval_in.p, oval_out.p, U, 0, 34, st));
+  DBuf<int> number(static_cast<size_t>(U)), class_first(3), dofmap(static_cast<size_t>(nt));
+  DBuf<long long> node(static_cast<size_t>(U) * dim);
+  const int init[3] = {-1, -1, -1};
+  PM_CUDA(cudaMemcpyAsync(class_first.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  const int ugrid = std::max(1, std::min((U + 255) / 256, c->num_sms * 8));
+  k_number<<<ugrid, 256, 0, st>>>(U, dim, W, okey_out.p, oval_out.p, ukey.p, number.p, node.p, class_first.p);
+  PM_CHECK_LAUNCH();
+  k_dofmap<<<grid, 256, 0, st>>>(nt, val_out.p, gid.p, number.p, dofmap.p);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 5;
+  int first[3];
+  s.dofmap.resize(static_cast<size_t>(nt));
+  s.node.resize(static_cast<size_t>(U) * dim);
+  PM_CUDA(cudaMemcpyAsync(first, class_first.p, sizeof(first), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaMemcpyAsync(s.dofmap.data(), dofmap.p, s.dofmap.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaMemcpyAsync(s.node.data(), node.p, s.node.size() * sizeof(long long), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaStreamSynchronize(st));
+  // class sizes from the first position of each class (absent classes: -1)
+  int count[3];
+  for (int k = 0; k < 3; ++k) {
+    int next = U;
+    for (int j = k + 1; j < 3; ++j)
+      if (first[j] >= 0) {
+        next = first[j];
+        break;
+      }
+    count[k] = first[k] >= 0 ? next - first[k] : 0;
+  }
+  s.n_dofs = U;
+  s.n_neumann = count[1];
+  s.n_active = boundary == pmsetup::BND_DIRICHLET ? count[0] + count[1] : U;
+  return s;
 }
 
 }  // namespace pm

@@ -11,4 +11,13 @@ namespace pm {
 // construction of build_disc.
 void device_level_structure(pm_ctx* c, DiscLevel& L);
 
+// build_hierarchy with the regular refinement on the context's GPU (the root
+// mesh from the host; every level copied back into the host hierarchy)
+pmsetup::Hierarchy device_hierarchy(pm_ctx* c, int geometry, int root_n, int n_refine);
+
+// build_space with the first-touch numbering on the context's GPU: the same
+// GlobalNumbers, node coordinates and class counts
+pmsetup::Space device_space(pm_ctx* c, const pmsetup::Hierarchy& h, int level, int elem, int boundary,
+                            int neumann_sides);
+
 }  // namespace pm

@@ -292,7 +292,7 @@ static void build_neumann_plan(const Hierarchy& h, DiscLevel& L, int neumann_sid
 }
 
 std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
-                                 int neumann_sides, const std::function<void(DiscLevel&)>& device_structure) {
+                                 int neumann_sides, const SetupParts* parts) {
   if (n_levels < 1 || n_levels > n_refine + 1)
     throw std::invalid_argument("multigrid levels must be between 1 and refinements + 1");
   auto D = std::make_unique<Disc>();
@@ -314,7 +314,8 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
   } else {
     if (geometry != GEO_CUBE_TETRA) throw std::invalid_argument("Stokes P2/P1 uses the tetrahedral unit cube");
     D->elem = EL_P2;
-    D->h = build_hierarchy(geometry, root_n, n_refine);
+    D->h = parts && parts->hierarchy ? parts->hierarchy(geometry, root_n, n_refine)
+                                     : build_hierarchy(geometry, root_n, n_refine);
     const int first = n_refine + 1 - n_levels;
     D->levels.resize(n_levels);
     for (int l = 0; l < n_levels; ++l) {
@@ -328,17 +329,19 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
     for (int l = 0; l + 1 < n_levels; ++l) build_stokes_transfer(D->h, D->levels[l], D->levels[l + 1]);
     return D;
   }
-  D->h = build_hierarchy(geometry, root_n, n_refine);
+  D->h = parts && parts->hierarchy ? parts->hierarchy(geometry, root_n, n_refine)
+                                   : build_hierarchy(geometry, root_n, n_refine);
   const int first = n_refine + 1 - n_levels;
   D->levels.resize(n_levels);
   for (int l = 0; l < n_levels; ++l) {
     DiscLevel& L = D->levels[l];
     L.level_in_hierarchy = first + l;
     L.n_cells = D->h.levels[first + l].n_cells;
-    L.space = build_space(D->h, first + l, elem, BND_DIRICHLET, neumann_sides);
+    L.space = parts && parts->space ? parts->space(D->h, first + l, elem, BND_DIRICHLET, neumann_sides)
+                                    : build_space(D->h, first + l, elem, BND_DIRICHLET, neumann_sides);
     L.verts = cell_vertices(D->h, first + l);
-    if (device_structure) {
-      device_structure(L);
+    if (parts && parts->structure) {
+      parts->structure(L);
     } else {
       L.sys = build_structure(L.space, L.n_cells);
       std::vector<char> act(L.space.n_dofs, 0);

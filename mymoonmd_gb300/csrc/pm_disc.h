@@ -65,12 +65,20 @@ struct Disc {
   int nvc() const { return h.nvc; }
 };
 
-// device_structure (optional): builds a convection-diffusion level's `sys`,
-// gather plans and diag_pos from its space in place of the host construction
-// (the GPU set-up, pm_devsetup.cu); the results are the same arrays
+// The parts of the set-up that can come from elsewhere (the GPU set-up,
+// pm_devsetup.cu); each gives the same arrays as the host construction it
+// replaces. hierarchy: the mesh hierarchy (build_hierarchy); space: a level's
+// numbering (build_space); structure: a convection-diffusion level's `sys`,
+// gather plans and diag_pos from its space.
+struct SetupParts {
+  std::function<pmsetup::Hierarchy(int geometry, int root_n, int n_refine)> hierarchy;
+  std::function<pmsetup::Space(const pmsetup::Hierarchy&, int level, int elem, int boundary, int neumann_sides)>
+      space;
+  std::function<void(DiscLevel&)> structure;
+};
+
 std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
-                                 int neumann_sides = 0,
-                                 const std::function<void(DiscLevel&)>& device_structure = nullptr);
+                                 int neumann_sides = 0, const SetupParts* parts = nullptr);
 
 }  // namespace pm
 

@@ -7,6 +7,8 @@
 #include <cstdlib>
 #include <stdexcept>
 
+#include "pm_refine_tables.h"
+
 namespace pmsetup {
 
 int element_nloc(int elem) {
@@ -21,7 +23,7 @@ int element_nloc(int elem) {
 
 int element_dim(int elem) { return (elem == EL_P1 || elem == EL_P2) ? 3 : 0; }
 
-static int space_nloc(int geometry, int elem) {
+int space_nloc(int geometry, int elem) {
   if (geometry == GEO_SQUARE_QUAD) {
     if (elem == EL_Q1) return 4;
     if (elem == EL_Q2) return 9;
@@ -35,44 +37,7 @@ static int space_nloc(int geometry, int elem) {
   throw std::invalid_argument("element does not fit the cell shape");
 }
 
-// ---------------------------------------------------------------------------
-// refinement tables (child -> refined-cell vertex), restated from the
-// DatChildVertex arrays of the regular refinement descriptors.
-static const int kQuadChild[4][4] = {{0, 4, 8, 7}, {1, 5, 8, 4}, {2, 6, 8, 5}, {3, 7, 8, 6}};
-// new quad vertices 4..8 as sets of parent vertices they average
-static const int kQuadNew[5][4] = {{0, 1, -1, -1}, {1, 2, -1, -1}, {2, 3, -1, -1},
-                                   {3, 0, -1, -1}, {0, 1, 2, 3}};
-
-static const int kHexChild[8][8] = {
-    {0, 8, 12, 11, 15, 16, 26, 24}, {1, 9, 12, 8, 13, 19, 26, 16},
-    {2, 10, 12, 9, 17, 22, 26, 19}, {3, 11, 12, 10, 20, 24, 26, 22},
-    {4, 23, 25, 14, 15, 24, 26, 16}, {5, 14, 25, 18, 13, 16, 26, 19},
-    {6, 18, 25, 21, 17, 19, 26, 22}, {7, 21, 25, 23, 20, 22, 26, 24}};
-// new hexa vertices 8..26: the children sharing them (DatVertexChild); child c
-// carries parent vertex c, so the new vertex is the mean of those parent vertices
-#define E -1, -1, -1, -1
-static const int kHexNew[19][8] = {
-    {0, 1, -1, -1, E}, {1, 2, -1, -1, E}, {2, 3, -1, -1, E}, {0, 3, -1, -1, E},
-    {0, 1, 2, 3, E},   {1, 5, -1, -1, E}, {4, 5, -1, -1, E}, {0, 4, -1, -1, E},
-    {0, 1, 4, 5, E},   {2, 6, -1, -1, E}, {5, 6, -1, -1, E}, {1, 2, 5, 6, E},
-    {3, 7, -1, -1, E}, {6, 7, -1, -1, E}, {2, 3, 6, 7, E},   {4, 7, -1, -1, E},
-    {0, 3, 4, 7, E},   {4, 5, 6, 7, E},   {0, 1, 2, 3, 4, 5, 6, 7}};
-#undef E
-
-static const int kTetChild[8][4] = {{0, 4, 6, 7}, {4, 1, 5, 8}, {6, 5, 2, 9}, {7, 8, 9, 3},
-                                    {4, 6, 7, 8}, {5, 6, 4, 8}, {6, 7, 8, 9}, {8, 5, 6, 9}};
-// new tetra vertices 4..9 are edge midpoints (DatEdgeVertex)
-static const int kTetNew[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
-
-// Kuhn split of a cube into 6 tetrahedra, KVERT of Default_UnitCube_Tetra
-// (src/Geometry/Tests.C:1859-1912), 0-based over the cube vertex numbering
-// (0,0,0) (1,0,0) (1,1,0) (0,1,0) (0,0,1) (1,0,1) (1,1,1) (0,1,1).
-static const int kKuhn[6][4] = {{0, 1, 2, 6}, {0, 5, 1, 6}, {0, 2, 3, 6},
-                                {0, 3, 7, 6}, {0, 4, 5, 6}, {0, 7, 4, 6}};
-static const int kCubeCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
-                                      {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
-
-Hierarchy build_hierarchy(int geometry, int root_n, int n_refine) {
+Hierarchy root_hierarchy(int geometry, int root_n, int n_refine) {
   if (root_n < 1 || n_refine < 0 || n_refine > 12)
     throw std::invalid_argument("bad mesh size");
   Hierarchy h;
@@ -125,7 +90,12 @@ Hierarchy build_hierarchy(int geometry, int root_n, int n_refine) {
   root.parent.assign(root.n_cells, -1);
   root.child_no.assign(root.n_cells, -1);
   h.levels.push_back(std::move(root));
+  return h;
+}
 
+Hierarchy build_hierarchy(int geometry, int root_n, int n_refine) {
+  Hierarchy h = root_hierarchy(geometry, root_n, n_refine);
+  const int dim = h.dim, nvc = h.nvc;
   for (int r = 0; r < n_refine; ++r) {
     const Level& coarse = h.levels.back();
     Level fine;

@@ -59,12 +59,18 @@ struct Hierarchy {
 };
 
 int element_nloc(int elem);
+// local DOFs of `elem` on the cells of `geometry` (Qk on quadrilaterals or
+// hexahedra, Pk on tetrahedra)
+int space_nloc(int geometry, int elem);
 int element_dim(int elem);
 
 // Builds the root mesh (root_n cells per side; root_n = 1 is ParMooN's default
 // UnitSquare / Default_UnitCube_Hexa / Default_UnitCube_Tetra) and refines it
 // regularly n_refine times, keeping every level.
 Hierarchy build_hierarchy(int geometry, int root_n, int n_refine);
+// the same hierarchy with the root mesh only (its lattice scale already that
+// of n_refine refinements): the start of a refinement done elsewhere
+Hierarchy root_hierarchy(int geometry, int root_n, int n_refine);
 
 // Sides of the unit square as the boundary components of UnitSquare number
 // them (Default_UnitSquare): 0 y=0, 1 x=1, 2 y=1, 3 x=0.

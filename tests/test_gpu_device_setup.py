@@ -1,9 +1,11 @@
-"""The set-up on the GPU (pm_disc_create_device): the CSR structure and the
-assembly gather plans of every convection-diffusion level come from one
-stable radix sort of the element entries instead of the host construction.
-The discretisation must be the same array for array: structure, numbering,
-prolongations, and - through the gather plans - the assembled matrices and
-right-hand sides, bit for bit."""
+"""The set-up on the GPU (pm_disc_create_device): the mesh hierarchy by
+regular refinement on the device, the first-touch DOF numbering by two
+radix sorts, and the CSR structure and the assembly gather plans of every
+convection-diffusion level by one stable radix sort of the element entries,
+instead of the host construction. The discretisation must be the same array
+for array: cell vertices, numbering, structure, prolongations, and - through
+the gather plans and the Dirichlet node coordinates - the assembled matrices
+and right-hand sides, bit for bit."""
 import numpy as np
 import pytest
 
@@ -14,8 +16,12 @@ pytestmark = pytest.mark.gpu
 CASES = [
     (m.GEO_SQUARE_QUAD, 2, 5, 3, 1, 0),   # 2D Q1 64^2 on a 2x2 root mesh
     (m.GEO_SQUARE_QUAD, 1, 4, 3, 2, 2),   # 2D Q2 16^2, Neumann side x = 1
+    (m.GEO_SQUARE_QUAD, 1, 3, 2, 1, 10),  # 2D Q1 8^2, Neumann sides x = 1 and x = 0
     (m.GEO_CUBE_HEXA, 1, 3, 3, 1, 0),     # 3D Q1 8^3
     (m.GEO_CUBE_HEXA, 1, 4, 3, 2, 0),     # 3D Q2 16^3
+    (m.GEO_CUBE_HEXA, 2, 2, 2, 2, 0),     # 3D Q2 8^3 on a 2x2x2 root mesh
+    (m.GEO_CUBE_TETRA, 1, 3, 3, 11, 0),   # P1 on 8^3 cubes x 6 tetrahedra
+    (m.GEO_CUBE_TETRA, 2, 2, 2, 12, 0),   # P2 on 8^3 cubes x 6 tetrahedra (2x2x2 root)
 ]
 
 
@@ -40,14 +46,17 @@ def test_device_setup_equals_the_host_setup(ctx, case):
     try:
         for l in range(nlev):
             assert host.level_info(l) == dev.level_info(l)
+            assert np.array_equal(host.cell_vertices(l), dev.cell_vertices(l)), l
             for a, b in zip(host.structure(l), dev.structure(l)):
                 assert np.array_equal(a, b), l
             assert np.array_equal(host.dofmap(l), dev.dofmap(l))
             if l + 1 < nlev:
                 for a, b in zip(host.prolongation(l)[:3], dev.prolongation(l)[:3]):
                     assert np.array_equal(a, b)
-        dim_b = (1.0, 0.5, 0.25) if geo == m.GEO_CUBE_HEXA else (1.0, 0.5)
-        cf = m.cd_coeffs(0.05, dim_b, 0.0, True)
+        dim_b = (1.0, 0.5, 0.25) if geo != m.GEO_SQUARE_QUAD else (1.0, 0.5)
+        # a quadratic exact solution: its Dirichlet values come from the
+        # coordinates of the boundary nodes of each numbering
+        cf = m.cd_coeffs(0.05, dim_b, 0.0, poly=(0.3, 1.0, -0.5, 0.25, 0.7, -0.2, 0.4, 0.9, -0.6, 0.1))
         for d in (host, dev):
             p = m.ConvectionDiffusion(ctx, d, cf, db())
             p.assemble()
