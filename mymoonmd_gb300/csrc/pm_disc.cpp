@@ -97,9 +97,10 @@ static void fill_bnd_xyz(const Hierarchy& h, DiscLevel& L) {
     }
 }
 
-static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L) {
-  L.space = build_space(h, lvl, EL_P2, BND_DIRICHLET);
-  L.pspace = build_space(h, lvl, EL_P1, BND_NEUMANN);
+static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L, const SetupParts* parts) {
+  const bool dev = parts && parts->space;
+  L.space = dev ? parts->space(h, lvl, EL_P2, BND_DIRICHLET, 0) : build_space(h, lvl, EL_P2, BND_DIRICHLET);
+  L.pspace = dev ? parts->space(h, lvl, EL_P1, BND_NEUMANN, 0) : build_space(h, lvl, EL_P1, BND_NEUMANN);
   const int nu = L.space.n_dofs, np = L.pspace.n_dofs, nau = L.space.n_active;
   const int N = 3 * nu + np, nc = L.n_cells;
   L.cdof.resize(size_t(nc) * 34);
@@ -323,7 +324,7 @@ std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_l
       L.level_in_hierarchy = first + l;
       L.n_cells = D->h.levels[first + l].n_cells;
       L.verts = cell_vertices(D->h, first + l);
-      build_stokes_level(D->h, first + l, L);
+      build_stokes_level(D->h, first + l, L, parts);
       fill_bnd_xyz(D->h, L);
     }
     for (int l = 0; l + 1 < n_levels; ++l) build_stokes_transfer(D->h, D->levels[l], D->levels[l + 1]);

@@ -94,3 +94,35 @@ def test_device_setup_time_of_the_32cube_q2_hierarchy(ctx):
     finally:
         host.close()
         dev.close()
+
+
+def test_device_numbering_of_the_stokes_spaces(ctx):
+    """the P2 velocity (Dirichlet) and P1 pressure (Neumann, all active)
+    numberings of a Stokes set-up from the GPU: the same GlobalNumbers, level
+    sizes, combined structure and Dirichlet node coordinates (through the
+    right-hand side of the polynomial example) as the host set-up"""
+    host = m.Discretization(m.GEO_CUBE_TETRA, 2, 2, 2, m.KIND_STOKES, 12)
+    dev = m.Discretization(m.GEO_CUBE_TETRA, 2, 2, 2, m.KIND_STOKES, 12, ctx=ctx)
+    probs = []
+    try:
+        for l in range(2):
+            for space in (0, 1):
+                assert host.level_info(l, space) == dev.level_info(l, space)
+                assert np.array_equal(host.dofmap(l, space), dev.dofmap(l, space))
+            assert np.array_equal(host.cell_vertices(l), dev.cell_vertices(l))
+            for a, b in zip(host.structure(l), dev.structure(l)):
+                assert np.array_equal(a, b)
+        for d in (host, dev):
+            sdb = db()
+            sdb["multigrid_smoother"] = "nodal_vanka"
+            sdb.add("example", -3)
+            p = m.StokesProblem(ctx, d, 1.0, sdb)
+            p.assemble()
+            probs.append(p)
+        assert np.array_equal(probs[0].rhs(), probs[1].rhs())
+        assert np.array_equal(probs[0].matrix(-1).values(), probs[1].matrix(-1).values())
+    finally:
+        for p in probs:
+            p.close()
+        host.close()
+        dev.close()

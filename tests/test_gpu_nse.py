@@ -157,3 +157,35 @@ def test_gpu_nonlinear_loop_options(ctx):
         prob.close()
         disc3.close()
     disc.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gpu_nse_known_answer_at_the_workload_size(ctx, precision):
+    """the Navier-Stokes workload (24^3 cubes x 6 tetrahedra, Reynolds number
+    10, the bench's solver): the Picard loop reaches the 1e-10 nonlinear
+    residual and the exact solution of example -3: velocity within 1e-8 and
+    the pressure, which the loop keeps in L2_0, within 1e-6 of the exact one
+    shifted to mean zero (maximum norms; the reference's nse3d_solvers_test
+    holds its multigrid runs to 1e-8 in the L2 norms; the 1e-10 nonlinear
+    residual leaves velocity errors of about 2e-9 here)"""
+    import bench
+    from test_gpu_stokes_example import exact_on, level_nodes
+    w = bench.WORKLOADS["nse3d_p2p1_24"]
+    disc = m.Discretization(m.GEO_CUBE_TETRA, w["root_n"], w["n_refine"], w["n_levels"], m.KIND_STOKES, 12)
+    prob = m.StokesProblem(ctx, disc, w["nu"], bench.solver_db(w, precision))
+    try:
+        prob.assemble()
+        hist = prob.solve_nonlinear()
+        assert hist[-1, 2] <= 1e-10 and len(hist) <= w["nl_maxit"] + 1
+        uc, pc, wp, meas = level_nodes(disc, w["n_levels"] - 1)
+        u, pe = exact_on(uc, pc)
+        x = prob.solution()
+        nu3 = 3 * uc.shape[0]
+        assert np.abs(x[:nu3] - u).max() <= 1e-8
+        # the loop keeps the pressure in L2_0 (P1 integral weights): the exact
+        # pressure's projection
+        p = x[nu3:]
+        assert np.abs(p - (pe - float(wp @ pe) / meas)).max() <= 1e-6
+    finally:
+        prob.close()
+        disc.close()
