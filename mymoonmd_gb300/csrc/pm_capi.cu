@@ -895,7 +895,7 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
     p->rhs_coarse.alloc(n);
     PM_CUDA(cudaMemsetAsync(p->sol.p, 0, sizeof(double) * n, c->stream));
     p->defect.alloc(n);
-    p->res2.alloc(4);
+    p->res2.alloc(kResidualScratch);
     if (p->problem_type == 5) {
       // velocities of the coarser levels (zero until the first restriction)
       size_t cmax = 0;

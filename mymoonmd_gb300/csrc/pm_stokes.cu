@@ -550,13 +550,18 @@ void project_pressure_l20(pm_ctx* c, const DevStokesLevel& L, double* p) {
   c->kernel_launches++;
 }
 
-// one block: the squared norms of the blocks [0, nv), [nv, 2 nv), [2 nv, 3 nv)
-// and [3 nv, n), each summed in a fixed order
-__global__ void __launch_bounds__(1024) k_block_norms(int nv, int n, const double* __restrict__ d,
-                                                       double* __restrict__ out4) {
-  __shared__ double red[4][32];
+// the squared norms of the blocks [0, nv), [nv, 2 nv), [2 nv, 3 nv) and
+// [3 nv, n): per thread block four partial sums over a contiguous chunk (in a
+// fixed order), then one block adds the partials in block order
+constexpr int kNormBlocks = 256;
+static_assert(kResidualScratch >= 4 + 4 * kNormBlocks, "the residual scratch holds the partial sums");
+__global__ void __launch_bounds__(256) k_block_norm_partials(int nv, int n, const double* __restrict__ d,
+                                                             double* __restrict__ part) {
+  __shared__ double red[4][8];
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int beg = blockIdx.x * chunk, end = min(n, beg + chunk);
   double a[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = beg + threadIdx.x; i < end; i += blockDim.x) {
     const double v = d[i];
     const int b = min(i / nv, 3);
 #pragma unroll
@@ -569,9 +574,17 @@ __global__ void __launch_bounds__(1024) k_block_norms(int nv, int n, const doubl
   }
   __syncthreads();
   if (threadIdx.x < 4) {
-    double s = 0.0;
-    for (int w = 0; w < int(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
-    out4[threadIdx.x] = s;
+    double sum = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) sum += red[threadIdx.x][w];
+    part[blockIdx.x * 4 + threadIdx.x] = sum;
+  }
+}
+
+__global__ void k_block_norm_finish(int nb, const double* __restrict__ part, double* __restrict__ out4) {
+  if (threadIdx.x < 4) {
+    double sum = 0.0;
+    for (int b = 0; b < nb; ++b) sum += part[b * 4 + threadIdx.x];
+    out4[threadIdx.x] = sum;
   }
 }
 
@@ -579,9 +592,11 @@ void nse_residuals(pm_ctx* c, const DevStokesLevel& L, const DevCsr& A, const do
                    double* d, double* out4) {
   csr_apply(c, A, EPI_DEFECT, x, d, rhs, 1.0);
   project_pressure_l20(c, L, d + 3 * size_t(L.nvel));
-  k_block_norms<<<1, 1024, 0, c->stream>>>(L.nvel, L.n, d, out4);
+  // the partials go to out4 + 4 (the caller's buffer holds 4 + 4 kNormBlocks)
+  k_block_norm_partials<<<kNormBlocks, 256, 0, c->stream>>>(L.nvel, L.n, d, out4 + 4);
+  k_block_norm_finish<<<1, 32, 0, c->stream>>>(kNormBlocks, out4 + 4, out4);
   PM_CHECK_LAUNCH();
-  c->kernel_launches++;
+  c->kernel_launches += 2;
 }
 
 // --------------------------------------------------- projected matrix ------

@@ -80,7 +80,9 @@ void project_pressure_l20(pm_ctx* c, const DevStokesLevel& L, double* p);
 
 // NavierStokes::compute_residuals (NavierStokes.C:820-870): d = rhs - A x,
 // the pressure part of d projected into L2_0, then the squared norms of the
-// blocks u1, u2, u3, p of d into out4[0..3] (device)
+// blocks u1, u2, u3, p of d into out4[0..3] (device; out4 holds
+// kResidualScratch doubles, the rest partial sums)
+constexpr int kResidualScratch = 4 + 4 * 256;
 void nse_residuals(pm_ctx* c, const DevStokesLevel& L, const DevCsr& A, const double* rhs, const double* x,
                    double* d, double* out4);
 

@@ -9,6 +9,10 @@
         one warm-up request, then one request of the 3D Stokes P2/P1 workload
         (24^3 cubes x 6 tetrahedra, 368,572 DOFs, 3 levels, V(1,1) Vanka);
         --cubes 12 runs the 12^3 mesh of the same family
+    python -m mymoonmd_gb300.profile_cases nse [--precision ...]
+        one warm-up request, then one request of the 3D Navier-Stokes workload
+        (24^3 cubes x 6 tetrahedra, Reynolds number 10, example -3): assembly
+        and the Picard loop to a 1e-10 nonlinear residual
     python -m mymoonmd_gb300.profile_cases tcd [--precision mixed|fp64] [--scheme ...]
         time-dependent convection-diffusion on the 3D Q2 32^3 mesh (4 levels,
         the request's solver): initial assembly, then 6 time steps of 0.01
@@ -54,7 +58,7 @@ def problem(ctx, precision="mixed", n_levels=4):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["request", "spmv", "stokes", "tcd"])
+    ap.add_argument("case", choices=["request", "spmv", "stokes", "nse", "tcd"])
     ap.add_argument("--scheme", default="crank_nicolson", choices=["backward_euler", "crank_nicolson", "bdf_two"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--smoother", default="nodal_vanka")
@@ -84,6 +88,28 @@ def main() -> None:
         print(f"tcd {args.scheme} {args.precision}: {np.mean(steady):.2f} ms per time step "
               f"(min {min(steady):.2f}, {len(steady)} steps after a warm-up), FGMRES iterations {its}")
         tcd.close()
+        ctx.close()
+        return
+    if args.case == "nse":
+        db = _db(args.precision)
+        db["multigrid_n_levels"] = 3
+        db["multigrid_smoother"] = "nodal_vanka"
+        db["multigrid_smoother_coarse"] = "nodal_vanka_jacobi"
+        db["multigrid_vanka_damp_factor"] = 0.8
+        db["multigrid_n_pre_smooth"] = 1
+        db["multigrid_n_post_smooth"] = 1
+        db.add("example", -3)
+        db.add("problem_type", 5)
+        db.add("nonlinloop_epsilon", 1e-10)
+        db.add("nonlinloop_maxit", 30)
+        disc = m.Discretization(m.GEO_CUBE_TETRA, 3, 3, 3, m.KIND_STOKES, 12)
+        prob = m.StokesProblem(ctx, disc, 0.1, db)
+        for _ in range(2):
+            prob.reset_solution()
+            prob.assemble()
+            hist = prob.solve_nonlinear()
+        print("nse", args.precision, "nonlinear steps", len(hist) - 1, "residual", hist[-1][2])
+        prob.close()
         ctx.close()
         return
     if args.case == "stokes":
