@@ -353,7 +353,11 @@ int pm_problem_create_stokes(pm_ctx* ctx, const pm_disc* d, double nu, const cha
  * P5Tetra rule (degree 3 x 2 for nonlinear problems, FEDatabase3D.C:1153-1219)
  * and adds the convective term (u . grad u_j, phi_i) of each level's current
  * velocity to A11, A22 and A33 (NSNonlinearTerm_convective,
- * src/AssembleRoutinesSaddle/NSE_local_assembling_routines.C). */
+ * src/AssembleRoutinesSaddle/NSE_local_assembling_routines.C); with
+ * "nse_nonlinear_form: skew_symmetric" its skew-symmetric form (1/2)
+ * [(u . grad phi_j, phi_i) - (u . grad phi_i, phi_j)] (NSNonlinearTerm_
+ * skew_symmetric). The rotational, divergence and emac forms couple the
+ * velocity components and return PM_E_UNSUPPORTED. */
 /* ConvectionDiffusion::assemble (src/System/ConvectionDiffusion.C:174);
  * NavierStokes::assemble_linear_terms (src/System/NavierStokes.C:407) for a
  * Stokes / Navier-Stokes problem */

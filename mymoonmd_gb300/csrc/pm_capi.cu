@@ -853,11 +853,17 @@ int pm_problem_create_stokes(pm_ctx* c, const pm_disc* d, double nu, const char*
     if (p->problem_type == 5 && p->stokes_example != -3)
       throw Error(PM_E_UNSUPPORTED, "the Navier-Stokes problem is implemented for example -3 (test_u_2_p_1)");
     p->params_text = params ? params : "";
+    // nse_nonlinear_form (LocalAssembling.C:593): the convective and the
+    // skew-symmetric forms act on the diagonal velocity blocks; rotational,
+    // divergence and emac couple the velocity components (blocks A12 ...)
+    const std::string form = Params::parse(params ? params : "").str("nse_nonlinear_form", "convective");
+    if (form != "convective" && form != "skew_symmetric")
+      throw Error(PM_E_UNSUPPORTED, "nse_nonlinear_form '" + form + "': convective or skew_symmetric");
     const Disc& D = *d->d;
     const int nl = int(D.levels.size());
     // the rule of the assembly: degree 2 x 2 for the linear (Stokes) problem,
     // 3 x 2 for the nonlinear one (FEDatabase3D.C:1153-1219)
-    p->stab.upload(c, p->problem_type == 5 ? 15 : 11);
+    p->stab.upload(c, p->problem_type == 5 ? 15 : 11, form == "skew_symmetric");
     size_t kmax = 0, fmax = 0;
     p->slev.resize(nl);
     const Params pre = Params::parse(params ? params : "");

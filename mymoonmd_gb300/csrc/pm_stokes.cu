@@ -32,7 +32,7 @@ __host__ __device__ constexpr int tab_off_xi(int qn) { return tab_off_w(qn) + qn
 __host__ __device__ constexpr int tab_off_c(int qn) { return tab_off_xi(qn) + 3 * qn; }
 __host__ __device__ constexpr int tab_size(int qn) { return tab_off_c(qn) + 3000; }
 
-void DevStokesTables::upload(pm_ctx* c, int nq) {
+void DevStokesTables::upload(pm_ctx* c, int nq, bool skew) {
   if (nq != kP4n && nq != kP5n) throw Error(PM_E_UNSUPPORTED, "Stokes tables: 11 or 15 quadrature points");
   qn = nq;
   const double* qw = nq == kP4n ? kP4w : kP5w;
@@ -76,15 +76,20 @@ void DevStokesTables::upload(pm_ctx* c, int nq) {
     t[tab_off_xi(nq) + q * 3 + 2] = qz[q];
   }
   // C[a][i][j][k]: test function i, ansatz function j (derivative a), velocity
-  // basis function k
+  // basis function k; for the skew-symmetric form (1/2) [((u.grad) phi_j,
+  // phi_i) - ((u.grad) phi_i, phi_j)] (NSNonlinearTerm_skew_symmetric) its
+  // antisymmetric part in (i, j)
+  auto conv = [&](int a, int i, int j, int l) {
+    double s = 0.0;
+    for (int q = 0; q < nq; ++q) s += qw[q] * phi[q * 10 + i] * D(a, q, j) * phi[q * 10 + l];
+    return s;
+  };
   for (int a = 0; a < 3; ++a)
     for (int i = 0; i < 10; ++i)
       for (int j = 0; j < 10; ++j)
-        for (int l = 0; l < 10; ++l) {
-          double s = 0.0;
-          for (int q = 0; q < nq; ++q) s += qw[q] * phi[q * 10 + i] * D(a, q, j) * phi[q * 10 + l];
-          t[tab_off_c(nq) + a * 1000 + i * 100 + j * 10 + l] = s;
-        }
+        for (int l = 0; l < 10; ++l)
+          t[tab_off_c(nq) + a * 1000 + i * 100 + j * 10 + l] =
+              skew ? 0.5 * (conv(a, i, j, l) - conv(a, j, i, l)) : conv(a, i, j, l);
   data.upload(t, c->stream);
 }
 

@@ -13,9 +13,10 @@ namespace pm {
 struct DevStokesTables {
   int qn = 11;
   // S (6 x 100), D (3 x 40), phi2 (qn x 10), w (qn), xi (qn x 3), and the
-  // convection tensor C[a][i][j][k] = sum_q w phi_i d_a phi_j phi_k (3 x 1000)
+  // convection tensor C[a][i][j][k] = sum_q w phi_i d_a phi_j phi_k (3 x 1000;
+  // with skew its antisymmetric part in i, j: the skew-symmetric form)
   DBuf<double> data;
-  void upload(pm_ctx* c, int qn = 11);
+  void upload(pm_ctx* c, int qn = 11, bool skew = false);
 };
 
 // device copy of one Stokes level's assembly inputs

@@ -14,7 +14,8 @@ test/nse3d_solvers_test.c++ drives it:
   convective term        : NSNonlinearTerm_convective
                            (src/AssembleRoutinesSaddle/
                            NSE_local_assembling_routines.C): (u . grad phi_j,
-                           phi_i) added to A11, A22 and A33
+                           phi_i) added to A11, A22 and A33; or its
+                           skew-symmetric form (NSNonlinearTerm_skew_symmetric)
   assemble_nonlinear_term: NavierStokes.C:573-750 - the finest velocity
                            restricted to every coarser level
                            (GridTransfer::RestrictFunction,
@@ -56,11 +57,19 @@ def _jacobians(lv: StokesLevel):
     return J, np.abs(np.linalg.det(J))
 
 
-def convection_tensor(qn: int = 15) -> np.ndarray:
-    """C[a, i, j, k] = sum_q w phi_i dhat_a phi_j phi_k on the reference cell"""
+def convection_tensor(qn: int = 15, form: str = "convective") -> np.ndarray:
+    """C[a, i, j, k] = sum_q w phi_i dhat_a phi_j phi_k on the reference cell;
+    for the skew-symmetric form (NSNonlinearTerm_skew_symmetric: (1/2)
+    [((u.grad) phi_j, phi_i) - ((u.grad) phi_i, phi_j)]) its antisymmetric
+    part in (i, j)"""
     x, y, z, w = _tet_rule(qn)
     phi, dphi = _pk_values(12, x, y, z)
-    return np.einsum("q,qi,aqj,qk->aijk", w, phi, dphi, phi)
+    C = np.einsum("q,qi,aqj,qk->aijk", w, phi, dphi, phi)
+    if form == "skew_symmetric":
+        return 0.5 * (C - np.transpose(C, (0, 2, 1, 3)))
+    if form != "convective":
+        raise ValueError("nonlinear forms: convective, skew_symmetric")
+    return C
 
 
 def restriction_matrices() -> np.ndarray:
@@ -98,11 +107,12 @@ class OracleNSE:
     """NavierStokes<3> (problem_type 5, convective form, example -3) on the
     CPU with the direct solver."""
 
-    def __init__(self, root_n: int, n_refine: int, n_levels: int, reynolds: float = 1.0):
+    def __init__(self, root_n: int, n_refine: int, n_levels: int, reynolds: float = 1.0,
+                 form: str = "convective"):
         self.nu = 1.0 / reynolds
         self.stokes = OracleStokes(root_n, n_refine, n_levels, self.nu, example=-3)
         self.levels = self.stokes.levels
-        self.C = convection_tensor(15)
+        self.C = convection_tensor(15, form)
         self.Q = restriction_matrices() if len(self.levels) > 1 else None
         self.x = np.zeros(self.levels[-1].n)
         self.u = [np.zeros(3 * lv.nu) for lv in self.levels]   # coarse velocities

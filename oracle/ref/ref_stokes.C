@@ -15,7 +15,7 @@
 // (BlockFEMatrix::get_combined_matrix) and the right-hand side; with SOLVER
 // direct, the direct solve's solution of the finest level.
 //
-// usage: ref_stokes OUTDIR N_REFINE N_LEVELS SOLVER [MODE RE EPS MAXIT]
+// usage: ref_stokes OUTDIR N_REFINE N_LEVELS SOLVER [MODE RE EPS MAXIT FORM]
 //   SOLVER direct (one level) | none (assemble only; N_LEVELS levels) |
 //          mg (FGMRES with a nodal Vanka multigrid, N_LEVELS levels)
 //   MODE stokes (default) | nse: the Navier-Stokes problem (problem_type 5,
@@ -23,7 +23,8 @@
 //   hold the convective term) at Reynolds number RE, run as the reference's
 //   nse3d_solvers_test runs it (assemble_linear_terms, stop_it(0), then
 //   solve / assemble_nonlinear_term / stop_it(k) until stop_it says so, with
-//   nonlinloop_epsilon EPS and nonlinloop_maxit MAXIT); dumps the residuals
+//   nonlinloop_epsilon EPS and nonlinloop_maxit MAXIT, and the nonlinear form
+//   FORM, nse_nonlinear_form: convective (default) or skew_symmetric); dumps the residuals
 //   of every nonlinear step, the linear iterations of every solve, the final
 //   solution and get_errors(). With SOLVER none, MODE nse sets the finest
 //   solution to u_b[i] = sin(0.7 i + 1.3 b + 0.1) (velocity component b, DOF
@@ -123,6 +124,7 @@ int main(int argc, char** argv) {
   const double reynolds = argc > 6 ? std::atof(argv[6]) : 1.0;
   const double nl_eps = argc > 7 ? std::atof(argv[7]) : 1e-10;
   const size_t nl_maxit = argc > 8 ? size_t(std::atoi(argv[8])) : 10;
+  const std::string nl_form = argc > 9 ? argv[9] : "convective";
 
   Output::setVerbosity(1);
   TDatabase database;
@@ -136,7 +138,7 @@ int main(int argc, char** argv) {
   db["problem_type"].set<size_t>(nse_mode ? 5 : 3);
   db["example"] = -3;
   if (nse_mode) {
-    db["nse_nonlinear_form"] = "convective";
+    db["nse_nonlinear_form"] = nl_form;
     db["reynolds_number"] = reynolds;
     db["nonlinloop_epsilon"] = nl_eps;
     db["nonlinloop_maxit"] = nl_maxit;

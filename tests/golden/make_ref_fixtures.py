@@ -91,12 +91,15 @@ STOKES_CASES = {
 }
 
 # name: (refinements, levels, solver (direct | mg | none), Reynolds number,
-#        nonlinloop_epsilon, nonlinloop_maxit)
+#        nonlinloop_epsilon, nonlinloop_maxit[, nse_nonlinear_form])
 NSE_CASES = {
     "nse_p2p1_4": (2, 1, "direct", 1.0, 1e-10, 10),
     "nse_p2p1_4_re100": (2, 1, "direct", 100.0, 1e-10, 30),
     "nse_p2p1_8_mg": (3, 3, "mg", 10.0, 1e-10, 10),
     "nse_p2p1_8_nl": (3, 3, "none", 1.0, 1e-10, 10),
+    # the skew-symmetric form (1/2) [((u.grad) u, v) - ((u.grad) v, u)]
+    "nse_p2p1_4_skew_re100": (2, 1, "direct", 100.0, 1e-10, 30, "skew_symmetric"),
+    "nse_p2p1_8_nl_skew": (3, 3, "none", 1.0, 1e-10, 10, "skew_symmetric"),
 }
 
 
@@ -214,12 +217,14 @@ def run_stokes_case(name: str) -> None:
 
 def run_nse_case(name: str) -> None:
     import build_ref
-    nref, nlev, solver, re, eps, maxit = NSE_CASES[name]
+    nref, nlev, solver, re, eps, maxit = NSE_CASES[name][:6]
+    form = NSE_CASES[name][6] if len(NSE_CASES[name]) > 6 else "convective"
     exe = build_ref.link_program("3", build_ref.HERE / "ref_stokes.C", build_ref.OUT / "ref_stokes3d")
     out: dict[str, np.ndarray] = {"config": np.array([nref, nlev, maxit], dtype=np.int64),
-                                  "params": np.array([re, eps]), "solver": np.array(solver)}
+                                  "params": np.array([re, eps]), "solver": np.array(solver),
+                                  "form": np.array(form)}
     with tempfile.TemporaryDirectory() as tmp:
-        subprocess.run([str(exe), tmp, str(nref), str(nlev), solver, "nse", repr(re), repr(eps), str(maxit)],
+        subprocess.run([str(exe), tmp, str(nref), str(nlev), solver, "nse", repr(re), repr(eps), str(maxit), form],
                        check=True, capture_output=True)
         lines = Path(tmp, "meta.txt").read_text().splitlines()
         if solver == "none":

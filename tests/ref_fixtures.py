@@ -149,6 +149,8 @@ class NseRefCase(StokesRefCase):
         self.n_refine, self.n_levels, self.maxit = (int(v) for v in self.z["config"])
         self.reynolds, self.epsilon = (float(v) for v in self.z["params"])
         self.solver = str(self.z["solver"])
+        # nse_nonlinear_form: convective or skew_symmetric
+        self.form = str(self.z["form"]) if "form" in self.z.files else "convective"
 
     def level(self, l: int) -> dict:
         p = f"L{l}_"

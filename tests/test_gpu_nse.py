@@ -3,8 +3,9 @@
 oracle (oracle/nse.py):
 
   * one assemble_nonlinear_term from a fixed finest velocity: every level's
-    projected matrix within 1e-13 of the reference's (the convective term and
-    the restriction of the velocity to the coarser levels);
+    projected matrix within 1e-13 of the reference's (the convective or the
+    skew-symmetric term and the restriction of the velocity to the coarser
+    levels);
   * the nonlinear loop of test/nse3d_solvers_test.c++ with FGMRES + nodal
     Vanka multigrid in FP64 and in the mixed form: the same number of
     nonlinear steps as the reference, the residual of every step within 1e-4
@@ -25,13 +26,14 @@ from test_gpu_stokes import stokes_db
 pytestmark = pytest.mark.gpu
 
 
-def nse_db(n_levels, epsilon=1e-10, maxit=10, precision="fp64"):
+def nse_db(n_levels, epsilon=1e-10, maxit=10, precision="fp64", form="convective"):
     db = stokes_db(n_levels, "nodal_vanka", 1.0, max_it=100, reduction=0.0, restart=20, precision=precision)
     db["residual_tolerance"] = 1e-12
     db.add("example", -3)
     db.add("problem_type", 5)
     db.add("nonlinloop_epsilon", epsilon)
     db.add("nonlinloop_maxit", maxit)
+    db.add("nse_nonlinear_form", form)
     return db
 
 
@@ -41,9 +43,10 @@ def make(ctx, nref, nlev, reynolds, db):
     return disc, prob
 
 
-def test_gpu_nonlinear_assembly_matches_the_reference(ctx):
-    rc = NseRefCase("nse_p2p1_8_nl")
-    disc, prob = make(ctx, rc.n_refine, rc.n_levels, rc.reynolds, nse_db(rc.n_levels))
+@pytest.mark.parametrize("name", nse_names("none"))
+def test_gpu_nonlinear_assembly_matches_the_reference(ctx, name):
+    rc = NseRefCase(name)
+    disc, prob = make(ctx, rc.n_refine, rc.n_levels, rc.reynolds, nse_db(rc.n_levels, form=rc.form))
     try:
         prob.assemble_linear_terms()
         nu, _, _ = prob.blocks()
@@ -93,7 +96,7 @@ def test_gpu_picard_loop_matches_the_reference(ctx, name, precision):
     rc = NseRefCase(name)
     # the direct-solver cases run on two levels of the same mesh
     nlev = max(rc.n_levels, 2)
-    disc, prob = make(ctx, rc.n_refine, nlev, rc.reynolds, nse_db(nlev, rc.epsilon, rc.maxit, precision))
+    disc, prob = make(ctx, rc.n_refine, nlev, rc.reynolds, nse_db(nlev, rc.epsilon, rc.maxit, precision, rc.form))
     try:
         prob.assemble()
         hist = prob.solve_nonlinear()
@@ -115,6 +118,19 @@ def test_gpu_picard_loop_matches_the_reference(ctx, name, precision):
         assert abs(float(w @ x[nu3:])) <= 1e-13
     finally:
         prob.close()
+        disc.close()
+
+
+def test_gpu_unsupported_nonlinear_forms_are_refused(ctx):
+    """rotational, divergence and emac couple the velocity components (the
+    off-diagonal velocity blocks this set-up does not hold): PM_E_UNSUPPORTED"""
+    disc = m.Discretization(m.GEO_CUBE_TETRA, 1, 1, 1, m.KIND_STOKES, 12)
+    try:
+        for form in ("rotational", "divergence", "emac"):
+            with pytest.raises(m.PmError) as e:
+                m.StokesProblem(ctx, disc, 1.0, nse_db(1, form=form))
+            assert e.value.code == 8, form
+    finally:
         disc.close()
 
 

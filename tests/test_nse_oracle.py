@@ -1,11 +1,11 @@
 """The oracle's Navier-Stokes restatement (oracle/nse.py) against the
 compiled reference's fixtures: one assemble_nonlinear_term from a fixed
 finest velocity (every level's combined matrix and restricted velocity:
-the convective term and GridTransfer::RestrictFunction), and the nonlinear
-loop of test/nse3d_solvers_test.c++ with the direct solver at Reynolds
-numbers 1 and 100 (the residuals of every step, the number of steps, the
-solution and the known answer: the exact solution of example -3 lies in
-P2 / P1)."""
+the convective or skew-symmetric term and GridTransfer::RestrictFunction),
+and the nonlinear loop of test/nse3d_solvers_test.c++ with the direct solver
+at Reynolds numbers 1 and 100 in both forms (the residuals of every step, the
+number of steps, the solution and the known answer: the exact solution of
+example -3 lies in P2 / P1)."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -14,9 +14,10 @@ from oracle import nse
 from ref_fixtures import NseRefCase, nse_names
 
 
-def test_nonlinear_assembly_matches_the_reference():
-    rc = NseRefCase("nse_p2p1_8_nl")
-    o = nse.OracleNSE(1, rc.n_refine, rc.n_levels, rc.reynolds)
+@pytest.mark.parametrize("name", nse_names("none"))
+def test_nonlinear_assembly_matches_the_reference(name):
+    rc = NseRefCase(name)
+    o = nse.OracleNSE(1, rc.n_refine, rc.n_levels, rc.reynolds, rc.form)
     o.assemble_linear_terms()
     fin = o.levels[-1]
     o.x = rc.fixed_velocity(fin.nu, fin.n)
@@ -33,7 +34,7 @@ def test_nonlinear_assembly_matches_the_reference():
 @pytest.mark.parametrize("name", nse_names("direct"))
 def test_picard_loop_matches_the_reference(name):
     rc = NseRefCase(name)
-    o = nse.OracleNSE(1, rc.n_refine, rc.n_levels, rc.reynolds)
+    o = nse.OracleNSE(1, rc.n_refine, rc.n_levels, rc.reynolds, rc.form)
     hist = o.run(rc.epsilon, rc.maxit)
     ref = rc.z["residuals"]
     assert hist.shape == ref.shape
