@@ -253,9 +253,10 @@ int pm_disc_create_bc(int geometry, int root_n, int n_refine, int n_levels, int 
  * the distinct nodes by class and first touch) and its CSR structure
  * (TStructure(space), src/Matrix/Structure.C:829-1283, sorted) with the
  * assembly gather plans (one stable radix sort of the element entries by
- * (row, column)); for a Stokes set-up the refinement and the numbering of
- * both spaces. The result is the same discretisation, array for array; the
- * grid transfer and the Stokes combined structure stay on the host. The context's
+ * (row, column)); for a Stokes set-up the refinement, the numbering of both
+ * spaces and the combined structure of the NSTYPE 4 blocks with its gather
+ * plans. The result is the same discretisation, array for array; the grid
+ * transfer stays on the host. The context's
  * stream is synchronised; temporary device memory of about 40 bytes per
  * element-matrix entry of the finest level is freed before the call returns. */
 int pm_disc_create_device(pm_ctx* ctx, int geometry, int root_n, int n_refine, int n_levels, int kind,

@@ -651,6 +651,7 @@ int pm_disc_create_device(pm_ctx* c, int geometry, int root_n, int n_refine, int
       return device_space(c, h, level, elem_, bnd, ns);
     };
     parts.structure = [c](DiscLevel& L) { device_level_structure(c, L); };
+    parts.stokes_structure = [c](DiscLevel& L, const std::vector<char>& act) { device_stokes_structure(c, L, act); };
     d->d = build_disc(geometry, root_n, n_refine, n_levels, kind, elem, neumann_sides, &parts);
   } catch (...) {
     delete d;

@@ -296,6 +296,81 @@ __global__ void k_dofmap(long long nt, const int* __restrict__ val, const int* _
     dofmap[val[i]] = number[gid[i] - 1];
 }
 
+// ------------------------------------------------------- Stokes structure --
+// the local coupling of the Stokes element (pm_disc.cpp stokes_local()) on
+// the device: item j of a cell is the pair (lm[j], lk[j]) with storage lpos[j]
+struct StokesItems {
+  short lm[540], lk[540], lpos[540];
+  int n;
+};
+
+// items t = c * n + j: key row * N + column for active rows (invalid key
+// otherwise), value = element storage position c * 220 + lpos; then one
+// unit-diagonal item per non-active row (value -1)
+__global__ void k_stokes_pairs(int n_cells, int N, int n_inactive, const int* __restrict__ cdof,
+                               const unsigned char* __restrict__ act, const int* __restrict__ inactive_rows,
+                               StokesItems S, unsigned long long* __restrict__ key, int* __restrict__ val) {
+  const long long ne = (long long)n_cells * S.n;
+  const long long total = ne + n_inactive;
+  const unsigned long long invalid = (unsigned long long)N * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    if (e < ne) {
+      const long long c = e / S.n;
+      const int j = int(e % S.n);
+      const int row = cdof[c * 34 + S.lm[j]];
+      if (act[row]) {
+        key[e] = (unsigned long long)row * N + (unsigned long long)cdof[c * 34 + S.lk[j]];
+        val[e] = int(c * 220 + S.lpos[j]);
+      } else {
+        key[e] = invalid;
+        val[e] = -1;
+      }
+    } else {
+      const int i = inactive_rows[e - ne];
+      key[e] = (unsigned long long)i * N + i;
+      val[e] = -1;
+    }
+  }
+}
+
+// as k_fill_structure, with the non-active rows' diagonal positions indexed
+// by their rank among the non-active rows
+__global__ void k_fill_structure_ranked(long long total, int n, const unsigned long long* __restrict__ key,
+                                        const int* __restrict__ val, const int* __restrict__ head,
+                                        const int* __restrict__ hpos, const int* __restrict__ cpos,
+                                        const int* __restrict__ inactive_rank, int* __restrict__ row_ptr,
+                                        int* __restrict__ cols, int* __restrict__ gat_ptr, int* __restrict__ gat_idx,
+                                        int* __restrict__ diag_pos) {
+  const unsigned long long invalid = (unsigned long long)n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long k = key[i];
+    if (k >= invalid) continue;
+    const int row = int(k / n);
+    if (head[i]) {
+      const int p = hpos[i];
+      cols[p] = int(k % n);
+      gat_ptr[p] = cpos[i];
+      if (i == 0 || int(key[i - 1] / n) != row) row_ptr[row] = p;
+      if (val[i] < 0) diag_pos[inactive_rank[row]] = p;
+    }
+    if (val[i] >= 0) gat_idx[cpos[i]] = val[i];
+  }
+}
+
+// right-hand side items t = c * 34 + m: key = row for active rows, N otherwise
+__global__ void k_stokes_rhs_pairs(long long nt, int N, const int* __restrict__ cdof,
+                                   const unsigned char* __restrict__ act, unsigned int* __restrict__ key,
+                                   int* __restrict__ val) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nt;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int d = cdof[t];
+    key[t] = act[d] ? unsigned(d) : unsigned(N);
+    val[t] = int(t);
+  }
+}
+
 int bits_for(unsigned long long v) {
   int b = 0;
   while (b < 64 && (v >> b) != 0) ++b;
@@ -526,6 +601,119 @@ pmsetup::Space device_space(pm_ctx* c, const pmsetup::Hierarchy& h, int level, i
   s.n_neumann = count[1];
   s.n_active = boundary == pmsetup::BND_DIRICHLET ? count[0] + count[1] : U;
   return s;
+}
+
+void device_stokes_structure(pm_ctx* c, DiscLevel& L, const std::vector<char>& active) {
+  const int N = int(active.size()), nc = L.n_cells;
+  const StokesLocal& loc = stokes_local();
+  StokesItems S{};
+  S.n = loc.n;
+  for (int j = 0; j < loc.n; ++j) {
+    S.lm[j] = short(loc.m[j]);
+    S.lk[j] = short(loc.k[j]);
+    S.lpos[j] = short(loc.pos[j]);
+  }
+  std::vector<int> inactive, rank(N, -1);
+  for (int i = 0; i < N; ++i)
+    if (!active[i]) {
+      rank[i] = int(inactive.size());
+      inactive.push_back(i);
+    }
+  const int ni = int(inactive.size()), na = N - ni;
+  const long long ne = (long long)nc * S.n, total = ne + ni;
+  const long long nt = (long long)nc * 34;
+  if (total >= (1LL << 31) || (unsigned long long)N * N >= (1ULL << 63))
+    throw Error(PM_E_INVALID, "level too large for the device structure build");
+  const int grid = std::max(1, std::min(int((total + 255) / 256), c->num_sms * 8));
+  cudaStream_t st = c->stream;
+  DBuf<int> cdof, inact, irank;
+  DBuf<unsigned char> act;
+  cdof.upload(L.cdof, st);
+  std::vector<unsigned char> a8(active.begin(), active.end());
+  act.upload(a8, st);
+  inact.upload(inactive.empty() ? std::vector<int>{0} : inactive, st);
+  irank.upload(rank, st);
+  DBuf<unsigned long long> key_in(static_cast<size_t>(total)), key_out(static_cast<size_t>(total));
+  DBuf<int> val_in(static_cast<size_t>(total)), val_out(static_cast<size_t>(total));
+  k_stokes_pairs<<<grid, 256, 0, st>>>(nc, N, ni, cdof.p, act.p, inact.p, S, key_in.p, val_in.p);
+  PM_CHECK_LAUNCH();
+  const int end_bit = bits_for((unsigned long long)N * N);
+  size_t tmp_bytes = 0, scan_bytes = 0;
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, key_in.p, key_out.p, val_in.p, val_out.p,
+                                          int(total), 0, end_bit, st));
+  PM_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, val_in.p, val_out.p, int(total), st));
+  DBuf<unsigned char> tmp(std::max(tmp_bytes, scan_bytes));
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, key_in.p, key_out.p, val_in.p, val_out.p,
+                                          int(total), 0, end_bit, st));
+  key_in.release();
+  const size_t tn = static_cast<size_t>(total);
+  DBuf<int> head(tn), contrib(tn), hpos(tn), cpos(tn);
+  k_heads<<<grid, 256, 0, st>>>(total, N, key_out.p, val_out.p, head.p, contrib.p);
+  PM_CHECK_LAUNCH();
+  size_t sb = tmp.n;
+  PM_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sb, head.p, hpos.p, int(total), st));
+  sb = tmp.n;
+  PM_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sb, contrib.p, cpos.p, int(total), st));
+  int last[4] = {0, 0, 0, 0};
+  PM_CUDA(cudaMemcpyAsync(&last[0], hpos.p + total - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaMemcpyAsync(&last[1], head.p + total - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaMemcpyAsync(&last[2], cpos.p + total - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaMemcpyAsync(&last[3], contrib.p + total - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaStreamSynchronize(st));
+  const int nnz = last[0] + last[1], ncontrib = last[2] + last[3];
+  DBuf<int> row_ptr(static_cast<size_t>(N) + 1), cols(static_cast<size_t>(nnz));
+  DBuf<int> gat_ptr(static_cast<size_t>(nnz) + 1), gat_idx(static_cast<size_t>(std::max(1, ncontrib)));
+  DBuf<int> diag_pos(static_cast<size_t>(std::max(1, ni)));
+  k_fill_structure_ranked<<<grid, 256, 0, st>>>(total, N, key_out.p, val_out.p, head.p, hpos.p, cpos.p, irank.p,
+                                                row_ptr.p, cols.p, gat_ptr.p, gat_idx.p, diag_pos.p);
+  PM_CHECK_LAUNCH();
+  k_set_tail<<<1, 32, 0, st>>>(row_ptr.p, N, N + 1, nnz);
+  k_set_tail<<<1, 32, 0, st>>>(gat_ptr.p, nnz, nnz + 1, ncontrib);
+  PM_CHECK_LAUNCH();
+  c->kernel_launches += 5;
+  // right-hand side plan
+  DBuf<unsigned int> rkey_in(static_cast<size_t>(nt)), rkey_out(static_cast<size_t>(nt));
+  DBuf<int> rval_in(static_cast<size_t>(nt)), rval_out(static_cast<size_t>(nt));
+  const int rgrid = std::max(1, std::min(int((nt + 255) / 256), c->num_sms * 8));
+  k_stokes_rhs_pairs<<<rgrid, 256, 0, st>>>(nt, N, cdof.p, act.p, rkey_in.p, rval_in.p);
+  PM_CHECK_LAUNCH();
+  size_t rb = 0;
+  const int rend = bits_for((unsigned long long)N);
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, rb, rkey_in.p, rkey_out.p, rval_in.p, rval_out.p, int(nt), 0,
+                                          rend, st));
+  if (rb > tmp.n) tmp.alloc(rb);
+  rb = tmp.n;
+  PM_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, rb, rkey_in.p, rkey_out.p, rval_in.p, rval_out.p, int(nt), 0,
+                                          rend, st));
+  c->kernel_launches++;
+  // results into the host level
+  L.sys = pmsetup::Csr();
+  L.sys.n_rows = N;
+  L.sys.n_cols = N;
+  L.sys.n_active = na;
+  download(c, L.sys.row_ptr, row_ptr, size_t(N) + 1);
+  download(c, L.sys.cols, cols, size_t(nnz));
+  download(c, L.gat_ptr, gat_ptr, size_t(nnz) + 1);
+  download(c, L.gat_idx, gat_idx, size_t(ncontrib));
+  download(c, L.diag_pos, diag_pos, size_t(ni));
+  std::vector<unsigned> rk(static_cast<size_t>(nt));
+  std::vector<int> rv;
+  download(c, rv, rval_out, size_t(nt));
+  PM_CUDA(cudaMemcpyAsync(rk.data(), rkey_out.p, rk.size() * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  PM_CUDA(cudaStreamSynchronize(st));
+  L.sys.vals.assign(L.sys.cols.size(), 0.0);
+  // the rhs items of active rows come first, in row order and, per row, in
+  // the order of t; rows without items (non-active) get empty ranges
+  std::vector<int> rp(size_t(N) + 1, 0);
+  size_t valid = 0;
+  while (valid < rk.size() && rk[valid] < unsigned(N)) {
+    rp[rk[valid] + 1]++;
+    ++valid;
+  }
+  for (int i = 0; i < N; ++i) rp[size_t(i) + 1] += rp[size_t(i)];
+  rv.resize(valid);
+  L.rgat_ptr = std::move(rp);
+  L.rgat_idx = std::move(rv);
 }
 
 }  // namespace pm

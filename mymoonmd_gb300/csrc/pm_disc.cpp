@@ -82,6 +82,23 @@ static inline int stokes_pos(int c, int m, int k) {
   return -1;
 }
 
+const StokesLocal& stokes_local() {
+  static const StokesLocal t = [] {
+    StokesLocal r;
+    for (int m = 0; m < 34; ++m)
+      for (int k = 0; k < 34; ++k) {
+        const int p = stokes_pos(0, m, k);
+        if (p < 0) continue;
+        r.m[r.n] = m;
+        r.k[r.n] = k;
+        r.pos[r.n] = p;
+        ++r.n;
+      }
+    return r;
+  }();
+  return t;
+}
+
 // physical coordinates of the non-active DOFs of L.space (lattice coordinates
 // converted the way cell_vertices converts them)
 static void fill_bnd_xyz(const Hierarchy& h, DiscLevel& L) {
@@ -97,6 +114,9 @@ static void fill_bnd_xyz(const Hierarchy& h, DiscLevel& L) {
     }
 }
 
+static void build_stokes_structure(DiscLevel& L, const std::vector<char>& act);
+static void finish_stokes_level(DiscLevel& L, int nu, int np, int nau);
+
 static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L, const SetupParts* parts) {
   const bool dev = parts && parts->space;
   L.space = dev ? parts->space(h, lvl, EL_P2, BND_DIRICHLET, 0) : build_space(h, lvl, EL_P2, BND_DIRICHLET);
@@ -111,6 +131,19 @@ static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L, const 
   std::vector<char> act(N, 1);
   for (int b = 0; b < 3; ++b)
     for (int i = nau; i < nu; ++i) act[size_t(b) * nu + i] = 0;
+  if (parts && parts->stokes_structure) {
+    parts->stokes_structure(L, act);
+  } else {
+    build_stokes_structure(L, act);
+  }
+  finish_stokes_level(L, nu, np, nau);
+}
+
+// the combined pattern and the gather plans of a Stokes level (host)
+static void build_stokes_structure(DiscLevel& L, const std::vector<char>& act) {
+  const int N = int(act.size()), nc = L.n_cells;
+  int n_inactive = 0;
+  for (char a : act) n_inactive += a ? 0 : 1;
   // incidence: combined DOF -> (cell, local index), cells in order
   std::vector<int> iptr(N + 1, 0), inc;
   for (size_t t = 0; t < L.cdof.size(); ++t) iptr[L.cdof[t] + 1]++;
@@ -124,7 +157,7 @@ static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L, const 
   Csr& A = L.sys;
   A = Csr();
   A.n_rows = A.n_cols = N;
-  A.n_active = 3 * nau + np;
+  A.n_active = N - n_inactive;
   A.row_ptr.assign(N + 1, 0);
   std::vector<int> marker(N, -1), row;
   for (int i = 0; i < N; ++i) {
@@ -193,6 +226,20 @@ static void build_stokes_level(const Hierarchy& h, int lvl, DiscLevel& L, const 
   L.diag_pos.clear();
   for (int i = 0; i < N; ++i)
     if (!act[i]) L.diag_pos.push_back(find(i, i));
+}
+
+// block layout, Vanka patches and the cell colouring of a Stokes level
+static void finish_stokes_level(DiscLevel& L, int nu, int np, int nau) {
+  const int N = 3 * nu + np, nc = L.n_cells;
+  // incidence: combined DOF -> (cell, local index), cells in order
+  std::vector<int> iptr(N + 1, 0), inc;
+  for (size_t t = 0; t < L.cdof.size(); ++t) iptr[L.cdof[t] + 1]++;
+  for (int i = 0; i < N; ++i) iptr[i + 1] += iptr[i];
+  inc.resize(iptr[N]);
+  {
+    std::vector<int> fill(iptr.begin(), iptr.end() - 1);
+    for (size_t t = 0; t < L.cdof.size(); ++t) inc[fill[L.cdof[t]]++] = int(t);
+  }
   L.elem_stride = 220;
   L.rhs_stride = 34;
   L.n_blocks = 4;

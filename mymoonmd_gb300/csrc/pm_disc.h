@@ -75,7 +75,20 @@ struct SetupParts {
   std::function<pmsetup::Space(const pmsetup::Hierarchy&, int level, int elem, int boundary, int neumann_sides)>
       space;
   std::function<void(DiscLevel&)> structure;
+  // a Stokes level's combined `sys`, gather plans and diag_pos from its cdof
+  // and the active flags of the combined DOFs
+  std::function<void(DiscLevel&, const std::vector<char>& active)> stokes_structure;
 };
+
+// the Stokes element's local coupling: (local row m, local column k) pairs of
+// the 34 combined local DOFs (3 x 10 velocity, then 4 pressure) that carry a
+// block entry, in row-major order, with their position in the 220-entry
+// element storage (A 10 x 10, then B_0, B_1, B_2 4 x 10; B^T read transposed)
+struct StokesLocal {
+  int n = 0;
+  int m[540], k[540], pos[540];
+};
+const StokesLocal& stokes_local();
 
 std::unique_ptr<Disc> build_disc(int geometry, int root_n, int n_refine, int n_levels, int kind, int elem,
                                  int neumann_sides = 0, const SetupParts* parts = nullptr);

@@ -98,9 +98,11 @@ def test_device_setup_time_of_the_32cube_q2_hierarchy(ctx):
 
 def test_device_numbering_of_the_stokes_spaces(ctx):
     """the P2 velocity (Dirichlet) and P1 pressure (Neumann, all active)
-    numberings of a Stokes set-up from the GPU: the same GlobalNumbers, level
-    sizes, combined structure and Dirichlet node coordinates (through the
-    right-hand side of the polynomial example) as the host set-up"""
+    numberings and the combined structure of a Stokes set-up from the GPU:
+    the same GlobalNumbers, level sizes and structure as the host set-up, and
+    through the gather plans and the Dirichlet node coordinates the same
+    assembled matrix and right-hand side of the polynomial example, bit for
+    bit"""
     host = m.Discretization(m.GEO_CUBE_TETRA, 2, 2, 2, m.KIND_STOKES, 12)
     dev = m.Discretization(m.GEO_CUBE_TETRA, 2, 2, 2, m.KIND_STOKES, 12, ctx=ctx)
     probs = []
@@ -124,5 +126,32 @@ def test_device_numbering_of_the_stokes_spaces(ctx):
     finally:
         for p in probs:
             p.close()
+        host.close()
+        dev.close()
+
+
+def test_device_setup_of_the_stokes_workload_mesh(ctx):
+    """the Stokes workload's hierarchy (24^3 cubes x 6 tetrahedra, 3 levels)
+    from the GPU set-up (refinement, both numberings, the combined structure
+    and its gather plans): the same arrays as the host set-up (timings
+    printed)"""
+    import time
+    t0 = time.perf_counter()
+    host = m.Discretization(m.GEO_CUBE_TETRA, 3, 3, 3, m.KIND_STOKES, 12)
+    t1 = time.perf_counter()
+    dev = m.Discretization(m.GEO_CUBE_TETRA, 3, 3, 3, m.KIND_STOKES, 12, ctx=ctx)
+    t2 = time.perf_counter()
+    try:
+        for l in range(3):
+            for space in (0, 1):
+                assert host.level_info(l, space) == dev.level_info(l, space)
+                assert np.array_equal(host.dofmap(l, space), dev.dofmap(l, space))
+            for a, b in zip(host.structure(l), dev.structure(l)):
+                assert np.array_equal(a, b), l
+            if l < 2:
+                for a, b in zip(host.prolongation(l)[:3], dev.prolongation(l)[:3]):
+                    assert np.array_equal(a, b)
+        print(f"24^3 Stokes set-up: host {t1 - t0:.3f} s, GPU {t2 - t1:.3f} s")
+    finally:
         host.close()
         dev.close()
